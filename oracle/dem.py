@@ -1,0 +1,624 @@
+"""NumPy FP64 restatement of the reference bonded-DEM Newton path.
+
+TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the CPU baseline
+that ``bench.py`` times.  Nothing in the product imports this module.
+
+Every function cites the reference file:line (paths inside the reference
+project) whose algorithm it restates.  Parity of this restatement with the
+reference itself is pinned by ``tests/test_oracle_golden.py`` against vectors
+generated by the reference's own code (``tests/golden/make_golden.py``).
+
+Layouts follow the reference: per-site 6-vectors ``[tx, ty, tz, rx, ry, rz]``
+as (N, 6) float64; per-bond vectors (M, 3); ``edges`` (M, 2) int64 with the
+bond normal pointing from ``edges[:, 0]`` to ``edges[:, 1]``.
+"""
+import numpy as np
+
+COS_QUARTER = float(np.cos(.25))
+
+
+class SubdivideError(RuntimeError):
+    """Recoverable failure; message starts with 'Subdivide:' as in the reference."""
+
+
+def dot(a, b):
+    return np.einsum('...i,...i->...', a, b)
+
+
+def cross(a, b):
+    return np.cross(a, b)
+
+
+def scatter_add(n, index, values):
+    """out[index[k]] += values[k] for (K, C) values; deterministic bincount per column."""
+    out = np.empty((n, values.shape[1]))
+    for c in range(values.shape[1]):
+        out[:, c] = np.bincount(index, weights=values[:, c], minlength=n)
+    return out
+
+
+def transport(v, n0, n1, spin):
+    """Shortest-arc transport n0 -> n1 then rotation about n1 by spin . bisector.
+
+    Restates ``experiments/bonded_dem_finite_gpu.py:22-32`` (same algorithm as
+    ``experiments/bonded_dem_core.py:31-42``); raises when a normal turns by
+    more than 0.25 rad.
+    """
+    k = cross(n0, n1)
+    cosine = np.clip(dot(n0, n1), -1., 1.)
+    if np.any(cosine < COS_QUARTER):
+        raise SubdivideError('Subdivide: normal turns more than .25 rad per half-step')
+    out = v + cross(k, v)
+    out = out + cross(k, cross(k, v))/(1+cosine)[:, None]
+    b = n0 + n1
+    b = b/np.maximum(np.linalg.norm(b, axis=1), 1e-12)[:, None]
+    angle = dot(spin, b)[:, None]
+    c, s = np.cos(angle), np.sin(angle)
+    return c*out + s*cross(n1, out) + (1-c)*dot(n1, out)[:, None]*n1
+
+
+def skew(v):
+    s = np.zeros(v.shape[:-1] + (3, 3))
+    s[..., 0, 1], s[..., 0, 2] = -v[..., 2], v[..., 1]
+    s[..., 1, 0], s[..., 1, 2] = v[..., 2], -v[..., 0]
+    s[..., 2, 0], s[..., 2, 1] = -v[..., 1], v[..., 0]
+    return s
+
+
+def exp_rotation(v):
+    """SO(3) exponential via sinc; ``experiments/bonded_dem_finite_gpu.py:35-43``."""
+    angle = np.linalg.norm(v, axis=1)
+    s = skew(v)
+    a = np.sinc(angle/np.pi)
+    b = .5*np.sinc(angle/(2*np.pi))**2
+    return np.eye(3) + a[:, None, None]*s + b[:, None, None]*(s@s)
+
+
+class LinearBonds:
+    """Stress-free linearised bonds; ``experiments/bonded_dem_linear_gpu.py:14-124``."""
+
+    def __init__(self, points, radii, pairs, areas, contacts, masses, fixed,
+                 young=1200., shear=480.):
+        # bonded_dem_linear_gpu.py:15-40
+        self.p = np.array(points, dtype=np.float64)
+        self.edges = np.array(pairs, dtype=np.int64)
+        self.i, self.j = self.edges[:, 0].copy(), self.edges[:, 1].copy()
+        r = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(self.p),)).copy()
+        area = np.broadcast_to(np.asarray(areas, dtype=np.float64), (len(self.edges),)).copy()
+        c = np.asarray(contacts, dtype=np.float64)
+        distance = self.p[self.j] - self.p[self.i]
+        length = np.linalg.norm(distance, axis=1)
+        self.n = distance/length[:, None]
+        self.ri, self.rj = c - self.p[self.i], c - self.p[self.j]
+        self.kn, self.ks = young*area/length, shear*area/length
+        second = area**2/(4*np.pi)
+        self.kb, self.kt = young*second/length, shear*(2*second)/length
+        mass = np.broadcast_to(np.asarray(masses, dtype=np.float64), (len(self.p),)).copy()
+        inertia = .4*mass*r*r
+        self.mass = np.concatenate((np.repeat(mass[:, None], 3, 1), np.repeat(inertia[:, None], 3, 1)), 1)
+        if np.any(self.mass <= 0):
+            raise ValueError('Only positive-mass bodies can enter this solver')
+        self.fixed = np.array(fixed, dtype=bool)
+        self.q, self.v = np.zeros_like(self.mass), np.zeros_like(self.mass)
+        self.kq = np.zeros_like(self.mass)
+        self.diagonal = self._diagonal_blocks()
+        self.preconditioner = None
+        self.preconditioner_dt = None
+
+    @property
+    def n_sites(self):
+        return len(self.p)
+
+    def stiffness(self, q):
+        """Frozen-tangent K q; ``bonded_dem_linear_gpu.py:42-52``."""
+        a, b = q[self.i], q[self.j]
+        du = b[:, :3] - a[:, :3] + cross(b[:, 3:], self.rj) - cross(a[:, 3:], self.ri)
+        dw = b[:, 3:] - a[:, 3:]
+        f = self.ks[:, None]*du + (self.kn-self.ks)[:, None]*dot(du, self.n)[:, None]*self.n
+        m = self.kb[:, None]*dw + (self.kt-self.kb)[:, None]*dot(dw, self.n)[:, None]*self.n
+        out = scatter_add(self.n_sites, self.i, np.concatenate((-f, -cross(self.ri, f) - m), 1))
+        out += scatter_add(self.n_sites, self.j, np.concatenate((f, cross(self.rj, f) + m), 1))
+        return out
+
+    def _diagonal_blocks(self):
+        """Per-site 6x6 diagonal blocks of K; ``bonded_dem_linear_gpu.py:54-72``."""
+        eye = np.eye(3)
+        nn = self.n[:, :, None]*self.n[:, None, :]
+        d = self.ks[:, None, None]*eye + (self.kn-self.ks)[:, None, None]*nn
+        h = self.kb[:, None, None]*eye + (self.kt-self.kb)[:, None, None]*nn
+        diagonal = np.zeros((self.n_sites, 36))
+        for indices, r in ((self.i, self.ri), (self.j, self.rj)):
+            s = skew(r)
+            block = np.zeros((len(indices), 6, 6))
+            block[:, :3, :3] = d
+            block[:, :3, 3:] = -d@s
+            block[:, 3:, :3] = np.transpose(block[:, :3, 3:], (0, 2, 1))
+            block[:, 3:, 3:] = np.transpose(s, (0, 2, 1))@d@s + h
+            diagonal += scatter_add(self.n_sites, indices, block.reshape(-1, 36))
+        return diagonal.reshape(-1, 6, 6)
+
+    def _operator(self, q, alpha):
+        """(diag M + alpha K) q with identity fixed rows; ``bonded_dem_linear_gpu.py:74-77``."""
+        out = self.mass*q + alpha*self.stiffness(q)
+        out[self.fixed] = q[self.fixed]
+        return out
+
+    def solve_increment(self, rhs, dt, guess=None, tolerance=2e-8, max_iterations=1000):
+        """Block-Jacobi PCG; ``bonded_dem_linear_gpu.py:79-112``."""
+        alpha = dt*dt/4
+        if self.preconditioner_dt != dt:
+            diagonal = np.einsum('ni,ij->nij', self.mass, np.eye(6)) + alpha*self.diagonal
+            diagonal[self.fixed] = np.eye(6)
+            self.preconditioner = np.linalg.inv(diagonal)
+            self.preconditioner_dt = dt
+        rhs = rhs.copy(); rhs[self.fixed] = 0
+        norm = float(np.linalg.norm(rhs))
+        if norm < 1e-30:
+            return np.zeros_like(rhs), dict(iterations=0, relative_residual=0.)
+        x = np.zeros_like(rhs) if guess is None else guess.copy()
+        x[self.fixed] = 0
+        residual = rhs - self._operator(x, alpha)
+        z = np.einsum('nij,nj->ni', self.preconditioner, residual)
+        direction = z.copy(); rz = (residual*z).sum()
+        for iteration in range(max_iterations):
+            ad = self._operator(direction, alpha)
+            step = rz/(direction*ad).sum()
+            x += step*direction; residual -= step*ad
+            if iteration % 10 == 0:
+                relative = float(np.linalg.norm(residual))/norm
+                if relative < tolerance:
+                    break
+                if not np.isfinite(relative):
+                    raise RuntimeError('Nonfinite conjugate-gradient residual')
+            z = np.einsum('nij,nj->ni', self.preconditioner, residual)
+            next_rz = (residual*z).sum()
+            direction = z + (next_rz/rz)*direction; rz = next_rz
+        actual = float(np.linalg.norm(rhs - self._operator(x, alpha)))/norm
+        if actual > 5*tolerance or not np.isfinite(actual):
+            raise RuntimeError(f'Linear solve failed after {iteration+1} iterations: {actual}')
+        return x, dict(iterations=iteration+1, relative_residual=actual)
+
+    def step(self, dt, external):
+        """Linear implicit midpoint; ``bonded_dem_linear_gpu.py:114-121``."""
+        rhs = dt*self.mass*self.v + .5*dt*dt*(external - self.kq)
+        dq, metrics = self.solve_increment(rhs, dt, guess=dt*self.v)
+        self.v = 2*dq/dt - self.v
+        self.q = self.q + dq; self.kq = self.stiffness(self.q)
+        return float((external*dq).sum()), metrics
+
+    def energy(self):
+        return float(.5*((self.mass*self.v*self.v).sum() + (self.q*self.kq).sum()))
+
+
+class FiniteBonds(LinearBonds):
+    """Finite-motion rate law; ``experiments/bonded_dem_finite_gpu.py:46-261``."""
+
+    STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
+
+    def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None,
+                 young=1200., shear=480.):
+        # bonded_dem_finite_gpu.py:47-64
+        p = np.asarray(points, dtype=np.float64)
+        i, j = np.asarray(pairs).T
+        radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
+        n = p[j] - p[i]
+        n /= np.linalg.norm(n, axis=1)[:, None]
+        classical = .5*(p[i]+p[j])
+        classical += .5*(radii_a[i]-radii_a[j])[:, None]*n
+        if contacts is None:
+            contacts = classical
+        contacts = np.asarray(contacts, dtype=np.float64)
+        super().__init__(p, radii_a, pairs, areas, contacts, masses, fixed, young, shear)
+        self.x = self.p.copy()
+        self.radii = np.array(radii_a)
+        self.normal = self.n.copy()
+        self.offset = contacts - classical
+        self.fn, self.mt = np.zeros_like(self.kn), np.zeros_like(self.kn)
+        self.fs, self.mb = np.zeros_like(self.n), np.zeros_like(self.n)
+        self.rotation = np.repeat(np.eye(3)[None], len(p), 0)
+        self.time = 0.
+
+    def geometry(self, x):
+        """Normal and classical contact; ``bonded_dem_finite_gpu.py:66-73``."""
+        d = x[self.j] - x[self.i]
+        length = np.linalg.norm(d, axis=1)
+        if np.any(length <= 1e-12):
+            raise SubdivideError('Subdivide: coincident centers')
+        n = d/length[:, None]
+        c = .5*(x[self.i]+x[self.j]) + .5*(self.radii[self.i]-self.radii[self.j])[:, None]*n
+        return n, c
+
+    def assemble(self, fn, fs, mt, mb, n, ri, rj):
+        """Scatter bond force and couple; ``bonded_dem_finite_gpu.py:75-80``."""
+        f, couple = fn[:, None]*n + fs, mt[:, None]*n + mb
+        out = scatter_add(self.n_sites, self.i, np.concatenate((f, cross(ri, f)+couple), 1))
+        out += scatter_add(self.n_sites, self.j, np.concatenate((-f, -cross(rj, f)-couple), 1))
+        return out
+
+    def loads(self):
+        """``bonded_dem_finite_gpu.py:82-85``."""
+        n, c = self.geometry(self.x)
+        c = c + self.offset
+        return self.assemble(self.fn, self.fs, self.mt, self.mb, n, c-self.x[self.i], c-self.x[self.j])
+
+    def trial(self, increment, *, mid_positions=None, end_positions=None):
+        """Pure constitutive trial; ``bonded_dem_finite_gpu.py:87-116``."""
+        if float(np.linalg.norm(increment[:, 3:], axis=1).max()) > .25:
+            raise SubdivideError('Subdivide: body rotation exceeds .25 rad in a step')
+        mid = self.x + .5*increment[:, :3] if mid_positions is None else mid_positions
+        end = self.x + increment[:, :3] if end_positions is None else end_positions
+        nm, contact = self.geometry(mid)
+        ne, _ = self.geometry(end)
+        spin = .5*(increment[self.i, 3:] + increment[self.j, 3:])
+        offset_mid = transport(self.offset, self.normal, nm, .5*spin)
+        contact = contact + offset_mid
+        ri, rj = contact - mid[self.i], contact - mid[self.j]
+        fs0 = transport(self.fs, self.normal, nm, .5*spin)
+        mb0 = transport(self.mb, self.normal, nm, .5*spin)
+        du = (increment[self.j, :3] - increment[self.i, :3]
+              + cross(increment[self.j, 3:], rj) - cross(increment[self.i, 3:], ri))
+        dw = increment[self.j, 3:] - increment[self.i, 3:]
+        dn, twist = dot(du, nm), dot(dw, nm)
+        fn = self.fn + self.kn*dn
+        fs = fs0 + self.ks[:, None]*(du - dn[:, None]*nm)
+        mt = self.mt + self.kt*twist
+        mb = mb0 + self.kb[:, None]*(dw - twist[:, None]*nm)
+        force = self.assemble(.5*(self.fn+fn), .5*(fs0+fs), .5*(self.mt+mt), .5*(mb0+mb), nm, ri, rj)
+        return dict(force=force, n=nm, ri=ri, rj=rj, x=end, normal=ne, fn=fn, mt=mt,
+                    fs=transport(fs, nm, ne, .5*spin),
+                    mb=transport(mb, nm, ne, .5*spin),
+                    offset=transport(offset_mid, nm, ne, .5*spin))
+
+    def commit(self, trial):
+        """``bonded_dem_finite_gpu.py:118-120``."""
+        for name in ('x', 'normal', 'fn', 'fs', 'mt', 'mb', 'offset'):
+            setattr(self, name, np.array(trial[name]))
+
+    def energy(self):
+        """Elastic + kinetic; ``bonded_dem_finite_gpu.py:122-125``."""
+        elastic = .5*(self.fn**2/self.kn + dot(self.fs, self.fs)/self.ks
+                      + self.mt**2/self.kt + dot(self.mb, self.mb)/self.kb).sum()
+        return float(elastic + .5*(self.mass*self.v*self.v).sum())
+
+    def local_defect(self, residual):
+        """``bonded_dem_finite_gpu.py:127-131``."""
+        correction = np.einsum('nij,nj->ni', self.preconditioner, residual)
+        scale = np.ones_like(correction)
+        scale[:, :3] = self.radii[:, None]
+        return float(np.abs(correction/scale).max())
+
+    def advance_interval(self, dt, force_at_time, depth=0):
+        """Recursive dt bisection on 'Subdivide:'; ``bonded_dem_finite_gpu.py:252-261``."""
+        try:
+            work, info = self.step(dt, force_at_time(self.time + .5*dt))
+            return work, [dict(dt=dt, subdivision_depth=depth, **info)]
+        except RuntimeError as error:
+            if depth >= 8 or 'Subdivide:' not in str(error):
+                raise
+            a, ia = self.advance_interval(.5*dt, force_at_time, depth+1)
+            b, ib = self.advance_interval(.5*dt, force_at_time, depth+1)
+            return a+b, ia+ib
+
+
+def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iterations=256):
+    """Right-preconditioned flexible GMRES with CGS2 Arnoldi.
+
+    Restates ``experiments/bonded_dem_newton.py:13-60``.
+    """
+    shape = rhs.shape
+    b = rhs.ravel(); norm = float(np.linalg.norm(b))
+    x = np.zeros_like(b)
+    if norm == 0:
+        return x.reshape(shape), dict(iterations=0, relative_residual=0.)
+    residual = b.copy(); iterations = 0
+    relative = float('nan')
+    while iterations < max_iterations:
+        width = min(restart, max_iterations - iterations)
+        basis = np.empty((width+1, len(b)))
+        transformed = np.empty((width, len(b)))
+        h = np.zeros((width+1, width)); cs, sn = np.zeros(width), np.zeros(width)
+        g = np.zeros(width+1); g[0] = float(np.linalg.norm(residual))
+        basis[0] = residual/g[0]
+        for j in range(width):
+            z = precondition(basis[j].reshape(shape)).ravel()
+            transformed[j] = z
+            w = operator(z.reshape(shape)).ravel()
+            projections = np.zeros(j+1)
+            for _ in range(2):
+                values = basis[:j+1]@w
+                projections += values
+                w = w - basis[:j+1].T@values
+            h[:j+1, j] = projections
+            h[j+1, j] = float(np.linalg.norm(w))
+            breakdown = h[j+1, j] < 1e-14
+            if not breakdown:
+                basis[j+1] = w/h[j+1, j]
+            for k in range(j):
+                h[k, j], h[k+1, j] = cs[k]*h[k, j] + sn[k]*h[k+1, j], -sn[k]*h[k, j] + cs[k]*h[k+1, j]
+            denominator = np.hypot(h[j, j], h[j+1, j])
+            if denominator == 0:
+                raise SubdivideError('Subdivide: singular Newton linear system')
+            cs[j], sn[j] = h[j, j]/denominator, h[j+1, j]/denominator
+            h[j, j], h[j+1, j] = denominator, 0.
+            g[j+1], g[j] = -sn[j]*g[j], cs[j]*g[j]
+            iterations += 1
+            if abs(g[j+1]) <= tolerance*norm or breakdown or j+1 == width:
+                coefficients = np.linalg.solve(h[:j+1, :j+1], g[:j+1])
+                x = x + transformed[:j+1].T@coefficients
+                residual = b - operator(x.reshape(shape)).ravel()
+                relative = float(np.linalg.norm(residual))/norm
+                if relative <= 1.05*tolerance:
+                    return x.reshape(shape), dict(iterations=iterations, relative_residual=relative)
+                break
+    raise SubdivideError(f'Subdivide: FGMRES did not converge ({relative:g})')
+
+
+def rotate_jvp(v, n0, n, dn, spin, dspin):
+    """Value and directional derivative of ``transport`` with respect to (n, spin).
+
+    Restates the analytic derivative of ``experiments/bonded_dem_jvp_warp.py:17-42``
+    (vectorised over bonds).
+    """
+    raw = dot(n0, n)
+    cosine = np.clip(raw, -1., 1.)
+    dc = dot(n0, dn)
+    dc = np.where((raw < -1.) | (raw > 1.), 0., dc)
+    k, dk = cross(n0, n), cross(n0, dn)
+    kv = cross(k, v)
+    kkv = cross(k, kv)
+    one_c = (1. + cosine)[:, None]
+    t = v + kv + kkv/one_c
+    dt = cross(dk, v) + (cross(dk, kv) + cross(k, cross(dk, v)))/one_c
+    dt = dt - kkv*dc[:, None]/(one_c*one_c)
+    length = np.linalg.norm(n0 + n, axis=1)[:, None]
+    b = (n0 + n)/length
+    db = (dn - b*dot(b, dn)[:, None])/length
+    angle = dot(spin, b)
+    da = (dot(dspin, b) + dot(spin, db))[:, None]
+    c, s = np.cos(angle)[:, None], np.sin(angle)[:, None]
+    nt = dot(n, t)[:, None]
+    value = c*t + s*cross(n, t) + (1-c)*nt*n
+    derivative = c*dt - s*da*t + c*da*cross(n, t)
+    derivative = derivative + s*(cross(dn, t) + cross(n, dt)) + s*da*nt*n
+    derivative = derivative + (1-c)*((dot(dn, t) + dot(n, dt))[:, None]*n + nt*dn)
+    return value, derivative
+
+
+class NewtonBonds(FiniteBonds):
+    """Scaled Newton-FGMRES; ``experiments/bonded_dem_newton.py:63-201``."""
+
+    def midpoint_force(self, y):
+        """``bonded_dem_newton.py:64-81``."""
+        mid = self.x + .5*y[:, :3]
+        n, contact = self.geometry(mid)
+        half_spin = .25*(y[self.i, 3:] + y[self.j, 3:])
+        contact = contact + transport(self.offset, self.normal, n, half_spin)
+        ri, rj = contact - mid[self.i], contact - mid[self.j]
+        fs0 = transport(self.fs, self.normal, n, half_spin)
+        mb0 = transport(self.mb, self.normal, n, half_spin)
+        du = y[self.j, :3] - y[self.i, :3] + cross(y[self.j, 3:], rj) - cross(y[self.i, 3:], ri)
+        dw = y[self.j, 3:] - y[self.i, 3:]
+        dn, twist = dot(du, n), dot(dw, n)
+        return self.assemble(self.fn + .5*self.kn*dn, fs0 + .5*self.ks[:, None]*(du - dn[:, None]*n),
+                             self.mt + .5*self.kt*twist, mb0 + .5*self.kb[:, None]*(dw - twist[:, None]*n),
+                             n, ri, rj)
+
+    def residual(self, y, dt, external):
+        """``bonded_dem_newton.py:83-86``."""
+        trial = self.trial(y)
+        r = self.mass*(y - dt*self.v) - .5*dt*dt*(trial['force'] + external)
+        return np.where(self.fixed[:, None], y, r)
+
+    def midpoint_force_jvp(self, y, direction):
+        """Analytic d f_mid(y)[direction]; ``bonded_dem_jvp_warp.py:45-97``."""
+        i, j = self.i, self.j
+        ui, uj, wi, wj = y[i, :3], y[j, :3], y[i, 3:], y[j, 3:]
+        dui, duj, dwi, dwj = direction[i, :3], direction[j, :3], direction[i, 3:], direction[j, 3:]
+        mi, mj = self.x[i] + .5*ui, self.x[j] + .5*uj
+        displacement = mj - mi
+        length = np.linalg.norm(displacement, axis=1)[:, None]
+        n = displacement/length
+        dd = .5*(duj - dui)
+        dn = (dd - n*dot(n, dd)[:, None])/length
+        spin, dspin = .25*(wi + wj), .25*(dwi + dwj)
+        rotated, drotated = rotate_jvp(self.offset, self.normal, n, dn, spin, dspin)
+        rad = .5*(self.radii[i] - self.radii[j])[:, None]
+        contact = .5*(mi + mj) + rad*n + rotated
+        dcontact = .25*(dui + duj) + rad*dn + drotated
+        ri, rj = contact - mi, contact - mj
+        dri, drj = dcontact - .5*dui, dcontact - .5*duj
+        fs0, dfs0 = rotate_jvp(self.fs, self.normal, n, dn, spin, dspin)
+        mb0, dmb0 = rotate_jvp(self.mb, self.normal, n, dn, spin, dspin)
+        du = uj - ui + cross(wj, rj) - cross(wi, ri)
+        ddu = duj - dui + cross(dwj, rj) + cross(wj, drj) - cross(dwi, ri) - cross(wi, dri)
+        dw, ddw = wj - wi, dwj - dwi
+        nd, tw = dot(du, n)[:, None], dot(dw, n)[:, None]
+        dnd = dot(ddu, n)[:, None] + dot(du, dn)[:, None]
+        dtw = dot(ddw, n)[:, None] + dot(dw, dn)[:, None]
+        kn, ks, kt, kb = (k[:, None] for k in (self.kn, self.ks, self.kt, self.kb))
+        fn_mid = self.fn[:, None] + .5*kn*nd
+        dfn_mid = .5*kn*dnd
+        fs_mid = fs0 + .5*ks*(du - nd*n)
+        dfs_mid = dfs0 + .5*ks*(ddu - dnd*n - nd*dn)
+        mt_mid = self.mt[:, None] + .5*kt*tw
+        dmt_mid = .5*kt*dtw
+        dmb_mid = dmb0 + .5*kb*(ddw - dtw*n - tw*dn)
+        f = fn_mid*n + fs_mid
+        df = dfn_mid*n + fn_mid*dn + dfs_mid
+        dcouple = dmt_mid*n + mt_mid*dn + dmb_mid
+        dti = cross(dri, f) + cross(ri, df) + dcouple
+        dtj = -cross(drj, f) - cross(rj, df) - dcouple
+        out = scatter_add(self.n_sites, i, np.concatenate((df, dti), 1))
+        out += scatter_add(self.n_sites, j, np.concatenate((-df, dtj), 1))
+        return out
+
+    def jacobian_vector(self, y, direction, dt, external):
+        """J d of the midpoint residual; ``bonded_dem_newton.py:88-92`` (torch.func.jvp
+        there) with the derivative of ``bonded_dem_jvp_warp.py:106-116``."""
+        result = self.mass*direction - .5*dt*dt*self.midpoint_force_jvp(y, direction)
+        return np.where(self.fixed[:, None], direction, result)
+
+    def prepare_scaling(self, trial, dt):
+        """``bonded_dem_newton.py:94-102``."""
+        self.n, self.ri, self.rj = trial['n'], trial['ri'], trial['rj']
+        self.diagonal = self._diagonal_blocks()
+        self.block = np.einsum('ni,ij->nij', self.mass, np.eye(6)) + .25*dt*dt*self.diagonal
+        self.block[self.fixed] = np.eye(6)
+        self.preconditioner = np.linalg.inv(self.block)
+        self.units = np.ones_like(self.mass)
+        self.units[:, :3] = self.radii[:, None]
+        self.units[self.fixed] = 1.
+
+    def scale_residual(self, r):
+        """``bonded_dem_newton.py:104-105``."""
+        return np.einsum('nij,nj->ni', self.preconditioner, r)/self.units
+
+    def elastic_precondition(self, vector, dt, tolerance=.03, max_iterations=80):
+        """Block-Jacobi PCG on M + dt^2/4 K; ``bonded_dem_newton.py:107-130``."""
+        rhs = np.einsum('nij,nj->ni', self.block, self.units*vector)
+        rhs[self.fixed] = 0
+        x = np.zeros_like(rhs); r = rhs.copy()
+        z = np.einsum('nij,nj->ni', self.preconditioner, r)
+        direction = z.copy(); rz = (r*z).sum(); initial = float(rz)
+        if initial == 0:
+            return x
+        for iteration in range(max_iterations):
+            ad = self._operator(direction, .25*dt*dt)
+            denominator = (direction*ad).sum()
+            alpha = rz/denominator
+            x += alpha*direction; r -= alpha*ad
+            z = np.einsum('nij,nj->ni', self.preconditioner, r)
+            following = (r*z).sum()
+            if iteration % 5 == 0 and float(following) <= tolerance*tolerance*initial:
+                break
+            direction = z + (following/rz)*direction; rz = following
+        self.inner_iterations += iteration+1
+        return x/self.units
+
+    def step(self, dt, external, tolerance=2e-7, max_iterations=12, *,
+             pose_tolerance=2e-6, backend='fgmres', linear_tolerance=1e-6,
+             preconditioning='elastic'):
+        """Line-searched Newton on the implicit-midpoint residual; ``bonded_dem_newton.py:132-201``."""
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('Positive finite dt required')
+        y = np.zeros_like(self.v)
+        rhs_scale = max(float(np.linalg.norm(dt*self.mass*self.v + .5*dt*dt*external)),
+                        .5*dt*dt*float(np.linalg.norm(self.loads()[~self.fixed])), 1e-30)
+        krylov, self.inner_iterations = 0, 0
+        residual_trace = []
+        relative = local = float('nan')
+        for iteration in range(max_iterations+1):
+            trial = self.trial(y)
+            self.prepare_scaling(trial, dt)
+            r = self.residual(y, dt, external)
+            scaled = self.scale_residual(r)
+            relative, local = float(np.linalg.norm(r))/rhs_scale, float(np.abs(scaled).max())
+            residual_trace.append([relative, local])
+            if relative < tolerance and local < pose_tolerance:
+                velocity = 2*y/dt - self.v
+                rotation = exp_rotation(y[:, 3:])@self.rotation
+                self.commit(trial)
+                self.v, self.rotation = velocity, rotation
+                self.time += dt
+                return float((external*y).sum()), dict(
+                    nonlinear_iterations=iteration, nonlinear_relative_residual=relative,
+                    local_pose_defect=local, krylov_iterations=krylov,
+                    cg_iterations=self.inner_iterations, residual_trace=residual_trace,
+                    max_step_rotation=float(np.linalg.norm(y[:, 3:], axis=1).max()))
+            if iteration == max_iterations:
+                break
+
+            def operator(v):
+                return self.scale_residual(self.jacobian_vector(y, self.units*v, dt, external))
+            if backend == 'dense':
+                free = np.flatnonzero(~np.repeat(self.fixed, 6))
+                if len(free) > 400:
+                    raise ValueError('Dense reference limited to 400 free DOFs')
+                columns = []
+                for col in np.eye(len(free)):
+                    direction = np.zeros(y.size); direction[free] = col
+                    columns.append(operator(direction.reshape(y.shape)).ravel()[free])
+                jac = np.stack(columns, 1)
+                delta = np.zeros(y.size)
+                delta[free] = np.linalg.solve(jac, -scaled.ravel()[free])
+                delta = delta.reshape(y.shape)
+            elif backend == 'fgmres':
+                if preconditioning == 'elastic':
+                    precondition = lambda v: self.elastic_precondition(v, dt)
+                elif preconditioning == 'block':
+                    precondition = lambda v: v
+                else:
+                    raise ValueError(preconditioning)
+                delta, metrics = fgmres(operator, -scaled, precondition, tolerance=linear_tolerance)
+                krylov += metrics['iterations']
+            else:
+                raise ValueError(backend)
+            correction = self.units*delta
+            correction[self.fixed] = 0
+            merit = float(np.linalg.norm(scaled))
+            accepted = False
+            for power in range(10):
+                factor = 2.**(-power)
+                candidate = y + factor*correction
+                try:
+                    value = self.scale_residual(self.residual(candidate, dt, external))
+                except RuntimeError as error:
+                    if 'Subdivide:' not in str(error):
+                        raise
+                    continue
+                if float(np.linalg.norm(value)) < (1-1e-4*factor)*merit:
+                    y = candidate; accepted = True; break
+            if not accepted:
+                raise SubdivideError('Subdivide: Newton line search failed')
+        raise SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
+
+
+class AdaptiveIntervals:
+    """Remembered subdivision depth; ``experiments/bonded_dem_adaptive.py:4-23``."""
+
+    def __init__(self, solver):
+        self.solver = solver
+        self.depth = 0
+        self.easy_intervals = 0
+
+    def advance(self, dt, load):
+        work, records = 0., []
+        for _ in range(2**self.depth):
+            value, info = self.solver.advance_interval(dt/(2**self.depth), load, depth=self.depth)
+            work += value; records.extend(info)
+        self.depth = max(item['subdivision_depth'] for item in records)
+        if max(item['nonlinear_iterations'] for item in records) <= 3:
+            self.easy_intervals += 1
+        else:
+            self.easy_intervals = 0
+        if self.easy_intervals >= 8 and self.depth:
+            self.depth -= 1
+            self.easy_intervals = 0
+        return work, records
+
+
+def reference_stiffness(points, pairs, contacts, kn, ks, kb, kt):
+    """Dense 6N x 6N stress-free K from B^T D B + A^T H A.
+
+    Restates ``experiments/bonded_dem_dynamics.py:22-47`` (returned dense for
+    the small oracle cases instead of SciPy CSR).
+    """
+    x = np.asarray(points, dtype=np.float64)
+    i, j = np.asarray(pairs).T
+    d = x[j] - x[i]
+    n = d/np.linalg.norm(d, axis=1)[:, None]
+    ri, rj = contacts - x[i], contacts - x[j]
+    count = len(n)
+    b, a = np.zeros((count, 3, 12)), np.zeros((count, 3, 12))
+    b[:, :, :3], b[:, :, 3:6] = -np.eye(3), skew(ri)
+    b[:, :, 6:9], b[:, :, 9:12] = np.eye(3), -skew(rj)
+    a[:, :, 3:6], a[:, :, 9:12] = -np.eye(3), np.eye(3)
+    nn = n[:, :, None]*n[:, None, :]
+    dd = ks[:, None, None]*np.eye(3) + (kn-ks)[:, None, None]*nn
+    hh = kb[:, None, None]*np.eye(3) + (kt-kb)[:, None, None]*nn
+    local = np.einsum('eai,eab,ebj->eij', b, dd, b) + np.einsum('eai,eab,ebj->eij', a, hh, a)
+    idx = np.concatenate((6*i[:, None] + np.arange(6), 6*j[:, None] + np.arange(6)), 1)
+    k = np.zeros((6*len(x), 6*len(x)))
+    for e in range(count):
+        k[np.ix_(idx[e], idx[e])] += local[e]
+    return k

@@ -1,0 +1,134 @@
+"""Pin the NumPy oracle against vectors produced by the reference's own code."""
+import numpy as np
+import pytest
+
+from oracle import dem
+from tests.conftest import golden, newton_inputs, STATE
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b))/max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_newton(g, prefix='state_'):
+    s = dem.NewtonBonds(**newton_inputs(g))
+    for k in STATE:
+        setattr(s, k, np.array(g[prefix + k]))
+    return s
+
+
+@pytest.mark.parametrize('case', ['newton_prestressed', 'newton_unstressed'])
+def test_trial_force_jvp_precondition(case):
+    g = golden(case)
+    s = oracle_newton(g)
+    y, dt, ext = g['y'], float(g['dt']), g['external']
+    trial = s.trial(y)
+    for k in ('force', 'n', 'ri', 'rj', 'x', 'normal', 'fn', 'fs', 'mt', 'mb', 'offset'):
+        assert rel(trial[k], g[f'trial_{k}']) < 1e-13, k
+    assert rel(s.midpoint_force(y), g['midpoint_force']) < 1e-13
+    assert rel(s.residual(y, dt, ext), g['residual']) < 1e-13
+    assert rel(s.loads(), g['loads']) < 1e-13
+    assert abs(s.energy() - float(g['energy'])) <= 1e-13*abs(float(g['energy']))
+    s.prepare_scaling(trial, dt)
+    for k in ('diagonal', 'block', 'units'):
+        assert rel(getattr(s, k), g[f'scaling_{k}']) < 1e-13, k
+    assert rel(s.preconditioner, g['scaling_preconditioner']) < 1e-9
+    # analytic JVP vs the reference's torch.func.jvp (reference bar 2e-11, scaled norm)
+    jv = s.jacobian_vector(y, g['jvp_direction'], dt, ext)
+    ref = g['jvp']
+    err = np.linalg.norm(s.scale_residual(jv - ref))/np.linalg.norm(s.scale_residual(ref))
+    assert err < 2e-11
+    assert rel(s.stiffness(g['q']), g['stiffness_q']) < 1e-13
+    s.inner_iterations = 0
+    x = s.elastic_precondition(g['vector'], dt)
+    assert rel(x, g['elastic_precondition']) < 1e-8
+    assert s.inner_iterations == int(g['elastic_inner_iterations'])
+
+
+@pytest.mark.parametrize('case', ['newton_prestressed', 'newton_unstressed'])
+@pytest.mark.parametrize('tag,backend,pc', [('fgmres_elastic', 'fgmres', 'elastic'),
+                                            ('fgmres_block', 'fgmres', 'block'),
+                                            ('dense', 'dense', 'elastic')])
+def test_full_step(case, tag, backend, pc):
+    g = golden(case)
+    s = oracle_newton(g)
+    work, info = s.step(float(g['dt']), g['step_load'], tolerance=2e-7, backend=backend,
+                        preconditioning=pc, linear_tolerance=1e-7)
+    assert info['nonlinear_iterations'] == int(g[f'step_{tag}_nonlinear_iterations'])
+    assert info['krylov_iterations'] == int(g[f'step_{tag}_krylov_iterations'])
+    assert info['cg_iterations'] == int(g[f'step_{tag}_cg_iterations'])
+    # the reference's own cross-solver bars (bonded_dem_newton_checks.py:130-132)
+    assert np.abs(s.x - g[f'step_{tag}_state_x']).max() < 1e-9
+    assert np.abs(s.rotation - g[f'step_{tag}_state_rotation']).max() < 1e-8
+    assert abs(work - float(g[f'step_{tag}_work'])) <= 1e-9*abs(float(g[f'step_{tag}_work']))
+
+
+def test_linear_217_against_dense_k():
+    g = golden('linear_217')
+    p, pairs = g['points'], g['pairs']
+    s = dem.LinearBonds(p, g['radii'], pairs, g['areas'], g['contacts'], np.ones(len(p)),
+                        np.zeros(len(p), bool))
+    q = g['q']
+    assert rel(s.stiffness(q), g['stiffness_q']) < 1e-13
+    assert rel(s.stiffness(q).ravel(), g['dense_k']@q.ravel()) < 1e-12
+    assert np.abs(s.diagonal - g['diagonal']).max() < 1e-12
+    k = dem.reference_stiffness(p, pairs, g['contacts'], s.kn, s.ks, s.kb, s.kt)
+    assert np.abs(k - g['dense_k']).max() < 1e-10
+
+
+def test_tangent_81():
+    g = golden('tangent_81')
+    s = dem.LinearBonds(g['points'], np.ones(50), g['pairs'], np.ones(len(g['pairs'])), g['contacts'],
+                        np.ones(50), np.zeros(50, bool))
+    assert rel(s.stiffness(g['q']), g['stiffness_q']) < 1e-13
+    assert rel(s.diagonal, g['diagonal']) < 1e-13
+
+
+def test_finite_history_953():
+    g = golden('finite_953')
+    s = dem.FiniteBonds(g['points'], g['radii'], g['pairs'], g['areas'], np.ones(8), np.zeros(8, bool))
+    for end, v, w in zip(g['ends'], g['vs'], g['ws']):
+        s.commit(s.trial(np.c_[v, w]*.01, end_positions=end))
+    for k in ('fn', 'fs', 'mt', 'mb'):
+        assert rel(getattr(s, k), g[f'fin_{k}']) < 1e-12
+        assert rel(getattr(s, k), g[f'cpu_{k}']) < 1e-12
+    loads = s.loads()
+    assert rel(loads, g['fin_loads']) < 1e-12
+    assert np.linalg.norm(loads[:, :3] - g['cpu_force']) + np.linalg.norm(loads[:, 3:] - g['cpu_torque']) < 1e-10
+
+
+def test_fgmres_381():
+    g = golden('fgmres_381')
+    a, b = g['a'], g['b']
+    calls = [0]
+
+    def variable_precondition(v):
+        calls[0] += 1
+        return v/(np.diag(a)*(1+.08*np.sin(calls[0])))
+    x, info = dem.fgmres(lambda z: a@z, b, variable_precondition, tolerance=1e-10, restart=24)
+    assert info['iterations'] == int(g['iterations'])
+    assert rel(x, g['x']) < 1e-12
+    assert rel(x, np.linalg.solve(a, b)) < 1e-9
+
+
+def test_lattice8_three_steps():
+    g = golden('lattice8')
+    s = dem.NewtonBonds(g['points'], g['radii'], g['pairs'], g['areas'], g['masses'], g['fixed'],
+                        young=float(g['young']), shear=float(g['shear']))
+    infos = []
+    for step in range(3):
+        work, info = s.step(float(g['dt']), g['load'], tolerance=1e-6)
+        infos.append([info['nonlinear_iterations'], info['krylov_iterations'], info['cg_iterations']])
+        assert abs(work - float(g[f'work_{step}'])) <= 1e-9*abs(float(g[f'work_{step}']))
+    assert np.array_equal(np.array(infos), g['iterations'])
+    for k in STATE:
+        assert np.abs(getattr(s, k) - g[f'state_{k}']).max() <= 1e-9*max(1., np.abs(g[f'state_{k}']).max()), k
+
+
+def test_transport_guard_and_transactional_trial():
+    g = golden('newton_prestressed')
+    s = oracle_newton(g)
+    before = {k: getattr(s, k).copy() for k in STATE}
+    with pytest.raises(RuntimeError, match='Subdivide:'):
+        s.trial(np.ones_like(s.mass))
+    assert all(np.array_equal(getattr(s, k), v) for k, v in before.items())
