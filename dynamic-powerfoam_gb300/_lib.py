@@ -1,0 +1,103 @@
+"""ctypes binding of ``libdpf_gb300.so`` (declared in ``include/dpf_gb300.h``).
+
+There is no fallback: if the library cannot be loaded the import of the
+solver fails with an error naming the missing file and how to build it.
+"""
+import ctypes
+import os
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIBRARY = HERE/'libdpf_gb300.so'
+
+DPF_ERR_ROTATION = 1
+DPF_ERR_COINCIDENT = 2
+DPF_ERR_NORMAL_TURN = 4
+DPF_ERR_NONFINITE = 8
+DPF_ERR_NOT_CONVERGED = 16
+DPF_ERR_BARRIER_TIMEOUT = 32
+DPF_ERR_ARGUMENT = 1 << 16
+DPF_ERR_CUDA = 1 << 17
+
+c_double_p = ctypes.c_void_p
+i64, i32, f64, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+
+
+class Graph(ctypes.Structure):
+    _fields_ = [('n_sites', i64), ('n_bonds', i64), ('edges', vp), ('inc_ptr', vp), ('inc_bond', vp)]
+
+
+class Stiffness(ctypes.Structure):
+    _fields_ = [('kn', vp), ('ks', vp), ('kb', vp), ('kt', vp)]
+
+
+class History(ctypes.Structure):
+    _fields_ = [('x', vp), ('radii', vp), ('normal', vp), ('offset', vp), ('fn', vp), ('fs', vp),
+                ('mt', vp), ('mb', vp)]
+
+
+class Tangent(ctypes.Structure):
+    _fields_ = [('n', vp), ('ri', vp), ('rj', vp)]
+
+
+class TrialOut(ctypes.Structure):
+    _fields_ = [('force', vp), ('n', vp), ('ri', vp), ('rj', vp), ('x_end', vp), ('normal_end', vp),
+                ('offset_end', vp), ('fs_end', vp), ('mb_end', vp), ('fn_end', vp), ('mt_end', vp)]
+
+
+P = ctypes.POINTER
+SIGNATURES = {
+    'dpf_wrench_scratch_doubles': (i64, [i64]),
+    'dpf_partials_doubles': (i64, []),
+    'dpf_elastic_workspace_doubles': (i64, [i64]),
+    'dpf_stiffness_apply': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp, vp]),
+    'dpf_diagonal_blocks': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp]),
+    'dpf_prepare_scaling': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp, f64, vp, vp, vp, vp, vp]),
+    'dpf_trial': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, i32, P(TrialOut), vp, vp, vp]),
+    'dpf_residual': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, vp, f64, P(TrialOut), vp, vp,
+                           vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_scale_residual': (i32, [i64, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_jacobian_vector': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, f64, vp, vp, vp, vp, vp]),
+    'dpf_elastic_precondition': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp, vp, vp, vp, f64, f64, i32,
+                                       vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_loads': (i32, [P(Graph), P(History), vp, vp, vp]),
+    'dpf_accept_step': (i32, [i64, vp, f64, vp, vp, vp]),
+    'dpf_energy': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, vp]),
+    'dpf_arnoldi_cgs2': (i32, [i64, vp, i64, i32, vp, vp, vp, vp]),
+    'dpf_combine_rows': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
+    'dpf_dot_norm': (i32, [i64, vp, vp, vp, vp, vp]),
+    'dpf_axpby': (i32, [i64, f64, vp, f64, vp, vp, vp]),
+    'dpf_rhs_scale': (i32, [i64, vp, vp, vp, vp, vp, f64, vp, vp, vp]),
+    'dpf_masked_scale': (i32, [i64, vp, vp, vp, vp, vp]),
+}
+
+
+class LibraryError(RuntimeError):
+    pass
+
+
+_LIB = None
+
+
+def load():
+    """Load the CUDA library once; raise if it is missing or incomplete."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = Path(os.environ.get('DPF_GB300_LIBRARY', LIBRARY))
+    if not path.exists():
+        raise LibraryError(f'{path} is missing: build it with `python -c "import __graft_entry__ as g; g.build()"` '
+                           'or `python dynamic-powerfoam_gb300/build.py` (needs nvcc); there is no CPU fallback')
+    lib = ctypes.CDLL(str(path))
+    for name, (restype, argtypes) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    _LIB = lib
+    return lib
+
+
+def check(code, name):
+    """Raise for argument/launch errors returned by an entry point."""
+    if code:
+        raise LibraryError(f'{name} failed with status {code:#x}')

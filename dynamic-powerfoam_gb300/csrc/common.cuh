@@ -1,0 +1,203 @@
+// Shared device code for the bonded-DEM kernels: 3-vector math, the contact
+// transport of the rate law, block reductions and a time-limited grid barrier.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "dpf_gb300.h"
+
+namespace dpf {
+
+constexpr int kThreads = 256;
+// cos(0.25) rounded to double, the threshold of the reference transport guard.
+constexpr double kCosQuarter = 0.9689124217106447;
+// Grid barriers give up after this many nanoseconds and report
+// DPF_ERR_BARRIER_TIMEOUT instead of waiting forever.
+constexpr unsigned long long kBarrierTimeoutNs = 1000000000ull;
+
+struct d3 {
+    double x, y, z;
+};
+
+__device__ __forceinline__ d3 mk(double a, double b, double c) { return {a, b, c}; }
+__device__ __forceinline__ d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ d3 operator-(d3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ d3 operator*(double s, d3 a) { return {s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ d3 operator/(d3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ d3 cross(d3 a, d3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ double norm(d3 a) { return sqrt(dot(a, a)); }
+
+__device__ __forceinline__ d3 ld3(const double *p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ d3 ld3(const double *p, int64_t i) { return ld3(p + 3 * i); }
+__device__ __forceinline__ void st3(double *p, d3 v) { p[0] = v.x; p[1] = v.y; p[2] = v.z; }
+__device__ __forceinline__ void st3(double *p, int64_t i, d3 v) { st3(p + 3 * i, v); }
+
+__device__ __forceinline__ void edge(const int64_t *edges, int64_t b, int64_t &i, int64_t &j) {
+    const longlong2 e = reinterpret_cast<const longlong2 *>(edges)[b];
+    i = e.x;
+    j = e.y;
+}
+
+// Rotation that carries vectors from a bond frame with normal n0 to one with
+// normal n1 (shortest arc) and then spins them about n1 by spin . bisector:
+// the `transport` of experiments/bonded_dem_finite_gpu.py:22-32.
+struct Transport {
+    d3 k, n1;
+    double inv1pc, c, s;
+};
+
+__device__ __forceinline__ Transport make_transport(d3 n0, d3 n1, d3 spin, int &flags) {
+    Transport t;
+    t.k = cross(n0, n1);
+    const double cosine = fmin(fmax(dot(n0, n1), -1.0), 1.0);
+    if (cosine < kCosQuarter) flags |= DPF_ERR_NORMAL_TURN;
+    t.inv1pc = 1.0 / (1.0 + cosine);
+    d3 b = n0 + n1;
+    b = b / fmax(norm(b), 1e-12);
+    sincos(dot(spin, b), &t.s, &t.c);
+    t.n1 = n1;
+    return t;
+}
+
+__device__ __forceinline__ d3 apply(const Transport &t, d3 v) {
+    const d3 kv = cross(t.k, v);
+    d3 out = v + kv;
+    out = out + t.inv1pc * cross(t.k, kv);
+    return t.c * out + t.s * cross(t.n1, out) + ((1.0 - t.c) * dot(t.n1, out)) * t.n1;
+}
+
+// ---- reductions -----------------------------------------------------------
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// Block-wide sum (all threads get the result).  Fixed order: deterministic.
+__device__ __forceinline__ double block_sum(double v) {
+    __shared__ double buf[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) buf[warp] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? buf[threadIdx.x] : 0.0;
+    if (warp == 0) v = warp_sum(v);
+    if (threadIdx.x == 0) buf[0] = v;
+    __syncthreads();
+    v = buf[0];
+    __syncthreads();
+    return v;
+}
+
+__device__ __forceinline__ double block_max(double v) {
+    __shared__ double buf[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    v = warp_max(v);
+    __syncthreads();
+    if (lane == 0) buf[warp] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    v = (threadIdx.x < nw) ? buf[threadIdx.x] : -INFINITY;
+    if (warp == 0) v = warp_max(v);
+    if (threadIdx.x == 0) buf[0] = v;
+    __syncthreads();
+    v = buf[0];
+    __syncthreads();
+    return v;
+}
+
+// Sum of `count` values spaced `stride` apart, in a fixed order (every block
+// that calls this with the same data gets the bit-identical result).
+__device__ __forceinline__ double block_sum_array(const double *p, int count, int stride = 1) {
+    double v = 0.0;
+    for (int k = threadIdx.x; k < count; k += blockDim.x) v += p[(int64_t)k * stride];
+    return block_sum(v);
+}
+
+__device__ __forceinline__ double block_max_array(const double *p, int count, int stride = 1) {
+    double v = -INFINITY;
+    for (int k = threadIdx.x; k < count; k += blockDim.x) v = fmax(v, p[(int64_t)k * stride]);
+    return block_max(v);
+}
+
+// "Last block finishes" protocol: every block has written its partial(s);
+// returns true in exactly one block, after all partials are visible.  The
+// counter lives in device memory, starts at zero and is reset by the last block.
+__device__ __forceinline__ bool last_block(unsigned *counter) {
+    __shared__ bool is_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned ticket = atomicAdd(counter, 1u);
+        is_last = (ticket == gridDim.x - 1);
+        if (is_last) *counter = 0u;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
+// ---- grid barrier for cooperative (co-resident) launches --------------------
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// barrier[0] = arrival count, barrier[1] = generation.  Returns false when the
+// wait ran past kBarrierTimeoutNs (the status word then carries the error).
+__device__ __forceinline__ bool grid_barrier(unsigned *barrier, int *status) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        ok = 1;
+        const unsigned gen = ld_acquire(barrier + 1);
+        __threadfence();
+        const unsigned arrived = atomicAdd(barrier, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(barrier, 0u);
+            __threadfence();
+            atomicAdd(barrier + 1, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire(barrier + 1) == gen) {
+                if (global_ns() - t0 > kBarrierTimeoutNs) {
+                    atomicOr(status, DPF_ERR_BARRIER_TIMEOUT);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+}  // namespace dpf
+
+#define DPF_CHECK_LAUNCH()                                   \
+    do {                                                     \
+        if (cudaGetLastError() != cudaSuccess) return DPF_ERR_CUDA; \
+    } while (0)

@@ -1,0 +1,745 @@
+"""Drop-in GPU bonded-DEM solvers: ``LinearBonds``, ``FiniteBonds``, ``NewtonBonds``.
+
+The classes keep the constructors, attributes (tensor names, shapes and
+layouts), methods, plug-in points and error behaviour of the reference's
+``LinearBondsGPU`` (``experiments/bonded_dem_linear_gpu.py``),
+``FiniteBondsGPU`` (``experiments/bonded_dem_finite_gpu.py``) and
+``NewtonBonds`` / ``FastNewtonBonds`` (``experiments/bonded_dem_newton.py``,
+``experiments/bonded_dem_newton_fast.py``).  All tensors are float64 CUDA
+tensors in the reference layouts; every bond sweep, block operation, Krylov
+vector operation and reduction of the Newton path runs in the sm_103a kernels
+of ``libdpf_gb300.so`` on ``torch.cuda.current_stream()``.
+
+A method the caller replaces on an instance (``s.jacobian_vector = f`` as
+``FastNewtonBonds`` does) is honoured: ``step`` then calls the replacement
+through the reference's generic code path.
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+F64 = torch.float64
+
+
+class SubdivideError(RuntimeError):
+    """Recoverable failure; the message starts with 'Subdivide:' as in the reference."""
+
+
+_GUARD_MESSAGES = (
+    (_lib.DPF_ERR_ROTATION, 'Subdivide: body rotation exceeds .25 rad in a step'),
+    (_lib.DPF_ERR_COINCIDENT, 'Subdivide: coincident centers'),
+    (_lib.DPF_ERR_NORMAL_TURN, 'Subdivide: normal turns more than .25 rad per half-step'),
+    (_lib.DPF_ERR_NONFINITE, 'Subdivide: non-finite residual'),
+    (_lib.DPF_ERR_BARRIER_TIMEOUT, 'Subdivide: device barrier timed out'),
+)
+
+
+def guard_error(status):
+    """The reference's exception for a device status bitmask (first guard in reference order)."""
+    for bit, message in _GUARD_MESSAGES:
+        if status & bit:
+            return SubdivideError(message)
+    return SubdivideError(f'Subdivide: device status {status:#x}')
+
+
+def _addr(t):
+    return None if t is None else t.data_ptr()
+
+
+def incidence(edges, n_sites):
+    """Incidence CSR of the bond graph in the reference's index_add_ order.
+
+    For every site: first the bonds whose first endpoint it is (value b, in
+    increasing b), then those whose second endpoint it is (value ~b).
+    """
+    edges = np.asarray(edges, dtype=np.int64).reshape(-1, 2)
+    m = len(edges)
+    site = np.concatenate((edges[:, 0], edges[:, 1]))
+    value = np.concatenate((np.arange(m, dtype=np.int64), ~np.arange(m, dtype=np.int64)))
+    order = np.argsort(site, kind='stable')
+    counts = np.bincount(site, minlength=n_sites)
+    ptr = np.zeros(n_sites + 1, dtype=np.int64)
+    np.cumsum(counts, out=ptr[1:])
+    return ptr.astype(np.int32), value[order].astype(np.int32)
+
+
+class LinearBonds:
+    """Stress-free linearised bonds (drop-in for ``LinearBondsGPU``,
+    ``experiments/bonded_dem_linear_gpu.py:14-124``)."""
+
+    def __init__(self, points, radii, pairs, areas, contacts, masses, fixed,
+                 young=1200., shear=480., device='cuda'):
+        self.device = torch.device(device)
+        if self.device.type != 'cuda':
+            raise ValueError('dpf_gb300 solvers run on CUDA devices only')
+        if self.device.index is None:
+            self.device = torch.device('cuda', torch.cuda.current_device())
+        self._lib = _lib.load()
+        self.tensor = lambda x: torch.as_tensor(x, dtype=F64, device=self.device)
+        # Setup arithmetic (bonded_dem_linear_gpu.py:15-40) on the host, once.
+        p = np.array(points, dtype=np.float64)
+        edges = np.array(pairs, dtype=np.int64).reshape(-1, 2)
+        if len(edges) and (edges.min() < 0 or edges.max() >= len(p)):
+            raise ValueError('Invalid endpoint index')
+        r = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
+        area = np.broadcast_to(np.asarray(areas, dtype=np.float64), (len(edges),))
+        c = np.asarray(contacts, dtype=np.float64).reshape(-1, 3)
+        i, j = edges[:, 0], edges[:, 1]
+        distance = p[j] - p[i]
+        length = np.linalg.norm(distance, axis=1)
+        second = area**2/(4*np.pi)
+        mass = np.broadcast_to(np.asarray(masses, dtype=np.float64), (len(p),))
+        inertia = .4*mass*r*r
+        mass6 = np.concatenate((np.repeat(mass[:, None], 3, 1), np.repeat(inertia[:, None], 3, 1)), 1)
+        if np.any(mass6 <= 0):
+            raise ValueError('Only positive-mass bodies can enter this solver')
+        self.p = self.tensor(p)
+        self.edges = torch.as_tensor(edges, dtype=torch.long, device=self.device).contiguous()
+        self.i, self.j = self.edges.T
+        self.n = self.tensor(distance/length[:, None])
+        self.ri, self.rj = self.tensor(c - p[i]), self.tensor(c - p[j])
+        self.kn, self.ks = self.tensor(young*area/length), self.tensor(shear*area/length)
+        self.kb, self.kt = self.tensor(young*second/length), self.tensor(shear*(2*second)/length)
+        self.mass = self.tensor(mass6)
+        self.fixed = torch.as_tensor(np.asarray(fixed, dtype=bool), device=self.device)
+        ptr, inc = incidence(edges, len(p))
+        self._inc_ptr = torch.as_tensor(ptr, device=self.device)
+        self._inc_bond = torch.as_tensor(inc, device=self.device)
+        n_sites, n_bonds = len(p), len(edges)
+        self._graph = _lib.Graph(n_sites, n_bonds, self.edges.data_ptr() if n_bonds else None,
+                                 self._inc_ptr.data_ptr(), self._inc_bond.data_ptr())
+        self._wrench = torch.empty(max(1, self._lib.dpf_wrench_scratch_doubles(n_bonds)), dtype=F64,
+                                   device=self.device)
+        self._partials = torch.zeros(self._lib.dpf_partials_doubles(), dtype=F64, device=self.device)
+        self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._scalars = torch.zeros(8, dtype=F64, device=self.device)
+        self._host_status = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self._host_scalars = torch.zeros(64, dtype=F64).pin_memory()
+        self.q, self.v = torch.zeros_like(self.mass), torch.zeros_like(self.mass)
+        self.kq = torch.zeros_like(self.mass)
+        self.diagonal = self._diagonal_blocks()
+        self.preconditioner = None
+        self.preconditioner_dt = None
+
+    # ---- plumbing ---------------------------------------------------------
+    @property
+    def n_sites(self):
+        return int(self._graph.n_sites)
+
+    @property
+    def n_bonds(self):
+        return int(self._graph.n_bonds)
+
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _vec(self, a, shape=None):
+        a = torch.as_tensor(a, dtype=F64, device=self.device)
+        return a.contiguous()
+
+    def _stiffness_struct(self):
+        return _lib.Stiffness(*(_addr(t.contiguous()) for t in (self.kn, self.ks, self.kb, self.kt)))
+
+    def _tangent_struct(self):
+        for name in ('n', 'ri', 'rj'):
+            t = getattr(self, name)
+            if not t.is_contiguous():
+                setattr(self, name, t.contiguous())
+        return _lib.Tangent(self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr())
+
+    def _call(self, name, *args):
+        _lib.check(getattr(self._lib, name)(*args), name)
+
+    def _fetch(self, scalars=0, status=False):
+        """Copy device scalars (and the status word) to the host with one sync."""
+        stream = torch.cuda.current_stream(self.device)
+        if scalars:
+            self._host_scalars[:scalars].copy_(self._scalars[:scalars], non_blocking=True)
+        if status:
+            self._host_status.copy_(self._status, non_blocking=True)
+        stream.synchronize()
+        return self._host_scalars[:scalars].tolist(), int(self._host_status[0]) if status else 0
+
+    # ---- reference methods ------------------------------------------------
+    @torch.no_grad()
+    def stiffness(self, q):
+        """Frozen-tangent K q (``bonded_dem_linear_gpu.py:42-52``)."""
+        q = self._vec(q)
+        out = torch.empty_like(q)
+        self._call('dpf_stiffness_apply', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), q.data_ptr(), out.data_ptr(), self._wrench.data_ptr(),
+                   self._stream())
+        return out
+
+    @torch.no_grad()
+    def _diagonal_blocks(self):
+        """Per-site 6x6 diagonal blocks of K (``bonded_dem_linear_gpu.py:54-72``)."""
+        out = torch.empty((self.n_sites, 6, 6), dtype=F64, device=self.device)
+        self._call('dpf_diagonal_blocks', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), out.data_ptr(), self._stream())
+        return out
+
+    def _operator(self, q, alpha):
+        """(diag M + alpha K) q, identity rows on fixed sites (``bonded_dem_linear_gpu.py:74-77``)."""
+        out = self.mass*q + alpha*self.stiffness(q)
+        out[self.fixed] = q[self.fixed]
+        return out
+
+    @torch.no_grad()
+    def solve_increment(self, rhs, dt, guess=None, tolerance=2e-8, max_iterations=1000):
+        """Block-Jacobi PCG of the linear model (``bonded_dem_linear_gpu.py:79-112``)."""
+        alpha = dt*dt/4
+        if self.preconditioner_dt != dt:
+            diagonal = torch.diag_embed(self.mass) + alpha*self.diagonal
+            diagonal[self.fixed] = torch.eye(6, device=self.device, dtype=F64)
+            self.preconditioner = torch.linalg.inv(diagonal)
+            self.preconditioner_dt = dt
+        rhs = rhs.clone(); rhs[self.fixed] = 0
+        norm = float(torch.linalg.vector_norm(rhs))
+        if norm < 1e-30:
+            return torch.zeros_like(rhs), dict(iterations=0, relative_residual=0.)
+        x = torch.zeros_like(rhs) if guess is None else guess.clone()
+        x[self.fixed] = 0
+        residual = rhs - self._operator(x, alpha)
+        z = torch.einsum('nij,nj->ni', self.preconditioner, residual)
+        direction = z.clone(); rz = (residual*z).sum()
+        for iteration in range(max_iterations):
+            ad = self._operator(direction, alpha)
+            step = rz/(direction*ad).sum()
+            x += step*direction; residual -= step*ad
+            if iteration % 10 == 0:
+                relative = float(torch.linalg.vector_norm(residual))/norm
+                if relative < tolerance:
+                    break
+                if not np.isfinite(relative):
+                    raise RuntimeError('Nonfinite conjugate-gradient residual')
+            z = torch.einsum('nij,nj->ni', self.preconditioner, residual)
+            next_rz = (residual*z).sum()
+            direction = z + (next_rz/rz)*direction; rz = next_rz
+        actual = float(torch.linalg.vector_norm(rhs - self._operator(x, alpha)))/norm
+        if actual > 5*tolerance or not np.isfinite(actual):
+            raise RuntimeError(f'Linear solve failed after {iteration+1} iterations: {actual}')
+        return x, dict(iterations=iteration+1, relative_residual=actual)
+
+    @torch.no_grad()
+    def step(self, dt, external):
+        """Linear implicit midpoint (``bonded_dem_linear_gpu.py:114-121``)."""
+        rhs = dt*self.mass*self.v + .5*dt*dt*(external - self.kq)
+        dq, metrics = self.solve_increment(rhs, dt, guess=dt*self.v)
+        self.v = 2*dq/dt - self.v
+        self.q += dq; self.kq = self.stiffness(self.q)
+        return float((external*dq).sum()), metrics
+
+    def energy(self):
+        return float(.5*((self.mass*self.v*self.v).sum() + (self.q*self.kq).sum()))
+
+
+class FiniteBonds(LinearBonds):
+    """Finite-motion rate law (drop-in for ``FiniteBondsGPU``,
+    ``experiments/bonded_dem_finite_gpu.py:46-261``)."""
+
+    PHYSICAL_STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
+
+    def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None,
+                 young=1200., shear=480., device='cuda'):
+        p = np.asarray(points, dtype=np.float64)
+        i, j = np.asarray(pairs, dtype=np.int64).reshape(-1, 2).T
+        radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
+        n = p[j] - p[i]
+        n /= np.linalg.norm(n, axis=1)[:, None]
+        classical = .5*(p[i] + p[j]) + .5*(radii_a[i] - radii_a[j])[:, None]*n
+        if contacts is None:
+            contacts = classical
+        contacts = np.asarray(contacts, dtype=np.float64)
+        super().__init__(p, radii_a, pairs, areas, contacts, masses, fixed, young, shear, device)
+        self.x = self.p.clone()
+        self.radii = self.tensor(np.array(radii_a))
+        self.normal = self.n.clone()
+        self.offset = self.tensor(contacts - classical)
+        self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
+        self.fs, self.mb = torch.zeros_like(self.n), torch.zeros_like(self.n)
+        self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(self.n_sites, 1, 1)
+        self.time = 0.
+
+    def _history_struct(self):
+        for name in ('x', 'radii', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb'):
+            t = getattr(self, name)
+            if not (t.is_contiguous() and t.dtype == F64):
+                setattr(self, name, t.to(F64).contiguous())
+        return _lib.History(self.x.data_ptr(), self.radii.data_ptr(), self.normal.data_ptr(), self.offset.data_ptr(),
+                            self.fn.data_ptr(), self.fs.data_ptr(), self.mt.data_ptr(), self.mb.data_ptr())
+
+    def _raise_status(self):
+        _, status = self._fetch(status=True)
+        if status:
+            raise guard_error(status)
+
+    def geometry(self, x):
+        """Bond normal and classical contact (``bonded_dem_finite_gpu.py:66-73``)."""
+        d = x[self.j] - x[self.i]
+        length = torch.linalg.vector_norm(d, dim=1)
+        if bool(torch.any(length <= 1e-12)):
+            raise SubdivideError('Subdivide: coincident centers')
+        n = d/length[:, None]
+        c = .5*(x[self.i] + x[self.j]) + .5*(self.radii[self.i] - self.radii[self.j])[:, None]*n
+        return n, c
+
+    def assemble(self, fn, fs, mt, mb, n, ri, rj):
+        """Scatter bond force and couple to sites (``bonded_dem_finite_gpu.py:75-80``)."""
+        f, couple = fn[:, None]*n + fs, mt[:, None]*n + mb
+        out = torch.zeros_like(self.mass)
+        out.index_add_(0, self.i, torch.cat((f, torch.linalg.cross(ri, f) + couple), 1))
+        out.index_add_(0, self.j, torch.cat((-f, -torch.linalg.cross(rj, f) - couple), 1))
+        return out
+
+    @torch.no_grad()
+    def loads(self):
+        """Net force and torque of the committed state (``bonded_dem_finite_gpu.py:82-85``)."""
+        out = torch.empty_like(self.mass)
+        self._call('dpf_loads', ctypes.byref(self._graph), ctypes.byref(self._history_struct()), out.data_ptr(),
+                   self._wrench.data_ptr(), self._stream())
+        return out
+
+    def _new_trial(self):
+        m, n = self.n_bonds, self.n_sites
+        e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
+        return dict(force=e(n, 6), n=e(m, 3), ri=e(m, 3), rj=e(m, 3), x=e(n, 3), normal=e(m, 3), fn=e(m),
+                    mt=e(m), fs=e(m, 3), mb=e(m, 3), offset=e(m, 3))
+
+    @staticmethod
+    def _trial_struct(t, end=True):
+        g = lambda k: _addr(t.get(k)) if t is not None else None
+        if not end:
+            return _lib.TrialOut(g('force'), g('n'), g('ri'), g('rj'))
+        return _lib.TrialOut(g('force'), g('n'), g('ri'), g('rj'), g('x'), g('normal'), g('offset'), g('fs'),
+                             g('mb'), g('fn'), g('mt'))
+
+    @torch.no_grad()
+    def trial(self, increment, *, mid_positions=None, end_positions=None, _check=True):
+        """Pure constitutive trial from committed history (``bonded_dem_finite_gpu.py:87-116``)."""
+        y = self._vec(increment)
+        mid = None if mid_positions is None else self._vec(mid_positions)
+        end = None if end_positions is None else self._vec(end_positions)
+        out = self._new_trial()
+        self._status.zero_()
+        self._call('dpf_trial', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._history_struct()), y.data_ptr(), _addr(mid), _addr(end), 1,
+                   ctypes.byref(self._trial_struct(out)), self._wrench.data_ptr(), self._status.data_ptr(),
+                   self._stream())
+        if _check:
+            self._raise_status()
+        return out
+
+    def commit(self, trial):
+        """Adopt a trial's end state (``bonded_dem_finite_gpu.py:118-120``)."""
+        for name in ('x', 'normal', 'fn', 'fs', 'mt', 'mb', 'offset'):
+            setattr(self, name, trial[name])
+
+    @torch.no_grad()
+    def energy(self):
+        """Elastic plus kinetic energy (``bonded_dem_finite_gpu.py:122-125``)."""
+        v = self._vec(self.v)
+        self._call('dpf_energy', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._history_struct()), self.mass.data_ptr(), v.data_ptr(),
+                   self._scalars.data_ptr(), self._partials.data_ptr(), self._stream())
+        values, _ = self._fetch(1)
+        return values[0]
+
+    def local_defect(self, residual):
+        """Max block-scaled pose defect (``bonded_dem_finite_gpu.py:127-131``)."""
+        correction = torch.einsum('nij,nj->ni', self.preconditioner, residual)
+        scale = torch.ones_like(correction)
+        scale[:, :3] = self.radii[:, None]
+        return float((correction/scale).abs().max())
+
+    def advance_interval(self, dt, force_at_time, depth=0):
+        """Recursive dt bisection on 'Subdivide:' (``bonded_dem_finite_gpu.py:252-261``)."""
+        try:
+            work, info = self.step(dt, force_at_time(self.time + .5*dt))
+            return work, [dict(dt=dt, subdivision_depth=depth, **info)]
+        except RuntimeError as error:
+            if depth >= 8 or 'Subdivide:' not in str(error):
+                raise
+            a, ia = self.advance_interval(.5*dt, force_at_time, depth+1)
+            b, ib = self.advance_interval(.5*dt, force_at_time, depth+1)
+            return a+b, ia+ib
+
+
+class _Krylov:
+    """Device workspace of one FGMRES cycle (basis, transformed rows, h column)."""
+
+    def __init__(self, length, width, device):
+        self.length, self.width = length, width
+        self.basis = torch.empty((width+1, length), dtype=F64, device=device)
+        self.transformed = torch.empty((width, length), dtype=F64, device=device)
+        self.h = torch.zeros(72, dtype=F64, device=device)
+
+
+def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iterations=256, *, workspace=None):
+    """Right-preconditioned flexible GMRES with CGS2 Arnoldi on CUDA tensors.
+
+    Same signature, iteration and stopping rules as the reference
+    (``experiments/bonded_dem_newton.py:13-60``); the Arnoldi
+    orthogonalisation, row combination and norms run in library kernels and
+    the (restart+1) x restart Hessenberg/Givens recurrence stays on the host,
+    read back once per Arnoldi step as in the reference.
+    """
+    lib = _lib.load()
+    device = rhs.device
+    stream = torch.cuda.current_stream(device).cuda_stream
+    shape = rhs.shape
+    b = rhs.reshape(-1).to(F64).contiguous()
+    length = b.numel()
+    partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=device)
+    scal = torch.zeros(2, dtype=F64, device=device)
+
+    def norm_of(v):
+        _lib.check(lib.dpf_dot_norm(length, v.data_ptr(), None, scal.data_ptr(), partials.data_ptr(), stream),
+                   'dpf_dot_norm')
+        return float(scal[1])
+
+    norm = norm_of(b)
+    x = torch.zeros_like(b)
+    if norm == 0:
+        return x.reshape(shape), dict(iterations=0, relative_residual=0.)
+    residual = b.clone(); iterations = 0
+    relative = float('nan')
+    while iterations < max_iterations:
+        width = min(restart, max_iterations - iterations)
+        ws = workspace if (workspace is not None and workspace.width >= width and workspace.length == length) \
+            else _Krylov(length, width, device)
+        h = np.zeros((width+1, width)); cs, sn = np.zeros(width), np.zeros(width)
+        g = np.zeros(width+1); g[0] = norm_of(residual)
+        _lib.check(lib.dpf_axpby(length, 1./g[0], residual.data_ptr(), 0., residual.data_ptr(),
+                                 ws.basis[0].data_ptr(), stream), 'dpf_axpby')
+        for j in range(width):
+            z = precondition(ws.basis[j].reshape(shape)).reshape(-1).to(F64).contiguous()
+            _lib.check(lib.dpf_axpby(length, 1., z.data_ptr(), 0., z.data_ptr(), ws.transformed[j].data_ptr(),
+                                     stream), 'dpf_axpby')
+            w = operator(ws.transformed[j].reshape(shape)).reshape(-1).to(F64).contiguous()
+            if w.data_ptr() == ws.transformed[j].data_ptr():
+                w = w.clone()
+            _lib.check(lib.dpf_arnoldi_cgs2(length, ws.basis.data_ptr(), length, j, w.data_ptr(), ws.h.data_ptr(),
+                                            partials.data_ptr(), stream), 'dpf_arnoldi_cgs2')
+            column = ws.h[:j+2].cpu().numpy()
+            h[:j+1, j] = column[:j+1]
+            h[j+1, j] = column[j+1]
+            breakdown = h[j+1, j] < 1e-14
+            for k in range(j):
+                h[k, j], h[k+1, j] = cs[k]*h[k, j] + sn[k]*h[k+1, j], -sn[k]*h[k, j] + cs[k]*h[k+1, j]
+            denominator = np.hypot(h[j, j], h[j+1, j])
+            if denominator == 0:
+                raise SubdivideError('Subdivide: singular Newton linear system')
+            cs[j], sn[j] = h[j, j]/denominator, h[j+1, j]/denominator
+            h[j, j], h[j+1, j] = denominator, 0.
+            g[j+1], g[j] = -sn[j]*g[j], cs[j]*g[j]
+            iterations += 1
+            if abs(g[j+1]) <= tolerance*norm or breakdown or j+1 == width:
+                coefficients = np.ascontiguousarray(np.linalg.solve(h[:j+1, :j+1], g[:j+1]), dtype=np.float64)
+                _lib.check(lib.dpf_combine_rows(length, ws.transformed.data_ptr(), length, j+1,
+                                                coefficients.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                                x.data_ptr(), stream), 'dpf_combine_rows')
+                ax = operator(x.reshape(shape)).reshape(-1).to(F64).contiguous()
+                _lib.check(lib.dpf_axpby(length, 1., b.data_ptr(), -1., ax.data_ptr(), residual.data_ptr(), stream),
+                           'dpf_axpby')
+                relative = norm_of(residual)/norm
+                if relative <= 1.05*tolerance:
+                    return x.reshape(shape), dict(iterations=iterations, relative_residual=relative)
+                break
+    raise SubdivideError(f'Subdivide: FGMRES did not converge ({relative:g})')
+
+
+class NewtonBonds(FiniteBonds):
+    """Scaled Newton-FGMRES on the unchanged rate law (drop-in for ``NewtonBonds``
+    and ``FastNewtonBonds``, ``experiments/bonded_dem_newton.py:63-201``)."""
+
+    PLUGINS = ('jacobian_vector', 'elastic_precondition', '_diagonal_blocks', 'stiffness')
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        self._inner = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self._inner_host = 0
+        self._pcg_workspace = None
+        self._barrier = torch.zeros(2, dtype=torch.int32, device=self.device)
+        self._krylov = None
+        self.block = None
+        self.units = None
+
+    # inner_iterations accumulates on the device; reading it synchronises.
+    @property
+    def inner_iterations(self):
+        return self._inner_host + int(self._inner.item())
+
+    @inner_iterations.setter
+    def inner_iterations(self, value):
+        self._inner.zero_()
+        self._inner_host = int(value)
+
+    def _overridden(self, name):
+        return name in self.__dict__
+
+    @torch.no_grad()
+    def midpoint_force(self, y):
+        """Midpoint force of the trial (``bonded_dem_newton.py:64-81``)."""
+        return self.trial(y, _check=False)['force']
+
+    @torch.no_grad()
+    def residual(self, y, dt, external):
+        """``bonded_dem_newton.py:83-86``."""
+        y, v, ext = self._vec(y), self._vec(self.v), self._vec(external)
+        r = torch.empty_like(y)
+        self._status.zero_()
+        self._call('dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._history_struct()), y.data_ptr(), v.data_ptr(), ext.data_ptr(),
+                   self.mass.data_ptr(), self.fixed.data_ptr(), float(dt), None, None, None, r.data_ptr(), None,
+                   None, self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(),
+                   self._stream())
+        self._raise_status()
+        return r
+
+    @torch.no_grad()
+    def jacobian_vector(self, y, direction, dt, external):
+        """J d of the midpoint residual (``bonded_dem_newton.py:88-92``,
+        ``bonded_dem_jvp_warp.py:45-116``)."""
+        return self._jvp(self._vec(y), self._vec(direction), dt)
+
+    def _jvp(self, y, direction, dt, units=None, preconditioner=None):
+        out = torch.empty_like(direction)
+        self._call('dpf_jacobian_vector', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._history_struct()), y.data_ptr(), direction.data_ptr(), self.mass.data_ptr(),
+                   self.fixed.data_ptr(), float(dt), _addr(units), _addr(preconditioner), out.data_ptr(),
+                   self._wrench.data_ptr(), self._stream())
+        return out
+
+    @torch.no_grad()
+    def prepare_scaling(self, trial, dt):
+        """Block scaling of the Newton system (``bonded_dem_newton.py:94-102``)."""
+        self.n, self.ri, self.rj = trial['n'], trial['ri'], trial['rj']
+        if self._overridden('_diagonal_blocks'):
+            self.diagonal = self._diagonal_blocks()
+            self.block = torch.diag_embed(self.mass) + .25*dt*dt*self.diagonal
+            self.block[self.fixed] = torch.eye(6, dtype=F64, device=self.device)
+            self.preconditioner = torch.linalg.inv(self.block)
+            self.units = torch.ones_like(self.mass)
+            self.units[:, :3] = self.radii[:, None]
+            self.units[self.fixed] = 1.
+            return
+        n = self.n_sites
+        if self.block is None or self.block.shape[0] != n:
+            self.diagonal = torch.empty((n, 6, 6), dtype=F64, device=self.device)
+            self.block = torch.empty_like(self.diagonal)
+            self.preconditioner = torch.empty_like(self.diagonal)
+            self.units = torch.empty_like(self.mass)
+        self._call('dpf_prepare_scaling', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(),
+                   self.radii.data_ptr(), float(dt), self.diagonal.data_ptr(), self.block.data_ptr(),
+                   self.preconditioner.data_ptr(), self.units.data_ptr(), self._stream())
+
+    @torch.no_grad()
+    def scale_residual(self, r):
+        """P r / units (``bonded_dem_newton.py:104-105``)."""
+        r = self._vec(r)
+        out = torch.empty_like(r)
+        self._call('dpf_scale_residual', self.n_sites, self.preconditioner.data_ptr(), self.units.data_ptr(),
+                   r.data_ptr(), out.data_ptr(), None, None, self._stream())
+        return out
+
+    @torch.no_grad()
+    def elastic_precondition(self, vector, dt, tolerance=.03, max_iterations=80):
+        """Block-Jacobi PCG on M + dt^2/4 K (``bonded_dem_newton.py:107-130``,
+        ``bonded_dem_precondition_warp.py:127-151``), one cooperative launch."""
+        vector = self._vec(vector)
+        if self._overridden('stiffness'):
+            return self._elastic_precondition_generic(vector, dt, tolerance, max_iterations)
+        if self._pcg_workspace is None:
+            self._pcg_workspace = torch.empty(self._lib.dpf_elastic_workspace_doubles(self.n_sites), dtype=F64,
+                                              device=self.device)
+        out = torch.empty_like(vector)
+        self._call('dpf_elastic_precondition', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(),
+                   self.block.data_ptr(), self.preconditioner.data_ptr(), self.units.data_ptr(), vector.data_ptr(),
+                   float(dt), float(tolerance), int(max_iterations), out.data_ptr(), self._inner.data_ptr(),
+                   self._wrench.data_ptr(), self._pcg_workspace.data_ptr(), self._barrier.data_ptr(),
+                   self._status.data_ptr(), self._stream())
+        return out
+
+    def _elastic_precondition_generic(self, vector, dt, tolerance, max_iterations):
+        rhs = torch.einsum('nij,nj->ni', self.block, self.units*vector)
+        rhs[self.fixed] = 0
+        x = torch.zeros_like(rhs); r = rhs.clone()
+        z = torch.einsum('nij,nj->ni', self.preconditioner, r)
+        direction = z.clone(); rz = (r*z).sum(); initial = float(rz)
+        if initial == 0:
+            return x
+        for iteration in range(max_iterations):
+            ad = self._operator(direction, .25*dt*dt)
+            alpha = rz/(direction*ad).sum()
+            x += alpha*direction; r -= alpha*ad
+            z = torch.einsum('nij,nj->ni', self.preconditioner, r)
+            following = (r*z).sum()
+            if iteration % 5 == 0 and float(following) <= tolerance*tolerance*initial:
+                break
+            direction = z + (following/rz)*direction; rz = following
+        self._inner_host += iteration+1
+        return x/self.units
+
+    # ---- the Newton step ---------------------------------------------------
+    def _evaluate(self, y, dt, external, tangent_out=None, scaled=None):
+        """Residual at y with every trial guard; returns (r, [|r|, max|s|, |s|], status)."""
+        r = torch.empty_like(y)
+        self._status.zero_()
+        use_p = tangent_out is None
+        self._call('dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._history_struct()), y.data_ptr(), self._v.data_ptr(), external.data_ptr(),
+                   self.mass.data_ptr(), self.fixed.data_ptr(), float(dt),
+                   ctypes.byref(self._trial_struct(tangent_out, end=False)) if tangent_out else None,
+                   self.preconditioner.data_ptr() if use_p else None, self.units.data_ptr() if use_p else None,
+                   r.data_ptr(), _addr(scaled) if use_p else None, self._scalars.data_ptr() if use_p else None,
+                   self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream())
+        return r
+
+    @torch.no_grad()
+    def step(self, dt, external, tolerance=2e-7, max_iterations=12, *,
+             pose_tolerance=2e-6, backend='fgmres', linear_tolerance=1e-6,
+             preconditioning='elastic'):
+        """Line-searched Newton on the implicit-midpoint residual (``bonded_dem_newton.py:132-201``)."""
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('Positive finite dt required')
+        dt = float(dt)
+        external = self._vec(external)
+        self._v = self._vec(self.v).clone()
+        y = torch.zeros_like(self._v)
+        stream = self._stream()
+        loads = self.loads()
+        self._call('dpf_rhs_scale', self.n_sites, self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
+                   loads.data_ptr(), self.fixed.data_ptr(), dt, self._scalars.data_ptr(), self._partials.data_ptr(),
+                   stream)
+        (a, l), _ = self._fetch(2)
+        rhs_scale = max(a, .5*dt*dt*l, 1e-30)
+        krylov = 0
+        self.inner_iterations = 0
+        residual_trace = []
+        relative = local = float('nan')
+        generic_jvp = self._overridden('jacobian_vector')
+        generic_pc = self._overridden('elastic_precondition')
+        m, n6 = self.n_bonds, 6*self.n_sites
+        for iteration in range(max_iterations+1):
+            tangent = dict(force=None, n=torch.empty((m, 3), dtype=F64, device=self.device),
+                           ri=torch.empty((m, 3), dtype=F64, device=self.device),
+                           rj=torch.empty((m, 3), dtype=F64, device=self.device))
+            r = self._evaluate(y, dt, external, tangent_out=tangent)
+            _, status = self._fetch(status=True)
+            if status:
+                raise guard_error(status)
+            self.prepare_scaling(tangent, dt)
+            scaled = torch.empty_like(r)
+            self._call('dpf_scale_residual', self.n_sites, self.preconditioner.data_ptr(), self.units.data_ptr(),
+                       r.data_ptr(), scaled.data_ptr(), self._scalars.data_ptr(), self._partials.data_ptr(), stream)
+            (rnorm, local, merit), _ = self._fetch(3)
+            relative = rnorm/rhs_scale
+            if not np.isfinite(relative) or not np.isfinite(local):
+                raise SubdivideError(f'Subdivide: non-finite Newton residual ({relative:g}, {local:g})')
+            residual_trace.append([relative, local])
+            if relative < tolerance and local < pose_tolerance:
+                state = self.trial(y)
+                rotation = self._vec(self.rotation).clone()
+                self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(),
+                           rotation.data_ptr(), stream)
+                self.commit(state)
+                self.v, self.rotation = self._v, rotation
+                self.time += dt
+                self._call('dpf_dot_norm', n6, external.data_ptr(), y.data_ptr(), self._scalars.data_ptr(),
+                           self._partials.data_ptr(), stream)
+                (work,), _ = self._fetch(1)
+                max_rotation = float(torch.linalg.vector_norm(y[:, 3:], dim=1).max()) if len(y) else 0.
+                return work, dict(nonlinear_iterations=iteration, nonlinear_relative_residual=relative,
+                                  local_pose_defect=local, krylov_iterations=krylov,
+                                  cg_iterations=self.inner_iterations, residual_trace=residual_trace,
+                                  max_step_rotation=max_rotation)
+            if iteration == max_iterations:
+                break
+            units, pre = self.units, self.preconditioner
+            if generic_jvp:
+                def operator(v):
+                    return self.scale_residual(self.jacobian_vector(y, units*v, dt, external))
+            else:
+                def operator(v):
+                    return self._jvp(y, self._vec(v), dt, units=units, preconditioner=pre)
+            if backend == 'dense':
+                free = torch.nonzero(~self.fixed.repeat_interleave(6)).flatten()
+                if len(free) > 400:
+                    raise ValueError('Dense reference limited to 400 free DOFs')
+                eye = torch.eye(len(free), dtype=F64, device=self.device)
+                columns = []
+                for col in eye:
+                    direction = torch.zeros_like(y).flatten(); direction[free] = col
+                    columns.append(operator(direction.reshape_as(y)).flatten()[free])
+                jac = torch.stack(columns, dim=1)
+                delta = torch.zeros_like(y).flatten()
+                delta[free] = torch.linalg.solve(jac, -scaled.flatten()[free])
+                delta = delta.reshape_as(y)
+            elif backend == 'fgmres':
+                if preconditioning == 'elastic':
+                    precondition = (lambda v: self.elastic_precondition(v, dt))
+                elif preconditioning == 'block':
+                    precondition = (lambda v: v)
+                else:
+                    raise ValueError(preconditioning)
+                if self._krylov is None or self._krylov.length != n6:
+                    self._krylov = _Krylov(n6, 32, self.device)
+                rhs = torch.empty_like(scaled)
+                self._call('dpf_axpby', n6, -1., scaled.data_ptr(), 0., scaled.data_ptr(), rhs.data_ptr(), stream)
+                delta, metrics = fgmres(operator, rhs, precondition, tolerance=linear_tolerance,
+                                        workspace=self._krylov)
+                krylov += metrics['iterations']
+            else:
+                raise ValueError(backend)
+            delta = self._vec(delta)
+            correction = torch.empty_like(delta)
+            self._call('dpf_masked_scale', self.n_sites, delta.data_ptr(), self.units.data_ptr(),
+                       self.fixed.data_ptr(), correction.data_ptr(), stream)
+            accepted = False
+            candidate = torch.empty_like(y)
+            for power in range(10):
+                factor = 2.**(-power)
+                self._call('dpf_axpby', n6, 1., y.data_ptr(), factor, correction.data_ptr(), candidate.data_ptr(),
+                           stream)
+                self._evaluate(candidate, dt, external)
+                (_, _, value), status = self._fetch(3, status=True)
+                if status:
+                    continue
+                if value < (1 - 1e-4*factor)*merit:
+                    y = candidate; accepted = True; break
+            if not accepted:
+                raise SubdivideError('Subdivide: Newton line search failed')
+        raise SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
+
+
+FastNewtonBonds = NewtonBonds
+
+
+class AdaptiveIntervals:
+    """Remember a successful subdivision depth (``experiments/bonded_dem_adaptive.py:4-23``)."""
+
+    def __init__(self, solver):
+        self.solver = solver
+        self.depth = 0
+        self.easy_intervals = 0
+
+    def advance(self, dt, load):
+        work, records = 0., []
+        for _ in range(2**self.depth):
+            value, info = self.solver.advance_interval(dt/(2**self.depth), load, depth=self.depth)
+            work += value; records.extend(info)
+        self.depth = max(item['subdivision_depth'] for item in records)
+        if max(item['nonlinear_iterations'] for item in records) <= 3:
+            self.easy_intervals += 1
+        else:
+            self.easy_intervals = 0
+        if self.easy_intervals >= 8 and self.depth:
+            self.depth -= 1
+            self.easy_intervals = 0
+        return work, records

@@ -1,0 +1,230 @@
+/*
+ * dpf_gb300.h — C ABI of the GB300 bonded-DEM Newton path (libdpf_gb300.so).
+ *
+ * Every entry point takes borrowed device pointers in the reference's tensor
+ * layouts, sizes, and a cudaStream_t passed as void*.  The library never
+ * allocates, frees or keeps a pointer after the call returns; scratch buffers
+ * are supplied by the caller and their sizes are given next to each entry.
+ *
+ * Layouts (row-major, float64 unless stated):
+ *   per-site 6-vectors  (N, 6) = [tx, ty, tz, rx, ry, rz]
+ *   positions           (N, 3); radii, masses (N); mass (N, 6)
+ *   fixed               (N) uint8 (0/1, the bytes of a torch.bool tensor)
+ *   edges               (M, 2) int64, the bond normal points edges[b,0] -> edges[b,1]
+ *   per-bond vectors    (M, 3); per-bond scalars (M)
+ *   6x6 site blocks     (N, 6, 6)
+ *
+ * Incidence CSR (built once by the caller from edges): for site s the entries
+ * inc_bond[inc_ptr[s] .. inc_ptr[s+1]) list first the bonds b with
+ * edges[b,0] == s as the value b, in increasing b, then the bonds with
+ * edges[b,1] == s as the value ~b (= -b-1), in increasing b.  This order is the
+ * order in which the reference's index_add_ adds the two endpoints.
+ *
+ * Status: every entry returns 0 on success or a bitmask of dpf_status.  Guard
+ * failures detected on the device (the reference's 'Subdivide:' errors) are
+ * OR-ed into a caller-supplied device int (`status`), which the caller reads
+ * after the stream reaches the call; the return value only reports argument
+ * and launch errors.  No kernel traps or waits without a time limit.
+ */
+#ifndef DPF_GB300_H
+#define DPF_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum dpf_status {
+    DPF_OK = 0,
+    DPF_ERR_ROTATION = 1,        /* body rotation > 0.25 rad in a step        */
+    DPF_ERR_COINCIDENT = 2,      /* bond length <= 1e-12                       */
+    DPF_ERR_NORMAL_TURN = 4,     /* contact normal turns > 0.25 rad per half step */
+    DPF_ERR_NONFINITE = 8,       /* non-finite value in a reduction            */
+    DPF_ERR_NOT_CONVERGED = 16,  /* bounded iteration limit reached            */
+    DPF_ERR_BARRIER_TIMEOUT = 32,/* a grid barrier gave up after its time limit */
+    DPF_ERR_ARGUMENT = 1 << 16,  /* invalid argument (host check)              */
+    DPF_ERR_CUDA = 1 << 17       /* CUDA launch/runtime error                  */
+};
+
+/* Bond graph: reference edges plus the incidence CSR described above. */
+typedef struct dpf_graph {
+    int64_t n_sites;
+    int64_t n_bonds;
+    const int64_t *edges;      /* (M, 2)   */
+    const int32_t *inc_ptr;    /* (N + 1)  */
+    const int32_t *inc_bond;   /* (2 M)    */
+} dpf_graph;
+
+/* Bond stiffnesses kn = E A/L, ks = G A/L, kb = E I/L, kt = 2 G I/L (M each). */
+typedef struct dpf_stiffness {
+    const double *kn, *ks, *kb, *kt;
+} dpf_stiffness;
+
+/* Committed state of the finite-motion rate law (FiniteBondsGPU attributes). */
+typedef struct dpf_history {
+    const double *x;       /* (N, 3) centres            */
+    const double *radii;   /* (N)                        */
+    const double *normal;  /* (M, 3) committed normals   */
+    const double *offset;  /* (M, 3) contact offsets     */
+    const double *fn;      /* (M)   normal force         */
+    const double *fs;      /* (M, 3) shear force on i    */
+    const double *mt;      /* (M)   twist couple         */
+    const double *mb;      /* (M, 3) bending couple      */
+} dpf_history;
+
+/* Frozen tangent geometry: bond normal and contact levers (M, 3) each. */
+typedef struct dpf_tangent {
+    const double *n, *ri, *rj;
+} dpf_tangent;
+
+/* Outputs of a constitutive trial.  Any pointer except `force` may be NULL. */
+typedef struct dpf_trial_out {
+    double *force;                       /* (N, 6) midpoint force and torque       */
+    double *n, *ri, *rj;                 /* (M, 3) midpoint tangent geometry        */
+    double *x_end;                       /* (N, 3)                                  */
+    double *normal_end, *offset_end;     /* (M, 3)                                  */
+    double *fs_end, *mb_end;             /* (M, 3)                                  */
+    double *fn_end, *mt_end;             /* (M)                                     */
+} dpf_trial_out;
+
+/* Size in doubles of the per-bond wrench scratch used by bond sweeps: 9 M. */
+int64_t dpf_wrench_scratch_doubles(int64_t n_bonds);
+
+/* K q, the frozen-tangent stiffness product.
+ * Replaces LinearBondsGPU.stiffness (experiments/bonded_dem_linear_gpu.py:42-52)
+ * and WarpTangent.__call__ (experiments/bonded_dem_tangent_warp.py:33-44).
+ * wrench: scratch of dpf_wrench_scratch_doubles(M) doubles. */
+int dpf_stiffness_apply(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
+                        const double *q, double *out, double *wrench, void *stream);
+
+/* Per-site 6x6 diagonal blocks of K (N, 6, 6).
+ * Replaces LinearBondsGPU._diagonal_blocks (experiments/bonded_dem_linear_gpu.py:54-72)
+ * and WarpDiagonal.__call__ (experiments/bonded_dem_precondition_warp.py:111-118). */
+int dpf_diagonal_blocks(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
+                        double *diagonal, void *stream);
+
+/* Block scaling of the Newton system: diagonal = D(K), block = diag(mass) +
+ * dt^2/4 D with identity rows on fixed sites, preconditioner = block^-1,
+ * units = [r, r, r, 1, 1, 1] (1 on fixed sites).  Any output may be NULL
+ * except preconditioner.
+ * Replaces NewtonBonds.prepare_scaling (experiments/bonded_dem_newton.py:94-102). */
+int dpf_prepare_scaling(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
+                        const double *mass, const uint8_t *fixed, const double *radii, double dt,
+                        double *diagonal, double *block, double *preconditioner, double *units,
+                        void *stream);
+
+/* Pure constitutive trial at increment y (N, 6); no committed state changes.
+ * mid_positions / end_positions (N, 3) may be NULL (then x + y/2, x + y).
+ * want_end = 0 skips the end-of-step histories but keeps every guard.
+ * Replaces FiniteBondsGPU.trial (experiments/bonded_dem_finite_gpu.py:87-116). */
+int dpf_trial(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+              const double *y, const double *mid_positions, const double *end_positions,
+              int want_end, const dpf_trial_out *out, double *wrench, int *status, void *stream);
+
+/* Midpoint residual r = M (y - dt v) - dt^2/2 (f_mid(y) + external), fixed
+ * rows r = y, computed with the guards of a full trial; optionally also the
+ * scaled residual s = P r / units and, in `norms` (3 doubles, device),
+ * [|r|_2, max|s|, |s|_2].  preconditioner/units/scaled may be NULL.
+ * Replaces NewtonBonds.residual + scale_residual (experiments/bonded_dem_newton.py:83-86, 104-105). */
+int dpf_residual(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+                 const double *y, const double *v, const double *external, const double *mass,
+                 const uint8_t *fixed, double dt, const dpf_trial_out *trial,
+                 const double *preconditioner, const double *units,
+                 double *residual, double *scaled, double *norms,
+                 double *wrench, double *partials, int *status, void *stream);
+
+/* Scaled residual s = P r / units and norms[0..2] = [|r|_2, max|s|, |s|_2]
+ * (device doubles; scaled and norms may be NULL).
+ * Replaces NewtonBonds.scale_residual and the norms of NewtonBonds.step
+ * (experiments/bonded_dem_newton.py:104-105, 146-147). */
+int dpf_scale_residual(int64_t n_sites, const double *preconditioner, const double *units,
+                       const double *residual, double *scaled, double *norms, double *partials,
+                       void *stream);
+
+/* Jacobian-vector product of the midpoint residual:
+ * out = mass * d - dt^2/2 * (d f_mid(y)[d]), fixed rows out = d, where
+ * d = units * direction when units != NULL.  When preconditioner != NULL the
+ * result is scaled: out = P (J d) / units (the Newton operator).
+ * Replaces NewtonBonds.jacobian_vector (experiments/bonded_dem_newton.py:88-92)
+ * and WarpJacobian (experiments/bonded_dem_jvp_warp.py:45-116). */
+int dpf_jacobian_vector(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+                        const double *y, const double *direction, const double *mass,
+                        const uint8_t *fixed, double dt, const double *units,
+                        const double *preconditioner, double *out, double *wrench, void *stream);
+
+/* Size in doubles of the elastic PCG workspace for N sites. */
+int64_t dpf_elastic_workspace_doubles(int64_t n_sites);
+
+/* Block-Jacobi PCG on (diag M + dt^2/4 K) with the reference's stopping rule
+ * (test every 5th iteration at r.z <= tol^2 r0.z0), rhs = block (units * vector),
+ * result out = x / units.  One cooperative launch runs all iterations; the
+ * iteration count (0 when the right-hand side vanishes) is ADDED to
+ * *iterations (device int), as the reference adds to inner_iterations.  workspace: dpf_elastic_workspace_doubles(N);
+ * barrier: 2 zeroed unsigned ints (device).
+ * Replaces NewtonBonds.elastic_precondition (experiments/bonded_dem_newton.py:107-130)
+ * and WarpElastic (experiments/bonded_dem_precondition_warp.py:127-151). */
+int dpf_elastic_precondition(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
+                             const double *mass, const uint8_t *fixed, const double *block,
+                             const double *preconditioner, const double *units,
+                             const double *vector, double dt, double tolerance, int max_iterations,
+                             double *out, int *iterations, double *wrench, double *workspace,
+                             unsigned *barrier, int *status, void *stream);
+
+/* Net loads (force, torque) of the committed state (N, 6).
+ * Replaces FiniteBondsGPU.loads (experiments/bonded_dem_finite_gpu.py:82-85). */
+int dpf_loads(const dpf_graph *g, const dpf_history *h, double *out, double *wrench, void *stream);
+
+/* Accepted-step update: v <- 2 y / dt - v and rotation <- exp(y_w) rotation.
+ * Replaces the commit block of NewtonBonds.step (experiments/bonded_dem_newton.py:149-154)
+ * with exp_rotation (experiments/bonded_dem_finite_gpu.py:35-43). */
+int dpf_accept_step(int64_t n_sites, const double *y, double dt, double *v, double *rotation,
+                    void *stream);
+
+/* Elastic plus kinetic energy (one double, device).
+ * Replaces FiniteBondsGPU.energy (experiments/bonded_dem_finite_gpu.py:122-125). */
+int dpf_energy(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+               const double *mass, const double *v, double *energy, double *partials, void *stream);
+
+/* ---- FGMRES building blocks (experiments/bonded_dem_newton.py:13-60) ---- */
+
+/* Size in doubles of the reduction partials used by the vector kernels. */
+int64_t dpf_partials_doubles(void);
+
+/* Twice-iterated classical Gram-Schmidt of w against basis rows 0..j
+ * (row stride ld) followed by h[0..j] = projections, h[j+1] = |w|, and, when
+ * |w| >= 1e-14, basis row j+1 = w / |w|.  h is a device array of j+2 doubles.
+ * Replaces the Arnoldi body of fgmres (experiments/bonded_dem_newton.py:35-43). */
+int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w, double *h,
+                     double *partials, void *stream);
+
+/* x += sum_{k<count} coefficients[k] * rows[k]  (coefficients on the host, count <= 64).
+ * Replaces `x += transformed[:j+1].T @ coefficients` (experiments/bonded_dem_newton.py:54). */
+int dpf_combine_rows(int64_t length, const double *rows, int64_t ld, int count,
+                     const double *coefficients, double *x, void *stream);
+
+/* result[0] = sum a*b and result[1] = sqrt(sum a*a) over `length` doubles (device). */
+int dpf_dot_norm(int64_t length, const double *a, const double *b, double *result,
+                 double *partials, void *stream);
+
+/* out = alpha * a + beta * b over `length` doubles. */
+int dpf_axpby(int64_t length, double alpha, const double *a, double beta, const double *b,
+              double *out, void *stream);
+
+/* out[0] = |dt mass*v + dt^2/2 external|_2, out[1] = |loads on free sites|_2
+ * (device doubles); the two terms of rhs_scale in NewtonBonds.step
+ * (experiments/bonded_dem_newton.py:138-139). */
+int dpf_rhs_scale(int64_t n_sites, const double *mass, const double *v, const double *external,
+                  const double *loads, const uint8_t *fixed, double dt, double *out,
+                  double *partials, void *stream);
+
+/* out = units * a with zero rows on fixed sites, the Newton correction of
+ * NewtonBonds.step (experiments/bonded_dem_newton.py:186-187). */
+int dpf_masked_scale(int64_t n_sites, const double *a, const double *units, const uint8_t *fixed,
+                     double *out, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DPF_GB300_H */
