@@ -1,0 +1,292 @@
+#!/usr/bin/env python
+"""Benchmark: implicit Newton solves per second of the bonded-DEM solver.
+
+Workload (one "step" = one Newton solve of one implicit-midpoint time step,
+``NewtonBonds.step`` at relative residual 1e-6): a 64^3 jittered-lattice foam
+(262,144 sites, ~1.95M bonds; seeded synthetic input, generator in
+``dynamic-powerfoam_gb300/foam.py``) with density 1000, gravity -9.81 z,
+bottom layer fixed, dt = 1e-3, successive steps of one trajectory.
+
+Prints one JSON line.  ``value`` is solves/s with the load already in HBM;
+``e2e`` is the same through the public API with the load copied from pinned
+host memory and the new positions copied back every step.  The working set
+(about 0.5 GB of bond state) is larger than L2, so no flush is needed.
+
+``--impl reference`` times the reference algorithm on the host CPU instead
+(the NumPy restatement in ``oracle/``, the reference code itself does not
+travel), on a bounded sample of the same workload.
+Multi-GPU (torchrun): independent replicas, one foam per rank, no collective
+on the data path; rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = 'implicit Newton solves/s at rel. residual 1e-6 (64^3 jittered foam, 262k sites, ~1.95M bonds)'
+UNIT = 'solves/s'
+SMI_FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+              'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+              'clocks_event_reasons.sw_power_cap')
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument('--gpus', type=int, default=1)
+    p.add_argument('--steps', type=int, default=10)
+    p.add_argument('--warmup', type=int, default=3)
+    p.add_argument('--impl', default='ours', choices=('ours', 'reference'))
+    p.add_argument('--lattice', type=int, default=64)
+    p.add_argument('--dt', type=float, default=1e-3)
+    p.add_argument('--tolerance', type=float, default=1e-6)
+    p.add_argument('--seed', type=int, default=0)
+    p.add_argument('--no-cpu-baseline', action='store_true')
+    return p.parse_args()
+
+
+def foam_and_load(m, seed):
+    import dpf_gb300
+    foam = dpf_gb300.jittered_lattice_foam(m, seed=seed)
+    return foam, dpf_gb300.gravity_load(foam)
+
+
+def corner_subfoam(foam, load):
+    """Sites with all unit coordinates < 1/2 (one eighth of the foam, same spacing)."""
+    keep = np.all(foam['unit'] < .5, axis=1)
+    index = -np.ones(len(keep), dtype=np.int64)
+    index[keep] = np.arange(keep.sum())
+    pairs = foam['pairs']
+    both = keep[pairs[:, 0]] & keep[pairs[:, 1]]
+    sub = dict(points=foam['points'][keep], radii=foam['radii'][keep], pairs=index[pairs[both]],
+               areas=foam['areas'][both], masses=foam['masses'][keep], fixed=foam['fixed'][keep],
+               young=foam['young'], shear=foam['shear'])
+    return sub, load[keep]
+
+
+def oracle_rate(foam, load, dt, tol, steps, warmup, budget_s):
+    """Solves/s of the NumPy reference restatement on the one-eighth corner sub-foam,
+    scaled to the full foam by bond count."""
+    from oracle import dem
+    sub, sload = corner_subfoam(foam, load)
+    s = dem.NewtonBonds(sub['points'], sub['radii'], sub['pairs'], sub['areas'], sub['masses'], sub['fixed'],
+                        young=sub['young'], shear=sub['shear'])
+    for _ in range(warmup):
+        s.step(dt, sload, tolerance=tol)
+    t0 = time.perf_counter()
+    done = 0
+    while done < steps:
+        s.step(dt, sload, tolerance=tol)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    elapsed = time.perf_counter() - t0
+    scale = len(sub['pairs'])/len(foam['pairs'])
+    sample = (f'{done} Newton step(s) of the NumPy float64 restatement of NewtonBonds.step on the one-eighth '
+              f'corner sub-foam ({len(sub["points"])} sites, {len(sub["pairs"])} bonds, same spacing), '
+              f'{elapsed:.1f} s, solves/s scaled by the bond-count ratio {scale:.4f}')
+    return done/elapsed*scale, sample
+
+
+class ClockSampler:
+    def __init__(self, index):
+        self.index = index
+        self.file = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', f'--id={self.index}', f'--query-gpu={SMI_FIELDS}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(',')]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return dict(sm_mhz=None, sm_max_mhz=None, reasons=['unsampled'], samples=0)
+        sm = [float(r[0]) for r in rows if r[0].replace('.', '').isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        names = ('hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap')
+        reasons = sorted({n for r in rows for n, v in zip(names, r[4:8]) if v.lower() == 'active'})
+        return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
+                    reasons=reasons, samples=len(rows))
+
+
+def run_reference(args):
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    foam, load = foam_and_load(args.lattice, args.seed)
+    rate, sample = oracle_rate(foam, load, args.dt, args.tolerance, max(1, args.steps), min(args.warmup, 1),
+                               budget_s=150.)
+    line = dict(impl='reference', metric=METRIC, value=rate, unit=UNIT, n_gpus=args.gpus, steps=args.steps,
+                warmup=args.warmup, ms_per_step=1e3/rate if rate else None, higher_is_better=True,
+                scaling='weak', vs_baseline=None, dtype='f64', data='synthetic',
+                config=dict(workload=f'{args.lattice}^3 jittered-lattice foam, gravity, bottom fixed, '
+                                     f'dt={args.dt}, NewtonBonds.step tol={args.tolerance}', lattice=args.lattice,
+                            sites=len(foam['points']), bonds=len(foam['pairs'])),
+                cpu_baseline=dict(value=rate, unit=UNIT, cores=1, kind='port', sample=sample),
+                e2e=dict(value=rate, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import dpf_gb300
+    from dpf_gb300 import _lib
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    device = torch.device('cuda', local)
+    if world > 1:
+        dist.init_process_group('nccl', device_id=device)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    foam, load = foam_and_load(args.lattice, args.seed + rank)
+    s = dpf_gb300.NewtonBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
+                              foam['fixed'], young=foam['young'], shear=foam['shear'], device=device)
+    ext = s.tensor(load)
+    n_sites, n_bonds = s.n_sites, s.n_bonds
+    for _ in range(args.warmup):
+        s.step(args.dt, ext, tolerance=args.tolerance)
+    torch.cuda.synchronize()
+
+    # device-resident throughput, with launch timing of the hot kernels
+    s.profile = {}
+    infos = []
+    launches0 = _lib.LAUNCHES['count']
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        barrier()
+        torch.cuda.synchronize()
+        start.record()
+        for _ in range(args.steps):
+            infos.append(s.step(args.dt, ext, tolerance=args.tolerance)[1])
+        end.record()
+        torch.cuda.synchronize()
+        barrier()
+    launches = _lib.LAUNCHES['count'] - launches0
+    ms = start.elapsed_time(end)
+    profile, s.profile = s.profile, None
+    clock = clocks.summary()
+
+    # end to end through the public API: pinned host load in, positions out, every step
+    host_load = torch.from_numpy(load).pin_memory()
+    host_x = torch.empty((n_sites, 3), dtype=torch.float64).pin_memory()
+    dev_load = torch.empty_like(ext)
+    barrier()
+    torch.cuda.synchronize()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record()
+    for _ in range(args.steps):
+        dev_load.copy_(host_load, non_blocking=True)
+        s.step(args.dt, dev_load, tolerance=args.tolerance)
+        host_x.copy_(s.x, non_blocking=True)
+    e_end.record()
+    torch.cuda.synchronize()
+    barrier()
+    e_ms = e_start.elapsed_time(e_end)
+
+    times = torch.tensor([ms, e_ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    ms, e_ms = times.tolist()
+
+    # roofline of the dominant launch
+    kernels = {}
+    for key, pairs in profile.items():
+        durations = [a.elapsed_time(b) for a, b in pairs]
+        kernels[key] = dict(launches=len(durations), total_ms=sum(durations),
+                            mean_ms=sum(durations)/len(durations))
+    cg = sum(i['cg_iterations'] for i in infos)
+    # Algorithmic bytes (float64): JVP 160 B/bond + 192 B/site; one PCG iteration's
+    # K d sweep 120 B/bond + 112 B/site plus its 6x6 block and vector traffic
+    # (P 288 + 6 vectors x 48 = 576 B/site).
+    bytes_jvp = 160*n_bonds + 192*n_sites
+    bytes_cg_iter = 120*n_bonds + (112 + 576)*n_sites
+    alg = dict(jvp=bytes_jvp, pcg=bytes_cg_iter*cg/max(1, kernels.get('pcg', {}).get('launches', 1)),
+               residual=bytes_jvp)
+    dominant = max(kernels, key=lambda k: kernels[k]['total_ms']) if kernels else None
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    peak = float(peaks.get('hbm_gbs', 6800.))
+    roof = None
+    if dominant:
+        achieved = alg[dominant]/(kernels[dominant]['mean_ms']*1e-3)/1e9
+        roof = dict(bound='hbm', kernel=dominant, achieved=achieved, peak=peak, unit='GB/s', frac=achieved/peak,
+                    traffic=None, peak_source='measured' if peaks else 'fallback',
+                    launches=kernels[dominant]['launches'], mean_ms=kernels[dominant]['mean_ms'])
+
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline and world == 1:
+        rate, sample = oracle_rate(foam, load, args.dt, args.tolerance, steps=1, warmup=0, budget_s=30.)
+        cpu = dict(value=rate, unit=UNIT, cores=1, kind='port', sample=sample)
+    value = world*args.steps/(ms*1e-3)
+    e2e = world*args.steps/(e_ms*1e-3)
+    mean = lambda k: sum(i[k] for i in infos)/len(infos)
+    line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
+                ms_per_step=ms/args.steps, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
+                data='synthetic (seeded jittered-lattice foam; no dataset)',
+                config=dict(workload=f'{args.lattice}^3 jittered-lattice foam, gravity, bottom fixed, dt={args.dt}, '
+                                     f'NewtonBonds.step tol={args.tolerance}, fgmres+elastic PCG, float64',
+                            lattice=args.lattice, sites=n_sites, bonds=n_bonds, parallelism=f'replicas{world}',
+                            l2='working set > L2 (no flush)',
+                            newton_per_solve=mean('nonlinear_iterations'),
+                            krylov_per_solve=mean('krylov_iterations'), cg_per_solve=mean('cg_iterations')),
+                e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
+                         d2h_bytes_per_step=int(n_sites*3*8)),
+                gpu_launches=launches, kernels=kernels, roofline=roof, cpu_baseline=cpu,
+                clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -72,6 +72,16 @@ SIGNATURES = {
 }
 
 
+# Kernels each entry point launches (the launch counter's unit).
+KERNELS = {
+    'dpf_stiffness_apply': 2, 'dpf_diagonal_blocks': 1, 'dpf_prepare_scaling': 1, 'dpf_trial': 2,
+    'dpf_residual': 2, 'dpf_scale_residual': 1, 'dpf_jacobian_vector': 2, 'dpf_elastic_precondition': 1,
+    'dpf_loads': 2, 'dpf_accept_step': 1, 'dpf_energy': 1, 'dpf_arnoldi_cgs2': 4, 'dpf_combine_rows': 1,
+    'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
+}
+LAUNCHES = {'count': 0}
+
+
 class LibraryError(RuntimeError):
     pass
 
@@ -98,6 +108,12 @@ def load():
 
 
 def check(code, name):
-    """Raise for argument/launch errors returned by an entry point."""
+    """Raise for argument/launch errors returned by an entry point; count its kernels."""
     if code:
         raise LibraryError(f'{name} failed with status {code:#x}')
+    LAUNCHES['count'] += KERNELS.get(name, 0)
+
+
+def call(name, *args):
+    """Call an entry point of the loaded library and check its status."""
+    check(getattr(load(), name)(*args), name)

@@ -467,6 +467,18 @@ class NewtonBonds(FiniteBonds):
         self._krylov = None
         self.block = None
         self.units = None
+        # Optional {name: [(start_event, end_event), ...]} timing of the hot launches.
+        self.profile = None
+
+    def _timed(self, key, fn):
+        if self.profile is None:
+            return fn()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        out = fn()
+        end.record()
+        self.profile.setdefault(key, []).append((start, end))
+        return out
 
     # inner_iterations accumulates on the device; reading it synchronises.
     @property
@@ -508,10 +520,10 @@ class NewtonBonds(FiniteBonds):
 
     def _jvp(self, y, direction, dt, units=None, preconditioner=None):
         out = torch.empty_like(direction)
-        self._call('dpf_jacobian_vector', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+        self._timed('jvp', lambda: self._call('dpf_jacobian_vector', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                    ctypes.byref(self._history_struct()), y.data_ptr(), direction.data_ptr(), self.mass.data_ptr(),
                    self.fixed.data_ptr(), float(dt), _addr(units), _addr(preconditioner), out.data_ptr(),
-                   self._wrench.data_ptr(), self._stream())
+                   self._wrench.data_ptr(), self._stream()))
         return out
 
     @torch.no_grad()
@@ -558,12 +570,12 @@ class NewtonBonds(FiniteBonds):
             self._pcg_workspace = torch.empty(self._lib.dpf_elastic_workspace_doubles(self.n_sites), dtype=F64,
                                               device=self.device)
         out = torch.empty_like(vector)
-        self._call('dpf_elastic_precondition', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+        self._timed('pcg', lambda: self._call('dpf_elastic_precondition', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                    ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(),
                    self.block.data_ptr(), self.preconditioner.data_ptr(), self.units.data_ptr(), vector.data_ptr(),
                    float(dt), float(tolerance), int(max_iterations), out.data_ptr(), self._inner.data_ptr(),
                    self._wrench.data_ptr(), self._pcg_workspace.data_ptr(), self._barrier.data_ptr(),
-                   self._status.data_ptr(), self._stream())
+                   self._status.data_ptr(), self._stream()))
         return out
 
     def _elastic_precondition_generic(self, vector, dt, tolerance, max_iterations):
@@ -592,13 +604,13 @@ class NewtonBonds(FiniteBonds):
         r = torch.empty_like(y)
         self._status.zero_()
         use_p = tangent_out is None
-        self._call('dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+        self._timed('residual', lambda: self._call('dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                    ctypes.byref(self._history_struct()), y.data_ptr(), self._v.data_ptr(), external.data_ptr(),
                    self.mass.data_ptr(), self.fixed.data_ptr(), float(dt),
                    ctypes.byref(self._trial_struct(tangent_out, end=False)) if tangent_out else None,
                    self.preconditioner.data_ptr() if use_p else None, self.units.data_ptr() if use_p else None,
                    r.data_ptr(), _addr(scaled) if use_p else None, self._scalars.data_ptr() if use_p else None,
-                   self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream())
+                   self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream()))
         return r
 
     @torch.no_grad()
