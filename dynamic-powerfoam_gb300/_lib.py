@@ -18,6 +18,7 @@ DPF_ERR_NOT_CONVERGED = 16
 DPF_ERR_BARRIER_TIMEOUT = 32
 DPF_ERR_ARGUMENT = 1 << 16
 DPF_ERR_CUDA = 1 << 17
+DPF_ERR_TOO_LARGE = 1 << 18
 
 c_double_p = ctypes.c_void_p
 i64, i32, f64, vp = ctypes.c_int64, ctypes.c_int, ctypes.c_double, ctypes.c_void_p
@@ -69,6 +70,8 @@ SIGNATURES = {
     'dpf_axpby': (i32, [i64, f64, vp, f64, vp, vp, vp]),
     'dpf_rhs_scale': (i32, [i64, vp, vp, vp, vp, vp, f64, vp, vp, vp]),
     'dpf_masked_scale': (i32, [i64, vp, vp, vp, vp, vp]),
+    'dpf_stiffness_apply_static': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp]),
+    'dpf_static_max_bonds': (i64, []),
 }
 
 
@@ -78,6 +81,7 @@ KERNELS = {
     'dpf_residual': 2, 'dpf_scale_residual': 1, 'dpf_jacobian_vector': 2, 'dpf_elastic_precondition': 1,
     'dpf_loads': 2, 'dpf_accept_step': 1, 'dpf_energy': 1, 'dpf_arnoldi_cgs2': 4, 'dpf_combine_rows': 1,
     'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
+    'dpf_stiffness_apply_static': 2,
 }
 LAUNCHES = {'count': 0}
 

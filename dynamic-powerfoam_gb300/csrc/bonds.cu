@@ -5,6 +5,8 @@
 // doubles [F, T_i, T_j] (endpoint i receives (F, T_i), endpoint j (-F, T_j));
 // a site pass walks the site's incidence list in the reference's index_add_
 // order and sums them.  Results are deterministic run to run.
+#include <mutex>
+
 #include "common.cuh"
 
 namespace dpf {
@@ -743,6 +745,63 @@ int dpf_loads(const dpf_graph *g, const dpf_history *h, double *out, double *wre
     if (g->n_bonds)
         loads_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(g->n_bonds, g->edges, *h, wrench,
                                                                             nullptr);
+    site_gather<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, g->inc_ptr, g->inc_bond,
+                                                                        wrench, out);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// K q without any allocation by anyone: the bond-wrench scratch lives in a
+// file-scope device array instead of a caller buffer.  For callers that
+// cannot call cudaMalloc (see dpf_stiffness_apply_static in dpf_gb300.h).
+
+namespace {
+
+__device__ __align__(256) double g_static_wrench[9 * DPF_STATIC_MAX_BONDS];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+double *g_static_wrench_ptr[kMaxDevices] = {};
+
+// Device address of g_static_wrench on the current device.  The host-side
+// name is only a stand-in for the device symbol, so it is resolved once per
+// device with cudaGetSymbolAddress while that device is current.
+int static_wrench(double **out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return DPF_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_wrench_ptr[dev]) {
+        void *ptr = nullptr;
+        if (cudaGetSymbolAddress(&ptr, g_static_wrench) != cudaSuccess || !ptr) return DPF_ERR_CUDA;
+        g_static_wrench_ptr[dev] = static_cast<double *>(ptr);
+    }
+    *out = g_static_wrench_ptr[dev];
+    return DPF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t dpf_static_max_bonds(void) { return DPF_STATIC_MAX_BONDS; }
+
+int dpf_stiffness_apply_static(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t, const double *q,
+                               double *out, void *stream) {
+    if (!graph_ok(g) || !k || !t || !q || !out) return DPF_ERR_ARGUMENT;
+    if (g->n_bonds > DPF_STATIC_MAX_BONDS) return DPF_ERR_TOO_LARGE;
+    double *wrench = nullptr;
+    const int rc = static_wrench(&wrench);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    // Every bond slot read by site_gather is written by stiffness_bonds first
+    // in the same call, so the array needs no clearing between calls.
+    if (g->n_bonds) {
+        StiffnessBondArgs a{g->n_bonds, g->edges, *k, *t, q, wrench};
+        stiffness_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
     site_gather<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, g->inc_ptr, g->inc_bond,
                                                                         wrench, out);
     DPF_CHECK_LAUNCH();

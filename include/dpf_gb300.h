@@ -44,8 +44,12 @@ enum dpf_status {
     DPF_ERR_NOT_CONVERGED = 16,  /* bounded iteration limit reached            */
     DPF_ERR_BARRIER_TIMEOUT = 32,/* a grid barrier gave up after its time limit */
     DPF_ERR_ARGUMENT = 1 << 16,  /* invalid argument (host check)              */
-    DPF_ERR_CUDA = 1 << 17       /* CUDA launch/runtime error                  */
+    DPF_ERR_CUDA = 1 << 17,      /* CUDA launch/runtime error                  */
+    DPF_ERR_TOO_LARGE = 1 << 18  /* problem exceeds a fixed static capacity    */
 };
+
+/* Bond capacity of the static scratch of dpf_stiffness_apply_static. */
+#define DPF_STATIC_MAX_BONDS 65536
 
 /* Bond graph: reference edges plus the incidence CSR described above. */
 typedef struct dpf_graph {
@@ -97,6 +101,29 @@ int64_t dpf_wrench_scratch_doubles(int64_t n_bonds);
  * wrench: scratch of dpf_wrench_scratch_doubles(M) doubles. */
 int dpf_stiffness_apply(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
                         const double *q, double *out, double *wrench, void *stream);
+
+/* K q like dpf_stiffness_apply, but nobody allocates scratch: no counterpart
+ * in the reference.  It exists for callers that cannot call cudaMalloc, such
+ * as a host application that gives this library only its inputs and outputs
+ * from a device-memory pool it manages itself under a fixed budget, where an
+ * extra allocation could fail, or a cudaFree could stall the whole device, in
+ * the middle of the host's own work.
+ * The bond-wrench scratch is a file-scope device array of
+ * 9 * DPF_STATIC_MAX_BONDS doubles (4.5 MiB) that every GPU which loads the
+ * library holds until the process exits.  Graphs with more than
+ * DPF_STATIC_MAX_BONDS bonds are rejected with DPF_ERR_TOO_LARGE before any
+ * launch.  The first call on a device looks up the array's device address for
+ * that device (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls on a device share the one array: calls whose work
+ * overlaps on the GPU (concurrent streams, several host threads) race on it,
+ * so serialise them.  The array keeps the last call's contents; every value a
+ * call reads from it is written earlier in the same call, so nothing needs
+ * clearing.  The function allocates nothing and frees nothing. */
+int dpf_stiffness_apply_static(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
+                               const double *q, double *out, void *stream);
+
+/* DPF_STATIC_MAX_BONDS, for callers binding the library without the header. */
+int64_t dpf_static_max_bonds(void);
 
 /* Per-site 6x6 diagonal blocks of K (N, 6, 6).
  * Replaces LinearBondsGPU._diagonal_blocks (experiments/bonded_dem_linear_gpu.py:54-72)
