@@ -6,7 +6,7 @@ Import as ``dpf_gb300``.  The solver classes need ``libdpf_gb300.so``
 CPU fallback.
 """
 from .foam import jittered_lattice_foam, gravity_load, regular_edges, morton_order
-from .newton import (LinearBonds, FiniteBonds, NewtonBonds, FastNewtonBonds, AdaptiveIntervals,
+from .newton import (LinearBonds, FiniteBonds, NewtonBonds, FastNewtonBonds, MixedNewtonBonds, AdaptiveIntervals,
                      SubdivideError, fgmres, incidence, guard_error)
 
 # Reference class names (experiments/bonded_dem_linear_gpu.py, bonded_dem_finite_gpu.py).
@@ -14,5 +14,5 @@ LinearBondsGPU = LinearBonds
 FiniteBondsGPU = FiniteBonds
 
 __all__ = ['jittered_lattice_foam', 'gravity_load', 'regular_edges', 'morton_order', 'LinearBonds',
-           'FiniteBonds', 'NewtonBonds', 'FastNewtonBonds', 'LinearBondsGPU', 'FiniteBondsGPU',
+           'FiniteBonds', 'NewtonBonds', 'FastNewtonBonds', 'MixedNewtonBonds', 'LinearBondsGPU', 'FiniteBondsGPU',
            'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error']

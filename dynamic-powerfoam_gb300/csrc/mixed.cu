@@ -1,0 +1,990 @@
+// Mixed-precision Newton path: float32 bond sweeps, float64 reductions and a
+// float64-accurate residual.
+//
+// Per time step, one float64 pass (mixed_setup) builds the float32 bond
+// records and the float64 constant part of the residual,
+//     r0 = -dt M v - dt^2/2 (loads(x) + external),
+// so that for any increment y
+//     r(y) = r0 + M y - dt^2/2 sum_bonds [f_mid(y) - f_mid(0)],
+// where the bond increments are evaluated in float32 from small quantities
+// only (normal change, transport increments, lever changes; see mixed.cuh)
+// and summed per site in float64.  The JVP is the forward-mode derivative of
+// the same float32 increment.  Site sums walk the incidence CSR (no atomics).
+#include "mixed.cuh"
+
+namespace dpf {
+namespace mp {
+
+constexpr int kMaxReduceBlocks = 1024;
+constexpr int64_t kPartialsOffset = 8;
+constexpr int kMaxPcgBlocks = 4096;
+
+inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
+inline int reduce_grid(int64_t n) {
+    int g = blocks_for(n, kThreads);
+    return g > kMaxReduceBlocks ? kMaxReduceBlocks : (g < 1 ? 1 : g);
+}
+
+__device__ __forceinline__ unsigned *counter_slot(double *partials, int slot) {
+    return reinterpret_cast<unsigned *>(partials) + slot;
+}
+
+// Bond data block: records (7 float4 per bond) then the float32 tangent used
+// by K q and the blocks (4 float4 per bond: (n, kn), (ri, ks), (rj, kb), (kt, i, j, 0)).
+struct BondData {
+    Records rec;
+    float4 *t0, *t1, *t2, *t3;
+};
+
+inline BondData split_bond_data(float *base, int64_t m) {
+    float4 *p = reinterpret_cast<float4 *>(base);
+    BondData d;
+    d.rec = {p, p + m, p + 2 * m, p + 3 * m, p + 4 * m, p + 5 * m, p + 6 * m};
+    d.t0 = p + 7 * m;
+    d.t1 = p + 8 * m;
+    d.t2 = p + 9 * m;
+    d.t3 = p + 10 * m;
+    return d;
+}
+
+__device__ __forceinline__ V3<float> f3(const double *p) {
+    return {(float)p[0], (float)p[1], (float)p[2]};
+}
+__device__ __forceinline__ float3 tof3(d3 a) { return make_float3((float)a.x, (float)a.y, (float)a.z); }
+
+__device__ __forceinline__ void store9(float *w, int64_t b, V3<float> f, V3<float> ti, V3<float> tj) {
+    float *p = w + 9 * b;
+    p[0] = f.x; p[1] = f.y; p[2] = f.z;
+    p[3] = ti.x; p[4] = ti.y; p[5] = ti.z;
+    p[6] = tj.x; p[7] = tj.y; p[8] = tj.z;
+}
+
+// Site sum of a float32 bond wrench in float64.
+__device__ __forceinline__ void gather9(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                        const float *__restrict__ w, int64_t s, double acc[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = 0.0;
+    const int e1 = ptr[s + 1];
+    for (int e = ptr[s]; e < e1; ++e) {
+        const int v = inc[e];
+        if (v >= 0) {
+            const float *p = w + 9 * (int64_t)v;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] += (double)p[c];
+        } else {
+            const float *p = w + 9 * (int64_t)(~v);
+            acc[0] -= (double)p[0];
+            acc[1] -= (double)p[1];
+            acc[2] -= (double)p[2];
+            acc[3] += (double)p[6];
+            acc[4] += (double)p[7];
+            acc[5] += (double)p[8];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-step setup (float64): records, loads(x) wrench.
+
+struct SetupArgs {
+    int64_t m;
+    const int64_t *edges;
+    dpf_stiffness k;
+    dpf_history h;
+    BondData out;
+    double *wrench;
+    int *status;
+};
+
+__global__ void __launch_bounds__(kThreads) setup_bonds(SetupArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    int64_t i, j;
+    edge(a.edges, b, i, j);
+    const d3 xi = ld3(a.h.x, i), xj = ld3(a.h.x, j);
+    const d3 dx = xj - xi;
+    const double L0 = norm(dx);
+    if (L0 <= 1e-12) atomicOr(a.status, DPF_ERR_COINCIDENT);
+    const d3 nx = dx / L0;
+    const d3 n0 = ld3(a.h.normal, b);
+    const double rh = 0.5 * (a.h.radii[i] - a.h.radii[j]);
+    const d3 off = ld3(a.h.offset, b), fs = ld3(a.h.fs, b), mb = ld3(a.h.mb, b);
+    const double fn = a.h.fn[b], mt = a.h.mt[b];
+    const d3 c = 0.5 * (xi + xj) + rh * nx + off;
+    const d3 ri = c - xi, rj = c - xj;
+    const d3 f = fn * nx + fs;
+    const d3 couple = mt * nx + mb;
+    // loads(x) exactly as dpf_loads (experiments/bonded_dem_finite_gpu.py:82-85)
+    double *w = a.wrench + 9 * b;
+    st3(w, f);
+    st3(w + 3, cross(ri, f) + couple);
+    st3(w + 6, -cross(rj, f) - couple);
+    const float kn = (float)a.k.kn[b], ks = (float)a.k.ks[b], kb = (float)a.k.kb[b], kt = (float)a.k.kt[b];
+    const float3 n0f = tof3(n0), dn0 = tof3(nx - n0), rif = tof3(ri);
+    a.out.rec.r0[b] = make_float4(n0f.x, n0f.y, n0f.z, (float)L0);
+    a.out.rec.r1[b] = make_float4(dn0.x, dn0.y, dn0.z, (float)rh);
+    a.out.rec.r2[b] = make_float4(rif.x, rif.y, rif.z, (float)fn);
+    a.out.rec.r3[b] = make_float4((float)fs.x, (float)fs.y, (float)fs.z, (float)mt);
+    a.out.rec.r4[b] = make_float4((float)mb.x, (float)mb.y, (float)mb.z, kn);
+    a.out.rec.r5[b] = make_float4((float)off.x, (float)off.y, (float)off.z, ks);
+    a.out.rec.r6[b] = make_float4(kb, kt, __int_as_float((int)i), __int_as_float((int)j));
+    a.out.t3[b] = make_float4(kt, __int_as_float((int)i), __int_as_float((int)j), 0.0f);
+}
+
+// r0 = -dt M v - dt^2/2 (L + ext); norms [|dt M v + dt^2/2 ext|, |L on free sites|].
+struct SetupSiteArgs {
+    int64_t n;
+    const int32_t *ptr, *inc;
+    const double *wrench, *mass, *v, *external;
+    const uint8_t *fixed;
+    double dt, half_dt2;
+    double *r0, *loads, *scales, *partials;
+};
+
+__global__ void __launch_bounds__(kThreads) setup_sites(SetupSiteArgs a) {
+    double a2 = 0.0, l2 = 0.0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n; s += (int64_t)gridDim.x * blockDim.x) {
+        double acc[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] = 0.0;
+        const int e1 = a.ptr[s + 1];
+        for (int e = a.ptr[s]; e < e1; ++e) {
+            const int v = a.inc[e];
+            if (v >= 0) {
+                const double *p = a.wrench + 9 * (int64_t)v;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[c] += p[c];
+            } else {
+                const double *p = a.wrench + 9 * (int64_t)(~v);
+                acc[0] -= p[0];
+                acc[1] -= p[1];
+                acc[2] -= p[2];
+                acc[3] += p[6];
+                acc[4] += p[7];
+                acc[5] += p[8];
+            }
+        }
+        const bool fx = a.fixed[s] != 0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const int64_t e = 6 * s + c;
+            const double mv = a.dt * a.mass[e] * a.v[e];
+            const double rhs = mv + a.half_dt2 * a.external[e];
+            a2 += rhs * rhs;
+            if (!fx) l2 += acc[c] * acc[c];
+            a.r0[e] = -mv - a.half_dt2 * (acc[c] + a.external[e]);
+            if (a.loads) a.loads[e] = acc[c];
+        }
+    }
+    a2 = block_sum(a2);
+    l2 = block_sum(l2);
+    double *part = a.partials + kPartialsOffset;
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = a2;
+        part[2 * blockIdx.x + 1] = l2;
+    }
+    if (last_block(counter_slot(a.partials, 5))) {
+        const double sa = block_sum_array(part, gridDim.x, 2);
+        const double sl = block_sum_array(part + 1, gridDim.x, 2);
+        if (threadIdx.x == 0) {
+            a.scales[0] = sqrt(sa);
+            a.scales[1] = sqrt(sl);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Residual increment (float32 bonds) and the float64 residual (sites).
+
+struct ResidualBondArgs {
+    int64_t m;
+    BondData bd;
+    const double *y;
+    int want_tangent;
+    float *wrench;
+    int *status;
+};
+
+__device__ __forceinline__ void load_y(const double *y, int s, V3<float> &u, V3<float> &w) {
+    const double *p = y + 6 * (int64_t)s;
+    u = f3(p);
+    w = f3(p + 3);
+}
+
+__global__ void __launch_bounds__(kThreads) residual_bonds(ResidualBondArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    const Bond B = load_bond(a.bd.rec, b);
+    V3<float> ui, wi, uj, wj;
+    load_y(a.y, B.i, ui, wi);
+    load_y(a.y, B.j, uj, wj);
+    const BondIncrement<float> o = bond_increment<float>(B, ui, wi, uj, wj);
+    store9(a.wrench, b, o.dF, o.dTi, o.dTj);
+    int flags = 0;
+    if (!(o.length > 1e-12f)) flags |= DPF_ERR_COINCIDENT;
+    if (o.turn2 > kTurn2) flags |= DPF_ERR_NORMAL_TURN;
+    // end-of-step guards: end length and the mid -> end normal turn
+    const V3<float> nx = lift3<float>(B.n0) + lift3<float>(B.dn0);
+    float le;
+    const V3<float> dnx_e = normal_change(B.L0, nx, uj - ui, le);
+    const V3<float> turn = dnx_e - o.dn_x;
+    if (!(le > 1e-12f)) flags |= DPF_ERR_COINCIDENT;
+    if (dot(turn, turn) > kTurn2) flags |= DPF_ERR_NORMAL_TURN;
+    if (flags) atomicOr(a.status, flags);
+    if (a.want_tangent) {
+        a.bd.t0[b] = make_float4(o.n.x, o.n.y, o.n.z, B.kn);
+        a.bd.t1[b] = make_float4(o.ri.x, o.ri.y, o.ri.z, B.ks);
+        a.bd.t2[b] = make_float4(o.rj.x, o.rj.y, o.rj.z, B.kb);
+    }
+}
+
+struct ResidualSiteArgs {
+    int64_t n;
+    const int32_t *ptr, *inc;
+    const float *wrench;
+    const double *y, *mass, *r0;
+    const uint8_t *fixed;
+    double half_dt2;
+    const float *P;
+    const double *units;
+    double *residual, *scaled, *norms, *partials;
+    int *status;
+};
+
+__device__ __forceinline__ void matvec6f(const float *P, const double x[6], double y[6]) {
+    float xf[6];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) xf[c] = (float)x[c];
+#pragma unroll
+    for (int row = 0; row < 6; ++row) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v = fmaf(P[6 * row + c], xf[c], v);
+        y[row] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
+    double sum_r = 0.0, max_s = 0.0, sum_s = 0.0;
+    int flags = 0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n; s += (int64_t)gridDim.x * blockDim.x) {
+        double acc[6], r[6];
+        gather9(a.ptr, a.inc, a.wrench, s, acc);
+        const double *ys = a.y + 6 * s;
+        if (norm(ld3(ys + 3)) > 0.25) flags |= DPF_ERR_ROTATION;
+        const bool fx = a.fixed[s] != 0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double val = a.r0[6 * s + c] + a.mass[6 * s + c] * ys[c] - a.half_dt2 * acc[c];
+            r[c] = fx ? ys[c] : val;
+            a.residual[6 * s + c] = r[c];
+            sum_r += r[c] * r[c];
+        }
+        if (a.P) {
+            // scale in float64 from the float32 block inverse: P r / units
+            const float *P = a.P + 36 * s;
+#pragma unroll
+            for (int row = 0; row < 6; ++row) {
+                double v = 0.0;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) v += (double)P[6 * row + c] * r[c];
+                v = v / a.units[6 * s + row];
+                if (a.scaled) a.scaled[6 * s + row] = v;
+                max_s = fmax(max_s, fabs(v));
+                sum_s += v * v;
+            }
+        }
+    }
+    if (flags) atomicOr(a.status, flags);
+    if (!a.norms) return;
+    sum_r = block_sum(sum_r);
+    max_s = block_max(max_s);
+    sum_s = block_sum(sum_s);
+    double *part = a.partials + kPartialsOffset;
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = sum_r;
+        part[3 * blockIdx.x + 1] = max_s;
+        part[3 * blockIdx.x + 2] = sum_s;
+    }
+    if (last_block(counter_slot(a.partials, 6))) {
+        const double r2 = block_sum_array(part, gridDim.x, 3);
+        const double mx = block_max_array(part + 1, gridDim.x, 3);
+        const double s2 = block_sum_array(part + 2, gridDim.x, 3);
+        if (threadIdx.x == 0) {
+            a.norms[0] = sqrt(r2);
+            a.norms[1] = mx;
+            a.norms[2] = sqrt(s2);
+            if (!isfinite(r2) || !isfinite(s2)) atomicOr(a.status, DPF_ERR_NONFINITE);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const float *P, const double *units,
+                                                            const double *r, double *scaled, double *norms,
+                                                            double *partials) {
+    double sum_r = 0.0, max_s = 0.0, sum_s = 0.0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        double rr[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            rr[c] = r[6 * s + c];
+            sum_r += rr[c] * rr[c];
+        }
+        const float *Ps = P + 36 * s;
+#pragma unroll
+        for (int row = 0; row < 6; ++row) {
+            double v = 0.0;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) v += (double)Ps[6 * row + c] * rr[c];
+            v = v / units[6 * s + row];
+            if (scaled) scaled[6 * s + row] = v;
+            max_s = fmax(max_s, fabs(v));
+            sum_s += v * v;
+        }
+    }
+    if (!norms) return;
+    sum_r = block_sum(sum_r);
+    max_s = block_max(max_s);
+    sum_s = block_sum(sum_s);
+    double *part = partials + kPartialsOffset;
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = sum_r;
+        part[3 * blockIdx.x + 1] = max_s;
+        part[3 * blockIdx.x + 2] = sum_s;
+    }
+    if (last_block(counter_slot(partials, 7))) {
+        const double r2 = block_sum_array(part, gridDim.x, 3);
+        const double mx = block_max_array(part + 1, gridDim.x, 3);
+        const double s2 = block_sum_array(part + 2, gridDim.x, 3);
+        if (threadIdx.x == 0) {
+            norms[0] = sqrt(r2);
+            norms[1] = mx;
+            norms[2] = sqrt(s2);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// JVP: forward-mode derivative of the float32 increment.
+
+struct JvpArgs {
+    int64_t m;
+    BondData bd;
+    const double *y, *direction, *units;
+    float *wrench;
+};
+
+__device__ __forceinline__ V3<Dual> dual3(V3<float> v, V3<float> d) {
+    return {{v.x, d.x}, {v.y, d.y}, {v.z, d.z}};
+}
+
+__device__ __forceinline__ void load_dir(const double *d, const double *units, int s, V3<float> &u, V3<float> &w) {
+    const double *p = d + 6 * (int64_t)s;
+    if (units) {
+        const double *q = units + 6 * (int64_t)s;
+        u = {(float)(p[0] * q[0]), (float)(p[1] * q[1]), (float)(p[2] * q[2])};
+        w = {(float)(p[3] * q[3]), (float)(p[4] * q[4]), (float)(p[5] * q[5])};
+    } else {
+        u = f3(p);
+        w = f3(p + 3);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) jvp_bonds_mixed(JvpArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    const Bond B = load_bond(a.bd.rec, b);
+    V3<float> ui, wi, uj, wj, dui, dwi, duj, dwj;
+    load_y(a.y, B.i, ui, wi);
+    load_y(a.y, B.j, uj, wj);
+    load_dir(a.direction, a.units, B.i, dui, dwi);
+    load_dir(a.direction, a.units, B.j, duj, dwj);
+    const BondIncrement<Dual> o =
+        bond_increment<Dual>(B, dual3(ui, dui), dual3(wi, dwi), dual3(uj, duj), dual3(wj, dwj));
+    store9(a.wrench, b, der3(o.dF), der3(o.dTi), der3(o.dTj));
+}
+
+struct JvpSiteArgs {
+    int64_t n;
+    const int32_t *ptr, *inc;
+    const float *wrench;
+    const double *direction, *units, *mass;
+    const float *P;
+    const uint8_t *fixed;
+    double half_dt2;
+    double *out;
+};
+
+__global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    double acc[6], r[6];
+    gather9(a.ptr, a.inc, a.wrench, s, acc);
+    const bool fx = a.fixed[s] != 0;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        double d = a.direction[6 * s + c];
+        if (a.units) d *= a.units[6 * s + c];
+        r[c] = fx ? d : a.mass[6 * s + c] * d - a.half_dt2 * acc[c];
+    }
+    if (a.P) {
+        double o[6];
+        matvec6f(a.P + 36 * s, r, o);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = o[c] / a.units[6 * s + c];
+    } else {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = r[c];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Frozen tangent K q in float32 (experiments/bonded_dem_linear_gpu.py:42-52).
+
+__device__ __forceinline__ void stiffness_bond_f32(const BondData &bd, const float *q, float *wrench, int64_t b) {
+    const float4 a = __ldg(bd.t0 + b), c = __ldg(bd.t1 + b), e = __ldg(bd.t2 + b), g = __ldg(bd.t3 + b);
+    const int i = __float_as_int(g.y), j = __float_as_int(g.z);
+    const V3<float> n = {a.x, a.y, a.z}, ri = {c.x, c.y, c.z}, rj = {e.x, e.y, e.z};
+    const float kn = a.w, ks = c.w, kb = e.w, kt = g.x;
+    const float *qi = q + 6 * (int64_t)i, *qj = q + 6 * (int64_t)j;
+    const V3<float> wi = {qi[3], qi[4], qi[5]}, wj = {qj[3], qj[4], qj[5]};
+    const V3<float> du = V3<float>{qj[0] - qi[0], qj[1] - qi[1], qj[2] - qi[2]} + cross(wj, rj) - cross(wi, ri);
+    const V3<float> dw = wj - wi;
+    const V3<float> f = ks * du + ((kn - ks) * dot(du, n)) * n;
+    const V3<float> m = kb * dw + ((kt - kb) * dot(dw, n)) * n;
+    store9(wrench, b, -f, -cross(ri, f) - m, cross(rj, f) + m);
+}
+
+__global__ void __launch_bounds__(kThreads) stiffness_bonds_f32(int64_t m, BondData bd, const float *q, float *w) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b < m) stiffness_bond_f32(bd, q, w, b);
+}
+
+__global__ void __launch_bounds__(kThreads) to_f32(int64_t n, const double *a, float *out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e < n) out[e] = (float)a[e];
+}
+
+__global__ void __launch_bounds__(kThreads) gather_to_f64(int64_t n, const int32_t *ptr, const int32_t *inc,
+                                                          const float *w, double *out) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    double acc[6];
+    gather9(ptr, inc, w, s, acc);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) out[6 * s + c] = acc[c];
+}
+
+// ---------------------------------------------------------------------------
+// Blocks and their inverse in float32 (experiments/bonded_dem_newton.py:94-102).
+
+__device__ __forceinline__ void add_block_f32(float D[36], V3<float> n, V3<float> r, float kn, float ks, float kb,
+                                              float kt) {
+    const float nv[3] = {n.x, n.y, n.z};
+    float d[9], h[9];
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float nn = nv[p] * nv[q];
+            d[3 * p + q] = (p == q ? ks : 0.0f) + (kn - ks) * nn;
+            h[3 * p + q] = (p == q ? kb : 0.0f) + (kt - kb) * nn;
+        }
+    const float S[9] = {0.0f, -r.z, r.y, r.z, 0.0f, -r.x, -r.y, r.x, 0.0f};
+    float dS[9];
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            dS[3 * p + q] = d[3 * p] * S[q] + d[3 * p + 1] * S[3 + q] + d[3 * p + 2] * S[6 + q];
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            D[6 * p + q] += d[3 * p + q];
+            D[6 * p + 3 + q] -= dS[3 * p + q];
+            D[6 * (3 + q) + p] -= dS[3 * p + q];
+            D[6 * (3 + p) + 3 + q] += S[p] * dS[q] + S[3 + p] * dS[3 + q] + S[6 + p] * dS[6 + q] + h[3 * p + q];
+        }
+}
+
+// In-place inverse of a symmetric positive definite 6x6 after symmetric
+// diagonal scaling (Jacobi), Cholesky based; A is overwritten with A^-1.
+__device__ __forceinline__ void spd_inverse6_f32(float A[36]) {
+    float sc[6];
+#pragma unroll
+    for (int p = 0; p < 6; ++p) sc[p] = rsqrtf(A[7 * p]);
+#pragma unroll
+    for (int p = 0; p < 6; ++p)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) A[6 * p + q] *= sc[p] * sc[q];
+    // Cholesky: lower triangle of A becomes L
+#pragma unroll
+    for (int jj = 0; jj < 6; ++jj) {
+        float s = A[7 * jj];
+#pragma unroll
+        for (int kk = 0; kk < jj; ++kk) s -= A[6 * jj + kk] * A[6 * jj + kk];
+        const float l = sqrtf(s);
+        A[7 * jj] = l;
+        const float inv = 1.0f / l;
+#pragma unroll
+        for (int ii = jj + 1; ii < 6; ++ii) {
+            float v = A[6 * ii + jj];
+#pragma unroll
+            for (int kk = 0; kk < jj; ++kk) v -= A[6 * ii + kk] * A[6 * jj + kk];
+            A[6 * ii + jj] = v * inv;
+        }
+    }
+    // W = L^-1 into the upper triangle (transposed): U[jj][ii] = W[ii][jj]
+    float W[21];
+#pragma unroll
+    for (int ii = 0; ii < 6; ++ii) {
+        const int base = ii * (ii + 1) / 2;
+        W[base + ii] = 1.0f / A[7 * ii];
+#pragma unroll
+        for (int jj = 0; jj < ii; ++jj) {
+            float v = 0.0f;
+#pragma unroll
+            for (int kk = jj; kk < ii; ++kk) v += A[6 * ii + kk] * W[kk * (kk + 1) / 2 + jj];
+            W[base + jj] = -v * W[base + ii];
+        }
+    }
+#pragma unroll
+    for (int ii = 0; ii < 6; ++ii)
+#pragma unroll
+        for (int jj = 0; jj <= ii; ++jj) {
+            float v = 0.0f;
+#pragma unroll
+            for (int kk = ii; kk < 6; ++kk) v += W[kk * (kk + 1) / 2 + ii] * W[kk * (kk + 1) / 2 + jj];
+            v *= sc[ii] * sc[jj];
+            A[6 * ii + jj] = v;
+            A[6 * jj + ii] = v;
+        }
+}
+
+struct ScalingArgs {
+    int64_t n;
+    const int32_t *ptr, *inc;
+    BondData bd;
+    const double *mass, *radii;
+    const uint8_t *fixed;
+    float alpha;
+    float *block, *P;
+    double *units;
+};
+
+__global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= a.n) return;
+    float D[36];
+#pragma unroll
+    for (int c = 0; c < 36; ++c) D[c] = 0.0f;
+    const int e1 = a.ptr[s + 1];
+    for (int e = a.ptr[s]; e < e1; ++e) {
+        const int v = a.inc[e];
+        const int64_t b = v >= 0 ? v : ~v;
+        const float4 t0 = __ldg(a.bd.t0 + b), t1 = __ldg(a.bd.t1 + b), t2 = __ldg(a.bd.t2 + b);
+        const float kt = __ldg(a.bd.t3 + b).x;
+        const V3<float> r = v >= 0 ? V3<float>{t1.x, t1.y, t1.z} : V3<float>{t2.x, t2.y, t2.z};
+        add_block_f32(D, {t0.x, t0.y, t0.z}, r, t0.w, t1.w, t2.w, kt);
+    }
+    const bool fx = a.fixed[s] != 0;
+#pragma unroll
+    for (int p = 0; p < 6; ++p)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float val = (p == q ? (float)a.mass[6 * s + p] : 0.0f) + a.alpha * D[6 * p + q];
+            D[6 * p + q] = fx ? (p == q ? 1.0f : 0.0f) : val;
+        }
+    if (a.block) {
+#pragma unroll
+        for (int c = 0; c < 36; ++c) a.block[36 * s + c] = D[c];
+    }
+    spd_inverse6_f32(D);
+#pragma unroll
+    for (int c = 0; c < 36; ++c) a.P[36 * s + c] = D[c];
+    const double r = fx ? 1.0 : a.radii[s];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) a.units[6 * s + c] = c < 3 ? r : 1.0;
+}
+
+// ---------------------------------------------------------------------------
+// Elastic PCG in float32 with float64 dot products, one cooperative launch
+// (experiments/bonded_dem_newton.py:107-130).
+
+struct PcgArgs {
+    int64_t n, m;
+    const int32_t *ptr, *inc;
+    BondData bd;
+    const double *mass, *units, *vector;
+    const float *block, *P;
+    const uint8_t *fixed;
+    float alpha_op;
+    double tol2;
+    int max_it;
+    double *out;
+    int *iterations;
+    float *wrench, *x, *r, *z, *d, *ad;
+    double *part_a, *part_b;
+    unsigned *barrier;
+    int *status;
+};
+
+__device__ __forceinline__ void mv6(const float *P, const float x[6], float y[6]) {
+#pragma unroll
+    for (int row = 0; row < 6; ++row) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v = fmaf(P[6 * row + c], x[c], v);
+        y[row] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    double p = 0.0;
+    for (int64_t s = tid; s < a.n; s += stride) {
+        float u[6], rr[6], zz[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) u[c] = (float)(a.units[6 * s + c] * a.vector[6 * s + c]);
+        if (a.fixed[s]) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) rr[c] = 0.0f;
+        } else {
+            mv6(a.block + 36 * s, u, rr);
+        }
+        mv6(a.P + 36 * s, rr, zz);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            a.x[6 * s + c] = 0.0f;
+            a.r[6 * s + c] = rr[c];
+            a.d[6 * s + c] = zz[c];
+            p += (double)rr[c] * (double)zz[c];
+        }
+    }
+    p = block_sum(p);
+    if (threadIdx.x == 0) a.part_b[blockIdx.x] = p;
+    if (!grid_barrier(a.barrier, a.status)) return;
+    double rz = block_sum_array(a.part_b, gridDim.x);
+    const double initial = rz;
+    if (initial == 0.0) {
+        for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = 0.0;
+        return;
+    }
+    int it = 0;
+    for (; it < a.max_it; ++it) {
+        for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_f32(a.bd, a.d, a.wrench, b);
+        if (!grid_barrier(a.barrier, a.status)) return;
+        p = 0.0;
+        for (int64_t s = tid; s < a.n; s += stride) {
+            float acc[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
+            const int e1 = a.ptr[s + 1];
+            for (int e = a.ptr[s]; e < e1; ++e) {
+                const int v = a.inc[e];
+                if (v >= 0) {
+                    const float *q = a.wrench + 9 * (int64_t)v;
+#pragma unroll
+                    for (int c = 0; c < 6; ++c) acc[c] += q[c];
+                } else {
+                    const float *q = a.wrench + 9 * (int64_t)(~v);
+                    acc[0] -= q[0];
+                    acc[1] -= q[1];
+                    acc[2] -= q[2];
+                    acc[3] += q[6];
+                    acc[4] += q[7];
+                    acc[5] += q[8];
+                }
+            }
+            const bool fx = a.fixed[s] != 0;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                const float dv = a.d[6 * s + c];
+                const float v = fx ? dv : (float)a.mass[6 * s + c] * dv + a.alpha_op * acc[c];
+                a.ad[6 * s + c] = v;
+                p += (double)dv * (double)v;
+            }
+        }
+        p = block_sum(p);
+        if (threadIdx.x == 0) a.part_a[blockIdx.x] = p;
+        if (!grid_barrier(a.barrier, a.status)) return;
+        const float alpha = (float)(rz / block_sum_array(a.part_a, gridDim.x));
+        p = 0.0;
+        for (int64_t s = tid; s < a.n; s += stride) {
+            float rr[6], zz[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                a.x[6 * s + c] += alpha * a.d[6 * s + c];
+                rr[c] = a.r[6 * s + c] - alpha * a.ad[6 * s + c];
+                a.r[6 * s + c] = rr[c];
+            }
+            mv6(a.P + 36 * s, rr, zz);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                a.z[6 * s + c] = zz[c];
+                p += (double)rr[c] * (double)zz[c];
+            }
+        }
+        p = block_sum(p);
+        if (threadIdx.x == 0) a.part_b[blockIdx.x] = p;
+        if (!grid_barrier(a.barrier, a.status)) return;
+        const double following = block_sum_array(a.part_b, gridDim.x);
+        if (it % 5 == 0 && following <= a.tol2 * initial) break;
+        const float beta = (float)(following / rz);
+        for (int64_t e = tid; e < 6 * a.n; e += stride) a.d[e] = a.z[e] + beta * a.d[e];
+        rz = following;
+        if (!grid_barrier(a.barrier, a.status)) return;
+    }
+    for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = (double)a.x[e] / a.units[e];
+    if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
+}
+
+// ---------------------------------------------------------------------------
+// End state of an accepted increment (experiments/bonded_dem_finite_gpu.py:102-116):
+// float32 increments added to the float64 committed history.
+
+struct CommitArgs {
+    int64_t m;
+    BondData bd;
+    dpf_history h;
+    const double *y;
+    double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
+};
+
+__global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    const Bond B = load_bond(a.bd.rec, b);
+    V3<float> ui, wi, uj, wj;
+    load_y(a.y, B.i, ui, wi);
+    load_y(a.y, B.j, uj, wj);
+    const BondIncrement<float> o = bond_increment<float>(B, ui, wi, uj, wj);
+    a.fn_end[b] = a.h.fn[b] + (double)(B.kn * value(o.dn));
+    a.mt_end[b] = a.h.mt[b] + (double)(B.kt * value(o.tw));
+    // end normal in float64 from the end positions (geometry(end))
+    const double *yi = a.y + 6 * (int64_t)B.i, *yj = a.y + 6 * (int64_t)B.j;
+    const d3 de = (ld3(a.h.x, B.j) + ld3(yj)) - (ld3(a.h.x, B.i) + ld3(yi));
+    st3(a.normal_end, b, de / norm(de));
+    const V3<float> nx = lift3<float>(B.n0) + lift3<float>(B.dn0);
+    float le;
+    const V3<float> dnx_e = normal_change(B.L0, nx, uj - ui, le);
+    const TransportInc<float> t2 = make_transport_inc(o.n, dnx_e - o.dn_x, 0.25f * (wi + wj));
+    const V3<float> fs1 = lift3<float>(B.fs) + o.dfs1;
+    const V3<float> mb1 = lift3<float>(B.mb) + o.dmb1;
+    const V3<float> off1 = lift3<float>(B.off) + o.doff;
+    const V3<float> dfs = o.dfs1 + t2.apply(fs1);
+    const V3<float> dmb = o.dmb1 + t2.apply(mb1);
+    const V3<float> doff = o.doff + t2.apply(off1);
+    const d3 fs = ld3(a.h.fs, b), mb = ld3(a.h.mb, b), off = ld3(a.h.offset, b);
+    st3(a.fs_end, b, fs + mk(dfs.x, dfs.y, dfs.z));
+    st3(a.mb_end, b, mb + mk(dmb.x, dmb.y, dmb.z));
+    st3(a.offset_end, b, off + mk(doff.x, doff.y, doff.z));
+}
+
+__global__ void __launch_bounds__(kThreads) commit_sites(int64_t n, const double *x, const double *y, double *x_end) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    st3(x_end, s, ld3(x, s) + ld3(y + 6 * s));
+}
+
+}  // namespace mp
+}  // namespace dpf
+
+using namespace dpf;
+using namespace dpf::mp;
+
+extern "C" {
+
+int64_t dpf_mixed_bond_floats(int64_t n_bonds) { return 4 * 11 * n_bonds; }
+
+int64_t dpf_mixed_workspace_floats(int64_t n_sites) { return 30 * n_sites + 4 * (int64_t)kMaxPcgBlocks; }
+
+static bool mixed_graph_ok(const dpf_graph *g) {
+    return g && g->n_sites > 0 && g->n_bonds >= 0 && g->n_bonds < (int64_t(1) << 31) && g->inc_ptr && g->inc_bond;
+}
+
+int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h, const double *mass,
+                    const double *v, const double *external, const uint8_t *fixed, double dt, float *bond_data,
+                    double *r0, double *loads, double *scales, double *wrench, double *partials, int *status,
+                    void *stream) {
+    if (!mixed_graph_ok(g) || !k || !h || !h->x || !h->radii || !h->normal || !h->offset || !h->fn || !h->fs ||
+        !h->mt || !h->mb || !mass || !v || !external || !fixed || !bond_data || !r0 || !scales || !partials ||
+        !status || (g->n_bonds && (!wrench || !g->edges)))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (g->n_bonds) {
+        SetupArgs a{g->n_bonds, g->edges, *k, *h, split_bond_data(bond_data, g->n_bonds), wrench, status};
+        setup_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
+    SetupSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, mass, v, external, fixed, dt, 0.5 * dt * dt,
+                    r0, loads, scales, partials};
+    setup_sites<<<reduce_grid(g->n_sites), kThreads, 0, st>>>(s);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const double *mass,
+                       const uint8_t *fixed, double dt, const double *r0, int want_tangent, const float *preconditioner,
+                       const double *units, double *residual, double *scaled, double *norms, float *wrench,
+                       double *partials, int *status, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !y || !mass || !fixed || !r0 || !residual || !status ||
+        (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (g->n_bonds) {
+        ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y, want_tangent, wrench, status};
+        residual_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
+    ResidualSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, y, mass, r0, fixed, 0.5 * dt * dt,
+                       preconditioner, units, residual, scaled, norms, partials, status};
+    residual_sites<<<reduce_grid(g->n_sites), kThreads, 0, st>>>(s);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const double *mass, const uint8_t *fixed,
+                      const double *radii, double dt, float *block, float *preconditioner, double *units,
+                      void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !mass || !fixed || !radii || !preconditioner || !units)
+        return DPF_ERR_ARGUMENT;
+    ScalingArgs a{g->n_sites, g->inc_ptr, g->inc_bond, split_bond_data(bond_data, g->n_bonds), mass, radii, fixed,
+                  (float)(0.25 * dt * dt), block, preconditioner, units};
+    scaling_sites_f32<<<blocks_for(g->n_sites, 128), 128, 0, (cudaStream_t)stream>>>(a);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const double *units,
+                             const double *residual, double *scaled, double *norms, double *partials, void *stream) {
+    if (n_sites <= 0 || !preconditioner || !units || !residual || (norms && !partials)) return DPF_ERR_ARGUMENT;
+    scale_sites_f32<<<reduce_grid(n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units,
+                                                                                  residual, scaled, norms, partials);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const double *y, const double *direction,
+                              const double *mass, const uint8_t *fixed, double dt, const double *units,
+                              const float *preconditioner, double *out, float *wrench, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !y || !direction || !mass || !fixed || !out || (g->n_bonds && !wrench) ||
+        (preconditioner && !units))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (g->n_bonds) {
+        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y, direction, units, wrench};
+        jvp_bonds_mixed<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
+    JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, direction, units, mass, preconditioner, fixed,
+                  0.5 * dt * dt, out};
+    jvp_sites_mixed<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(s);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_stiffness_apply(const dpf_graph *g, float *bond_data, const float *q, double *out, float *wrench,
+                              void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !q || !out || (g->n_bonds && !wrench)) return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (g->n_bonds)
+        stiffness_bonds_f32<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(
+            g->n_bonds, split_bond_data(bond_data, g->n_bonds), q, wrench);
+    gather_to_f64<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, g->inc_ptr, g->inc_bond,
+                                                                          wrench, out);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_to_float(int64_t count, const double *a, float *out, void *stream) {
+    if (count <= 0 || !a || !out) return DPF_ERR_ARGUMENT;
+    to_f32<<<blocks_for(count, kThreads), kThreads, 0, (cudaStream_t)stream>>>(count, a, out);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+struct MixedDeviceInfo {
+    int sms = 0, blocks_per_sm = 0;
+};
+
+static MixedDeviceInfo &mixed_info() {
+    static MixedDeviceInfo info[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    MixedDeviceInfo &d = info[dev & 63];
+    if (d.sms == 0) {
+        cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, pcg_kernel_f32, kThreads, 0);
+    }
+    return d;
+}
+
+int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *mass, const uint8_t *fixed,
+                           const float *block, const float *preconditioner, const double *units,
+                           const double *vector, double dt, double tolerance, int max_iterations, double *out,
+                           int *iterations, float *wrench, float *workspace, unsigned *barrier, int *status,
+                           void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !mass || !fixed || !block || !preconditioner || !units || !vector ||
+        !out || !iterations || !workspace || !barrier || !status || max_iterations < 1 || (g->n_bonds && !wrench))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    MixedDeviceInfo &info = mixed_info();
+    if (info.sms <= 0 || info.blocks_per_sm <= 0) return DPF_ERR_CUDA;
+    const int64_t want = blocks_for(g->n_sites > g->n_bonds ? g->n_sites : g->n_bonds, kThreads);
+    int64_t cap = (int64_t)info.sms * info.blocks_per_sm;
+    if (cap > kMaxPcgBlocks) cap = kMaxPcgBlocks;
+    const int grid = (int)(want < cap ? (want < 1 ? 1 : want) : cap);
+    const int64_t n6 = 6 * g->n_sites;
+    PcgArgs a{};
+    a.n = g->n_sites;
+    a.m = g->n_bonds;
+    a.ptr = g->inc_ptr;
+    a.inc = g->inc_bond;
+    a.bd = split_bond_data(bond_data, g->n_bonds);
+    a.mass = mass;
+    a.units = units;
+    a.vector = vector;
+    a.block = block;
+    a.P = preconditioner;
+    a.fixed = fixed;
+    a.alpha_op = (float)(0.25 * dt * dt);
+    a.tol2 = tolerance * tolerance;
+    a.max_it = max_iterations;
+    a.out = out;
+    a.iterations = iterations;
+    a.wrench = wrench;
+    a.x = workspace;
+    a.r = workspace + n6;
+    a.z = workspace + 2 * n6;
+    a.d = workspace + 3 * n6;
+    a.ad = workspace + 4 * n6;
+    double *parts = reinterpret_cast<double *>(workspace + 30 * g->n_sites + (30 * g->n_sites) % 2);
+    a.part_a = parts;
+    a.part_b = parts + kMaxPcgBlocks;
+    a.barrier = barrier;
+    a.status = status;
+    if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return DPF_ERR_CUDA;
+    void *args[] = {&a};
+    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel_f32, grid, kThreads, args, 0, st) != cudaSuccess)
+        return DPF_ERR_CUDA;
+    return DPF_OK;
+}
+
+int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y, double *x_end,
+                     double *normal_end, double *offset_end, double *fn_end, double *fs_end, double *mt_end,
+                     double *mb_end, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !h || !h->x || !h->fn || !h->fs || !h->mt || !h->mb || !h->offset ||
+        !y || !x_end || ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (g->n_bonds) {
+        CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y, normal_end, offset_end, fs_end, mb_end,
+                     fn_end, mt_end};
+        commit_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
+    commit_sites<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, h->x, y, x_end);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+}  // extern "C"

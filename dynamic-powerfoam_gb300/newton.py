@@ -600,18 +600,73 @@ class NewtonBonds(FiniteBonds):
 
     # ---- the Newton step ---------------------------------------------------
     def _evaluate(self, y, dt, external, tangent_out=None, scaled=None):
-        """Residual at y with every trial guard; returns (r, [|r|, max|s|, |s|], status)."""
+        """Residual at y with every trial guard (status in self._status)."""
         r = torch.empty_like(y)
         self._status.zero_()
         use_p = tangent_out is None
-        self._timed('residual', lambda: self._call('dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
-                   ctypes.byref(self._history_struct()), y.data_ptr(), self._v.data_ptr(), external.data_ptr(),
-                   self.mass.data_ptr(), self.fixed.data_ptr(), float(dt),
-                   ctypes.byref(self._trial_struct(tangent_out, end=False)) if tangent_out else None,
-                   self.preconditioner.data_ptr() if use_p else None, self.units.data_ptr() if use_p else None,
-                   r.data_ptr(), _addr(scaled) if use_p else None, self._scalars.data_ptr() if use_p else None,
-                   self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream()))
+        self._timed('residual', lambda: self._call(
+            'dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+            ctypes.byref(self._history_struct()), y.data_ptr(), self._v.data_ptr(), external.data_ptr(),
+            self.mass.data_ptr(), self.fixed.data_ptr(), float(dt),
+            ctypes.byref(self._trial_struct(tangent_out, end=False)) if tangent_out else None,
+            self.preconditioner.data_ptr() if use_p else None, self.units.data_ptr() if use_p else None,
+            r.data_ptr(), _addr(scaled) if use_p else None, self._scalars.data_ptr() if use_p else None,
+            self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream()))
         return r
+
+    # Precision-specific stages of step(); the control flow in step() is the
+    # reference's (bonded_dem_newton.py:132-201).
+    def _step_begin(self, dt, external):
+        """rhs_scale of the step (bonded_dem_newton.py:138-139)."""
+        loads = self.loads()
+        self._call('dpf_rhs_scale', self.n_sites, self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
+                   loads.data_ptr(), self.fixed.data_ptr(), dt, self._scalars.data_ptr(), self._partials.data_ptr(),
+                   self._stream())
+        (a, l), _ = self._fetch(2)
+        return max(a, .5*dt*dt*l, 1e-30)
+
+    def _iteration_residual(self, y, dt, external):
+        """trial + prepare_scaling + residual + scaling at the iterate; returns
+        (scaled residual, [|r|, max|s|, |s|]) and raises on a trial guard."""
+        m = self.n_bonds
+        tangent = dict(force=None, n=torch.empty((m, 3), dtype=F64, device=self.device),
+                       ri=torch.empty((m, 3), dtype=F64, device=self.device),
+                       rj=torch.empty((m, 3), dtype=F64, device=self.device))
+        r = self._evaluate(y, dt, external, tangent_out=tangent)
+        _, status = self._fetch(status=True)
+        if status:
+            raise guard_error(status)
+        self.prepare_scaling(tangent, dt)
+        scaled = torch.empty_like(r)
+        self._call('dpf_scale_residual', self.n_sites, self.preconditioner.data_ptr(), self.units.data_ptr(),
+                   r.data_ptr(), scaled.data_ptr(), self._scalars.data_ptr(), self._partials.data_ptr(),
+                   self._stream())
+        norms, _ = self._fetch(3)
+        return scaled, norms
+
+    def _newton_operator(self, y, dt, external):
+        units, pre = self.units, self.preconditioner
+        if self._overridden('jacobian_vector'):
+            return lambda v: self.scale_residual(self.jacobian_vector(y, units*v, dt, external))
+        return lambda v: self._jvp(y, self._vec(v), dt, units=units, preconditioner=pre)
+
+    def _newton_preconditioner(self, dt):
+        return lambda v: self.elastic_precondition(v, dt)
+
+    def _line_merit(self, candidate, dt, external):
+        """|P r(candidate) / units| and the guard status (one device sync)."""
+        self._evaluate(candidate, dt, external)
+        (_, _, value), status = self._fetch(3, status=True)
+        return value, status
+
+    def _accept(self, y, dt):
+        """Commit the trial at y and update velocity and rotation (bonded_dem_newton.py:149-154)."""
+        state = self.trial(y)
+        rotation = self._vec(self.rotation).clone()
+        self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(), rotation.data_ptr(),
+                   self._stream())
+        self.commit(state)
+        self.v, self.rotation = self._v, rotation
 
     @torch.no_grad()
     def step(self, dt, external, tolerance=2e-7, max_iterations=12, *,
@@ -625,43 +680,20 @@ class NewtonBonds(FiniteBonds):
         self._v = self._vec(self.v).clone()
         y = torch.zeros_like(self._v)
         stream = self._stream()
-        loads = self.loads()
-        self._call('dpf_rhs_scale', self.n_sites, self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
-                   loads.data_ptr(), self.fixed.data_ptr(), dt, self._scalars.data_ptr(), self._partials.data_ptr(),
-                   stream)
-        (a, l), _ = self._fetch(2)
-        rhs_scale = max(a, .5*dt*dt*l, 1e-30)
+        rhs_scale = self._step_begin(dt, external)
         krylov = 0
         self.inner_iterations = 0
         residual_trace = []
         relative = local = float('nan')
-        generic_jvp = self._overridden('jacobian_vector')
-        generic_pc = self._overridden('elastic_precondition')
-        m, n6 = self.n_bonds, 6*self.n_sites
+        n6 = 6*self.n_sites
         for iteration in range(max_iterations+1):
-            tangent = dict(force=None, n=torch.empty((m, 3), dtype=F64, device=self.device),
-                           ri=torch.empty((m, 3), dtype=F64, device=self.device),
-                           rj=torch.empty((m, 3), dtype=F64, device=self.device))
-            r = self._evaluate(y, dt, external, tangent_out=tangent)
-            _, status = self._fetch(status=True)
-            if status:
-                raise guard_error(status)
-            self.prepare_scaling(tangent, dt)
-            scaled = torch.empty_like(r)
-            self._call('dpf_scale_residual', self.n_sites, self.preconditioner.data_ptr(), self.units.data_ptr(),
-                       r.data_ptr(), scaled.data_ptr(), self._scalars.data_ptr(), self._partials.data_ptr(), stream)
-            (rnorm, local, merit), _ = self._fetch(3)
+            scaled, (rnorm, local, merit) = self._iteration_residual(y, dt, external)
             relative = rnorm/rhs_scale
             if not np.isfinite(relative) or not np.isfinite(local):
                 raise SubdivideError(f'Subdivide: non-finite Newton residual ({relative:g}, {local:g})')
             residual_trace.append([relative, local])
             if relative < tolerance and local < pose_tolerance:
-                state = self.trial(y)
-                rotation = self._vec(self.rotation).clone()
-                self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(),
-                           rotation.data_ptr(), stream)
-                self.commit(state)
-                self.v, self.rotation = self._v, rotation
+                self._accept(y, dt)
                 self.time += dt
                 self._call('dpf_dot_norm', n6, external.data_ptr(), y.data_ptr(), self._scalars.data_ptr(),
                            self._partials.data_ptr(), stream)
@@ -673,13 +705,7 @@ class NewtonBonds(FiniteBonds):
                                   max_step_rotation=max_rotation)
             if iteration == max_iterations:
                 break
-            units, pre = self.units, self.preconditioner
-            if generic_jvp:
-                def operator(v):
-                    return self.scale_residual(self.jacobian_vector(y, units*v, dt, external))
-            else:
-                def operator(v):
-                    return self._jvp(y, self._vec(v), dt, units=units, preconditioner=pre)
+            operator = self._newton_operator(y, dt, external)
             if backend == 'dense':
                 free = torch.nonzero(~self.fixed.repeat_interleave(6)).flatten()
                 if len(free) > 400:
@@ -695,7 +721,7 @@ class NewtonBonds(FiniteBonds):
                 delta = delta.reshape_as(y)
             elif backend == 'fgmres':
                 if preconditioning == 'elastic':
-                    precondition = (lambda v: self.elastic_precondition(v, dt))
+                    precondition = self._newton_preconditioner(dt)
                 elif preconditioning == 'block':
                     precondition = (lambda v: v)
                 else:
@@ -719,8 +745,7 @@ class NewtonBonds(FiniteBonds):
                 factor = 2.**(-power)
                 self._call('dpf_axpby', n6, 1., y.data_ptr(), factor, correction.data_ptr(), candidate.data_ptr(),
                            stream)
-                self._evaluate(candidate, dt, external)
-                (_, _, value), status = self._fetch(3, status=True)
+                value, status = self._line_merit(candidate, dt, external)
                 if status:
                     continue
                 if value < (1 - 1e-4*factor)*merit:
@@ -755,3 +780,111 @@ class AdaptiveIntervals:
             self.depth -= 1
             self.easy_intervals = 0
         return work, records
+
+
+class MixedNewtonBonds(NewtonBonds):
+    """Mixed-precision form of ``NewtonBonds.step``: the same equations, control
+    flow, tolerances and ``info`` as the reference solver
+    (``experiments/bonded_dem_newton.py:132-201``) with float32 bond sweeps
+    (residual increment, JVP, K q, 6x6 blocks, elastic PCG) and float64
+    reductions, float64 Krylov vectors and a float64-accurate residual:
+    r(y) = r0 + M y - dt^2/2 sum of float32 bond increments, r0 computed in
+    float64 once per step.  Every other method is the float64 one it inherits.
+    """
+
+    def __init__(self, *args, **kwargs):
+        super().__init__(*args, **kwargs)
+        lib, n, m = self._lib, self.n_sites, self.n_bonds
+        dev = self.device
+        self._bond_data = torch.empty(max(4, lib.dpf_mixed_bond_floats(m)), dtype=torch.float32, device=dev)
+        self._wrench32 = torch.empty(max(1, 9*m), dtype=torch.float32, device=dev)
+        self._r0 = torch.empty((n, 6), dtype=F64, device=dev)
+        self._block32 = torch.empty((n, 6, 6), dtype=torch.float32, device=dev)
+        self._p32 = torch.empty((n, 6, 6), dtype=torch.float32, device=dev)
+        self._units = torch.empty((n, 6), dtype=F64, device=dev)
+        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n), dtype=torch.float32, device=dev)
+
+    def _step_begin(self, dt, external):
+        self._status.zero_()
+        self._timed('setup', lambda: self._call(
+            'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+            ctypes.byref(self._history_struct()), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
+            self.fixed.data_ptr(), dt, self._bond_data.data_ptr(), self._r0.data_ptr(), None,
+            self._scalars.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(),
+            self._stream()))
+        (a, l), status = self._fetch(2, status=True)
+        if status:
+            raise guard_error(status)
+        return max(a, .5*dt*dt*l, 1e-30)
+
+    def _mixed_residual(self, y, dt, want_tangent, scaled=None, norms=True):
+        r = torch.empty_like(y)
+        self._status.zero_()
+        use_p = not want_tangent
+        self._timed('residual', lambda: self._call(
+            'dpf_mixed_residual', ctypes.byref(self._graph), self._bond_data.data_ptr(), y.data_ptr(),
+            self.mass.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(), int(want_tangent),
+            self._p32.data_ptr() if use_p else None, self._units.data_ptr() if use_p else None, r.data_ptr(),
+            _addr(scaled) if use_p else None, self._scalars.data_ptr() if (use_p and norms) else None,
+            self._wrench32.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream()))
+        return r
+
+    def _iteration_residual(self, y, dt, external):
+        r = self._mixed_residual(y, dt, want_tangent=True)
+        self._timed('scaling', lambda: self._call(
+            'dpf_mixed_scaling', ctypes.byref(self._graph), self._bond_data.data_ptr(), self.mass.data_ptr(),
+            self.fixed.data_ptr(), self.radii.data_ptr(), dt, self._block32.data_ptr(), self._p32.data_ptr(),
+            self._units.data_ptr(), self._stream()))
+        scaled = torch.empty_like(r)
+        self._call('dpf_mixed_scale_residual', self.n_sites, self._p32.data_ptr(), self._units.data_ptr(),
+                   r.data_ptr(), scaled.data_ptr(), self._scalars.data_ptr(), self._partials.data_ptr(),
+                   self._stream())
+        norms, status = self._fetch(3, status=True)
+        if status:
+            raise guard_error(status)
+        self.units = self._units
+        return scaled, norms
+
+    def _newton_operator(self, y, dt, external):
+        def operator(v):
+            v = self._vec(v)
+            out = torch.empty_like(v)
+            self._timed('jvp', lambda: self._call(
+                'dpf_mixed_jacobian_vector', ctypes.byref(self._graph), self._bond_data.data_ptr(), y.data_ptr(),
+                v.data_ptr(), self.mass.data_ptr(), self.fixed.data_ptr(), dt, self._units.data_ptr(),
+                self._p32.data_ptr(), out.data_ptr(), self._wrench32.data_ptr(), self._stream()))
+            return out
+        return operator
+
+    def _newton_preconditioner(self, dt):
+        def precondition(vector, tolerance=.03, max_iterations=80):
+            vector = self._vec(vector)
+            out = torch.empty_like(vector)
+            self._timed('pcg', lambda: self._call(
+                'dpf_mixed_precondition', ctypes.byref(self._graph), self._bond_data.data_ptr(),
+                self.mass.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p32.data_ptr(),
+                self._units.data_ptr(), vector.data_ptr(), dt, tolerance, max_iterations, out.data_ptr(),
+                self._inner.data_ptr(), self._wrench32.data_ptr(), self._mixed_workspace.data_ptr(),
+                self._barrier.data_ptr(), self._status.data_ptr(), self._stream()))
+            return out
+        return precondition
+
+    def _line_merit(self, candidate, dt, external):
+        self._mixed_residual(candidate, dt, want_tangent=False)
+        (_, _, value), status = self._fetch(3, status=True)
+        return value, status
+
+    def _accept(self, y, dt):
+        m, n = self.n_bonds, self.n_sites
+        e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
+        state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
+        self._timed('commit', lambda: self._call(
+            'dpf_mixed_commit', ctypes.byref(self._graph), self._bond_data.data_ptr(),
+            ctypes.byref(self._history_struct()), y.data_ptr(), state['x'].data_ptr(), state['normal'].data_ptr(),
+            state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(), state['mt'].data_ptr(),
+            state['mb'].data_ptr(), self._stream()))
+        rotation = self._vec(self.rotation).clone()
+        self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(), rotation.data_ptr(),
+                   self._stream())
+        self.commit(state)
+        self.v, self.rotation = self._v, rotation

@@ -250,6 +250,88 @@ int dpf_rhs_scale(int64_t n_sites, const double *mass, const double *v, const do
 int dpf_masked_scale(int64_t n_sites, const double *a, const double *units, const uint8_t *fixed,
                      double *out, void *stream);
 
+/* ---- Mixed precision: float32 bond sweeps, float64 reductions and residual ----
+ * One step of NewtonBonds.step (experiments/bonded_dem_newton.py:132-201) in
+ * float32 bulk arithmetic.  The residual keeps float64 accuracy: a float64
+ * setup per step computes r0 = -dt M v - dt^2/2 (loads(x) + external); for an
+ * increment y the residual is r0 + M y - dt^2/2 sum of per-bond float32
+ * increments f_mid(y) - f_mid(0), evaluated from small quantities only and
+ * summed per site in float64.  bond_data: dpf_mixed_bond_floats(M) floats
+ * (float4 records + float32 tangent, 16-byte aligned); wrench: 9 M floats. */
+int64_t dpf_mixed_bond_floats(int64_t n_bonds);
+
+/* Float workspace of dpf_mixed_precondition for N sites. */
+int64_t dpf_mixed_workspace_floats(int64_t n_sites);
+
+/* Per-step float64 setup: bond records from the committed state, r0 (N, 6),
+ * optionally loads(x) (N, 6), and scales[0..1] = [|dt M v + dt^2/2 ext|,
+ * |loads on free sites|] (the two terms of rhs_scale).  wrench: 9 M doubles.
+ * Replaces the loads/rhs_scale prologue of NewtonBonds.step
+ * (experiments/bonded_dem_newton.py:137-139, experiments/bonded_dem_finite_gpu.py:82-85). */
+int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+                    const double *mass, const double *v, const double *external,
+                    const uint8_t *fixed, double dt, float *bond_data, double *r0, double *loads,
+                    double *scales, double *wrench, double *partials, int *status, void *stream);
+
+/* Residual at increment y with every trial guard (status bits as dpf_trial);
+ * want_tangent stores the midpoint tangent for dpf_mixed_scaling and K q;
+ * preconditioner (float32 (N, 6, 6)) / units / scaled / norms as in dpf_residual.
+ * Replaces NewtonBonds.residual + scale_residual (experiments/bonded_dem_newton.py:83-86, 104-105). */
+int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const double *mass,
+                       const uint8_t *fixed, double dt, const double *r0, int want_tangent,
+                       const float *preconditioner, const double *units, double *residual,
+                       double *scaled, double *norms, float *wrench, double *partials, int *status,
+                       void *stream);
+
+/* Blocks and scaling from the stored float32 tangent: block (float32 (N,6,6),
+ * may be NULL), preconditioner = block^-1 (float32, Jacobi-scaled Cholesky),
+ * units (float64 (N, 6)).
+ * Replaces NewtonBonds.prepare_scaling (experiments/bonded_dem_newton.py:94-102). */
+int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const double *mass, const uint8_t *fixed,
+                      const double *radii, double dt, float *block, float *preconditioner,
+                      double *units, void *stream);
+
+/* Scaled residual with the float32 block inverse: s = P r / units and
+ * norms = [|r|, max|s|, |s|] (float64).
+ * Replaces NewtonBonds.scale_residual (experiments/bonded_dem_newton.py:104-105). */
+int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const double *units,
+                             const double *residual, double *scaled, double *norms, double *partials,
+                             void *stream);
+
+/* J d, the forward-mode derivative of the float32 residual increment; the
+ * same options as dpf_jacobian_vector (units, float32 preconditioner).
+ * Replaces NewtonBonds.jacobian_vector (experiments/bonded_dem_newton.py:88-92). */
+int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const double *y,
+                              const double *direction, const double *mass, const uint8_t *fixed,
+                              double dt, const double *units, const float *preconditioner,
+                              double *out, float *wrench, void *stream);
+
+/* K q in float32 from the stored tangent; q float32 (N, 6), out float64 (N, 6).
+ * Replaces LinearBondsGPU.stiffness (experiments/bonded_dem_linear_gpu.py:42-52). */
+int dpf_mixed_stiffness_apply(const dpf_graph *g, float *bond_data, const float *q, double *out,
+                              float *wrench, void *stream);
+
+/* out[e] = (float) a[e] for e < count. */
+int dpf_to_float(int64_t count, const double *a, float *out, void *stream);
+
+/* Elastic PCG in float32 with float64 dot products (same stopping rule and
+ * iteration accounting as dpf_elastic_precondition); workspace:
+ * dpf_mixed_workspace_floats(N) floats; block/preconditioner float32.
+ * Replaces NewtonBonds.elastic_precondition (experiments/bonded_dem_newton.py:107-130). */
+int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *mass,
+                           const uint8_t *fixed, const float *block, const float *preconditioner,
+                           const double *units, const double *vector, double dt, double tolerance,
+                           int max_iterations, double *out, int *iterations, float *wrench,
+                           float *workspace, unsigned *barrier, int *status, void *stream);
+
+/* End state of the accepted increment y: float32 increments added to the
+ * float64 committed history (end normal recomputed in float64 from x + y).
+ * Replaces FiniteBondsGPU.trial's end-of-step outputs and commit
+ * (experiments/bonded_dem_finite_gpu.py:102-120). */
+int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y,
+                     double *x_end, double *normal_end, double *offset_end, double *fn_end,
+                     double *fs_end, double *mt_end, double *mb_end, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

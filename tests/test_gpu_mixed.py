@@ -1,0 +1,125 @@
+"""Mixed-precision form (float32 bond sweeps, float64 reductions and residual)
+against the float64 path and the reference's golden vectors.
+
+Tolerances: the residual must agree with the float64 residual to 1e-7 of the
+step's rhs scale (well inside the 1e-6 Newton tolerance); the float32 JVP to
+1e-4 relative (float32 operator inside an inexact Newton); accepted states to
+the reference's own cross-solver bars (positions 1e-7, rotations 1e-6,
+bonded_dem_newton_checks.py:130-132) and, for the foam trajectories, a
+relative displacement error <= 1e-6 and a float64 relative force residual
+<= 1e-6 against the float64 solve of the same inputs.
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import golden, newton_inputs, STATE
+from tests.helpers import host
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip('torch')
+
+
+@pytest.fixture(scope='module', autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip('needs a CUDA GPU')
+
+
+def mixed_from_golden(g, cls=None):
+    import dpf_gb300
+    cls = cls or dpf_gb300.MixedNewtonBonds
+    s = cls(**newton_inputs(g))
+    for k in STATE:
+        setattr(s, k, torch.as_tensor(np.array(g['state_' + k]), dtype=torch.float64, device=s.device).contiguous())
+    return s
+
+
+@pytest.mark.parametrize('case', ['newton_prestressed', 'newton_unstressed'])
+def test_mixed_residual_matches_float64(case):
+    import dpf_gb300
+    g = golden(case)
+    s = mixed_from_golden(g)
+    dt, ext = float(g['dt']), s.tensor(g['external'])
+    s._v = s._vec(s.v).clone()
+    rhs_scale = s._step_begin(dt, ext)
+    for scale in (0., .3, 1.):
+        y = s.tensor(g['y'])*scale
+        ref = s.residual(y, dt, ext)
+        r = s._mixed_residual(y, dt, want_tangent=True)
+        err = float(torch.linalg.vector_norm(r - ref))/rhs_scale
+        assert err < 1e-7, (scale, err)
+    # float32 tangent geometry
+    y = s.tensor(g['y'])
+    s._mixed_residual(y, dt, want_tangent=True)
+    m = s.n_bonds
+    t = s._bond_data[7*4*m:10*4*m].view(3, m, 4)
+    trial = s.trial(y)
+    for row, key in enumerate(('n', 'ri', 'rj')):
+        got = t[row, :, :3].double()
+        assert float(torch.linalg.vector_norm(got - trial[key])/torch.linalg.vector_norm(trial[key])) < 1e-6
+
+
+@pytest.mark.parametrize('case', ['newton_prestressed', 'newton_unstressed'])
+def test_mixed_jvp_matches_float64(case):
+    g = golden(case)
+    s = mixed_from_golden(g)
+    dt, ext = float(g['dt']), s.tensor(g['external'])
+    y = s.tensor(g['y'])
+    s._v = s._vec(s.v).clone()
+    s._step_begin(dt, ext)
+    s._iteration_residual(y, dt, ext)
+    d = s.tensor(g['jvp_direction'])
+    ref = s.jacobian_vector(y, d, dt, ext)
+    op = s._newton_operator(y, dt, ext)
+    got = op(d/s._units)          # operator includes units and the float32 block scaling
+    ref_scaled = torch.einsum('nij,nj->ni', s._p32.double(), ref)/s._units
+    err = float(torch.linalg.vector_norm(got - ref_scaled)/torch.linalg.vector_norm(ref_scaled))
+    assert err < 1e-4, err
+
+
+@pytest.mark.parametrize('case', ['newton_prestressed', 'newton_unstressed'])
+def test_mixed_step_matches_reference_step(case):
+    g = golden(case)
+    s = mixed_from_golden(g)
+    energy0 = s.energy()
+    work, info = s.step(float(g['dt']), s.tensor(g['step_load']), tolerance=2e-7, linear_tolerance=1e-7)
+    tag = 'fgmres_elastic'
+    assert np.abs(host(s.x) - g[f'step_{tag}_state_x']).max() < 1e-7
+    assert np.abs(host(s.rotation) - g[f'step_{tag}_state_rotation']).max() < 1e-6
+    for k in ('v', 'fn', 'fs', 'mt', 'mb', 'normal', 'offset'):
+        ref = g[f'step_{tag}_state_{k}']
+        assert np.abs(host(getattr(s, k)) - ref).max() <= 1e-6*max(1., np.abs(ref).max()), k
+    assert abs(work - float(g[f'step_{tag}_work'])) <= 1e-6*abs(float(g[f'step_{tag}_work']))
+    assert abs(s.energy() - energy0 - work)/max(energy0, abs(work), 1e-30) < 1e-5
+
+
+@pytest.mark.parametrize('lattice,steps', [(8, 5), (16, 3)])
+def test_mixed_trajectory_matches_float64_solve(lattice, steps):
+    """Relative displacement error and float64 force residual <= 1e-6 against
+    the float64 solver on the same inputs."""
+    import dpf_gb300
+    foam = dpf_gb300.jittered_lattice_foam(lattice, seed=2)
+    load = dpf_gb300.gravity_load(foam)
+    args = (foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'], foam['fixed'])
+    kw = dict(young=foam['young'], shear=foam['shear'])
+    a = dpf_gb300.NewtonBonds(*args, **kw)
+    b = dpf_gb300.MixedNewtonBonds(*args, **kw)
+    ext = a.tensor(load)
+    x0 = a.x.clone()
+    for _ in range(steps):
+        wa, ia = a.step(1e-3, ext, tolerance=1e-6)
+        wb, ib = b.step(1e-3, ext, tolerance=1e-6)
+        assert ib['nonlinear_relative_residual'] < 1e-6
+    disp = float(torch.linalg.vector_norm(a.x - x0))
+    err = float(torch.linalg.vector_norm(b.x - a.x))/disp
+    assert err < 1e-6, err
+    # the mixed end state, checked with the float64 residual of a zero increment
+    # of a fresh float64 solver carrying the mixed state and velocity
+    c = dpf_gb300.NewtonBonds(*args, **kw)
+    for k in STATE:
+        setattr(c, k, getattr(b, k).clone())
+    for k in ('fn', 'mt'):
+        assert float(torch.linalg.vector_norm(getattr(b, k) - getattr(a, k))/torch.linalg.vector_norm(getattr(a, k))) < 1e-5
+    ev = float(torch.linalg.vector_norm(b.v - a.v)/torch.linalg.vector_norm(a.v))
+    assert ev < 1e-5, ev
