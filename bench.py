@@ -50,6 +50,9 @@ def parse():
     p.add_argument('--tolerance', type=float, default=1e-6)
     p.add_argument('--seed', type=int, default=0)
     p.add_argument('--no-cpu-baseline', action='store_true')
+    p.add_argument('--precision', default='mixed', choices=('mixed', 'f64'))
+    p.add_argument('--plain-steps', type=int, default=3,
+                   help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
     return p.parse_args()
 
 
@@ -175,8 +178,9 @@ def run_ours(args):
             dist.barrier()
 
     foam, load = foam_and_load(args.lattice, args.seed + rank)
-    s = dpf_gb300.NewtonBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
-                              foam['fixed'], young=foam['young'], shear=foam['shear'], device=device)
+    cls = dpf_gb300.MixedNewtonBonds if args.precision == 'mixed' else dpf_gb300.NewtonBonds
+    s = cls(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
+            foam['fixed'], young=foam['young'], shear=foam['shear'], device=device)
     ext = s.tensor(load)
     n_sites, n_bonds = s.n_sites, s.n_bonds
     for _ in range(args.warmup):
@@ -224,6 +228,24 @@ def run_ours(args):
         dist.all_reduce(times, op=dist.ReduceOp.MAX)
     ms, e_ms = times.tolist()
 
+    # the plain float64 solver on the same foam, one-at-a-time (spec comparator)
+    plain = None
+    if args.precision == 'mixed' and args.plain_steps > 0:
+        p64 = dpf_gb300.NewtonBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
+                                    foam['fixed'], young=foam['young'], shear=foam['shear'], device=device)
+        p64.step(args.dt, ext, tolerance=args.tolerance)
+        torch.cuda.synchronize()
+        p_start, p_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p_start.record()
+        for _ in range(args.plain_steps):
+            p64.step(args.dt, ext, tolerance=args.tolerance)
+        p_end.record()
+        torch.cuda.synchronize()
+        p_ms = p_start.elapsed_time(p_end)
+        plain = dict(value=args.plain_steps/(p_ms*1e-3), unit=UNIT, steps=args.plain_steps, dtype='f64',
+                     ms_per_step=p_ms/args.plain_steps)
+        del p64
+
     # roofline of the dominant launch
     kernels = {}
     for key, pairs in profile.items():
@@ -231,13 +253,21 @@ def run_ours(args):
         kernels[key] = dict(launches=len(durations), total_ms=sum(durations),
                             mean_ms=sum(durations)/len(durations))
     cg = sum(i['cg_iterations'] for i in infos)
-    # Algorithmic bytes (float64): JVP 160 B/bond + 192 B/site; one PCG iteration's
-    # K d sweep 120 B/bond + 112 B/site plus its 6x6 block and vector traffic
-    # (P 288 + 6 vectors x 48 = 576 B/site).
-    bytes_jvp = 160*n_bonds + 192*n_sites
-    bytes_cg_iter = 120*n_bonds + (112 + 576)*n_sites
-    alg = dict(jvp=bytes_jvp, pcg=bytes_cg_iter*cg/max(1, kernels.get('pcg', {}).get('launches', 1)),
-               residual=bytes_jvp)
+    pcg_launches = max(1, kernels.get('pcg', {}).get('launches', 1))
+    if args.precision == 'f64':
+        # float64: JVP 160 B/bond + 192 B/site; one PCG iteration's K d sweep
+        # 120 B/bond + 112 B/site plus 6x6 block and vector traffic (576 B/site).
+        bytes_jvp = 160*n_bonds + 192*n_sites
+        alg = dict(jvp=bytes_jvp, pcg=(120*n_bonds + 688*n_sites)*cg/pcg_launches, residual=bytes_jvp)
+    else:
+        # float32 bond data: JVP 80 B/bond + 96 B/site; HVP (K d) 60 B/bond +
+        # 56 B/site plus the float32 block and vector traffic of a CG
+        # iteration (288 B/site); residual 80 B/bond + 72 B/site; blocks 128 B/bond
+        # (two incidences of the tangent) + 296 B/site; setup 160 B/bond of
+        # float64 state read + 112 B/bond of records written + 144 B/site.
+        alg = dict(jvp=80*n_bonds + 96*n_sites, pcg=(60*n_bonds + 344*n_sites)*cg/pcg_launches,
+                   residual=80*n_bonds + 72*n_sites, scaling=128*n_bonds + 296*n_sites,
+                   setup=272*n_bonds + 144*n_sites, commit=112*n_bonds + 208*n_bonds + 48*n_sites)
     dominant = max(kernels, key=lambda k: kernels[k]['total_ms']) if kernels else None
     peaks = {}
     try:
@@ -263,17 +293,21 @@ def run_ours(args):
     e2e = world*args.steps/(e_ms*1e-3)
     mean = lambda k: sum(i[k] for i in infos)/len(infos)
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
-                ms_per_step=ms/args.steps, higher_is_better=True, scaling='weak', vs_baseline=None, dtype='f64',
+                ms_per_step=ms/args.steps, higher_is_better=True, scaling='weak', vs_baseline=None,
+                dtype='f32+f64' if args.precision == 'mixed' else 'f64',
                 data='synthetic (seeded jittered-lattice foam; no dataset)',
                 config=dict(workload=f'{args.lattice}^3 jittered-lattice foam, gravity, bottom fixed, dt={args.dt}, '
-                                     f'NewtonBonds.step tol={args.tolerance}, fgmres+elastic PCG, float64',
+                                     f'NewtonBonds.step tol={args.tolerance}, fgmres+elastic PCG, '
+                                     + ('float32 bond sweeps + float64 reductions/residual'
+                                        if args.precision == 'mixed' else 'float64'),
                             lattice=args.lattice, sites=n_sites, bonds=n_bonds, parallelism=f'replicas{world}',
                             l2='working set > L2 (no flush)',
                             newton_per_solve=mean('nonlinear_iterations'),
                             krylov_per_solve=mean('krylov_iterations'), cg_per_solve=mean('cg_iterations')),
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
-                gpu_launches=launches, kernels=kernels, roofline=roof, cpu_baseline=cpu,
+                gpu_launches=launches, kernels=kernels, roofline=roof, cpu_baseline=cpu, plain_f64=plain,
+                relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)
     if world > 1:
