@@ -1,8 +1,8 @@
 """Mixed-precision form (float32 bond sweeps, float64 reductions and residual)
 against the float64 path and the reference's golden vectors.
 
-Tolerances: the residual must agree with the float64 residual to 1e-7 of the
-step's rhs scale (well inside the 1e-6 Newton tolerance); the float32 JVP to
+Tolerances: the residual must agree with the float64 residual to 1e-7 of
+max(rhs scale, |r|) (well inside the 1e-6 Newton tolerance); the float32 JVP to
 1e-4 relative (float32 operator inside an inexact Newton); accepted states to
 the reference's own cross-solver bars (positions 1e-7, rotations 1e-6,
 bonded_dem_newton_checks.py:130-132) and, for the foam trajectories, a
@@ -47,7 +47,8 @@ def test_mixed_residual_matches_float64(case):
         y = s.tensor(g['y'])*scale
         ref = s.residual(y, dt, ext)
         r = s._mixed_residual(y, dt, want_tangent=True)
-        err = float(torch.linalg.vector_norm(r - ref))/rhs_scale
+        # relative accuracy of the residual itself (random increments put it far above rhs_scale)
+        err = float(torch.linalg.vector_norm(r - ref))/max(rhs_scale, float(torch.linalg.vector_norm(ref)))
         assert err < 1e-7, (scale, err)
     # float32 tangent geometry
     y = s.tensor(g['y'])
