@@ -75,15 +75,15 @@ SIGNATURES = {
     'dpf_mixed_workspace_floats': (i64, [i64]),
     'dpf_mixed_setup': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp, vp,
                               vp]),
-    'dpf_mixed_residual': (i32, [P(Graph), vp, vp, vp, vp, f64, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
-    'dpf_mixed_scaling': (i32, [P(Graph), vp, vp, vp, vp, f64, vp, vp, vp, vp]),
+    'dpf_mixed_residual': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_scaling': (i32, [P(Graph), vp, vp, vp, vp, f64, vp, vp, vp, vp, vp]),
     'dpf_mixed_scale_residual': (i32, [i64, vp, vp, vp, vp, vp, vp, vp]),
-    'dpf_mixed_jacobian_vector': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp]),
+    'dpf_mixed_jacobian_vector': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp]),
     'dpf_mixed_stiffness_apply': (i32, [P(Graph), vp, vp, vp, vp, vp]),
     'dpf_to_float': (i32, [i64, vp, vp, vp]),
     'dpf_mixed_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, f64, i32, vp, vp, vp, vp, vp, vp,
                                      vp]),
-    'dpf_mixed_commit': (i32, [P(Graph), vp, P(History), vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_commit': (i32, [P(Graph), vp, P(History), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_static_max_bonds': (i64, []),
 }
 
@@ -95,7 +95,7 @@ KERNELS = {
     'dpf_loads': 2, 'dpf_accept_step': 1, 'dpf_energy': 1, 'dpf_arnoldi_cgs2': 4, 'dpf_combine_rows': 1,
     'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
     'dpf_stiffness_apply_static': 2, 'dpf_mixed_setup': 2, 'dpf_mixed_residual': 2, 'dpf_mixed_scaling': 1,
-    'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 2, 'dpf_mixed_stiffness_apply': 2,
+    'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 3, 'dpf_mixed_stiffness_apply': 2,
     'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2,
 }
 LAUNCHES = {'count': 0}

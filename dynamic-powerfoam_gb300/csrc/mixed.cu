@@ -59,6 +59,63 @@ __device__ __forceinline__ void store9(float *w, int64_t b, V3<float> f, V3<floa
     p[6] = tj.x; p[7] = tj.y; p[8] = tj.z;
 }
 
+// Error-free sum a + b = s + e (Knuth's TwoSum), float32.
+__device__ __forceinline__ void two_sum(float &s, float &e, float b) {
+    const float t = s + b;
+    const float bp = t - s;
+    e += (s - (t - bp)) + (b - bp);
+    s = t;
+}
+
+// Compensated float32 site sum of a float32 bond wrench: hi + lo carries the
+// sum to about float64 accuracy without float64 arithmetic per incidence.
+__device__ __forceinline__ void gather9c(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                         const float *__restrict__ w, int64_t s, float hi[6], float lo[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) hi[c] = lo[c] = 0.0f;
+    const int e1 = ptr[s + 1];
+    for (int e = ptr[s]; e < e1; ++e) {
+        const int v = inc[e];
+        if (v >= 0) {
+            const float *p = w + 9 * (int64_t)v;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], p[c]);
+        } else {
+            const float *p = w + 9 * (int64_t)(~v);
+            two_sum(hi[0], lo[0], -p[0]);
+            two_sum(hi[1], lo[1], -p[1]);
+            two_sum(hi[2], lo[2], -p[2]);
+            two_sum(hi[3], lo[3], p[6]);
+            two_sum(hi[4], lo[4], p[7]);
+            two_sum(hi[5], lo[5], p[8]);
+        }
+    }
+}
+
+// Plain float32 site sum.
+__device__ __forceinline__ void gather9f(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                         const float *__restrict__ w, int64_t s, float acc[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
+    const int e1 = ptr[s + 1];
+    for (int e = ptr[s]; e < e1; ++e) {
+        const int v = inc[e];
+        if (v >= 0) {
+            const float *p = w + 9 * (int64_t)v;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] += p[c];
+        } else {
+            const float *p = w + 9 * (int64_t)(~v);
+            acc[0] -= p[0];
+            acc[1] -= p[1];
+            acc[2] -= p[2];
+            acc[3] += p[6];
+            acc[4] += p[7];
+            acc[5] += p[8];
+        }
+    }
+}
+
 // Site sum of a float32 bond wrench in float64.
 __device__ __forceinline__ void gather9(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
                                         const float *__restrict__ w, int64_t s, double acc[6]) {
@@ -199,16 +256,16 @@ __global__ void __launch_bounds__(kThreads) setup_sites(SetupSiteArgs a) {
 struct ResidualBondArgs {
     int64_t m;
     BondData bd;
-    const double *y;
+    const float *y;
     int want_tangent;
     float *wrench;
     int *status;
 };
 
-__device__ __forceinline__ void load_y(const double *y, int s, V3<float> &u, V3<float> &w) {
-    const double *p = y + 6 * (int64_t)s;
-    u = f3(p);
-    w = f3(p + 3);
+__device__ __forceinline__ void load_y(const float *y, int s, V3<float> &u, V3<float> &w) {
+    const float *p = y + 6 * (int64_t)s;
+    u = {p[0], p[1], p[2]};
+    w = {p[3], p[4], p[5]};
 }
 
 __global__ void __launch_bounds__(kThreads) residual_bonds(ResidualBondArgs a) {
@@ -245,104 +302,42 @@ struct ResidualSiteArgs {
     const double *y, *mass, *r0;
     const uint8_t *fixed;
     double half_dt2;
-    const float *P;
-    const double *units;
+    const float *P, *units32;
     double *residual, *scaled, *norms, *partials;
     int *status;
 };
 
-__device__ __forceinline__ void matvec6f(const float *P, const double x[6], double y[6]) {
-    float xf[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) xf[c] = (float)x[c];
+__device__ __forceinline__ void matvec6f(const float *P, const float x[6], float y[6]) {
 #pragma unroll
     for (int row = 0; row < 6; ++row) {
         float v = 0.0f;
 #pragma unroll
-        for (int c = 0; c < 6; ++c) v = fmaf(P[6 * row + c], xf[c], v);
+        for (int c = 0; c < 6; ++c) v = fmaf(P[6 * row + c], x[c], v);
         y[row] = v;
     }
 }
 
-__global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
-    double sum_r = 0.0, max_s = 0.0, sum_s = 0.0;
-    int flags = 0;
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n; s += (int64_t)gridDim.x * blockDim.x) {
-        double acc[6], r[6];
-        gather9(a.ptr, a.inc, a.wrench, s, acc);
-        const double *ys = a.y + 6 * s;
-        if (norm(ld3(ys + 3)) > 0.25) flags |= DPF_ERR_ROTATION;
-        const bool fx = a.fixed[s] != 0;
+// Scaled residual in float32 from a float64 residual: s = P r / units;
+// returns max |s| and accumulates |s|^2.
+__device__ __forceinline__ float scale_site(const float *P, const float *units32, const double r[6], double *scaled,
+                                            float &sum_s) {
+    float rf[6], sf[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double val = a.r0[6 * s + c] + a.mass[6 * s + c] * ys[c] - a.half_dt2 * acc[c];
-            r[c] = fx ? ys[c] : val;
-            a.residual[6 * s + c] = r[c];
-            sum_r += r[c] * r[c];
-        }
-        if (a.P) {
-            // scale in float64 from the float32 block inverse: P r / units
-            const float *P = a.P + 36 * s;
+    for (int c = 0; c < 6; ++c) rf[c] = (float)r[c];
+    matvec6f(P, rf, sf);
+    float mx = 0.0f;
 #pragma unroll
-            for (int row = 0; row < 6; ++row) {
-                double v = 0.0;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) v += (double)P[6 * row + c] * r[c];
-                v = v / a.units[6 * s + row];
-                if (a.scaled) a.scaled[6 * s + row] = v;
-                max_s = fmax(max_s, fabs(v));
-                sum_s += v * v;
-            }
-        }
+    for (int c = 0; c < 6; ++c) {
+        const float v = sf[c] / units32[c];
+        if (scaled) scaled[c] = v;
+        mx = fmaxf(mx, fabsf(v));
+        sum_s = fmaf(v, v, sum_s);
     }
-    if (flags) atomicOr(a.status, flags);
-    if (!a.norms) return;
-    sum_r = block_sum(sum_r);
-    max_s = block_max(max_s);
-    sum_s = block_sum(sum_s);
-    double *part = a.partials + kPartialsOffset;
-    if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = sum_r;
-        part[3 * blockIdx.x + 1] = max_s;
-        part[3 * blockIdx.x + 2] = sum_s;
-    }
-    if (last_block(counter_slot(a.partials, 6))) {
-        const double r2 = block_sum_array(part, gridDim.x, 3);
-        const double mx = block_max_array(part + 1, gridDim.x, 3);
-        const double s2 = block_sum_array(part + 2, gridDim.x, 3);
-        if (threadIdx.x == 0) {
-            a.norms[0] = sqrt(r2);
-            a.norms[1] = mx;
-            a.norms[2] = sqrt(s2);
-            if (!isfinite(r2) || !isfinite(s2)) atomicOr(a.status, DPF_ERR_NONFINITE);
-        }
-    }
+    return mx;
 }
 
-__global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const float *P, const double *units,
-                                                            const double *r, double *scaled, double *norms,
-                                                            double *partials) {
-    double sum_r = 0.0, max_s = 0.0, sum_s = 0.0;
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-        double rr[6];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            rr[c] = r[6 * s + c];
-            sum_r += rr[c] * rr[c];
-        }
-        const float *Ps = P + 36 * s;
-#pragma unroll
-        for (int row = 0; row < 6; ++row) {
-            double v = 0.0;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) v += (double)Ps[6 * row + c] * rr[c];
-            v = v / units[6 * s + row];
-            if (scaled) scaled[6 * s + row] = v;
-            max_s = fmax(max_s, fabs(v));
-            sum_s += v * v;
-        }
-    }
-    if (!norms) return;
+__device__ __forceinline__ void finish_norms(double sum_r, double max_s, double sum_s, double *partials, int slot,
+                                             double *norms, int *status) {
     sum_r = block_sum(sum_r);
     max_s = block_max(max_s);
     sum_s = block_sum(sum_s);
@@ -352,7 +347,7 @@ __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const flo
         part[3 * blockIdx.x + 1] = max_s;
         part[3 * blockIdx.x + 2] = sum_s;
     }
-    if (last_block(counter_slot(partials, 7))) {
+    if (last_block(counter_slot(partials, slot))) {
         const double r2 = block_sum_array(part, gridDim.x, 3);
         const double mx = block_max_array(part + 1, gridDim.x, 3);
         const double s2 = block_sum_array(part + 2, gridDim.x, 3);
@@ -360,8 +355,56 @@ __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const flo
             norms[0] = sqrt(r2);
             norms[1] = mx;
             norms[2] = sqrt(s2);
+            if (status && (!isfinite(r2) || !isfinite(s2))) atomicOr(status, DPF_ERR_NONFINITE);
         }
     }
+}
+
+__global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
+    double sum_r = 0.0;
+    float max_s = 0.0f, sum_s = 0.0f;
+    int flags = 0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n; s += (int64_t)gridDim.x * blockDim.x) {
+        float hi[6], lo[6];
+        double r[6];
+        gather9c(a.ptr, a.inc, a.wrench, s, hi, lo);
+        const double *ys = a.y + 6 * s;
+        const float w0 = (float)ys[3], w1 = (float)ys[4], w2 = (float)ys[5];
+        if (sqrtf(w0 * w0 + w1 * w1 + w2 * w2) > 0.25f) flags |= DPF_ERR_ROTATION;
+        const bool fx = a.fixed[s] != 0;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const double acc = (double)hi[c] + (double)lo[c];
+            const double val = fma(a.mass[6 * s + c], ys[c], a.r0[6 * s + c]) - a.half_dt2 * acc;
+            r[c] = fx ? ys[c] : val;
+            a.residual[6 * s + c] = r[c];
+            sum_r = fma(r[c], r[c], sum_r);
+        }
+        if (a.P)
+            max_s = fmaxf(max_s, scale_site(a.P + 36 * s, a.units32 + 6 * s, r, a.scaled ? a.scaled + 6 * s : nullptr,
+                                            sum_s));
+    }
+    if (flags) atomicOr(a.status, flags);
+    if (!a.norms) return;
+    finish_norms(sum_r, max_s, sum_s, a.partials, 6, a.norms, a.status);
+}
+
+__global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const float *P, const float *units32,
+                                                            const double *r, double *scaled, double *norms,
+                                                            double *partials) {
+    double sum_r = 0.0;
+    float max_s = 0.0f, sum_s = 0.0f;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        double rr[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            rr[c] = r[6 * s + c];
+            sum_r = fma(rr[c], rr[c], sum_r);
+        }
+        max_s = fmaxf(max_s, scale_site(P + 36 * s, units32 + 6 * s, rr, scaled ? scaled + 6 * s : nullptr, sum_s));
+    }
+    if (!norms) return;
+    finish_norms(sum_r, max_s, sum_s, partials, 7, norms, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -370,7 +413,7 @@ __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const flo
 struct JvpArgs {
     int64_t m;
     BondData bd;
-    const double *y, *direction, *units;
+    const float *y, *d;
     float *wrench;
 };
 
@@ -378,16 +421,13 @@ __device__ __forceinline__ V3<Dual> dual3(V3<float> v, V3<float> d) {
     return {{v.x, d.x}, {v.y, d.y}, {v.z, d.z}};
 }
 
-__device__ __forceinline__ void load_dir(const double *d, const double *units, int s, V3<float> &u, V3<float> &w) {
-    const double *p = d + 6 * (int64_t)s;
-    if (units) {
-        const double *q = units + 6 * (int64_t)s;
-        u = {(float)(p[0] * q[0]), (float)(p[1] * q[1]), (float)(p[2] * q[2])};
-        w = {(float)(p[3] * q[3]), (float)(p[4] * q[4]), (float)(p[5] * q[5])};
-    } else {
-        u = f3(p);
-        w = f3(p + 3);
-    }
+// d32 = units * direction in float32 (one conversion per entry).
+__global__ void __launch_bounds__(kThreads) prepare_direction(int64_t count, const double *direction,
+                                                              const float *units32, float *d32) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= count) return;
+    const float d = (float)direction[e];
+    d32[e] = units32 ? d * units32[e] : d;
 }
 
 __global__ void __launch_bounds__(kThreads) jvp_bonds_mixed(JvpArgs a) {
@@ -397,8 +437,8 @@ __global__ void __launch_bounds__(kThreads) jvp_bonds_mixed(JvpArgs a) {
     V3<float> ui, wi, uj, wj, dui, dwi, duj, dwj;
     load_y(a.y, B.i, ui, wi);
     load_y(a.y, B.j, uj, wj);
-    load_dir(a.direction, a.units, B.i, dui, dwi);
-    load_dir(a.direction, a.units, B.j, duj, dwj);
+    load_y(a.d, B.i, dui, dwi);
+    load_y(a.d, B.j, duj, dwj);
     const BondIncrement<Dual> o =
         bond_increment<Dual>(B, dual3(ui, dui), dual3(wi, dwi), dual3(uj, duj), dual3(wj, dwj));
     store9(a.wrench, b, der3(o.dF), der3(o.dTi), der3(o.dTj));
@@ -407,34 +447,31 @@ __global__ void __launch_bounds__(kThreads) jvp_bonds_mixed(JvpArgs a) {
 struct JvpSiteArgs {
     int64_t n;
     const int32_t *ptr, *inc;
-    const float *wrench;
-    const double *direction, *units, *mass;
-    const float *P;
+    const float *wrench, *d, *mass32, *P, *units32;
     const uint8_t *fixed;
-    double half_dt2;
+    float half_dt2;
     double *out;
 };
 
 __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= a.n) return;
-    double acc[6], r[6];
-    gather9(a.ptr, a.inc, a.wrench, s, acc);
+    float acc[6], r[6];
+    gather9f(a.ptr, a.inc, a.wrench, s, acc);
     const bool fx = a.fixed[s] != 0;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-        double d = a.direction[6 * s + c];
-        if (a.units) d *= a.units[6 * s + c];
-        r[c] = fx ? d : a.mass[6 * s + c] * d - a.half_dt2 * acc[c];
+        const float d = a.d[6 * s + c];
+        r[c] = fx ? d : fmaf(a.mass32[6 * s + c], d, -a.half_dt2 * acc[c]);
     }
     if (a.P) {
-        double o[6];
+        float o[6];
         matvec6f(a.P + 36 * s, r, o);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = o[c] / a.units[6 * s + c];
+        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)(o[c] / a.units32[6 * s + c]);
     } else {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = r[c];
+        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)r[c];
     }
 }
 
@@ -566,10 +603,11 @@ struct ScalingArgs {
     int64_t n;
     const int32_t *ptr, *inc;
     BondData bd;
-    const double *mass, *radii;
+    const float *mass32;
+    const double *radii;
     const uint8_t *fixed;
     float alpha;
-    float *block, *P;
+    float *block, *P, *units32;
     double *units;
 };
 
@@ -593,7 +631,7 @@ __global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
     for (int p = 0; p < 6; ++p)
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-            const float val = (p == q ? (float)a.mass[6 * s + p] : 0.0f) + a.alpha * D[6 * p + q];
+            const float val = (p == q ? a.mass32[6 * s + p] : 0.0f) + a.alpha * D[6 * p + q];
             D[6 * p + q] = fx ? (p == q ? 1.0f : 0.0f) : val;
         }
     if (a.block) {
@@ -605,7 +643,10 @@ __global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
     for (int c = 0; c < 36; ++c) a.P[36 * s + c] = D[c];
     const double r = fx ? 1.0 : a.radii[s];
 #pragma unroll
-    for (int c = 0; c < 6; ++c) a.units[6 * s + c] = c < 3 ? r : 1.0;
+    for (int c = 0; c < 6; ++c) {
+        a.units[6 * s + c] = c < 3 ? r : 1.0;
+        a.units32[6 * s + c] = c < 3 ? (float)r : 1.0f;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -616,7 +657,8 @@ struct PcgArgs {
     int64_t n, m;
     const int32_t *ptr, *inc;
     BondData bd;
-    const double *mass, *units, *vector;
+    const float *mass32, *units32;
+    const double *vector;
     const float *block, *P;
     const uint8_t *fixed;
     float alpha_op;
@@ -643,11 +685,11 @@ __device__ __forceinline__ void mv6(const float *P, const float x[6], float y[6]
 __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    double p = 0.0;
+    float pf = 0.0f;
     for (int64_t s = tid; s < a.n; s += stride) {
         float u[6], rr[6], zz[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) u[c] = (float)(a.units[6 * s + c] * a.vector[6 * s + c]);
+        for (int c = 0; c < 6; ++c) u[c] = a.units32[6 * s + c] * (float)a.vector[6 * s + c];
         if (a.fixed[s]) {
 #pragma unroll
             for (int c = 0; c < 6; ++c) rr[c] = 0.0f;
@@ -660,10 +702,10 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
             a.x[6 * s + c] = 0.0f;
             a.r[6 * s + c] = rr[c];
             a.d[6 * s + c] = zz[c];
-            p += (double)rr[c] * (double)zz[c];
+            pf = fmaf(rr[c], zz[c], pf);
         }
     }
-    p = block_sum(p);
+    double p = block_sum((double)pf);
     if (threadIdx.x == 0) a.part_b[blockIdx.x] = p;
     if (!grid_barrier(a.barrier, a.status)) return;
     double rz = block_sum_array(a.part_b, gridDim.x);
@@ -676,42 +718,24 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
     for (; it < a.max_it; ++it) {
         for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_f32(a.bd, a.d, a.wrench, b);
         if (!grid_barrier(a.barrier, a.status)) return;
-        p = 0.0;
+        pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) {
             float acc[6];
-#pragma unroll
-            for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
-            const int e1 = a.ptr[s + 1];
-            for (int e = a.ptr[s]; e < e1; ++e) {
-                const int v = a.inc[e];
-                if (v >= 0) {
-                    const float *q = a.wrench + 9 * (int64_t)v;
-#pragma unroll
-                    for (int c = 0; c < 6; ++c) acc[c] += q[c];
-                } else {
-                    const float *q = a.wrench + 9 * (int64_t)(~v);
-                    acc[0] -= q[0];
-                    acc[1] -= q[1];
-                    acc[2] -= q[2];
-                    acc[3] += q[6];
-                    acc[4] += q[7];
-                    acc[5] += q[8];
-                }
-            }
+            gather9f(a.ptr, a.inc, a.wrench, s, acc);
             const bool fx = a.fixed[s] != 0;
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 const float dv = a.d[6 * s + c];
-                const float v = fx ? dv : (float)a.mass[6 * s + c] * dv + a.alpha_op * acc[c];
+                const float v = fx ? dv : fmaf(a.mass32[6 * s + c], dv, a.alpha_op * acc[c]);
                 a.ad[6 * s + c] = v;
-                p += (double)dv * (double)v;
+                pf = fmaf(dv, v, pf);
             }
         }
-        p = block_sum(p);
+        p = block_sum((double)pf);
         if (threadIdx.x == 0) a.part_a[blockIdx.x] = p;
         if (!grid_barrier(a.barrier, a.status)) return;
         const float alpha = (float)(rz / block_sum_array(a.part_a, gridDim.x));
-        p = 0.0;
+        pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) {
             float rr[6], zz[6];
 #pragma unroll
@@ -724,10 +748,10 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
                 a.z[6 * s + c] = zz[c];
-                p += (double)rr[c] * (double)zz[c];
+                pf = fmaf(rr[c], zz[c], pf);
             }
         }
-        p = block_sum(p);
+        p = block_sum((double)pf);
         if (threadIdx.x == 0) a.part_b[blockIdx.x] = p;
         if (!grid_barrier(a.barrier, a.status)) return;
         const double following = block_sum_array(a.part_b, gridDim.x);
@@ -737,7 +761,7 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
         rz = following;
         if (!grid_barrier(a.barrier, a.status)) return;
     }
-    for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = (double)a.x[e] / a.units[e];
+    for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = (double)(a.x[e] / a.units32[e]);
     if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
 }
 
@@ -749,6 +773,7 @@ struct CommitArgs {
     int64_t m;
     BondData bd;
     dpf_history h;
+    const float *y32;
     const double *y;
     double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
 };
@@ -758,8 +783,8 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     if (b >= a.m) return;
     const Bond B = load_bond(a.bd.rec, b);
     V3<float> ui, wi, uj, wj;
-    load_y(a.y, B.i, ui, wi);
-    load_y(a.y, B.j, uj, wj);
+    load_y(a.y32, B.i, ui, wi);
+    load_y(a.y32, B.j, uj, wj);
     const BondIncrement<float> o = bond_increment<float>(B, ui, wi, uj, wj);
     a.fn_end[b] = a.h.fn[b] + (double)(B.kn * value(o.dn));
     a.mt_end[b] = a.h.mt[b] + (double)(B.kt * value(o.tw));
@@ -825,59 +850,61 @@ int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_histor
     return DPF_OK;
 }
 
-int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const double *mass,
+int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const float *y32, const double *mass,
                        const uint8_t *fixed, double dt, const double *r0, int want_tangent, const float *preconditioner,
-                       const double *units, double *residual, double *scaled, double *norms, float *wrench,
+                       const float *units32, double *residual, double *scaled, double *norms, float *wrench,
                        double *partials, int *status, void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !y || !mass || !fixed || !r0 || !residual || !status ||
-        (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units))
+    if (!mixed_graph_ok(g) || !bond_data || !y || !y32 || !mass || !fixed || !r0 || !residual || !status ||
+        (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units32))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
-        ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y, want_tangent, wrench, status};
+        ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, want_tangent, wrench, status};
         residual_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     ResidualSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, y, mass, r0, fixed, 0.5 * dt * dt,
-                       preconditioner, units, residual, scaled, norms, partials, status};
+                       preconditioner, units32, residual, scaled, norms, partials, status};
     residual_sites<<<reduce_grid(g->n_sites), kThreads, 0, st>>>(s);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
 
-int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const double *mass, const uint8_t *fixed,
+int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32, const uint8_t *fixed,
                       const double *radii, double dt, float *block, float *preconditioner, double *units,
-                      void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !mass || !fixed || !radii || !preconditioner || !units)
+                      float *units32, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !mass32 || !fixed || !radii || !preconditioner || !units || !units32)
         return DPF_ERR_ARGUMENT;
-    ScalingArgs a{g->n_sites, g->inc_ptr, g->inc_bond, split_bond_data(bond_data, g->n_bonds), mass, radii, fixed,
-                  (float)(0.25 * dt * dt), block, preconditioner, units};
+    ScalingArgs a{g->n_sites, g->inc_ptr, g->inc_bond, split_bond_data(bond_data, g->n_bonds), mass32, radii, fixed,
+                  (float)(0.25 * dt * dt), block, preconditioner, units32, units};
     scaling_sites_f32<<<blocks_for(g->n_sites, 128), 128, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
 
-int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const double *units,
+int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const float *units32,
                              const double *residual, double *scaled, double *norms, double *partials, void *stream) {
-    if (n_sites <= 0 || !preconditioner || !units || !residual || (norms && !partials)) return DPF_ERR_ARGUMENT;
-    scale_sites_f32<<<reduce_grid(n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units,
+    if (n_sites <= 0 || !preconditioner || !units32 || !residual || (norms && !partials)) return DPF_ERR_ARGUMENT;
+    scale_sites_f32<<<reduce_grid(n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units32,
                                                                                   residual, scaled, norms, partials);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
 
-int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const double *y, const double *direction,
-                              const double *mass, const uint8_t *fixed, double dt, const double *units,
-                              const float *preconditioner, double *out, float *wrench, void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !y || !direction || !mass || !fixed || !out || (g->n_bonds && !wrench) ||
-        (preconditioner && !units))
+int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float *y32, const double *direction,
+                              const float *mass32, const uint8_t *fixed, double dt, const float *units32,
+                              const float *preconditioner, double *out, float *d32, float *wrench, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !y32 || !direction || !mass32 || !fixed || !out || !d32 ||
+        (g->n_bonds && !wrench) || (preconditioner && !units32))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n6 = 6 * g->n_sites;
+    prepare_direction<<<blocks_for(n6, kThreads), kThreads, 0, st>>>(n6, direction, units32, d32);
     if (g->n_bonds) {
-        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y, direction, units, wrench};
+        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, d32, wrench};
         jvp_bonds_mixed<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
-    JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, direction, units, mass, preconditioner, fixed,
-                  0.5 * dt * dt, out};
+    JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, d32, mass32, preconditioner, units32, fixed,
+                  (float)(0.5 * dt * dt), out};
     jvp_sites_mixed<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(s);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
@@ -919,12 +946,12 @@ static MixedDeviceInfo &mixed_info() {
     return d;
 }
 
-int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *mass, const uint8_t *fixed,
-                           const float *block, const float *preconditioner, const double *units,
+int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *mass32, const uint8_t *fixed,
+                           const float *block, const float *preconditioner, const float *units32,
                            const double *vector, double dt, double tolerance, int max_iterations, double *out,
                            int *iterations, float *wrench, float *workspace, unsigned *barrier, int *status,
                            void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !mass || !fixed || !block || !preconditioner || !units || !vector ||
+    if (!mixed_graph_ok(g) || !bond_data || !mass32 || !fixed || !block || !preconditioner || !units32 || !vector ||
         !out || !iterations || !workspace || !barrier || !status || max_iterations < 1 || (g->n_bonds && !wrench))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
@@ -941,8 +968,8 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *m
     a.ptr = g->inc_ptr;
     a.inc = g->inc_bond;
     a.bd = split_bond_data(bond_data, g->n_bonds);
-    a.mass = mass;
-    a.units = units;
+    a.mass32 = mass32;
+    a.units32 = units32;
     a.vector = vector;
     a.block = block;
     a.P = preconditioner;
@@ -970,16 +997,17 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *m
     return DPF_OK;
 }
 
-int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y, double *x_end,
-                     double *normal_end, double *offset_end, double *fn_end, double *fs_end, double *mt_end,
-                     double *mb_end, void *stream) {
+int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y, const float *y32,
+                     double *x_end, double *normal_end, double *offset_end, double *fn_end, double *fs_end,
+                     double *mt_end, double *mb_end, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !h || !h->x || !h->fn || !h->fs || !h->mt || !h->mb || !h->offset ||
-        !y || !x_end || ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
+        !y || !y32 || !x_end ||
+        ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
-        CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y, normal_end, offset_end, fs_end, mb_end,
-                     fn_end, mt_end};
+        CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y32, y, normal_end, offset_end, fs_end,
+                     mb_end, fn_end, mt_end};
         commit_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     commit_sites<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, h->x, y, x_end);

@@ -786,25 +786,39 @@ class MixedNewtonBonds(NewtonBonds):
     """Mixed-precision form of ``NewtonBonds.step``: the same equations, control
     flow, tolerances and ``info`` as the reference solver
     (``experiments/bonded_dem_newton.py:132-201``) with float32 bond sweeps
-    (residual increment, JVP, K q, 6x6 blocks, elastic PCG) and float64
-    reductions, float64 Krylov vectors and a float64-accurate residual:
-    r(y) = r0 + M y - dt^2/2 sum of float32 bond increments, r0 computed in
-    float64 once per step.  Every other method is the float64 one it inherits.
+    (residual increment, JVP, K q, 6x6 blocks, elastic PCG), float64
+    reductions and Krylov vectors, and a float64-accurate residual:
+    r(y) = r0 + M y - dt^2/2 sum of float32 bond increments, with r0 computed
+    in float64 once per step and site sums compensated.  The accepted line-search
+    evaluation (with its tangent) is reused as the next iteration's residual,
+    as the reference's next trial at the same increment gives the same values.
+    Every other method is the float64 one it inherits.
     """
 
     def __init__(self, *args, **kwargs):
         super().__init__(*args, **kwargs)
         lib, n, m = self._lib, self.n_sites, self.n_bonds
         dev = self.device
-        self._bond_data = torch.empty(max(4, lib.dpf_mixed_bond_floats(m)), dtype=torch.float32, device=dev)
-        self._wrench32 = torch.empty(max(1, 9*m), dtype=torch.float32, device=dev)
+        f32 = torch.float32
+        self._bond_data = torch.empty(max(4, lib.dpf_mixed_bond_floats(m)), dtype=f32, device=dev)
+        self._wrench32 = torch.empty(max(1, 9*m), dtype=f32, device=dev)
         self._r0 = torch.empty((n, 6), dtype=F64, device=dev)
-        self._block32 = torch.empty((n, 6, 6), dtype=torch.float32, device=dev)
-        self._p32 = torch.empty((n, 6, 6), dtype=torch.float32, device=dev)
+        self._block32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
+        self._p32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
         self._units = torch.empty((n, 6), dtype=F64, device=dev)
-        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n), dtype=torch.float32, device=dev)
+        self._units32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._mass32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._y32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._d32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n), dtype=f32, device=dev)
+        self._call('dpf_to_float', 6*n, self.mass.data_ptr(), self._mass32.data_ptr(), self._stream())
+        self._cached = None
+
+    def _to_y32(self, y):
+        self._call('dpf_to_float', 6*self.n_sites, y.data_ptr(), self._y32.data_ptr(), self._stream())
 
     def _step_begin(self, dt, external):
+        self._cached = None
         self._status.zero_()
         self._timed('setup', lambda: self._call(
             'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
@@ -817,29 +831,31 @@ class MixedNewtonBonds(NewtonBonds):
             raise guard_error(status)
         return max(a, .5*dt*dt*l, 1e-30)
 
-    def _mixed_residual(self, y, dt, want_tangent, scaled=None, norms=True):
+    def _mixed_residual(self, y, dt, want_tangent, use_p, scaled=None):
         r = torch.empty_like(y)
+        self._to_y32(y)
         self._status.zero_()
-        use_p = not want_tangent
         self._timed('residual', lambda: self._call(
             'dpf_mixed_residual', ctypes.byref(self._graph), self._bond_data.data_ptr(), y.data_ptr(),
-            self.mass.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(), int(want_tangent),
-            self._p32.data_ptr() if use_p else None, self._units.data_ptr() if use_p else None, r.data_ptr(),
-            _addr(scaled) if use_p else None, self._scalars.data_ptr() if (use_p and norms) else None,
+            self._y32.data_ptr(), self.mass.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(),
+            int(want_tangent), self._p32.data_ptr() if use_p else None, self._units32.data_ptr() if use_p else None,
+            r.data_ptr(), _addr(scaled) if use_p else None, self._scalars.data_ptr() if use_p else None,
             self._wrench32.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(), self._stream()))
         return r
 
     def _iteration_residual(self, y, dt, external):
-        r = self._mixed_residual(y, dt, want_tangent=True)
+        reuse = self._cached is not None and self._cached[0] is y
+        r = self._cached[1] if reuse else self._mixed_residual(y, dt, want_tangent=True, use_p=False)
+        self._cached = None
         self._timed('scaling', lambda: self._call(
-            'dpf_mixed_scaling', ctypes.byref(self._graph), self._bond_data.data_ptr(), self.mass.data_ptr(),
+            'dpf_mixed_scaling', ctypes.byref(self._graph), self._bond_data.data_ptr(), self._mass32.data_ptr(),
             self.fixed.data_ptr(), self.radii.data_ptr(), dt, self._block32.data_ptr(), self._p32.data_ptr(),
-            self._units.data_ptr(), self._stream()))
+            self._units.data_ptr(), self._units32.data_ptr(), self._stream()))
         scaled = torch.empty_like(r)
-        self._call('dpf_mixed_scale_residual', self.n_sites, self._p32.data_ptr(), self._units.data_ptr(),
+        self._call('dpf_mixed_scale_residual', self.n_sites, self._p32.data_ptr(), self._units32.data_ptr(),
                    r.data_ptr(), scaled.data_ptr(), self._scalars.data_ptr(), self._partials.data_ptr(),
                    self._stream())
-        norms, status = self._fetch(3, status=True)
+        norms, status = self._fetch(3, status=not reuse)
         if status:
             raise guard_error(status)
         self.units = self._units
@@ -850,9 +866,10 @@ class MixedNewtonBonds(NewtonBonds):
             v = self._vec(v)
             out = torch.empty_like(v)
             self._timed('jvp', lambda: self._call(
-                'dpf_mixed_jacobian_vector', ctypes.byref(self._graph), self._bond_data.data_ptr(), y.data_ptr(),
-                v.data_ptr(), self.mass.data_ptr(), self.fixed.data_ptr(), dt, self._units.data_ptr(),
-                self._p32.data_ptr(), out.data_ptr(), self._wrench32.data_ptr(), self._stream()))
+                'dpf_mixed_jacobian_vector', ctypes.byref(self._graph), self._bond_data.data_ptr(),
+                self._y32.data_ptr(), v.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), dt,
+                self._units32.data_ptr(), self._p32.data_ptr(), out.data_ptr(), self._d32.data_ptr(),
+                self._wrench32.data_ptr(), self._stream()))
             return out
         return operator
 
@@ -862,29 +879,34 @@ class MixedNewtonBonds(NewtonBonds):
             out = torch.empty_like(vector)
             self._timed('pcg', lambda: self._call(
                 'dpf_mixed_precondition', ctypes.byref(self._graph), self._bond_data.data_ptr(),
-                self.mass.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p32.data_ptr(),
-                self._units.data_ptr(), vector.data_ptr(), dt, tolerance, max_iterations, out.data_ptr(),
+                self._mass32.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p32.data_ptr(),
+                self._units32.data_ptr(), vector.data_ptr(), dt, tolerance, max_iterations, out.data_ptr(),
                 self._inner.data_ptr(), self._wrench32.data_ptr(), self._mixed_workspace.data_ptr(),
                 self._barrier.data_ptr(), self._status.data_ptr(), self._stream()))
             return out
         return precondition
 
     def _line_merit(self, candidate, dt, external):
-        self._mixed_residual(candidate, dt, want_tangent=False)
+        # The candidate's tangent overwrites the iterate's (FGMRES is done with it);
+        # an accepted candidate's residual and tangent start the next iteration.
+        r = self._mixed_residual(candidate, dt, want_tangent=True, use_p=True)
         (_, _, value), status = self._fetch(3, status=True)
+        self._cached = (candidate, r)
         return value, status
 
     def _accept(self, y, dt):
         m, n = self.n_bonds, self.n_sites
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
+        self._to_y32(y)
         self._timed('commit', lambda: self._call(
             'dpf_mixed_commit', ctypes.byref(self._graph), self._bond_data.data_ptr(),
-            ctypes.byref(self._history_struct()), y.data_ptr(), state['x'].data_ptr(), state['normal'].data_ptr(),
-            state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(), state['mt'].data_ptr(),
-            state['mb'].data_ptr(), self._stream()))
+            ctypes.byref(self._history_struct()), y.data_ptr(), self._y32.data_ptr(), state['x'].data_ptr(),
+            state['normal'].data_ptr(), state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(),
+            state['mt'].data_ptr(), state['mb'].data_ptr(), self._stream()))
         rotation = self._vec(self.rotation).clone()
         self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(), rotation.data_ptr(),
                    self._stream())
         self.commit(state)
         self.v, self.rotation = self._v, rotation
+        self._cached = None

@@ -256,8 +256,12 @@ int dpf_masked_scale(int64_t n_sites, const double *a, const double *units, cons
  * setup per step computes r0 = -dt M v - dt^2/2 (loads(x) + external); for an
  * increment y the residual is r0 + M y - dt^2/2 sum of per-bond float32
  * increments f_mid(y) - f_mid(0), evaluated from small quantities only and
- * summed per site in float64.  bond_data: dpf_mixed_bond_floats(M) floats
- * (float4 records + float32 tangent, 16-byte aligned); wrench: 9 M floats. */
+ * summed per site in compensated float32 (about float64 accuracy).
+ * bond_data: dpf_mixed_bond_floats(M) floats (float4 records + float32
+ * tangent, 16-byte aligned); wrench: 9 M floats.  The *32 arguments are
+ * float32 copies of the float64 arrays of the same name (y32 of the increment,
+ * mass32 of the (N, 6) mass, units32 of the units written by
+ * dpf_mixed_scaling); d32 is a float32 (N, 6) scratch. */
 int64_t dpf_mixed_bond_floats(int64_t n_bonds);
 
 /* Float workspace of dpf_mixed_precondition for N sites. */
@@ -277,34 +281,34 @@ int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_histor
  * want_tangent stores the midpoint tangent for dpf_mixed_scaling and K q;
  * preconditioner (float32 (N, 6, 6)) / units / scaled / norms as in dpf_residual.
  * Replaces NewtonBonds.residual + scale_residual (experiments/bonded_dem_newton.py:83-86, 104-105). */
-int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const double *mass,
-                       const uint8_t *fixed, double dt, const double *r0, int want_tangent,
-                       const float *preconditioner, const double *units, double *residual,
-                       double *scaled, double *norms, float *wrench, double *partials, int *status,
-                       void *stream);
+int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const float *y32,
+                       const double *mass, const uint8_t *fixed, double dt, const double *r0,
+                       int want_tangent, const float *preconditioner, const float *units32,
+                       double *residual, double *scaled, double *norms, float *wrench,
+                       double *partials, int *status, void *stream);
 
 /* Blocks and scaling from the stored float32 tangent: block (float32 (N,6,6),
  * may be NULL), preconditioner = block^-1 (float32, Jacobi-scaled Cholesky),
  * units (float64 (N, 6)).
  * Replaces NewtonBonds.prepare_scaling (experiments/bonded_dem_newton.py:94-102). */
-int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const double *mass, const uint8_t *fixed,
+int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32, const uint8_t *fixed,
                       const double *radii, double dt, float *block, float *preconditioner,
-                      double *units, void *stream);
+                      double *units, float *units32, void *stream);
 
 /* Scaled residual with the float32 block inverse: s = P r / units and
  * norms = [|r|, max|s|, |s|] (float64).
  * Replaces NewtonBonds.scale_residual (experiments/bonded_dem_newton.py:104-105). */
-int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const double *units,
+int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const float *units32,
                              const double *residual, double *scaled, double *norms, double *partials,
                              void *stream);
 
 /* J d, the forward-mode derivative of the float32 residual increment; the
  * same options as dpf_jacobian_vector (units, float32 preconditioner).
  * Replaces NewtonBonds.jacobian_vector (experiments/bonded_dem_newton.py:88-92). */
-int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const double *y,
-                              const double *direction, const double *mass, const uint8_t *fixed,
-                              double dt, const double *units, const float *preconditioner,
-                              double *out, float *wrench, void *stream);
+int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float *y32,
+                              const double *direction, const float *mass32, const uint8_t *fixed,
+                              double dt, const float *units32, const float *preconditioner,
+                              double *out, float *d32, float *wrench, void *stream);
 
 /* K q in float32 from the stored tangent; q float32 (N, 6), out float64 (N, 6).
  * Replaces LinearBondsGPU.stiffness (experiments/bonded_dem_linear_gpu.py:42-52). */
@@ -318,9 +322,9 @@ int dpf_to_float(int64_t count, const double *a, float *out, void *stream);
  * iteration accounting as dpf_elastic_precondition); workspace:
  * dpf_mixed_workspace_floats(N) floats; block/preconditioner float32.
  * Replaces NewtonBonds.elastic_precondition (experiments/bonded_dem_newton.py:107-130). */
-int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *mass,
+int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *mass32,
                            const uint8_t *fixed, const float *block, const float *preconditioner,
-                           const double *units, const double *vector, double dt, double tolerance,
+                           const float *units32, const double *vector, double dt, double tolerance,
                            int max_iterations, double *out, int *iterations, float *wrench,
                            float *workspace, unsigned *barrier, int *status, void *stream);
 
@@ -329,8 +333,8 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const double *m
  * Replaces FiniteBondsGPU.trial's end-of-step outputs and commit
  * (experiments/bonded_dem_finite_gpu.py:102-120). */
 int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y,
-                     double *x_end, double *normal_end, double *offset_end, double *fn_end,
-                     double *fs_end, double *mt_end, double *mb_end, void *stream);
+                     const float *y32, double *x_end, double *normal_end, double *offset_end,
+                     double *fn_end, double *fs_end, double *mt_end, double *mb_end, void *stream);
 
 #ifdef __cplusplus
 }
