@@ -456,13 +456,16 @@ struct JvpSiteArgs {
 __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= a.n) return;
-    float acc[6], r[6];
-    gather9f(a.ptr, a.inc, a.wrench, s, acc);
+    float hi[6], lo[6], r[6];
+    gather9c(a.ptr, a.inc, a.wrench, s, hi, lo);
     const bool fx = a.fixed[s] != 0;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
-        const float d = a.d[6 * s + c];
-        r[c] = fx ? d : fmaf(a.mass32[6 * s + c], d, -a.half_dt2 * acc[c]);
+        // m d - h (hi + lo) with the rounding errors of both products recovered by FMA
+        const float d = a.d[6 * s + c], m = a.mass32[6 * s + c];
+        const float p = m * d, q = a.half_dt2 * hi[c];
+        const float e = fmaf(m, d, -p) - fmaf(a.half_dt2, hi[c], -q) - a.half_dt2 * lo[c];
+        r[c] = fx ? d : (p - q) + e;
     }
     if (a.P) {
         float o[6];
