@@ -793,7 +793,20 @@ class MixedNewtonBonds(NewtonBonds):
     evaluation (with its tangent) is reused as the next iteration's residual,
     as the reference's next trial at the same increment gives the same values.
     Every other method is the float64 one it inherits.
+
+    The JVP is a float32 operator (relative accuracy ~1e-7), so FGMRES cannot
+    certify linear tolerances below ``min_linear_tolerance`` (1e-6): smaller
+    requests are raised to it.  The float64-accurate nonlinear residual still
+    decides convergence of the step.
     """
+
+    min_linear_tolerance = 1e-6
+
+    def step(self, dt, external, tolerance=2e-7, max_iterations=12, *, pose_tolerance=2e-6, backend='fgmres',
+             linear_tolerance=1e-6, preconditioning='elastic'):
+        return super().step(dt, external, tolerance, max_iterations, pose_tolerance=pose_tolerance, backend=backend,
+                            linear_tolerance=max(linear_tolerance, self.min_linear_tolerance),
+                            preconditioning=preconditioning)
 
     def __init__(self, *args, **kwargs):
         super().__init__(*args, **kwargs)
