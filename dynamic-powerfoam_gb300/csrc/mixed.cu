@@ -116,6 +116,45 @@ __device__ __forceinline__ void gather9f(const int32_t *__restrict__ ptr, const 
     }
 }
 
+// Segmented site sum by groups of kGroupJ lanes (xor-shuffle reduction),
+// compensated: used by the residual and JVP site passes.
+constexpr int kGroupJ = 4;
+
+__device__ __forceinline__ void group_gather9c_j(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                                 const float *__restrict__ w, int64_t s, bool valid, int lane,
+                                                 float hi[6], float lo[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) hi[c] = lo[c] = 0.0f;
+    if (valid) {
+        const int e1 = ptr[s + 1];
+        for (int e = ptr[s] + lane; e < e1; e += kGroupJ) {
+            const int v = inc[e];
+            if (v >= 0) {
+                const float *p = w + 9 * (int64_t)v;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], p[c]);
+            } else {
+                const float *p = w + 9 * (int64_t)(~v);
+                two_sum(hi[0], lo[0], -p[0]);
+                two_sum(hi[1], lo[1], -p[1]);
+                two_sum(hi[2], lo[2], -p[2]);
+                two_sum(hi[3], lo[3], p[6]);
+                two_sum(hi[4], lo[4], p[7]);
+                two_sum(hi[5], lo[5], p[8]);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < kGroupJ; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float h = __shfl_xor_sync(0xffffffffu, hi[c], o);
+            const float l = __shfl_xor_sync(0xffffffffu, lo[c], o);
+            two_sum(hi[c], lo[c], h);
+            lo[c] += l;
+        }
+}
+
 // Site sum of a float32 bond wrench in float64.
 __device__ __forceinline__ void gather9(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
                                         const float *__restrict__ w, int64_t s, double acc[6]) {
@@ -364,10 +403,15 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
     double sum_r = 0.0;
     float max_s = 0.0f, sum_s = 0.0f;
     int flags = 0;
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < a.n; s += (int64_t)gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & (kGroupJ - 1);
+    const int64_t groups = (int64_t)gridDim.x * blockDim.x / kGroupJ;
+    const int64_t n_padded = (a.n + groups - 1) / groups * groups;
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroupJ; s < n_padded; s += groups) {
+        const bool valid = s < a.n;
         float hi[6], lo[6];
+        group_gather9c_j(a.ptr, a.inc, a.wrench, s, valid, lane, hi, lo);
+        if (!valid || lane != 0) continue;
         double r[6];
-        gather9c(a.ptr, a.inc, a.wrench, s, hi, lo);
         const double *ys = a.y + 6 * s;
         const float w0 = (float)ys[3], w1 = (float)ys[4], w2 = (float)ys[5];
         if (sqrtf(w0 * w0 + w1 * w1 + w2 * w2) > 0.25f) flags |= DPF_ERR_ROTATION;
@@ -454,10 +498,13 @@ struct JvpSiteArgs {
 };
 
 __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (s >= a.n) return;
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroupJ;
+    const int lane = threadIdx.x & (kGroupJ - 1);
+    const bool valid = g < a.n;
     float hi[6], lo[6], r[6];
-    gather9c(a.ptr, a.inc, a.wrench, s, hi, lo);
+    group_gather9c_j(a.ptr, a.inc, a.wrench, g, valid, lane, hi, lo);
+    if (!valid || lane != 0) return;
+    const int64_t s = g;
     const bool fx = a.fixed[s] != 0;
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -653,8 +700,94 @@ __global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
 }
 
 // ---------------------------------------------------------------------------
+
+
+__device__ __forceinline__ void mv6(const float *P, const float x[6], float y[6]) {
+#pragma unroll
+    for (int row = 0; row < 6; ++row) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v = fmaf(P[6 * row + c], x[c], v);
+        y[row] = v;
+    }
+}
+
+// Lanes per site in the segmented (lane-group) site gathers: each lane of a
+// group walks every kGroup-th incidence of the site, then the group reduces
+// with xor shuffles.  Groups never straddle a warp.
+constexpr int kGroup = 4;
+
+__device__ __forceinline__ void group_gather9f(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                               const float *__restrict__ w, int64_t s, bool valid, int lane,
+                                               float acc[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
+    if (valid) {
+        const int e1 = ptr[s + 1];
+        for (int e = ptr[s] + lane; e < e1; e += kGroup) {
+            const int v = inc[e];
+            if (v >= 0) {
+                const float *p = w + 9 * (int64_t)v;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) acc[c] += p[c];
+            } else {
+                const float *p = w + 9 * (int64_t)(~v);
+                acc[0] -= p[0];
+                acc[1] -= p[1];
+                acc[2] -= p[2];
+                acc[3] += p[6];
+                acc[4] += p[7];
+                acc[5] += p[8];
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < kGroup; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+}
+
+__device__ __forceinline__ void group_gather9c(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                               const float *__restrict__ w, int64_t s, bool valid, int lane,
+                                               float hi[6], float lo[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) hi[c] = lo[c] = 0.0f;
+    if (valid) {
+        const int e1 = ptr[s + 1];
+        for (int e = ptr[s] + lane; e < e1; e += kGroup) {
+            const int v = inc[e];
+            if (v >= 0) {
+                const float *p = w + 9 * (int64_t)v;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], p[c]);
+            } else {
+                const float *p = w + 9 * (int64_t)(~v);
+                two_sum(hi[0], lo[0], -p[0]);
+                two_sum(hi[1], lo[1], -p[1]);
+                two_sum(hi[2], lo[2], -p[2]);
+                two_sum(hi[3], lo[3], p[6]);
+                two_sum(hi[4], lo[4], p[7]);
+                two_sum(hi[5], lo[5], p[8]);
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < kGroup; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            const float h = __shfl_xor_sync(0xffffffffu, hi[c], o);
+            const float l = __shfl_xor_sync(0xffffffffu, lo[c], o);
+            two_sum(hi[c], lo[c], h);
+            lo[c] += l;
+        }
+}
+
 // Elastic PCG in float32 with float64 dot products, one cooperative launch
-// (experiments/bonded_dem_newton.py:107-130).
+// (experiments/bonded_dem_newton.py:107-130).  Three grid barriers per
+// iteration: the direction update d = z + beta d is folded into the next
+// iteration's bond pass (recomputed per endpoint) and site pass (stored).
+
+constexpr int kPcgThreads = 1024;
 
 struct PcgArgs {
     int64_t n, m;
@@ -675,17 +808,27 @@ struct PcgArgs {
     int *status;
 };
 
-__device__ __forceinline__ void mv6(const float *P, const float x[6], float y[6]) {
+__device__ __forceinline__ void stiffness_bond_dir(const BondData &bd, const float *z, const float *d, float beta,
+                                                   float *wrench, int64_t b) {
+    const float4 a = __ldg(bd.t0 + b), c = __ldg(bd.t1 + b), e = __ldg(bd.t2 + b), g = __ldg(bd.t3 + b);
+    const int i = __float_as_int(g.y), j = __float_as_int(g.z);
+    const V3<float> n = {a.x, a.y, a.z}, ri = {c.x, c.y, c.z}, rj = {e.x, e.y, e.z};
+    const float kn = a.w, ks = c.w, kb = e.w, kt = g.x;
+    float qi[6], qj[6];
 #pragma unroll
-    for (int row = 0; row < 6; ++row) {
-        float v = 0.0f;
-#pragma unroll
-        for (int c = 0; c < 6; ++c) v = fmaf(P[6 * row + c], x[c], v);
-        y[row] = v;
+    for (int k = 0; k < 6; ++k) {
+        qi[k] = fmaf(beta, d[6 * (int64_t)i + k], z[6 * (int64_t)i + k]);
+        qj[k] = fmaf(beta, d[6 * (int64_t)j + k], z[6 * (int64_t)j + k]);
     }
+    const V3<float> wi = {qi[3], qi[4], qi[5]}, wj = {qj[3], qj[4], qj[5]};
+    const V3<float> du = V3<float>{qj[0] - qi[0], qj[1] - qi[1], qj[2] - qi[2]} + cross(wj, rj) - cross(wi, ri);
+    const V3<float> dw = wj - wi;
+    const V3<float> f = ks * du + ((kn - ks) * dot(du, n)) * n;
+    const V3<float> mm = kb * dw + ((kt - kb) * dot(dw, n)) * n;
+    store9(wrench, b, -f, -cross(ri, f) - mm, cross(rj, f) + mm);
 }
 
-__global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
+__global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     float pf = 0.0f;
@@ -704,7 +847,8 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
         for (int c = 0; c < 6; ++c) {
             a.x[6 * s + c] = 0.0f;
             a.r[6 * s + c] = rr[c];
-            a.d[6 * s + c] = zz[c];
+            a.z[6 * s + c] = zz[c];
+            a.d[6 * s + c] = 0.0f;
             pf = fmaf(rr[c], zz[c], pf);
         }
     }
@@ -717,21 +861,31 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
         for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = 0.0;
         return;
     }
+    const int lane = threadIdx.x & (kGroup - 1);
+    const int64_t groups = stride / kGroup;
+    const int64_t n_padded = (a.n + groups - 1) / groups * groups;
+    float beta = 0.0f;
     int it = 0;
     for (; it < a.max_it; ++it) {
-        for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_f32(a.bd, a.d, a.wrench, b);
+        // K d_k with d_k = z_k + beta d_{k-1} formed per endpoint
+        for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_dir(a.bd, a.z, a.d, beta, a.wrench, b);
         if (!grid_barrier(a.barrier, a.status)) return;
+        // ad = (diag M + alpha K) d_k with identity rows on fixed sites; store d_k
         pf = 0.0f;
-        for (int64_t s = tid; s < a.n; s += stride) {
+        for (int64_t s = tid / kGroup; s < n_padded; s += groups) {
+            const bool valid = s < a.n;
             float acc[6];
-            gather9f(a.ptr, a.inc, a.wrench, s, acc);
-            const bool fx = a.fixed[s] != 0;
+            group_gather9f(a.ptr, a.inc, a.wrench, s, valid, lane, acc);
+            if (valid && lane == 0) {
+                const bool fx = a.fixed[s] != 0;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                const float dv = a.d[6 * s + c];
-                const float v = fx ? dv : fmaf(a.mass32[6 * s + c], dv, a.alpha_op * acc[c]);
-                a.ad[6 * s + c] = v;
-                pf = fmaf(dv, v, pf);
+                for (int c = 0; c < 6; ++c) {
+                    const float dv = fmaf(beta, a.d[6 * s + c], a.z[6 * s + c]);
+                    const float v = fx ? dv : fmaf(a.mass32[6 * s + c], dv, a.alpha_op * acc[c]);
+                    a.d[6 * s + c] = dv;
+                    a.ad[6 * s + c] = v;
+                    pf = fmaf(dv, v, pf);
+                }
             }
         }
         p = block_sum((double)pf);
@@ -743,8 +897,8 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
             float rr[6], zz[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
-                a.x[6 * s + c] += alpha * a.d[6 * s + c];
-                rr[c] = a.r[6 * s + c] - alpha * a.ad[6 * s + c];
+                a.x[6 * s + c] = fmaf(alpha, a.d[6 * s + c], a.x[6 * s + c]);
+                rr[c] = fmaf(-alpha, a.ad[6 * s + c], a.r[6 * s + c]);
                 a.r[6 * s + c] = rr[c];
             }
             mv6(a.P + 36 * s, rr, zz);
@@ -759,10 +913,8 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel_f32(PcgArgs a) {
         if (!grid_barrier(a.barrier, a.status)) return;
         const double following = block_sum_array(a.part_b, gridDim.x);
         if (it % 5 == 0 && following <= a.tol2 * initial) break;
-        const float beta = (float)(following / rz);
-        for (int64_t e = tid; e < 6 * a.n; e += stride) a.d[e] = a.z[e] + beta * a.d[e];
+        beta = (float)(following / rz);
         rz = following;
-        if (!grid_barrier(a.barrier, a.status)) return;
     }
     for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = (double)(a.x[e] / a.units32[e]);
     if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
@@ -867,7 +1019,7 @@ int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, co
     }
     ResidualSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, y, mass, r0, fixed, 0.5 * dt * dt,
                        preconditioner, units32, residual, scaled, norms, partials, status};
-    residual_sites<<<reduce_grid(g->n_sites), kThreads, 0, st>>>(s);
+    residual_sites<<<reduce_grid(kGroupJ * g->n_sites), kThreads, 0, st>>>(s);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
@@ -908,7 +1060,7 @@ int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float 
     }
     JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, d32, mass32, preconditioner, units32, fixed,
                   (float)(0.5 * dt * dt), out};
-    jvp_sites_mixed<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(s);
+    jvp_sites_mixed<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(s);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
@@ -944,7 +1096,7 @@ static MixedDeviceInfo &mixed_info() {
     MixedDeviceInfo &d = info[dev & 63];
     if (d.sms == 0) {
         cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, pcg_kernel_f32, kThreads, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&d.blocks_per_sm, pcg_kernel_f32, kPcgThreads, 0);
     }
     return d;
 }
@@ -960,7 +1112,7 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
     cudaStream_t st = (cudaStream_t)stream;
     MixedDeviceInfo &info = mixed_info();
     if (info.sms <= 0 || info.blocks_per_sm <= 0) return DPF_ERR_CUDA;
-    const int64_t want = blocks_for(g->n_sites > g->n_bonds ? g->n_sites : g->n_bonds, kThreads);
+    const int64_t want = blocks_for(g->n_sites > g->n_bonds ? g->n_sites : g->n_bonds, kPcgThreads);
     int64_t cap = (int64_t)info.sms * info.blocks_per_sm;
     if (cap > kMaxPcgBlocks) cap = kMaxPcgBlocks;
     const int grid = (int)(want < cap ? (want < 1 ? 1 : want) : cap);
@@ -995,7 +1147,7 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
     a.status = status;
     if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return DPF_ERR_CUDA;
     void *args[] = {&a};
-    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel_f32, grid, kThreads, args, 0, st) != cudaSuccess)
+    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel_f32, grid, kPcgThreads, args, 0, st) != cudaSuccess)
         return DPF_ERR_CUDA;
     return DPF_OK;
 }
