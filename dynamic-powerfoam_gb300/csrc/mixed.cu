@@ -786,6 +786,8 @@ __device__ __forceinline__ void group_gather9c(const int32_t *__restrict__ ptr, 
 // (experiments/bonded_dem_newton.py:107-130).  Three grid barriers per
 // iteration: the direction update d = z + beta d is folded into the next
 // iteration's bond pass (recomputed per endpoint) and site pass (stored).
+// Work vectors are 16-byte aligned per site: zd = [z, 0, 0, d, 0, 0] (64 B),
+// x, r, ad = [v, 0, 0] (32 B); the bond wrench is three float4 [F, T_i, T_j].
 
 constexpr int kPcgThreads = 1024;
 
@@ -802,35 +804,81 @@ struct PcgArgs {
     int max_it;
     double *out;
     int *iterations;
-    float *wrench, *x, *r, *z, *d, *ad;
+    float4 *wrench, *zd, *x, *r, *ad;
     double *part_a, *part_b;
     unsigned *barrier;
     int *status;
 };
 
-__device__ __forceinline__ void stiffness_bond_dir(const BondData &bd, const float *z, const float *d, float beta,
-                                                   float *wrench, int64_t b) {
+__device__ __forceinline__ void ld8(const float4 *p, float v[6]) {
+    const float4 a = p[0], b = p[1];
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y;
+}
+__device__ __forceinline__ void st8(float4 *p, const float v[6]) {
+    p[0] = make_float4(v[0], v[1], v[2], v[3]);
+    p[1] = make_float4(v[4], v[5], 0.0f, 0.0f);
+}
+
+// Direction at a site: z + beta d from the interleaved record.
+__device__ __forceinline__ void direction_at(const float4 *zd, int64_t s, float beta, float q[6]) {
+    const float4 *p = zd + 4 * s;
+    const float4 z0 = p[0], z1 = p[1], d0 = p[2], d1 = p[3];
+    q[0] = fmaf(beta, d0.x, z0.x); q[1] = fmaf(beta, d0.y, z0.y); q[2] = fmaf(beta, d0.z, z0.z);
+    q[3] = fmaf(beta, d0.w, z0.w); q[4] = fmaf(beta, d1.x, z1.x); q[5] = fmaf(beta, d1.y, z1.y);
+}
+
+__device__ __forceinline__ void stiffness_bond_dir(const BondData &bd, const float4 *zd, float beta, float4 *wrench,
+                                                   int64_t b) {
     const float4 a = __ldg(bd.t0 + b), c = __ldg(bd.t1 + b), e = __ldg(bd.t2 + b), g = __ldg(bd.t3 + b);
     const int i = __float_as_int(g.y), j = __float_as_int(g.z);
     const V3<float> n = {a.x, a.y, a.z}, ri = {c.x, c.y, c.z}, rj = {e.x, e.y, e.z};
     const float kn = a.w, ks = c.w, kb = e.w, kt = g.x;
     float qi[6], qj[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-        qi[k] = fmaf(beta, d[6 * (int64_t)i + k], z[6 * (int64_t)i + k]);
-        qj[k] = fmaf(beta, d[6 * (int64_t)j + k], z[6 * (int64_t)j + k]);
-    }
+    direction_at(zd, i, beta, qi);
+    direction_at(zd, j, beta, qj);
     const V3<float> wi = {qi[3], qi[4], qi[5]}, wj = {qj[3], qj[4], qj[5]};
     const V3<float> du = V3<float>{qj[0] - qi[0], qj[1] - qi[1], qj[2] - qi[2]} + cross(wj, rj) - cross(wi, ri);
     const V3<float> dw = wj - wi;
     const V3<float> f = ks * du + ((kn - ks) * dot(du, n)) * n;
     const V3<float> mm = kb * dw + ((kt - kb) * dot(dw, n)) * n;
-    store9(wrench, b, -f, -cross(ri, f) - mm, cross(rj, f) + mm);
+    const V3<float> ti = -cross(ri, f) - mm, tj = cross(rj, f) + mm;
+    float4 *w = wrench + 3 * b;
+    w[0] = make_float4(-f.x, -f.y, -f.z, 0.0f);
+    w[1] = make_float4(ti.x, ti.y, ti.z, 0.0f);
+    w[2] = make_float4(tj.x, tj.y, tj.z, 0.0f);
+}
+
+__device__ __forceinline__ void group_gather_w4(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                                const float4 *__restrict__ w, int64_t s, bool valid, int lane,
+                                                float acc[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
+    if (valid) {
+        const int e1 = ptr[s + 1];
+        for (int e = ptr[s] + lane; e < e1; e += kGroup) {
+            const int v = inc[e];
+            const int64_t b = v >= 0 ? v : ~v;
+            const float4 f = w[3 * b];
+            const float4 t = w[3 * b + (v >= 0 ? 1 : 2)];
+            const float sg = v >= 0 ? 1.0f : -1.0f;
+            acc[0] = fmaf(sg, f.x, acc[0]);
+            acc[1] = fmaf(sg, f.y, acc[1]);
+            acc[2] = fmaf(sg, f.z, acc[2]);
+            acc[3] += t.x;
+            acc[4] += t.y;
+            acc[5] += t.z;
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < kGroup; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
 }
 
 __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const float zero6[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
     float pf = 0.0f;
     for (int64_t s = tid; s < a.n; s += stride) {
         float u[6], rr[6], zz[6];
@@ -843,14 +891,12 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
             mv6(a.block + 36 * s, u, rr);
         }
         mv6(a.P + 36 * s, rr, zz);
+        st8(a.x + 2 * s, zero6);
+        st8(a.r + 2 * s, rr);
+        st8(a.zd + 4 * s, zz);
+        st8(a.zd + 4 * s + 2, zero6);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            a.x[6 * s + c] = 0.0f;
-            a.r[6 * s + c] = rr[c];
-            a.z[6 * s + c] = zz[c];
-            a.d[6 * s + c] = 0.0f;
-            pf = fmaf(rr[c], zz[c], pf);
-        }
+        for (int c = 0; c < 6; ++c) pf = fmaf(rr[c], zz[c], pf);
     }
     double p = block_sum((double)pf);
     if (threadIdx.x == 0) a.part_b[blockIdx.x] = p;
@@ -868,24 +914,27 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
     int it = 0;
     for (; it < a.max_it; ++it) {
         // K d_k with d_k = z_k + beta d_{k-1} formed per endpoint
-        for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_dir(a.bd, a.z, a.d, beta, a.wrench, b);
+#pragma unroll 2
+        for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_dir(a.bd, a.zd, beta, a.wrench, b);
         if (!grid_barrier(a.barrier, a.status)) return;
         // ad = (diag M + alpha K) d_k with identity rows on fixed sites; store d_k
         pf = 0.0f;
         for (int64_t s = tid / kGroup; s < n_padded; s += groups) {
             const bool valid = s < a.n;
             float acc[6];
-            group_gather9f(a.ptr, a.inc, a.wrench, s, valid, lane, acc);
+            group_gather_w4(a.ptr, a.inc, a.wrench, s, valid, lane, acc);
             if (valid && lane == 0) {
                 const bool fx = a.fixed[s] != 0;
+                float dv[6], v[6];
+                direction_at(a.zd, s, beta, dv);
 #pragma unroll
                 for (int c = 0; c < 6; ++c) {
-                    const float dv = fmaf(beta, a.d[6 * s + c], a.z[6 * s + c]);
-                    const float v = fx ? dv : fmaf(a.mass32[6 * s + c], dv, a.alpha_op * acc[c]);
-                    a.d[6 * s + c] = dv;
-                    a.ad[6 * s + c] = v;
-                    pf = fmaf(dv, v, pf);
+                    const float m = a.mass32[6 * s + c];
+                    v[c] = fx ? dv[c] : fmaf(m, dv[c], a.alpha_op * acc[c]);
+                    pf = fmaf(dv[c], v[c], pf);
                 }
+                st8(a.zd + 4 * s + 2, dv);
+                st8(a.ad + 2 * s, v);
             }
         }
         p = block_sum((double)pf);
@@ -894,19 +943,22 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
         const float alpha = (float)(rz / block_sum_array(a.part_a, gridDim.x));
         pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) {
-            float rr[6], zz[6];
+            float xv[6], rv[6], dv[6], av[6], zz[6];
+            ld8(a.x + 2 * s, xv);
+            ld8(a.r + 2 * s, rv);
+            ld8(a.zd + 4 * s + 2, dv);
+            ld8(a.ad + 2 * s, av);
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
-                a.x[6 * s + c] = fmaf(alpha, a.d[6 * s + c], a.x[6 * s + c]);
-                rr[c] = fmaf(-alpha, a.ad[6 * s + c], a.r[6 * s + c]);
-                a.r[6 * s + c] = rr[c];
+                xv[c] = fmaf(alpha, dv[c], xv[c]);
+                rv[c] = fmaf(-alpha, av[c], rv[c]);
             }
-            mv6(a.P + 36 * s, rr, zz);
+            mv6(a.P + 36 * s, rv, zz);
+            st8(a.x + 2 * s, xv);
+            st8(a.r + 2 * s, rv);
+            st8(a.zd + 4 * s, zz);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                a.z[6 * s + c] = zz[c];
-                pf = fmaf(rr[c], zz[c], pf);
-            }
+            for (int c = 0; c < 6; ++c) pf = fmaf(rv[c], zz[c], pf);
         }
         p = block_sum((double)pf);
         if (threadIdx.x == 0) a.part_b[blockIdx.x] = p;
@@ -916,7 +968,12 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
         beta = (float)(following / rz);
         rz = following;
     }
-    for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = (double)(a.x[e] / a.units32[e]);
+    for (int64_t s = tid; s < a.n; s += stride) {
+        float xv[6];
+        ld8(a.x + 2 * s, xv);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)(xv[c] / a.units32[6 * s + c]);
+    }
     if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
 }
 
@@ -979,7 +1036,9 @@ extern "C" {
 
 int64_t dpf_mixed_bond_floats(int64_t n_bonds) { return 4 * 11 * n_bonds; }
 
-int64_t dpf_mixed_workspace_floats(int64_t n_sites) { return 30 * n_sites + 4 * (int64_t)kMaxPcgBlocks; }
+int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds) {
+    return 40 * n_sites + 12 * n_bonds + 4 * (int64_t)kMaxPcgBlocks;
+}
 
 static bool mixed_graph_ok(const dpf_graph *g) {
     return g && g->n_sites > 0 && g->n_bonds >= 0 && g->n_bonds < (int64_t(1) << 31) && g->inc_ptr && g->inc_bond;
@@ -1134,15 +1193,18 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
     a.max_it = max_iterations;
     a.out = out;
     a.iterations = iterations;
-    a.wrench = wrench;
-    a.x = workspace;
-    a.r = workspace + n6;
-    a.z = workspace + 2 * n6;
-    a.d = workspace + 3 * n6;
-    a.ad = workspace + 4 * n6;
-    double *parts = reinterpret_cast<double *>(workspace + 30 * g->n_sites + (30 * g->n_sites) % 2);
+    float4 *w4 = reinterpret_cast<float4 *>(workspace);
+    const int64_t n = g->n_sites;
+    a.zd = w4;                 // 4 float4 per site
+    a.x = w4 + 4 * n;          // 2 float4 per site
+    a.r = w4 + 6 * n;
+    a.ad = w4 + 8 * n;
+    a.wrench = w4 + 10 * n;    // 3 float4 per bond
+    double *parts = reinterpret_cast<double *>(w4 + 10 * n + 3 * g->n_bonds);
     a.part_a = parts;
     a.part_b = parts + kMaxPcgBlocks;
+    (void)n6;
+    (void)wrench;
     a.barrier = barrier;
     a.status = status;
     if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return DPF_ERR_CUDA;

@@ -823,7 +823,7 @@ class MixedNewtonBonds(NewtonBonds):
         self._mass32 = torch.empty((n, 6), dtype=f32, device=dev)
         self._y32 = torch.empty((n, 6), dtype=f32, device=dev)
         self._d32 = torch.empty((n, 6), dtype=f32, device=dev)
-        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n), dtype=f32, device=dev)
+        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n, m), dtype=f32, device=dev)
         self._call('dpf_to_float', 6*n, self.mass.data_ptr(), self._mass32.data_ptr(), self._stream())
         self._cached = None
 

@@ -264,8 +264,9 @@ int dpf_masked_scale(int64_t n_sites, const double *a, const double *units, cons
  * dpf_mixed_scaling); d32 is a float32 (N, 6) scratch. */
 int64_t dpf_mixed_bond_floats(int64_t n_bonds);
 
-/* Float workspace of dpf_mixed_precondition for N sites. */
-int64_t dpf_mixed_workspace_floats(int64_t n_sites);
+/* Float workspace of dpf_mixed_precondition for N sites and M bonds
+ * (16-byte aligned; holds the padded work vectors and the bond wrench). */
+int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds);
 
 /* Per-step float64 setup: bond records from the committed state, r0 (N, 6),
  * optionally loads(x) (N, 6), and scales[0..1] = [|dt M v + dt^2/2 ext|,
@@ -320,7 +321,8 @@ int dpf_to_float(int64_t count, const double *a, float *out, void *stream);
 
 /* Elastic PCG in float32 with float64 dot products (same stopping rule and
  * iteration accounting as dpf_elastic_precondition); workspace:
- * dpf_mixed_workspace_floats(N) floats; block/preconditioner float32.
+ * dpf_mixed_workspace_floats(N, M) floats (the wrench argument is unused);
+ * block/preconditioner float32.
  * Replaces NewtonBonds.elastic_precondition (experiments/bonded_dem_newton.py:107-130). */
 int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *mass32,
                            const uint8_t *fixed, const float *block, const float *preconditioner,
