@@ -25,7 +25,12 @@ __device__ __forceinline__ d3 operator+(d3 a, d3 b) { return {a.x + b.x, a.y + b
 __device__ __forceinline__ d3 operator-(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 __device__ __forceinline__ d3 operator-(d3 a) { return {-a.x, -a.y, -a.z}; }
 __device__ __forceinline__ d3 operator*(double s, d3 a) { return {s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ d3 operator/(d3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+// One reciprocal and three products: a float64 division costs many times a
+// multiply on GB300's float64 pipe.
+__device__ __forceinline__ d3 operator/(d3 a, double s) {
+    const double inv = 1.0 / s;
+    return {a.x * inv, a.y * inv, a.z * inv};
+}
 __device__ __forceinline__ double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 __device__ __forceinline__ d3 cross(d3 a, d3 b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};

@@ -18,6 +18,10 @@ namespace mp {
 constexpr int kMaxReduceBlocks = 1024;
 constexpr int64_t kPartialsOffset = 8;
 constexpr int kMaxPcgBlocks = 4096;
+// Lanes per site in the segmented (lane-group) site gathers: each lane of a
+// group walks every kGroup-th incidence of the site, then the group reduces
+// with xor shuffles.  Groups never straddle a warp.
+constexpr int kGroup = 4;
 
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
 inline int reduce_grid(int64_t n) {
@@ -661,36 +665,85 @@ struct ScalingArgs {
     double *units;
 };
 
-__global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (s >= a.n) return;
-    float D[36];
+// Packed upper triangle of a symmetric 6x6: k(p, q), p <= q.
+__host__ __device__ constexpr int sym6(int p, int q) { return p <= q ? p * 6 - p * (p - 1) / 2 + (q - p) : sym6(q, p); }
+
+// Adds the site-diagonal block of one bond to the packed upper triangle
+// (same block as add_block_f32 / experiments/bonded_dem_linear_gpu.py:54-72).
+__device__ __forceinline__ void add_block_sym(float D[21], V3<float> n, V3<float> r, float kn, float ks, float kb,
+                                              float kt) {
+    const float nv[3] = {n.x, n.y, n.z};
+    float d[9], h[9];
 #pragma unroll
-    for (int c = 0; c < 36; ++c) D[c] = 0.0f;
-    const int e1 = a.ptr[s + 1];
-    for (int e = a.ptr[s]; e < e1; ++e) {
-        const int v = a.inc[e];
-        const int64_t b = v >= 0 ? v : ~v;
-        const float4 t0 = __ldg(a.bd.t0 + b), t1 = __ldg(a.bd.t1 + b), t2 = __ldg(a.bd.t2 + b);
-        const float kt = __ldg(a.bd.t3 + b).x;
-        const V3<float> r = v >= 0 ? V3<float>{t1.x, t1.y, t1.z} : V3<float>{t2.x, t2.y, t2.z};
-        add_block_f32(D, {t0.x, t0.y, t0.z}, r, t0.w, t1.w, t2.w, kt);
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            const float nn = nv[p] * nv[q];
+            d[3 * p + q] = (p == q ? ks : 0.0f) + (kn - ks) * nn;
+            h[3 * p + q] = (p == q ? kb : 0.0f) + (kt - kb) * nn;
+        }
+    const float S[9] = {0.0f, -r.z, r.y, r.z, 0.0f, -r.x, -r.y, r.x, 0.0f};
+    float dS[9];
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            dS[3 * p + q] = d[3 * p] * S[q] + d[3 * p + 1] * S[3 + q] + d[3 * p + 2] * S[6 + q];
+#pragma unroll
+    for (int p = 0; p < 3; ++p)
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            if (p <= q) {
+                D[sym6(p, q)] += d[3 * p + q];
+                D[sym6(3 + p, 3 + q)] += S[p] * dS[q] + S[3 + p] * dS[3 + q] + S[6 + p] * dS[6 + q] + h[3 * p + q];
+            }
+            D[sym6(p, 3 + q)] -= dS[3 * p + q];
+        }
+}
+
+// One group of kGroup lanes per site: each lane sums every kGroup-th
+// incidence, the group reduces with xor shuffles, lane 0 inverts.
+__global__ void __launch_bounds__(256) scaling_sites_f32(ScalingArgs a) {
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
+    const int lane = threadIdx.x & (kGroup - 1);
+    const bool valid = s < a.n;
+    float D[21];
+#pragma unroll
+    for (int c = 0; c < 21; ++c) D[c] = 0.0f;
+    if (valid) {
+        const int e1 = a.ptr[s + 1];
+        for (int e = a.ptr[s] + lane; e < e1; e += kGroup) {
+            const int v = a.inc[e];
+            const int64_t b = v >= 0 ? v : ~v;
+            const float4 t0 = __ldg(a.bd.t0 + b), tr = __ldg((v >= 0 ? a.bd.t1 : a.bd.t2) + b);
+            const float4 t1w = __ldg(a.bd.t1 + b), t2w = __ldg(a.bd.t2 + b);
+            const float kt = __ldg(a.bd.t3 + b).x;
+            add_block_sym(D, {t0.x, t0.y, t0.z}, {tr.x, tr.y, tr.z}, t0.w, t1w.w, t2w.w, kt);
+        }
     }
+#pragma unroll
+    for (int o = 1; o < kGroup; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 21; ++c) D[c] += __shfl_xor_sync(0xffffffffu, D[c], o);
+    if (!valid || lane != 0) return;
     const bool fx = a.fixed[s] != 0;
+    float B[36];
 #pragma unroll
     for (int p = 0; p < 6; ++p)
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-            const float val = (p == q ? a.mass32[6 * s + p] : 0.0f) + a.alpha * D[6 * p + q];
-            D[6 * p + q] = fx ? (p == q ? 1.0f : 0.0f) : val;
+            const float val = (p == q ? a.mass32[6 * s + p] : 0.0f) + a.alpha * D[sym6(p, q)];
+            B[6 * p + q] = fx ? (p == q ? 1.0f : 0.0f) : val;
         }
     if (a.block) {
+        float4 *out = reinterpret_cast<float4 *>(a.block + 36 * s);
 #pragma unroll
-        for (int c = 0; c < 36; ++c) a.block[36 * s + c] = D[c];
+        for (int c = 0; c < 9; ++c) out[c] = make_float4(B[4 * c], B[4 * c + 1], B[4 * c + 2], B[4 * c + 3]);
     }
-    spd_inverse6_f32(D);
+    spd_inverse6_f32(B);
+    float4 *out = reinterpret_cast<float4 *>(a.P + 36 * s);
 #pragma unroll
-    for (int c = 0; c < 36; ++c) a.P[36 * s + c] = D[c];
+    for (int c = 0; c < 9; ++c) out[c] = make_float4(B[4 * c], B[4 * c + 1], B[4 * c + 2], B[4 * c + 3]);
     const double r = fx ? 1.0 : a.radii[s];
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -711,11 +764,6 @@ __device__ __forceinline__ void mv6(const float *P, const float x[6], float y[6]
         y[row] = v;
     }
 }
-
-// Lanes per site in the segmented (lane-group) site gathers: each lane of a
-// group walks every kGroup-th incidence of the site, then the group reduces
-// with xor shuffles.  Groups never straddle a warp.
-constexpr int kGroup = 4;
 
 __device__ __forceinline__ void group_gather9f(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
                                                const float *__restrict__ w, int64_t s, bool valid, int lane,
@@ -1090,7 +1138,7 @@ int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32,
         return DPF_ERR_ARGUMENT;
     ScalingArgs a{g->n_sites, g->inc_ptr, g->inc_bond, split_bond_data(bond_data, g->n_bonds), mass32, radii, fixed,
                   (float)(0.25 * dt * dt), block, preconditioner, units32, units};
-    scaling_sites_f32<<<blocks_for(g->n_sites, 128), 128, 0, (cudaStream_t)stream>>>(a);
+    scaling_sites_f32<<<blocks_for(kGroup * g->n_sites, 256), 256, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -70,7 +70,10 @@ __device__ __forceinline__ V3<T> cross(V3<T> a, V3<T> b) {
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 template <class T>
-__device__ __forceinline__ V3<T> operator/(V3<T> a, T s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ V3<T> operator/(V3<T> a, T s) {
+    const T inv = lift<T>(1.0f) / s;
+    return {a.x * inv, a.y * inv, a.z * inv};
+}
 template <class T>
 __device__ __forceinline__ V3<T> lift3(float3 a) { return {lift<T>(a.x), lift<T>(a.y), lift<T>(a.z)}; }
 __device__ __forceinline__ V3<float> val3(V3<Dual> a) { return {a.x.v, a.y.v, a.z.v}; }
