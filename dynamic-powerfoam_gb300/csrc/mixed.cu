@@ -701,18 +701,17 @@ __device__ __forceinline__ void add_block_sym(float D[21], V3<float> n, V3<float
         }
 }
 
-// One group of kGroup lanes per site: each lane sums every kGroup-th
-// incidence, the group reduces with xor shuffles, lane 0 inverts.
-__global__ void __launch_bounds__(256) scaling_sites_f32(ScalingArgs a) {
-    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroup;
-    const int lane = threadIdx.x & (kGroup - 1);
+// One thread per site: the 6x6 inverse dominates, so lane groups would idle.
+__global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const bool valid = s < a.n;
     float D[21];
 #pragma unroll
     for (int c = 0; c < 21; ++c) D[c] = 0.0f;
     if (valid) {
         const int e1 = a.ptr[s + 1];
-        for (int e = a.ptr[s] + lane; e < e1; e += kGroup) {
+#pragma unroll 2
+        for (int e = a.ptr[s]; e < e1; ++e) {
             const int v = a.inc[e];
             const int64_t b = v >= 0 ? v : ~v;
             const float4 t0 = __ldg(a.bd.t0 + b), tr = __ldg((v >= 0 ? a.bd.t1 : a.bd.t2) + b);
@@ -721,11 +720,7 @@ __global__ void __launch_bounds__(256) scaling_sites_f32(ScalingArgs a) {
             add_block_sym(D, {t0.x, t0.y, t0.z}, {tr.x, tr.y, tr.z}, t0.w, t1w.w, t2w.w, kt);
         }
     }
-#pragma unroll
-    for (int o = 1; o < kGroup; o <<= 1)
-#pragma unroll
-        for (int c = 0; c < 21; ++c) D[c] += __shfl_xor_sync(0xffffffffu, D[c], o);
-    if (!valid || lane != 0) return;
+    if (!valid) return;
     const bool fx = a.fixed[s] != 0;
     float B[36];
 #pragma unroll
@@ -1138,7 +1133,7 @@ int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32,
         return DPF_ERR_ARGUMENT;
     ScalingArgs a{g->n_sites, g->inc_ptr, g->inc_bond, split_bond_data(bond_data, g->n_bonds), mass32, radii, fixed,
                   (float)(0.25 * dt * dt), block, preconditioner, units32, units};
-    scaling_sites_f32<<<blocks_for(kGroup * g->n_sites, 256), 256, 0, (cudaStream_t)stream>>>(a);
+    scaling_sites_f32<<<blocks_for(g->n_sites, 128), 128, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
