@@ -83,7 +83,8 @@ SIGNATURES = {
     'dpf_to_float': (i32, [i64, vp, vp, vp]),
     'dpf_mixed_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, f64, i32, vp, vp, vp, vp, vp, vp,
                                      vp]),
-    'dpf_mixed_commit': (i32, [P(Graph), vp, P(History), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_commit': (i32, [P(Graph), vp, P(History), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_begin': (i32, [i64, vp, vp, vp, vp, vp, f64, vp, vp, vp, vp]),
     'dpf_static_max_bonds': (i64, []),
 }
 
@@ -96,7 +97,7 @@ KERNELS = {
     'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
     'dpf_stiffness_apply_static': 2, 'dpf_mixed_setup': 2, 'dpf_mixed_residual': 2, 'dpf_mixed_scaling': 1,
     'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 3, 'dpf_mixed_stiffness_apply': 2,
-    'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2,
+    'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1,
 }
 LAUNCHES = {'count': 0}
 

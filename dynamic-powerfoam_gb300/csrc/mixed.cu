@@ -1031,8 +1031,12 @@ struct CommitArgs {
     const float *y32;
     const double *y;
     double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
+    float *dloads;  // optional: increment of the committed loads (9 floats per bond)
 };
 
+// End state of the accepted increment; with dloads it also rewrites the bond
+// records for the next step in place (the bond's own record only) and emits
+// loads(x_end) - loads(x) per bond as float32 increments.
 __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
@@ -1041,12 +1045,16 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     load_y(a.y32, B.i, ui, wi);
     load_y(a.y32, B.j, uj, wj);
     const BondIncrement<float> o = bond_increment<float>(B, ui, wi, uj, wj);
-    a.fn_end[b] = a.h.fn[b] + (double)(B.kn * value(o.dn));
-    a.mt_end[b] = a.h.mt[b] + (double)(B.kt * value(o.tw));
+    const float dfn = B.kn * value(o.dn), dmt = B.kt * value(o.tw);
+    const double fn_end = a.h.fn[b] + (double)dfn, mt_end = a.h.mt[b] + (double)dmt;
+    a.fn_end[b] = fn_end;
+    a.mt_end[b] = mt_end;
     // end normal in float64 from the end positions (geometry(end))
     const double *yi = a.y + 6 * (int64_t)B.i, *yj = a.y + 6 * (int64_t)B.j;
     const d3 de = (ld3(a.h.x, B.j) + ld3(yj)) - (ld3(a.h.x, B.i) + ld3(yi));
-    st3(a.normal_end, b, de / norm(de));
+    const double le64 = norm(de);
+    const d3 ne = de / le64;
+    st3(a.normal_end, b, ne);
     const V3<float> nx = lift3<float>(B.n0) + lift3<float>(B.dn0);
     float le;
     const V3<float> dnx_e = normal_change(B.L0, nx, uj - ui, le);
@@ -1057,16 +1065,86 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     const V3<float> dfs = o.dfs1 + t2.apply(fs1);
     const V3<float> dmb = o.dmb1 + t2.apply(mb1);
     const V3<float> doff = o.doff + t2.apply(off1);
-    const d3 fs = ld3(a.h.fs, b), mb = ld3(a.h.mb, b), off = ld3(a.h.offset, b);
-    st3(a.fs_end, b, fs + mk(dfs.x, dfs.y, dfs.z));
-    st3(a.mb_end, b, mb + mk(dmb.x, dmb.y, dmb.z));
-    st3(a.offset_end, b, off + mk(doff.x, doff.y, doff.z));
+    const d3 fs_end = ld3(a.h.fs, b) + mk(dfs.x, dfs.y, dfs.z);
+    const d3 mb_end = ld3(a.h.mb, b) + mk(dmb.x, dmb.y, dmb.z);
+    const d3 off_end = ld3(a.h.offset, b) + mk(doff.x, doff.y, doff.z);
+    st3(a.fs_end, b, fs_end);
+    st3(a.mb_end, b, mb_end);
+    st3(a.offset_end, b, off_end);
+    if (!a.dloads) return;
+    // loads(x_end) - loads(x) of this bond from the small increments
+    const V3<float> ne32 = nx + dnx_e;
+    const V3<float> fx = B.fn * nx + lift3<float>(B.fs);
+    const V3<float> dF = dfn * ne32 + B.fn * dnx_e + dfs;
+    const V3<float> dcp = dmt * ne32 + B.mt * dnx_e + dmb;
+    const V3<float> f_new = fx + dF;
+    const V3<float> dc = 0.5f * (ui + uj) + B.rh * dnx_e + doff;
+    const V3<float> ri_x = lift3<float>(B.ri_x), rj_x = ri_x - B.L0 * nx;
+    const V3<float> dTi = cross(dc - ui, f_new) + cross(ri_x, dF) + dcp;
+    const V3<float> dTj = -(cross(dc - uj, f_new) + cross(rj_x, dF) + dcp);
+    store9(a.dloads, b, dF, dTi, dTj);
+    // records of the next step: n0 = normal_end (= geometry(x_end), so dn0 = 0)
+    const d3 ri_end = 0.5 * de + B.rh * ne + off_end;
+    a.bd.rec.r0[b] = make_float4((float)ne.x, (float)ne.y, (float)ne.z, (float)le64);
+    a.bd.rec.r1[b] = make_float4(0.0f, 0.0f, 0.0f, B.rh);
+    a.bd.rec.r2[b] = make_float4((float)ri_end.x, (float)ri_end.y, (float)ri_end.z, (float)fn_end);
+    a.bd.rec.r3[b] = make_float4((float)fs_end.x, (float)fs_end.y, (float)fs_end.z, (float)mt_end);
+    a.bd.rec.r4[b] = make_float4((float)mb_end.x, (float)mb_end.y, (float)mb_end.z, B.kn);
+    a.bd.rec.r5[b] = make_float4((float)off_end.x, (float)off_end.y, (float)off_end.z, B.ks);
 }
 
-__global__ void __launch_bounds__(kThreads) commit_sites(int64_t n, const double *x, const double *y, double *x_end) {
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    st3(x_end, s, ld3(x, s) + ld3(y + 6 * s));
+// x_end = x + u; with dloads, loads += site sum of the load increments.
+__global__ void __launch_bounds__(kThreads) commit_sites(int64_t n, const int32_t *ptr, const int32_t *inc,
+                                                         const double *x, const double *y, double *x_end,
+                                                         const float *dloads, double *loads) {
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroupJ;
+    const int lane = threadIdx.x & (kGroupJ - 1);
+    const bool valid = g < n;
+    if (dloads) {
+        float hi[6], lo[6];
+        group_gather9c_j(ptr, inc, dloads, g, valid, lane, hi, lo);
+        if (valid && lane == 0) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) loads[6 * g + c] += (double)hi[c] + (double)lo[c];
+        }
+    }
+    if (valid && lane == 0) st3(x_end, g, ld3(x, g) + ld3(y + 6 * g));
+}
+
+// Per-step constants from maintained loads: r0 and the rhs scale terms.
+struct BeginArgs {
+    int64_t n;
+    const double *loads, *mass, *v, *external;
+    const uint8_t *fixed;
+    double dt, half_dt2;
+    double *r0, *scales, *partials;
+};
+
+__global__ void __launch_bounds__(kThreads) begin_sites(BeginArgs a) {
+    double a2 = 0.0, l2 = 0.0;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 6 * a.n; e += (int64_t)gridDim.x * blockDim.x) {
+        const double mv = a.dt * a.mass[e] * a.v[e];
+        const double rhs = mv + a.half_dt2 * a.external[e];
+        a2 += rhs * rhs;
+        const double L = a.loads[e];
+        if (!a.fixed[e / 6]) l2 += L * L;
+        a.r0[e] = -mv - a.half_dt2 * (L + a.external[e]);
+    }
+    a2 = block_sum(a2);
+    l2 = block_sum(l2);
+    double *part = a.partials + kPartialsOffset;
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = a2;
+        part[2 * blockIdx.x + 1] = l2;
+    }
+    if (last_block(counter_slot(a.partials, 5))) {
+        const double sa = block_sum_array(part, gridDim.x, 2);
+        const double sl = block_sum_array(part + 1, gridDim.x, 2);
+        if (threadIdx.x == 0) {
+            a.scales[0] = sqrt(sa);
+            a.scales[1] = sqrt(sl);
+        }
+    }
 }
 
 }  // namespace mp
@@ -1259,18 +1337,29 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
 
 int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y, const float *y32,
                      double *x_end, double *normal_end, double *offset_end, double *fn_end, double *fs_end,
-                     double *mt_end, double *mb_end, void *stream) {
+                     double *mt_end, double *mb_end, float *dloads, double *loads, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !h || !h->x || !h->fn || !h->fs || !h->mt || !h->mb || !h->offset ||
-        !y || !y32 || !x_end ||
+        !y || !y32 || !x_end || (dloads && !loads) ||
         ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
         CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y32, y, normal_end, offset_end, fs_end,
-                     mb_end, fn_end, mt_end};
+                     mb_end, fn_end, mt_end, dloads};
         commit_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
-    commit_sites<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, h->x, y, x_end);
+    commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(
+        g->n_sites, g->inc_ptr, g->inc_bond, h->x, y, x_end, g->n_bonds ? dloads : nullptr, loads);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_begin(int64_t n_sites, const double *loads, const double *mass, const double *v, const double *external,
+                    const uint8_t *fixed, double dt, double *r0, double *scales, double *partials, void *stream) {
+    if (n_sites <= 0 || !loads || !mass || !v || !external || !fixed || !r0 || !scales || !partials)
+        return DPF_ERR_ARGUMENT;
+    BeginArgs a{n_sites, loads, mass, v, external, fixed, dt, 0.5 * dt * dt, r0, scales, partials};
+    begin_sites<<<reduce_grid(6 * n_sites), kThreads, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

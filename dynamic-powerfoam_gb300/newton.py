@@ -801,6 +801,9 @@ class MixedNewtonBonds(NewtonBonds):
     """
 
     min_linear_tolerance = 1e-6
+    # Steps between float64 rebuilds of the bond records and committed loads
+    # (in between they are advanced by the commit's float32 increments).
+    refresh_interval = 32
 
     def step(self, dt, external, tolerance=2e-7, max_iterations=12, *, pose_tolerance=2e-6, backend='fgmres',
              linear_tolerance=1e-6, preconditioning='elastic'):
@@ -826,6 +829,14 @@ class MixedNewtonBonds(NewtonBonds):
         self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n, m), dtype=f32, device=dev)
         self._call('dpf_to_float', 6*n, self.mass.data_ptr(), self._mass32.data_ptr(), self._stream())
         self._cached = None
+        self._loads = torch.empty((n, 6), dtype=F64, device=dev)
+        self._token = None
+        self._since_refresh = 0
+
+    def _state_token(self):
+        # identity and in-place version of every committed tensor the records depend on
+        return tuple((t.data_ptr(), t._version) for t in (self.x, self.normal, self.offset, self.fn, self.fs,
+                                                           self.mt, self.mb, self.radii))
 
     def _to_y32(self, y):
         self._call('dpf_to_float', 6*self.n_sites, y.data_ptr(), self._y32.data_ptr(), self._stream())
@@ -833,12 +844,21 @@ class MixedNewtonBonds(NewtonBonds):
     def _step_begin(self, dt, external):
         self._cached = None
         self._status.zero_()
-        self._timed('setup', lambda: self._call(
-            'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
-            ctypes.byref(self._history_struct()), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
-            self.fixed.data_ptr(), dt, self._bond_data.data_ptr(), self._r0.data_ptr(), None,
-            self._scalars.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(), self._status.data_ptr(),
-            self._stream()))
+        history = self._history_struct()
+        if self._token is not None and self._token == self._state_token() and \
+                self._since_refresh < self.refresh_interval:
+            self._timed('setup', lambda: self._call(
+                'dpf_mixed_begin', self.n_sites, self._loads.data_ptr(), self.mass.data_ptr(), self._v.data_ptr(),
+                external.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(), self._scalars.data_ptr(),
+                self._partials.data_ptr(), self._stream()))
+        else:
+            self._since_refresh = 0
+            self._timed('setup', lambda: self._call(
+                'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                ctypes.byref(history), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
+                self.fixed.data_ptr(), dt, self._bond_data.data_ptr(), self._r0.data_ptr(), self._loads.data_ptr(),
+                self._scalars.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(),
+                self._status.data_ptr(), self._stream()))
         (a, l), status = self._fetch(2, status=True)
         if status:
             raise guard_error(status)
@@ -912,14 +932,17 @@ class MixedNewtonBonds(NewtonBonds):
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
         self._to_y32(y)
+        history = self._history_struct()
         self._timed('commit', lambda: self._call(
-            'dpf_mixed_commit', ctypes.byref(self._graph), self._bond_data.data_ptr(),
-            ctypes.byref(self._history_struct()), y.data_ptr(), self._y32.data_ptr(), state['x'].data_ptr(),
-            state['normal'].data_ptr(), state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(),
-            state['mt'].data_ptr(), state['mb'].data_ptr(), self._stream()))
+            'dpf_mixed_commit', ctypes.byref(self._graph), self._bond_data.data_ptr(), ctypes.byref(history),
+            y.data_ptr(), self._y32.data_ptr(), state['x'].data_ptr(), state['normal'].data_ptr(),
+            state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(), state['mt'].data_ptr(),
+            state['mb'].data_ptr(), self._wrench32.data_ptr(), self._loads.data_ptr(), self._stream()))
         rotation = self._vec(self.rotation).clone()
         self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(), rotation.data_ptr(),
                    self._stream())
         self.commit(state)
         self.v, self.rotation = self._v, rotation
         self._cached = None
+        self._token = self._state_token()
+        self._since_refresh += 1

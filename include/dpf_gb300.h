@@ -332,11 +332,23 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
 
 /* End state of the accepted increment y: float32 increments added to the
  * float64 committed history (end normal recomputed in float64 from x + y).
+ * With dloads (9 M floats scratch) and loads (float64 (N, 6), the committed
+ * loads(x) kept by the caller) it also rewrites the bond records for the next
+ * step and adds loads(x_end) - loads(x), from float32 increments, to loads.
  * Replaces FiniteBondsGPU.trial's end-of-step outputs and commit
  * (experiments/bonded_dem_finite_gpu.py:102-120). */
 int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y,
                      const float *y32, double *x_end, double *normal_end, double *offset_end,
-                     double *fn_end, double *fs_end, double *mt_end, double *mb_end, void *stream);
+                     double *fn_end, double *fs_end, double *mt_end, double *mb_end, float *dloads,
+                     double *loads, void *stream);
+
+/* Per-step constants from loads maintained by dpf_mixed_commit: r0 (N, 6) and
+ * scales[0..1] as dpf_mixed_setup, without rebuilding the bond records.
+ * Replaces the loads/rhs_scale prologue of NewtonBonds.step
+ * (experiments/bonded_dem_newton.py:137-139). */
+int dpf_mixed_begin(int64_t n_sites, const double *loads, const double *mass, const double *v,
+                    const double *external, const uint8_t *fixed, double dt, double *r0,
+                    double *scales, double *partials, void *stream);
 
 #ifdef __cplusplus
 }

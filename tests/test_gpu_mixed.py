@@ -124,3 +124,24 @@ def test_mixed_trajectory_matches_float64_solve(lattice, steps):
         assert float(torch.linalg.vector_norm(getattr(b, k) - getattr(a, k))/torch.linalg.vector_norm(getattr(a, k))) < 1e-5
     ev = float(torch.linalg.vector_norm(b.v - a.v)/torch.linalg.vector_norm(a.v))
     assert ev < 1e-5, ev
+
+
+def test_incremental_loads_match_float64_rebuild():
+    """The commit-maintained records and loads agree with a float64 rebuild."""
+    import dpf_gb300
+    foam = dpf_gb300.jittered_lattice_foam(10, seed=4)
+    load = dpf_gb300.gravity_load(foam)
+    args = (foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'], foam['fixed'])
+    kw = dict(young=foam['young'], shear=foam['shear'])
+    a = dpf_gb300.MixedNewtonBonds(*args, **kw)
+    b = dpf_gb300.MixedNewtonBonds(*args, **kw)
+    b.refresh_interval = 0          # rebuild in float64 every step
+    ext = a.tensor(load)
+    for _ in range(12):
+        a.step(1e-3, ext, tolerance=1e-6)
+        b.step(1e-3, ext, tolerance=1e-6)
+    ref = a.loads()                 # float64 loads of the committed state
+    err = float(torch.linalg.vector_norm(a._loads - ref)/torch.linalg.vector_norm(ref))
+    assert err < 1e-6, err
+    dx = float(torch.linalg.vector_norm(a.x - b.x)/torch.linalg.vector_norm(b.x - a.p))
+    assert dx < 1e-6, dx
