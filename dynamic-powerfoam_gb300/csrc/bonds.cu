@@ -449,7 +449,8 @@ __device__ __forceinline__ void site_diagonal(const int32_t *ptr, const int32_t 
 }
 
 // Inverse of a symmetric positive definite 6x6 matrix via Cholesky
-// (A = L L^T, A^-1 = L^-T L^-1), fully unrolled into registers.
+// (A = L L^T, A^-1 = L^-T L^-1), fully unrolled into registers: every loop
+// has a constant trip count so all indices fold.
 __device__ __forceinline__ void spd_inverse6(const double A[36], double P[36]) {
     double L[36];
 #pragma unroll
@@ -458,16 +459,20 @@ __device__ __forceinline__ void spd_inverse6(const double A[36], double P[36]) {
     for (int jj = 0; jj < 6; ++jj) {
         double s = A[6 * jj + jj];
 #pragma unroll
-        for (int kk = 0; kk < jj; ++kk) s -= L[6 * jj + kk] * L[6 * jj + kk];
+        for (int kk = 0; kk < 6; ++kk)
+            if (kk < jj) s -= L[6 * jj + kk] * L[6 * jj + kk];
         const double ljj = sqrt(s);
         L[6 * jj + jj] = ljj;
         const double inv = 1.0 / ljj;
 #pragma unroll
-        for (int ii = jj + 1; ii < 6; ++ii) {
-            double v = A[6 * ii + jj];
+        for (int ii = 0; ii < 6; ++ii) {
+            if (ii > jj) {
+                double v = A[6 * ii + jj];
 #pragma unroll
-            for (int kk = 0; kk < jj; ++kk) v -= L[6 * ii + kk] * L[6 * jj + kk];
-            L[6 * ii + jj] = v * inv;
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk < jj) v -= L[6 * ii + kk] * L[6 * jj + kk];
+                L[6 * ii + jj] = v * inv;
+            }
         }
     }
     double W[36];  // W = L^-1 (lower triangular)
@@ -477,22 +482,28 @@ __device__ __forceinline__ void spd_inverse6(const double A[36], double P[36]) {
     for (int ii = 0; ii < 6; ++ii) {
         W[6 * ii + ii] = 1.0 / L[6 * ii + ii];
 #pragma unroll
-        for (int jj = 0; jj < ii; ++jj) {
-            double v = 0.0;
+        for (int jj = 0; jj < 6; ++jj) {
+            if (jj < ii) {
+                double v = 0.0;
 #pragma unroll
-            for (int kk = jj; kk < ii; ++kk) v += L[6 * ii + kk] * W[6 * kk + jj];
-            W[6 * ii + jj] = -v * W[6 * ii + ii];
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk >= jj && kk < ii) v += L[6 * ii + kk] * W[6 * kk + jj];
+                W[6 * ii + jj] = -v * W[6 * ii + ii];
+            }
         }
     }
 #pragma unroll
     for (int ii = 0; ii < 6; ++ii)
 #pragma unroll
-        for (int jj = 0; jj <= ii; ++jj) {
-            double v = 0.0;
+        for (int jj = 0; jj < 6; ++jj) {
+            if (jj <= ii) {
+                double v = 0.0;
 #pragma unroll
-            for (int kk = ii; kk < 6; ++kk) v += W[6 * kk + ii] * W[6 * kk + jj];
-            P[6 * ii + jj] = v;
-            P[6 * jj + ii] = v;
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk >= ii) v += W[6 * kk + ii] * W[6 * kk + jj];
+                P[6 * ii + jj] = v;
+                P[6 * jj + ii] = v;
+            }
         }
 }
 

@@ -601,6 +601,7 @@ __device__ __forceinline__ void add_block_f32(float D[36], V3<float> n, V3<float
 
 // In-place inverse of a symmetric positive definite 6x6 after symmetric
 // diagonal scaling (Jacobi), Cholesky based; A is overwritten with A^-1.
+// Every loop has a constant trip count so all indices fold to registers.
 __device__ __forceinline__ void spd_inverse6_f32(float A[36]) {
     float sc[6];
 #pragma unroll
@@ -609,47 +610,57 @@ __device__ __forceinline__ void spd_inverse6_f32(float A[36]) {
     for (int p = 0; p < 6; ++p)
 #pragma unroll
         for (int q = 0; q < 6; ++q) A[6 * p + q] *= sc[p] * sc[q];
-    // Cholesky: lower triangle of A becomes L
+    // Cholesky: the lower triangle of A becomes L
 #pragma unroll
     for (int jj = 0; jj < 6; ++jj) {
         float s = A[7 * jj];
 #pragma unroll
-        for (int kk = 0; kk < jj; ++kk) s -= A[6 * jj + kk] * A[6 * jj + kk];
+        for (int kk = 0; kk < 6; ++kk)
+            if (kk < jj) s -= A[6 * jj + kk] * A[6 * jj + kk];
         const float l = sqrtf(s);
         A[7 * jj] = l;
         const float inv = 1.0f / l;
 #pragma unroll
-        for (int ii = jj + 1; ii < 6; ++ii) {
-            float v = A[6 * ii + jj];
+        for (int ii = 0; ii < 6; ++ii) {
+            if (ii > jj) {
+                float v = A[6 * ii + jj];
 #pragma unroll
-            for (int kk = 0; kk < jj; ++kk) v -= A[6 * ii + kk] * A[6 * jj + kk];
-            A[6 * ii + jj] = v * inv;
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk < jj) v -= A[6 * ii + kk] * A[6 * jj + kk];
+                A[6 * ii + jj] = v * inv;
+            }
         }
     }
-    // W = L^-1 into the upper triangle (transposed): U[jj][ii] = W[ii][jj]
-    float W[21];
+    // W = L^-1 (lower triangular), kept in the upper triangle of A as W^T
+    float W[36];
 #pragma unroll
     for (int ii = 0; ii < 6; ++ii) {
-        const int base = ii * (ii + 1) / 2;
-        W[base + ii] = 1.0f / A[7 * ii];
+        W[7 * ii] = 1.0f / A[7 * ii];
 #pragma unroll
-        for (int jj = 0; jj < ii; ++jj) {
-            float v = 0.0f;
+        for (int jj = 0; jj < 6; ++jj) {
+            if (jj < ii) {
+                float v = 0.0f;
 #pragma unroll
-            for (int kk = jj; kk < ii; ++kk) v += A[6 * ii + kk] * W[kk * (kk + 1) / 2 + jj];
-            W[base + jj] = -v * W[base + ii];
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk >= jj && kk < ii) v += A[6 * ii + kk] * W[6 * kk + jj];
+                W[6 * ii + jj] = -v * W[7 * ii];
+            }
         }
     }
+    // A^-1 = W^T W, unscaled
 #pragma unroll
     for (int ii = 0; ii < 6; ++ii)
 #pragma unroll
-        for (int jj = 0; jj <= ii; ++jj) {
-            float v = 0.0f;
+        for (int jj = 0; jj < 6; ++jj) {
+            if (jj <= ii) {
+                float v = 0.0f;
 #pragma unroll
-            for (int kk = ii; kk < 6; ++kk) v += W[kk * (kk + 1) / 2 + ii] * W[kk * (kk + 1) / 2 + jj];
-            v *= sc[ii] * sc[jj];
-            A[6 * ii + jj] = v;
-            A[6 * jj + ii] = v;
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk >= ii) v += W[6 * kk + ii] * W[6 * kk + jj];
+                v *= sc[ii] * sc[jj];
+                A[6 * ii + jj] = v;
+                A[6 * jj + ii] = v;
+            }
         }
 }
 
@@ -666,7 +677,9 @@ struct ScalingArgs {
 };
 
 // Packed upper triangle of a symmetric 6x6: k(p, q), p <= q.
-__host__ __device__ constexpr int sym6(int p, int q) { return p <= q ? p * 6 - p * (p - 1) / 2 + (q - p) : sym6(q, p); }
+__host__ __device__ __forceinline__ constexpr int sym6(int p, int q) {
+    return (p < q ? p : q) * 6 - (p < q ? p : q) * ((p < q ? p : q) - 1) / 2 + ((p < q ? q : p) - (p < q ? p : q));
+}
 
 // Adds the site-diagonal block of one bond to the packed upper triangle
 // (same block as add_block_f32 / experiments/bonded_dem_linear_gpu.py:54-72).
@@ -1083,14 +1096,19 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     const V3<float> dTi = cross(dc - ui, f_new) + cross(ri_x, dF) + dcp;
     const V3<float> dTj = -(cross(dc - uj, f_new) + cross(rj_x, dF) + dcp);
     store9(a.dloads, b, dF, dTi, dTj);
-    // records of the next step: n0 = normal_end (= geometry(x_end), so dn0 = 0)
-    const d3 ri_end = 0.5 * de + B.rh * ne + off_end;
-    a.bd.rec.r0[b] = make_float4((float)ne.x, (float)ne.y, (float)ne.z, (float)le64);
+    // records of the next step: n0 = normal_end (= geometry(x_end), so dn0 = 0);
+    // the other fields are float32 quantities, formed in float32
+    const float3 ne32f = tof3(ne);
+    const float le32 = (float)le64;
+    const V3<float> nef = {ne32f.x, ne32f.y, ne32f.z};
+    const V3<float> ri_end = (0.5f * le32) * nef + B.rh * nef + (lift3<float>(B.off) + doff);
+    const V3<float> fsr = lift3<float>(B.fs) + dfs, mbr = lift3<float>(B.mb) + dmb, offr = lift3<float>(B.off) + doff;
+    a.bd.rec.r0[b] = make_float4(ne32f.x, ne32f.y, ne32f.z, le32);
     a.bd.rec.r1[b] = make_float4(0.0f, 0.0f, 0.0f, B.rh);
-    a.bd.rec.r2[b] = make_float4((float)ri_end.x, (float)ri_end.y, (float)ri_end.z, (float)fn_end);
-    a.bd.rec.r3[b] = make_float4((float)fs_end.x, (float)fs_end.y, (float)fs_end.z, (float)mt_end);
-    a.bd.rec.r4[b] = make_float4((float)mb_end.x, (float)mb_end.y, (float)mb_end.z, B.kn);
-    a.bd.rec.r5[b] = make_float4((float)off_end.x, (float)off_end.y, (float)off_end.z, B.ks);
+    a.bd.rec.r2[b] = make_float4(ri_end.x, ri_end.y, ri_end.z, B.fn + dfn);
+    a.bd.rec.r3[b] = make_float4(fsr.x, fsr.y, fsr.z, B.mt + dmt);
+    a.bd.rec.r4[b] = make_float4(mbr.x, mbr.y, mbr.z, B.kn);
+    a.bd.rec.r5[b] = make_float4(offr.x, offr.y, offr.z, B.ks);
 }
 
 // x_end = x + u; with dloads, loads += site sum of the load increments.
