@@ -355,6 +355,124 @@ class FiniteBonds(LinearBonds):
         scale[:, :3] = self.radii[:, None]
         return float((correction/scale).abs().max())
 
+    @torch.no_grad()
+    def solve_increment(self, rhs, dt, tolerance=2e-7, max_iterations=1600):
+        """Block-Jacobi PCG with local and global checks (``bonded_dem_finite_gpu.py:133-167``).
+
+        The blocks and their inverse come from the library (``dpf_prepare_scaling``);
+        K q from ``dpf_stiffness_apply``; the short vector recurrences are torch ops.
+        """
+        n = self.n_sites
+        block = torch.empty((n, 6, 6), dtype=F64, device=self.device)
+        preconditioner = torch.empty_like(block)
+        units = torch.empty_like(self.mass)
+        self._call('dpf_prepare_scaling', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(),
+                   self.radii.data_ptr(), float(dt), None, block.data_ptr(), preconditioner.data_ptr(),
+                   units.data_ptr(), self._stream())
+        self.preconditioner = preconditioner
+        rhs = rhs.clone(); rhs[self.fixed] = 0
+        norm = float(torch.linalg.vector_norm(rhs))
+        if norm < 1e-40:
+            return torch.zeros_like(rhs), dict(iterations=0)
+        x, residual = torch.zeros_like(rhs), rhs.clone()
+        z = torch.einsum('nij,nj->ni', preconditioner, residual)
+        direction = z.clone(); rz = (residual*z).sum()
+        alpha = dt*dt/4
+        for iteration in range(max_iterations):
+            ad = LinearBonds._operator(self, direction, alpha)
+            step = rz/(direction*ad).sum()
+            x += step*direction; residual -= step*ad
+            if iteration % 10 == 0:
+                relative = float(torch.linalg.vector_norm(residual))/norm
+                if relative < tolerance and self.local_defect(residual) < 2e-8:
+                    actual = rhs - LinearBonds._operator(self, x, alpha)
+                    if (float(torch.linalg.vector_norm(actual))/norm < 5*tolerance
+                            and self.local_defect(actual) < 1e-7):
+                        return x, dict(iterations=iteration+1)
+                if not np.isfinite(relative):
+                    raise RuntimeError('Nonfinite PCG residual')
+            z = torch.einsum('nij,nj->ni', preconditioner, residual)
+            next_rz = (residual*z).sum()
+            direction = z + (next_rz/rz)*direction; rz = next_rz
+        raise SubdivideError('Subdivide: balanced PCG did not converge')
+
+    @torch.no_grad()
+    def step(self, dt, external, tolerance=2e-7, max_iterations=18):
+        """Anderson-accelerated nonlinear implicit midpoint, the reference's
+        previous solver (``bonded_dem_finite_gpu.py:169-250``)."""
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('Positive finite dt required')
+        external = self._vec(external)
+        y = torch.zeros_like(self.mass)
+        v = self._vec(self.v)
+        rhs_scale = float(torch.linalg.vector_norm(dt*self.mass*v + .5*dt*dt*external))
+        rhs_scale = max(rhs_scale, .5*dt*dt*float(torch.linalg.vector_norm(self.loads()[~self.fixed])), 1e-30)
+        cg_total = 0
+        iterates, corrections = [], []
+        units = torch.ones_like(self.mass)
+        units[:, 3:] = self.radii[:, None]
+        relative = float('nan')
+        for iteration in range(max_iterations):
+            trial = self.trial(y)
+            residual = self.mass*(y - dt*v) - .5*dt*dt*(trial['force'] + external)
+            residual[self.fixed] = 0
+            relative = float(torch.linalg.vector_norm(residual))/rhs_scale
+            local = self.local_defect(residual) if iteration else (0. if relative == 0 else float('inf'))
+            if relative < tolerance and local < 2e-6:
+                velocity = 2*y/dt - v
+                rotation = self._vec(self.rotation).clone()
+                self._call('dpf_accept_step', self.n_sites, y.data_ptr(), float(dt), v.clone().data_ptr(),
+                           rotation.data_ptr(), self._stream())
+                self.commit(trial)
+                self.v, self.rotation = velocity, rotation
+                self.time += dt
+                return float((external*y).sum()), dict(
+                    nonlinear_iterations=iteration, nonlinear_relative_residual=relative, cg_iterations=cg_total,
+                    local_pose_defect=local,
+                    max_step_rotation=float(torch.linalg.vector_norm(y[:, 3:], dim=1).max()))
+            self.n, self.ri, self.rj = trial['n'], trial['ri'], trial['rj']
+            self.diagonal = self._diagonal_blocks()
+            self.preconditioner_dt = None
+            correction, cg = self.solve_increment(-residual, dt)
+            cg_total += cg['iterations']
+            merit = max(relative/tolerance, self.local_defect(residual)/2e-6)
+            iterates.append(y.clone()); corrections.append(correction.clone())
+            iterates, corrections = iterates[-6:], corrections[-6:]
+            directions = []
+            if len(corrections) > 1:
+                dc = torch.stack([b - a for a, b in zip(corrections[:-1], corrections[1:])])
+                dg = torch.stack([b + db - a - da for a, b, da, db in
+                                  zip(iterates[:-1], iterates[1:], corrections[:-1], corrections[1:])])
+                weighted = (dc*units).flatten(1)
+                gram = weighted@weighted.T
+                ridge = 1e-10*torch.trace(gram).clamp_min(1e-40)
+                coefficients = torch.linalg.solve(gram + ridge*torch.eye(len(gram), dtype=F64, device=self.device),
+                                                  weighted@(correction*units).flatten())
+                accelerated = correction - torch.einsum('h,hij->ij', coefficients, dg)
+                if bool(torch.isfinite(accelerated).all()):
+                    directions.append(accelerated)
+            directions.append(correction)
+            accepted = False
+            for direction in directions:
+                for factor in (1., .5, .25, .125, .0625):
+                    candidate = y + factor*direction
+                    try:
+                        state = self.trial(candidate)
+                    except RuntimeError:
+                        continue
+                    r = self.mass*(candidate - dt*v) - .5*dt*dt*(state['force'] + external)
+                    r[self.fixed] = 0
+                    candidate_merit = max(float(torch.linalg.vector_norm(r))/rhs_scale/tolerance,
+                                          self.local_defect(r)/2e-6)
+                    if candidate_merit < merit:
+                        y = candidate; accepted = True; break
+                if accepted:
+                    break
+            if not accepted:
+                raise SubdivideError('Subdivide: nonlinear line search failed')
+        raise SubdivideError(f'Subdivide: nonlinear residual {relative} did not converge')
+
     def advance_interval(self, dt, force_at_time, depth=0):
         """Recursive dt bisection on 'Subdivide:' (``bonded_dem_finite_gpu.py:252-261``)."""
         try:

@@ -287,6 +287,102 @@ class FiniteBonds(LinearBonds):
         scale[:, :3] = self.radii[:, None]
         return float(np.abs(correction/scale).max())
 
+    def solve_increment(self, rhs, dt, tolerance=2e-7, max_iterations=1600):
+        """PCG with local and global checks; ``bonded_dem_finite_gpu.py:133-167``."""
+        diagonal = np.einsum('ni,ij->nij', self.mass, np.eye(6)) + dt*dt*self.diagonal/4
+        diagonal[self.fixed] = np.eye(6)
+        self.preconditioner = np.linalg.inv(diagonal)
+        rhs = rhs.copy(); rhs[self.fixed] = 0
+        norm = float(np.linalg.norm(rhs))
+        if norm < 1e-40:
+            return np.zeros_like(rhs), dict(iterations=0)
+        x, residual = np.zeros_like(rhs), rhs.copy()
+        z = np.einsum('nij,nj->ni', self.preconditioner, residual)
+        direction = z.copy(); rz = dot(residual.ravel(), z.ravel())
+        for iteration in range(max_iterations):
+            ad = self._operator(direction, dt*dt/4)
+            step = rz/(direction*ad).sum()
+            x += step*direction; residual -= step*ad
+            if iteration % 10 == 0:
+                relative = float(np.linalg.norm(residual))/norm
+                if relative < tolerance and self.local_defect(residual) < 2e-8:
+                    actual = rhs - self._operator(x, dt*dt/4)
+                    if float(np.linalg.norm(actual))/norm < 5*tolerance and self.local_defect(actual) < 1e-7:
+                        return x, dict(iterations=iteration+1)
+                if not np.isfinite(relative):
+                    raise RuntimeError('Nonfinite PCG residual')
+            z = np.einsum('nij,nj->ni', self.preconditioner, residual)
+            next_rz = (residual*z).sum()
+            direction = z + (next_rz/rz)*direction; rz = next_rz
+        raise SubdivideError('Subdivide: balanced PCG did not converge')
+
+    def step(self, dt, external, tolerance=2e-7, max_iterations=18):
+        """Anderson-accelerated implicit midpoint; ``bonded_dem_finite_gpu.py:169-250``."""
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('Positive finite dt required')
+        y = np.zeros_like(self.v)
+        rhs_scale = float(np.linalg.norm(dt*self.mass*self.v + .5*dt*dt*external))
+        rhs_scale = max(rhs_scale, .5*dt*dt*float(np.linalg.norm(self.loads()[~self.fixed])), 1e-30)
+        cg_total = 0
+        iterates, corrections = [], []
+        units = np.ones_like(self.mass)
+        units[:, 3:] = self.radii[:, None]
+        relative = float('nan')
+        for iteration in range(max_iterations):
+            trial = self.trial(y)
+            residual = self.mass*(y - dt*self.v) - .5*dt*dt*(trial['force'] + external)
+            residual[self.fixed] = 0
+            relative = float(np.linalg.norm(residual))/rhs_scale
+            local = self.local_defect(residual) if iteration else (0. if relative == 0 else float('inf'))
+            if relative < tolerance and local < 2e-6:
+                velocity = 2*y/dt - self.v
+                rotation = exp_rotation(y[:, 3:])@self.rotation
+                self.commit(trial)
+                self.v, self.rotation = velocity, rotation
+                self.time += dt
+                return float((external*y).sum()), dict(
+                    nonlinear_iterations=iteration, nonlinear_relative_residual=relative, cg_iterations=cg_total,
+                    local_pose_defect=local, max_step_rotation=float(np.linalg.norm(y[:, 3:], axis=1).max()))
+            self.n, self.ri, self.rj = trial['n'], trial['ri'], trial['rj']
+            self.diagonal = self._diagonal_blocks()
+            self.preconditioner_dt = None
+            correction, cg = self.solve_increment(-residual, dt)
+            cg_total += cg['iterations']
+            merit = max(relative/tolerance, self.local_defect(residual)/2e-6)
+            iterates.append(y.copy()); corrections.append(correction.copy())
+            iterates, corrections = iterates[-6:], corrections[-6:]
+            directions = []
+            if len(corrections) > 1:
+                dc = np.stack([b - a for a, b in zip(corrections[:-1], corrections[1:])])
+                dg = np.stack([b + db - a - da for a, b, da, db in
+                               zip(iterates[:-1], iterates[1:], corrections[:-1], corrections[1:])])
+                weighted = (dc*units).reshape(len(dc), -1)
+                gram = weighted@weighted.T
+                ridge = 1e-10*max(np.trace(gram), 1e-40)
+                coefficients = np.linalg.solve(gram + ridge*np.eye(len(gram)), weighted@(correction*units).ravel())
+                accelerated = correction - np.einsum('h,hij->ij', coefficients, dg)
+                if np.isfinite(accelerated).all():
+                    directions.append(accelerated)
+            directions.append(correction)
+            accepted = False
+            for direction in directions:
+                for factor in (1., .5, .25, .125, .0625):
+                    candidate = y + factor*direction
+                    try:
+                        state = self.trial(candidate)
+                    except RuntimeError:
+                        continue
+                    r = self.mass*(candidate - dt*self.v) - .5*dt*dt*(state['force'] + external)
+                    r[self.fixed] = 0
+                    candidate_merit = max(float(np.linalg.norm(r))/rhs_scale/tolerance, self.local_defect(r)/2e-6)
+                    if candidate_merit < merit:
+                        y = candidate; accepted = True; break
+                if accepted:
+                    break
+            if not accepted:
+                raise SubdivideError('Subdivide: nonlinear line search failed')
+        raise SubdivideError(f'Subdivide: nonlinear residual {relative} did not converge')
+
     def advance_interval(self, dt, force_at_time, depth=0):
         """Recursive dt bisection on 'Subdivide:'; ``bonded_dem_finite_gpu.py:252-261``."""
         try:

@@ -48,7 +48,7 @@ def main(reference):
                 ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')}
 
     # ---- bonded_dem_newton_checks.fixture (restated inputs, reference state) ----
-    def newton_fixture(prestress, minimum_mass=1e-14):
+    def newton_fixture(prestress, minimum_mass=1e-14, cls=NewtonBonds):
         rng = np.random.default_rng(906)
         p = np.array(np.meshgrid(np.arange(3), np.arange(2), np.arange(2))).reshape(3, -1).T*.4
         p = p + rng.normal(0, .008, p.shape)
@@ -59,7 +59,7 @@ def main(reference):
         contacts = .5*(p[pairs[:, 0]]+p[pairs[:, 1]]) + rng.normal(0, .025, (len(pairs), 3))
         mass = np.geomspace(minimum_mass, 1., len(p)); rng.shuffle(mass)
         fixed = p[:, 0] < .1
-        s = NewtonBonds(p, radii, pairs, area, mass, fixed, contacts=contacts, device='cpu')
+        s = cls(p, radii, pairs, area, mass, fixed, contacts=contacts, device='cpu')
         if prestress:
             y = torch.zeros_like(s.mass)
             y[:, 1] = .025*s.p[:, 0]
@@ -126,6 +126,14 @@ def main(reference):
                 out[f'step_{tag}_{k}'] = info[k]
             out[f'step_{tag}_relative'] = info['nonlinear_relative_residual']
             out[f'step_{tag}_local'] = info['local_pose_defect']
+        # the previous solver (FiniteBondsGPU.step, Anderson), as in bonded_dem_newton_checks.py:107-112
+        solver, _ = newton_fixture(prestress, minimum_mass, cls=FiniteBondsGPU)
+        work, info = solver.step(dt, load, tolerance=2e-7)
+        for k, v in state_of(solver).items():
+            out[f'step_previous_{k}'] = v
+        out['step_previous_work'] = work
+        out['step_previous_nonlinear_iterations'] = info['nonlinear_iterations']
+        out['step_previous_cg_iterations'] = info['cg_iterations']
         np.savez_compressed(HERE/f'{name}.npz', **out)
         print(name, {k: out[k] for k in out if k.endswith('iterations')})
 

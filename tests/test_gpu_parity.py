@@ -211,3 +211,20 @@ def test_advance_interval_bisects_on_subdivide():
     assert [r['subdivision_depth'] for r in records] == [r['subdivision_depth'] for r in orecords]
     assert np.abs(host(s.x) - o.x).max() < 1e-8
     assert abs(work - ow) <= 1e-8*abs(ow)
+
+
+@pytest.mark.parametrize('case', CASES)
+def test_previous_solver_step_matches_reference(case):
+    """FiniteBondsGPU.step (PCG + Anderson + merit backtracking) on the GPU."""
+    import dpf_gb300
+    from tests.conftest import newton_inputs
+    g = golden(case)
+    s = dpf_gb300.FiniteBonds(**newton_inputs(g))
+    for k in STATE:
+        setattr(s, k, torch.as_tensor(np.array(g['state_' + k]), dtype=torch.float64, device=s.device).contiguous())
+    work, info = s.step(float(g['dt']), s.tensor(g['step_load']), tolerance=2e-7)
+    assert info['nonlinear_iterations'] == int(g['step_previous_nonlinear_iterations'])
+    assert abs(info['cg_iterations'] - int(g['step_previous_cg_iterations'])) <= 10
+    assert np.abs(host(s.x) - g['step_previous_state_x']).max() < 1e-8
+    assert np.abs(host(s.rotation) - g['step_previous_state_rotation']).max() < 1e-7
+    assert abs(work - float(g['step_previous_work'])) <= 1e-8*abs(float(g['step_previous_work']))

@@ -132,3 +132,17 @@ def test_transport_guard_and_transactional_trial():
     with pytest.raises(RuntimeError, match='Subdivide:'):
         s.trial(np.ones_like(s.mass))
     assert all(np.array_equal(getattr(s, k), v) for k, v in before.items())
+
+
+@pytest.mark.parametrize('case', ['newton_prestressed', 'newton_unstressed'])
+def test_previous_solver_step(case):
+    """FiniteBondsGPU.step (Anderson + merit backtracking) restated."""
+    g = golden(case)
+    s = dem.FiniteBonds(**newton_inputs(g))
+    for k in STATE:
+        setattr(s, k, np.array(g['state_' + k]))
+    work, info = s.step(float(g['dt']), g['step_load'], tolerance=2e-7)
+    assert info['nonlinear_iterations'] == int(g['step_previous_nonlinear_iterations'])
+    assert info['cg_iterations'] == int(g['step_previous_cg_iterations'])
+    assert np.abs(s.x - g['step_previous_state_x']).max() < 1e-9
+    assert abs(work - float(g['step_previous_work'])) <= 1e-9*abs(float(g['step_previous_work']))
