@@ -303,6 +303,7 @@ struct ResidualBondArgs {
     int want_tangent;
     float *wrench;
     int *status;
+    const int32_t *seg;  // optional per-bond segment: status[seg[b]]
 };
 
 __device__ __forceinline__ void load_y(const float *y, int s, V3<float> &u, V3<float> &w) {
@@ -330,7 +331,7 @@ __global__ void __launch_bounds__(kThreads) residual_bonds(ResidualBondArgs a) {
     const V3<float> turn = dnx_e - o.dn_x;
     if (!(le > 1e-12f)) flags |= DPF_ERR_COINCIDENT;
     if (dot(turn, turn) > kTurn2) flags |= DPF_ERR_NORMAL_TURN;
-    if (flags) atomicOr(a.status, flags);
+    if (flags) atomicOr(a.status + (a.seg ? a.seg[b] : 0), flags);
     if (a.want_tangent) {
         a.bd.t0[b] = make_float4(o.n.x, o.n.y, o.n.z, B.kn);
         a.bd.t1[b] = make_float4(o.ri.x, o.ri.y, o.ri.z, B.ks);
@@ -348,6 +349,7 @@ struct ResidualSiteArgs {
     const float *P, *units32;
     double *residual, *scaled, *norms, *partials;
     int *status;
+    const int32_t *seg;  // optional per-site segment: status[seg[s]]
 };
 
 __device__ __forceinline__ void matvec6f(const float *P, const float x[6], float y[6]) {
@@ -418,7 +420,12 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
         double r[6];
         const double *ys = a.y + 6 * s;
         const float w0 = (float)ys[3], w1 = (float)ys[4], w2 = (float)ys[5];
-        if (sqrtf(w0 * w0 + w1 * w1 + w2 * w2) > 0.25f) flags |= DPF_ERR_ROTATION;
+        if (sqrtf(w0 * w0 + w1 * w1 + w2 * w2) > 0.25f) {
+            if (a.seg)
+                atomicOr(a.status + a.seg[s], DPF_ERR_ROTATION);
+            else
+                flags |= DPF_ERR_ROTATION;
+        }
         const bool fx = a.fixed[s] != 0;
 #pragma unroll
         for (int c = 0; c < 6; ++c) {
@@ -1165,6 +1172,54 @@ __global__ void __launch_bounds__(kThreads) begin_sites(BeginArgs a) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Segmented (per-request) reductions and updates for batches of requests
+// stored as contiguous site ranges [seg_ptr[r], seg_ptr[r+1]).
+
+// out[r] = [|a|_2, max|a|, |b|_2 or a.b] over the segment's 6-vectors,
+// skipping masked sites (mask[s] != 0) when mask is given.  One block per
+// segment, fixed order: deterministic and independent of the other segments.
+__global__ void __launch_bounds__(kThreads) segment_norms_kernel(const int64_t *seg_ptr, const double *a,
+                                                                 const double *b, int b_dot, const uint8_t *mask,
+                                                                 double *out) {
+    const int r = blockIdx.x;
+    const int64_t e0 = 6 * seg_ptr[r], e1 = 6 * seg_ptr[r + 1];
+    double s2 = 0.0, mx = 0.0, t = 0.0;
+    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+        if (mask && mask[e / 6]) continue;
+        const double v = a[e];
+        s2 = fma(v, v, s2);
+        mx = fmax(mx, fabs(v));
+        if (b) t = fma(b_dot ? v : b[e], b[e], t);
+    }
+    s2 = block_sum(s2);
+    mx = block_max(mx);
+    t = block_sum(t);
+    if (threadIdx.x == 0) {
+        out[3 * r] = sqrt(s2);
+        out[3 * r + 1] = mx;
+        out[3 * r + 2] = b_dot ? t : sqrt(t);
+    }
+}
+
+// out = a + factor[seg[s]] * c on every site (factor 0 leaves a).
+__global__ void __launch_bounds__(kThreads) segment_axpy_kernel(int64_t n, const int32_t *seg, const double *factor,
+                                                                const double *a, const double *c, double *out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= 6 * n) return;
+    out[e] = fma(factor[seg[e / 6]], c[e], a[e]);
+}
+
+// out = keep[seg[s]] ? a : b  (per-segment select of 6-vectors).
+__global__ void __launch_bounds__(kThreads) segment_select_kernel(int64_t n, const int32_t *seg,
+                                                                  const uint8_t *keep, const double *a,
+                                                                  const double *b, double *out) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= 6 * n) return;
+    out[e] = keep[seg[e / 6]] ? a[e] : b[e];
+}
+
 }  // namespace mp
 }  // namespace dpf
 
@@ -1203,20 +1258,37 @@ int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_histor
     return DPF_OK;
 }
 
+int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const double *y, const float *y32,
+                                 const double *mass, const uint8_t *fixed, double dt, const double *r0,
+                                 int want_tangent, const float *preconditioner, const float *units32, double *residual,
+                                 double *scaled, double *norms, float *wrench, double *partials, int *status,
+                                 const int32_t *seg_bond, const int32_t *seg_site, void *stream);
+
 int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const float *y32, const double *mass,
                        const uint8_t *fixed, double dt, const double *r0, int want_tangent, const float *preconditioner,
                        const float *units32, double *residual, double *scaled, double *norms, float *wrench,
                        double *partials, int *status, void *stream) {
+    return dpf_mixed_residual_segmented(g, bond_data, y, y32, mass, fixed, dt, r0, want_tangent, preconditioner,
+                                        units32, residual, scaled, norms, wrench, partials, status, nullptr, nullptr,
+                                        stream);
+}
+
+int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const double *y, const float *y32,
+                                 const double *mass, const uint8_t *fixed, double dt, const double *r0,
+                                 int want_tangent, const float *preconditioner, const float *units32, double *residual,
+                                 double *scaled, double *norms, float *wrench, double *partials, int *status,
+                                 const int32_t *seg_bond, const int32_t *seg_site, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !y || !y32 || !mass || !fixed || !r0 || !residual || !status ||
         (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units32))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
-        ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, want_tangent, wrench, status};
+        ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, want_tangent, wrench, status,
+                           seg_bond};
         residual_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     ResidualSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, y, mass, r0, fixed, 0.5 * dt * dt,
-                       preconditioner, units32, residual, scaled, norms, partials, status};
+                       preconditioner, units32, residual, scaled, norms, partials, status, seg_site};
     residual_sites<<<reduce_grid(kGroupJ * g->n_sites), kThreads, 0, st>>>(s);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
@@ -1378,6 +1450,32 @@ int dpf_mixed_begin(int64_t n_sites, const double *loads, const double *mass, co
         return DPF_ERR_ARGUMENT;
     BeginArgs a{n_sites, loads, mass, v, external, fixed, dt, 0.5 * dt * dt, r0, scales, partials};
     begin_sites<<<reduce_grid(6 * n_sites), kThreads, 0, (cudaStream_t)stream>>>(a);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_segment_norms(int n_segments, const int64_t *seg_ptr, const double *a, const double *b, int b_dot,
+                      const uint8_t *mask, double *out, void *stream) {
+    if (n_segments <= 0 || !seg_ptr || !a || !out) return DPF_ERR_ARGUMENT;
+    segment_norms_kernel<<<n_segments, kThreads, 0, (cudaStream_t)stream>>>(seg_ptr, a, b, b_dot, mask, out);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_segment_axpy(int64_t n_sites, const int32_t *seg, const double *factor, const double *a, const double *c,
+                     double *out, void *stream) {
+    if (n_sites <= 0 || !seg || !factor || !a || !c || !out) return DPF_ERR_ARGUMENT;
+    segment_axpy_kernel<<<blocks_for(6 * n_sites, kThreads), kThreads, 0, (cudaStream_t)stream>>>(n_sites, seg, factor,
+                                                                                                    a, c, out);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_segment_select(int64_t n_sites, const int32_t *seg, const uint8_t *keep, const double *a, const double *b,
+                       double *out, void *stream) {
+    if (n_sites <= 0 || !seg || !keep || !a || !b || !out) return DPF_ERR_ARGUMENT;
+    segment_select_kernel<<<blocks_for(6 * n_sites, kThreads), kThreads, 0, (cudaStream_t)stream>>>(n_sites, seg, keep,
+                                                                                                      a, b, out);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -159,7 +159,7 @@ class LinearBonds:
         if scalars:
             self._host_scalars[:scalars].copy_(self._scalars[:scalars], non_blocking=True)
         if status:
-            self._host_status.copy_(self._status, non_blocking=True)
+            self._host_status.copy_(self._status[:1], non_blocking=True)
         stream.synchronize()
         return self._host_scalars[:scalars].tolist(), int(self._host_status[0]) if status else 0
 

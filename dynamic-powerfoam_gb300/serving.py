@@ -1,0 +1,491 @@
+"""Serving form: continuous batching of Newton solve requests on one GPU.
+
+A *batch* is the disjoint union of the active requests' bond graphs
+(concatenated sites, bonds and incidence lists, built on the device from the
+requests' resident tensors).  Every kernel launch of a batched Newton step
+covers all requests at once; each request still follows its own control flow
+of ``NewtonBonds.step`` (``experiments/bonded_dem_newton.py:132-201``):
+
+* per-request scalars (rhs scale, residual norm, pose defect, merit, work) come
+  from segmented reductions (``dpf_segment_norms``), guard failures from
+  per-request status words (``dpf_mixed_residual_segmented``);
+* a request that has converged is frozen: its rows of the Newton right-hand
+  side are zero, which keeps its blocks exactly zero through FGMRES and the
+  block-diagonal PCG, so its increment stays put while others iterate;
+* the backtracking line search runs with one step factor per request.
+
+The shared FGMRES/PCG over the batch only changes how accurately each Newton
+direction is computed, not the converged answer: every request stops at its
+own relative residual and pose tolerance, so a request's result agrees alone
+and in any mix within that tolerance.
+
+``Service`` admits requests by HBM footprint into free batch capacity at the
+boundaries of batched steps (requests arriving while a batch runs join the
+next one), keeps each request's state resident until it has done all its time
+steps, and records per-request latency.
+"""
+import ctypes
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .newton import MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64
+
+_PER_SITE = ('p', 'mass', 'fixed', 'radii', 'x', 'v', 'rotation', '_mass32')
+_PER_BOND = ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
+_STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
+
+
+class Batch(MixedNewtonBonds):
+    """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
+
+    def __init__(self, parts):
+        if not parts:
+            raise ValueError('empty batch')
+        first = parts[0]
+        self.parts = list(parts)
+        self.device = first.device
+        self._lib = first._lib
+        self.tensor = first.tensor
+        sites = [p.n_sites for p in parts]
+        bonds = [p.n_bonds for p in parts]
+        site_off = np.concatenate(([0], np.cumsum(sites)))
+        bond_off = np.concatenate(([0], np.cumsum(bonds)))
+        self.site_ptr = torch.as_tensor(site_off, dtype=torch.int64, device=self.device)
+        self.bond_ptr = bond_off
+        self.site_range = [(int(site_off[k]), int(site_off[k+1])) for k in range(len(parts))]
+        self.bond_range = [(int(bond_off[k]), int(bond_off[k+1])) for k in range(len(parts))]
+        n, m = int(site_off[-1]), int(bond_off[-1])
+        for name in _PER_SITE + _PER_BOND:
+            setattr(self, name, torch.cat([getattr(p, name).contiguous() for p in parts]))
+        self.edges = torch.cat([p.edges + int(site_off[k]) for k, p in enumerate(parts)]).contiguous()
+        self.i, self.j = self.edges.T
+        inc_ptr, inc_bond = [], []
+        inc_off = 0
+        for k, p in enumerate(parts):
+            ptr = p._inc_ptr.to(torch.int64)
+            inc_ptr.append((ptr[:-1] if k < len(parts) - 1 else ptr) + inc_off)
+            v = p._inc_bond.to(torch.int64)
+            inc_bond.append(torch.where(v >= 0, v + int(bond_off[k]), v - int(bond_off[k])))
+            inc_off += 2*p.n_bonds
+        self._inc_ptr = torch.cat(inc_ptr).to(torch.int32).contiguous()
+        self._inc_bond = torch.cat(inc_bond).to(torch.int32).contiguous()
+        self.seg_site = torch.repeat_interleave(torch.arange(len(parts), dtype=torch.int32, device=self.device),
+                                                torch.as_tensor(sites, device=self.device)).contiguous()
+        self.seg_bond = torch.repeat_interleave(torch.arange(len(parts), dtype=torch.int32, device=self.device),
+                                                torch.as_tensor(bonds, device=self.device)).contiguous()
+        self._graph = _lib.Graph(n, m, self.edges.data_ptr() if m else None, self._inc_ptr.data_ptr(),
+                                 self._inc_bond.data_ptr())
+        lib, dev, f32 = self._lib, self.device, torch.float32
+        self._wrench = torch.empty(max(1, 9*m), dtype=F64, device=dev)
+        self._partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=dev)
+        self._status = torch.zeros(max(1, len(parts)), dtype=torch.int32, device=dev)
+        self._scalars = torch.zeros(8, dtype=F64, device=dev)
+        self._host_status = torch.zeros(1, dtype=torch.int32).pin_memory()
+        self._host_scalars = torch.zeros(64, dtype=F64).pin_memory()
+        self.q = self.kq = self.diagonal = None
+        self.preconditioner, self.preconditioner_dt = None, None
+        self.time = 0.
+        self._inner = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._inner_host = 0
+        self._pcg_workspace = None
+        self._barrier = torch.zeros(2, dtype=torch.int32, device=dev)
+        self._krylov = None
+        self.block = self.units = None
+        self.profile = None
+        self._bond_data = torch.empty(max(4, lib.dpf_mixed_bond_floats(m)), dtype=f32, device=dev)
+        self._wrench32 = torch.empty(max(1, 9*m), dtype=f32, device=dev)
+        self._r0 = torch.empty((n, 6), dtype=F64, device=dev)
+        self._block32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
+        self._p32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
+        self._units = torch.empty((n, 6), dtype=F64, device=dev)
+        self._units32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._y32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._d32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n, m), dtype=f32, device=dev)
+        self._cached = None
+        self._loads = torch.empty((n, 6), dtype=F64, device=dev)
+        self._token = None
+        self._since_refresh = 0
+        self._seg_norms = torch.zeros((len(parts), 3), dtype=F64, device=dev)
+        self._seg_norms2 = torch.zeros((len(parts), 3), dtype=F64, device=dev)
+        self._host_seg = torch.zeros((2, len(parts), 3), dtype=F64).pin_memory()
+        self._host_seg_status = torch.zeros(len(parts), dtype=torch.int32).pin_memory()
+
+    @property
+    def n_segments(self):
+        return len(self.parts)
+
+    def scatter_state(self):
+        """Copy the batch's committed state back into the requests' own tensors."""
+        for k, p in enumerate(self.parts):
+            s0, s1 = self.site_range[k]
+            b0, b1 = self.bond_range[k]
+            for name in _STATE:
+                src = getattr(self, name)
+                part = src[s0:s1] if name in ('x', 'v', 'rotation') else src[b0:b1]
+                setattr(p, name, part.clone())
+            p.time = self.time
+
+    # ---- per-request reductions ---------------------------------------------------
+    def _segment(self, a, b=None, b_dot=False, mask=None, out=None):
+        out = self._seg_norms if out is None else out
+        self._call('dpf_segment_norms', self.n_segments, self.site_ptr.data_ptr(), a.data_ptr(),
+                   None if b is None else b.data_ptr(), int(b_dot), None if mask is None else mask.data_ptr(),
+                   out.data_ptr(), self._stream())
+        return out
+
+    def _fetch_segments(self, second=False, status=False):
+        self._host_seg[0].copy_(self._seg_norms, non_blocking=True)
+        if second:
+            self._host_seg[1].copy_(self._seg_norms2, non_blocking=True)
+        if status:
+            self._host_seg_status.copy_(self._status[:self.n_segments], non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        return (self._host_seg[0].numpy().copy(), self._host_seg[1].numpy().copy() if second else None,
+                self._host_seg_status.numpy().copy() if status else None)
+
+    def _residual_segmented(self, y, dt, want_tangent, use_p, scaled=None):
+        r = torch.empty_like(y)
+        self._to_y32(y)
+        self._status.zero_()
+        self._call('dpf_mixed_residual_segmented', ctypes.byref(self._graph), self._bond_data.data_ptr(),
+                   y.data_ptr(), self._y32.data_ptr(), self.mass.data_ptr(), self.fixed.data_ptr(), dt,
+                   self._r0.data_ptr(), int(want_tangent), self._p32.data_ptr() if use_p else None,
+                   self._units32.data_ptr() if use_p else None, r.data_ptr(),
+                   _addr_or_none(scaled) if use_p else None, None, self._wrench32.data_ptr(),
+                   self._partials.data_ptr(), self._status.data_ptr(), self.seg_bond.data_ptr(),
+                   self.seg_site.data_ptr(), self._stream())
+        return r
+
+    # ---- the batched Newton step ------------------------------------------------------
+    @torch.no_grad()
+    def step_batch(self, dt, external, tolerance=1e-6, max_iterations=12, *, pose_tolerance=2e-6,
+                   linear_tolerance=1e-6):
+        """One implicit-midpoint Newton solve for every request of the batch.
+
+        Returns one entry per request: ``(work, info)`` or the ``SubdivideError``
+        that request raised (its state is left untouched).
+        """
+        R, dt = self.n_segments, float(dt)
+        linear_tolerance = max(linear_tolerance, self.min_linear_tolerance)
+        external = self._vec(external)
+        self._v = self._vec(self.v).clone()
+        self._status.zero_()
+        MixedNewtonBonds._step_begin(self, dt, external)     # r0, maintained loads (global)
+        h = .5*dt*dt
+        rhs_vec = -(self._r0 + h*self._loads)                 # dt M v + dt^2/2 ext
+        self._segment(rhs_vec)
+        self._segment(self._loads, mask=self.fixed, out=self._seg_norms2)
+        first, second, _ = self._fetch_segments(second=True)
+        rhs_scale = np.maximum(np.maximum(first[:, 0], h*second[:, 0]), 1e-30)
+        y = torch.zeros_like(self._v)
+        n6 = 6*self.n_sites
+        stream = self._stream()
+        done = [None]*R                 # None: active; dict: converged info; Exception: failed
+        trace = [[] for _ in range(R)]
+        iters = np.zeros(R, dtype=np.int64)
+        krylov = np.zeros(R, dtype=np.int64)
+        cg = np.zeros(R, dtype=np.int64)
+        for iteration in range(max_iterations+1):
+            r = self._residual_segmented(y, dt, want_tangent=True, use_p=False)
+            self._call('dpf_mixed_scaling', ctypes.byref(self._graph), self._bond_data.data_ptr(),
+                       self._mass32.data_ptr(), self.fixed.data_ptr(), self.radii.data_ptr(), dt,
+                       self._block32.data_ptr(), self._p32.data_ptr(), self._units.data_ptr(),
+                       self._units32.data_ptr(), stream)
+            scaled = torch.empty_like(r)
+            self._call('dpf_mixed_scale_residual', self.n_sites, self._p32.data_ptr(), self._units32.data_ptr(),
+                       r.data_ptr(), scaled.data_ptr(), None, None, stream)
+            self._segment(r)
+            self._segment(scaled, out=self._seg_norms2)
+            rn, sn, status = self._fetch_segments(second=True, status=True)
+            for k in range(R):
+                if done[k] is not None:
+                    continue
+                if status[k]:
+                    done[k] = guard_error(int(status[k]))
+                    continue
+                relative, local = rn[k, 0]/rhs_scale[k], sn[k, 1]
+                if not (np.isfinite(relative) and np.isfinite(local)):
+                    done[k] = SubdivideError(f'Subdivide: non-finite Newton residual ({relative:g}, {local:g})')
+                    continue
+                trace[k].append([relative, local])
+                if relative < tolerance and local < pose_tolerance:
+                    done[k] = dict(nonlinear_iterations=iteration, nonlinear_relative_residual=relative,
+                                   local_pose_defect=local)
+            active = [k for k in range(R) if done[k] is None]
+            if not active:
+                break
+            if iteration == max_iterations:
+                for k in active:
+                    relative, local = trace[k][-1]
+                    done[k] = SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
+                break
+            keep = torch.zeros(R, dtype=torch.uint8)
+            keep[active] = 1
+            keep = keep.to(self.device)
+            rhs = torch.empty_like(scaled)
+            self._call('dpf_axpby', n6, -1., scaled.data_ptr(), 0., scaled.data_ptr(), rhs.data_ptr(), stream)
+            zero = torch.zeros_like(rhs)
+            self._call('dpf_segment_select', self.n_sites, self.seg_site.data_ptr(), keep.data_ptr(),
+                       rhs.data_ptr(), zero.data_ptr(), rhs.data_ptr(), stream)
+            if self._krylov is None or self._krylov.length != n6:
+                self._krylov = _Krylov(n6, 32, self.device)
+            self.inner_iterations = 0
+            delta, metrics = fgmres(self._newton_operator(y, dt, external), rhs, self._newton_preconditioner(dt),
+                                    tolerance=linear_tolerance, workspace=self._krylov)
+            inner = self.inner_iterations
+            for k in active:
+                krylov[k] += metrics['iterations']
+                cg[k] += inner
+                iters[k] = iteration + 1
+            correction = torch.empty_like(delta)
+            self._call('dpf_masked_scale', self.n_sites, delta.data_ptr(), self._units.data_ptr(),
+                       self.fixed.data_ptr(), correction.data_ptr(), stream)
+            merit = {k: sn[k, 2] for k in active}
+            factor = {k: 1. for k in active}
+            pending = list(active)
+            candidate = torch.empty_like(y)
+            for power in range(10):
+                f = np.zeros(R)
+                for k in pending:
+                    f[k] = factor[k]
+                fdev = torch.as_tensor(f, dtype=F64).to(self.device)
+                self._call('dpf_segment_axpy', self.n_sites, self.seg_site.data_ptr(), fdev.data_ptr(),
+                           y.data_ptr(), correction.data_ptr(), candidate.data_ptr(), stream)
+                cscaled = torch.empty_like(y)
+                self._residual_segmented(candidate, dt, want_tangent=False, use_p=True, scaled=cscaled)
+                self._segment(cscaled)
+                values, _, status = self._fetch_segments(status=True)
+                accept = torch.zeros(R, dtype=torch.uint8)
+                still = []
+                for k in pending:
+                    if status[k] == 0 and values[k, 0] < (1 - 1e-4*factor[k])*merit[k]:
+                        accept[k] = 1
+                    else:
+                        factor[k] *= .5
+                        still.append(k)
+                if int(accept.sum()):
+                    self._call('dpf_segment_select', self.n_sites, self.seg_site.data_ptr(),
+                               accept.to(self.device).data_ptr(), candidate.data_ptr(), y.data_ptr(),
+                               y.data_ptr(), stream)
+                pending = still
+                if not pending:
+                    break
+            for k in pending:
+                done[k] = SubdivideError('Subdivide: Newton line search failed')
+        # commit the converged requests; failed ones keep their state
+        failed = [k for k in range(R) if isinstance(done[k], Exception)]
+        if failed:
+            keep_y = torch.zeros(R, dtype=torch.uint8)
+            keep_y[[k for k in range(R) if k not in failed]] = 1
+            zero = torch.zeros_like(y)
+            self._call('dpf_segment_select', self.n_sites, self.seg_site.data_ptr(), keep_y.to(self.device).data_ptr(),
+                       y.data_ptr(), zero.data_ptr(), y.data_ptr(), stream)
+            saved = {name: getattr(self, name).clone() for name in _STATE}
+        self._accept(y, dt)
+        self.time += dt
+        if failed:
+            for k in failed:
+                s0, s1 = self.site_range[k]
+                b0, b1 = self.bond_range[k]
+                for name in _STATE:
+                    rows = slice(s0, s1) if name in ('x', 'v', 'rotation') else slice(b0, b1)
+                    getattr(self, name)[rows] = saved[name][rows]
+            self._token = None
+        self._segment(external, b=y, b_dot=True)
+        work, _, _ = self._fetch_segments()
+        out = []
+        for k in range(R):
+            if isinstance(done[k], Exception):
+                out.append(done[k])
+            else:
+                info = dict(done[k], krylov_iterations=int(krylov[k]), cg_iterations=int(cg[k]),
+                            residual_trace=trace[k])
+                out.append((float(work[k, 2]), info))
+        return out
+
+
+def _addr_or_none(t):
+    return None if t is None else t.data_ptr()
+
+
+# ---------------------------------------------------------------------------------
+# Requests and the continuous-batching service
+
+
+@dataclass(order=True)
+class Request:
+    """One served job: ``steps`` implicit Newton solves of one foam."""
+    arrival: float
+    rid: int = field(compare=False)
+    foam: dict = field(compare=False, repr=False)
+    load: np.ndarray = field(compare=False, repr=False)
+    dt: float = field(compare=False, default=1e-3)
+    steps: int = field(compare=False, default=1)
+    # filled by the service
+    solver: object = field(compare=False, default=None, repr=False)
+    done_steps: int = field(compare=False, default=0)
+    started: float = field(compare=False, default=None)
+    finished: float = field(compare=False, default=None)
+    infos: list = field(compare=False, default_factory=list, repr=False)
+    error: Exception = field(compare=False, default=None)
+
+    @property
+    def sites(self):
+        return len(self.foam['points'])
+
+    @property
+    def bonds(self):
+        return len(self.foam['pairs'])
+
+
+def footprint_bytes(sites, bonds):
+    """HBM bytes a resident request and its share of a batch take (upper estimate).
+
+    Per site: state and solver vectors (float64 and float32 copies, 6x6 blocks,
+    FGMRES basis of 33 + 32 vectors of 6 doubles); per bond: float64 state and
+    tangent, float32 records/tangent and wrench scratch.
+    """
+    per_site = 8*(3 + 6 + 9 + 6 + 1) + 8*6*12 + 4*36*2 + 4*6*10 + 8*6*65
+    per_bond = 8*(2 + 3*8 + 4*2) + 4*(44 + 9*2 + 12) + 8*9 + 8
+    return int(2*(per_site*sites + per_bond*bonds))
+
+
+class Service:
+    """Continuous batching of solve requests under an HBM budget.
+
+    ``run(requests)`` plays the request stream in real time (``arrival`` in
+    seconds from the start): a request is constructed (resident state on the
+    device) once it has arrived, admitted when its footprint fits the budget
+    and the batch has room, and solved by batched Newton steps together with
+    every other admitted request.  Requests that arrive while a batch step is
+    running join at the next step boundary.  Latency = completion - arrival.
+    """
+
+    def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=2_000_000, tolerance=1e-6,
+                 solver_cls=MixedNewtonBonds):
+        self.device = torch.device(device)
+        self.hbm_budget = float(hbm_budget)
+        self.max_batch_sites = int(max_batch_sites)
+        self.tolerance = float(tolerance)
+        self.solver_cls = solver_cls
+        self.in_use = 0.
+        self.batches = 0
+
+    def _construct(self, req):
+        f = req.foam
+        req.solver = self.solver_cls(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
+                                     young=f['young'], shear=f['shear'], device=self.device)
+        req.load_dev = req.solver.tensor(req.load)
+
+    def run(self, requests, clock=time.perf_counter):
+        pending = sorted(requests)
+        waiting, active, finished = [], [], []
+        t0 = clock()
+        now = lambda: clock() - t0
+        batch, members = None, None
+        while pending or waiting or active:
+            while pending and pending[0].arrival <= now():
+                req = pending.pop(0)
+                self._construct(req)
+                waiting.append(req)
+            changed = False
+            sites = sum(r.sites for r in active)
+            while waiting:
+                req = waiting[0]
+                need = footprint_bytes(req.sites, req.bonds)
+                if self.in_use + need > self.hbm_budget or (active and sites + req.sites > self.max_batch_sites):
+                    break
+                waiting.pop(0)
+                self.in_use += need
+                req.started = now()
+                active.append(req)
+                sites += req.sites
+                changed = True
+            if not active:
+                if pending:
+                    time.sleep(max(0., min(pending[0].arrival - now(), .001)))
+                continue
+            if changed or batch is None:
+                if batch is not None:
+                    batch.scatter_state()
+                batch = Batch([r.solver for r in active])
+                members = list(active)
+            ext = torch.cat([r.load_dev for r in members])
+            results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
+            self.batches += 1
+            leaving = []
+            for req, res in zip(members, results):
+                if isinstance(res, Exception):
+                    req.error = res
+                    leaving.append(req)
+                    continue
+                req.infos.append(res[1])
+                req.done_steps += 1
+                if req.done_steps >= req.steps:
+                    leaving.append(req)
+            if leaving:
+                batch.scatter_state()
+                stamp = now()
+                for req in leaving:
+                    req.finished = stamp
+                    active.remove(req)
+                    finished.append(req)
+                    self.in_use -= footprint_bytes(req.sites, req.bonds)
+                batch = None
+        return finished
+
+
+def latency_stats(finished):
+    lat = np.array([r.finished - r.arrival for r in finished if r.error is None])
+    if not len(lat):
+        return dict(p50=None, p99=None, mean=None)
+    return dict(p50=float(np.percentile(lat, 50)), p99=float(np.percentile(lat, 99)), mean=float(lat.mean()))
+
+
+# ---------------------------------------------------------------------------------
+# Synthetic request stream (the mixed-size served workload)
+
+def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, strain=None, seed=0):
+    """A jittered ``m^3`` foam with box aspect ratios, material and top load.
+
+    The top layer (unit z > 0.95) carries a compressive force equivalent to the
+    nominal strain ``strain`` of a bar of the foam's height: E * strain * (top
+    area) spread over the top sites; gravity acts on every free site.
+    """
+    from .foam import jittered_lattice_foam, gravity_load
+    aspect = rng.uniform(.5, 2., 3) if aspect is None else np.asarray(aspect, dtype=float)
+    young = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6)))) if young is None else young
+    poisson = float(rng.uniform(.2, .4)) if poisson is None else poisson
+    strain = float(rng.uniform(.01, .1)) if strain is None else strain
+    foam = jittered_lattice_foam(m, seed=seed, aspect=aspect, young=young, poisson=poisson)
+    load = gravity_load(foam)
+    top = foam['unit'][:, 2] > .95
+    top &= ~foam['fixed']
+    if top.any():
+        load[top, 2] -= young*strain*aspect[0]*aspect[1]/top.sum()
+    return foam, load
+
+
+def synthetic_stream(count, seed=0, sites=(1024, 131072), rate=None, buckets=8, steps=1):
+    """Mixed-size requests: site counts log-uniform in ``sites`` (rounded to
+    ``buckets`` lattice sizes so that foams can be generated once per size),
+    random aspect ratios, E log-uniform [1e4, 1e6], nu U[0.2, 0.4], top strain
+    U[1%, 10%]; Poisson arrivals at ``rate`` per second (None: all at t=0)."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(sites[0])/3, np.log(sites[1])/3
+    sizes = np.unique(np.round(np.exp(np.linspace(lo, hi, buckets))).astype(int))
+    arrival = 0.
+    out = []
+    for rid in range(count):
+        target = np.exp(rng.uniform(np.log(sites[0]), np.log(sites[1])))
+        m = int(sizes[np.argmin(abs(np.log(sizes**3) - np.log(target)))])
+        foam, load = compressed_foam_request(m, rng, seed=seed*1000 + m)
+        if rate:
+            arrival += float(rng.exponential(1./rate))
+        out.append(Request(arrival=arrival, rid=rid, foam=foam, load=load, steps=steps))
+    return out

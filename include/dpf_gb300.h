@@ -350,6 +350,35 @@ int dpf_mixed_begin(int64_t n_sites, const double *loads, const double *mass, co
                     const double *external, const uint8_t *fixed, double dt, double *r0,
                     double *scales, double *partials, void *stream);
 
+/* ---- Batches of requests: contiguous per-request site ranges ----
+ * A batch concatenates the graphs of several requests (sites and bonds of
+ * request r in one contiguous range each).  These entry points keep every
+ * request's scalars separate, so a request follows its own Newton control
+ * (experiments/bonded_dem_newton.py:132-201) inside the batch. */
+
+/* dpf_mixed_residual with guard bits per request: status[seg_site[s]] and
+ * status[seg_bond[b]] (status is an array of request ints). */
+int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const double *y,
+                                 const float *y32, const double *mass, const uint8_t *fixed, double dt,
+                                 const double *r0, int want_tangent, const float *preconditioner,
+                                 const float *units32, double *residual, double *scaled,
+                                 double *norms, float *wrench, double *partials, int *status,
+                                 const int32_t *seg_bond, const int32_t *seg_site, void *stream);
+
+/* Per-request [|a|_2, max|a|, |b|_2] (or [.., .., a.b] with b_dot) over the
+ * 6-vectors of sites seg_ptr[r] .. seg_ptr[r+1]-1, skipping sites with mask
+ * != 0 when mask is given; out: 3 doubles per request (device). */
+int dpf_segment_norms(int n_segments, const int64_t *seg_ptr, const double *a, const double *b,
+                      int b_dot, const uint8_t *mask, double *out, void *stream);
+
+/* out = a + factor[seg[s]] * c for every site's 6-vector (factor: device doubles). */
+int dpf_segment_axpy(int64_t n_sites, const int32_t *seg, const double *factor, const double *a,
+                     const double *c, double *out, void *stream);
+
+/* out = keep[seg[s]] ? a : b for every site's 6-vector. */
+int dpf_segment_select(int64_t n_sites, const int32_t *seg, const uint8_t *keep, const double *a,
+                       const double *b, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,89 @@
+"""Serving form: batched Newton steps over concatenated graphs and the
+continuous-batching service.  A request's result must agree alone and in the
+mix within the solve tolerance: both runs satisfy the float64-accurate relative
+residual 1e-6 of their own request, and positions agree to 1e-5 of the step's
+displacement."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip('torch')
+
+
+@pytest.fixture(scope='module', autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip('needs a CUDA GPU')
+
+
+def _solver(req):
+    import dpf_gb300
+    f = req.foam
+    return dpf_gb300.MixedNewtonBonds(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
+                                      young=f['young'], shear=f['shear'])
+
+
+def _alone(req, steps):
+    s = _solver(req)
+    x0 = s.x.clone()
+    for _ in range(steps):
+        s.step(req.dt, s.tensor(req.load), tolerance=1e-6)
+    return s, x0
+
+
+def test_batch_matches_alone():
+    from dpf_gb300 import serving
+    reqs = serving.synthetic_stream(4, seed=3, sites=(800, 9000))
+    parts = [_solver(r) for r in reqs]
+    batch = serving.Batch(parts)
+    ext = torch.cat([p.tensor(r.load) for p, r in zip(parts, reqs)])
+    for step in range(2):
+        results = batch.step_batch(1e-3, ext, tolerance=1e-6)
+        for res in results:
+            assert not isinstance(res, Exception), res
+            assert res[1]['nonlinear_relative_residual'] < 1e-6
+    batch.scatter_state()
+    for req, part in zip(reqs, parts):
+        alone, x0 = _alone(req, 2)
+        disp = float(torch.linalg.vector_norm(alone.x - x0))
+        err = float(torch.linalg.vector_norm(part.x - alone.x))/disp
+        assert err < 1e-5, err
+        ev = float(torch.linalg.vector_norm(part.v - alone.v)/torch.linalg.vector_norm(alone.v))
+        assert ev < 1e-4, ev
+
+
+def test_failed_request_is_isolated():
+    """A request whose step trips a guard fails alone; the others commit."""
+    from dpf_gb300 import serving
+    reqs = serving.synthetic_stream(3, seed=5, sites=(800, 3000))
+    reqs[1].load = reqs[1].load*1e7          # rotation/turn guards everywhere
+    parts = [_solver(r) for r in reqs]
+    before = {k: getattr(parts[1], k).clone() for k in ('x', 'v', 'fn', 'fs')}
+    batch = serving.Batch(parts)
+    ext = torch.cat([p.tensor(r.load) for p, r in zip(parts, reqs)])
+    results = batch.step_batch(1e-3, ext, tolerance=1e-6)
+    assert isinstance(results[1], RuntimeError) and 'Subdivide:' in str(results[1])
+    assert not isinstance(results[0], Exception) and not isinstance(results[2], Exception)
+    batch.scatter_state()
+    for k, v in before.items():
+        assert torch.equal(getattr(parts[1], k), v), k
+    alone, x0 = _alone(reqs[0], 1)
+    err = float(torch.linalg.vector_norm(parts[0].x - alone.x)/torch.linalg.vector_norm(alone.x - x0))
+    assert err < 1e-5, err
+
+
+def test_service_stream_with_arrivals():
+    from dpf_gb300 import serving
+    reqs = serving.synthetic_stream(6, seed=7, sites=(700, 6000), rate=200., steps=2)
+    service = serving.Service(hbm_budget=4e9, max_batch_sites=12000)
+    finished = service.run(reqs)
+    assert len(finished) == 6
+    assert all(r.error is None and r.done_steps == 2 for r in finished)
+    stats = serving.latency_stats(finished)
+    assert stats['p50'] > 0 and stats['p99'] >= stats['p50']
+    assert service.batches >= 2
+    for req in finished[:3]:
+        alone, x0 = _alone(req, 2)
+        err = float(torch.linalg.vector_norm(req.solver.x - alone.x)/torch.linalg.vector_norm(alone.x - x0))
+        assert err < 1e-5, err
