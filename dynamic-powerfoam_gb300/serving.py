@@ -224,19 +224,27 @@ class Batch(MixedNewtonBonds):
                     relative, local = trace[k][-1]
                     done[k] = SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
                 break
-            keep = torch.zeros(R, dtype=torch.uint8)
-            keep[active] = 1
-            keep = keep.to(self.device)
+            # Each active request's block of the right-hand side is normalised to
+            # unit norm (frozen requests: zero), so the shared Krylov tolerance
+            # bounds every request's own relative linear residual by tol*sqrt(R).
+            scale = np.zeros(R)
+            for k in active:
+                scale[k] = -1./max(sn[k, 2], 1e-300)
+            sdev = torch.as_tensor(scale, dtype=F64).to(self.device)
+            zero = torch.zeros_like(scaled)
             rhs = torch.empty_like(scaled)
-            self._call('dpf_axpby', n6, -1., scaled.data_ptr(), 0., scaled.data_ptr(), rhs.data_ptr(), stream)
-            zero = torch.zeros_like(rhs)
-            self._call('dpf_segment_select', self.n_sites, self.seg_site.data_ptr(), keep.data_ptr(),
-                       rhs.data_ptr(), zero.data_ptr(), rhs.data_ptr(), stream)
+            self._call('dpf_segment_axpy', self.n_sites, self.seg_site.data_ptr(), sdev.data_ptr(), zero.data_ptr(),
+                       scaled.data_ptr(), rhs.data_ptr(), stream)
             if self._krylov is None or self._krylov.length != n6:
                 self._krylov = _Krylov(n6, 32, self.device)
             self.inner_iterations = 0
             delta, metrics = fgmres(self._newton_operator(y, dt, external), rhs, self._newton_preconditioner(dt),
-                                    tolerance=linear_tolerance, workspace=self._krylov)
+                                    tolerance=linear_tolerance/np.sqrt(len(active)), workspace=self._krylov)
+            unscale = torch.as_tensor(np.where(scale != 0, -1./np.where(scale != 0, scale, 1.), 0.),
+                                      dtype=F64).to(self.device)
+            delta = delta.contiguous()
+            self._call('dpf_segment_axpy', self.n_sites, self.seg_site.data_ptr(), unscale.data_ptr(),
+                       zero.data_ptr(), delta.data_ptr(), delta.data_ptr(), stream)
             inner = self.inner_iterations
             for k in active:
                 krylov[k] += metrics['iterations']
