@@ -229,7 +229,7 @@ class Batch(MixedNewtonBonds):
             # bounds every request's own relative linear residual by tol*sqrt(R).
             scale = np.zeros(R)
             for k in active:
-                scale[k] = -1./max(sn[k, 2], 1e-300)
+                scale[k] = -1./max(sn[k, 0], 1e-300)
             sdev = torch.as_tensor(scale, dtype=F64).to(self.device)
             zero = torch.zeros_like(scaled)
             rhs = torch.empty_like(scaled)
@@ -253,7 +253,7 @@ class Batch(MixedNewtonBonds):
             correction = torch.empty_like(delta)
             self._call('dpf_masked_scale', self.n_sites, delta.data_ptr(), self._units.data_ptr(),
                        self.fixed.data_ptr(), correction.data_ptr(), stream)
-            merit = {k: sn[k, 2] for k in active}
+            merit = {k: sn[k, 0] for k in active}
             factor = {k: 1. for k in active}
             pending = list(active)
             candidate = torch.empty_like(y)
