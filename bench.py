@@ -53,6 +53,10 @@ def parse():
     p.add_argument('--precision', default='mixed', choices=('mixed', 'f64'))
     p.add_argument('--plain-steps', type=int, default=3,
                    help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
+    p.add_argument('--served', type=int, default=512, help='requests of the served mixed-size stream (0: skip)')
+    p.add_argument('--served-plain', type=int, default=64,
+                   help='requests of the same stream solved one at a time by the plain float64 solver')
+    p.add_argument('--served-rate', type=float, default=4000., help='Poisson arrival rate of the stream (1/s)')
     return p.parse_args()
 
 
@@ -139,6 +143,60 @@ class ClockSampler:
         reasons = sorted({n for r in rows for n, v in zip(names, r[4:8]) if v.lower() == 'active'})
         return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
                     reasons=reasons, samples=len(rows))
+
+
+def run_served(args, device):
+    """Served stream vs the plain float64 solver (one request at a time).
+
+    Stream: ``args.served`` requests, site counts log-uniform 1,024-131,072,
+    box aspect U[0.5, 2], E log-uniform [1e4, 1e6], nu U[0.2, 0.4], top strain
+    U[1%, 10%] (as a top load), Poisson arrivals; one implicit Newton solve per
+    request at relative residual 1e-6.  Served: continuous batching of mixed-
+    precision batched Newton steps under a 150 GB HBM budget.  Plain: float64
+    ``NewtonBonds`` constructed and solved per request in arrival order.
+    Latency = completion - arrival, request construction included in both arms.
+    """
+    import torch
+    import dpf_gb300
+    from dpf_gb300 import serving
+    stream = serving.synthetic_stream(args.served, seed=11, sites=(1024, 131072), rate=args.served_rate)
+    warm = serving.synthetic_stream(4, seed=12, sites=(1024, 4096))
+    serving.Service(device=device).run(warm)
+    torch.cuda.synchronize()
+    service = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=2_000_000)
+    t0 = time.perf_counter()
+    finished = service.run(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ok = [r for r in finished if r.error is None]
+    stats = serving.latency_stats(finished)
+    served = dict(requests=len(stream), solved=len(ok), failed=len(stream) - len(ok), wall_s=wall,
+                  solves_per_s=len(ok)/wall, p50_ms=1e3*stats['p50'], p99_ms=1e3*stats['p99'],
+                  batched_steps=service.batches, sites=int(sum(r.sites for r in stream)),
+                  newton_per_solve=float(np.mean([r.infos[0]['nonlinear_iterations'] for r in ok])),
+                  max_relative_residual=float(max(r.infos[0]['nonlinear_relative_residual'] for r in ok)))
+    del finished, ok, stream
+    plain = None
+    if args.served_plain > 0:
+        stream = serving.synthetic_stream(args.served_plain, seed=11, sites=(1024, 131072), rate=args.served_rate)
+        lat = []
+        t0 = time.perf_counter()
+        for req in stream:
+            wait = req.arrival - (time.perf_counter() - t0)
+            if wait > 0:
+                time.sleep(wait)
+            f = req.foam
+            s = dpf_gb300.NewtonBonds(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
+                                      young=f['young'], shear=f['shear'], device=device)
+            s.step(req.dt, s.tensor(req.load), tolerance=args.tolerance)
+            lat.append(time.perf_counter() - t0 - req.arrival)
+        torch.cuda.synchronize()
+        pwall = time.perf_counter() - t0
+        plain = dict(requests=len(stream), solves_per_s=len(stream)/pwall, p50_ms=1e3*float(np.percentile(lat, 50)),
+                     p99_ms=1e3*float(np.percentile(lat, 99)), dtype='f64', sample='first requests of the same stream')
+        served['speedup_vs_plain'] = served['solves_per_s']/plain['solves_per_s']
+    served['plain_f64'] = plain
+    return served
 
 
 def run_reference(args):
@@ -283,6 +341,7 @@ def run_ours(args):
                     traffic=None, peak_source='measured' if peaks else 'fallback',
                     launches=kernels[dominant]['launches'], mean_ms=kernels[dominant]['mean_ms'])
 
+    served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None
     if rank != 0:
         return
     cpu = None
@@ -306,7 +365,7 @@ def run_ours(args):
                             krylov_per_solve=mean('krylov_iterations'), cg_per_solve=mean('cg_iterations')),
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
-                gpu_launches=launches, kernels=kernels, roofline=roof, cpu_baseline=cpu, plain_f64=plain,
+                gpu_launches=launches, kernels=kernels, roofline=roof, cpu_baseline=cpu, plain_f64=plain, served=served,
                 relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)

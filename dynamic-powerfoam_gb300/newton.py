@@ -66,6 +66,41 @@ def incidence(edges, n_sites):
     return ptr.astype(np.int32), value[order].astype(np.int32)
 
 
+def bond_setup(points, radii, pairs, areas, contacts, masses, young, shear):
+    """Host-side setup arithmetic of ``LinearBondsGPU.__init__``
+    (``experiments/bonded_dem_linear_gpu.py:15-40``): bond normals, contact
+    levers, stiffnesses kn = E A/L, ks = G A/L, kb = E I/L, kt = 2 G I/L with
+    I = A^2/(4 pi), and the (N, 6) mass [m, m, m, 0.4 m r^2 x 3]."""
+    p = np.array(points, dtype=np.float64)
+    edges = np.array(pairs, dtype=np.int64).reshape(-1, 2)
+    if len(edges) and (edges.min() < 0 or edges.max() >= len(p)):
+        raise ValueError('Invalid endpoint index')
+    r = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
+    area = np.broadcast_to(np.asarray(areas, dtype=np.float64), (len(edges),))
+    c = np.asarray(contacts, dtype=np.float64).reshape(-1, 3)
+    i, j = edges[:, 0], edges[:, 1]
+    distance = p[j] - p[i]
+    length = np.linalg.norm(distance, axis=1)
+    second = area**2/(4*np.pi)
+    mass = np.broadcast_to(np.asarray(masses, dtype=np.float64), (len(p),))
+    inertia = .4*mass*r*r
+    mass6 = np.concatenate((np.repeat(mass[:, None], 3, 1), np.repeat(inertia[:, None], 3, 1)), 1)
+    if np.any(mass6 <= 0):
+        raise ValueError('Only positive-mass bodies can enter this solver')
+    return dict(p=p, edges=edges, n=distance/length[:, None], ri=c - p[i], rj=c - p[j], kn=young*area/length,
+                ks=shear*area/length, kb=young*second/length, kt=shear*(2*second)/length, mass=mass6)
+
+
+def classical_contacts(points, radii, pairs):
+    """Classical ball contacts ``bonded_dem_finite_gpu.py:49-53``: midpoint shifted by the radius difference."""
+    p = np.asarray(points, dtype=np.float64)
+    i, j = np.asarray(pairs, dtype=np.int64).reshape(-1, 2).T
+    radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
+    n = p[j] - p[i]
+    n /= np.linalg.norm(n, axis=1)[:, None]
+    return .5*(p[i] + p[j]) + .5*(radii_a[i] - radii_a[j])[:, None]*n
+
+
 class LinearBonds:
     """Stress-free linearised bonds (drop-in for ``LinearBondsGPU``,
     ``experiments/bonded_dem_linear_gpu.py:14-124``)."""
@@ -80,30 +115,14 @@ class LinearBonds:
         self._lib = _lib.load()
         self.tensor = lambda x: torch.as_tensor(x, dtype=F64, device=self.device)
         # Setup arithmetic (bonded_dem_linear_gpu.py:15-40) on the host, once.
-        p = np.array(points, dtype=np.float64)
-        edges = np.array(pairs, dtype=np.int64).reshape(-1, 2)
-        if len(edges) and (edges.min() < 0 or edges.max() >= len(p)):
-            raise ValueError('Invalid endpoint index')
-        r = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
-        area = np.broadcast_to(np.asarray(areas, dtype=np.float64), (len(edges),))
-        c = np.asarray(contacts, dtype=np.float64).reshape(-1, 3)
-        i, j = edges[:, 0], edges[:, 1]
-        distance = p[j] - p[i]
-        length = np.linalg.norm(distance, axis=1)
-        second = area**2/(4*np.pi)
-        mass = np.broadcast_to(np.asarray(masses, dtype=np.float64), (len(p),))
-        inertia = .4*mass*r*r
-        mass6 = np.concatenate((np.repeat(mass[:, None], 3, 1), np.repeat(inertia[:, None], 3, 1)), 1)
-        if np.any(mass6 <= 0):
-            raise ValueError('Only positive-mass bodies can enter this solver')
+        h = bond_setup(points, radii, pairs, areas, contacts, masses, young, shear)
+        p, edges = h['p'], h['edges']
         self.p = self.tensor(p)
         self.edges = torch.as_tensor(edges, dtype=torch.long, device=self.device).contiguous()
         self.i, self.j = self.edges.T
-        self.n = self.tensor(distance/length[:, None])
-        self.ri, self.rj = self.tensor(c - p[i]), self.tensor(c - p[j])
-        self.kn, self.ks = self.tensor(young*area/length), self.tensor(shear*area/length)
-        self.kb, self.kt = self.tensor(young*second/length), self.tensor(shear*(2*second)/length)
-        self.mass = self.tensor(mass6)
+        self.n, self.ri, self.rj = self.tensor(h['n']), self.tensor(h['ri']), self.tensor(h['rj'])
+        self.kn, self.ks, self.kb, self.kt = (self.tensor(h[k]) for k in ('kn', 'ks', 'kb', 'kt'))
+        self.mass = self.tensor(h['mass'])
         self.fixed = torch.as_tensor(np.asarray(fixed, dtype=bool), device=self.device)
         ptr, inc = incidence(edges, len(p))
         self._inc_ptr = torch.as_tensor(ptr, device=self.device)
@@ -246,11 +265,8 @@ class FiniteBonds(LinearBonds):
     def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None,
                  young=1200., shear=480., device='cuda'):
         p = np.asarray(points, dtype=np.float64)
-        i, j = np.asarray(pairs, dtype=np.int64).reshape(-1, 2).T
         radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
-        n = p[j] - p[i]
-        n /= np.linalg.norm(n, axis=1)[:, None]
-        classical = .5*(p[i] + p[j]) + .5*(radii_a[i] - radii_a[j])[:, None]*n
+        classical = classical_contacts(p, radii_a, pairs)
         if contacts is None:
             contacts = classical
         contacts = np.asarray(contacts, dtype=np.float64)

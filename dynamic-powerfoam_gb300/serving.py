@@ -32,11 +32,50 @@ import numpy as np
 import torch
 
 from . import _lib
-from .newton import MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64
+from .newton import (MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64, bond_setup,
+                     classical_contacts, incidence)
 
 _PER_SITE = ('p', 'mass', 'fixed', 'radii', 'x', 'v', 'rotation', '_mass32')
 _PER_BOND = ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
 _STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
+
+
+class RequestState:
+    """Resident state of one request: exactly what a ``Batch`` concatenates
+    (the attributes of a fresh ``MixedNewtonBonds``, without solver scratch)."""
+
+    def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None, young=1200., shear=480.,
+                 device='cuda'):
+        self.device = torch.device(device)
+        if self.device.index is None:
+            self.device = torch.device('cuda', torch.cuda.current_device())
+        self._lib = _lib.load()
+        t = self.tensor = lambda a: torch.as_tensor(a, dtype=F64, device=self.device)
+        p = np.asarray(points, dtype=np.float64)
+        radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
+        classical = classical_contacts(p, radii_a, pairs)
+        contacts = classical if contacts is None else np.asarray(contacts, dtype=np.float64)
+        h = bond_setup(p, radii_a, pairs, areas, contacts, masses, young, shear)
+        self.n_sites, self.n_bonds = len(p), len(h['edges'])
+        self.p = self.x = t(p)
+        self.x = self.p.clone()
+        self.edges = torch.as_tensor(h['edges'], dtype=torch.long, device=self.device).contiguous()
+        self.n, self.ri, self.rj = t(h['n']), t(h['ri']), t(h['rj'])
+        self.kn, self.ks, self.kb, self.kt = (t(h[k]) for k in ('kn', 'ks', 'kb', 'kt'))
+        self.mass = t(h['mass'])
+        self._mass32 = self.mass.float()
+        self.fixed = torch.as_tensor(np.asarray(fixed, dtype=bool), device=self.device)
+        self.radii = t(np.array(radii_a))
+        self.normal = self.n.clone()
+        self.offset = t(contacts - classical)
+        self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
+        self.fs, self.mb = torch.zeros_like(self.n), torch.zeros_like(self.n)
+        self.v = torch.zeros_like(self.mass)
+        self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(self.n_sites, 1, 1)
+        ptr, inc = incidence(h['edges'], self.n_sites)
+        self._inc_ptr = torch.as_tensor(ptr, device=self.device)
+        self._inc_bond = torch.as_tensor(inc, device=self.device)
+        self.time = 0.
 
 
 class Batch(MixedNewtonBonds):
@@ -375,7 +414,7 @@ class Service:
     """
 
     def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=2_000_000, tolerance=1e-6,
-                 solver_cls=MixedNewtonBonds):
+                 solver_cls=RequestState):
         self.device = torch.device(device)
         self.hbm_budget = float(hbm_budget)
         self.max_batch_sites = int(max_batch_sites)
@@ -458,22 +497,41 @@ def latency_stats(finished):
 # ---------------------------------------------------------------------------------
 # Synthetic request stream (the mixed-size served workload)
 
-def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, strain=None, seed=0):
-    """A jittered ``m^3`` foam with box aspect ratios, material and top load.
+_UNIT_FOAMS = {}
 
-    The top layer (unit z > 0.95) carries a compressive force equivalent to the
-    nominal strain ``strain`` of a bar of the foam's height: E * strain * (top
-    area) spread over the top sites; gravity acts on every free site.
+
+def _unit_foam(m, seed):
+    """Jittered unit-cube foam of lattice size m (bond graph computed once per (m, seed))."""
+    from .foam import jittered_lattice_foam
+    key = (m, seed)
+    if key not in _UNIT_FOAMS:
+        _UNIT_FOAMS[key] = jittered_lattice_foam(m, seed=seed)
+    return _UNIT_FOAMS[key]
+
+
+def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, strain=None, seed=0, density=1000.):
+    """A jittered ``m^3`` foam stretched by box aspect ratios, with its material and top load.
+
+    The bond graph is that of the unit-cube foam (computed once per lattice
+    size); positions, cross sections, masses and lever radii follow the
+    stretched box.  The top layer (unit z > 0.95) carries a compressive force
+    equivalent to the nominal strain ``strain``: E * strain * (top area) spread
+    over the top sites; gravity acts on every free site.
     """
-    from .foam import jittered_lattice_foam, gravity_load
+    from .foam import gravity_load
+    base = _unit_foam(m, seed)
     aspect = rng.uniform(.5, 2., 3) if aspect is None else np.asarray(aspect, dtype=float)
     young = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6)))) if young is None else young
     poisson = float(rng.uniform(.2, .4)) if poisson is None else poisson
     strain = float(rng.uniform(.01, .1)) if strain is None else strain
-    foam = jittered_lattice_foam(m, seed=seed, aspect=aspect, young=young, poisson=poisson)
+    h = base['h']
+    scale = float(np.prod(aspect))**(1/3)
+    foam = dict(points=base['unit']*aspect, radii=np.full(len(base['unit']), .5*h*scale), pairs=base['pairs'],
+                areas=rng.uniform(.5, 1., len(base['pairs']))*(h*scale)**2,
+                masses=np.full(len(base['unit']), density*h**3*float(np.prod(aspect))), fixed=base['fixed'],
+                contacts=None, young=young, shear=young/(2*(1+poisson)), h=h, unit=base['unit'])
     load = gravity_load(foam)
-    top = foam['unit'][:, 2] > .95
-    top &= ~foam['fixed']
+    top = (base['unit'][:, 2] > .95) & ~base['fixed']
     if top.any():
         load[top, 2] -= young*strain*aspect[0]*aspect[1]/top.sum()
     return foam, load
@@ -481,9 +539,10 @@ def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, st
 
 def synthetic_stream(count, seed=0, sites=(1024, 131072), rate=None, buckets=8, steps=1):
     """Mixed-size requests: site counts log-uniform in ``sites`` (rounded to
-    ``buckets`` lattice sizes so that foams can be generated once per size),
-    random aspect ratios, E log-uniform [1e4, 1e6], nu U[0.2, 0.4], top strain
-    U[1%, 10%]; Poisson arrivals at ``rate`` per second (None: all at t=0)."""
+    ``buckets`` lattice sizes so that bond graphs are generated once per size),
+    random box aspect ratios U[0.5, 2], E log-uniform [1e4, 1e6], nu U[0.2, 0.4],
+    top strain U[1%, 10%]; Poisson arrivals at ``rate`` per second (None: all
+    at t = 0)."""
     rng = np.random.default_rng(seed)
     lo, hi = np.log(sites[0])/3, np.log(sites[1])/3
     sizes = np.unique(np.round(np.exp(np.linspace(lo, hi, buckets))).astype(int))
@@ -492,7 +551,7 @@ def synthetic_stream(count, seed=0, sites=(1024, 131072), rate=None, buckets=8, 
     for rid in range(count):
         target = np.exp(rng.uniform(np.log(sites[0]), np.log(sites[1])))
         m = int(sizes[np.argmin(abs(np.log(sizes**3) - np.log(target)))])
-        foam, load = compressed_foam_request(m, rng, seed=seed*1000 + m)
+        foam, load = compressed_foam_request(m, rng, seed=seed)
         if rate:
             arrival += float(rng.exponential(1./rate))
         out.append(Request(arrival=arrival, rid=rid, foam=foam, load=load, steps=steps))
