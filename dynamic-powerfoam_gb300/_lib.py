@@ -62,6 +62,7 @@ SIGNATURES = {
     'dpf_elastic_precondition': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp, vp, vp, vp, f64, f64, i32,
                                        vp, vp, vp, vp, vp, vp, vp]),
     'dpf_loads': (i32, [P(Graph), P(History), vp, vp, vp]),
+    'dpf_bond_setup': (i32, [i64, i64, vp, vp, vp, vp, vp, vp, f64, f64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_accept_step': (i32, [i64, vp, f64, vp, vp, vp]),
     'dpf_energy': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, vp]),
     'dpf_arnoldi_cgs2': (i32, [i64, vp, i64, i32, vp, vp, vp, vp]),
@@ -98,7 +99,7 @@ SIGNATURES = {
 KERNELS = {
     'dpf_stiffness_apply': 2, 'dpf_diagonal_blocks': 1, 'dpf_prepare_scaling': 1, 'dpf_trial': 2,
     'dpf_residual': 2, 'dpf_scale_residual': 1, 'dpf_jacobian_vector': 2, 'dpf_elastic_precondition': 1,
-    'dpf_loads': 2, 'dpf_accept_step': 1, 'dpf_energy': 1, 'dpf_arnoldi_cgs2': 4, 'dpf_combine_rows': 1,
+    'dpf_loads': 2, 'dpf_bond_setup': 2, 'dpf_accept_step': 1, 'dpf_energy': 1, 'dpf_arnoldi_cgs2': 4, 'dpf_combine_rows': 1,
     'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
     'dpf_stiffness_apply_static': 2, 'dpf_mixed_setup': 2, 'dpf_mixed_residual': 2, 'dpf_mixed_scaling': 1,
     'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 3, 'dpf_mixed_stiffness_apply': 2,

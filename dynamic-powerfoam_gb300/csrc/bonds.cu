@@ -587,6 +587,51 @@ __global__ void __launch_bounds__(kThreads) loads_bonds(int64_t m, const int64_t
 
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
 
+// Bond setup of LinearBondsGPU / FiniteBondsGPU (experiments/bonded_dem_linear_gpu.py:15-40,
+// experiments/bonded_dem_finite_gpu.py:49-63) on the device: normal, contact
+// levers, stiffnesses and the contact offset from the classical contact.
+struct BondSetupArgs {
+    int64_t m;
+    const int64_t *edges;
+    const double *points, *radii, *areas, *contacts;
+    double young, shear;
+    double *n, *ri, *rj, *kn, *ks, *kb, *kt, *offset;
+};
+
+__global__ void __launch_bounds__(kThreads) bond_setup_kernel(BondSetupArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    int64_t i, j;
+    edge(a.edges, b, i, j);
+    const d3 pi = ld3(a.points, i), pj = ld3(a.points, j);
+    const d3 d = pj - pi;
+    const double length = norm(d);
+    const d3 n = d / length;
+    const d3 classical = 0.5 * (pi + pj) + (0.5 * (a.radii[i] - a.radii[j])) * n;
+    const d3 c = a.contacts ? ld3(a.contacts, b) : classical;
+    st3(a.n, b, n);
+    st3(a.ri, b, c - pi);
+    st3(a.rj, b, c - pj);
+    if (a.offset) st3(a.offset, b, c - classical);
+    const double area = a.areas[b];
+    const double second = area * area / (4.0 * 3.14159265358979323846);
+    const double inv = 1.0 / length;
+    a.kn[b] = a.young * area * inv;
+    a.ks[b] = a.shear * area * inv;
+    a.kb[b] = a.young * second * inv;
+    a.kt[b] = a.shear * (2.0 * second) * inv;
+}
+
+__global__ void __launch_bounds__(kThreads) site_mass_kernel(int64_t n, const double *masses, const double *radii,
+                                                             double *mass6) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const double m = masses[s], r = radii[s];
+    const double inertia = 0.4 * m * r * r;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) mass6[6 * s + c] = c < 3 ? m : inertia;
+}
+
 }  // namespace dpf
 
 using namespace dpf;
@@ -746,6 +791,23 @@ int dpf_jacobian_vector(const dpf_graph *g, const dpf_stiffness *k, const dpf_hi
     SiteJvpArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, direction, units, mass, preconditioner, fixed,
                   0.5 * dt * dt, out};
     site_jvp<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(s);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_bond_setup(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const double *points, const double *radii,
+                   const double *areas, const double *contacts, const double *masses, double young, double shear,
+                   double *n, double *ri, double *rj, double *kn, double *ks, double *kb, double *kt, double *offset,
+                   double *mass6, void *stream) {
+    if (n_sites <= 0 || n_bonds < 0 || (n_bonds && (!edges || !areas || !n || !ri || !rj || !kn || !ks || !kb || !kt)) ||
+        !points || !radii || (mass6 && !masses))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (n_bonds) {
+        BondSetupArgs a{n_bonds, edges, points, radii, areas, contacts, young, shear, n, ri, rj, kn, ks, kb, kt, offset};
+        bond_setup_kernel<<<blocks_for(n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
+    if (mass6) site_mass_kernel<<<blocks_for(n_sites, kThreads), kThreads, 0, st>>>(n_sites, masses, radii, mass6);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -40,9 +40,22 @@ _PER_BOND = ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'normal', 'offset', 'fn', 
 _STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
 
 
+def device_incidence(edges, n_sites):
+    """Incidence CSR of ``incidence`` built on the device (stable sort by site)."""
+    m = edges.shape[0]
+    site = torch.cat((edges[:, 0], edges[:, 1]))
+    ids = torch.arange(m, dtype=torch.int64, device=edges.device)
+    value = torch.cat((ids, -ids - 1))
+    order = torch.sort(site, stable=True).indices
+    ptr = torch.zeros(n_sites + 1, dtype=torch.int64, device=edges.device)
+    ptr[1:] = torch.cumsum(torch.bincount(site, minlength=n_sites), 0)
+    return ptr.to(torch.int32).contiguous(), value[order].to(torch.int32).contiguous()
+
+
 class RequestState:
     """Resident state of one request: exactly what a ``Batch`` concatenates
-    (the attributes of a fresh ``MixedNewtonBonds``, without solver scratch)."""
+    (the attributes of a fresh ``MixedNewtonBonds``, without solver scratch),
+    set up on the device (``dpf_bond_setup`` and a device-sorted incidence list)."""
 
     def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None, young=1200., shear=480.,
                  device='cuda'):
@@ -51,37 +64,76 @@ class RequestState:
             self.device = torch.device('cuda', torch.cuda.current_device())
         self._lib = _lib.load()
         t = self.tensor = lambda a: torch.as_tensor(a, dtype=F64, device=self.device)
-        p = np.asarray(points, dtype=np.float64)
-        radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
-        classical = classical_contacts(p, radii_a, pairs)
-        contacts = classical if contacts is None else np.asarray(contacts, dtype=np.float64)
-        h = bond_setup(p, radii_a, pairs, areas, contacts, masses, young, shear)
-        self.n_sites, self.n_bonds = len(p), len(h['edges'])
-        self.p = self.x = t(p)
-        self.x = self.p.clone()
-        self.edges = torch.as_tensor(h['edges'], dtype=torch.long, device=self.device).contiguous()
-        self.n, self.ri, self.rj = t(h['n']), t(h['ri']), t(h['rj'])
-        self.kn, self.ks, self.kb, self.kt = (t(h[k]) for k in ('kn', 'ks', 'kb', 'kt'))
-        self.mass = t(h['mass'])
+        n = len(points)
+        edges = torch.as_tensor(np.asarray(pairs, dtype=np.int64).reshape(-1, 2), device=self.device).contiguous()
+        m = edges.shape[0]
+        if m and (int(edges.min()) < 0 or int(edges.max()) >= n):
+            raise ValueError('Invalid endpoint index')
+        self.n_sites, self.n_bonds = n, m
+        self.p = t(points).contiguous()
+        self.radii = t(np.broadcast_to(np.asarray(radii, dtype=np.float64), (n,))).contiguous()
+        areas = t(np.broadcast_to(np.asarray(areas, dtype=np.float64), (m,))).contiguous()
+        masses = t(np.broadcast_to(np.asarray(masses, dtype=np.float64), (n,))).contiguous()
+        cont = None if contacts is None else t(contacts).contiguous()
+        e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
+        self.n, self.ri, self.rj, self.offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
+        self.kn, self.ks, self.kb, self.kt = e(m), e(m), e(m), e(m)
+        self.mass = e(n, 6)
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        _lib.check(self._lib.dpf_bond_setup(n, m, edges.data_ptr() if m else None, self.p.data_ptr(),
+                                            self.radii.data_ptr(), areas.data_ptr(), None if cont is None else
+                                            cont.data_ptr(), masses.data_ptr(), float(young), float(shear),
+                                            self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr(),
+                                            self.kn.data_ptr(), self.ks.data_ptr(), self.kb.data_ptr(),
+                                            self.kt.data_ptr(), self.offset.data_ptr(), self.mass.data_ptr(),
+                                            stream), 'dpf_bond_setup')
+        if bool((self.mass <= 0).any()):
+            raise ValueError('Only positive-mass bodies can enter this solver')
+        self.edges = edges
         self._mass32 = self.mass.float()
         self.fixed = torch.as_tensor(np.asarray(fixed, dtype=bool), device=self.device)
-        self.radii = t(np.array(radii_a))
+        self.x = self.p.clone()
         self.normal = self.n.clone()
-        self.offset = t(contacts - classical)
         self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
         self.fs, self.mb = torch.zeros_like(self.n), torch.zeros_like(self.n)
         self.v = torch.zeros_like(self.mass)
-        self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(self.n_sites, 1, 1)
-        ptr, inc = incidence(h['edges'], self.n_sites)
-        self._inc_ptr = torch.as_tensor(ptr, device=self.device)
-        self._inc_bond = torch.as_tensor(inc, device=self.device)
+        self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(n, 1, 1)
+        self._inc_ptr, self._inc_bond = device_incidence(edges, n)
         self.time = 0.
+
+
+class Pool:
+    """Batch scratch, allocated once for the largest batch and carved per batch."""
+
+    def __init__(self, device, max_sites, max_bonds):
+        lib = _lib.load()
+        self.max_sites, self.max_bonds = int(max_sites), int(max_bonds)
+        n, m = self.max_sites, self.max_bonds
+        self.f64 = torch.empty(9*m + 3*6*n + 65*6*n + 1024, dtype=F64, device=device)
+        self.f32 = torch.empty(lib.dpf_mixed_bond_floats(m) + 9*m + 2*36*n + 3*6*n +
+                               lib.dpf_mixed_workspace_floats(n, m) + 1024, dtype=torch.float32, device=device)
+
+    def carve(self, n, m):
+        if n > self.max_sites or m > self.max_bonds:
+            raise ValueError('batch exceeds the pool')
+        o64, o32 = [0], [0]
+
+        def take64(count, shape=None):
+            start = o64[0]; o64[0] += (count + 31)//32*32
+            v = self.f64[start:start + count]
+            return v.view(shape) if shape else v
+
+        def take32(count, shape=None):
+            start = o32[0]; o32[0] += (count + 63)//64*64
+            v = self.f32[start:start + count]
+            return v.view(shape) if shape else v
+        return take64, take32
 
 
 class Batch(MixedNewtonBonds):
     """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
 
-    def __init__(self, parts):
+    def __init__(self, parts, pool=None):
         if not parts:
             raise ValueError('empty batch')
         first = parts[0]
@@ -119,7 +171,12 @@ class Batch(MixedNewtonBonds):
         self._graph = _lib.Graph(n, m, self.edges.data_ptr() if m else None, self._inc_ptr.data_ptr(),
                                  self._inc_bond.data_ptr())
         lib, dev, f32 = self._lib, self.device, torch.float32
-        self._wrench = torch.empty(max(1, 9*m), dtype=F64, device=dev)
+        if pool is not None:
+            take64, take32 = pool.carve(n, m)
+        else:
+            take64 = lambda count, shape=None: torch.empty(shape or (count,), dtype=F64, device=dev)
+            take32 = lambda count, shape=None: torch.empty(shape or (count,), dtype=f32, device=dev)
+        self._wrench = take64(max(1, 9*m))
         self._partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=dev)
         self._status = torch.zeros(max(1, len(parts)), dtype=torch.int32, device=dev)
         self._scalars = torch.zeros(8, dtype=F64, device=dev)
@@ -132,21 +189,25 @@ class Batch(MixedNewtonBonds):
         self._inner_host = 0
         self._pcg_workspace = None
         self._barrier = torch.zeros(2, dtype=torch.int32, device=dev)
-        self._krylov = None
+        self._krylov = _Krylov.__new__(_Krylov)
+        self._krylov.length, self._krylov.width = 6*n, 32
+        self._krylov.basis = take64(33*6*n, (33, 6*n))
+        self._krylov.transformed = take64(32*6*n, (32, 6*n))
+        self._krylov.h = torch.zeros(72, dtype=F64, device=dev)
         self.block = self.units = None
         self.profile = None
-        self._bond_data = torch.empty(max(4, lib.dpf_mixed_bond_floats(m)), dtype=f32, device=dev)
-        self._wrench32 = torch.empty(max(1, 9*m), dtype=f32, device=dev)
-        self._r0 = torch.empty((n, 6), dtype=F64, device=dev)
-        self._block32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
-        self._p32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
-        self._units = torch.empty((n, 6), dtype=F64, device=dev)
-        self._units32 = torch.empty((n, 6), dtype=f32, device=dev)
-        self._y32 = torch.empty((n, 6), dtype=f32, device=dev)
-        self._d32 = torch.empty((n, 6), dtype=f32, device=dev)
-        self._mixed_workspace = torch.empty(lib.dpf_mixed_workspace_floats(n, m), dtype=f32, device=dev)
+        self._bond_data = take32(max(4, lib.dpf_mixed_bond_floats(m)))
+        self._wrench32 = take32(max(1, 9*m))
+        self._r0 = take64(6*n, (n, 6))
+        self._block32 = take32(36*n, (n, 6, 6))
+        self._p32 = take32(36*n, (n, 6, 6))
+        self._units = take64(6*n, (n, 6))
+        self._units32 = take32(6*n, (n, 6))
+        self._y32 = take32(6*n, (n, 6))
+        self._d32 = take32(6*n, (n, 6))
+        self._mixed_workspace = take32(lib.dpf_mixed_workspace_floats(n, m))
         self._cached = None
-        self._loads = torch.empty((n, 6), dtype=F64, device=dev)
+        self._loads = take64(6*n, (n, 6))
         self._token = None
         self._since_refresh = 0
         self._seg_norms = torch.zeros((len(parts), 3), dtype=F64, device=dev)
@@ -274,8 +335,6 @@ class Batch(MixedNewtonBonds):
             rhs = torch.empty_like(scaled)
             self._call('dpf_segment_axpy', self.n_sites, self.seg_site.data_ptr(), sdev.data_ptr(), zero.data_ptr(),
                        scaled.data_ptr(), rhs.data_ptr(), stream)
-            if self._krylov is None or self._krylov.length != n6:
-                self._krylov = _Krylov(n6, 32, self.device)
             self.inner_iterations = 0
             delta, metrics = fgmres(self._newton_operator(y, dt, external), rhs, self._newton_preconditioner(dt),
                                     tolerance=linear_tolerance/np.sqrt(len(active)), workspace=self._krylov)
@@ -391,14 +450,15 @@ class Request:
 
 
 def footprint_bytes(sites, bonds):
-    """HBM bytes a resident request and its share of a batch take (upper estimate).
+    """HBM bytes of a resident request's state plus its copy inside a batch.
 
-    Per site: state and solver vectors (float64 and float32 copies, 6x6 blocks,
-    FGMRES basis of 33 + 32 vectors of 6 doubles); per bond: float64 state and
-    tangent, float32 records/tangent and wrench scratch.
+    Per site: positions, reference points, velocity, rotation, mass (float64
+    and float32), radius, flag and incidence pointer; per bond: edges, tangent,
+    stiffnesses, history and two incidence entries.  Batch scratch comes from
+    the service's pool, counted once.
     """
-    per_site = 8*(3 + 6 + 9 + 6 + 1) + 8*6*12 + 4*36*2 + 4*6*10 + 8*6*65
-    per_bond = 8*(2 + 3*8 + 4*2) + 4*(44 + 9*2 + 12) + 8*9 + 8
+    per_site = 8*(3 + 3 + 6 + 9 + 6 + 1) + 4*6 + 1 + 4
+    per_bond = 16 + 8*(3*3 + 4 + 3*2 + 2 + 3*2) + 8
     return int(2*(per_site*sites + per_bond*bonds))
 
 
@@ -422,6 +482,7 @@ class Service:
         self.solver_cls = solver_cls
         self.in_use = 0.
         self.batches = 0
+        self.pool = None
 
     def _construct(self, req):
         f = req.foam
@@ -432,14 +493,17 @@ class Service:
     def run(self, requests, clock=time.perf_counter):
         pending = sorted(requests)
         waiting, active, finished = [], [], []
+        if self.pool is None and self.solver_cls is RequestState:
+            largest = max((r.bonds for r in requests), default=1)
+            max_bonds = int(self.max_batch_sites*max(r.bonds/max(r.sites, 1) for r in requests)*1.05) + largest
+            self.pool = Pool(self.device, self.max_batch_sites + max(r.sites for r in requests), max_bonds)
+            self.in_use += self.pool.f64.numel()*8 + self.pool.f32.numel()*4
         t0 = clock()
         now = lambda: clock() - t0
         batch, members = None, None
         while pending or waiting or active:
             while pending and pending[0].arrival <= now():
-                req = pending.pop(0)
-                self._construct(req)
-                waiting.append(req)
+                waiting.append(pending.pop(0))
             changed = False
             sites = sum(r.sites for r in active)
             while waiting:
@@ -448,6 +512,7 @@ class Service:
                 if self.in_use + need > self.hbm_budget or (active and sites + req.sites > self.max_batch_sites):
                     break
                 waiting.pop(0)
+                self._construct(req)
                 self.in_use += need
                 req.started = now()
                 active.append(req)
@@ -460,7 +525,7 @@ class Service:
             if changed or batch is None:
                 if batch is not None:
                     batch.scatter_state()
-                batch = Batch([r.solver for r in active])
+                batch = Batch([r.solver for r in active], pool=self.pool)
                 members = list(active)
             ext = torch.cat([r.load_dev for r in members])
             results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
