@@ -62,7 +62,8 @@ SIGNATURES = {
     'dpf_elastic_precondition': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp, vp, vp, vp, f64, f64, i32,
                                        vp, vp, vp, vp, vp, vp, vp]),
     'dpf_loads': (i32, [P(Graph), P(History), vp, vp, vp]),
-    'dpf_bond_setup': (i32, [i64, i64, vp, vp, vp, vp, vp, vp, f64, f64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_bond_setup': (i32, [i64, i64, vp, vp, vp, vp, vp, vp, f64, f64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                             vp]),
     'dpf_accept_step': (i32, [i64, vp, f64, vp, vp, vp]),
     'dpf_energy': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, vp]),
     'dpf_arnoldi_cgs2': (i32, [i64, vp, i64, i32, vp, vp, vp, vp]),

@@ -593,7 +593,7 @@ inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) /
 struct BondSetupArgs {
     int64_t m;
     const int64_t *edges;
-    const double *points, *radii, *areas, *contacts;
+    const double *points, *radii, *areas, *contacts, *young_b, *shear_b;
     double young, shear;
     double *n, *ri, *rj, *kn, *ks, *kb, *kt, *offset;
 };
@@ -616,10 +616,11 @@ __global__ void __launch_bounds__(kThreads) bond_setup_kernel(BondSetupArgs a) {
     const double area = a.areas[b];
     const double second = area * area / (4.0 * 3.14159265358979323846);
     const double inv = 1.0 / length;
-    a.kn[b] = a.young * area * inv;
-    a.ks[b] = a.shear * area * inv;
-    a.kb[b] = a.young * second * inv;
-    a.kt[b] = a.shear * (2.0 * second) * inv;
+    const double E = a.young_b ? a.young_b[b] : a.young, G = a.shear_b ? a.shear_b[b] : a.shear;
+    a.kn[b] = E * area * inv;
+    a.ks[b] = G * area * inv;
+    a.kb[b] = E * second * inv;
+    a.kt[b] = G * (2.0 * second) * inv;
 }
 
 __global__ void __launch_bounds__(kThreads) site_mass_kernel(int64_t n, const double *masses, const double *radii,
@@ -797,14 +798,15 @@ int dpf_jacobian_vector(const dpf_graph *g, const dpf_stiffness *k, const dpf_hi
 
 int dpf_bond_setup(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const double *points, const double *radii,
                    const double *areas, const double *contacts, const double *masses, double young, double shear,
-                   double *n, double *ri, double *rj, double *kn, double *ks, double *kb, double *kt, double *offset,
-                   double *mass6, void *stream) {
+                   const double *young_b, const double *shear_b, double *n, double *ri, double *rj, double *kn,
+                   double *ks, double *kb, double *kt, double *offset, double *mass6, void *stream) {
     if (n_sites <= 0 || n_bonds < 0 || (n_bonds && (!edges || !areas || !n || !ri || !rj || !kn || !ks || !kb || !kt)) ||
         !points || !radii || (mass6 && !masses))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (n_bonds) {
-        BondSetupArgs a{n_bonds, edges, points, radii, areas, contacts, young, shear, n, ri, rj, kn, ks, kb, kt, offset};
+        BondSetupArgs a{n_bonds, edges, points, radii, areas, contacts, young_b, shear_b, young, shear,
+                        n, ri, rj, kn, ks, kb, kt, offset};
         bond_setup_kernel<<<blocks_for(n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     if (mass6) site_mass_kernel<<<blocks_for(n_sites, kThreads), kThreads, 0, st>>>(n_sites, masses, radii, mass6);

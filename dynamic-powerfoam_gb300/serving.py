@@ -53,45 +53,75 @@ def device_incidence(edges, n_sites):
 
 
 class RequestState:
-    """Resident state of one request: exactly what a ``Batch`` concatenates
-    (the attributes of a fresh ``MixedNewtonBonds``, without solver scratch),
-    set up on the device (``dpf_bond_setup`` and a device-sorted incidence list)."""
+    """Resident state of one or several requests: exactly what a ``Batch``
+    concatenates (the attributes of fresh ``MixedNewtonBonds`` solvers, without
+    solver scratch), set up on the device with one ``dpf_bond_setup`` and one
+    device sort of the incidence list for the whole group."""
 
     def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None, young=1200., shear=480.,
                  device='cuda'):
+        self._build([dict(points=points, radii=radii, pairs=pairs, areas=areas, masses=masses, fixed=fixed,
+                          contacts=contacts, young=young, shear=shear)], device)
+
+    @classmethod
+    def group(cls, foams, device='cuda'):
+        """Several requests' foams as one resident state (sites and bonds in order)."""
+        self = cls.__new__(cls)
+        self._build(foams, device)
+        return self
+
+    def _build(self, foams, device):
         self.device = torch.device(device)
         if self.device.index is None:
             self.device = torch.device('cuda', torch.cuda.current_device())
         self._lib = _lib.load()
         t = self.tensor = lambda a: torch.as_tensor(a, dtype=F64, device=self.device)
-        n = len(points)
-        edges = torch.as_tensor(np.asarray(pairs, dtype=np.int64).reshape(-1, 2), device=self.device).contiguous()
-        m = edges.shape[0]
-        if m and (int(edges.min()) < 0 or int(edges.max()) >= n):
+        sites = [len(f['points']) for f in foams]
+        bonds = [len(f['pairs']) for f in foams]
+        self.sites, self.bonds = sites, bonds
+        off = np.concatenate(([0], np.cumsum(sites)))
+        n, m = int(off[-1]), int(sum(bonds))
+        cat = lambda key, count: np.concatenate([np.broadcast_to(np.asarray(f[key], dtype=np.float64), (c,) +
+                                                                 np.shape(f[key])[1:]) for f, c in zip(foams, count)])
+        points = np.concatenate([np.asarray(f['points'], dtype=np.float64) for f in foams])
+        pairs = np.concatenate([np.asarray(f['pairs'], dtype=np.int64).reshape(-1, 2) + off[k]
+                                for k, f in enumerate(foams)])
+        if m and (pairs.min() < 0 or any(np.asarray(f['pairs']).max() >= c for f, c in zip(foams, sites) if len(f['pairs']))):
             raise ValueError('Invalid endpoint index')
+        radii = cat('radii', sites)
+        masses = cat('masses', sites)
+        areas = cat('areas', bonds)
+        young_b = np.concatenate([np.full(c, float(f['young'])) for f, c in zip(foams, bonds)])
+        shear_b = np.concatenate([np.full(c, float(f['shear'])) for f, c in zip(foams, bonds)])
+        fixed = np.concatenate([np.asarray(f['fixed'], dtype=bool) for f in foams])
+        if any(f.get('contacts') is not None for f in foams):
+            raise ValueError('explicit contacts are not supported in a group; use MixedNewtonBonds')
+        host = np.concatenate((points.ravel(), radii, masses, areas, young_b, shear_b))
+        dev = torch.from_numpy(host).pin_memory().to(self.device, non_blocking=True)
+        o = np.cumsum([0, 3*n, n, n, m, m, m])
+        self.p = dev[o[0]:o[1]].view(n, 3)
+        self.radii = dev[o[1]:o[2]]
+        masses_d, areas_d = dev[o[2]:o[3]], dev[o[3]:o[4]]
+        young_d, shear_d = dev[o[4]:o[5]], dev[o[5]:o[6]]
+        edges = torch.from_numpy(pairs).pin_memory().to(self.device, non_blocking=True)
         self.n_sites, self.n_bonds = n, m
-        self.p = t(points).contiguous()
-        self.radii = t(np.broadcast_to(np.asarray(radii, dtype=np.float64), (n,))).contiguous()
-        areas = t(np.broadcast_to(np.asarray(areas, dtype=np.float64), (m,))).contiguous()
-        masses = t(np.broadcast_to(np.asarray(masses, dtype=np.float64), (n,))).contiguous()
-        cont = None if contacts is None else t(contacts).contiguous()
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         self.n, self.ri, self.rj, self.offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
         self.kn, self.ks, self.kb, self.kt = e(m), e(m), e(m), e(m)
         self.mass = e(n, 6)
         stream = torch.cuda.current_stream(self.device).cuda_stream
         _lib.check(self._lib.dpf_bond_setup(n, m, edges.data_ptr() if m else None, self.p.data_ptr(),
-                                            self.radii.data_ptr(), areas.data_ptr(), None if cont is None else
-                                            cont.data_ptr(), masses.data_ptr(), float(young), float(shear),
+                                            self.radii.data_ptr(), areas_d.data_ptr(), None, masses_d.data_ptr(),
+                                            0., 0., young_d.data_ptr(), shear_d.data_ptr(),
                                             self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr(),
                                             self.kn.data_ptr(), self.ks.data_ptr(), self.kb.data_ptr(),
                                             self.kt.data_ptr(), self.offset.data_ptr(), self.mass.data_ptr(),
                                             stream), 'dpf_bond_setup')
-        if bool((self.mass <= 0).any()):
+        if np.any(masses <= 0):
             raise ValueError('Only positive-mass bodies can enter this solver')
         self.edges = edges
         self._mass32 = self.mass.float()
-        self.fixed = torch.as_tensor(np.asarray(fixed, dtype=bool), device=self.device)
+        self.fixed = torch.from_numpy(fixed).pin_memory().to(self.device, non_blocking=True)
         self.x = self.p.clone()
         self.normal = self.n.clone()
         self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
@@ -100,6 +130,23 @@ class RequestState:
         self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(n, 1, 1)
         self._inc_ptr, self._inc_bond = device_incidence(edges, n)
         self.time = 0.
+
+
+class Slice:
+    """One request's state inside a previous batch (views, no copies), ready
+    to be concatenated into the next batch."""
+
+    def __init__(self, batch, k):
+        s0, s1 = batch.site_range[k]
+        b0, b1 = batch.bond_range[k]
+        self.device, self._lib, self.tensor = batch.device, batch._lib, batch.tensor
+        self.n_sites, self.n_bonds = s1 - s0, b1 - b0
+        for name in _PER_SITE:
+            setattr(self, name, getattr(batch, name)[s0:s1])
+        for name in _PER_BOND:
+            setattr(self, name, getattr(batch, name)[b0:b1])
+        self.edges = batch.edges[b0:b1] - s0
+        self.time = batch.time
 
 
 class Pool:
@@ -141,33 +188,32 @@ class Batch(MixedNewtonBonds):
         self.device = first.device
         self._lib = first._lib
         self.tensor = first.tensor
+        # segments: one per request (a group part holds several requests)
+        seg_sites, seg_bonds = [], []
+        for p in parts:
+            seg_sites += list(getattr(p, 'sites', [p.n_sites]))
+            seg_bonds += list(getattr(p, 'bonds', [p.n_bonds]))
+        self.n_requests = len(seg_sites)
         sites = [p.n_sites for p in parts]
         bonds = [p.n_bonds for p in parts]
         site_off = np.concatenate(([0], np.cumsum(sites)))
         bond_off = np.concatenate(([0], np.cumsum(bonds)))
-        self.site_ptr = torch.as_tensor(site_off, dtype=torch.int64, device=self.device)
-        self.bond_ptr = bond_off
-        self.site_range = [(int(site_off[k]), int(site_off[k+1])) for k in range(len(parts))]
-        self.bond_range = [(int(bond_off[k]), int(bond_off[k+1])) for k in range(len(parts))]
         n, m = int(site_off[-1]), int(bond_off[-1])
+        rs = np.concatenate(([0], np.cumsum(seg_sites)))
+        rb = np.concatenate(([0], np.cumsum(seg_bonds)))
+        self.site_ptr = torch.as_tensor(rs, dtype=torch.int64, device=self.device)
+        self.site_range = [(int(rs[k]), int(rs[k+1])) for k in range(self.n_requests)]
+        self.bond_range = [(int(rb[k]), int(rb[k+1])) for k in range(self.n_requests)]
         for name in _PER_SITE + _PER_BOND:
             setattr(self, name, torch.cat([getattr(p, name).contiguous() for p in parts]))
         self.edges = torch.cat([p.edges + int(site_off[k]) for k, p in enumerate(parts)]).contiguous()
         self.i, self.j = self.edges.T
-        inc_ptr, inc_bond = [], []
-        inc_off = 0
-        for k, p in enumerate(parts):
-            ptr = p._inc_ptr.to(torch.int64)
-            inc_ptr.append((ptr[:-1] if k < len(parts) - 1 else ptr) + inc_off)
-            v = p._inc_bond.to(torch.int64)
-            inc_bond.append(torch.where(v >= 0, v + int(bond_off[k]), v - int(bond_off[k])))
-            inc_off += 2*p.n_bonds
-        self._inc_ptr = torch.cat(inc_ptr).to(torch.int32).contiguous()
-        self._inc_bond = torch.cat(inc_bond).to(torch.int32).contiguous()
-        self.seg_site = torch.repeat_interleave(torch.arange(len(parts), dtype=torch.int32, device=self.device),
-                                                torch.as_tensor(sites, device=self.device)).contiguous()
-        self.seg_bond = torch.repeat_interleave(torch.arange(len(parts), dtype=torch.int32, device=self.device),
-                                                torch.as_tensor(bonds, device=self.device)).contiguous()
+        self._inc_ptr, self._inc_bond = device_incidence(self.edges, n)
+        R = self.n_requests
+        self.seg_site = torch.repeat_interleave(torch.arange(R, dtype=torch.int32, device=self.device),
+                                                torch.as_tensor(seg_sites, device=self.device)).contiguous()
+        self.seg_bond = torch.repeat_interleave(torch.arange(R, dtype=torch.int32, device=self.device),
+                                                torch.as_tensor(seg_bonds, device=self.device)).contiguous()
         self._graph = _lib.Graph(n, m, self.edges.data_ptr() if m else None, self._inc_ptr.data_ptr(),
                                  self._inc_bond.data_ptr())
         lib, dev, f32 = self._lib, self.device, torch.float32
@@ -178,7 +224,7 @@ class Batch(MixedNewtonBonds):
             take32 = lambda count, shape=None: torch.empty(shape or (count,), dtype=f32, device=dev)
         self._wrench = take64(max(1, 9*m))
         self._partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=dev)
-        self._status = torch.zeros(max(1, len(parts)), dtype=torch.int32, device=dev)
+        self._status = torch.zeros(max(1, R), dtype=torch.int32, device=dev)
         self._scalars = torch.zeros(8, dtype=F64, device=dev)
         self._host_status = torch.zeros(1, dtype=torch.int32).pin_memory()
         self._host_scalars = torch.zeros(64, dtype=F64).pin_memory()
@@ -210,25 +256,34 @@ class Batch(MixedNewtonBonds):
         self._loads = take64(6*n, (n, 6))
         self._token = None
         self._since_refresh = 0
-        self._seg_norms = torch.zeros((len(parts), 3), dtype=F64, device=dev)
-        self._seg_norms2 = torch.zeros((len(parts), 3), dtype=F64, device=dev)
-        self._host_seg = torch.zeros((2, len(parts), 3), dtype=F64).pin_memory()
-        self._host_seg_status = torch.zeros(len(parts), dtype=torch.int32).pin_memory()
+        self._seg_norms = torch.zeros((R, 3), dtype=F64, device=dev)
+        self._seg_norms2 = torch.zeros((R, 3), dtype=F64, device=dev)
+        self._host_seg = torch.zeros((2, R, 3), dtype=F64).pin_memory()
+        self._host_seg_status = torch.zeros(R, dtype=torch.int32).pin_memory()
 
     @property
     def n_segments(self):
-        return len(self.parts)
+        return self.n_requests
+
+    def request_state(self, k):
+        """Views of request k's committed state inside the batch."""
+        s0, s1 = self.site_range[k]
+        b0, b1 = self.bond_range[k]
+        return {name: getattr(self, name)[s0:s1] if name in ('x', 'v', 'rotation') else getattr(self, name)[b0:b1]
+                for name in _STATE}
 
     def scatter_state(self):
-        """Copy the batch's committed state back into the requests' own tensors."""
-        for k, p in enumerate(self.parts):
-            s0, s1 = self.site_range[k]
-            b0, b1 = self.bond_range[k]
+        """Copy the batch's committed state back into its parts' own tensors."""
+        site0 = bond0 = 0
+        for p in self.parts:
             for name in _STATE:
                 src = getattr(self, name)
-                part = src[s0:s1] if name in ('x', 'v', 'rotation') else src[b0:b1]
-                setattr(p, name, part.clone())
+                rows = (slice(site0, site0 + p.n_sites) if name in ('x', 'v', 'rotation')
+                        else slice(bond0, bond0 + p.n_bonds))
+                setattr(p, name, src[rows].clone())
             p.time = self.time
+            site0 += p.n_sites
+            bond0 += p.n_bonds
 
     # ---- per-request reductions ---------------------------------------------------
     def _segment(self, a, b=None, b_dot=False, mask=None, out=None):
@@ -473,61 +528,57 @@ class Service:
     running join at the next step boundary.  Latency = completion - arrival.
     """
 
-    def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=2_000_000, tolerance=1e-6,
-                 solver_cls=RequestState):
+    def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=4_000_000, tolerance=1e-6):
         self.device = torch.device(device)
         self.hbm_budget = float(hbm_budget)
         self.max_batch_sites = int(max_batch_sites)
         self.tolerance = float(tolerance)
-        self.solver_cls = solver_cls
         self.in_use = 0.
         self.batches = 0
         self.pool = None
 
-    def _construct(self, req):
-        f = req.foam
-        req.solver = self.solver_cls(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
-                                     young=f['young'], shear=f['shear'], device=self.device)
-        req.load_dev = req.solver.tensor(req.load)
-
     def run(self, requests, clock=time.perf_counter):
         pending = sorted(requests)
         waiting, active, finished = [], [], []
-        if self.pool is None and self.solver_cls is RequestState:
+        if self.pool is None:
             largest = max((r.bonds for r in requests), default=1)
             max_bonds = int(self.max_batch_sites*max(r.bonds/max(r.sites, 1) for r in requests)*1.05) + largest
             self.pool = Pool(self.device, self.max_batch_sites + max(r.sites for r in requests), max_bonds)
             self.in_use += self.pool.f64.numel()*8 + self.pool.f32.numel()*4
         t0 = clock()
         now = lambda: clock() - t0
-        batch, members = None, None
+        batch, members = None, []
         while pending or waiting or active:
             while pending and pending[0].arrival <= now():
                 waiting.append(pending.pop(0))
-            changed = False
+            admitted = []
             sites = sum(r.sites for r in active)
             while waiting:
                 req = waiting[0]
                 need = footprint_bytes(req.sites, req.bonds)
-                if self.in_use + need > self.hbm_budget or (active and sites + req.sites > self.max_batch_sites):
+                if self.in_use + need > self.hbm_budget or ((active or admitted) and
+                                                              sites + req.sites > self.max_batch_sites):
                     break
                 waiting.pop(0)
-                self._construct(req)
                 self.in_use += need
                 req.started = now()
-                active.append(req)
+                admitted.append(req)
                 sites += req.sites
-                changed = True
-            if not active:
+            if not active and not admitted:
                 if pending:
                     time.sleep(max(0., min(pending[0].arrival - now(), .001)))
                 continue
-            if changed or batch is None:
-                if batch is not None:
-                    batch.scatter_state()
-                batch = Batch([r.solver for r in active], pool=self.pool)
+            if admitted or batch is None:
+                # staying requests keep their resident state; the admitted ones are
+                # set up together on the device (one upload, one setup, one sort)
+                parts = [r.part for r in active]
+                if admitted:
+                    parts.append(RequestState.group([r.foam for r in admitted], device=self.device))
+                active += admitted
                 members = list(active)
-            ext = torch.cat([r.load_dev for r in members])
+                batch = Batch(parts, pool=self.pool)
+                ext = torch.from_numpy(np.concatenate([r.load for r in members])).pin_memory().to(
+                    self.device, non_blocking=True)
             results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
             self.batches += 1
             leaving = []
@@ -540,14 +591,17 @@ class Service:
                 req.done_steps += 1
                 if req.done_steps >= req.steps:
                     leaving.append(req)
-            if leaving:
-                batch.scatter_state()
+            if leaving or (waiting or (pending and pending[0].arrival <= now())):
                 stamp = now()
-                for req in leaving:
-                    req.finished = stamp
-                    active.remove(req)
-                    finished.append(req)
-                    self.in_use -= footprint_bytes(req.sites, req.bonds)
+                for k, req in enumerate(members):
+                    if req in leaving:
+                        req.state = batch.request_state(k)
+                        req.finished = stamp
+                        active.remove(req)
+                        finished.append(req)
+                        self.in_use -= footprint_bytes(req.sites, req.bonds)
+                    else:
+                        req.part = Slice(batch, k)
                 batch = None
         return finished
 

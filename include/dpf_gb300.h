@@ -201,14 +201,15 @@ int dpf_elastic_precondition(const dpf_graph *g, const dpf_stiffness *k, const d
 /* Bond setup on the device: normal n, contact levers ri = c - p_i, rj = c - p_j,
  * kn = E A/L, ks = G A/L, kb = E I/L, kt = 2 G I/L (I = A^2/(4 pi)), the contact
  * offset c - classical (may be NULL) and the (N, 6) mass [m, m, m, 0.4 m r^2 x 3]
- * (may be NULL).  contacts (M, 3) may be NULL (classical ball contacts).
+ * (may be NULL).  contacts (M, 3) may be NULL (classical ball contacts);
+ * young_b / shear_b (M) give per-bond moduli (NULL: the scalars young, shear).
  * Replaces LinearBondsGPU.__init__ / FiniteBondsGPU.__init__ arithmetic
  * (experiments/bonded_dem_linear_gpu.py:15-40, experiments/bonded_dem_finite_gpu.py:49-63). */
 int dpf_bond_setup(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const double *points,
                    const double *radii, const double *areas, const double *contacts,
-                   const double *masses, double young, double shear, double *n, double *ri, double *rj,
-                   double *kn, double *ks, double *kb, double *kt, double *offset, double *mass6,
-                   void *stream);
+                   const double *masses, double young, double shear, const double *young_b,
+                   const double *shear_b, double *n, double *ri, double *rj, double *kn, double *ks,
+                   double *kb, double *kt, double *offset, double *mass6, void *stream);
 
 /* Net loads (force, torque) of the committed state (N, 6).
  * Replaces FiniteBondsGPU.loads (experiments/bonded_dem_finite_gpu.py:82-85). */

@@ -76,7 +76,7 @@ def test_failed_request_is_isolated():
 def test_service_stream_with_arrivals():
     from dpf_gb300 import serving
     reqs = serving.synthetic_stream(6, seed=7, sites=(700, 6000), rate=200., steps=2)
-    service = serving.Service(hbm_budget=4e9, max_batch_sites=12000)
+    service = serving.Service(hbm_budget=8e9, max_batch_sites=12000)
     finished = service.run(reqs)
     assert len(finished) == 6
     assert all(r.error is None and r.done_steps == 2 for r in finished)
@@ -85,5 +85,22 @@ def test_service_stream_with_arrivals():
     assert service.batches >= 2
     for req in finished[:3]:
         alone, x0 = _alone(req, 2)
-        err = float(torch.linalg.vector_norm(req.solver.x - alone.x)/torch.linalg.vector_norm(alone.x - x0))
+        err = float(torch.linalg.vector_norm(req.state['x'] - alone.x)/torch.linalg.vector_norm(alone.x - x0))
         assert err < 1e-5, err
+
+
+def test_group_state_matches_solver_setup():
+    """Device setup of a group of requests equals the float64 host setup of each."""
+    from dpf_gb300 import serving
+    reqs = serving.synthetic_stream(3, seed=9, sites=(700, 3000))
+    group = serving.RequestState.group([r.foam for r in reqs])
+    site0 = bond0 = 0
+    for r in reqs:
+        s = _solver(r)
+        for name in ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'offset'):
+            got = getattr(group, name)[bond0:bond0 + s.n_bonds]
+            assert float(torch.linalg.vector_norm(got - getattr(s, name))) <= 1e-12*max(
+                1., float(torch.linalg.vector_norm(getattr(s, name)))), name
+        assert torch.allclose(group.mass[site0:site0 + s.n_sites], s.mass, rtol=1e-14, atol=0)
+        site0 += s.n_sites
+        bond0 += s.n_bonds
