@@ -173,6 +173,7 @@ def run_served(args, device):
     served = dict(requests=len(stream), solved=len(ok), failed=len(stream) - len(ok), wall_s=wall,
                   solves_per_s=len(ok)/wall, p50_ms=1e3*stats['p50'], p99_ms=1e3*stats['p99'],
                   batched_steps=service.batches, sites=int(sum(r.sites for r in stream)),
+                  phase_s={k: round(v, 4) for k, v in service.timers.items()},
                   newton_per_solve=float(np.mean([r.infos[0]['nonlinear_iterations'] for r in ok])),
                   max_relative_residual=float(max(r.infos[0]['nonlinear_relative_residual'] for r in ok)))
     del finished, ok, stream

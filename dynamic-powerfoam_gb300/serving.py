@@ -40,6 +40,31 @@ _PER_BOND = ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'normal', 'offset', 'fn', 
 _STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
 
 
+class Staging:
+    """Reusable pinned host buffer for uploads (pinned allocations are slow)."""
+
+    def __init__(self):
+        self.buffers = {}
+
+    def upload(self, array, device):
+        array = np.ascontiguousarray(array)
+        key = array.dtype.str
+        need = array.size
+        buf = self.buffers.get(key)
+        if buf is None or buf.numel() < need:
+            buf = torch.empty(max(need, 1 << 20), dtype=torch.from_numpy(array[:0]).dtype).pin_memory()
+            self.buffers[key] = buf
+        view = buf[:need]
+        view.numpy()[...] = array.ravel()
+        out = view.to(device, non_blocking=True)
+        # the pinned buffer is reused by the next upload: wait for this copy
+        torch.cuda.current_stream(device).synchronize()
+        return out.view(array.shape)
+
+
+_STAGING = Staging()
+
+
 def device_incidence(edges, n_sites):
     """Incidence CSR of ``incidence`` built on the device (stable sort by site)."""
     m = edges.shape[0]
@@ -97,13 +122,13 @@ class RequestState:
         if any(f.get('contacts') is not None for f in foams):
             raise ValueError('explicit contacts are not supported in a group; use MixedNewtonBonds')
         host = np.concatenate((points.ravel(), radii, masses, areas, young_b, shear_b))
-        dev = torch.from_numpy(host).pin_memory().to(self.device, non_blocking=True)
+        dev = _STAGING.upload(host, self.device)
         o = np.cumsum([0, 3*n, n, n, m, m, m])
         self.p = dev[o[0]:o[1]].view(n, 3)
         self.radii = dev[o[1]:o[2]]
         masses_d, areas_d = dev[o[2]:o[3]], dev[o[3]:o[4]]
         young_d, shear_d = dev[o[4]:o[5]], dev[o[5]:o[6]]
-        edges = torch.from_numpy(pairs).pin_memory().to(self.device, non_blocking=True)
+        edges = _STAGING.upload(pairs, self.device)
         self.n_sites, self.n_bonds = n, m
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         self.n, self.ri, self.rj, self.offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
@@ -121,7 +146,7 @@ class RequestState:
             raise ValueError('Only positive-mass bodies can enter this solver')
         self.edges = edges
         self._mass32 = self.mass.float()
-        self.fixed = torch.from_numpy(fixed).pin_memory().to(self.device, non_blocking=True)
+        self.fixed = _STAGING.upload(fixed, self.device)
         self.x = self.p.clone()
         self.normal = self.n.clone()
         self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
@@ -535,6 +560,7 @@ class Service:
         self.tolerance = float(tolerance)
         self.in_use = 0.
         self.batches = 0
+        self.timers = dict(setup=0., batch=0., solve=0., other=0.)
         self.pool = None
 
     def run(self, requests, clock=time.perf_counter):
@@ -571,15 +597,21 @@ class Service:
             if admitted or batch is None:
                 # staying requests keep their resident state; the admitted ones are
                 # set up together on the device (one upload, one setup, one sort)
+                t1 = clock()
                 parts = [r.part for r in active]
                 if admitted:
                     parts.append(RequestState.group([r.foam for r in admitted], device=self.device))
+                t2 = clock()
                 active += admitted
                 members = list(active)
                 batch = Batch(parts, pool=self.pool)
-                ext = torch.from_numpy(np.concatenate([r.load for r in members])).pin_memory().to(
-                    self.device, non_blocking=True)
+                ext = _STAGING.upload(np.concatenate([r.load for r in members]), self.device)
+                t3 = clock()
+                self.timers['setup'] += t2 - t1
+                self.timers['batch'] += t3 - t2
+            t4 = clock()
             results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
+            self.timers['solve'] += clock() - t4
             self.batches += 1
             leaving = []
             for req, res in zip(members, results):
