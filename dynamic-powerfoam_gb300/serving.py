@@ -41,10 +41,26 @@ _STATE = ('x', 'v', 'rotation', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
 
 
 class Staging:
-    """Reusable pinned host buffer for uploads (pinned allocations are slow)."""
+    """Reusable pinned host buffers for uploads (pinned allocations are slow)."""
 
     def __init__(self):
         self.buffers = {}
+
+    def host(self, kind, count):
+        """A pinned host array of ``count`` elements of numpy kind ``kind`` to fill."""
+        dtype = np.dtype(kind)
+        buf = self.buffers.get(dtype.str)
+        if buf is None or buf.numel() < count:
+            buf = torch.empty(max(count, 1 << 20), dtype=torch.from_numpy(np.zeros(0, dtype)).dtype).pin_memory()
+            self.buffers[dtype.str] = buf
+        return buf[:count].numpy()
+
+    def send(self, kind, count, device):
+        """Upload the first ``count`` elements of the pinned buffer of ``kind``."""
+        buf = self.buffers[np.dtype(kind).str][:count]
+        out = buf.to(device, non_blocking=True)
+        torch.cuda.current_stream(device).synchronize()
+        return out
 
     def upload(self, array, device):
         array = np.ascontiguousarray(array)
@@ -100,35 +116,42 @@ class RequestState:
         if self.device.index is None:
             self.device = torch.device('cuda', torch.cuda.current_device())
         self._lib = _lib.load()
-        t = self.tensor = lambda a: torch.as_tensor(a, dtype=F64, device=self.device)
+        self.tensor = lambda a: torch.as_tensor(a, dtype=F64, device=self.device)
+        if any(f.get('contacts') is not None for f in foams):
+            raise ValueError('explicit contacts are not supported in a group; use MixedNewtonBonds')
         sites = [len(f['points']) for f in foams]
         bonds = [len(f['pairs']) for f in foams]
         self.sites, self.bonds = sites, bonds
-        off = np.concatenate(([0], np.cumsum(sites)))
-        n, m = int(off[-1]), int(sum(bonds))
-        cat = lambda key, count: np.concatenate([np.broadcast_to(np.asarray(f[key], dtype=np.float64), (c,) +
-                                                                 np.shape(f[key])[1:]) for f, c in zip(foams, count)])
-        points = np.concatenate([np.asarray(f['points'], dtype=np.float64) for f in foams])
-        pairs = np.concatenate([np.asarray(f['pairs'], dtype=np.int64).reshape(-1, 2) + off[k]
-                                for k, f in enumerate(foams)])
-        if m and (pairs.min() < 0 or any(np.asarray(f['pairs']).max() >= c for f, c in zip(foams, sites) if len(f['pairs']))):
-            raise ValueError('Invalid endpoint index')
-        radii = cat('radii', sites)
-        masses = cat('masses', sites)
-        areas = cat('areas', bonds)
-        young_b = np.concatenate([np.full(c, float(f['young'])) for f, c in zip(foams, bonds)])
-        shear_b = np.concatenate([np.full(c, float(f['shear'])) for f, c in zip(foams, bonds)])
-        fixed = np.concatenate([np.asarray(f['fixed'], dtype=bool) for f in foams])
-        if any(f.get('contacts') is not None for f in foams):
-            raise ValueError('explicit contacts are not supported in a group; use MixedNewtonBonds')
-        host = np.concatenate((points.ravel(), radii, masses, areas, young_b, shear_b))
-        dev = _STAGING.upload(host, self.device)
-        o = np.cumsum([0, 3*n, n, n, m, m, m])
-        self.p = dev[o[0]:o[1]].view(n, 3)
-        self.radii = dev[o[1]:o[2]]
-        masses_d, areas_d = dev[o[2]:o[3]], dev[o[3]:o[4]]
-        young_d, shear_d = dev[o[4]:o[5]], dev[o[5]:o[6]]
-        edges = _STAGING.upload(pairs, self.device)
+        so = np.concatenate(([0], np.cumsum(sites))).astype(np.int64)
+        bo = np.concatenate(([0], np.cumsum(bonds))).astype(np.int64)
+        n, m = int(so[-1]), int(bo[-1])
+        # one copy of each input into pinned staging: per-site float64 [points, radii,
+        # masses], per-bond float64 areas, int32 endpoints (global ids), uint8 flags
+        f64 = _STAGING.host('f8', 5*n + m)
+        i32 = _STAGING.host('i4', 2*m)
+        u8 = _STAGING.host('u1', n)
+        pts, rad, mas, are = f64[:3*n].reshape(n, 3), f64[3*n:4*n], f64[4*n:5*n], f64[5*n:5*n + m]
+        pairs = i32.reshape(m, 2)
+        for k, f in enumerate(foams):
+            a, b, c, d = so[k], so[k+1], bo[k], bo[k+1]
+            pts[a:b] = f['points']
+            rad[a:b] = f['radii']
+            mas[a:b] = f['masses']
+            are[c:d] = f['areas']
+            fp = np.asarray(f['pairs'])
+            if len(fp) and (fp.min() < 0 or fp.max() >= b - a):
+                raise ValueError('Invalid endpoint index')
+            np.add(fp, a, out=pairs[c:d], casting='unsafe')
+            u8[a:b] = np.asarray(f['fixed'], dtype=bool)
+        if np.any(mas <= 0):
+            raise ValueError('Only positive-mass bodies can enter this solver')
+        dev64 = _STAGING.send('f8', 5*n + m, self.device)
+        dev32 = _STAGING.send('i4', 2*m, self.device)
+        self.fixed = _STAGING.send('u1', n, self.device).view(torch.bool)
+        self.p = dev64[:3*n].view(n, 3)
+        self.radii = dev64[3*n:4*n]
+        masses_d, areas_d = dev64[4*n:5*n], dev64[5*n:5*n + m]
+        edges = dev32.view(m, 2).to(torch.int64).contiguous()
         self.n_sites, self.n_bonds = n, m
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         self.n, self.ri, self.rj, self.offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
@@ -137,16 +160,17 @@ class RequestState:
         stream = torch.cuda.current_stream(self.device).cuda_stream
         _lib.check(self._lib.dpf_bond_setup(n, m, edges.data_ptr() if m else None, self.p.data_ptr(),
                                             self.radii.data_ptr(), areas_d.data_ptr(), None, masses_d.data_ptr(),
-                                            0., 0., young_d.data_ptr(), shear_d.data_ptr(),
-                                            self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr(),
-                                            self.kn.data_ptr(), self.ks.data_ptr(), self.kb.data_ptr(),
-                                            self.kt.data_ptr(), self.offset.data_ptr(), self.mass.data_ptr(),
-                                            stream), 'dpf_bond_setup')
-        if np.any(masses <= 0):
-            raise ValueError('Only positive-mass bodies can enter this solver')
+                                            1., 1., None, None, self.n.data_ptr(), self.ri.data_ptr(),
+                                            self.rj.data_ptr(), self.kn.data_ptr(), self.ks.data_ptr(),
+                                            self.kb.data_ptr(), self.kt.data_ptr(), self.offset.data_ptr(),
+                                            self.mass.data_ptr(), stream), 'dpf_bond_setup')
+        # per-request moduli (kn, kb scale with E; ks, kt with G)
+        counts = torch.as_tensor(bonds, device=self.device)
+        E = torch.repeat_interleave(self.tensor([float(f['young']) for f in foams]), counts)
+        G = torch.repeat_interleave(self.tensor([float(f['shear']) for f in foams]), counts)
+        self.kn.mul_(E); self.kb.mul_(E); self.ks.mul_(G); self.kt.mul_(G)
         self.edges = edges
         self._mass32 = self.mass.float()
-        self.fixed = _STAGING.upload(fixed, self.device)
         self.x = self.p.clone()
         self.normal = self.n.clone()
         self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
