@@ -57,6 +57,7 @@ def parse():
     p.add_argument('--served-plain', type=int, default=64,
                    help='requests of the same stream solved one at a time by the plain float64 solver')
     p.add_argument('--served-rate', type=float, default=4000., help='Poisson arrival rate of the stream (1/s)')
+    p.add_argument('--served-batch-sites', type=int, default=8_000_000, help='site capacity of one batch')
     return p.parse_args()
 
 
@@ -163,7 +164,7 @@ def run_served(args, device):
     warm = serving.synthetic_stream(4, seed=12, sites=(1024, 4096))
     serving.Service(device=device).run(warm)
     torch.cuda.synchronize()
-    service = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=2_000_000)
+    service = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=args.served_batch_sites)
     t0 = time.perf_counter()
     finished = service.run(stream)
     torch.cuda.synchronize()
@@ -174,6 +175,7 @@ def run_served(args, device):
                   solves_per_s=len(ok)/wall, p50_ms=1e3*stats['p50'], p99_ms=1e3*stats['p99'],
                   batched_steps=service.batches, sites=int(sum(r.sites for r in stream)),
                   phase_s={k: round(v, 4) for k, v in service.timers.items()},
+                  batch_sizes=service.batch_sizes,
                   newton_per_solve=float(np.mean([r.infos[0]['nonlinear_iterations'] for r in ok])),
                   max_relative_residual=float(max(r.infos[0]['nonlinear_relative_residual'] for r in ok)))
     del finished, ok, stream

@@ -584,7 +584,8 @@ class Service:
         self.tolerance = float(tolerance)
         self.in_use = 0.
         self.batches = 0
-        self.timers = dict(setup=0., batch=0., solve=0., other=0.)
+        self.timers = dict(setup=0., batch=0., solve=0.)
+        self.batch_sizes = []
         self.pool = None
 
     def run(self, requests, clock=time.perf_counter):
@@ -636,6 +637,7 @@ class Service:
             t4 = clock()
             results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
             self.timers['solve'] += clock() - t4
+            self.batch_sizes.append([len(members), batch.n_sites])
             self.batches += 1
             leaving = []
             for req, res in zip(members, results):
