@@ -429,8 +429,9 @@ class Batch(MixedNewtonBonds):
                     done[k] = SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
                 break
             # Each active request's block of the right-hand side is normalised to
-            # unit norm (frozen requests: zero), so the shared Krylov tolerance
-            # bounds every request's own relative linear residual by tol*sqrt(R).
+            # unit norm (frozen requests: zero), so that the shared Krylov
+            # tolerance weighs every request's own relative linear residual
+            # alike; the direction is then judged by each request's line search.
             scale = np.zeros(R)
             for k in active:
                 scale[k] = -1./max(sn[k, 0], 1e-300)
@@ -441,7 +442,7 @@ class Batch(MixedNewtonBonds):
                        scaled.data_ptr(), rhs.data_ptr(), stream)
             self.inner_iterations = 0
             delta, metrics = fgmres(self._newton_operator(y, dt, external), rhs, self._newton_preconditioner(dt),
-                                    tolerance=linear_tolerance/np.sqrt(len(active)), workspace=self._krylov)
+                                    tolerance=linear_tolerance, workspace=self._krylov, strict=False)
             unscale = torch.as_tensor(np.where(scale != 0, -1./np.where(scale != 0, scale, 1.), 0.),
                                       dtype=F64).to(self.device)
             delta = delta.contiguous()
