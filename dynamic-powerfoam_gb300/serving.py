@@ -25,7 +25,9 @@ next one), keeps each request's state resident until it has done all its time
 steps, and records per-request latency.
 """
 import ctypes
+import threading
 import time
+from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -78,7 +80,16 @@ class Staging:
         return out.view(array.shape)
 
 
-_STAGING = Staging()
+_LOCAL = threading.local()
+_PREFETCH = ThreadPoolExecutor(max_workers=1)
+_COPIERS = ThreadPoolExecutor(max_workers=8)
+
+
+def _staging():
+    """The calling thread's pinned staging buffers."""
+    if not hasattr(_LOCAL, 'staging'):
+        _LOCAL.staging = Staging()
+    return _LOCAL.staging
 
 
 def device_incidence(edges, n_sites):
@@ -127,12 +138,15 @@ class RequestState:
         n, m = int(so[-1]), int(bo[-1])
         # one copy of each input into pinned staging: per-site float64 [points, radii,
         # masses], per-bond float64 areas, int32 endpoints (global ids), uint8 flags
-        f64 = _STAGING.host('f8', 5*n + m)
-        i32 = _STAGING.host('i4', 2*m)
-        u8 = _STAGING.host('u1', n)
+        staging = _staging()
+        f64 = staging.host('f8', 5*n + m)
+        i32 = staging.host('i4', 2*m)
+        u8 = staging.host('u1', n)
         pts, rad, mas, are = f64[:3*n].reshape(n, 3), f64[3*n:4*n], f64[4*n:5*n], f64[5*n:5*n + m]
         pairs = i32.reshape(m, 2)
-        for k, f in enumerate(foams):
+
+        def copy(k):
+            f = foams[k]
             a, b, c, d = so[k], so[k+1], bo[k], bo[k+1]
             pts[a:b] = f['points']
             rad[a:b] = f['radii']
@@ -143,11 +157,13 @@ class RequestState:
                 raise ValueError('Invalid endpoint index')
             np.add(fp, a, out=pairs[c:d], casting='unsafe')
             u8[a:b] = np.asarray(f['fixed'], dtype=bool)
+        # numpy releases the GIL for these copies: spread the requests over threads
+        list(_COPIERS.map(copy, range(len(foams))))
         if np.any(mas <= 0):
             raise ValueError('Only positive-mass bodies can enter this solver')
-        dev64 = _STAGING.send('f8', 5*n + m, self.device)
-        dev32 = _STAGING.send('i4', 2*m, self.device)
-        self.fixed = _STAGING.send('u1', n, self.device).view(torch.bool)
+        dev64 = staging.send('f8', 5*n + m, self.device)
+        dev32 = staging.send('i4', 2*m, self.device)
+        self.fixed = staging.send('u1', n, self.device).view(torch.bool)
         self.p = dev64[:3*n].view(n, 3)
         self.radii = dev64[3*n:4*n]
         masses_d, areas_d = dev64[4*n:5*n], dev64[5*n:5*n + m]
@@ -600,12 +616,26 @@ class Service:
         t0 = clock()
         now = lambda: clock() - t0
         batch, members = None, []
+        side = torch.cuda.Stream(device=self.device)
+        prefetch = None      # (requests, future of their group state) being set up on the side stream
+
+        def build(foams):
+            with torch.cuda.stream(side):
+                group = RequestState.group(foams, device=self.device)
+                event = torch.cuda.Event()
+                event.record(side)
+            return group, event
+
         while pending or waiting or active:
             while pending and pending[0].arrival <= now():
                 waiting.append(pending.pop(0))
             admitted = []
             sites = sum(r.sites for r in active)
-            while waiting:
+            if prefetch is not None:
+                # requests already being set up are admitted first, as one group
+                admitted = prefetch[0]
+                sites += sum(r.sites for r in admitted)
+            while waiting and prefetch is None:
                 req = waiting[0]
                 need = footprint_bytes(req.sites, req.bonds)
                 if self.in_use + need > self.hbm_budget or ((active or admitted) and
@@ -626,15 +656,39 @@ class Service:
                 t1 = clock()
                 parts = [r.part for r in active]
                 if admitted:
-                    parts.append(RequestState.group([r.foam for r in admitted], device=self.device))
+                    if prefetch is not None:
+                        group, event = prefetch[1].result()
+                        torch.cuda.current_stream(self.device).wait_event(event)
+                        prefetch = None
+                    else:
+                        group, event = build([r.foam for r in admitted])
+                        torch.cuda.current_stream(self.device).wait_event(event)
+                    parts.append(group)
                 t2 = clock()
                 active += admitted
                 members = list(active)
                 batch = Batch(parts, pool=self.pool)
-                ext = _STAGING.upload(np.concatenate([r.load for r in members]), self.device)
+                ext = _staging().upload(np.concatenate([r.load for r in members]), self.device)
                 t3 = clock()
                 self.timers['setup'] += t2 - t1
                 self.timers['batch'] += t3 - t2
+            # set up the next group (requests waiting now) while this batch solves
+            if prefetch is None and waiting:
+                nxt, cap = [], 0
+                budget = self.in_use
+                while waiting:
+                    req = waiting[0]
+                    need = footprint_bytes(req.sites, req.bonds)
+                    if budget + need > self.hbm_budget or (nxt and cap + req.sites > self.max_batch_sites):
+                        break
+                    waiting.pop(0)
+                    budget += need
+                    self.in_use += need
+                    req.started = now()
+                    nxt.append(req)
+                    cap += req.sites
+                if nxt:
+                    prefetch = (nxt, _PREFETCH.submit(build, [r.foam for r in nxt]))
             t4 = clock()
             results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
             self.timers['solve'] += clock() - t4
@@ -650,7 +704,7 @@ class Service:
                 req.done_steps += 1
                 if req.done_steps >= req.steps:
                     leaving.append(req)
-            if leaving or (waiting or (pending and pending[0].arrival <= now())):
+            if leaving or waiting or prefetch is not None or (pending and pending[0].arrival <= now()):
                 stamp = now()
                 for k, req in enumerate(members):
                     if req in leaving:
