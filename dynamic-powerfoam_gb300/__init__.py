@@ -8,6 +8,7 @@ CPU fallback.
 from .foam import jittered_lattice_foam, gravity_load, regular_edges, morton_order
 from .newton import (LinearBonds, FiniteBonds, NewtonBonds, FastNewtonBonds, MixedNewtonBonds, AdaptiveIntervals,
                      SubdivideError, fgmres, incidence, guard_error)
+from .adjoint import DifferentiableBonds
 
 # Reference class names (experiments/bonded_dem_linear_gpu.py, bonded_dem_finite_gpu.py).
 LinearBondsGPU = LinearBonds
@@ -15,4 +16,4 @@ FiniteBondsGPU = FiniteBonds
 
 __all__ = ['jittered_lattice_foam', 'gravity_load', 'regular_edges', 'morton_order', 'LinearBonds',
            'FiniteBonds', 'NewtonBonds', 'FastNewtonBonds', 'MixedNewtonBonds', 'LinearBondsGPU', 'FiniteBondsGPU',
-           'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error']
+           'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error', 'DifferentiableBonds']

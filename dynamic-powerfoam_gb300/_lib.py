@@ -93,6 +93,12 @@ SIGNATURES = {
     'dpf_segment_axpy': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_segment_select': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_static_max_bonds': (i64, []),
+    'dpf_adjoint_jacobian_doubles': (i64, [i64]),
+    'dpf_adjoint_slot_doubles': (i64, [i64]),
+    'dpf_adjoint_local_jacobian': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp]),
+    'dpf_adjoint_apply_jt': (i32, [P(Graph), vp, vp, vp, f64, vp, vp, vp, vp]),
+    'dpf_adjoint_bond_vjp': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, f64, vp, i32, vp, vp, vp, vp, vp,
+                                   vp]),
 }
 
 
@@ -106,6 +112,7 @@ KERNELS = {
     'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 3, 'dpf_mixed_stiffness_apply': 2,
     'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 1,
     'dpf_segment_axpy': 1, 'dpf_segment_select': 1,
+    'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
 }
 LAUNCHES = {'count': 0}
 

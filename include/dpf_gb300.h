@@ -392,6 +392,43 @@ int dpf_segment_axpy(int64_t n_sites, const int32_t *seg, const double *factor, 
 int dpf_segment_select(int64_t n_sites, const int32_t *seg, const uint8_t *keep, const double *a,
                        const double *b, double *out, void *stream);
 
+/* ---- Adjoint of the implicit step (implicit-function theorem) ----
+ * Replace the dense autograd Jacobians of _ImplicitIncrement.backward and of
+ * DifferentiableBonds.step (experiments/bonded_dem_differentiable.py:26-38,
+ * 139-144) with per-bond forward-mode derivatives of the float64 trial
+ * (experiments/bonded_dem_finite_gpu.py:87-116).  Bond inputs, in order:
+ * y_i (6), y_j (6), x_i (3), x_j (3), normal (3), offset (3), fn, fs (3), mt,
+ * mb (3), kn, ks, kb, kt.  Bond outputs: the midpoint wrench F, T_i, T_j
+ * (site i receives (F, T_i), site j (-F, T_j)) and the end history normal (3),
+ * offset (3), fn, fs (3), mt, mb (3). */
+
+/* Doubles of the local-Jacobian array (108 per bond) and of the per-bond
+ * slot scratch (18 per bond) of the entry points below. */
+int64_t dpf_adjoint_jacobian_doubles(int64_t n_bonds);
+int64_t dpf_adjoint_slot_doubles(int64_t n_bonds);
+
+/* jacobian[b] = d(F, T_i, T_j)/d(y_i, y_j) at increment y (9 x 12 row-major). */
+int dpf_adjoint_local_jacobian(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+                               const double *y, double *jacobian, void *stream);
+
+/* out = J^T lam of the unscaled midpoint residual M y - M dt v - dt^2/2 (F + e)
+ * on free sites, out = lam on fixed sites; lam's fixed rows must be zero.
+ * slots: dpf_adjoint_slot_doubles scratch. */
+int dpf_adjoint_apply_jt(const dpf_graph *g, const double *jacobian, const double *mass,
+                         const uint8_t *fixed, double dt, const double *lam, double *out,
+                         double *slots, void *stream);
+
+/* Vector-Jacobian product of the trial at increment y for the output adjoints
+ * coef * (wrench adjoint of the site vector lam) + end_adjoint (M x 14, the
+ * end-history layout); either may be null.  ADDS the input adjoints to
+ * history_adjoint (M x 14, same layout), stiffness_adjoint (M x 4: kn ks kb kt),
+ * y_adjoint (N x 6, only when with_increment) and x_adjoint (N x 3); a null
+ * site array is skipped.  Site sums follow the incidence order: deterministic. */
+int dpf_adjoint_bond_vjp(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
+                         const double *y, const double *lam, double coef, const double *end_adjoint,
+                         int with_increment, double *history_adjoint, double *stiffness_adjoint,
+                         double *y_adjoint, double *x_adjoint, double *slots, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -203,6 +203,42 @@ def main(reference):
     np.savez_compressed(HERE/'fgmres_381.npz', a=np64(a), b=np64(b), x=np64(x),
                         iterations=info['iterations'], relative=info['relative_residual'])
 
+    # ---- differentiable rollout (bonded_dem_differentiable.py): per-cell log
+    # stiffness multipliers, three implicit steps, weighted-position loss ----
+    from experiments.bonded_dem_differentiable import DifferentiableBonds
+    for name, prestress_case in (('adjoint_unstressed', False),):
+        rng = np.random.default_rng(906)
+        p = np.array(np.meshgrid(np.arange(3), np.arange(2), np.arange(2))).reshape(3, -1).T*.4
+        p = p + rng.normal(0, .008, p.shape)
+        pairs = np.array([(i, j) for i in range(len(p)) for j in range(i+1, len(p))
+                          if np.linalg.norm(p[i]-p[j]) < .65])
+        radii = rng.uniform(.3, .4, len(p))
+        area = rng.uniform(.008, .016, len(pairs))
+        contacts = .5*(p[pairs[:, 0]]+p[pairs[:, 1]]) + rng.normal(0, .025, (len(pairs), 3))
+        mass = np.geomspace(.01, 1., len(p)); rng.shuffle(mass)
+        fixed = p[:, 0] < .1
+        model = DifferentiableBonds(points=p, radii=radii, pairs=pairs, areas=area, masses=mass, fixed=fixed,
+                                    contacts=contacts, device='cpu')
+        arng = np.random.default_rng(4242)
+        theta = torch.tensor(arng.normal(0, .1, (len(p), 4)), dtype=torch.float64, requires_grad=True)
+        steps, dt = 3, .02
+        loads = []
+        for t in range(steps):
+            load = torch.zeros((len(p), 6), dtype=torch.float64)
+            load[:, :3] = torch.tensor(arng.normal(0, .05, (len(p), 3)))
+            load[:, 2] -= .3*torch.tensor(mass)
+            load[torch.tensor(fixed)] = 0
+            loads.append(load.requires_grad_(True))
+        weights = torch.tensor(arng.normal(size=(steps+1, len(p), 3)), dtype=torch.float64)
+        positions, _ = model.rollout(theta, loads, dt)
+        loss = (positions*weights).sum()
+        grads = torch.autograd.grad(loss, [theta] + loads)
+        np.savez_compressed(HERE/f'{name}.npz', points=p, radii=radii, pairs=pairs, areas=area, masses=mass,
+                            fixed=fixed, contacts=contacts, theta=np64(theta), loads=np.stack([np64(l) for l in loads]),
+                            weights=np64(weights), dt=dt, positions=np64(positions), loss=float(loss),
+                            grad_theta=np64(grads[0]), grad_loads=np.stack([np64(g) for g in grads[1:]]))
+        print(name, float(loss), np.abs(np64(grads[0])).max())
+
     # ---- jittered 8^3 lattice foam under gravity, three reference steps ----
     foam = dpf_gb300.jittered_lattice_foam(8, seed=0)
     load = dpf_gb300.gravity_load(foam)
