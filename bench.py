@@ -53,6 +53,7 @@ def parse():
     p.add_argument('--precision', default='mixed', choices=('mixed', 'f64'))
     p.add_argument('--plain-steps', type=int, default=3,
                    help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
+    p.add_argument('--hvp-launches', type=int, default=50, help='timed launches of the standalone tiled HVP (0: skip)')
     p.add_argument('--served', type=int, default=512, help='requests of the served mixed-size stream (0: skip)')
     p.add_argument('--served-plain', type=int, default=64,
                    help='requests of the same stream solved one at a time by the plain float64 solver')
@@ -144,6 +145,50 @@ class ClockSampler:
         reasons = sorted({n for r in rows for n, v in zip(names, r[4:8]) if v.lower() == 'active'})
         return dict(sm_mhz=statistics.median(sm) if sm else None, sm_max_mhz=max(mx) if mx else None,
                     reasons=reasons, samples=len(rows))
+
+
+def run_hvp(s, dt, peak, peaks, launches=50):
+    """Bond-HVPs/s of the tiled float32 operator y = (diag M + dt^2/4 K) q on the
+    bench foam: each launch timed alone with CUDA events on the launching
+    stream, L2 flushed (a 256 MB write) between launches."""
+    import ctypes
+    import torch
+    from dpf_gb300 import _lib
+    tiles = s._tiles
+    s._pack_tiles(tiles, dt)
+    stream = torch.cuda.current_stream()
+    n, m = s.n_sites, s.n_bonds
+    q = torch.randn((n, 6), dtype=torch.float32, device=s.device)
+    y = torch.empty_like(q)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device=s.device)
+
+    def launch():
+        _lib.call('dpf_tiled_hvp', ctypes.byref(s._graph), ctypes.byref(tiles.struct), tiles.entries.data_ptr(),
+                  s._mass2.data_ptr(), s.fixed.data_ptr(), q.data_ptr(), y.data_ptr(), tiles.status.data_ptr(),
+                  tiles.threads, tiles.stages, stream.cuda_stream)
+    for _ in range(3):
+        launch()
+    times = []
+    for _ in range(launches):
+        flush.fill_(1.0)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        launch()
+        end.record(stream)
+        times.append((start, end))
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in times]
+    mean = sum(ms)/len(ms)
+    # algorithmic bytes of one float32 HVP: per bond i,j 8 + n, ri, rj 36 + k 16 = 60 B;
+    # per site q 24 + y 24 + (m, I) 8 = 56 B
+    alg = 60*m + 56*n
+    achieved = alg/(mean*1e-3)/1e9
+    return dict(kernel='tiled_hvp_kernel', bond_hvps_per_s=m/(mean*1e-3), mean_ms=mean, min_ms=min(ms),
+                launches=len(ms), algorithmic_bytes=alg, achieved=achieved, peak=peak, unit='GB/s',
+                frac=achieved/peak, peak_source='measured' if peaks else 'fallback', l2='flushed between launches',
+                tile=dict(max_entries=int(tiles.host['max_entries']), threads=tiles.threads, stages=tiles.stages,
+                          tiles=int(tiles.host['n_tiles']), entries_per_bond=tiles.n_entries/max(1, m)),
+                autotune_ms={'x'.join(map(str, k)): v for k, v in (s.tile_timings or {}).items()})
 
 
 def run_served(args, device):
@@ -322,11 +367,12 @@ def run_ours(args):
         alg = dict(jvp=bytes_jvp, pcg=(120*n_bonds + 688*n_sites)*cg/pcg_launches, residual=bytes_jvp)
     else:
         # float32 bond data: JVP 80 B/bond + 96 B/site; HVP (K d) 60 B/bond +
-        # 56 B/site plus the float32 block and vector traffic of a CG
-        # iteration (288 B/site); residual 80 B/bond + 72 B/site; blocks 128 B/bond
+        # 56 B/site plus the vector traffic of a single-reduction CG iteration
+        # (read u, w, p, s, x, r and the 21-float block inverse, write p, s, x,
+        # r, u: 348 B/site); residual 80 B/bond + 72 B/site; blocks 128 B/bond
         # (two incidences of the tangent) + 296 B/site; setup 160 B/bond of
         # float64 state read + 112 B/bond of records written + 144 B/site.
-        alg = dict(jvp=80*n_bonds + 96*n_sites, pcg=(60*n_bonds + 344*n_sites)*cg/pcg_launches,
+        alg = dict(jvp=80*n_bonds + 96*n_sites, pcg=(60*n_bonds + 404*n_sites)*cg/pcg_launches,
                    residual=80*n_bonds + 72*n_sites, scaling=128*n_bonds + 296*n_sites,
                    setup=272*n_bonds + 144*n_sites, commit=112*n_bonds + 208*n_bonds + 48*n_sites)
     dominant = max(kernels, key=lambda k: kernels[k]['total_ms']) if kernels else None
@@ -344,6 +390,8 @@ def run_ours(args):
                     traffic=None, peak_source='measured' if peaks else 'fallback',
                     launches=kernels[dominant]['launches'], mean_ms=kernels[dominant]['mean_ms'])
 
+    hvp = run_hvp(s, args.dt, peak, peaks, launches=args.hvp_launches) \
+        if args.precision == 'mixed' and args.hvp_launches > 0 and getattr(s, '_tiles', None) is not None else None
     served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None
     if rank != 0:
         return
@@ -368,7 +416,8 @@ def run_ours(args):
                             krylov_per_solve=mean('krylov_iterations'), cg_per_solve=mean('cg_iterations')),
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
-                gpu_launches=launches, kernels=kernels, roofline=roof, cpu_baseline=cpu, plain_f64=plain, served=served,
+                gpu_launches=launches, kernels=kernels, roofline=roof, hvp=hvp, cpu_baseline=cpu, plain_f64=plain,
+                served=served,
                 relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)

@@ -1,0 +1,956 @@
+// Site tiles of the bond graph and the tiled float32 Hessian-vector product
+// y = (diag M + dt^2/4 K) q (experiments/bonded_dem_linear_gpu.py:42-52, 74-77)
+// with the elastic block-Jacobi PCG built on it
+// (experiments/bonded_dem_newton.py:107-130).
+//
+// A tile is a contiguous range of sites (the foam generator orders sites along
+// a Morton curve, so a range is a compact patch) plus every bond touching it
+// ("entries"; a bond between two tiles is an entry of both) and the outside
+// endpoints of those bonds ("halo").  Persistent CTAs walk their tiles with
+// two shared-memory buffers: while one tile computes, the next tile's entry
+// records and incidence metadata arrive by TMA bulk copies (completing on an
+// mbarrier) and its site vectors by cp.async.  Per tile:
+//   1. each thread reads its entries' records to registers;
+//   2. computes the entry wrenches [F_i, T_i, T_j] into the records' space;
+//   3. sums each site's wrench contributions over its incidence list in the
+//      list's order (no atomics: deterministic) and hands the sum to the
+//      caller's epilogue (y of the HVP, w and (w, u) of the PCG).
+// Only bonds cut by tile boundaries are read twice; wrenches never go to
+// global memory.
+#include <algorithm>
+#include <vector>
+
+#include "common.cuh"
+
+namespace dpf {
+namespace tiles {
+
+#ifndef DPF_TILE_LANES
+#define DPF_TILE_LANES 2
+#endif
+
+constexpr int kLanes = DPF_TILE_LANES;  // lanes per site in the site sums
+constexpr int kPer = 2;                 // entries per thread and tile (read to registers before W overwrites them)
+#ifndef DPF_TILE_THREADS_MAX
+#define DPF_TILE_THREADS_MAX 384
+#endif
+#ifndef DPF_TILE_MIN_BLOCKS
+#define DPF_TILE_MIN_BLOCKS 2
+#endif
+constexpr int kTileThreadsMax = DPF_TILE_THREADS_MAX;
+constexpr unsigned long long kWaitNs = 1000000000ull;  // mbarrier waits give up after 1 s
+
+struct TileGraph {
+    int32_t n_tiles;
+    const int32_t *tile_site, *tile_entry, *tile_halo, *tile_meta_off, *halo_site;
+    const uint32_t *tile_meta;
+    const float4 *e0, *e1, *e2;  // entry planes: (n, ri.x), (ri.y, ri.z, L, a kn), (a ks, a kb, a kt, ends)
+};
+
+// Byte offsets inside one of the two shared-memory tile buffers.
+struct Layout {
+    uint32_t plane;   // bytes of one record plane (16 * max entries)
+    uint32_t qown, qhalo, meta, size;
+    int stages;       // tile buffers in the ring
+};
+
+// ---- asynchronous copies (TMA bulk + mbarrier, cp.async) -------------------
+
+__device__ __forceinline__ uint32_t saddr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(saddr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(saddr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(saddr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Global -> shared bulk copy completing on `bar` (16-byte aligned, multiple of 16 bytes).
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     saddr(dst)),
+                 "l"(src), "r"(bytes), "r"(saddr(bar))
+                 : "memory");
+}
+// Order this thread's earlier generic-proxy shared accesses before later bulk writes.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(saddr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Wait for phase `parity` of `bar`; false (and the status bit) after kWaitNs.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *status) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try_wait(bar, parity)) {
+        if (global_ns() - t0 > kWaitNs) {
+            atomicOr(status, DPF_ERR_BARRIER_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+
+// ---- one entry -------------------------------------------------------------------
+
+// alpha K q wrench of one entry as three float4: (F, Ti.x), (Ti.y, Ti.z, Tj.x,
+// Tj.y), (Tj.z, -, -, -) with F = F_i (site i adds F_i, T_i; site j adds -F_i, T_j).
+__device__ __forceinline__ void entry_wrench(float4 a, float4 b, float4 c, const float *qown, const float *qhalo,
+                                             int T, float4 *W) {
+    const uint32_t ends = __float_as_uint(c.w);
+    const int li = (int)(ends & 0xffffu), lj = (int)(ends >> 16);
+    const float2 *qi = reinterpret_cast<const float2 *>(li < T ? qown + 6 * li : qhalo + 6 * (li - T));
+    const float2 *qj = reinterpret_cast<const float2 *>(lj < T ? qown + 6 * lj : qhalo + 6 * (lj - T));
+    const float2 ui0 = qi[0], ui1 = qi[1], ui2 = qi[2], uj0 = qj[0], uj1 = qj[1], uj2 = qj[2];
+    const float nx = a.x, ny = a.y, nz = a.z;
+    const float rix = a.w, riy = b.x, riz = b.y, L = b.z;
+    const float rjx = rix - L * nx, rjy = riy - L * ny, rjz = riz - L * nz;
+    const float kn = b.w, ks = c.x, kb = c.y, kt = c.z;
+    const float wix = ui1.y, wiy = ui2.x, wiz = ui2.y, wjx = uj1.y, wjy = uj2.x, wjz = uj2.y;
+    // du = u_j - u_i + w_j x r_j - w_i x r_i ; dw = w_j - w_i
+    const float dux = uj0.x - ui0.x + (wjy * rjz - wjz * rjy) - (wiy * riz - wiz * riy);
+    const float duy = uj0.y - ui0.y + (wjz * rjx - wjx * rjz) - (wiz * rix - wix * riz);
+    const float duz = uj1.x - ui1.x + (wjx * rjy - wjy * rjx) - (wix * riy - wiy * rix);
+    const float dwx = wjx - wix, dwy = wjy - wiy, dwz = wjz - wiz;
+    const float un = (kn - ks) * (dux * nx + duy * ny + duz * nz);
+    const float wn = (kt - kb) * (dwx * nx + dwy * ny + dwz * nz);
+    const float fx = ks * dux + un * nx, fy = ks * duy + un * ny, fz = ks * duz + un * nz;
+    const float mx = kb * dwx + wn * nx, my = kb * dwy + wn * ny, mz = kb * dwz + wn * nz;
+    const float tix = -(riy * fz - riz * fy) - mx, tiy = -(riz * fx - rix * fz) - my;
+    const float tiz = -(rix * fy - riy * fx) - mz;
+    const float tjx = (rjy * fz - rjz * fy) + mx, tjy = (rjz * fx - rjx * fz) + my;
+    const float tjz = (rjx * fy - rjy * fx) + mz;
+    W[0] = make_float4(-fx, -fy, -fz, tix);
+    W[1] = make_float4(tiy, tiz, tjx, tjy);
+    W[2] = make_float4(tjz, 0.0f, 0.0f, 0.0f);
+}
+
+struct TileView {
+    int64_t a, e0, h0, meta;
+    int T, E, H, words, halo_word;  // halo_word: first halo-site word in the metadata
+};
+
+__device__ __forceinline__ TileView tile_view(const TileGraph &G, int t) {
+    TileView v;
+    v.a = G.tile_site[t];
+    v.T = G.tile_site[t + 1] - G.tile_site[t];
+    v.e0 = G.tile_entry[t];
+    v.E = G.tile_entry[t + 1] - G.tile_entry[t];
+    v.h0 = G.tile_halo[t];
+    v.H = G.tile_halo[t + 1] - G.tile_halo[t];
+    v.meta = G.tile_meta_off[t];
+    v.words = G.tile_meta_off[t + 1] - G.tile_meta_off[t];
+    v.halo_word = v.words - ((v.H + 3) & ~3);
+    return v;
+}
+
+// Own-site q of a tile in shared memory starts at buf + L.qown + (24 a mod 16),
+// so the 16-byte-aligned interior of its global range maps to an aligned
+// shared address (bulk copy) and the at most two 8-byte ends go by cp.async.
+struct OwnRange {
+    uint64_t begin, end, lo, hi;  // global byte offsets in q; [lo, hi) 16-aligned interior
+    uint32_t shift;               // (24 a) mod 16
+};
+
+__device__ __forceinline__ OwnRange own_range(const TileView &v) {
+    OwnRange r;
+    r.begin = 24ull * (uint64_t)v.a;
+    r.end = r.begin + 24ull * (uint64_t)v.T;
+    r.lo = (r.begin + 15) & ~15ull;
+    r.hi = r.end & ~15ull;
+    if (r.hi < r.lo) r.hi = r.lo;
+    r.shift = (uint32_t)(r.begin & 15u);
+    return r;
+}
+
+// Thread 0: bulk copies of a tile's entry records, metadata and own-site q interior.
+__device__ __forceinline__ void issue_bulk(const TileGraph &G, const Layout &L, const TileView &v, const float *q,
+                                           unsigned char *buf, uint64_t *bar) {
+    fence_proxy_async();
+    const uint32_t plane = 16u * (uint32_t)v.E, meta = 4u * (uint32_t)v.words;
+    const OwnRange o = own_range(v);
+    const uint32_t own = (uint32_t)(o.hi - o.lo);
+    mbar_expect_tx(bar, 3 * plane + meta + own);
+    if (v.E) {
+        bulk_load(buf, G.e0 + v.e0, plane, bar);
+        bulk_load(buf + L.plane, G.e1 + v.e0, plane, bar);
+        bulk_load(buf + 2 * L.plane, G.e2 + v.e0, plane, bar);
+    }
+    bulk_load(buf + L.meta, G.tile_meta + v.meta, meta, bar);
+    if (own)
+        bulk_load(buf + L.qown + o.shift + (uint32_t)(o.lo - o.begin),
+                  reinterpret_cast<const unsigned char *>(q) + o.lo, own, bar);
+}
+
+// All threads, once the tile's bulk copies have landed: cp.async of the
+// own-site q ends outside the bulk interior and of the halo sites' q (halo
+// site list at the end of the tile's metadata).
+__device__ __forceinline__ void issue_q(const TileView &v, const Layout &L, unsigned char *buf, const float *q) {
+    const OwnRange o = own_range(v);
+    const unsigned char *qb = reinterpret_cast<const unsigned char *>(q);
+    unsigned char *own = buf + L.qown + o.shift;
+    const int head = (int)((o.lo - o.begin) >> 3), tail = (int)((o.end - o.hi) >> 3);
+    for (int k = threadIdx.x; k < head + tail; k += blockDim.x) {
+        const uint64_t off = k < head ? 8ull * k : (o.hi - o.begin) + 8ull * (k - head);
+        cp_async8(own + off, qb + o.begin + off);
+    }
+    const int32_t *meta = reinterpret_cast<const int32_t *>(buf + L.meta);
+    const int32_t *halo = meta + v.halo_word;
+    float2 *hal = reinterpret_cast<float2 *>(buf + L.qhalo);
+    for (int k = threadIdx.x; k < 3 * v.H; k += blockDim.x) {
+        const int slot = k / 3, part = k - 3 * slot;
+        cp_async8(hal + k, reinterpret_cast<const float2 *>(q + 6 * (int64_t)halo[slot]) + part);
+    }
+    cp_async_commit();
+}
+
+// The alpha K q part of local site sl from the tile's wrenches (all kLanes
+// lanes of a group call it together).  span[sl] = start | mid << 16: the
+// site's incidences [start, mid) are i ends, [mid, next start) j ends, in
+// incidence order with a fixed lane split.
+__device__ __forceinline__ void site_sum(const float4 *W, const uint32_t *span, const uint16_t *codes, int sl,
+                                         bool valid, int lane, float acc[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
+    if (valid) {
+        const uint32_t sp = span[sl];
+        const int k0 = (int)(sp & 0xffffu), mid = (int)(sp >> 16), k1 = (int)(span[sl + 1] & 0xffffu);
+        for (int k = k0 + lane; k < mid; k += kLanes) {
+            const float4 *w = W + 3 * codes[k];
+            const float4 w0 = w[0], w1 = w[1];
+            acc[0] += w0.x;
+            acc[1] += w0.y;
+            acc[2] += w0.z;
+            acc[3] += w0.w;
+            acc[4] += w1.x;
+            acc[5] += w1.y;
+        }
+        for (int k = mid + lane; k < k1; k += kLanes) {
+            const float4 *w = W + 3 * codes[k];
+            const float4 w0 = w[0], w1 = w[1];
+            const float w2 = w[2].x;
+            acc[0] -= w0.x;
+            acc[1] -= w0.y;
+            acc[2] -= w0.z;
+            acc[3] += w1.z;
+            acc[4] += w1.w;
+            acc[5] += w2;
+        }
+    }
+#pragma unroll
+    for (int o = 1; o < kLanes; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+}
+
+// Ring of L.stages shared-memory tile buffers, one mbarrier each.
+struct Pipe {
+    unsigned char *base;
+    uint64_t *bar;
+    uint32_t parity;  // bit b: phase parity of buffer b's next completion
+};
+
+__device__ __forceinline__ Pipe pipe_init(unsigned char *smem, const Layout &L) {
+    Pipe P;
+    P.base = smem;
+    P.bar = reinterpret_cast<uint64_t *>(smem + (size_t)L.stages * L.size);
+    P.parity = 0u;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < L.stages; ++b) mbar_init(P.bar + b, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    return P;
+}
+
+// Wait (all threads) for buffer b's bulk copies; false after the time limit.
+__device__ __forceinline__ bool wait_bulk(Pipe &P, int b, int *status) {
+    const bool ok = mbar_wait(P.bar + b, (P.parity >> b) & 1u, status);
+    P.parity ^= 1u << b;
+    return !__syncthreads_or(!ok);
+}
+
+// For each own site s of every tile of this block: epi(s, q_s (shared), acc)
+// with acc the alpha K q sum.  Tile j of the block uses buffer j mod S: the
+// bulk copies of tile j + S - 1 are issued while tile j computes, and the
+// q gather of tile j + 1 (whose metadata has landed) overlaps it too.
+// False on a wait timeout.
+template <class Epi>
+__device__ __forceinline__ bool for_tiles(const TileGraph &G, const Layout &L, Pipe &P, const float *q, int *status,
+                                          Epi &epi) {
+    if ((int)blockIdx.x >= G.n_tiles) return true;
+    const int S = L.stages;
+    const int n_local = (G.n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
+    auto tile_of = [&](int j) { return (int)blockIdx.x + j * (int)gridDim.x; };
+    auto buf_of = [&](int b) { return P.base + (size_t)b * L.size; };
+    if (threadIdx.x == 0)
+        for (int j = 0; j < S - 1 && j < n_local; ++j)
+            issue_bulk(G, L, tile_view(G, tile_of(j)), q, buf_of(j), P.bar + j);
+    if (!wait_bulk(P, 0, status)) return false;
+    issue_q(tile_view(G, tile_of(0)), L, buf_of(0), q);
+    const int lane = threadIdx.x & (kLanes - 1);
+    const int groups = blockDim.x / kLanes;
+    int b = 0;
+    for (int j = 0; j < n_local; ++j) {
+        const TileView v = tile_view(G, tile_of(j));
+        const int bn = b + 1 == S ? 0 : b + 1;
+        if (threadIdx.x == 0 && j + S - 1 < n_local) {
+            const int bf = b == 0 ? S - 1 : b - 1;  // buffer of tile j - 1, free
+            issue_bulk(G, L, tile_view(G, tile_of(j + S - 1)), q, buf_of(bf), P.bar + bf);
+        }
+        if (j + 1 < n_local) {
+            if (!wait_bulk(P, bn, status)) return false;
+            issue_q(tile_view(G, tile_of(j + 1)), L, buf_of(bn), q);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            cp_async_wait_all();
+        }
+        __syncthreads();
+        unsigned char *buf = buf_of(b);
+        const float4 *p0 = reinterpret_cast<const float4 *>(buf);
+        const float4 *p1 = reinterpret_cast<const float4 *>(buf + L.plane);
+        const float4 *p2 = reinterpret_cast<const float4 *>(buf + 2 * L.plane);
+        float4 ra[kPer], rb[kPer], rc[kPer];
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int e = threadIdx.x + u * blockDim.x;
+            if (e < v.E) {
+                ra[u] = p0[e];
+                rb[u] = p1[e];
+                rc[u] = p2[e];
+            }
+        }
+        __syncthreads();  // records consumed: the wrenches overwrite them
+        float4 *W = reinterpret_cast<float4 *>(buf);
+        const float *qown = reinterpret_cast<const float *>(buf + L.qown + own_range(v).shift);
+        const float *qhalo = reinterpret_cast<const float *>(buf + L.qhalo);
+#pragma unroll
+        for (int u = 0; u < kPer; ++u) {
+            const int e = threadIdx.x + u * blockDim.x;
+            if (e < v.E) entry_wrench(ra[u], rb[u], rc[u], qown, qhalo, v.T, W + 3 * e);
+        }
+        __syncthreads();
+        const uint32_t *span = reinterpret_cast<const uint32_t *>(buf + L.meta);
+        const uint16_t *codes = reinterpret_cast<const uint16_t *>(span + v.T + 1);
+        const int rounds = (v.T + groups - 1) / groups;
+        for (int rd = 0; rd < rounds; ++rd) {
+            const int sl = rd * groups + (int)threadIdx.x / kLanes;
+            const bool valid = sl < v.T;
+            float acc[6];
+            site_sum(W, span, codes, sl, valid, lane, acc);
+            if (valid && lane == 0) epi(v.a + sl, qown + 6 * sl, acc);
+        }
+        __syncthreads();  // buffer b free
+        b = bn;
+    }
+    return true;
+}
+
+__device__ __forceinline__ void ld6(const float *p, float v[6]) {
+    const float2 *q = reinterpret_cast<const float2 *>(p);
+    const float2 a = q[0], b = q[1], c = q[2];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
+}
+__device__ __forceinline__ void st6(float *p, const float v[6]) {
+    float2 *q = reinterpret_cast<float2 *>(p);
+    q[0] = make_float2(v[0], v[1]);
+    q[1] = make_float2(v[2], v[3]);
+    q[2] = make_float2(v[4], v[5]);
+}
+
+// (diag M) q + alpha K q with identity rows on fixed sites.
+__device__ __forceinline__ void operator_row(const float2 *mass2, const uint8_t *fixed, int64_t s, const float *qs,
+                                             const float acc[6], float out[6]) {
+    if (fixed[s]) {
+#pragma unroll
+        for (int c = 0; c < 6; ++c) out[c] = qs[c];
+    } else {
+        const float2 m = mass2[s];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) out[c] = fmaf(c < 3 ? m.x : m.y, qs[c], acc[c]);
+    }
+}
+
+// ---- standalone HVP ------------------------------------------------------------
+
+struct HvpArgs {
+    TileGraph G;
+    Layout L;
+    const float2 *mass2;  // (m, I) per site
+    const uint8_t *fixed;
+    const float *q;
+    float *y;
+    int *status;
+};
+
+struct HvpEpi {
+    const HvpArgs &a;
+    __device__ __forceinline__ void operator()(int64_t s, const float *qs, const float acc[6]) const {
+        float out[6];
+        operator_row(a.mass2, a.fixed, s, qs, acc, out);
+        st6(a.y + 6 * s, out);
+    }
+};
+
+__global__ void __launch_bounds__(kTileThreadsMax, DPF_TILE_MIN_BLOCKS) tiled_hvp_kernel(HvpArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Pipe P = pipe_init(smem, a.L);
+    HvpEpi epi{a};
+    for_tiles(a.G, a.L, P, a.q, a.status, epi);
+}
+
+// ---- packing -----------------------------------------------------------------
+
+struct PackArgs {
+    int64_t n_entries;
+    const int32_t *entry_bond;
+    const uint32_t *entry_ends;
+    const float4 *t0, *t1, *t2, *t3;  // tangent records (n, kn), (ri, ks), (rj, kb), (kt, i, j, -)
+    float alpha;
+    float4 *e0, *e1, *e2;
+};
+
+__global__ void __launch_bounds__(kThreads) pack_entries_kernel(PackArgs a) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= a.n_entries) return;
+    const int64_t b = a.entry_bond[e];
+    const float4 n = a.t0[b], ri = a.t1[b], rj = a.t2[b], g = a.t3[b];
+    const float L = (ri.x - rj.x) * n.x + (ri.y - rj.y) * n.y + (ri.z - rj.z) * n.z;
+    a.e0[e] = make_float4(n.x, n.y, n.z, ri.x);
+    a.e1[e] = make_float4(ri.y, ri.z, L, a.alpha * n.w);
+    a.e2[e] = make_float4(a.alpha * ri.w, a.alpha * rj.w, a.alpha * g.x, __uint_as_float(a.entry_ends[e]));
+}
+
+// P (36 floats, symmetric) -> 21 upper-triangle floats padded to 24; (m, I).
+__global__ void __launch_bounds__(kThreads) pack_sites_kernel(int64_t n, const float *P36, const float *mass32,
+                                                              float4 *P24, float2 *mass2) {
+    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const float *p = P36 + 36 * s;
+    float u[24];
+    int k = 0;
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+        for (int c = r; c < 6; ++c) u[k++] = p[6 * r + c];
+    u[21] = u[22] = u[23] = 0.0f;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) P24[6 * s + q] = make_float4(u[4 * q], u[4 * q + 1], u[4 * q + 2], u[4 * q + 3]);
+    if (mass2) mass2[s] = make_float2(mass32[6 * s], mass32[6 * s + 3]);
+}
+
+__device__ __forceinline__ void sym6(const float4 *P24, float P[21]) {
+    float u[24];
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const float4 v = P24[q];
+        u[4 * q] = v.x;
+        u[4 * q + 1] = v.y;
+        u[4 * q + 2] = v.z;
+        u[4 * q + 3] = v.w;
+    }
+#pragma unroll
+    for (int k = 0; k < 21; ++k) P[k] = u[k];
+}
+
+__device__ __forceinline__ void sym_mv6(const float P[21], const float x[6], float y[6]) {
+    // upper-triangle row-major index of (r, c), r <= c
+#define DPF_SYM(r, c) P[(r) * 6 - ((r) * ((r)-1)) / 2 + (c) - (r)]
+#pragma unroll
+    for (int r = 0; r < 6; ++r) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v = fmaf(r <= c ? DPF_SYM(r, c) : DPF_SYM(c, r), x[c], v);
+        y[r] = v;
+    }
+#undef DPF_SYM
+}
+
+// ---- tiled elastic PCG (single-reduction form: two grid barriers per iteration) ----
+//
+// Same equations and stopping rule as the reference loop: after iteration k's
+// update, following = (r, z) is tested when k % 5 == 0 against tol^2 (r0, z0).
+// The single-reduction recurrence keeps s = A p and forms (p, A p) from
+// (u, A u) = (z, A z):  p = z + beta p, s = w + beta s,
+// alpha = gamma / (delta - beta gamma / alpha_prev).
+
+struct PcgArgs {
+    int64_t n;
+    TileGraph G;
+    Layout L;
+    const float2 *mass2;
+    const uint8_t *fixed;
+    const float4 *P24;
+    const float *block, *units32;
+    const double *vector;
+    double tol2;
+    int max_it;
+    double *out;
+    int *iterations;
+    float *x, *r, *u, *p, *s, *w;  // (N, 6) each
+    double *part_a, *part_b;
+    unsigned *barrier;
+    int *status;
+};
+
+struct PcgEpi {
+    const PcgArgs &a;
+    float dot;
+    __device__ __forceinline__ void operator()(int64_t s, const float *qs, const float acc[6]) {
+        float wv[6];
+        operator_row(a.mass2, a.fixed, s, qs, acc, wv);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) dot = fmaf(wv[c], qs[c], dot);
+        st6(a.w + 6 * s, wv);
+    }
+};
+
+__device__ __forceinline__ void mv36(const float *B, const float x[6], float y[6]) {
+#pragma unroll
+    for (int row = 0; row < 6; ++row) {
+        float v = 0.0f;
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v = fmaf(B[6 * row + c], x[c], v);
+        y[row] = v;
+    }
+}
+
+__global__ void __launch_bounds__(kTileThreadsMax, DPF_TILE_MIN_BLOCKS) tiled_pcg_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const float zero6[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    Pipe P = pipe_init(smem, a.L);
+    // r0 = B (units v) with fixed rows zero, u0 = P r0, x = p = s = 0
+    float pf = 0.0f;
+    for (int64_t s = tid; s < a.n; s += stride) {
+        float v[6], rr[6], zz[6], Pm[21];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) v[c] = a.units32[6 * s + c] * (float)a.vector[6 * s + c];
+        if (a.fixed[s]) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) rr[c] = 0.0f;
+        } else {
+            mv36(a.block + 36 * s, v, rr);
+        }
+        sym6(a.P24 + 6 * s, Pm);
+        sym_mv6(Pm, rr, zz);
+        st6(a.r + 6 * s, rr);
+        st6(a.u + 6 * s, zz);
+        st6(a.x + 6 * s, zero6);
+        st6(a.p + 6 * s, zero6);
+        st6(a.s + 6 * s, zero6);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) pf = fmaf(rr[c], zz[c], pf);
+    }
+    double part = block_sum((double)pf);
+    if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
+    if (!grid_barrier(a.barrier, a.status)) return;
+    double gamma = block_sum_array(a.part_b, gridDim.x);
+    const double initial = gamma;
+    if (initial == 0.0) {
+        for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = 0.0;
+        return;
+    }
+    double alpha_prev = 1.0, gamma_prev = 1.0;
+    int it = 0;
+    for (; it < a.max_it; ++it) {
+        // w = A u over the tiles of this block, delta partial (w, u)
+        PcgEpi epi{a, 0.0f};
+        const bool ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
+        part = block_sum((double)epi.dot);
+        if (threadIdx.x == 0) a.part_a[blockIdx.x] = part;
+        if (!ok) return;
+        if (!grid_barrier(a.barrier, a.status)) return;
+        const double delta = block_sum_array(a.part_a, gridDim.x);
+        double beta, alpha;
+        if (it == 0) {
+            beta = 0.0;
+            alpha = gamma / delta;
+        } else {
+            beta = gamma / gamma_prev;
+            alpha = gamma / (delta - beta * gamma / alpha_prev);
+        }
+        const float fa = (float)alpha, fb = (float)beta;
+        pf = 0.0f;
+        for (int64_t s = tid; s < a.n; s += stride) {
+            float pv[6], tv[6], rv[6];
+            // p = u + beta p ; x += alpha p
+            ld6(a.u + 6 * s, tv);
+            ld6(a.p + 6 * s, pv);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) pv[c] = fmaf(fb, pv[c], tv[c]);
+            st6(a.p + 6 * s, pv);
+            ld6(a.x + 6 * s, tv);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) tv[c] = fmaf(fa, pv[c], tv[c]);
+            st6(a.x + 6 * s, tv);
+            // s = w + beta s ; r -= alpha s
+            ld6(a.w + 6 * s, tv);
+            ld6(a.s + 6 * s, pv);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) pv[c] = fmaf(fb, pv[c], tv[c]);
+            st6(a.s + 6 * s, pv);
+            ld6(a.r + 6 * s, rv);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) rv[c] = fmaf(-fa, pv[c], rv[c]);
+            st6(a.r + 6 * s, rv);
+            // u = P r
+            float Pm[21];
+            sym6(a.P24 + 6 * s, Pm);
+            sym_mv6(Pm, rv, tv);
+            st6(a.u + 6 * s, tv);
+#pragma unroll
+            for (int c = 0; c < 6; ++c) pf = fmaf(rv[c], tv[c], pf);
+        }
+        part = block_sum((double)pf);
+        if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
+        if (!grid_barrier(a.barrier, a.status)) return;
+        const double following = block_sum_array(a.part_b, gridDim.x);
+        if (it % 5 == 0 && following <= a.tol2 * initial) break;
+        gamma_prev = gamma;
+        gamma = following;
+        alpha_prev = alpha;
+    }
+    for (int64_t s = tid; s < a.n; s += stride) {
+        float xv[6];
+        ld6(a.x + 6 * s, xv);
+#pragma unroll
+        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)(xv[c] / a.units32[6 * s + c]);
+    }
+    if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
+}
+
+inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
+
+}  // namespace tiles
+}  // namespace dpf
+
+using namespace dpf;
+using namespace dpf::tiles;
+
+namespace {
+
+constexpr int kMaxPcgBlocksTiled = 4096;
+// dynamic shared memory cap per CTA (the static reduction buffers need the rest)
+constexpr size_t kMaxTileSmem = 220 * 1024;
+
+bool tiles_ok(const dpf_tiles *t) {
+    return t && t->n_tiles > 0 && t->tile_site && t->tile_entry && t->tile_halo && t->tile_meta_off &&
+           t->tile_meta && t->max_entries >= 0 && t->max_sites > 0 && t->max_meta_words > 0 &&
+           (t->n_halo == 0 || t->halo_site) && (t->n_entries == 0 || (t->entry_ends && t->entry_bond));
+}
+
+TileGraph tile_graph(const dpf_tiles *t, const float *entries) {
+    const float4 *p = reinterpret_cast<const float4 *>(entries);
+    return TileGraph{(int32_t)t->n_tiles, t->tile_site, t->tile_entry, t->tile_halo, t->tile_meta_off, t->halo_site,
+                     t->tile_meta, p, p + t->n_entries, p + 2 * t->n_entries};
+}
+
+size_t round16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+Layout layout_of(const dpf_tiles *t, int stages) {
+    Layout L;
+    L.plane = 16u * (uint32_t)t->max_entries;
+    L.qown = 3 * L.plane;
+    L.qhalo = L.qown + (uint32_t)round16(24 * (size_t)t->max_sites + 16);
+    L.meta = L.qhalo + (uint32_t)round16(24 * (size_t)(t->max_halo > 0 ? t->max_halo : 1));
+    L.size = L.meta + 4u * (uint32_t)t->max_meta_words;
+    L.stages = stages;
+    return L;
+}
+
+size_t smem_bytes(const Layout &L) { return (size_t)L.stages * L.size + 8 * (size_t)L.stages; }
+
+// A ring of `stages` buffers (2..4); 0 picks the deepest within the cap.
+Layout pick_layout(const dpf_tiles *t, int stages) {
+    if (stages >= 2) return layout_of(t, stages);
+    for (stages = 4; stages > 2; --stages) {
+        const Layout L = layout_of(t, stages);
+        if (smem_bytes(L) <= kMaxTileSmem) return L;
+    }
+    return layout_of(t, 2);
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+// Launch checks shared by the tiled kernels; returns the dynamic shared memory.
+int tile_launch_check(const dpf_tiles *t, int threads, int stages, size_t &smem) {
+    if (threads < 64 || threads > kTileThreadsMax || threads % 32 || stages < 0 || stages == 1 || stages > 4)
+        return DPF_ERR_ARGUMENT;
+    if (t->max_entries > kPer * threads) return DPF_ERR_TOO_LARGE;
+    smem = smem_bytes(pick_layout(t, stages));
+    if (smem > kMaxTileSmem) return DPF_ERR_TOO_LARGE;
+    return DPF_OK;
+}
+
+template <class K>
+int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t cap, int &grid) {
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+        return DPF_ERR_CUDA;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    if (sms <= 0 || per_sm <= 0) return DPF_ERR_CUDA;
+    int64_t g = (int64_t)sms * per_sm;
+    if (g > n_tiles) g = n_tiles;
+    if (g > cap) g = cap;
+    grid = (int)g;
+    return DPF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dpf_tile_graph(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const int32_t *inc_ptr,
+                   const int32_t *inc_bond, int32_t max_entries, int32_t max_stage, int32_t *tile_site,
+                   int32_t *tile_entry, int32_t *tile_halo, int32_t *tile_meta_off, int32_t *halo_site,
+                   int32_t *entry_bond, uint32_t *entry_ends, uint32_t *tile_meta, int64_t meta_capacity,
+                   int64_t *counts) {
+    if (n_sites <= 0 || n_sites > INT32_MAX || n_bonds < 0 || n_bonds > INT32_MAX / 2 || !inc_ptr || !counts ||
+        (n_bonds && (!edges || !inc_bond || !entry_bond || !entry_ends || !halo_site)) || !tile_site ||
+        !tile_entry || !tile_halo || !tile_meta_off || !tile_meta || max_entries < 1 || max_entries > 32767 ||
+        max_stage < 1 || max_stage > 65535 || meta_capacity < 4)
+        return DPF_ERR_ARGUMENT;
+    if (inc_ptr[0] != 0 || inc_ptr[n_sites] != 2 * n_bonds) return DPF_ERR_ARGUMENT;
+    for (int64_t b = 0; b < n_bonds; ++b) {
+        const int64_t i = edges[2 * b], j = edges[2 * b + 1];
+        if (i < 0 || j < 0 || i >= n_sites || j >= n_sites || i == j) return DPF_ERR_ARGUMENT;
+    }
+    std::vector<int32_t> bond_mark((size_t)n_bonds, -1), site_mark((size_t)n_sites, -1);
+    // the far end of incidence v (v >= 0: the site is the bond's i end)
+    auto other = [&](int32_t v) -> int64_t {
+        const int64_t b = v >= 0 ? v : ~v;
+        return v >= 0 ? edges[2 * b + 1] : edges[2 * b];
+    };
+    // pass 1: tile boundaries (greedy in site order: grow while the entries and
+    // the staged own + halo sites fit)
+    int32_t t = 0;
+    int64_t s0 = 0, ent = 0, stage = 0;
+    tile_site[0] = 0;
+    for (int64_t s = 0; s < n_sites; ++s) {
+        int64_t ne = 0, nst = site_mark[s] != t ? 1 : 0;
+        for (int32_t k = inc_ptr[s]; k < inc_ptr[s + 1]; ++k) {
+            const int32_t v = inc_bond[k];
+            const int64_t b = v >= 0 ? v : ~v;
+            if (bond_mark[b] != t) ++ne;
+            if (site_mark[other(v)] != t) ++nst;
+        }
+        if (s > s0 && (ent + ne > max_entries || stage + nst > max_stage)) {
+            ++t;
+            tile_site[t] = (int32_t)s;
+            s0 = s;
+            ent = stage = 0;
+            ne = inc_ptr[s + 1] - inc_ptr[s];
+            nst = 1 + ne;
+        }
+        if (ne > max_entries || nst > max_stage) return DPF_ERR_TOO_LARGE;
+        for (int32_t k = inc_ptr[s]; k < inc_ptr[s + 1]; ++k) {
+            const int32_t v = inc_bond[k];
+            bond_mark[v >= 0 ? v : ~v] = t;
+            site_mark[other(v)] = t;
+        }
+        site_mark[s] = t;
+        ent += ne;
+        stage += nst;
+    }
+    const int32_t n_tiles = t + 1;
+    tile_site[n_tiles] = (int32_t)n_sites;
+    // pass 2: entries (first-encounter order), halo slots, local ends, metadata
+    std::fill(bond_mark.begin(), bond_mark.end(), -1);
+    std::fill(site_mark.begin(), site_mark.end(), -1);
+    std::vector<int32_t> bond_local((size_t)n_bonds, 0), site_local((size_t)n_sites, 0);
+    int64_t e = 0, h = 0, words = 0, max_e = 0, max_st = 0, max_t = 0, max_h = 0, max_w = 0;
+    for (int32_t tt = 0; tt < n_tiles; ++tt) {
+        const int64_t a = tile_site[tt], bnd = tile_site[tt + 1], T = bnd - a;
+        tile_entry[tt] = (int32_t)e;
+        tile_halo[tt] = (int32_t)h;
+        for (int64_t s = a; s < bnd; ++s)
+            for (int32_t k = inc_ptr[s]; k < inc_ptr[s + 1]; ++k) {
+                const int32_t v = inc_bond[k];
+                const int64_t b = v >= 0 ? v : ~v;
+                if (bond_mark[b] != tt) {
+                    bond_mark[b] = tt;
+                    bond_local[b] = (int32_t)(e - tile_entry[tt]);
+                    entry_bond[e++] = (int32_t)b;
+                }
+                const int64_t o = other(v);
+                if ((o < a || o >= bnd) && site_mark[o] != tt) {
+                    site_mark[o] = tt;
+                    site_local[o] = (int32_t)(T + (h - tile_halo[tt]));
+                    halo_site[h++] = (int32_t)o;
+                }
+            }
+        const int64_t n_e = e - tile_entry[tt], n_h = h - tile_halo[tt];
+        if (n_e > max_entries || T + n_h > max_stage) return DPF_ERR_TOO_LARGE;
+        max_e = std::max(max_e, n_e);
+        max_st = std::max(max_st, T + n_h);
+        max_t = std::max(max_t, T);
+        max_h = std::max(max_h, n_h);
+        for (int64_t k = tile_entry[tt]; k < e; ++k) {
+            const int64_t b = entry_bond[k];
+            const int64_t i = edges[2 * b], j = edges[2 * b + 1];
+            const uint32_t li = (uint32_t)(i >= a && i < bnd ? i - a : site_local[i]);
+            const uint32_t lj = (uint32_t)(j >= a && j < bnd ? j - a : site_local[j]);
+            entry_ends[k] = li | (lj << 16);
+        }
+        // metadata: T + 1 incidence offsets, the uint16 codes (padded to 16
+        // bytes), then the halo sites (int32, padded to 16 bytes)
+        const int64_t k0 = inc_ptr[a], n_inc = inc_ptr[bnd] - k0;
+        const int64_t w_codes = ((T + 1 + (n_inc + 1) / 2) + 3) & ~(int64_t)3;
+        const int64_t w = w_codes + ((n_h + 3) & ~(int64_t)3);
+        if (words + w > meta_capacity) return DPF_ERR_TOO_LARGE;
+        tile_meta_off[tt] = (int32_t)words;
+        uint32_t *m = tile_meta + words;
+        for (int64_t k = 0; k < w; ++k) m[k] = 0u;
+        if (n_inc > 65535) return DPF_ERR_TOO_LARGE;
+        for (int64_t k = 0; k <= T; ++k) {
+            const int64_t s = a + k, start = inc_ptr[s] - k0;
+            int64_t mid = start;
+            if (k < T) {
+                while (mid < inc_ptr[s + 1] - k0 && inc_bond[k0 + mid] >= 0) ++mid;
+                for (int64_t r = mid; r < inc_ptr[s + 1] - k0; ++r)
+                    if (inc_bond[k0 + r] >= 0) return DPF_ERR_ARGUMENT;  // i ends must precede j ends
+            }
+            m[k] = (uint32_t)start | ((uint32_t)mid << 16);
+        }
+        for (int64_t k = 0; k < n_inc; ++k) {
+            const int32_t v = inc_bond[k0 + k];
+            const uint32_t code = (uint32_t)bond_local[v >= 0 ? v : ~v];
+            const int64_t word = T + 1 + k / 2;
+            m[word] |= (k & 1) ? (code << 16) : code;  // little-endian uint16 pairs
+        }
+        for (int64_t k = 0; k < n_h; ++k) m[w_codes + k] = (uint32_t)halo_site[tile_halo[tt] + k];
+        words += w;
+        max_w = std::max(max_w, w);
+    }
+    tile_entry[n_tiles] = (int32_t)e;
+    tile_halo[n_tiles] = (int32_t)h;
+    tile_meta_off[n_tiles] = (int32_t)words;
+    counts[0] = n_tiles;
+    counts[1] = e;
+    counts[2] = h;
+    counts[3] = words;
+    counts[4] = max_e;
+    counts[5] = max_t;
+    counts[6] = max_h;
+    counts[7] = max_w;
+    counts[8] = max_st;
+    return DPF_OK;
+}
+
+int64_t dpf_tile_entry_floats(int64_t n_entries) { return 12 * n_entries; }
+
+int64_t dpf_tile_meta_capacity(int64_t n_sites, int64_t n_bonds) { return 9 * n_sites + 3 * n_bonds + 16; }
+
+int dpf_tile_pack(const dpf_tiles *t, const float *bond_data, int64_t n_bonds, double alpha, const float *P36,
+                  const float *mass32, int64_t n_sites, float *entries, float *P24, float *mass2, void *stream) {
+    if (!tiles_ok(t) || !bond_data || !entries || !aligned16(bond_data) || !aligned16(entries) ||
+        (P24 && (!P36 || !aligned16(P24) || n_sites <= 0)) || (mass2 && !mass32))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    // tangent planes of the mixed bond data: records (7 M float4) then t0..t3
+    const float4 *base = reinterpret_cast<const float4 *>(bond_data);
+    if (t->n_entries) {
+        float4 *e = reinterpret_cast<float4 *>(entries);
+        PackArgs a{t->n_entries, t->entry_bond, t->entry_ends, base + 7 * n_bonds, base + 8 * n_bonds,
+                   base + 9 * n_bonds, base + 10 * n_bonds, (float)alpha, e, e + t->n_entries,
+                   e + 2 * t->n_entries};
+        pack_entries_kernel<<<blocks_for(t->n_entries, kThreads), kThreads, 0, st>>>(a);
+    }
+    if (P24)
+        pack_sites_kernel<<<blocks_for(n_sites, kThreads), kThreads, 0, st>>>(
+            n_sites, P36, mass32, reinterpret_cast<float4 *>(P24), reinterpret_cast<float2 *>(mass2));
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *mass2,
+                  const uint8_t *fixed, const float *q, float *y, int *status, int threads, int stages,
+                  void *stream) {
+    if (!g || !tiles_ok(t) || !entries || !mass2 || !fixed || !q || !y || !status || !aligned16(entries) ||
+        !aligned16(q) || !aligned16(y))
+        return DPF_ERR_ARGUMENT;
+    size_t smem = 0;
+    int rc = tile_launch_check(t, threads, stages, smem);
+    if (rc) return rc;
+    int grid = 0;
+    rc = persistent_grid(tiled_hvp_kernel, threads, smem, t->n_tiles, INT32_MAX, grid);
+    if (rc) return rc;
+    HvpArgs a{tile_graph(t, entries), pick_layout(t, stages), reinterpret_cast<const float2 *>(mass2), fixed, q, y,
+              status};
+    tiled_hvp_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(a);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int64_t dpf_tiled_workspace_floats(int64_t n_sites) { return 36 * n_sites; }
+
+int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *mass2,
+                           const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
+                           const double *vector, double tolerance, int max_iterations, double *out, int *iterations,
+                           float *workspace, double *partials, unsigned *barrier, int *status, int threads,
+                           int stages, void *stream) {
+    if (!g || !tiles_ok(t) || g->n_sites <= 0 || !entries || !mass2 || !fixed || !block32 || !P24 || !units32 ||
+        !vector || !out || !iterations || !workspace || !partials || !barrier || !status || max_iterations < 1 ||
+        !aligned16(entries) || !aligned16(workspace) || !aligned16(P24))
+        return DPF_ERR_ARGUMENT;
+    size_t smem = 0;
+    int rc = tile_launch_check(t, threads, stages, smem);
+    if (rc) return rc;
+    int grid = 0;
+    rc = persistent_grid(tiled_pcg_kernel, threads, smem, t->n_tiles, kMaxPcgBlocksTiled, grid);
+    if (rc) return rc;
+    const int64_t n6 = 6 * g->n_sites;
+    PcgArgs a{};
+    a.n = g->n_sites;
+    a.G = tile_graph(t, entries);
+    a.L = pick_layout(t, stages);
+    a.mass2 = reinterpret_cast<const float2 *>(mass2);
+    a.fixed = fixed;
+    a.P24 = reinterpret_cast<const float4 *>(P24);
+    a.block = block32;
+    a.units32 = units32;
+    a.vector = vector;
+    a.tol2 = tolerance * tolerance;
+    a.max_it = max_iterations;
+    a.out = out;
+    a.iterations = iterations;
+    a.x = workspace;
+    a.r = workspace + n6;
+    a.u = workspace + 2 * n6;
+    a.p = workspace + 3 * n6;
+    a.s = workspace + 4 * n6;
+    a.w = workspace + 5 * n6;
+    a.part_a = partials;
+    a.part_b = partials + kMaxPcgBlocksTiled;
+    a.barrier = barrier;
+    a.status = status;
+    void *args[] = {&a};
+    if (cudaLaunchCooperativeKernel((const void *)tiled_pcg_kernel, grid, threads, args, smem,
+                                    (cudaStream_t)stream) != cudaSuccess)
+        return DPF_ERR_CUDA;
+    return DPF_OK;
+}
+
+int64_t dpf_tiled_partials_doubles(void) { return 2 * kMaxPcgBlocksTiled; }
+
+}  // extern "C"

@@ -943,6 +943,9 @@ class MixedNewtonBonds(NewtonBonds):
     # Steps between float64 rebuilds of the bond records and committed loads
     # (in between they are advanced by the commit's float32 increments).
     refresh_interval = 32
+    # Elastic PCG on site tiles (shared-memory HVP, two grid barriers per
+    # iteration); the tile size and CTA width are autotuned at the first use.
+    tiled = True
 
     def step(self, dt, external, tolerance=2e-7, max_iterations=12, *, pose_tolerance=2e-6, backend='fgmres',
              linear_tolerance=1e-6, preconditioning='elastic'):
@@ -971,6 +974,49 @@ class MixedNewtonBonds(NewtonBonds):
         self._loads = torch.empty((n, 6), dtype=F64, device=dev)
         self._token = None
         self._since_refresh = 0
+        self._init_tiles()
+
+    def _init_tiles(self):
+        n, dev = self.n_sites, self.device
+        self._tiles = None
+        self.tile_timings = {}
+        if not self.tiled:
+            return
+        lib = self._lib
+        self._mass2 = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        self._p24 = torch.empty(24*n, dtype=torch.float32, device=dev)
+        self._tiled_workspace = torch.empty(lib.dpf_tiled_workspace_floats(n), dtype=torch.float32, device=dev)
+        self._tiled_partials = torch.zeros(lib.dpf_tiled_partials_doubles(), dtype=F64, device=dev)
+        self._tune_iterations = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._packed = None
+
+    def _pack_tiles(self, tiles, dt):
+        """Entry records (alpha = dt^2/4 folded in), packed P and (m, I) for ``tiles``."""
+        self._call('dpf_tile_pack', ctypes.byref(tiles.struct), self._bond_data.data_ptr(), self.n_bonds,
+                   .25*dt*dt, self._p32.data_ptr(), self._mass32.data_ptr(), self.n_sites, tiles.entries.data_ptr(),
+                   self._p24.data_ptr(), self._mass2.data_ptr(), self._stream())
+        self._packed = (tiles, dt)
+
+    def _tiled_pcg(self, tiles, vector, out, tolerance, max_iterations, iterations):
+        self._call('dpf_tiled_precondition', ctypes.byref(self._graph), ctypes.byref(tiles.struct),
+                   tiles.entries.data_ptr(), self._mass2.data_ptr(), self.fixed.data_ptr(),
+                   self._block32.data_ptr(), self._p24.data_ptr(), self._units32.data_ptr(), vector.data_ptr(),
+                   float(tolerance), int(max_iterations), out.data_ptr(), iterations.data_ptr(),
+                   self._tiled_workspace.data_ptr(), self._tiled_partials.data_ptr(), self._barrier.data_ptr(),
+                   self._status.data_ptr(), tiles.threads, tiles.stages, self._stream())
+
+    def _ensure_tiles(self, dt, vector, tolerance, max_iterations):
+        if self._tiles is None:
+            from .tiles import autotune
+            scratch = torch.empty_like(vector)
+
+            def run(tiles):
+                self._pack_tiles(tiles, dt)
+                self._tiled_pcg(tiles, vector, scratch, tolerance, max_iterations, self._tune_iterations)
+            self._tiles, self.tile_timings = autotune(self, run)
+            self._packed = None
+        if self._packed != (self._tiles, dt):
+            self._pack_tiles(self._tiles, dt)
 
     def _state_token(self):
         # identity and in-place version of every committed tensor the records depend on
@@ -1031,6 +1077,8 @@ class MixedNewtonBonds(NewtonBonds):
         if status:
             raise guard_error(status)
         self.units = self._units
+        if self.tiled:
+            self._packed = None  # new tangent: repack before the next tiled PCG
         return scaled, norms
 
     def _newton_operator(self, y, dt, external):
@@ -1049,6 +1097,11 @@ class MixedNewtonBonds(NewtonBonds):
         def precondition(vector, tolerance=.03, max_iterations=80):
             vector = self._vec(vector)
             out = torch.empty_like(vector)
+            if self.tiled:
+                self._ensure_tiles(dt, vector, tolerance, max_iterations)
+                self._timed('pcg', lambda: self._tiled_pcg(self._tiles, vector, out, tolerance, max_iterations,
+                                                           self._inner))
+                return out
             self._timed('pcg', lambda: self._call(
                 'dpf_mixed_precondition', ctypes.byref(self._graph), self._bond_data.data_ptr(),
                 self._mass32.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p32.data_ptr(),

@@ -245,6 +245,8 @@ class Pool:
 class Batch(MixedNewtonBonds):
     """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
 
+    tiled = False
+
     def __init__(self, parts, pool=None):
         if not parts:
             raise ValueError('empty batch')
