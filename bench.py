@@ -54,6 +54,9 @@ def parse():
     p.add_argument('--plain-steps', type=int, default=3,
                    help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
     p.add_argument('--hvp-launches', type=int, default=50, help='timed launches of the standalone tiled HVP (0: skip)')
+    p.add_argument('--adjoint-lattice', type=int, default=32, help='lattice size of the inverse-fit workload (0: skip)')
+    p.add_argument('--adjoint-steps', type=int, default=50)
+    p.add_argument('--adjoint-fd', type=int, default=4, help='bonds checked against central differences')
     p.add_argument('--served', type=int, default=512, help='requests of the served mixed-size stream (0: skip)')
     p.add_argument('--served-plain', type=int, default=64,
                    help='requests of the same stream solved one at a time by the plain float64 solver')
@@ -189,6 +192,51 @@ def run_hvp(s, dt, peak, peaks, launches=50):
                 tile=dict(max_entries=int(tiles.host['max_entries']), threads=tiles.threads, stages=tiles.stages,
                           tiles=int(tiles.host['n_tiles']), entries_per_bond=tiles.n_entries/max(1, m)),
                 autotune_ms={'x'.join(map(str, k)): v for k, v in (s.tile_timings or {}).items()})
+
+
+def run_adjoint(args, device):
+    """Gradient of the inverse-fit loss by the adjoint (implicit-function
+    theorem, checkpoints every 10 steps), timed; checked against central
+    differences (h = 1e-4) of the loss in ``args.adjoint_fd`` random bonds."""
+    import torch
+    steps, dt = args.adjoint_steps, 2e-3
+    from dpf_gb300.adjoint import inverse_fit_problem
+    model, theta0, loss = inverse_fit_problem(args.adjoint_lattice, 4, device, steps, dt, 10, 1e-12)
+    theta = theta0.clone().requires_grad_(True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    value = loss(theta)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    grad, = torch.autograd.grad(value, [theta])
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    value = value.detach()
+    out = dict(workload=f'{args.adjoint_lattice}^3 jittered foam, {model.solver.n_bonds} bonds, {steps} implicit '
+                        f'steps dt={dt}, gravity + 3% top indentation load, hidden per-bond log-stiffness GRF '
+                        '(l=0.2, mean log 1e5, std 0.5), MSE of positions; adjoint with checkpoints every 10 steps',
+               loss=float(value), forward_s=t1 - t0, backward_s=t2 - t1, forward_ms_per_step=1e3*(t1 - t0)/steps,
+               backward_ms_per_step=1e3*(t2 - t1)/steps, gradient_norm=float(grad.norm()),
+               newton_tolerance=1e-12)
+    if args.adjoint_fd > 0:
+        rng = np.random.default_rng(5)
+        # bonds with the largest gradients are the ones the loss sees best; mix
+        # them with uniformly random bonds
+        bonds = np.unique(np.concatenate([rng.choice(len(theta0), args.adjoint_fd//2, replace=False),
+                                          torch.topk(grad.abs(), args.adjoint_fd - args.adjoint_fd//2)
+                                          .indices.cpu().numpy()]))
+        h, errs, rows = 1e-4, [], []
+        with torch.no_grad():
+            for b in bonds:
+                e = torch.zeros_like(theta0)
+                e[b] = h
+                fd = (float(loss(theta0 + e)) - float(loss(theta0 - e)))/(2*h)
+                g = float(grad[b])
+                errs.append(abs(fd - g)/max(abs(fd), 1e-300))
+                rows.append([int(b), g, fd])
+        out.update(fd_bonds=len(bonds), fd_h=h, fd_max_relative_error=float(max(errs)),
+                   fd_median_relative_error=float(np.median(errs)), fd_samples=rows[:8])
+    return out
 
 
 def run_served(args, device):
@@ -393,6 +441,7 @@ def run_ours(args):
     hvp = run_hvp(s, args.dt, peak, peaks, launches=args.hvp_launches) \
         if args.precision == 'mixed' and args.hvp_launches > 0 and getattr(s, '_tiles', None) is not None else None
     served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None
+    adjoint = run_adjoint(args, device) if args.adjoint_lattice > 0 and world == 1 else None
     if rank != 0:
         return
     cpu = None
@@ -417,7 +466,7 @@ def run_ours(args):
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
                 gpu_launches=launches, kernels=kernels, roofline=roof, hvp=hvp, cpu_baseline=cpu, plain_f64=plain,
-                served=served,
+                served=served, adjoint=adjoint,
                 relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)

@@ -310,3 +310,46 @@ class DifferentiableBonds:
                           workspace=krylov)
         self.stats.append(dict(adjoint_krylov=info['iterations'], adjoint_relative=info['relative_residual']))
         return to_lambda(mu)
+
+
+def inverse_fit_problem(m, seed, device, steps, dt, checkpoint_every, tolerance):
+    """The differentiable inverse material fit: an m^3 jittered foam with its
+    bottom layer fixed, under gravity and a 3% top indentation (equivalent load
+    E * 0.03 * top area spread over the top layer's sites), a hidden per-bond log-stiffness field (smooth Gaussian random
+    field by 512 random Fourier features of the bond midpoints: squared-
+    exponential covariance, length scale 0.2, mean log(1e5), std 0.5), and the
+    MSE of all site positions of a ``steps``-step trajectory against the
+    trajectory of the hidden field.  Returns (model, uniform initial guess
+    theta0 (M,), loss(theta)) with theta the per-bond log stiffness."""
+    from .foam import gravity_load, jittered_lattice_foam
+    # bottom lattice layer fixed, top layer loaded (jitter is +-0.2 spacing)
+    foam = jittered_lattice_foam(m, seed=seed, young=1.0, poisson=.3, fixed_below=1./m)
+    model = DifferentiableBonds(points=foam['points'], radii=foam['radii'], pairs=foam['pairs'],
+                                          areas=foam['areas'], masses=foam['masses'], fixed=foam['fixed'],
+                                          young=1.0, shear=1/2.6, device=device, checkpoint_every=checkpoint_every,
+                                          tolerance=tolerance, pose_tolerance=max(tolerance, 1e-12),
+                                          adjoint_tolerance=1e-11, max_iterations=24)
+    rng = np.random.default_rng(seed + 1)
+    pairs = np.asarray(foam['pairs'])
+    mid = .5*(foam['unit'][pairs[:, 0]] + foam['unit'][pairs[:, 1]])
+    k = 512
+    omega = rng.normal(0., 1/.2, (k, 3))
+    phase = rng.uniform(0., 2*np.pi, k)
+    field = np.sqrt(2./k)*np.cos(mid@omega.T + phase).sum(1)
+    hidden = np.log(1e5) + .5*field
+    load = gravity_load(foam)
+    top = (foam['unit'][:, 2] > 1. - 1./m) & ~np.asarray(foam['fixed'])
+    load[top, 2] -= 1e5*.03*1.0/max(1, top.sum())
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=device)
+    loads = t(np.repeat(load[None], steps, 0))
+    base = model.base_stiffness
+
+    def rollout(theta):
+        return model.rollout_bonds(base*torch.exp(theta)[:, None], loads, model.initial_state(), dt)[0]
+    with torch.no_grad():
+        target = rollout(t(hidden))
+    theta0 = t(np.full(len(pairs), np.log(1e5)))
+
+    def loss(theta):
+        return ((rollout(theta) - target)**2).mean()
+    return model, theta0, loss

@@ -116,13 +116,15 @@ class RequestState:
                           contacts=contacts, young=young, shear=shear)], device)
 
     @classmethod
-    def group(cls, foams, device='cuda'):
-        """Several requests' foams as one resident state (sites and bonds in order)."""
+    def group(cls, foams, device='cuda', loads=None):
+        """Several requests' foams as one resident state (sites and bonds in
+        order); with ``loads`` (one (n, 6) array per foam) also their external
+        loads, uploaded with the rest as ``external``."""
         self = cls.__new__(cls)
-        self._build(foams, device)
+        self._build(foams, device, loads)
         return self
 
-    def _build(self, foams, device):
+    def _build(self, foams, device, loads=None):
         self.device = torch.device(device)
         if self.device.index is None:
             self.device = torch.device('cuda', torch.cuda.current_device())
@@ -139,10 +141,12 @@ class RequestState:
         # one copy of each input into pinned staging: per-site float64 [points, radii,
         # masses], per-bond float64 areas, int32 endpoints (global ids), uint8 flags
         staging = _staging()
-        f64 = staging.host('f8', 5*n + m)
+        n_load = 6*n if loads is not None else 0
+        f64 = staging.host('f8', 5*n + m + n_load)
         i32 = staging.host('i4', 2*m)
         u8 = staging.host('u1', n)
         pts, rad, mas, are = f64[:3*n].reshape(n, 3), f64[3*n:4*n], f64[4*n:5*n], f64[5*n:5*n + m]
+        ext = f64[5*n + m:5*n + m + n_load].reshape(-1, 6)
         pairs = i32.reshape(m, 2)
 
         def copy(k):
@@ -157,11 +161,14 @@ class RequestState:
                 raise ValueError('Invalid endpoint index')
             np.add(fp, a, out=pairs[c:d], casting='unsafe')
             u8[a:b] = np.asarray(f['fixed'], dtype=bool)
+            if n_load:
+                ext[a:b] = loads[k]
         # numpy releases the GIL for these copies: spread the requests over threads
         list(_COPIERS.map(copy, range(len(foams))))
         if np.any(mas <= 0):
             raise ValueError('Only positive-mass bodies can enter this solver')
-        dev64 = staging.send('f8', 5*n + m, self.device)
+        dev64 = staging.send('f8', 5*n + m + n_load, self.device)
+        self.external = dev64[5*n + m:].view(n, 6) if n_load else None
         dev32 = staging.send('i4', 2*m, self.device)
         self.fixed = staging.send('u1', n, self.device).view(torch.bool)
         self.p = dev64[:3*n].view(n, 3)
@@ -271,11 +278,19 @@ class Batch(MixedNewtonBonds):
         self.site_ptr = torch.as_tensor(rs, dtype=torch.int64, device=self.device)
         self.site_range = [(int(rs[k]), int(rs[k+1])) for k in range(self.n_requests)]
         self.bond_range = [(int(rb[k]), int(rb[k+1])) for k in range(self.n_requests)]
-        for name in _PER_SITE + _PER_BOND:
-            setattr(self, name, torch.cat([getattr(p, name).contiguous() for p in parts]))
-        self.edges = torch.cat([p.edges + int(site_off[k]) for k, p in enumerate(parts)]).contiguous()
+        if len(parts) == 1 and isinstance(first, RequestState):
+            # a freshly set-up group alone: use its tensors and incidence as they
+            # are (the step replaces state tensors, it never writes into them)
+            for name in _PER_SITE + _PER_BOND:
+                setattr(self, name, getattr(first, name))
+            self.edges = first.edges
+            self._inc_ptr, self._inc_bond = first._inc_ptr, first._inc_bond
+        else:
+            for name in _PER_SITE + _PER_BOND:
+                setattr(self, name, torch.cat([getattr(p, name).contiguous() for p in parts]))
+            self.edges = torch.cat([p.edges + int(site_off[k]) for k, p in enumerate(parts)]).contiguous()
+            self._inc_ptr, self._inc_bond = device_incidence(self.edges, n)
         self.i, self.j = self.edges.T
-        self._inc_ptr, self._inc_bond = device_incidence(self.edges, n)
         R = self.n_requests
         self.seg_site = torch.repeat_interleave(torch.arange(R, dtype=torch.int32, device=self.device),
                                                 torch.as_tensor(seg_sites, device=self.device)).contiguous()
@@ -562,6 +577,7 @@ class Request:
     finished: float = field(compare=False, default=None)
     infos: list = field(compare=False, default_factory=list, repr=False)
     error: Exception = field(compare=False, default=None)
+    device_load: object = field(compare=False, default=None, repr=False)
 
     @property
     def sites(self):
@@ -621,11 +637,14 @@ class Service:
         side = torch.cuda.Stream(device=self.device)
         prefetch = None      # (requests, future of their group state) being set up on the side stream
 
-        def build(foams):
+        def build(reqs):
             with torch.cuda.stream(side):
-                group = RequestState.group(foams, device=self.device)
+                group = RequestState.group([r.foam for r in reqs], device=self.device,
+                                           loads=[r.load for r in reqs])
                 event = torch.cuda.Event()
                 event.record(side)
+            for (a, b), r in zip(zip(np.cumsum([0] + group.sites[:-1]), np.cumsum(group.sites)), reqs):
+                r.device_load = group.external[int(a):int(b)]
             return group, event
 
         while pending or waiting or active:
@@ -663,14 +682,15 @@ class Service:
                         torch.cuda.current_stream(self.device).wait_event(event)
                         prefetch = None
                     else:
-                        group, event = build([r.foam for r in admitted])
+                        group, event = build(admitted)
                         torch.cuda.current_stream(self.device).wait_event(event)
                     parts.append(group)
                 t2 = clock()
                 active += admitted
                 members = list(active)
                 batch = Batch(parts, pool=self.pool)
-                ext = _staging().upload(np.concatenate([r.load for r in members]), self.device)
+                ext = parts[0].external if len(parts) == 1 and isinstance(parts[0], RequestState) else \
+                    torch.cat([r.device_load for r in members])
                 t3 = clock()
                 self.timers['setup'] += t2 - t1
                 self.timers['batch'] += t3 - t2
@@ -690,7 +710,7 @@ class Service:
                     nxt.append(req)
                     cap += req.sites
                 if nxt:
-                    prefetch = (nxt, _PREFETCH.submit(build, [r.foam for r in nxt]))
+                    prefetch = (nxt, _PREFETCH.submit(build, nxt))
             t4 = clock()
             results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
             self.timers['solve'] += clock() - t4
