@@ -9,6 +9,7 @@ from .foam import jittered_lattice_foam, gravity_load, regular_edges, morton_ord
 from .newton import (LinearBonds, FiniteBonds, NewtonBonds, FastNewtonBonds, MixedNewtonBonds, AdaptiveIntervals,
                      SubdivideError, fgmres, incidence, guard_error)
 from .adjoint import DifferentiableBonds
+from .energy import EnergyFoam
 
 # Reference class names (experiments/bonded_dem_linear_gpu.py, bonded_dem_finite_gpu.py).
 LinearBondsGPU = LinearBonds
@@ -16,4 +17,5 @@ FiniteBondsGPU = FiniteBonds
 
 __all__ = ['jittered_lattice_foam', 'gravity_load', 'regular_edges', 'morton_order', 'LinearBonds',
            'FiniteBonds', 'NewtonBonds', 'FastNewtonBonds', 'MixedNewtonBonds', 'LinearBondsGPU', 'FiniteBondsGPU',
-           'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error', 'DifferentiableBonds']
+           'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error', 'DifferentiableBonds',
+           'EnergyFoam']

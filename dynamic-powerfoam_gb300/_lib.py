@@ -109,6 +109,8 @@ SIGNATURES = {
     'dpf_tiled_partials_doubles': (i64, []),
     'dpf_tiled_precondition': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp,
                                      i32, i32, vp]),
+    'dpf_energy_partials_doubles': (i64, []),
+    'dpf_bond_energy': (i32, [P(Graph), vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_adjoint_jacobian_doubles': (i64, [i64]),
     'dpf_adjoint_slot_doubles': (i64, [i64]),
     'dpf_adjoint_local_jacobian': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp]),
@@ -129,7 +131,7 @@ KERNELS = {
     'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 1,
     'dpf_segment_axpy': 1, 'dpf_segment_select': 1,
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
-    'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1,
+    'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_bond_energy': 3,
 }
 LAUNCHES = {'count': 0}
 

@@ -505,6 +505,22 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
                            float *workspace, double *partials, unsigned *barrier, int *status, int threads,
                            int stages, void *stream);
 
+/* ---- Energy law (bond part of EnergyFoam with volume=False, kinematics='small') ----
+ * Replaces EnergyFoam._bond_kinematics / energy / forces
+ * (experiments/foam_dem_energy.py:303-315, 405-421, 797-811).  base (M, 4):
+ * rest stiffnesses kn, ks, kb, kt; theta: per-site log multipliers (the first
+ * four of each row of theta_stride doubles); x (N, 3); q (N, 4) unit
+ * quaternions (w, x, y, z); n0, ri, rj (M, 3) rest normal and body-frame
+ * levers.  Outputs (any may be NULL, not all): force and torque (N, 3) =
+ * -dE/dx and -dE/d(world rotation), energy (1 double, device).  wrench: 9 M
+ * doubles when forces are requested; partials: dpf_energy_partials_doubles()
+ * doubles when the energy is.  Sums are in a fixed order (deterministic). */
+int64_t dpf_energy_partials_doubles(void);
+int dpf_bond_energy(const dpf_graph *g, const double *base, const double *theta, int64_t theta_stride,
+                    const double *x, const double *q, const double *n0, const double *ri, const double *rj,
+                    double *force, double *torque, double *energy, double *wrench, double *partials,
+                    void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -718,3 +718,67 @@ def reference_stiffness(points, pairs, contacts, kn, ks, kb, kt):
     for e in range(count):
         k[np.ix_(idx[e], idx[e])] += local[e]
     return k
+
+
+# ---------------------------------------------------------------------------
+# Energy law (experiments/foam_dem_energy.py, EnergyFoam with volume=False and
+# kinematics='small'): bond potential, closed-form force and world torque.
+
+def quat_matrix(q):
+    """Rotation matrix of unit quaternions (w, x, y, z) (foam_dem_energy.py:61-65)."""
+    w, x, y, z = np.moveaxis(np.asarray(q, dtype=np.float64), -1, 0)
+    return np.stack((1 - 2*(y*y + z*z), 2*(x*y - w*z), 2*(x*z + w*y),
+                     2*(x*y + w*z), 1 - 2*(x*x + z*z), 2*(y*z - w*x),
+                     2*(x*z - w*y), 2*(y*z + w*x), 1 - 2*(x*x + y*y)), -1).reshape(np.shape(q)[:-1] + (3, 3))
+
+
+class EnergyBonds:
+    """Bond part of ``EnergyFoam`` (foam_dem_energy.py:127-168 with volume=False):
+    rest normal n0 and levers ri, rj and base stiffness (kn, ks, kb, kt) of
+    ``LinearBonds`` (bonded_dem_linear_gpu.py:15-40)."""
+
+    def __init__(self, points, radii, pairs, areas, contacts, masses, fixed, young=1200., shear=480.):
+        b = LinearBonds(points, radii, pairs, areas, contacts, masses, fixed, young, shear)
+        self.X = b.p
+        self.i, self.j = b.i, b.j
+        self.n0, self.ri, self.rj = b.n, b.ri, b.rj
+        self.base = np.stack((b.kn, b.ks, b.kb, b.kt), 1)
+        self.mass, self.inertia = b.mass[:, 0], b.mass[:, 3]
+
+    def kinematics(self, theta, x, q):
+        """foam_dem_energy.py:303-315 (averaged-frame stretch, sin-angle rotation)."""
+        R = quat_matrix(q)
+        Ri, Rj = R[self.i], R[self.j]
+        pi = np.einsum('bij,bj->bi', Ri, self.ri)
+        pj = np.einsum('bij,bj->bi', Rj, self.rj)
+        D = x[self.j] + pj - x[self.i] - pi
+        d = .5*(np.einsum('bji,bj->bi', Ri, D) + np.einsum('bji,bj->bi', Rj, D))
+        Psi = np.einsum('bki,bkj->bij', Ri, Rj)
+        A = Psi - np.swapaxes(Psi, 1, 2)
+        phi = .5*np.stack((A[:, 2, 1], A[:, 0, 2], A[:, 1, 0]), -1)
+        k = self.base*np.exp(.5*(theta[self.i, :4] + theta[self.j, :4]))
+        dn, pn = dot(d, self.n0), dot(phi, self.n0)
+        dt, pt = d - dn[:, None]*self.n0, phi - pn[:, None]*self.n0
+        return Ri, Rj, pi, pj, D, Psi, k, dn, dt, pn, pt
+
+    def energy(self, theta, x, q):
+        """foam_dem_energy.py:405-421 (linear bond energy)."""
+        *_, k, dn, dt, pn, pt = self.kinematics(theta, x, q)
+        return float((.5*k[:, 0]*dn**2 + .5*(k[:, 1]*dot(dt, dt) + k[:, 2]*dot(pt, pt) + k[:, 3]*pn**2)).sum())
+
+    def forces(self, theta, x, q):
+        """-dE/dx and -dE/d(world rotation) (foam_dem_energy.py:797-811)."""
+        Ri, Rj, pi, pj, D, Psi, k, dn, dt, pn, pt = self.kinematics(theta, x, q)
+        gd = k[:, :1]*dn[:, None]*self.n0 + k[:, 1:2]*dt
+        gp = k[:, 3:4]*pn[:, None]*self.n0 + k[:, 2:3]*pt
+        Rgi, Rgj = np.einsum('bij,bj->bi', Ri, gd), np.einsum('bij,bj->bi', Rj, gd)
+        a = .5*(Rgi + Rgj)
+        trace = np.trace(Psi, axis1=1, axis2=2)
+        M = .5*(trace[:, None]*gp - np.einsum('bji,bj->bi', Psi, gp))
+        T = np.einsum('bij,bj->bi', Ri, M)
+        tj = cross(pj, a) - .5*cross(D, Rgj) + T
+        ti = -cross(pi, a) - .5*cross(D, Rgi) - T
+        n = len(x)
+        f = scatter_add(n, self.i, a) + scatter_add(n, self.j, -a)
+        tau = scatter_add(n, self.i, -ti) + scatter_add(n, self.j, -tj)
+        return f, tau

@@ -235,9 +235,36 @@ def main(reference):
         grads = torch.autograd.grad(loss, [theta] + loads)
         np.savez_compressed(HERE/f'{name}.npz', points=p, radii=radii, pairs=pairs, areas=area, masses=mass,
                             fixed=fixed, contacts=contacts, theta=np64(theta), loads=np.stack([np64(l) for l in loads]),
-                            weights=np64(weights), dt=dt, positions=np64(positions), loss=float(loss),
+                            weights=np64(weights), dt=dt, positions=np64(positions), loss=float(loss.detach()),
                             grad_theta=np64(grads[0]), grad_loads=np.stack([np64(g) for g in grads[1:]]))
         print(name, float(loss), np.abs(np64(grads[0])).max())
+
+    # ---- energy law (foam_dem_energy.py EnergyFoam, volume=False, small
+    # kinematics): bond energy, force and world torque at a perturbed state ----
+    from experiments.foam_dem_energy import EnergyFoam, quat_small
+    for name, geometry in (('energy_fixture', None), ('energy_foam5', 5)):
+        if geometry is None:
+            _, g = newton_fixture(False)
+            g = dict(g)
+        else:
+            foam = dpf_gb300.jittered_lattice_foam(geometry, seed=3)
+            g = dict(points=foam['points'], radii=foam['radii'], pairs=foam['pairs'], areas=foam['areas'],
+                     masses=foam['masses'], fixed=foam['fixed'], young=1200., shear=480.,
+                     contacts=dpf_gb300.newton.classical_contacts(foam['points'], foam['radii'], foam['pairs']))
+        young, shear = g.pop('young'), g.pop('shear')
+        model = EnergyFoam(g, volume=False, device='cpu', young=young, shear=shear, kinematics='small')
+        erng = np.random.default_rng(77)
+        n = len(g['points'])
+        scale = float(np.median(np.linalg.norm(g['points'][g['pairs'][:, 1]] - g['points'][g['pairs'][:, 0]], axis=1)))
+        theta = torch.tensor(erng.normal(0, .2, (n, 5)), dtype=torch.float64)
+        x = model.X + torch.tensor(erng.normal(0, .02*scale, (n, 3)), dtype=torch.float64)
+        q = quat_small(torch.tensor(erng.normal(0, .1, (n, 3)), dtype=torch.float64))
+        energy = model.energy(theta, x, q)
+        f, tau = model.forces(theta, x, q)
+        np.savez_compressed(HERE/f'{name}.npz', young=young, shear=shear, theta=np64(theta), x=np64(x), q=np64(q),
+                            energy=float(energy), force=np64(f), torque=np64(tau),
+                            **{f'in_{k}': np.asarray(v) for k, v in g.items()})
+        print(name, float(energy), float(np.abs(np64(f)).max()))
 
     # ---- jittered 8^3 lattice foam under gravity, three reference steps ----
     foam = dpf_gb300.jittered_lattice_foam(8, seed=0)

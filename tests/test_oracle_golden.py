@@ -146,3 +146,18 @@ def test_previous_solver_step(case):
     assert info['cg_iterations'] == int(g['step_previous_cg_iterations'])
     assert np.abs(s.x - g['step_previous_state_x']).max() < 1e-9
     assert abs(work - float(g['step_previous_work'])) <= 1e-9*abs(float(g['step_previous_work']))
+
+
+@pytest.mark.parametrize('name', ['energy_fixture', 'energy_foam5'])
+def test_energy_law_matches_reference(name):
+    """EnergyFoam (volume=False, small kinematics) energy, force and torque."""
+    from oracle import dem
+    g = golden(name)
+    inputs = {k[3:]: g[k] for k in g if k.startswith('in_')}
+    model = dem.EnergyBonds(inputs['points'], inputs['radii'], inputs['pairs'], inputs['areas'], inputs['contacts'],
+                            inputs['masses'], inputs['fixed'], float(g['young']), float(g['shear']))
+    e = model.energy(g['theta'], g['x'], g['q'])
+    f, tau = model.forces(g['theta'], g['x'], g['q'])
+    assert abs(e - float(g['energy'])) <= 1e-13*abs(float(g['energy']))
+    assert np.abs(f - g['force']).max() <= 1e-12*np.abs(g['force']).max()
+    assert np.abs(tau - g['torque']).max() <= 1e-12*np.abs(g['torque']).max()
