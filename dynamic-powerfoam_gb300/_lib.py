@@ -46,6 +46,15 @@ class TrialOut(ctypes.Structure):
                 ('offset_end', vp), ('fs_end', vp), ('mb_end', vp), ('fn_end', vp), ('mt_end', vp)]
 
 
+class ParallelParams(ctypes.Structure):
+    _fields_ = [(k, vp) for k in ('kn', 'ks', 'kb', 'kt', 'area', 'second_moment', 'polar_moment', 'radius',
+                                  'tensile', 'cohesion')] + [('tan_phi', f64), ('beta', f64)]
+
+
+class ParallelState(ctypes.Structure):
+    _fields_ = [(k, vp) for k in ('normal', 'fn', 'fs', 'mt', 'mb', 'break_energy', 'failure')]
+
+
 class Tiles(ctypes.Structure):
     _fields_ = [('n_tiles', i64), ('n_entries', i64), ('n_halo', i64), ('meta_words', i64), ('max_entries', i32),
                 ('max_sites', i32), ('max_halo', i32), ('max_meta_words', i32), ('tile_site', vp),
@@ -110,6 +119,10 @@ SIGNATURES = {
     'dpf_tiled_precondition': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp,
                                      i32, i32, vp]),
     'dpf_energy_partials_doubles': (i64, []),
+    'dpf_parallel_partials_doubles': (i64, []),
+    'dpf_parallel_advance': (i32, [P(Graph), P(ParallelParams), vp, vp, vp, vp, vp, vp, f64, P(ParallelState),
+                                   P(ParallelState), vp, vp, vp, vp]),
+    'dpf_parallel_loads': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_bond_energy': (i32, [P(Graph), vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_adjoint_jacobian_doubles': (i64, [i64]),
     'dpf_adjoint_slot_doubles': (i64, [i64]),
@@ -131,7 +144,7 @@ KERNELS = {
     'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 1,
     'dpf_segment_axpy': 1, 'dpf_segment_select': 1,
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
-    'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_bond_energy': 3,
+    'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
 }
 LAUNCHES = {'count': 0}
 

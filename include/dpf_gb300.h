@@ -521,6 +521,45 @@ int dpf_bond_energy(const dpf_graph *g, const double *base, const double *theta,
                     double *force, double *torque, double *energy, double *wrench, double *partials,
                     void *stream);
 
+/* ---- Parallel-bond component with brittle failure ----
+ * Replaces ParallelBonds.advance / loads (experiments/bonded_dem_core.py:132-208).
+ * Per bond: stiffnesses kn = kbar_n A, ks = kbar_s A, kb = kbar_n I, kt = kbar_s J,
+ * section area A, second and polar moments I, J, bond radius, tensile
+ * strength and cohesion (may be +inf); tan(friction angle) and the moment
+ * factor are shared. */
+typedef struct dpf_parallel_params {
+    const double *kn, *ks, *kb, *kt;
+    const double *area, *second_moment, *polar_moment, *radius;
+    const double *tensile, *cohesion;
+    double tan_phi, beta;
+} dpf_parallel_params;
+
+/* Bond history: normal, fs, mb (M, 3); fn, mt, break_energy (M); failure (M)
+ * int8 (0 intact, 1 tension, 2 shear).  Read through `in`, written to `out`. */
+typedef struct dpf_parallel_state {
+    double *normal, *fn, *fs, *mt, *mb, *break_energy;
+    int8_t *failure;
+} dpf_parallel_state;
+
+/* One step from the committed centres x to end (N, 3) with midpoint samples
+ * v, w (N, 3) (mid = (x + end)/2 when NULL).  Writes the new history to `out`
+ * (distinct arrays from `in`) and sums[4] = [constitutive work, elastic energy
+ * of the new state, removed energy of all broken bonds, newly broken bonds]
+ * (device doubles); guard failures (rotation > 0.25 rad, normal turn > 0.25
+ * rad per half step, coincident centres) are OR-ed into *status, and the
+ * caller then keeps `in`.  partials: dpf_parallel_partials_doubles(). */
+int64_t dpf_parallel_partials_doubles(void);
+int dpf_parallel_advance(const dpf_graph *g, const dpf_parallel_params *p, const double *radii, const double *x,
+                         const double *end, const double *mid, const double *v, const double *w, double dt,
+                         const dpf_parallel_state *in, const dpf_parallel_state *out, double *sums,
+                         double *partials, int *status, void *stream);
+
+/* Forces and torques about the centres x of the bond history (N, 3 each);
+ * wrench: 9 M doubles of scratch. */
+int dpf_parallel_loads(const dpf_graph *g, const double *radii, const double *x, const double *fn, const double *fs,
+                       const double *mt, const double *mb, double *force, double *torque, double *wrench,
+                       int *status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

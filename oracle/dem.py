@@ -782,3 +782,107 @@ class EnergyBonds:
         f = scatter_add(n, self.i, a) + scatter_add(n, self.j, -a)
         tau = scatter_add(n, self.i, -ti) + scatter_add(n, self.j, -tj)
         return f, tau
+
+
+# ---------------------------------------------------------------------------
+# Parallel-bond component with brittle failure (experiments/bonded_dem_core.py:45-208).
+
+class ParallelBonds:
+    """Stateful parallel bonds advanced once per step from midpoint samples.
+
+    Section constants (bonded_dem_core.py:86-93): A = pi r_b^2, I = pi r_b^4/4,
+    J = 2 I; kn = kbar_n A, ks = kbar_s A, kb = kbar_n I, kt = kbar_s J.
+    """
+
+    def __init__(self, reference, pairs, radii, bond_radius, kbar_n, kbar_s, tensile_strength=np.inf,
+                 cohesion=np.inf, friction_angle=0., moment_factor=1.):
+        self.x = np.array(reference, dtype=np.float64)
+        self.pairs = np.array(pairs, dtype=np.int64)
+        self.i, self.j = self.pairs.T
+        m = len(self.pairs)
+        per_bond = lambda v: np.broadcast_to(np.asarray(v, dtype=np.float64), (m,)).copy()
+        self.radii = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(self.x),)).copy()
+        self.rb = per_bond(bond_radius)
+        self.area = np.pi*self.rb**2
+        self.second_moment = np.pi*self.rb**4/4
+        self.polar_moment = 2*self.second_moment
+        kbn, kbs = per_bond(kbar_n), per_bond(kbar_s)
+        self.kn, self.ks = kbn*self.area, kbs*self.area
+        self.kb, self.kt = kbn*self.second_moment, kbs*self.polar_moment
+        self.tensile_strength, self.cohesion = per_bond(tensile_strength), per_bond(cohesion)
+        self.tan_phi, self.beta = np.tan(friction_angle), float(moment_factor)
+        self.normal, _ = self.geometry(self.x)
+        self.fn, self.mt = np.zeros(m), np.zeros(m)
+        self.fs, self.mb = np.zeros((m, 3)), np.zeros((m, 3))
+        self.failure = np.zeros(m, dtype=np.int8)
+        self.break_energy = np.zeros(m)
+        self.work, self.time = 0., 0.
+
+    def geometry(self, x):
+        """bonded_dem_core.py:117-126: unit normal i -> j and classical contact point."""
+        d = x[self.j] - x[self.i]
+        length = np.linalg.norm(d, axis=1)
+        if np.any(length <= 1e-12):
+            raise ValueError('Coincident centers are outside this baseline')
+        n = d/length[:, None]
+        return n, .5*(x[self.i] + x[self.j]) + .5*(self.radii[self.i] - self.radii[self.j])[:, None]*n
+
+    def elastic_energy_per_bond(self):
+        return .5*(self.fn**2/self.kn + dot(self.fs, self.fs)/self.ks + self.mt**2/self.kt
+                   + dot(self.mb, self.mb)/self.kb)
+
+    def loads(self):
+        """bonded_dem_core.py:132-142: forces and torques about the centres."""
+        n, c = self.geometry(self.x)
+        f = self.fn[:, None]*n + self.fs
+        couple = self.mt[:, None]*n + self.mb
+        size = len(self.x)
+        force = scatter_add(size, self.i, f) - scatter_add(size, self.j, f)
+        torque = (scatter_add(size, self.i, cross(c - self.x[self.i], f) + couple)
+                  + scatter_add(size, self.j, -cross(c - self.x[self.j], f) - couple))
+        return force, torque
+
+    def advance(self, x_next, velocity_mid, omega_mid, dt, *, x_mid=None):
+        """bonded_dem_core.py:144-208: midpoint increments, transports, failure."""
+        end = np.asarray(x_next, dtype=np.float64)
+        mid = .5*(self.x + end) if x_mid is None else np.asarray(x_mid, dtype=np.float64)
+        v, w = np.asarray(velocity_mid, dtype=np.float64), np.asarray(omega_mid, dtype=np.float64)
+        if np.max(np.linalg.norm(w, axis=1))*dt > .25:
+            raise ValueError('Body rotation > 0.25 rad per step; subdivide')
+        nm, contact = self.geometry(mid)
+        ne, _ = self.geometry(end)
+        half = .25*(w[self.i] + w[self.j])*dt
+        try:
+            fs0 = transport(self.fs, self.normal, nm, half)
+            mb0 = transport(self.mb, self.normal, nm, half)
+            transport(np.zeros_like(fs0), nm, ne, half)
+        except SubdivideError as e:
+            raise ValueError(str(e)) from e
+        du = (v[self.j] + cross(w[self.j], contact - mid[self.j]) - v[self.i]
+              - cross(w[self.i], contact - mid[self.i]))*dt
+        dth = (w[self.j] - w[self.i])*dt
+        on = (self.failure == 0).astype(np.float64)
+        dn, tw = dot(du, nm)*on, dot(dth, nm)*on
+        ds = (du - dot(du, nm)[:, None]*nm)*on[:, None]
+        bend = (dth - dot(dth, nm)[:, None]*nm)*on[:, None]
+        fn, mt = self.fn + self.kn*dn, self.mt + self.kt*tw
+        fs, mb = fs0 + self.ks[:, None]*ds, mb0 + self.kb[:, None]*bend
+        work = .5*((self.fn + fn)*dn + dot(fs0 + fs, ds) + (self.mt + mt)*tw + dot(mb0 + mb, bend))
+        sigma = fn/self.area + self.beta*np.linalg.norm(mb, axis=1)*self.rb/self.second_moment
+        tau = np.linalg.norm(fs, axis=1)/self.area + self.beta*np.abs(mt)*self.rb/self.polar_moment
+        intact = on > 0
+        tensile = intact & (sigma > self.tensile_strength)
+        shear = intact & ~tensile & (tau > self.cohesion - fn/self.area*self.tan_phi)
+        broken = tensile | shear
+        trial_energy = .5*(fn**2/self.kn + dot(fs, fs)/self.ks + mt**2/self.kt + dot(mb, mb)/self.kb)
+        self.break_energy = self.break_energy + np.where(broken, trial_energy, 0.)
+        self.failure = np.where(tensile, 1, np.where(shear, 2, self.failure)).astype(np.int8)
+        keep = (~broken).astype(np.float64)
+        fn, mt, fs, mb = fn*keep, mt*keep, fs*keep[:, None], mb*keep[:, None]
+        self.fn, self.mt = fn, mt
+        self.fs, self.mb = transport(fs, nm, ne, half), transport(mb, nm, ne, half)
+        self.work += float(work.sum())
+        self.x, self.normal = end.copy(), ne
+        self.time += dt
+        return dict(newly_broken=int(broken.sum()), energy=float(self.elastic_energy_per_bond().sum()),
+                    removed_bond_energy=float(self.break_energy.sum()))

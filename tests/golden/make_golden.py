@@ -190,6 +190,41 @@ def main(reference):
                         fin_mt=np64(fin.mt), fin_mb=np64(fin.mb), fin_loads=np64(fin.loads()),
                         fin_x=np64(fin.x), fin_normal=np64(fin.normal))
 
+    # ---- parallel bonds with brittle failure (bonded_dem_core.ParallelBonds):
+    # a jittered block pulled apart and sheared until bonds break ----
+    rng = np.random.default_rng(512)
+    g3 = np.array(np.meshgrid(np.arange(4), np.arange(3), np.arange(3), indexing='ij')).reshape(3, -1).T*.5
+    p = g3 + rng.normal(0, .02, g3.shape)
+    pairs = np.array([(i, j) for i in range(len(p)) for j in range(i+1, len(p))
+                      if np.linalg.norm(p[i]-p[j]) < .75])
+    r = rng.uniform(.25, .35, len(p))
+    length = np.linalg.norm(p[pairs[:, 1]]-p[pairs[:, 0]], axis=1)
+    core = ParallelBonds(p, pairs, r, .1, 1200/length, 480/length, tensile_strength=rng.uniform(40, 80, len(pairs)),
+                         cohesion=rng.uniform(30, 60, len(pairs)), friction_angle=.3, moment_factor=.7)
+    steps, ends, vs, ws = [], [], [], []
+    x = p.copy()
+    for step in range(40):
+        v = np.zeros_like(p)
+        v[:, 0] = .03*(p[:, 0] - p[:, 0].mean())          # stretch along x
+        v[:, 2] = .02*(p[:, 1] - p[:, 1].mean())          # shear z along y
+        v += rng.normal(0, .005, p.shape)
+        w = rng.normal(0, .05, p.shape)
+        dt = .05
+        end = x + v*dt
+        info = core.advance(end, v, w, dt)
+        steps.append([info['newly_broken'], info['energy'], info['removed_bond_energy']])
+        ends.append(end); vs.append(v); ws.append(w)
+        x = end
+    fc, tc = core.loads()
+    np.savez_compressed(HERE/'parallel_512.npz', points=p, radii=r, pairs=pairs, bond_radius=.1,
+                        kbar_n=1200/length, kbar_s=480/length, tensile=core.tensile_strength, cohesion=core.cohesion,
+                        friction_angle=.3, moment_factor=.7, dt=.05, ends=np.array(ends), vs=np.array(vs),
+                        ws=np.array(ws), steps=np.array(steps), fn=core.fn, fs=core.fs,
+                        mt=core.mt, mb=core.mb, failure=core.failure, break_energy=core.break_energy, work=core.work,
+                        x=core.x, normal=core.normal, force=fc, torque=tc)
+    print('parallel_512 broken', int((core.failure > 0).sum()), 'of', len(pairs), 'tension',
+          int((core.failure == 1).sum()), 'shear', int((core.failure == 2).sum()))
+
     # ---- FGMRES vs dense with a variable preconditioner, seed 381 ----
     rng = np.random.default_rng(381)
     a = torch.tensor(rng.normal(size=(36, 36)), dtype=torch.float64) + 8*torch.eye(36, dtype=torch.float64)

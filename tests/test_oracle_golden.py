@@ -161,3 +161,24 @@ def test_energy_law_matches_reference(name):
     assert abs(e - float(g['energy'])) <= 1e-13*abs(float(g['energy']))
     assert np.abs(f - g['force']).max() <= 1e-12*np.abs(g['force']).max()
     assert np.abs(tau - g['torque']).max() <= 1e-12*np.abs(g['torque']).max()
+
+
+def test_parallel_bonds_with_failure_match_reference():
+    """bonded_dem_core.ParallelBonds history with tensile and shear failure."""
+    from oracle import dem
+    g = golden('parallel_512')
+    b = dem.ParallelBonds(g['points'], g['pairs'], g['radii'], float(g['bond_radius']), g['kbar_n'], g['kbar_s'],
+                          g['tensile'], g['cohesion'], float(g['friction_angle']), float(g['moment_factor']))
+    for k, (end, v, w) in enumerate(zip(g['ends'], g['vs'], g['ws'])):
+        info = b.advance(end, v, w, float(g['dt']))
+        nb, e, removed = g['steps'][k]
+        assert info['newly_broken'] == int(nb)
+        assert abs(info['energy'] - e) <= 1e-10*max(abs(e), 1e-30)
+        assert abs(info['removed_bond_energy'] - removed) <= 1e-10*max(abs(removed), 1e-30)
+    assert np.array_equal(b.failure, g['failure'])
+    for k in ('fn', 'fs', 'mt', 'mb', 'break_energy', 'normal'):
+        assert np.abs(getattr(b, k) - g[k]).max() <= 1e-10*max(np.abs(g[k]).max(), 1e-30), k
+    assert abs(b.work - float(g['work'])) <= 1e-10*abs(float(g['work']))
+    f, t = b.loads()
+    assert np.abs(f - g['force']).max() <= 1e-10*np.abs(g['force']).max()
+    assert np.abs(t - g['torque']).max() <= 1e-10*np.abs(g['torque']).max()
