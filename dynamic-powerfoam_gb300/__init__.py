@@ -11,6 +11,7 @@ from .newton import (LinearBonds, FiniteBonds, NewtonBonds, FastNewtonBonds, Mix
 from .adjoint import DifferentiableBonds
 from .energy import EnergyFoam
 from .core import ParallelBonds
+from .static import reference_stiffness, solve_prescribed
 
 # Reference class names (experiments/bonded_dem_linear_gpu.py, bonded_dem_finite_gpu.py).
 LinearBondsGPU = LinearBonds
@@ -19,4 +20,4 @@ FiniteBondsGPU = FiniteBonds
 __all__ = ['jittered_lattice_foam', 'gravity_load', 'regular_edges', 'morton_order', 'LinearBonds',
            'FiniteBonds', 'NewtonBonds', 'FastNewtonBonds', 'MixedNewtonBonds', 'LinearBondsGPU', 'FiniteBondsGPU',
            'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error', 'DifferentiableBonds',
-           'EnergyFoam', 'ParallelBonds']
+           'EnergyFoam', 'ParallelBonds', 'reference_stiffness', 'solve_prescribed']

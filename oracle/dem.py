@@ -720,6 +720,22 @@ def reference_stiffness(points, pairs, contacts, kn, ks, kb, kt):
     return k
 
 
+def solve_prescribed(k, prescribed, values, load=None):
+    """Static linear equilibrium with the prescribed DOFs eliminated exactly
+    (restates ``experiments/bonded_dem_material.py:53-65`` with a dense solve)."""
+    q = np.array(values, dtype=np.float64).ravel()
+    mask = np.asarray(prescribed, dtype=bool).ravel()
+    free, fixed = np.flatnonzero(~mask), np.flatnonzero(mask)
+    rhs = np.zeros(len(q)) if load is None else np.asarray(load, dtype=np.float64).ravel()
+    q[free] = np.linalg.solve(k[np.ix_(free, free)], rhs[free] - k[np.ix_(free, fixed)]@q[fixed])
+    reaction = k@q - rhs
+    scale = max(np.linalg.norm(rhs), np.linalg.norm(reaction[fixed]), 1e-30)
+    residual = np.linalg.norm(reaction[free])/scale
+    if not np.isfinite(q).all() or residual > 1e-8:
+        raise AssertionError(f'Unresolved static equilibrium, relative residual {residual}')
+    return q, float(residual)
+
+
 # ---------------------------------------------------------------------------
 # Energy law (experiments/foam_dem_energy.py, EnergyFoam with volume=False and
 # kinematics='small'): bond potential, closed-form force and world torque.

@@ -225,6 +225,27 @@ def main(reference):
     print('parallel_512 broken', int((core.failure > 0).sum()), 'of', len(pairs), 'tension',
           int((core.failure == 1).sum()), 'shear', int((core.failure == 2).sum()))
 
+    # ---- static linear equilibrium (bonded_dem_material.solve_prescribed on the
+    # reference_stiffness of a jittered specimen): clamped face, prescribed
+    # stretch of the opposite face, random body loads ----
+    from experiments.bonded_dem_material import solve_prescribed, specimen
+    spec = specimen(3, length=2., jitter=.08)
+    sb, sx = spec['bonds'], spec['x']
+    k = reference_stiffness(sb)
+    prescribed = np.zeros((len(sx), 6), bool)
+    values = np.zeros((len(sx), 6))
+    left, right = sx[:, 0] < 1e-9, sx[:, 0] > spec['length'] - 1e-9
+    prescribed[left] = True
+    prescribed[right, 0] = True
+    values[right, 0] = .01
+    srng = np.random.default_rng(733)
+    load = srng.normal(0, 1e-3, (len(sx), 6))
+    q, residual = solve_prescribed(k, prescribed, values, load)
+    np.savez_compressed(HERE/'static_specimen.npz', points=sx, pairs=sb.pairs, radii=sb.radii, bond_radius=sb.rb,
+                        kbar_n=sb.kn/sb.area, kbar_s=sb.ks/sb.area, dense_k=k.toarray(), prescribed=prescribed,
+                        values=values, load=load, q=q.reshape(-1, 6), residual=residual)
+    print('static_specimen', len(sx), 'sites', len(sb.pairs), 'bonds', residual)
+
     # ---- FGMRES vs dense with a variable preconditioner, seed 381 ----
     rng = np.random.default_rng(381)
     a = torch.tensor(rng.normal(size=(36, 36)), dtype=torch.float64) + 8*torch.eye(36, dtype=torch.float64)

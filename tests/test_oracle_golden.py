@@ -182,3 +182,16 @@ def test_parallel_bonds_with_failure_match_reference():
     f, t = b.loads()
     assert np.abs(f - g['force']).max() <= 1e-10*np.abs(g['force']).max()
     assert np.abs(t - g['torque']).max() <= 1e-10*np.abs(g['torque']).max()
+
+
+def test_static_equilibrium_matches_reference():
+    """reference_stiffness + solve_prescribed on the reference's jittered specimen."""
+    from oracle import dem
+    g = golden('static_specimen')
+    b = dem.ParallelBonds(g['points'], g['pairs'], g['radii'], g['bond_radius'], g['kbar_n'], g['kbar_s'])
+    _, contacts = b.geometry(b.x)
+    k = dem.reference_stiffness(g['points'], g['pairs'], contacts, b.kn, b.ks, b.kb, b.kt)
+    assert np.abs(k - g['dense_k']).max() <= 1e-12*np.abs(g['dense_k']).max()
+    q, residual = dem.solve_prescribed(k, g['prescribed'], g['values'], g['load'])
+    assert np.abs(q.reshape(-1, 6) - g['q']).max() <= 1e-9*np.abs(g['q']).max()
+    assert residual < 1e-8
