@@ -32,6 +32,12 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture on
+# the 64^3 bench foam, profiles/tiled_pcg_hvp_64cube.txt): a tiled PCG launch of
+# exactly 20 iterations moved 5,359,088,640 B; a tiled HVP launch 174,099,456 B.
+PCG_DRAM_BYTES_PER_ITERATION_64 = 5359088640/20
+HVP_DRAM_BYTES_PER_LAUNCH_64 = 174099456
+
 METRIC = 'implicit Newton solves/s at rel. residual 1e-6 (64^3 jittered foam, 262k sites, ~1.95M bonds)'
 UNIT = 'solves/s'
 SMI_FIELDS = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
@@ -54,6 +60,9 @@ def parse():
     p.add_argument('--plain-steps', type=int, default=3,
                    help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
     p.add_argument('--hvp-launches', type=int, default=50, help='timed launches of the standalone tiled HVP (0: skip)')
+    p.add_argument('--profile-pcg', type=int, default=0,
+                   help='run one tiled PCG launch of exactly this many iterations in an NVTX range "profile_pcg" '
+                        '(for an ncu capture of its DRAM traffic)')
     p.add_argument('--adjoint-lattice', type=int, default=32, help='lattice size of the inverse-fit workload (0: skip)')
     p.add_argument('--adjoint-steps', type=int, default=50)
     p.add_argument('--adjoint-fd', type=int, default=4, help='bonds checked against central differences')
@@ -187,7 +196,8 @@ def run_hvp(s, dt, peak, peaks, launches=50):
     alg = 60*m + 56*n
     achieved = alg/(mean*1e-3)/1e9
     return dict(kernel='tiled_hvp_kernel', bond_hvps_per_s=m/(mean*1e-3), mean_ms=mean, min_ms=min(ms),
-                launches=len(ms), algorithmic_bytes=alg, achieved=achieved, peak=peak, unit='GB/s',
+                launches=len(ms), algorithmic_bytes=alg, traffic=HVP_DRAM_BYTES_PER_LAUNCH_64 if n == 262144 else None,
+                achieved=achieved, peak=peak, unit='GB/s',
                 frac=achieved/peak, peak_source='measured' if peaks else 'fallback', l2='flushed between launches',
                 tile=dict(max_entries=int(tiles.host['max_entries']), threads=tiles.threads, stages=tiles.stages,
                           tiles=int(tiles.host['n_tiles']), entries_per_bond=tiles.n_entries/max(1, m)),
@@ -434,12 +444,27 @@ def run_ours(args):
     roof = None
     if dominant:
         achieved = alg[dominant]/(kernels[dominant]['mean_ms']*1e-3)/1e9
+        traffic = None
+        if dominant == 'pcg' and args.precision == 'mixed' and args.lattice == 64 and args.seed == 0:
+            traffic = PCG_DRAM_BYTES_PER_ITERATION_64*cg/pcg_launches
         roof = dict(bound='hbm', kernel=dominant, achieved=achieved, peak=peak, unit='GB/s', frac=achieved/peak,
-                    traffic=None, peak_source='measured' if peaks else 'fallback',
+                    traffic=traffic, algorithmic_bytes=alg[dominant],
+                    traffic_source='ncu capture of this workload, scaled by CG iterations per launch'
+                    if traffic else None, peak_source='measured' if peaks else 'fallback',
                     launches=kernels[dominant]['launches'], mean_ms=kernels[dominant]['mean_ms'])
 
     hvp = run_hvp(s, args.dt, peak, peaks, launches=args.hvp_launches) \
         if args.precision == 'mixed' and args.hvp_launches > 0 and getattr(s, '_tiles', None) is not None else None
+    if args.profile_pcg > 0 and getattr(s, '_tiles', None) is not None:
+        s._pack_tiles(s._tiles, args.dt)
+        vec = torch.randn((n_sites, 6), dtype=torch.float64, device=device)
+        out = torch.empty_like(vec)
+        its = torch.zeros(1, dtype=torch.int32, device=device)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push('profile_pcg')
+        s._tiled_pcg(s._tiles, vec, out, 0.0, args.profile_pcg, its)
+        torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize()
     served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None
     adjoint = run_adjoint(args, device) if args.adjoint_lattice > 0 and world == 1 else None
     if rank != 0:
