@@ -105,3 +105,13 @@ def test_solver_refuses_cpu_device():
     import dpf_gb300
     with pytest.raises(ValueError):
         dpf_gb300.NewtonBonds(np.eye(3), 1., [[0, 1]], 1., 1., [False]*3, device='cpu')
+
+
+def test_mechanics_sources_cover_every_cuda_source():
+    from dpf_gb300.checkpoint import mechanics_sources
+    from pathlib import Path
+    hashes = mechanics_sources()
+    csrc = Path(__file__).resolve().parent.parent/'dynamic-powerfoam_gb300'/'csrc'
+    for f in list(csrc.glob('*.cu')) + list(csrc.glob('*.cuh')):
+        assert f.name in hashes and len(hashes[f.name]) == 64
+    assert 'dpf_gb300.h' in hashes and 'newton.py' in hashes
