@@ -246,6 +246,18 @@ def main(reference):
                         values=values, load=load, q=q.reshape(-1, 6), residual=residual)
     print('static_specimen', len(sx), 'sites', len(sb.pairs), 'bonds', residual)
 
+    # ---- render hand-off (bonded_dem_powerfoam.state_from_bodies) of body poses ----
+    from experiments.bonded_dem_powerfoam import appearance, state_from_bodies
+    hrng = np.random.default_rng(4040)
+    ref = hrng.uniform(0, 1, (30, 3))
+    base = appearance(ref, np.full(30, .12), hrng.uniform(size=30) < .2)
+    positions = ref + hrng.normal(0, .01, ref.shape)
+    rotations = Rotation.from_rotvec(hrng.normal(0, .3, (30, 3))).as_matrix()
+    state = state_from_bodies(base, positions, rotations)
+    np.savez_compressed(HERE/'handoff_30.npz', positions=positions, rotations=rotations,
+                        **{f'base_{k}': np.asarray(v) for k, v in base.items()},
+                        **{f'state_{k}': np.asarray(v) for k, v in state.items()})
+
     # ---- FGMRES vs dense with a variable preconditioner, seed 381 ----
     rng = np.random.default_rng(381)
     a = torch.tensor(rng.normal(size=(36, 36)), dtype=torch.float64) + 8*torch.eye(36, dtype=torch.float64)
