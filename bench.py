@@ -176,7 +176,7 @@ def run_hvp(s, dt, peak, peaks, launches=50):
 
     def launch():
         _lib.call('dpf_tiled_hvp', ctypes.byref(s._graph), ctypes.byref(tiles.struct), tiles.entries.data_ptr(),
-                  s._mass2.data_ptr(), s.fixed.data_ptr(), q.data_ptr(), y.data_ptr(), tiles.status.data_ptr(),
+                  s._site4.data_ptr(), q.data_ptr(), y.data_ptr(), tiles.status.data_ptr(),
                   tiles.threads, tiles.stages, stream.cuda_stream)
     for _ in range(3):
         launch()

@@ -59,7 +59,7 @@ class Tiles(ctypes.Structure):
     _fields_ = [('n_tiles', i64), ('n_entries', i64), ('n_halo', i64), ('meta_words', i64), ('max_entries', i32),
                 ('max_sites', i32), ('max_halo', i32), ('max_meta_words', i32), ('tile_site', vp),
                 ('tile_entry', vp), ('tile_halo', vp), ('tile_meta_off', vp), ('halo_site', vp), ('entry_bond', vp),
-                ('entry_ends', vp), ('tile_meta', vp)]
+                ('entry_ends', vp), ('tile_desc', vp), ('tile_meta', vp)]
 
 
 P = ctypes.POINTER
@@ -109,11 +109,11 @@ SIGNATURES = {
     'dpf_segment_axpy': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_segment_select': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_static_max_bonds': (i64, []),
-    'dpf_tile_graph': (i32, [i64, i64, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp]),
+    'dpf_tile_graph': (i32, [i64, i64, vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, i64, vp, vp]),
     'dpf_tile_meta_capacity': (i64, [i64, i64]),
     'dpf_tile_entry_floats': (i64, [i64]),
-    'dpf_tile_pack': (i32, [P(Tiles), vp, i64, f64, vp, vp, i64, vp, vp, vp, vp]),
-    'dpf_tiled_hvp': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, vp, i32, i32, vp]),
+    'dpf_tile_pack': (i32, [P(Tiles), vp, i64, f64, vp, vp, vp, i64, vp, vp, vp, vp]),
+    'dpf_tiled_hvp': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, i32, i32, vp]),
     'dpf_tiled_workspace_floats': (i64, [i64]),
     'dpf_tiled_partials_doubles': (i64, []),
     'dpf_tiled_precondition': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp,

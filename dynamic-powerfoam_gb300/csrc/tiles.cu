@@ -42,15 +42,16 @@ constexpr unsigned long long kWaitNs = 1000000000ull;  // mbarrier waits give up
 
 struct TileGraph {
     int32_t n_tiles;
-    const int32_t *tile_site, *tile_entry, *tile_halo, *tile_meta_off, *halo_site;
+    const int4 *desc;            // per tile (first site, sites, entries, halo), (first entry, -, meta word, words)
     const uint32_t *tile_meta;
     const float4 *e0, *e1, *e2;  // entry planes: (n, ri.x), (ri.y, ri.z, L, a kn), (a ks, a kb, a kt, ends)
+    const float4 *site;          // per site (mass, inertia, 1 free / 0 fixed, -); fixed sites (1, 1, 0, -)
 };
 
-// Byte offsets inside one of the two shared-memory tile buffers.
+// Byte offsets inside one of the shared-memory tile buffers.
 struct Layout {
     uint32_t plane;   // bytes of one record plane (16 * max entries)
-    uint32_t qown, qhalo, meta, size;
+    uint32_t qown, qhalo, site, meta, size;
     int stages;       // tile buffers in the ring
 };
 
@@ -141,20 +142,20 @@ __device__ __forceinline__ void entry_wrench(float4 a, float4 b, float4 c, const
 }
 
 struct TileView {
-    int64_t a, e0, h0, meta;
+    int64_t a, e0, meta;
     int T, E, H, words, halo_word;  // halo_word: first halo-site word in the metadata
 };
 
 __device__ __forceinline__ TileView tile_view(const TileGraph &G, int t) {
+    const int4 d0 = __ldg(G.desc + 2 * t), d1 = __ldg(G.desc + 2 * t + 1);
     TileView v;
-    v.a = G.tile_site[t];
-    v.T = G.tile_site[t + 1] - G.tile_site[t];
-    v.e0 = G.tile_entry[t];
-    v.E = G.tile_entry[t + 1] - G.tile_entry[t];
-    v.h0 = G.tile_halo[t];
-    v.H = G.tile_halo[t + 1] - G.tile_halo[t];
-    v.meta = G.tile_meta_off[t];
-    v.words = G.tile_meta_off[t + 1] - G.tile_meta_off[t];
+    v.a = d0.x;
+    v.T = d0.y;
+    v.E = d0.z;
+    v.H = d0.w;
+    v.e0 = d1.x;
+    v.meta = d1.z;
+    v.words = d1.w;
     v.halo_word = v.words - ((v.H + 3) & ~3);
     return v;
 }
@@ -184,8 +185,9 @@ __device__ __forceinline__ void issue_bulk(const TileGraph &G, const Layout &L, 
     fence_proxy_async();
     const uint32_t plane = 16u * (uint32_t)v.E, meta = 4u * (uint32_t)v.words;
     const OwnRange o = own_range(v);
-    const uint32_t own = (uint32_t)(o.hi - o.lo);
-    mbar_expect_tx(bar, 3 * plane + meta + own);
+    const uint32_t own = (uint32_t)(o.hi - o.lo), sites = 16u * (uint32_t)v.T;
+    mbar_expect_tx(bar, 3 * plane + meta + own + sites);
+    bulk_load(buf + L.site, G.site + v.a, sites, bar);
     if (v.E) {
         bulk_load(buf, G.e0 + v.e0, plane, bar);
         bulk_load(buf + L.plane, G.e1 + v.e0, plane, bar);
@@ -306,16 +308,18 @@ __device__ __forceinline__ bool for_tiles(const TileGraph &G, const Layout &L, P
     const int lane = threadIdx.x & (kLanes - 1);
     const int groups = blockDim.x / kLanes;
     int b = 0;
+    TileView v = tile_view(G, tile_of(0));
     for (int j = 0; j < n_local; ++j) {
-        const TileView v = tile_view(G, tile_of(j));
         const int bn = b + 1 == S ? 0 : b + 1;
         if (threadIdx.x == 0 && j + S - 1 < n_local) {
             const int bf = b == 0 ? S - 1 : b - 1;  // buffer of tile j - 1, free
             issue_bulk(G, L, tile_view(G, tile_of(j + S - 1)), q, buf_of(bf), P.bar + bf);
         }
+        TileView vn = v;
         if (j + 1 < n_local) {
+            vn = tile_view(G, tile_of(j + 1));
             if (!wait_bulk(P, bn, status)) return false;
-            issue_q(tile_view(G, tile_of(j + 1)), L, buf_of(bn), q);
+            issue_q(vn, L, buf_of(bn), q);
             asm volatile("cp.async.wait_group 1;" ::: "memory");
         } else {
             cp_async_wait_all();
@@ -353,10 +357,12 @@ __device__ __forceinline__ bool for_tiles(const TileGraph &G, const Layout &L, P
             const bool valid = sl < v.T;
             float acc[6];
             site_sum(W, span, codes, sl, valid, lane, acc);
-            if (valid && lane == 0) epi(v.a + sl, qown + 6 * sl, acc);
+            if (valid && lane == 0)
+                epi(v.a + sl, qown + 6 * sl, reinterpret_cast<const float4 *>(buf + L.site)[sl], acc);
         }
         __syncthreads();  // buffer b free
         b = bn;
+        v = vn;
     }
     return true;
 }
@@ -373,17 +379,10 @@ __device__ __forceinline__ void st6(float *p, const float v[6]) {
     q[2] = make_float2(v[4], v[5]);
 }
 
-// (diag M) q + alpha K q with identity rows on fixed sites.
-__device__ __forceinline__ void operator_row(const float2 *mass2, const uint8_t *fixed, int64_t s, const float *qs,
-                                             const float acc[6], float out[6]) {
-    if (fixed[s]) {
+// (diag M) q + alpha K q; fixed sites (record (1, 1, 0, -)) give q.
+__device__ __forceinline__ void operator_row(float4 rec, const float *qs, const float acc[6], float out[6]) {
 #pragma unroll
-        for (int c = 0; c < 6; ++c) out[c] = qs[c];
-    } else {
-        const float2 m = mass2[s];
-#pragma unroll
-        for (int c = 0; c < 6; ++c) out[c] = fmaf(c < 3 ? m.x : m.y, qs[c], acc[c]);
-    }
+    for (int c = 0; c < 6; ++c) out[c] = fmaf(c < 3 ? rec.x : rec.y, qs[c], rec.z * acc[c]);
 }
 
 // ---- standalone HVP ------------------------------------------------------------
@@ -391,8 +390,6 @@ __device__ __forceinline__ void operator_row(const float2 *mass2, const uint8_t 
 struct HvpArgs {
     TileGraph G;
     Layout L;
-    const float2 *mass2;  // (m, I) per site
-    const uint8_t *fixed;
     const float *q;
     float *y;
     int *status;
@@ -400,9 +397,9 @@ struct HvpArgs {
 
 struct HvpEpi {
     const HvpArgs &a;
-    __device__ __forceinline__ void operator()(int64_t s, const float *qs, const float acc[6]) const {
+    __device__ __forceinline__ void operator()(int64_t s, const float *qs, float4 rec, const float acc[6]) const {
         float out[6];
-        operator_row(a.mass2, a.fixed, s, qs, acc, out);
+        operator_row(rec, qs, acc, out);
         st6(a.y + 6 * s, out);
     }
 };
@@ -436,9 +433,10 @@ __global__ void __launch_bounds__(kThreads) pack_entries_kernel(PackArgs a) {
     a.e2[e] = make_float4(a.alpha * ri.w, a.alpha * rj.w, a.alpha * g.x, __uint_as_float(a.entry_ends[e]));
 }
 
-// P (36 floats, symmetric) -> 21 upper-triangle floats padded to 24; (m, I).
+// P (36 floats, symmetric) -> 21 upper-triangle floats padded to 24; site
+// records (m, I, 1, 0), fixed sites (1, 1, 0, 0).
 __global__ void __launch_bounds__(kThreads) pack_sites_kernel(int64_t n, const float *P36, const float *mass32,
-                                                              float4 *P24, float2 *mass2) {
+                                                              const uint8_t *fixed, float4 *P24, float4 *site) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= n) return;
     const float *p = P36 + 36 * s;
@@ -451,7 +449,9 @@ __global__ void __launch_bounds__(kThreads) pack_sites_kernel(int64_t n, const f
     u[21] = u[22] = u[23] = 0.0f;
 #pragma unroll
     for (int q = 0; q < 6; ++q) P24[6 * s + q] = make_float4(u[4 * q], u[4 * q + 1], u[4 * q + 2], u[4 * q + 3]);
-    if (mass2) mass2[s] = make_float2(mass32[6 * s], mass32[6 * s + 3]);
+    if (site)
+        site[s] = fixed[s] ? make_float4(1.0f, 1.0f, 0.0f, 0.0f)
+                           : make_float4(mass32[6 * s], mass32[6 * s + 3], 1.0f, 0.0f);
 }
 
 __device__ __forceinline__ void sym6(const float4 *P24, float P[21]) {
@@ -493,7 +493,6 @@ struct PcgArgs {
     int64_t n;
     TileGraph G;
     Layout L;
-    const float2 *mass2;
     const uint8_t *fixed;
     const float4 *P24;
     const float *block, *units32;
@@ -511,9 +510,9 @@ struct PcgArgs {
 struct PcgEpi {
     const PcgArgs &a;
     float dot;
-    __device__ __forceinline__ void operator()(int64_t s, const float *qs, const float acc[6]) {
+    __device__ __forceinline__ void operator()(int64_t s, const float *qs, float4 rec, const float acc[6]) {
         float wv[6];
-        operator_row(a.mass2, a.fixed, s, qs, acc, wv);
+        operator_row(rec, qs, acc, wv);
 #pragma unroll
         for (int c = 0; c < 6; ++c) dot = fmaf(wv[c], qs[c], dot);
         st6(a.w + 6 * s, wv);
@@ -651,15 +650,15 @@ constexpr int kMaxPcgBlocksTiled = 4096;
 constexpr size_t kMaxTileSmem = 220 * 1024;
 
 bool tiles_ok(const dpf_tiles *t) {
-    return t && t->n_tiles > 0 && t->tile_site && t->tile_entry && t->tile_halo && t->tile_meta_off &&
-           t->tile_meta && t->max_entries >= 0 && t->max_sites > 0 && t->max_meta_words > 0 &&
-           (t->n_halo == 0 || t->halo_site) && (t->n_entries == 0 || (t->entry_ends && t->entry_bond));
+    return t && t->n_tiles > 0 && t->tile_desc && t->tile_meta && t->max_entries >= 0 && t->max_sites > 0 &&
+           t->max_meta_words > 0 && (t->n_entries == 0 || (t->entry_ends && t->entry_bond)) &&
+           ((uintptr_t)t->tile_desc & 15u) == 0;
 }
 
-TileGraph tile_graph(const dpf_tiles *t, const float *entries) {
+TileGraph tile_graph(const dpf_tiles *t, const float *entries, const float *site) {
     const float4 *p = reinterpret_cast<const float4 *>(entries);
-    return TileGraph{(int32_t)t->n_tiles, t->tile_site, t->tile_entry, t->tile_halo, t->tile_meta_off, t->halo_site,
-                     t->tile_meta, p, p + t->n_entries, p + 2 * t->n_entries};
+    return TileGraph{(int32_t)t->n_tiles, reinterpret_cast<const int4 *>(t->tile_desc), t->tile_meta, p,
+                     p + t->n_entries, p + 2 * t->n_entries, reinterpret_cast<const float4 *>(site)};
 }
 
 size_t round16(size_t v) { return (v + 15) & ~(size_t)15; }
@@ -669,7 +668,8 @@ Layout layout_of(const dpf_tiles *t, int stages) {
     L.plane = 16u * (uint32_t)t->max_entries;
     L.qown = 3 * L.plane;
     L.qhalo = L.qown + (uint32_t)round16(24 * (size_t)t->max_sites + 16);
-    L.meta = L.qhalo + (uint32_t)round16(24 * (size_t)(t->max_halo > 0 ? t->max_halo : 1));
+    L.site = L.qhalo + (uint32_t)round16(24 * (size_t)(t->max_halo > 0 ? t->max_halo : 1));
+    L.meta = L.site + 16u * (uint32_t)t->max_sites;
     L.size = L.meta + 4u * (uint32_t)t->max_meta_words;
     L.stages = stages;
     return L;
@@ -699,17 +699,42 @@ int tile_launch_check(const dpf_tiles *t, int threads, int stages, size_t &smem)
     return DPF_OK;
 }
 
+// Launch shape of a persistent tiled kernel: shared-memory attributes and the
+// occupancy query run once per (device, kernel, threads, shared memory) and
+// are cached, so a launch costs no extra driver calls.
+struct GridKey {
+    int dev;
+    const void *kernel;
+    int threads;
+    size_t smem;
+};
+
 template <class K>
 int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t cap, int &grid) {
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-        return DPF_ERR_CUDA;
-    int dev = 0, sms = 0, per_sm = 0;
+    static GridKey keys[64];
+    static int values[64];
+    static int used = 0;
+    int dev = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-    if (sms <= 0 || per_sm <= 0) return DPF_ERR_CUDA;
-    int64_t g = (int64_t)sms * per_sm;
+    int per_grid = 0;
+    for (int k = 0; k < used; ++k)
+        if (keys[k].dev == dev && keys[k].kernel == (const void *)kernel && keys[k].threads == threads &&
+            keys[k].smem == smem)
+            per_grid = values[k];
+    if (per_grid == 0) {
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+            cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+            return DPF_ERR_CUDA;
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+        if (sms <= 0 || per_sm <= 0) return DPF_ERR_CUDA;
+        per_grid = sms * per_sm;
+        const int slot = used < 64 ? used++ : (int)(((uintptr_t)kernel + (uintptr_t)smem + threads) % 64);
+        keys[slot] = GridKey{dev, (const void *)kernel, threads, smem};
+        values[slot] = per_grid;
+    }
+    int64_t g = per_grid;
     if (g > n_tiles) g = n_tiles;
     if (g > cap) g = cap;
     grid = (int)g;
@@ -724,10 +749,11 @@ int dpf_tile_graph(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const
                    const int32_t *inc_bond, int32_t max_entries, int32_t max_stage, int32_t *tile_site,
                    int32_t *tile_entry, int32_t *tile_halo, int32_t *tile_meta_off, int32_t *halo_site,
                    int32_t *entry_bond, uint32_t *entry_ends, uint32_t *tile_meta, int64_t meta_capacity,
-                   int64_t *counts) {
+                   int32_t *tile_desc, int64_t *counts) {
     if (n_sites <= 0 || n_sites > INT32_MAX || n_bonds < 0 || n_bonds > INT32_MAX / 2 || !inc_ptr || !counts ||
         (n_bonds && (!edges || !inc_bond || !entry_bond || !entry_ends || !halo_site)) || !tile_site ||
-        !tile_entry || !tile_halo || !tile_meta_off || !tile_meta || max_entries < 1 || max_entries > 32767 ||
+        !tile_entry || !tile_halo || !tile_meta_off || !tile_meta || !tile_desc || max_entries < 1 ||
+        max_entries > 32767 ||
         max_stage < 1 || max_stage > 65535 || meta_capacity < 4)
         return DPF_ERR_ARGUMENT;
     if (inc_ptr[0] != 0 || inc_ptr[n_sites] != 2 * n_bonds) return DPF_ERR_ARGUMENT;
@@ -845,6 +871,17 @@ int dpf_tile_graph(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const
     tile_entry[n_tiles] = (int32_t)e;
     tile_halo[n_tiles] = (int32_t)h;
     tile_meta_off[n_tiles] = (int32_t)words;
+    for (int32_t tt = 0; tt < n_tiles; ++tt) {
+        int32_t *d = tile_desc + 8 * (int64_t)tt;
+        d[0] = tile_site[tt];
+        d[1] = tile_site[tt + 1] - tile_site[tt];
+        d[2] = tile_entry[tt + 1] - tile_entry[tt];
+        d[3] = tile_halo[tt + 1] - tile_halo[tt];
+        d[4] = tile_entry[tt];
+        d[5] = tile_halo[tt];
+        d[6] = tile_meta_off[tt];
+        d[7] = tile_meta_off[tt + 1] - tile_meta_off[tt];
+    }
     counts[0] = n_tiles;
     counts[1] = e;
     counts[2] = h;
@@ -862,9 +899,11 @@ int64_t dpf_tile_entry_floats(int64_t n_entries) { return 12 * n_entries; }
 int64_t dpf_tile_meta_capacity(int64_t n_sites, int64_t n_bonds) { return 9 * n_sites + 3 * n_bonds + 16; }
 
 int dpf_tile_pack(const dpf_tiles *t, const float *bond_data, int64_t n_bonds, double alpha, const float *P36,
-                  const float *mass32, int64_t n_sites, float *entries, float *P24, float *mass2, void *stream) {
+                  const float *mass32, const uint8_t *fixed, int64_t n_sites, float *entries, float *P24,
+                  float *site4, void *stream) {
     if (!tiles_ok(t) || !bond_data || !entries || !aligned16(bond_data) || !aligned16(entries) ||
-        (P24 && (!P36 || !aligned16(P24) || n_sites <= 0)) || (mass2 && !mass32))
+        (P24 && (!P36 || !aligned16(P24) || n_sites <= 0)) ||
+        (site4 && (!mass32 || !fixed || !aligned16(site4) || n_sites <= 0)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     // tangent planes of the mixed bond data: records (7 M float4) then t0..t3
@@ -876,18 +915,17 @@ int dpf_tile_pack(const dpf_tiles *t, const float *bond_data, int64_t n_bonds, d
                    e + 2 * t->n_entries};
         pack_entries_kernel<<<blocks_for(t->n_entries, kThreads), kThreads, 0, st>>>(a);
     }
-    if (P24)
+    if (P24 || site4)
         pack_sites_kernel<<<blocks_for(n_sites, kThreads), kThreads, 0, st>>>(
-            n_sites, P36, mass32, reinterpret_cast<float4 *>(P24), reinterpret_cast<float2 *>(mass2));
+            n_sites, P36, mass32, fixed, reinterpret_cast<float4 *>(P24), reinterpret_cast<float4 *>(site4));
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
 
-int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *mass2,
-                  const uint8_t *fixed, const float *q, float *y, int *status, int threads, int stages,
-                  void *stream) {
-    if (!g || !tiles_ok(t) || !entries || !mass2 || !fixed || !q || !y || !status || !aligned16(entries) ||
-        !aligned16(q) || !aligned16(y))
+int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4, const float *q,
+                  float *y, int *status, int threads, int stages, void *stream) {
+    if (!g || !tiles_ok(t) || !entries || !site4 || !q || !y || !status || !aligned16(entries) ||
+        !aligned16(site4) || !aligned16(q) || !aligned16(y))
         return DPF_ERR_ARGUMENT;
     size_t smem = 0;
     int rc = tile_launch_check(t, threads, stages, smem);
@@ -895,8 +933,7 @@ int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, 
     int grid = 0;
     rc = persistent_grid(tiled_hvp_kernel, threads, smem, t->n_tiles, INT32_MAX, grid);
     if (rc) return rc;
-    HvpArgs a{tile_graph(t, entries), pick_layout(t, stages), reinterpret_cast<const float2 *>(mass2), fixed, q, y,
-              status};
+    HvpArgs a{tile_graph(t, entries, site4), pick_layout(t, stages), q, y, status};
     tiled_hvp_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
@@ -904,14 +941,14 @@ int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, 
 
 int64_t dpf_tiled_workspace_floats(int64_t n_sites) { return 36 * n_sites; }
 
-int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *mass2,
+int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4,
                            const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
                            const double *vector, double tolerance, int max_iterations, double *out, int *iterations,
                            float *workspace, double *partials, unsigned *barrier, int *status, int threads,
                            int stages, void *stream) {
-    if (!g || !tiles_ok(t) || g->n_sites <= 0 || !entries || !mass2 || !fixed || !block32 || !P24 || !units32 ||
+    if (!g || !tiles_ok(t) || g->n_sites <= 0 || !entries || !site4 || !fixed || !block32 || !P24 || !units32 ||
         !vector || !out || !iterations || !workspace || !partials || !barrier || !status || max_iterations < 1 ||
-        !aligned16(entries) || !aligned16(workspace) || !aligned16(P24))
+        !aligned16(entries) || !aligned16(workspace) || !aligned16(P24) || !aligned16(site4))
         return DPF_ERR_ARGUMENT;
     size_t smem = 0;
     int rc = tile_launch_check(t, threads, stages, smem);
@@ -922,9 +959,8 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
     const int64_t n6 = 6 * g->n_sites;
     PcgArgs a{};
     a.n = g->n_sites;
-    a.G = tile_graph(t, entries);
+    a.G = tile_graph(t, entries, site4);
     a.L = pick_layout(t, stages);
-    a.mass2 = reinterpret_cast<const float2 *>(mass2);
     a.fixed = fixed;
     a.P24 = reinterpret_cast<const float4 *>(P24);
     a.block = block32;

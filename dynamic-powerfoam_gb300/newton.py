@@ -983,7 +983,7 @@ class MixedNewtonBonds(NewtonBonds):
         if not self.tiled:
             return
         lib = self._lib
-        self._mass2 = torch.empty((n, 2), dtype=torch.float32, device=dev)
+        self._site4 = torch.empty((n, 4), dtype=torch.float32, device=dev)
         self._p24 = torch.empty(24*n, dtype=torch.float32, device=dev)
         self._tiled_workspace = torch.empty(lib.dpf_tiled_workspace_floats(n), dtype=torch.float32, device=dev)
         self._tiled_partials = torch.zeros(lib.dpf_tiled_partials_doubles(), dtype=F64, device=dev)
@@ -991,15 +991,15 @@ class MixedNewtonBonds(NewtonBonds):
         self._packed = None
 
     def _pack_tiles(self, tiles, dt):
-        """Entry records (alpha = dt^2/4 folded in), packed P and (m, I) for ``tiles``."""
+        """Entry records (alpha = dt^2/4 folded in), packed P and site records for ``tiles``."""
         self._call('dpf_tile_pack', ctypes.byref(tiles.struct), self._bond_data.data_ptr(), self.n_bonds,
-                   .25*dt*dt, self._p32.data_ptr(), self._mass32.data_ptr(), self.n_sites, tiles.entries.data_ptr(),
-                   self._p24.data_ptr(), self._mass2.data_ptr(), self._stream())
+                   .25*dt*dt, self._p32.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), self.n_sites,
+                   tiles.entries.data_ptr(), self._p24.data_ptr(), self._site4.data_ptr(), self._stream())
         self._packed = (tiles, dt)
 
     def _tiled_pcg(self, tiles, vector, out, tolerance, max_iterations, iterations):
         self._call('dpf_tiled_precondition', ctypes.byref(self._graph), ctypes.byref(tiles.struct),
-                   tiles.entries.data_ptr(), self._mass2.data_ptr(), self.fixed.data_ptr(),
+                   tiles.entries.data_ptr(), self._site4.data_ptr(), self.fixed.data_ptr(),
                    self._block32.data_ptr(), self._p24.data_ptr(), self._units32.data_ptr(), vector.data_ptr(),
                    float(tolerance), int(max_iterations), out.data_ptr(), iterations.data_ptr(),
                    self._tiled_workspace.data_ptr(), self._tiled_partials.data_ptr(), self._barrier.data_ptr(),

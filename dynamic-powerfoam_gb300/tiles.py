@@ -32,13 +32,15 @@ def host_tiles(edges, inc_ptr, inc_bond, n_sites, max_entries=DEFAULT[0], max_st
     out = dict(tile_site=np.zeros(n_sites + 1, np.int32), tile_entry=np.zeros(n_sites + 1, np.int32),
                tile_halo=np.zeros(n_sites + 1, np.int32), tile_meta_off=np.zeros(n_sites + 1, np.int32),
                halo_site=np.zeros(max(1, 2*m), np.int32), entry_bond=np.zeros(max(1, 2*m), np.int32),
-               entry_ends=np.zeros(max(1, 2*m), np.uint32), tile_meta=np.zeros(capacity, np.uint32))
+               entry_ends=np.zeros(max(1, 2*m), np.uint32), tile_meta=np.zeros(capacity, np.uint32),
+               tile_desc=np.zeros(8*n_sites, np.int32))
     counts = np.zeros(9, np.int64)
     p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     _lib.check(lib.dpf_tile_graph(n_sites, m, p(edges), p(inc_ptr), p(inc_bond), int(max_entries), int(max_stage),
                                   p(out['tile_site']), p(out['tile_entry']), p(out['tile_halo']),
                                   p(out['tile_meta_off']), p(out['halo_site']), p(out['entry_bond']),
-                                  p(out['entry_ends']), p(out['tile_meta']), capacity, p(counts)),
+                                  p(out['entry_ends']), p(out['tile_meta']), capacity, p(out['tile_desc']),
+                                  p(counts)),
                'dpf_tile_graph')
     (n_tiles, n_entries, n_halo, meta_words, max_e, max_sites, max_halo, max_meta,
      max_stage_used) = (int(c) for c in counts)
@@ -48,6 +50,7 @@ def host_tiles(edges, inc_ptr, inc_bond, n_sites, max_entries=DEFAULT[0], max_st
     out['entry_bond'] = out['entry_bond'][:max(1, n_entries)]
     out['entry_ends'] = out['entry_ends'][:max(1, n_entries)]
     out['tile_meta'] = out['tile_meta'][:meta_words]
+    out['tile_desc'] = out['tile_desc'][:8*n_tiles]
     out.update(n_tiles=n_tiles, n_entries=n_entries, n_halo=n_halo, meta_words=meta_words, max_entries=max_e,
                max_sites=max_sites, max_halo=max_halo, max_meta_words=max_meta, max_stage=max_stage_used)
     return out
@@ -74,7 +77,7 @@ class Tiles:
         self.stages = int(stages)
         dev = lambda k: torch.as_tensor(host[k].view(np.int32), device=device).contiguous()
         for k in ('tile_site', 'tile_entry', 'tile_halo', 'tile_meta_off', 'halo_site', 'entry_bond', 'entry_ends',
-                  'tile_meta'):
+                  'tile_desc', 'tile_meta'):
             setattr(self, k, dev(k))
         self.n_entries = host['n_entries']
         lib = _lib.load()
@@ -85,7 +88,7 @@ class Tiles:
                                  host['max_entries'], host['max_sites'], host['max_halo'], host['max_meta_words'],
                                  *(getattr(self, k).data_ptr() for k in (
                                      'tile_site', 'tile_entry', 'tile_halo', 'tile_meta_off', 'halo_site',
-                                     'entry_bond', 'entry_ends', 'tile_meta')))
+                                     'entry_bond', 'entry_ends', 'tile_desc', 'tile_meta')))
 
     @classmethod
     def build(cls, edges, inc_ptr, inc_bond, n_sites, device, max_entries=DEFAULT[0], threads=DEFAULT[1],

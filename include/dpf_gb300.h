@@ -449,6 +449,8 @@ typedef struct {
     const int32_t *halo_site;      /* n_halo: global site of each halo slot */
     const int32_t *entry_bond;     /* n_entries: bond of each entry */
     const uint32_t *entry_ends;    /* n_entries: local i | local j << 16 (halo slots after own sites) */
+    const int32_t *tile_desc;      /* 8 per tile, 16-byte aligned: first site, sites, entries, halo
+                                      sites, first entry, first halo slot, first metadata word, words */
     const uint32_t *tile_meta;     /* per tile: T + 1 spans start | mid << 16 (the site's incidences
                                       [start, mid) are i ends, [mid, next start) j ends; offsets
                                       from the tile's first incidence), then the entry (uint16) of
@@ -460,7 +462,7 @@ typedef struct {
  * holding at most max_entries entries (<= 32767) and max_stage own + halo
  * sites (<= 65535).  Output arrays: tile_* n_sites + 1; halo_site,
  * entry_bond, entry_ends 2 n_bonds; tile_meta meta_capacity words
- * (dpf_tile_meta_capacity).  counts (9): n_tiles, n_entries, n_halo,
+ * (dpf_tile_meta_capacity); tile_desc 8 n_sites.  counts (9): n_tiles, n_entries, n_halo,
  * meta_words, max entries, max own sites, max halo sites, max metadata words
  * of a tile, max own + halo sites.  DPF_ERR_TOO_LARGE when one site's bonds
  * alone exceed the limits. */
@@ -468,7 +470,7 @@ int dpf_tile_graph(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const
                    const int32_t *inc_bond, int32_t max_entries, int32_t max_stage, int32_t *tile_site,
                    int32_t *tile_entry, int32_t *tile_halo, int32_t *tile_meta_off, int32_t *halo_site,
                    int32_t *entry_bond, uint32_t *entry_ends, uint32_t *tile_meta, int64_t meta_capacity,
-                   int64_t *counts);
+                   int32_t *tile_desc, int64_t *counts);
 int64_t dpf_tile_meta_capacity(int64_t n_sites, int64_t n_bonds);
 
 /* Floats of the packed entry records (three float4 planes per entry). */
@@ -477,20 +479,22 @@ int64_t dpf_tile_entry_floats(int64_t n_entries);
 /* Pack the float32 tangent of dpf_mixed_bond_floats bond data into entry
  * records with alpha (= dt^2/4) folded into the stiffnesses; optionally pack
  * the float32 block inverse P36 (N, 6, 6) into 24 floats per site (upper
- * triangle) and the mass pairs (m, I) from mass32 (N, 6). */
+ * triangle) and the site records site4 (N, 4) = (m, I, 1, 0) from mass32
+ * (N, 6), (1, 1, 0, 0) on fixed sites. */
 int dpf_tile_pack(const dpf_tiles *t, const float *bond_data, int64_t n_bonds, double alpha, const float *P36,
-                  const float *mass32, int64_t n_sites, float *entries, float *P24, float *mass2, void *stream);
+                  const float *mass32, const uint8_t *fixed, int64_t n_sites, float *entries, float *P24,
+                  float *site4, void *stream);
 
 /* y = (diag M + alpha K) q in float32 with identity rows on fixed sites;
- * q, y float32 (N, 6), 16-byte aligned; mass2 (N, 2) = (m, I).  Persistent
+ * q, y float32 (N, 6), 16-byte aligned; site4 the site records of
+ * dpf_tile_pack.  Persistent
  * CTAs of `threads` (<= 384, >= max_entries / 2) walk their tiles through a
  * ring of `stages` shared-memory buffers (2..4; 0 = the deepest that fits)
  * filled by TMA bulk copies (records, metadata, own-site q) and cp.async
  * (halo q); a wait past its time limit sets DPF_ERR_BARRIER_TIMEOUT in
  * *status. */
-int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *mass2,
-                  const uint8_t *fixed, const float *q, float *y, int *status, int threads, int stages,
-                  void *stream);
+int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4, const float *q,
+                  float *y, int *status, int threads, int stages, void *stream);
 
 /* Elastic PCG of dpf_mixed_precondition on the tiled operator, two grid
  * barriers per iteration (single-reduction recurrence); same stopping rule
@@ -499,7 +503,7 @@ int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, 
  * buffers per CTA (2..4; 0 = the deepest that fits). */
 int64_t dpf_tiled_workspace_floats(int64_t n_sites);
 int64_t dpf_tiled_partials_doubles(void);
-int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *mass2,
+int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4,
                            const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
                            const double *vector, double tolerance, int max_iterations, double *out, int *iterations,
                            float *workspace, double *partials, unsigned *barrier, int *status, int threads,

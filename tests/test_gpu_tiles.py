@@ -58,7 +58,7 @@ def test_tiled_hvp_matches_float64_product(max_entries, threads, stages):
     q32 = q.float().contiguous()
     y = torch.empty_like(q32)
     _lib.call('dpf_tiled_hvp', ctypes.byref(s._graph), ctypes.byref(tiles.struct), tiles.entries.data_ptr(),
-              s._mass2.data_ptr(), s.fixed.data_ptr(), q32.data_ptr(), y.data_ptr(), tiles.status.data_ptr(), threads,
+              s._site4.data_ptr(), q32.data_ptr(), y.data_ptr(), tiles.status.data_ptr(), threads,
               stages, s._stream())
     assert int(tiles.status.item()) == 0
     ref = _direct_operator(s, .25*dt*dt, q32.double())

@@ -67,6 +67,8 @@ def test_tiles_cover_graph(max_entries):
                 assert t['entry_bond'][e0 + code] == (v if v >= 0 else ~v)
                 assert (k - ptr[a] >= mid[s - a]) == (v < 0)
         assert t['max_sites'] >= b - a and t['max_halo'] >= h1 - h0
+        assert list(t['tile_desc'][8*tile:8*tile + 8]) == [a, b - a, e1 - e0, h1 - h0, e0, h0, t['tile_meta_off'][tile],
+                                                           t['tile_meta_off'][tile + 1] - t['tile_meta_off'][tile]]
         words = t['tile_meta'][t['tile_meta_off'][tile]:t['tile_meta_off'][tile + 1]]
         n_halo_words = (h1 - h0 + 3) // 4*4
         assert np.array_equal(words[len(words) - n_halo_words:][:h1 - h0].view(np.int32), t['halo_site'][h0:h1])
