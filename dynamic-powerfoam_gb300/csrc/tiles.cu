@@ -18,6 +18,7 @@
 // Only bonds cut by tile boundaries are read twice; wrenches never go to
 // global memory.
 #include <algorithm>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -26,7 +27,7 @@ namespace dpf {
 namespace tiles {
 
 #ifndef DPF_TILE_LANES
-#define DPF_TILE_LANES 2
+#define DPF_TILE_LANES 4
 #endif
 
 constexpr int kLanes = DPF_TILE_LANES;  // lanes per site in the site sums
@@ -714,6 +715,8 @@ int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t
     static GridKey keys[64];
     static int values[64];
     static int used = 0;
+    static std::mutex lock;
+    std::lock_guard<std::mutex> guard(lock);
     int dev = 0;
     cudaGetDevice(&dev);
     int per_grid = 0;
