@@ -382,7 +382,7 @@ using namespace dpf::adj;
 extern "C" {
 
 static bool adj_ok(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h, const double *y) {
-    return g && g->n_sites > 0 && g->inc_ptr && g->inc_bond && (g->n_bonds == 0 || g->edges) && k && h && h->x &&
+    return g && g->n_sites > 0 && g->inc_ptr && (g->n_bonds == 0 || (g->edges && g->inc_bond)) && k && h && h->x &&
            h->radii && h->normal && h->offset && h->fn && h->fs && h->mt && h->mb && y;
 }
 

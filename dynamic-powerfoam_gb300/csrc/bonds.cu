@@ -645,7 +645,7 @@ int64_t dpf_partials_doubles(void) { return kPartialsOffset + 2 * 64 * (int64_t)
 
 static bool graph_ok(const dpf_graph *g) {
     return g && g->n_sites > 0 && g->n_bonds >= 0 && g->n_bonds < (int64_t(1) << 31) && g->inc_ptr &&
-           g->inc_bond && (g->n_bonds == 0 || g->edges);
+           (g->n_bonds == 0 || (g->edges && g->inc_bond));
 }
 
 int dpf_stiffness_apply(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t, const double *q,
@@ -712,14 +712,16 @@ static int launch_trial_bonds(const dpf_graph *g, const dpf_stiffness *k, const 
     return DPF_OK;
 }
 
-static bool history_ok(const dpf_history *h) {
-    return h && h->x && h->radii && h->normal && h->offset && h->fn && h->fs && h->mt && h->mb;
+// Per-bond history arrays may be null (empty) when the graph has no bonds.
+static bool history_ok(const dpf_history *h, int64_t n_bonds = 1) {
+    return h && h->x && h->radii &&
+           (n_bonds == 0 || (h->normal && h->offset && h->fn && h->fs && h->mt && h->mb));
 }
 
 int dpf_trial(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h, const double *y,
               const double *mid_positions, const double *end_positions, int want_end, const dpf_trial_out *out,
               double *wrench, int *status, void *stream) {
-    if (!graph_ok(g) || !k || !history_ok(h) || !y || !out || !out->force || !status ||
+    if (!graph_ok(g) || !k || !history_ok(h, g->n_bonds) || !y || !out || !out->force || !status ||
         (g->n_bonds && !wrench))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
@@ -744,7 +746,7 @@ int dpf_residual(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *
                  const double *v, const double *external, const double *mass, const uint8_t *fixed, double dt,
                  const dpf_trial_out *trial, const double *preconditioner, const double *units, double *residual,
                  double *scaled, double *norms, double *wrench, double *partials, int *status, void *stream) {
-    if (!graph_ok(g) || !k || !history_ok(h) || !y || !v || !external || !mass || !fixed || !residual ||
+    if (!graph_ok(g) || !k || !history_ok(h, g->n_bonds) || !y || !v || !external || !mass || !fixed || !residual ||
         !status || (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
@@ -781,7 +783,7 @@ int dpf_jacobian_vector(const dpf_graph *g, const dpf_stiffness *k, const dpf_hi
                         const double *direction, const double *mass, const uint8_t *fixed, double dt,
                         const double *units, const double *preconditioner, double *out, double *wrench,
                         void *stream) {
-    if (!graph_ok(g) || !k || !history_ok(h) || !y || !direction || !mass || !fixed || !out ||
+    if (!graph_ok(g) || !k || !history_ok(h, g->n_bonds) || !y || !direction || !mass || !fixed || !out ||
         (g->n_bonds && !wrench) || (preconditioner && !units))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
@@ -815,7 +817,7 @@ int dpf_bond_setup(int64_t n_sites, int64_t n_bonds, const int64_t *edges, const
 }
 
 int dpf_loads(const dpf_graph *g, const dpf_history *h, double *out, double *wrench, void *stream) {
-    if (!graph_ok(g) || !history_ok(h) || !out || (g->n_bonds && !wrench)) return DPF_ERR_ARGUMENT;
+    if (!graph_ok(g) || !history_ok(h, g->n_bonds) || !out || (g->n_bonds && !wrench)) return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds)
         loads_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(g->n_bonds, g->edges, *h, wrench,

@@ -201,7 +201,8 @@ int dpf_parallel_advance(const dpf_graph *g, const dpf_parallel_params *p, const
 int dpf_parallel_loads(const dpf_graph *g, const double *radii, const double *x, const double *fn, const double *fs,
                        const double *mt, const double *mb, double *force, double *torque, double *wrench,
                        int *status, void *stream) {
-    if (!g || g->n_sites <= 0 || !g->inc_ptr || !g->inc_bond || !radii || !x || !force || !torque || !status ||
+    if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && !g->inc_bond) || !radii || !x || !force ||
+        !torque || !status ||
         (g->n_bonds && (!g->edges || !fn || !fs || !mt || !mb || !wrench)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;

@@ -144,7 +144,7 @@ int dpf_bond_energy(const dpf_graph *g, const double *base, const double *theta,
                     void *stream) {
     const bool want_forces = force || torque;
     if (!g || g->n_sites <= 0 || (g->n_bonds && (!g->edges || !base || !theta || !n0 || !ri || !rj)) || !x ||
-        !q || theta_stride < 4 || (want_forces && (!g->inc_ptr || !g->inc_bond || (g->n_bonds && !wrench))) ||
+        !q || theta_stride < 4 || (want_forces && (!g->inc_ptr || (g->n_bonds && (!g->inc_bond || !wrench)))) ||
         (energy && !partials) || (!want_forces && !energy))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;

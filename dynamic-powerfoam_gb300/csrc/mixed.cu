@@ -1235,16 +1235,18 @@ int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds) {
 }
 
 static bool mixed_graph_ok(const dpf_graph *g) {
-    return g && g->n_sites > 0 && g->n_bonds >= 0 && g->n_bonds < (int64_t(1) << 31) && g->inc_ptr && g->inc_bond;
+    return g && g->n_sites > 0 && g->n_bonds >= 0 && g->n_bonds < (int64_t(1) << 31) && g->inc_ptr &&
+           (g->n_bonds == 0 || g->inc_bond);
 }
 
 int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h, const double *mass,
                     const double *v, const double *external, const uint8_t *fixed, double dt, float *bond_data,
                     double *r0, double *loads, double *scales, double *wrench, double *partials, int *status,
                     void *stream) {
-    if (!mixed_graph_ok(g) || !k || !h || !h->x || !h->radii || !h->normal || !h->offset || !h->fn || !h->fs ||
-        !h->mt || !h->mb || !mass || !v || !external || !fixed || !bond_data || !r0 || !scales || !partials ||
-        !status || (g->n_bonds && (!wrench || !g->edges)))
+    if (!mixed_graph_ok(g) || !k || !h || !h->x || !h->radii ||
+        (g->n_bonds && (!h->normal || !h->offset || !h->fn || !h->fs || !h->mt || !h->mb)) || !mass || !v ||
+        !external || !fixed || !bond_data || !r0 || !scales || !partials || !status ||
+        (g->n_bonds && (!wrench || !g->edges)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
@@ -1420,16 +1422,19 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
     a.status = status;
     if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return DPF_ERR_CUDA;
     void *args[] = {&a};
-    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel_f32, grid, kPcgThreads, args, 0, st) != cudaSuccess)
+    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel_f32, grid, kPcgThreads, args, 0, st) != cudaSuccess) {
+        cudaGetLastError();
         return DPF_ERR_CUDA;
+    }
     return DPF_OK;
 }
 
 int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h, const double *y, const float *y32,
                      double *x_end, double *normal_end, double *offset_end, double *fn_end, double *fs_end,
                      double *mt_end, double *mb_end, float *dloads, double *loads, void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !h || !h->x || !h->fn || !h->fs || !h->mt || !h->mb || !h->offset ||
-        !y || !y32 || !x_end || (dloads && !loads) ||
+    if (!mixed_graph_ok(g) || !bond_data || !h || !h->x ||
+        (g->n_bonds && (!h->fn || !h->fs || !h->mt || !h->mb || !h->offset)) || !y || !y32 || !x_end ||
+        (dloads && !loads) ||
         ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;

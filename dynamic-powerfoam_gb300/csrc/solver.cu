@@ -461,7 +461,8 @@ int dpf_elastic_precondition(const dpf_graph *g, const dpf_stiffness *k, const d
                              const double *units, const double *vector, double dt, double tolerance,
                              int max_iterations, double *out, int *iterations, double *wrench, double *workspace,
                              unsigned *barrier, int *status, void *stream) {
-    if (!g || g->n_sites <= 0 || !g->inc_ptr || !g->inc_bond || !k || !t || !mass || !fixed || !block ||
+    if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && !g->inc_bond) || !k || !t || !mass || !fixed ||
+        !block ||
         !preconditioner || !units || !vector || !out || !iterations || !workspace || !barrier || !status ||
         max_iterations < 1 || (g->n_bonds && (!wrench || !g->edges)))
         return DPF_ERR_ARGUMENT;
@@ -504,8 +505,10 @@ int dpf_elastic_precondition(const dpf_graph *g, const dpf_stiffness *k, const d
     a.status = status;
     if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), st) != cudaSuccess) return DPF_ERR_CUDA;
     void *args[] = {&a};
-    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel, grid, kThreads, args, 0, st) != cudaSuccess)
+    if (cudaLaunchCooperativeKernel((const void *)pcg_kernel, grid, kThreads, args, 0, st) != cudaSuccess) {
+        cudaGetLastError();
         return DPF_ERR_CUDA;
+    }
     return DPF_OK;
 }
 

@@ -725,9 +725,13 @@ int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t
             keys[k].smem == smem)
             per_grid = values[k];
     if (per_grid == 0) {
-        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-            cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+        // the attribute is the cap (not this shape's size): any cached shape stays launchable
+        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxTileSmem) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess) {
+            cudaGetLastError();
             return DPF_ERR_CUDA;
+        }
         int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
@@ -985,8 +989,10 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
     a.status = status;
     void *args[] = {&a};
     if (cudaLaunchCooperativeKernel((const void *)tiled_pcg_kernel, grid, threads, args, smem,
-                                    (cudaStream_t)stream) != cudaSuccess)
+                                    (cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();  // report it here, not at the next caller's launch check
         return DPF_ERR_CUDA;
+    }
     return DPF_OK;
 }
 
