@@ -173,12 +173,17 @@ class LinearBonds:
         _lib.check(getattr(self._lib, name)(*args), name)
 
     def _fetch(self, scalars=0, status=False):
-        """Copy device scalars (and the status word) to the host with one sync."""
+        """Copy device scalars (and the status word) to the host with one sync;
+        a step's deferred scale (see ``MixedNewtonBonds._step_begin``) rides along."""
         stream = torch.cuda.current_stream(self.device)
         if scalars:
             self._host_scalars[:scalars].copy_(self._scalars[:scalars], non_blocking=True)
         if status:
             self._host_status.copy_(self._status[:1], non_blocking=True)
+        deferred = getattr(self, '_deferred_scale', None)
+        if deferred is not None:
+            self._host_scalars[8:10].copy_(deferred, non_blocking=True)
+            self._deferred_scale = None
         stream.synchronize()
         return self._host_scalars[:scalars].tolist(), int(self._host_status[0]) if status else 0
 
@@ -544,12 +549,14 @@ def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iteratio
         return x.reshape(shape), dict(iterations=0, relative_residual=0.)
     residual = b.clone(); iterations = 0
     relative = float('nan')
+    residual_norm = norm      # the first cycle starts from x = 0
     while iterations < max_iterations:
         width = min(restart, max_iterations - iterations)
         ws = workspace if (workspace is not None and workspace.width >= width and workspace.length == length) \
             else _Krylov(length, width, device)
         h = np.zeros((width+1, width)); cs, sn = np.zeros(width), np.zeros(width)
-        g = np.zeros(width+1); g[0] = norm_of(residual)
+        g = np.zeros(width+1); g[0] = residual_norm if residual_norm is not None else norm_of(residual)
+        residual_norm = None
         _lib.check(lib.dpf_axpby(length, 1./g[0], residual.data_ptr(), 0., residual.data_ptr(),
                                  ws.basis[0].data_ptr(), stream), 'dpf_axpby')
         for j in range(width):
@@ -819,7 +826,7 @@ class NewtonBonds(FiniteBonds):
         self._v = self._vec(self.v).clone()
         y = torch.zeros_like(self._v)
         stream = self._stream()
-        rhs_scale = self._step_begin(dt, external)
+        rhs_scale = self._step_begin(dt, external)    # a number, or a callable read after the first fetch
         krylov = 0
         self.inner_iterations = 0
         residual_trace = []
@@ -827,6 +834,8 @@ class NewtonBonds(FiniteBonds):
         n6 = 6*self.n_sites
         for iteration in range(max_iterations+1):
             scaled, (rnorm, local, merit) = self._iteration_residual(y, dt, external)
+            if callable(rhs_scale):
+                rhs_scale = rhs_scale()
             relative = rnorm/rhs_scale
             if not np.isfinite(relative) or not np.isfinite(local):
                 raise SubdivideError(f'Subdivide: non-finite Newton residual ({relative:g}, {local:g})')
@@ -836,8 +845,9 @@ class NewtonBonds(FiniteBonds):
                 self.time += dt
                 self._call('dpf_dot_norm', n6, external.data_ptr(), y.data_ptr(), self._scalars.data_ptr(),
                            self._partials.data_ptr(), stream)
-                (work,), _ = self._fetch(1)
-                max_rotation = float(torch.linalg.vector_norm(y[:, 3:], dim=1).max()) if len(y) else 0.
+                if len(y):
+                    self._scalars[2:3].copy_(torch.linalg.vector_norm(y[:, 3:], dim=1).max().reshape(1))
+                (work, _, max_rotation), _ = self._fetch(3)
                 return work, dict(nonlinear_iterations=iteration, nonlinear_relative_residual=relative,
                                   local_pose_defect=local, krylov_iterations=krylov,
                                   cg_iterations=self.inner_iterations, residual_trace=residual_trace,
@@ -1030,11 +1040,14 @@ class MixedNewtonBonds(NewtonBonds):
         self._cached = None
         self._status.zero_()
         history = self._history_struct()
+        if getattr(self, '_begin_scales', None) is None:
+            self._begin_scales = torch.zeros(2, dtype=F64, device=self.device)
+        scales = self._begin_scales
         if self._token is not None and self._token == self._state_token() and \
                 self._since_refresh < self.refresh_interval:
             self._timed('setup', lambda: self._call(
                 'dpf_mixed_begin', self.n_sites, self._loads.data_ptr(), self.mass.data_ptr(), self._v.data_ptr(),
-                external.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(), self._scalars.data_ptr(),
+                external.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(), scales.data_ptr(),
                 self._partials.data_ptr(), self._stream()))
         else:
             self._since_refresh = 0
@@ -1042,12 +1055,16 @@ class MixedNewtonBonds(NewtonBonds):
                 'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                 ctypes.byref(history), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
                 self.fixed.data_ptr(), dt, self._bond_data.data_ptr(), self._r0.data_ptr(), self._loads.data_ptr(),
-                self._scalars.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(),
+                scales.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(),
                 self._status.data_ptr(), self._stream()))
-        (a, l), status = self._fetch(2, status=True)
-        if status:
-            raise guard_error(status)
-        return max(a, .5*dt*dt*l, 1e-30)
+        # the scales reach the host with the first residual's fetch (one sync
+        # less per step); a setup guard is raised by that residual's own trial
+        self._deferred_scale = scales
+
+        def rhs_scale():
+            a, l = self._host_scalars[8:10].tolist()
+            return max(a, .5*dt*dt*l, 1e-30)
+        return rhs_scale
 
     def _mixed_residual(self, y, dt, want_tangent, use_p, scaled=None):
         r = torch.empty_like(y)

@@ -104,6 +104,33 @@ def device_incidence(edges, n_sites):
     return ptr.to(torch.int32).contiguous(), value[order].to(torch.int32).contiguous()
 
 
+# Device copies of request bond graphs, keyed by the host pairs array (many
+# requests share one graph, e.g. one per lattice size): edges (m, 2) int32 and
+# the incidence CSR, uploaded and sorted once.  The cache keeps the host array
+# alive, so its id is not reused while the entry exists.
+_GRAPHS = {}
+_GRAPHS_LOCK = threading.Lock()
+_GRAPHS_MAX = 64
+
+
+def _device_graph(pairs, n_sites, device):
+    key = (id(pairs), n_sites, str(device))
+    with _GRAPHS_LOCK:
+        hit = _GRAPHS.get(key)
+        if hit is not None and hit[0] is pairs:
+            return hit[1:]
+    fp = np.asarray(pairs)
+    if len(fp) and (fp.min() < 0 or fp.max() >= n_sites):
+        raise ValueError('Invalid endpoint index')
+    edges = torch.as_tensor(np.ascontiguousarray(fp, dtype=np.int32), device=device).reshape(-1, 2)
+    ptr, inc = device_incidence(edges.to(torch.int64), n_sites)
+    with _GRAPHS_LOCK:
+        if len(_GRAPHS) >= _GRAPHS_MAX:
+            _GRAPHS.pop(next(iter(_GRAPHS)))
+        _GRAPHS[key] = (pairs, edges, ptr, inc)
+    return edges, ptr, inc
+
+
 class RequestState:
     """Resident state of one or several requests: exactly what a ``Batch``
     concatenates (the attributes of fresh ``MixedNewtonBonds`` solvers, without
@@ -143,11 +170,9 @@ class RequestState:
         staging = _staging()
         n_load = 6*n if loads is not None else 0
         f64 = staging.host('f8', 5*n + m + n_load)
-        i32 = staging.host('i4', 2*m)
         u8 = staging.host('u1', n)
         pts, rad, mas, are = f64[:3*n].reshape(n, 3), f64[3*n:4*n], f64[4*n:5*n], f64[5*n:5*n + m]
         ext = f64[5*n + m:5*n + m + n_load].reshape(-1, 6)
-        pairs = i32.reshape(m, 2)
 
         def copy(k):
             f = foams[k]
@@ -156,10 +181,6 @@ class RequestState:
             rad[a:b] = f['radii']
             mas[a:b] = f['masses']
             are[c:d] = f['areas']
-            fp = np.asarray(f['pairs'])
-            if len(fp) and (fp.min() < 0 or fp.max() >= b - a):
-                raise ValueError('Invalid endpoint index')
-            np.add(fp, a, out=pairs[c:d], casting='unsafe')
             u8[a:b] = np.asarray(f['fixed'], dtype=bool)
             if n_load:
                 ext[a:b] = loads[k]
@@ -167,14 +188,23 @@ class RequestState:
         list(_COPIERS.map(copy, range(len(foams))))
         if np.any(mas <= 0):
             raise ValueError('Only positive-mass bodies can enter this solver')
+        # bond graphs from the device cache, concatenated with site and bond offsets
+        graphs = [_device_graph(f['pairs'], sites[k], self.device) for k, f in enumerate(foams)]
         dev64 = staging.send('f8', 5*n + m + n_load, self.device)
         self.external = dev64[5*n + m:].view(n, 6) if n_load else None
-        dev32 = staging.send('i4', 2*m, self.device)
         self.fixed = staging.send('u1', n, self.device).view(torch.bool)
         self.p = dev64[:3*n].view(n, 3)
         self.radii = dev64[3*n:4*n]
         masses_d, areas_d = dev64[4*n:5*n], dev64[5*n:5*n + m]
-        edges = dev32.view(m, 2).to(torch.int64).contiguous()
+        if len(foams) == 1:
+            edges = graphs[0][0].to(torch.int64).contiguous()
+            inc_ptr, inc_bond = graphs[0][1], graphs[0][2]
+        else:
+            edges = torch.cat([g[0].to(torch.int64) + int(so[k]) for k, g in enumerate(graphs)]).contiguous()
+            inc_ptr = torch.cat([g[1][:-1] + 2*int(bo[k]) for k, g in enumerate(graphs)] +
+                                [torch.full((1,), 2*m, dtype=torch.int32, device=self.device)]).contiguous()
+            inc_bond = torch.cat([torch.where(g[2] >= 0, g[2] + int(bo[k]), g[2] - int(bo[k]))
+                                  for k, g in enumerate(graphs)]).contiguous()
         self.n_sites, self.n_bonds = n, m
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         self.n, self.ri, self.rj, self.offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
@@ -200,7 +230,7 @@ class RequestState:
         self.fs, self.mb = torch.zeros_like(self.n), torch.zeros_like(self.n)
         self.v = torch.zeros_like(self.mass)
         self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(n, 1, 1)
-        self._inc_ptr, self._inc_bond = device_incidence(edges, n)
+        self._inc_ptr, self._inc_bond = inc_ptr, inc_bond
         self.time = 0.
 
 
@@ -413,6 +443,7 @@ class Batch(MixedNewtonBonds):
         self._v = self._vec(self.v).clone()
         self._status.zero_()
         MixedNewtonBonds._step_begin(self, dt, external)     # r0, maintained loads (global)
+        self._deferred_scale = None                           # per-request scales come from segments
         h = .5*dt*dt
         rhs_vec = -(self._r0 + h*self._loads)                 # dt M v + dt^2/2 ext
         self._segment(rhs_vec)

@@ -94,6 +94,9 @@ def test_group_state_matches_solver_setup():
     from dpf_gb300 import serving
     reqs = serving.synthetic_stream(3, seed=9, sites=(700, 3000))
     group = serving.RequestState.group([r.foam for r in reqs])
+    # the concatenated cached graphs give the incidence of the group's own edges
+    ptr, inc = serving.device_incidence(group.edges, group.n_sites)
+    assert torch.equal(ptr, group._inc_ptr) and torch.equal(inc, group._inc_bond)
     site0 = bond0 = 0
     for r in reqs:
         s = _solver(r)
