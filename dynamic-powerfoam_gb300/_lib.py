@@ -96,15 +96,15 @@ SIGNATURES = {
     'dpf_mixed_residual': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_mixed_scaling': (i32, [P(Graph), vp, vp, vp, vp, f64, vp, vp, vp, vp, vp]),
     'dpf_mixed_scale_residual': (i32, [i64, vp, vp, vp, vp, vp, vp, vp]),
-    'dpf_mixed_jacobian_vector': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_jacobian_vector': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_mixed_stiffness_apply': (i32, [P(Graph), vp, vp, vp, vp, vp]),
     'dpf_to_float': (i32, [i64, vp, vp, vp]),
     'dpf_mixed_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, f64, i32, vp, vp, vp, vp, vp, vp,
-                                     vp]),
+                                     vp, vp, vp]),
     'dpf_mixed_commit': (i32, [P(Graph), vp, P(History), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_mixed_begin': (i32, [i64, vp, vp, vp, vp, vp, f64, vp, vp, vp, vp]),
     'dpf_mixed_residual_segmented': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp,
-                                           vp, vp, vp]),
+                                           vp, vp, vp, vp]),
     'dpf_segment_norms': (i32, [i32, vp, vp, vp, i32, vp, vp, vp]),
     'dpf_segment_axpy': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_segment_select': (i32, [i64, vp, vp, vp, vp, vp, vp]),

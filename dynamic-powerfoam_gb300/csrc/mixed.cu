@@ -303,7 +303,8 @@ struct ResidualBondArgs {
     int want_tangent;
     float *wrench;
     int *status;
-    const int32_t *seg;  // optional per-bond segment: status[seg[b]]
+    const int32_t *seg;      // optional per-bond segment: status[seg[b]]
+    const uint8_t *active;   // optional per-segment flag: bonds of inactive segments are skipped
 };
 
 __device__ __forceinline__ void load_y(const float *y, int s, V3<float> &u, V3<float> &w) {
@@ -312,9 +313,19 @@ __device__ __forceinline__ void load_y(const float *y, int s, V3<float> &u, V3<f
     w = {p[3], p[4], p[5]};
 }
 
+__device__ __forceinline__ void store_zero9(float *w, int64_t b) {
+    float *p = w + 9 * b;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) p[c] = 0.0f;
+}
+
 __global__ void __launch_bounds__(kThreads) residual_bonds(ResidualBondArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
+    if (a.active && !a.active[a.seg[b]]) {  // a converged request of a batch: its rows are not read
+        store_zero9(a.wrench, b);
+        return;
+    }
     const Bond B = load_bond(a.bd.rec, b);
     V3<float> ui, wi, uj, wj;
     load_y(a.y, B.i, ui, wi);
@@ -470,6 +481,8 @@ struct JvpArgs {
     BondData bd;
     const float *y, *d;
     float *wrench;
+    const int32_t *seg;     // optional: bonds of inactive segments give zero
+    const uint8_t *active;
 };
 
 __device__ __forceinline__ V3<Dual> dual3(V3<float> v, V3<float> d) {
@@ -488,6 +501,10 @@ __global__ void __launch_bounds__(kThreads) prepare_direction(int64_t count, con
 __global__ void __launch_bounds__(kThreads) jvp_bonds_mixed(JvpArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
+    if (a.active && !a.active[a.seg[b]]) {
+        store_zero9(a.wrench, b);
+        return;
+    }
     const Bond B = load_bond(a.bd.rec, b);
     V3<float> ui, wi, uj, wj, dui, dwi, duj, dwj;
     load_y(a.y, B.i, ui, wi);
@@ -871,6 +888,8 @@ struct PcgArgs {
     double *part_a, *part_b;
     unsigned *barrier;
     int *status;
+    const int32_t *seg;     // optional: bonds of inactive segments are skipped (their direction is zero)
+    const uint8_t *active;
 };
 
 __device__ __forceinline__ void ld8(const float4 *p, float v[6]) {
@@ -978,7 +997,14 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
     for (; it < a.max_it; ++it) {
         // K d_k with d_k = z_k + beta d_{k-1} formed per endpoint
 #pragma unroll 2
-        for (int64_t b = tid; b < a.m; b += stride) stiffness_bond_dir(a.bd, a.zd, beta, a.wrench, b);
+        for (int64_t b = tid; b < a.m; b += stride) {
+            if (a.active && !a.active[a.seg[b]]) {
+                float4 *w = a.wrench + 3 * b;
+                w[0] = w[1] = w[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                continue;
+            }
+            stiffness_bond_dir(a.bd, a.zd, beta, a.wrench, b);
+        }
         if (!grid_barrier(a.barrier, a.status)) return;
         // ad = (diag M + alpha K) d_k with identity rows on fixed sites; store d_k
         pf = 0.0f;
@@ -1264,7 +1290,8 @@ int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const dou
                                  const double *mass, const uint8_t *fixed, double dt, const double *r0,
                                  int want_tangent, const float *preconditioner, const float *units32, double *residual,
                                  double *scaled, double *norms, float *wrench, double *partials, int *status,
-                                 const int32_t *seg_bond, const int32_t *seg_site, void *stream);
+                                 const int32_t *seg_bond, const int32_t *seg_site, const uint8_t *active,
+                                 void *stream);
 
 int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const float *y32, const double *mass,
                        const uint8_t *fixed, double dt, const double *r0, int want_tangent, const float *preconditioner,
@@ -1272,21 +1299,22 @@ int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, co
                        double *partials, int *status, void *stream) {
     return dpf_mixed_residual_segmented(g, bond_data, y, y32, mass, fixed, dt, r0, want_tangent, preconditioner,
                                         units32, residual, scaled, norms, wrench, partials, status, nullptr, nullptr,
-                                        stream);
+                                        nullptr, stream);
 }
 
 int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const double *y, const float *y32,
                                  const double *mass, const uint8_t *fixed, double dt, const double *r0,
                                  int want_tangent, const float *preconditioner, const float *units32, double *residual,
                                  double *scaled, double *norms, float *wrench, double *partials, int *status,
-                                 const int32_t *seg_bond, const int32_t *seg_site, void *stream) {
+                                 const int32_t *seg_bond, const int32_t *seg_site, const uint8_t *active,
+                                 void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !y || !y32 || !mass || !fixed || !r0 || !residual || !status ||
-        (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units32))
+        (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units32) || (active && !seg_bond))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
         ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, want_tangent, wrench, status,
-                           seg_bond};
+                           seg_bond, active};
         residual_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     ResidualSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, y, mass, r0, fixed, 0.5 * dt * dt,
@@ -1319,15 +1347,16 @@ int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const
 
 int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float *y32, const double *direction,
                               const float *mass32, const uint8_t *fixed, double dt, const float *units32,
-                              const float *preconditioner, double *out, float *d32, float *wrench, void *stream) {
+                              const float *preconditioner, double *out, float *d32, float *wrench,
+                              const int32_t *seg_bond, const uint8_t *active, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !y32 || !direction || !mass32 || !fixed || !out || !d32 ||
-        (g->n_bonds && !wrench) || (preconditioner && !units32))
+        (g->n_bonds && !wrench) || (preconditioner && !units32) || (active && !seg_bond))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n6 = 6 * g->n_sites;
     prepare_direction<<<blocks_for(n6, kThreads), kThreads, 0, st>>>(n6, direction, units32, d32);
     if (g->n_bonds) {
-        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, d32, wrench};
+        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, d32, wrench, seg_bond, active};
         jvp_bonds_mixed<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, d32, mass32, preconditioner, units32, fixed,
@@ -1377,9 +1406,10 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
                            const float *block, const float *preconditioner, const float *units32,
                            const double *vector, double dt, double tolerance, int max_iterations, double *out,
                            int *iterations, float *wrench, float *workspace, unsigned *barrier, int *status,
-                           void *stream) {
+                           const int32_t *seg_bond, const uint8_t *active, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !mass32 || !fixed || !block || !preconditioner || !units32 || !vector ||
-        !out || !iterations || !workspace || !barrier || !status || max_iterations < 1 || (g->n_bonds && !wrench))
+        !out || !iterations || !workspace || !barrier || !status || max_iterations < 1 || (g->n_bonds && !wrench) ||
+        (active && !seg_bond))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     MixedDeviceInfo &info = mixed_info();
@@ -1406,6 +1436,8 @@ int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *ma
     a.max_it = max_iterations;
     a.out = out;
     a.iterations = iterations;
+    a.seg = seg_bond;
+    a.active = active;
     float4 *w4 = reinterpret_cast<float4 *>(workspace);
     const int64_t n = g->n_sites;
     a.zd = w4;                 // 4 float4 per site

@@ -1106,9 +1106,14 @@ class MixedNewtonBonds(NewtonBonds):
                 'dpf_mixed_jacobian_vector', ctypes.byref(self._graph), self._bond_data.data_ptr(),
                 self._y32.data_ptr(), v.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), dt,
                 self._units32.data_ptr(), self._p32.data_ptr(), out.data_ptr(), self._d32.data_ptr(),
-                self._wrench32.data_ptr(), self._stream()))
+                self._wrench32.data_ptr(), *self._bond_mask(), self._stream()))
             return out
         return operator
+
+    def _bond_mask(self):
+        """(per-bond segment, per-segment active flag) device pointers that let
+        the bond passes skip bonds of finished segments; (None, None) here."""
+        return None, None
 
     def _newton_preconditioner(self, dt):
         def precondition(vector, tolerance=.03, max_iterations=80):
@@ -1124,7 +1129,7 @@ class MixedNewtonBonds(NewtonBonds):
                 self._mass32.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p32.data_ptr(),
                 self._units32.data_ptr(), vector.data_ptr(), dt, tolerance, max_iterations, out.data_ptr(),
                 self._inner.data_ptr(), self._wrench32.data_ptr(), self._mixed_workspace.data_ptr(),
-                self._barrier.data_ptr(), self._status.data_ptr(), self._stream()))
+                self._barrier.data_ptr(), self._status.data_ptr(), *self._bond_mask(), self._stream()))
             return out
         return precondition
 

@@ -283,6 +283,7 @@ class Batch(MixedNewtonBonds):
     """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
 
     tiled = False
+    _active_mask = None
 
     def __init__(self, parts, pool=None):
         if not parts:
@@ -425,8 +426,23 @@ class Batch(MixedNewtonBonds):
                    self._units32.data_ptr() if use_p else None, r.data_ptr(),
                    _addr_or_none(scaled) if use_p else None, None, self._wrench32.data_ptr(),
                    self._partials.data_ptr(), self._status.data_ptr(), self.seg_bond.data_ptr(),
-                   self.seg_site.data_ptr(), self._stream())
+                   self.seg_site.data_ptr(), self._bond_mask()[1], self._stream())
         return r
+
+    def _bond_mask(self):
+        if self._active_mask is None:
+            return None, None
+        return self.seg_bond.data_ptr(), self._active_mask.data_ptr()
+
+    def _set_active(self, requests):
+        """Bond passes of the following launches skip every request not in
+        ``requests`` (their sites' rows of those passes are not read)."""
+        if len(requests) == self.n_segments:
+            self._active_mask = None
+            return
+        flags = np.zeros(self.n_segments, dtype=np.uint8)
+        flags[list(requests)] = 1
+        self._active_mask = torch.as_tensor(flags).to(self.device)
 
     # ---- the batched Newton step ------------------------------------------------------
     @torch.no_grad()
@@ -458,7 +474,9 @@ class Batch(MixedNewtonBonds):
         iters = np.zeros(R, dtype=np.int64)
         krylov = np.zeros(R, dtype=np.int64)
         cg = np.zeros(R, dtype=np.int64)
+        self._active_mask = None
         for iteration in range(max_iterations+1):
+            self._set_active([k for k in range(R) if done[k] is None])
             r = self._residual_segmented(y, dt, want_tangent=True, use_p=False)
             self._call('dpf_mixed_scaling', ctypes.byref(self._graph), self._bond_data.data_ptr(),
                        self._mass32.data_ptr(), self.fixed.data_ptr(), self.radii.data_ptr(), dt,
@@ -492,6 +510,7 @@ class Batch(MixedNewtonBonds):
                     relative, local = trace[k][-1]
                     done[k] = SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
                 break
+            self._set_active(active)
             # Each active request's block of the right-hand side is normalised to
             # unit norm (frozen requests: zero), so that the shared Krylov
             # tolerance weighs every request's own relative linear residual
@@ -532,6 +551,7 @@ class Batch(MixedNewtonBonds):
                 self._call('dpf_segment_axpy', self.n_sites, self.seg_site.data_ptr(), fdev.data_ptr(),
                            y.data_ptr(), correction.data_ptr(), candidate.data_ptr(), stream)
                 cscaled = torch.empty_like(y)
+                self._set_active(pending)
                 self._residual_segmented(candidate, dt, want_tangent=False, use_p=True, scaled=cscaled)
                 self._segment(cscaled)
                 values, _, status = self._fetch_segments(status=True)
@@ -552,6 +572,7 @@ class Batch(MixedNewtonBonds):
                     break
             for k in pending:
                 done[k] = SubdivideError('Subdivide: Newton line search failed')
+        self._active_mask = None
         # commit the converged requests; failed ones keep their state
         failed = [k for k in range(R) if isinstance(done[k], Exception)]
         if failed:

@@ -318,11 +318,14 @@ int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const
 
 /* J d, the forward-mode derivative of the float32 residual increment; the
  * same options as dpf_jacobian_vector (units, float32 preconditioner).
+ * seg_bond/active (optional, for batches): a bond b with active[seg_bond[b]]
+ * == 0 contributes nothing (the rows of its request's sites are not read).
  * Replaces NewtonBonds.jacobian_vector (experiments/bonded_dem_newton.py:88-92). */
 int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float *y32,
                               const double *direction, const float *mass32, const uint8_t *fixed,
                               double dt, const float *units32, const float *preconditioner,
-                              double *out, float *d32, float *wrench, void *stream);
+                              double *out, float *d32, float *wrench, const int32_t *seg_bond,
+                              const uint8_t *active, void *stream);
 
 /* K q in float32 from the stored tangent; q float32 (N, 6), out float64 (N, 6).
  * Replaces LinearBondsGPU.stiffness (experiments/bonded_dem_linear_gpu.py:42-52). */
@@ -335,13 +338,14 @@ int dpf_to_float(int64_t count, const double *a, float *out, void *stream);
 /* Elastic PCG in float32 with float64 dot products (same stopping rule and
  * iteration accounting as dpf_elastic_precondition); workspace:
  * dpf_mixed_workspace_floats(N, M) floats (the wrench argument is unused);
- * block/preconditioner float32.
+ * block/preconditioner float32; seg_bond/active as dpf_mixed_jacobian_vector.
  * Replaces NewtonBonds.elastic_precondition (experiments/bonded_dem_newton.py:107-130). */
 int dpf_mixed_precondition(const dpf_graph *g, float *bond_data, const float *mass32,
                            const uint8_t *fixed, const float *block, const float *preconditioner,
                            const float *units32, const double *vector, double dt, double tolerance,
                            int max_iterations, double *out, int *iterations, float *wrench,
-                           float *workspace, unsigned *barrier, int *status, void *stream);
+                           float *workspace, unsigned *barrier, int *status, const int32_t *seg_bond,
+                           const uint8_t *active, void *stream);
 
 /* End state of the accepted increment y: float32 increments added to the
  * float64 committed history (end normal recomputed in float64 from x + y).
@@ -370,13 +374,16 @@ int dpf_mixed_begin(int64_t n_sites, const double *loads, const double *mass, co
  * (experiments/bonded_dem_newton.py:132-201) inside the batch. */
 
 /* dpf_mixed_residual with guard bits per request: status[seg_site[s]] and
- * status[seg_bond[b]] (status is an array of request ints). */
+ * status[seg_bond[b]] (status is an array of request ints); with active,
+ * bonds of requests whose flag is 0 are skipped (no tangent, no guard bits,
+ * zero wrench), so those requests' residual rows are not meaningful. */
 int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const double *y,
                                  const float *y32, const double *mass, const uint8_t *fixed, double dt,
                                  const double *r0, int want_tangent, const float *preconditioner,
                                  const float *units32, double *residual, double *scaled,
                                  double *norms, float *wrench, double *partials, int *status,
-                                 const int32_t *seg_bond, const int32_t *seg_site, void *stream);
+                                 const int32_t *seg_bond, const int32_t *seg_site, const uint8_t *active,
+                                 void *stream);
 
 /* Per-request [|a|_2, max|a|, |b|_2] (or [.., .., a.b] with b_dot) over the
  * 6-vectors of sites seg_ptr[r] .. seg_ptr[r+1]-1, skipping sites with mask
