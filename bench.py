@@ -33,10 +33,10 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture on
-# the 64^3 bench foam, profiles/tiled_pcg_hvp_64cube.txt): a tiled PCG launch of
-# exactly 20 iterations moved 5,359,088,640 B; a tiled HVP launch 174,099,456 B.
-PCG_DRAM_BYTES_PER_ITERATION_64 = 5359088640/20
-HVP_DRAM_BYTES_PER_LAUNCH_64 = 174099456
+# the 64^3 bench foam, profiles/end_pcg_hvp_64cube.txt): a bond-end PCG launch
+# of exactly 20 iterations, and one bond-end HVP launch.
+PCG_DRAM_BYTES_PER_ITERATION_64 = (4027809536 + 134359296)/20
+HVP_DRAM_BYTES_PER_LAUNCH_64 = 199288576 + 3624960
 
 METRIC = 'implicit Newton solves/s at rel. residual 1e-6 (64^3 jittered foam, 262k sites, ~1.95M bonds)'
 UNIT = 'solves/s'
@@ -59,9 +59,9 @@ def parse():
     p.add_argument('--precision', default='mixed', choices=('mixed', 'f64'))
     p.add_argument('--plain-steps', type=int, default=3,
                    help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
-    p.add_argument('--hvp-launches', type=int, default=50, help='timed launches of the standalone tiled HVP (0: skip)')
+    p.add_argument('--hvp-launches', type=int, default=50, help='timed launches of the standalone HVP (0: skip)')
     p.add_argument('--profile-pcg', type=int, default=0,
-                   help='run one tiled PCG launch of exactly this many iterations in an NVTX range "profile_pcg" '
+                   help='run one elastic PCG launch of exactly this many iterations in an NVTX range "profile_pcg" '
                         '(for an ncu capture of its DRAM traffic)')
     p.add_argument('--adjoint-lattice', type=int, default=32, help='lattice size of the inverse-fit workload (0: skip)')
     p.add_argument('--adjoint-steps', type=int, default=50)
@@ -160,14 +160,15 @@ class ClockSampler:
 
 
 def run_hvp(s, dt, peak, peaks, launches=50):
-    """Bond-HVPs/s of the tiled float32 operator y = (diag M + dt^2/4 K) q on the
-    bench foam: each launch timed alone with CUDA events on the launching
-    stream, L2 flushed (a 256 MB write) between launches."""
+    """Bond-HVPs/s of the float32 operator y = (diag M + dt^2/4 K) q of the
+    elastic PCG (the bond-end sweep) on the bench foam: each launch timed
+    alone with CUDA events on the launching stream, L2 flushed (a 256 MB
+    write) between launches; also back to back (the end records, 188 MB, are
+    larger than L2)."""
     import ctypes
     import torch
     from dpf_gb300 import _lib
-    tiles = s._tiles
-    s._pack_tiles(tiles, dt)
+    s._pack_ends(dt)
     stream = torch.cuda.current_stream()
     n, m = s.n_sites, s.n_bonds
     q = torch.randn((n, 6), dtype=torch.float32, device=s.device)
@@ -175,9 +176,8 @@ def run_hvp(s, dt, peak, peaks, launches=50):
     flush = torch.empty(64 << 20, dtype=torch.float32, device=s.device)
 
     def launch():
-        _lib.call('dpf_tiled_hvp', ctypes.byref(s._graph), ctypes.byref(tiles.struct), tiles.entries.data_ptr(),
-                  s._site4.data_ptr(), q.data_ptr(), y.data_ptr(), tiles.status.data_ptr(),
-                  tiles.threads, tiles.stages, stream.cuda_stream)
+        _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q.data_ptr(),
+                  y.data_ptr(), stream.cuda_stream)
     for _ in range(3):
         launch()
     times = []
@@ -188,20 +188,25 @@ def run_hvp(s, dt, peak, peaks, launches=50):
         launch()
         end.record(stream)
         times.append((start, end))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for _ in range(launches):
+        launch()
+    end.record(stream)
     torch.cuda.synchronize()
     ms = [a.elapsed_time(b) for a, b in times]
     mean = sum(ms)/len(ms)
+    back_to_back = start.elapsed_time(end)/launches
     # algorithmic bytes of one float32 HVP: per bond i,j 8 + n, ri, rj 36 + k 16 = 60 B;
     # per site q 24 + y 24 + (m, I) 8 = 56 B
     alg = 60*m + 56*n
     achieved = alg/(mean*1e-3)/1e9
-    return dict(kernel='tiled_hvp_kernel', bond_hvps_per_s=m/(mean*1e-3), mean_ms=mean, min_ms=min(ms),
+    return dict(kernel='end_hvp_kernel', bond_hvps_per_s=m/(mean*1e-3), mean_ms=mean, min_ms=min(ms),
                 launches=len(ms), algorithmic_bytes=alg, traffic=HVP_DRAM_BYTES_PER_LAUNCH_64 if n == 262144 else None,
                 achieved=achieved, peak=peak, unit='GB/s',
                 frac=achieved/peak, peak_source='measured' if peaks else 'fallback', l2='flushed between launches',
-                tile=dict(max_entries=int(tiles.host['max_entries']), threads=tiles.threads, stages=tiles.stages,
-                          tiles=int(tiles.host['n_tiles']), entries_per_bond=tiles.n_entries/max(1, m)),
-                autotune_ms={'x'.join(map(str, k)): v for k, v in (s.tile_timings or {}).items()})
+                back_to_back_ms=back_to_back, back_to_back_frac=alg/(back_to_back*1e-3)/1e9/peak,
+                end_records_bytes=int(s._ends.numel())*4)
 
 
 def run_adjoint(args, device):
@@ -486,7 +491,8 @@ def run_ours(args):
     if dominant:
         achieved = alg[dominant]/(kernels[dominant]['mean_ms']*1e-3)/1e9
         traffic = None
-        if dominant == 'pcg' and args.precision == 'mixed' and args.lattice == 64 and args.seed == 0:
+        if dominant == 'pcg' and args.precision == 'mixed' and args.lattice == 64 and args.seed == 0 and \
+                PCG_DRAM_BYTES_PER_ITERATION_64:
             traffic = PCG_DRAM_BYTES_PER_ITERATION_64*cg/pcg_launches
         roof = dict(bound='hbm', kernel=dominant, achieved=achieved, peak=peak, unit='GB/s', frac=achieved/peak,
                     traffic=traffic, algorithmic_bytes=alg[dominant],
@@ -495,15 +501,15 @@ def run_ours(args):
                     launches=kernels[dominant]['launches'], mean_ms=kernels[dominant]['mean_ms'])
 
     hvp = run_hvp(s, args.dt, peak, peaks, launches=args.hvp_launches) \
-        if args.precision == 'mixed' and args.hvp_launches > 0 and getattr(s, '_tiles', None) is not None else None
-    if args.profile_pcg > 0 and getattr(s, '_tiles', None) is not None:
-        s._pack_tiles(s._tiles, args.dt)
+        if args.precision == 'mixed' and args.hvp_launches > 0 and s.sweep == 'ends' else None
+    if args.profile_pcg > 0 and args.precision == 'mixed' and s.sweep == 'ends':
+        s._pack_ends(args.dt)
         vec = torch.randn((n_sites, 6), dtype=torch.float64, device=device)
         out = torch.empty_like(vec)
         its = torch.zeros(1, dtype=torch.int32, device=device)
         torch.cuda.synchronize()
         torch.cuda.nvtx.range_push('profile_pcg')
-        s._tiled_pcg(s._tiles, vec, out, 0.0, args.profile_pcg, its)
+        s._end_pcg(vec, out, 0.0, args.profile_pcg, its)
         torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
     served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None

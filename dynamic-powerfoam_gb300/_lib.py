@@ -115,6 +115,10 @@ SIGNATURES = {
     'dpf_tile_pack': (i32, [P(Tiles), vp, i64, f64, vp, vp, vp, i64, vp, vp, vp, vp]),
     'dpf_tiled_hvp': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, i32, i32, vp]),
     'dpf_tiled_workspace_floats': (i64, [i64]),
+    'dpf_end_floats': (i64, [i64]),
+    'dpf_end_pack': (i32, [P(Graph), vp, f64, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_end_hvp': (i32, [P(Graph), vp, vp, vp, vp, vp]),
+    'dpf_end_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_tiled_partials_doubles': (i64, []),
     'dpf_tiled_precondition': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp,
                                      i32, i32, vp]),
@@ -144,7 +148,8 @@ KERNELS = {
     'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 1,
     'dpf_segment_axpy': 1, 'dpf_segment_select': 1,
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
-    'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
+    'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_end_pack': 2, 'dpf_end_hvp': 1,
+    'dpf_end_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
 }
 LAUNCHES = {'count': 0}
 

@@ -7,14 +7,16 @@
 // a Morton curve, so a range is a compact patch) plus every bond touching it
 // ("entries"; a bond between two tiles is an entry of both) and the outside
 // endpoints of those bonds ("halo").  Persistent CTAs walk their tiles with
-// two shared-memory buffers: while one tile computes, the next tile's entry
-// records and incidence metadata arrive by TMA bulk copies (completing on an
-// mbarrier) and its site vectors by cp.async.  Per tile:
-//   1. each thread reads its entries' records to registers;
-//   2. computes the entry wrenches [F_i, T_i, T_j] into the records' space;
-//   3. sums each site's wrench contributions over its incidence list in the
-//      list's order (no atomics: deterministic) and hands the sum to the
-//      caller's epilogue (y of the HVP, w and (w, u) of the PCG).
+// a ring of three or four shared-memory buffers: while one tile computes, the
+// entry records and incidence metadata of the tiles after it arrive by TMA
+// bulk copies (completing on an mbarrier) and the next tile's site vectors by
+// cp.async.  Per tile:
+//   1. each thread computes its entries' wrenches [F_i, T_i, T_j] and writes
+//      them over the same entries' records;
+//   2. after one block barrier, each site sums its wrench contributions over
+//      its incidence list in the list's order (no atomics: deterministic) and
+//      hands the sum to the caller's epilogue (y of the HVP, w and (w, u) of
+//      the PCG).
 // Only bonds cut by tile boundaries are read twice; wrenches never go to
 // global memory.
 #include <algorithm>
@@ -33,10 +35,10 @@ namespace tiles {
 constexpr int kLanes = DPF_TILE_LANES;  // lanes per site in the site sums
 constexpr int kPer = 2;                 // entries per thread and tile (read to registers before W overwrites them)
 #ifndef DPF_TILE_THREADS_MAX
-#define DPF_TILE_THREADS_MAX 384
+#define DPF_TILE_THREADS_MAX 192  // consumer threads; the tiled kernels add a bulk and a halo warp
 #endif
 #ifndef DPF_TILE_MIN_BLOCKS
-#define DPF_TILE_MIN_BLOCKS 2
+#define DPF_TILE_MIN_BLOCKS 3
 #endif
 constexpr int kTileThreadsMax = DPF_TILE_THREADS_MAX;
 constexpr unsigned long long kWaitNs = 1000000000ull;  // mbarrier waits give up after 1 s
@@ -52,7 +54,7 @@ struct TileGraph {
 // Byte offsets inside one of the shared-memory tile buffers.
 struct Layout {
     uint32_t plane;   // bytes of one record plane (16 * max entries)
-    uint32_t qown, qhalo, site, meta, size;
+    uint32_t qown, qhalo, site, meta, head, size;  // head: the tile's descriptor (two int4)
     int stages;       // tile buffers in the ring
 };
 
@@ -110,10 +112,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *s
 
 // ---- one entry -------------------------------------------------------------------
 
-// alpha K q wrench of one entry as three float4: (F, Ti.x), (Ti.y, Ti.z, Tj.x,
-// Tj.y), (Tj.z, -, -, -) with F = F_i (site i adds F_i, T_i; site j adds -F_i, T_j).
+// alpha K q wrench of one entry, written over the entry's own records (slot e
+// of the three record planes, so no other thread's records are touched):
+// W0 = (F, Ti.x), W1 = (Ti.y, Ti.z, Tj.x, Tj.y), W2.x = Tj.z with F = F_i
+// (site i adds F_i, T_i; site j adds -F_i, T_j).
 __device__ __forceinline__ void entry_wrench(float4 a, float4 b, float4 c, const float *qown, const float *qhalo,
-                                             int T, float4 *W) {
+                                             int T, float4 *W0, float4 *W1, float *W2) {
     const uint32_t ends = __float_as_uint(c.w);
     const int li = (int)(ends & 0xffffu), lj = (int)(ends >> 16);
     const float2 *qi = reinterpret_cast<const float2 *>(li < T ? qown + 6 * li : qhalo + 6 * (li - T));
@@ -137,9 +141,9 @@ __device__ __forceinline__ void entry_wrench(float4 a, float4 b, float4 c, const
     const float tiz = -(rix * fy - riy * fx) - mz;
     const float tjx = (rjy * fz - rjz * fy) + mx, tjy = (rjz * fx - rjx * fz) + my;
     const float tjz = (rjx * fy - rjy * fx) + mz;
-    W[0] = make_float4(-fx, -fy, -fz, tix);
-    W[1] = make_float4(tiy, tiz, tjx, tjy);
-    W[2] = make_float4(tjz, 0.0f, 0.0f, 0.0f);
+    *W0 = make_float4(-fx, -fy, -fz, tix);
+    *W1 = make_float4(tiy, tiz, tjx, tjy);
+    *W2 = tjz;
 }
 
 struct TileView {
@@ -147,8 +151,7 @@ struct TileView {
     int T, E, H, words, halo_word;  // halo_word: first halo-site word in the metadata
 };
 
-__device__ __forceinline__ TileView tile_view(const TileGraph &G, int t) {
-    const int4 d0 = __ldg(G.desc + 2 * t), d1 = __ldg(G.desc + 2 * t + 1);
+__device__ __forceinline__ TileView view_of(int4 d0, int4 d1) {
     TileView v;
     v.a = d0.x;
     v.T = d0.y;
@@ -180,9 +183,14 @@ __device__ __forceinline__ OwnRange own_range(const TileView &v) {
     return r;
 }
 
-// Thread 0: bulk copies of a tile's entry records, metadata and own-site q interior.
-__device__ __forceinline__ void issue_bulk(const TileGraph &G, const Layout &L, const TileView &v, const float *q,
+// Bulk warp, lane 0: the tile's descriptor into the buffer header, then bulk copies of
+// the tile's entry records, metadata, site records and own-site q interior.
+__device__ __forceinline__ void issue_bulk(const TileGraph &G, const Layout &L, int4 d0, int4 d1, const float *q,
                                            unsigned char *buf, uint64_t *bar) {
+    const TileView v = view_of(d0, d1);
+    int4 *head = reinterpret_cast<int4 *>(buf + L.head);  // read by the consumers after the bulk barrier
+    head[0] = d0;
+    head[1] = d1;
     fence_proxy_async();
     const uint32_t plane = 16u * (uint32_t)v.E, meta = 4u * (uint32_t)v.words;
     const OwnRange o = own_range(v);
@@ -200,42 +208,68 @@ __device__ __forceinline__ void issue_bulk(const TileGraph &G, const Layout &L, 
                   reinterpret_cast<const unsigned char *>(q) + o.lo, own, bar);
 }
 
-// All threads, once the tile's bulk copies have landed: cp.async of the
-// own-site q ends outside the bulk interior and of the halo sites' q (halo
-// site list at the end of the tile's metadata).
-__device__ __forceinline__ void issue_q(const TileView &v, const Layout &L, unsigned char *buf, const float *q) {
+// Halo sites of a tile held in registers by the halo warp: slot lane + 32 k.
+constexpr int kHaloRegs = 8;
+
+__device__ __forceinline__ void load_halo(const TileView &v, const uint32_t *meta, int lane, int h[kHaloRegs]) {
+    const int32_t *src = reinterpret_cast<const int32_t *>(meta) + v.meta + v.halo_word;
+#pragma unroll
+    for (int k = 0; k < kHaloRegs; ++k) {
+        const int slot = lane + 32 * k;
+        h[k] = slot < v.H ? __ldg(src + slot) : 0;
+    }
+}
+
+// The halo warp, once the buffer is free: cp.async of the own-site q ends
+// outside the bulk interior and of the halo sites' q (the first 32 kHaloRegs
+// halo sites from registers, loaded a tile ahead; any further ones read from
+// the tile's metadata in global memory), then each lane's asynchronous
+// arrival on `bar` (it fires when that lane's copies have landed).
+__device__ __forceinline__ void issue_q(const TileView &v, const Layout &L, const uint32_t *meta, const int h[kHaloRegs],
+                                        unsigned char *buf, const float *q, int lane, uint64_t *bar) {
     const OwnRange o = own_range(v);
     const unsigned char *qb = reinterpret_cast<const unsigned char *>(q);
     unsigned char *own = buf + L.qown + o.shift;
     const int head = (int)((o.lo - o.begin) >> 3), tail = (int)((o.end - o.hi) >> 3);
-    for (int k = threadIdx.x; k < head + tail; k += blockDim.x) {
+    for (int k = lane; k < head + tail; k += 32) {
         const uint64_t off = k < head ? 8ull * k : (o.hi - o.begin) + 8ull * (k - head);
         cp_async8(own + off, qb + o.begin + off);
     }
-    const int32_t *meta = reinterpret_cast<const int32_t *>(buf + L.meta);
-    const int32_t *halo = meta + v.halo_word;
     float2 *hal = reinterpret_cast<float2 *>(buf + L.qhalo);
-    for (int k = threadIdx.x; k < 3 * v.H; k += blockDim.x) {
-        const int slot = k / 3, part = k - 3 * slot;
-        cp_async8(hal + k, reinterpret_cast<const float2 *>(q + 6 * (int64_t)halo[slot]) + part);
+#pragma unroll
+    for (int k = 0; k < kHaloRegs; ++k) {
+        const int slot = lane + 32 * k;
+        if (slot < v.H) {
+            const float2 *src = reinterpret_cast<const float2 *>(q + 6 * (int64_t)h[k]);
+            cp_async8(hal + 3 * slot, src);
+            cp_async8(hal + 3 * slot + 1, src + 1);
+            cp_async8(hal + 3 * slot + 2, src + 2);
+        }
     }
-    cp_async_commit();
+    const int32_t *list = reinterpret_cast<const int32_t *>(meta) + v.meta + v.halo_word;
+    for (int slot = lane + 32 * kHaloRegs; slot < v.H; slot += 32) {
+        const float2 *src = reinterpret_cast<const float2 *>(q + 6 * (int64_t)__ldg(list + slot));
+        cp_async8(hal + 3 * slot, src);
+        cp_async8(hal + 3 * slot + 1, src + 1);
+        cp_async8(hal + 3 * slot + 2, src + 2);
+    }
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(saddr(bar)) : "memory");
 }
 
-// The alpha K q part of local site sl from the tile's wrenches (all kLanes
-// lanes of a group call it together).  span[sl] = start | mid << 16: the
-// site's incidences [start, mid) are i ends, [mid, next start) j ends, in
+// The alpha K q part of local site sl from the tile's wrench planes (all
+// kLanes lanes of a group call it together).  span[sl] = start | mid << 16:
+// the site's incidences [start, mid) are i ends, [mid, next start) j ends, in
 // incidence order with a fixed lane split.
-__device__ __forceinline__ void site_sum(const float4 *W, const uint32_t *span, const uint16_t *codes, int sl,
-                                         bool valid, int lane, float acc[6]) {
+__device__ __forceinline__ void site_sum(const float4 *W0, const float4 *W1, const float4 *W2, const uint32_t *span,
+                                         const uint16_t *codes, int sl, bool valid, int lane, float acc[6]) {
 #pragma unroll
     for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
     if (valid) {
         const uint32_t sp = span[sl];
         const int k0 = (int)(sp & 0xffffu), mid = (int)(sp >> 16), k1 = (int)(span[sl + 1] & 0xffffu);
         for (int k = k0 + lane; k < mid; k += kLanes) {
-            const float4 *w = W + 3 * codes[k];
-            const float4 w0 = w[0], w1 = w[1];
+            const int e = codes[k];
+            const float4 w0 = W0[e], w1 = W1[e];
             acc[0] += w0.x;
             acc[1] += w0.y;
             acc[2] += w0.z;
@@ -244,9 +278,9 @@ __device__ __forceinline__ void site_sum(const float4 *W, const uint32_t *span, 
             acc[5] += w1.y;
         }
         for (int k = mid + lane; k < k1; k += kLanes) {
-            const float4 *w = W + 3 * codes[k];
-            const float4 w0 = w[0], w1 = w[1];
-            const float w2 = w[2].x;
+            const int e = codes[k];
+            const float4 w0 = W0[e], w1 = W1[e];
+            const float w2 = reinterpret_cast<const float *>(W2 + e)[0];
             acc[0] -= w0.x;
             acc[1] -= w0.y;
             acc[2] -= w0.z;
@@ -261,111 +295,180 @@ __device__ __forceinline__ void site_sum(const float4 *W, const uint32_t *span, 
         for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
 }
 
-// Ring of L.stages shared-memory tile buffers, one mbarrier each.
+// Ring of L.stages shared-memory tile buffers.  Per buffer three mbarriers:
+// bulk (the tile's bulk copies: one arrival with the byte count), halo (the
+// 32 lanes of the halo warp, each when its q copies have landed) and empty
+// (one arrival per consumer warp when it is done with the buffer).
 struct Pipe {
     unsigned char *base;
-    uint64_t *bar;
-    uint32_t parity;  // bit b: phase parity of buffer b's next completion
+    uint64_t *bulk, *halo, *empty;
+    uint32_t parity;  // this thread's next phase parity: bit b bulk, 8 + b halo, 16 + b empty
 };
 
-__device__ __forceinline__ Pipe pipe_init(unsigned char *smem, const Layout &L) {
+__device__ __forceinline__ Pipe pipe_init(unsigned char *smem, const Layout &L, int consumer_warps) {
     Pipe P;
     P.base = smem;
-    P.bar = reinterpret_cast<uint64_t *>(smem + (size_t)L.stages * L.size);
+    P.bulk = reinterpret_cast<uint64_t *>(smem + (size_t)L.stages * L.size);
+    P.halo = P.bulk + L.stages;
+    P.empty = P.halo + L.stages;
     P.parity = 0u;
     if (threadIdx.x == 0) {
-        for (int b = 0; b < L.stages; ++b) mbar_init(P.bar + b, 1);
+        for (int b = 0; b < L.stages; ++b) {
+            mbar_init(P.bulk + b, 1);
+            mbar_init(P.halo + b, 32);
+            mbar_init(P.empty + b, (uint32_t)consumer_warps);
+        }
         mbar_init_fence();
     }
     __syncthreads();
     return P;
 }
 
-// Wait (all threads) for buffer b's bulk copies; false after the time limit.
-__device__ __forceinline__ bool wait_bulk(Pipe &P, int b, int *status) {
-    const bool ok = mbar_wait(P.bar + b, (P.parity >> b) & 1u, status);
-    P.parity ^= 1u << b;
-    return !__syncthreads_or(!ok);
+// This thread's wait for the next phase of barrier `bar` (parity bit `bit`);
+// false after the time limit.
+__device__ __forceinline__ bool pipe_wait(Pipe &P, uint64_t *bar, int bit, int *status) {
+    const bool ok = mbar_wait(bar, (P.parity >> bit) & 1u, status);
+    P.parity ^= 1u << bit;
+    return ok;
 }
 
-// For each own site s of every tile of this block: epi(s, q_s (shared), acc)
-// with acc the alpha K q sum.  Tile j of the block uses buffer j mod S: the
-// bulk copies of tile j + S - 1 are issued while tile j computes, and the
-// q gather of tile j + 1 (whose metadata has landed) overlaps it too.
-// False on a wait timeout.
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(saddr(bar)) : "memory");
+}
+
+// OR of `pred` over the `count` consumer threads (named barrier 1).
+__device__ __forceinline__ bool consumers_or(bool pred, int count) {
+    uint32_t out;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 1, %2, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(out)
+        : "r"((uint32_t)pred), "r"(count)
+        : "memory");
+    return out != 0;
+}
+
+// For each own site s of every tile of this block: epi(s, q_s (shared), site
+// record, acc) with acc the alpha K q sum.  Warp roles (blockDim = consumer
+// threads + 64):
+//   * bulk warp (lane 0): for tile j in buffer j mod S, once the consumers
+//     have released the buffer's previous tile, the tile's bulk copies;
+//   * halo warp: once the buffer is free, the q gather of the tile's halo
+//     sites (list read from global memory) and own-site ends, arriving on
+//     halo[b];
+// (both producer warps read the descriptors of 32 tiles at a time, one per
+// lane; the consumers read the tile's descriptor from the buffer header).
+//   * consumer warps: wait for bulk[b] and halo[b], compute the entry
+//     wrenches in place, one named barrier among consumers, the site sums and
+//     the epilogue, then release the buffer (empty[b]).
+// So up to S - 1 tiles stream in while one computes.  False (for the whole
+// block) on a wait timeout.
 template <class Epi>
 __device__ __forceinline__ bool for_tiles(const TileGraph &G, const Layout &L, Pipe &P, const float *q, int *status,
                                           Epi &epi) {
-    if ((int)blockIdx.x >= G.n_tiles) return true;
-    const int S = L.stages;
-    const int n_local = (G.n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
-    auto tile_of = [&](int j) { return (int)blockIdx.x + j * (int)gridDim.x; };
-    auto buf_of = [&](int b) { return P.base + (size_t)b * L.size; };
-    if (threadIdx.x == 0)
-        for (int j = 0; j < S - 1 && j < n_local; ++j)
-            issue_bulk(G, L, tile_view(G, tile_of(j)), q, buf_of(j), P.bar + j);
-    if (!wait_bulk(P, 0, status)) return false;
-    issue_q(tile_view(G, tile_of(0)), L, buf_of(0), q);
-    const int lane = threadIdx.x & (kLanes - 1);
-    const int groups = blockDim.x / kLanes;
-    int b = 0;
-    TileView v = tile_view(G, tile_of(0));
-    for (int j = 0; j < n_local; ++j) {
-        const int bn = b + 1 == S ? 0 : b + 1;
-        if (threadIdx.x == 0 && j + S - 1 < n_local) {
-            const int bf = b == 0 ? S - 1 : b - 1;  // buffer of tile j - 1, free
-            issue_bulk(G, L, tile_view(G, tile_of(j + S - 1)), q, buf_of(bf), P.bar + bf);
-        }
-        TileView vn = v;
-        if (j + 1 < n_local) {
-            vn = tile_view(G, tile_of(j + 1));
-            if (!wait_bulk(P, bn, status)) return false;
-            issue_q(vn, L, buf_of(bn), q);
-            asm volatile("cp.async.wait_group 1;" ::: "memory");
-        } else {
-            cp_async_wait_all();
-        }
-        __syncthreads();
-        unsigned char *buf = buf_of(b);
-        const float4 *p0 = reinterpret_cast<const float4 *>(buf);
-        const float4 *p1 = reinterpret_cast<const float4 *>(buf + L.plane);
-        const float4 *p2 = reinterpret_cast<const float4 *>(buf + 2 * L.plane);
-        float4 ra[kPer], rb[kPer], rc[kPer];
+    bool ok = true;
+    if ((int)blockIdx.x < G.n_tiles) {
+        const int S = L.stages;
+        const int n_local = (G.n_tiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
+        const int consumers = (int)blockDim.x - 64, warp = (int)threadIdx.x >> 5, lane32 = (int)threadIdx.x & 31;
+        auto tile_of = [&](int j) { return (int)blockIdx.x + j * (int)gridDim.x; };
+        auto buf_of = [&](int b) { return P.base + (size_t)b * L.size; };
+        // the descriptors of tiles j .. j + 31 of this block, one per lane
+        auto fetch = [&](int j, int4 &d0, int4 &d1) {
+            const int t = j + lane32 < n_local ? tile_of(j + lane32) : tile_of(j);
+            d0 = __ldg(G.desc + 2 * t);
+            d1 = __ldg(G.desc + 2 * t + 1);
+        };
+        auto pick = [&](const int4 &d, int src) {
+            return make_int4(__shfl_sync(0xffffffffu, d.x, src), __shfl_sync(0xffffffffu, d.y, src),
+                             __shfl_sync(0xffffffffu, d.z, src), __shfl_sync(0xffffffffu, d.w, src));
+        };
+        if (warp == consumers / 32) {  // bulk warp
+            int4 d0, d1;
+            for (int j = 0; j < n_local && ok; ++j) {
+                if ((j & 31) == 0) fetch(j, d0, d1);
+                const int4 t0 = pick(d0, j & 31), t1 = pick(d1, j & 31);
+                const int b = j % S;
+                if (lane32 == 0) {
+                    if (j >= S) ok = pipe_wait(P, P.empty + b, 16 + b, status);
+                    if (ok) issue_bulk(G, L, t0, t1, q, buf_of(b), P.bulk + b);
+                }
+                ok = __shfl_sync(0xffffffffu, ok, 0);
+            }
+            // the consumers' release of the last tiles (keeps the phases in step)
+            if (lane32 == 0)
+                for (int j = n_local > S ? n_local - S : 0; j < n_local && ok; ++j)
+                    ok = pipe_wait(P, P.empty + j % S, 16 + j % S, status);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+        } else if (warp == consumers / 32 + 1) {  // halo warp
+            int4 d0, d1;
+            int h[kHaloRegs], hn[kHaloRegs];
+            fetch(0, d0, d1);
+            TileView vn = view_of(pick(d0, 0), pick(d1, 0));
+            load_halo(vn, G.tile_meta, lane32, hn);
+            for (int j = 0; j < n_local && ok; ++j) {
+                const TileView v = vn;
 #pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int e = threadIdx.x + u * blockDim.x;
-            if (e < v.E) {
-                ra[u] = p0[e];
-                rb[u] = p1[e];
-                rc[u] = p2[e];
+                for (int k = 0; k < kHaloRegs; ++k) h[k] = hn[k];
+                if (j + 1 < n_local) {  // the next tile's halo list, loaded while this one waits
+                    if (((j + 1) & 31) == 0) fetch(j + 1, d0, d1);
+                    vn = view_of(pick(d0, (j + 1) & 31), pick(d1, (j + 1) & 31));
+                    load_halo(vn, G.tile_meta, lane32, hn);
+                }
+                const int b = j % S;
+                if (j >= S) ok = __all_sync(0xffffffffu, pipe_wait(P, P.empty + b, 16 + b, status));
+                if (ok) issue_q(v, L, G.tile_meta, h, buf_of(b), q, lane32, P.halo + b);
+            }
+            for (int j = n_local > S ? n_local - S : 0; j < n_local && ok; ++j)
+                ok = __all_sync(0xffffffffu, pipe_wait(P, P.empty + j % S, 16 + j % S, status));
+            cp_async_wait_all();
+        } else {  // consumer warps
+            const int lane = threadIdx.x & (kLanes - 1);
+            const int groups = consumers / kLanes;
+            for (int j = 0; j < n_local; ++j) {
+                const int b = j % S;
+                bool here = pipe_wait(P, P.bulk + b, b, status);
+                here = pipe_wait(P, P.halo + b, 8 + b, status) && here;
+                unsigned char *buf = buf_of(b);
+                const int4 *head = reinterpret_cast<const int4 *>(buf + L.head);
+                const TileView v = view_of(head[0], head[1]);
+                float4 *p0 = reinterpret_cast<float4 *>(buf);
+                float4 *p1 = reinterpret_cast<float4 *>(buf + L.plane);
+                float4 *p2 = reinterpret_cast<float4 *>(buf + 2 * L.plane);
+                const float *qown = reinterpret_cast<const float *>(buf + L.qown + own_range(v).shift);
+                const float *qhalo = reinterpret_cast<const float *>(buf + L.qhalo);
+                if (here) {
+#pragma unroll
+                    for (int u = 0; u < kPer; ++u) {
+                        const int e = threadIdx.x + u * consumers;
+                        if (e < v.E)
+                            entry_wrench(p0[e], p1[e], p2[e], qown, qhalo, v.T, p0 + e, p1 + e,
+                                         reinterpret_cast<float *>(p2 + e));
+                    }
+                }
+                if (consumers_or(!here, consumers)) {  // the wrenches of tile j are written
+                    ok = false;
+                    break;
+                }
+                const uint32_t *span = reinterpret_cast<const uint32_t *>(buf + L.meta);
+                const uint16_t *codes = reinterpret_cast<const uint16_t *>(span + v.T + 1);
+                const int rounds = (v.T + groups - 1) / groups;
+                for (int rd = 0; rd < rounds; ++rd) {
+                    const int sl = rd * groups + (int)threadIdx.x / kLanes;
+                    const bool valid = sl < v.T;
+                    float acc[6];
+                    site_sum(p0, p1, p2, span, codes, sl, valid, lane, acc);
+                    if (valid && lane == 0)
+                        epi(v.a + sl, qown + 6 * sl, reinterpret_cast<const float4 *>(buf + L.site)[sl], acc);
+                }
+                __syncwarp();
+                if (lane32 == 0) mbar_arrive(P.empty + b);
             }
         }
-        __syncthreads();  // records consumed: the wrenches overwrite them
-        float4 *W = reinterpret_cast<float4 *>(buf);
-        const float *qown = reinterpret_cast<const float *>(buf + L.qown + own_range(v).shift);
-        const float *qhalo = reinterpret_cast<const float *>(buf + L.qhalo);
-#pragma unroll
-        for (int u = 0; u < kPer; ++u) {
-            const int e = threadIdx.x + u * blockDim.x;
-            if (e < v.E) entry_wrench(ra[u], rb[u], rc[u], qown, qhalo, v.T, W + 3 * e);
-        }
-        __syncthreads();
-        const uint32_t *span = reinterpret_cast<const uint32_t *>(buf + L.meta);
-        const uint16_t *codes = reinterpret_cast<const uint16_t *>(span + v.T + 1);
-        const int rounds = (v.T + groups - 1) / groups;
-        for (int rd = 0; rd < rounds; ++rd) {
-            const int sl = rd * groups + (int)threadIdx.x / kLanes;
-            const bool valid = sl < v.T;
-            float acc[6];
-            site_sum(W, span, codes, sl, valid, lane, acc);
-            if (valid && lane == 0)
-                epi(v.a + sl, qown + 6 * sl, reinterpret_cast<const float4 *>(buf + L.site)[sl], acc);
-        }
-        __syncthreads();  // buffer b free
-        b = bn;
-        v = vn;
     }
-    return true;
+    return !__syncthreads_or(!ok);
 }
 
 __device__ __forceinline__ void ld6(const float *p, float v[6]) {
@@ -405,9 +508,9 @@ struct HvpEpi {
     }
 };
 
-__global__ void __launch_bounds__(kTileThreadsMax, DPF_TILE_MIN_BLOCKS) tiled_hvp_kernel(HvpArgs a) {
+__global__ void __launch_bounds__(kTileThreadsMax + 64, DPF_TILE_MIN_BLOCKS) tiled_hvp_kernel(HvpArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    Pipe P = pipe_init(smem, a.L);
+    Pipe P = pipe_init(smem, a.L, ((int)blockDim.x - 64) / 32);
     HvpEpi epi{a};
     for_tiles(a.G, a.L, P, a.q, a.status, epi);
 }
@@ -482,6 +585,197 @@ __device__ __forceinline__ void sym_mv6(const float P[21], const float x[6], flo
 #undef DPF_SYM
 }
 
+// ---- bond-end sweep ------------------------------------------------------------
+//
+// The same operator over the site-sorted incidence CSR instead of tiles: one
+// end record per incidence (bond b seen from site s), in the CSR's order,
+//   (n', r_s.x) (r_s.y, r_s.z, L, a kn) (a ks, a kb, a kt, other site)
+// with n' the unit normal from s towards the other end o and r_s the lever
+// of s, so that r_o = r_s - L n' and the end's share of alpha K q is
+//   du = u_o - u_s + w_o x r_o - w_s x r_s,  dw = w_o - w_s,
+//   f = ks du + (kn - ks)(du.n') n',  m = kb dw + (kt - kb)(dw.n') n',
+//   F_s = -f,  T_s = -(r_s x f) - m
+// (for the i end this is the bond's wrench on i; for the j end n' = -n and the
+// same formula gives the wrench on j).  A group of kEndLanes lanes owns a
+// site, each lane sums the ends k = start + lane, start + lane + kEndLanes, ..
+// in registers and a fixed xor-shuffle tree adds the lanes: no shared
+// memory, no atomics, bitwise reproducible.  Records stream from HBM once per
+// sweep (evict-first); q of the other ends is gathered from L2.
+
+#ifndef DPF_END_LANES
+#define DPF_END_LANES 8
+#endif
+#ifndef DPF_END_MIN_BLOCKS
+#define DPF_END_MIN_BLOCKS 4
+#endif
+constexpr int kEndLanes = DPF_END_LANES;
+constexpr int kEndThreads = 256;
+
+struct EndGraph {
+    int64_t n;
+    const int32_t *ptr;           // incidence CSR pointers (n + 1)
+    const float4 *e0, *e1, *e2;   // end records in incidence order
+    const float4 *site;           // per site (mass, inertia, 1 free / 0 fixed, -); fixed sites (1, 1, 0, -)
+};
+
+__device__ __forceinline__ void end_wrench(float4 a, float4 b, float4 c, const float qs[6], const float qo[6],
+                                           float acc[6]) {
+    const float nx = a.x, ny = a.y, nz = a.z;
+    const float rx = a.w, ry = b.x, rz = b.y, L = b.z;
+    const float ox = rx - L * nx, oy = ry - L * ny, oz = rz - L * nz;
+    const float kn = b.w, ks = c.x, kb = c.y, kt = c.z;
+    const float wsx = qs[3], wsy = qs[4], wsz = qs[5], wox = qo[3], woy = qo[4], woz = qo[5];
+    const float dux = qo[0] - qs[0] + (woy * oz - woz * oy) - (wsy * rz - wsz * ry);
+    const float duy = qo[1] - qs[1] + (woz * ox - wox * oz) - (wsz * rx - wsx * rz);
+    const float duz = qo[2] - qs[2] + (wox * oy - woy * ox) - (wsx * ry - wsy * rx);
+    const float dwx = wox - wsx, dwy = woy - wsy, dwz = woz - wsz;
+    const float un = (kn - ks) * (dux * nx + duy * ny + duz * nz);
+    const float wn = (kt - kb) * (dwx * nx + dwy * ny + dwz * nz);
+    const float fx = ks * dux + un * nx, fy = ks * duy + un * ny, fz = ks * duz + un * nz;
+    const float mx = kb * dwx + wn * nx, my = kb * dwy + wn * ny, mz = kb * dwz + wn * nz;
+    acc[0] -= fx;
+    acc[1] -= fy;
+    acc[2] -= fz;
+    acc[3] -= (ry * fz - rz * fy) + mx;
+    acc[4] -= (rz * fx - rx * fz) + my;
+    acc[5] -= (rx * fy - ry * fx) + mz;
+}
+
+// q of a site: read-only for the whole launch (kConst) through the
+// non-coherent path, else with plain loads (a PCG updates q between sweeps).
+template <bool kConst>
+__device__ __forceinline__ void load_q(const float *q, int64_t s, float v[6]) {
+    const float2 *p = reinterpret_cast<const float2 *>(q + 6 * s);
+    float2 a, b, c;
+    if (kConst) {
+        a = __ldg(p);
+        b = __ldg(p + 1);
+        c = __ldg(p + 2);
+    } else {
+        a = p[0];
+        b = p[1];
+        c = p[2];
+    }
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
+}
+
+#ifndef DPF_END_PREFETCH
+#define DPF_END_PREFETCH 0
+#endif
+constexpr int kEndPrefetch = DPF_END_PREFETCH;  // rounds of L2 prefetch ahead of the loads (0: none)
+
+// L2 prefetch of [p, p + bytes) (fire and forget; 16-byte aligned, multiple of 16 bytes).
+__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// For every site s: epi(s, q_s, site record, acc) with acc the alpha K q sum.
+// Warp w of the grid takes the chunks w, w + W, ... of 32 / kEndLanes
+// consecutive sites (W warps in the grid); with kEndPrefetch > 0 lane 0
+// prefetches the end records of the chunk kEndPrefetch rounds ahead into L2.
+// The round count is the same for every warp, so the shuffles see full warps.
+template <bool kConst, class Epi>
+__device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi &epi) {
+    constexpr int kSites = 32 / kEndLanes;  // sites per warp and round
+    const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int lane32 = (int)threadIdx.x & 31, lane = lane32 & (kEndLanes - 1);
+    const int64_t chunks = (G.n + kSites - 1) / kSites;
+    const int64_t rounds = (chunks + warps - 1) / warps;
+    auto prefetch = [&](int64_t chunk) {
+        if (chunk >= chunks) return;
+        const int64_t s0 = chunk * kSites, s1 = s0 + kSites < G.n ? s0 + kSites : G.n;
+        const int k0 = G.ptr[s0], k1 = G.ptr[s1];
+        if (k1 > k0) {
+            const uint32_t bytes = 16u * (uint32_t)(k1 - k0);
+            prefetch_l2(G.e0 + k0, bytes);
+            prefetch_l2(G.e1 + k0, bytes);
+            prefetch_l2(G.e2 + k0, bytes);
+        }
+    };
+    if (kEndPrefetch > 0 && lane32 == 0)
+        for (int d = 0; d < kEndPrefetch; ++d) prefetch(warp + d * warps);
+    for (int64_t r = 0; r < rounds; ++r) {
+        if (kEndPrefetch > 0 && lane32 == 0) prefetch(warp + (r + kEndPrefetch) * warps);
+        const int64_t s = (warp + r * warps) * kSites + lane32 / kEndLanes;
+        const bool valid = s < G.n;
+        float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, qs[6];
+        if (valid) {
+            load_q<kConst>(q, s, qs);
+            const int k1 = G.ptr[s + 1];
+            // two ends per step: both ends' records, then both gathers, are in
+            // flight together
+            for (int k = G.ptr[s] + lane; k < k1; k += 2 * kEndLanes) {
+                const int k2 = k + kEndLanes;
+                const bool two = k2 < k1;
+                const float4 a = __ldcs(G.e0 + k), b = __ldcs(G.e1 + k), c = __ldcs(G.e2 + k);
+                float4 a2 = a, b2 = b, c2 = c;
+                if (two) {
+                    a2 = __ldcs(G.e0 + k2);
+                    b2 = __ldcs(G.e1 + k2);
+                    c2 = __ldcs(G.e2 + k2);
+                }
+                float qo[6], qo2[6];
+                load_q<kConst>(q, (int64_t)__float_as_int(c.w), qo);
+                load_q<kConst>(q, (int64_t)__float_as_int(c2.w), qo2);
+                end_wrench(a, b, c, qs, qo, acc);
+                if (two) end_wrench(a2, b2, c2, qs, qo2, acc);
+            }
+        }
+#pragma unroll
+        for (int o = 1; o < kEndLanes; o <<= 1)
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
+        if (valid && lane == 0) epi(s, qs, G.site[s], acc);
+    }
+}
+
+struct EndHvpEpi {
+    float *y;
+    __device__ __forceinline__ void operator()(int64_t s, const float *qs, float4 rec, const float acc[6]) const {
+        float out[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) out[c] = fmaf(c < 3 ? rec.x : rec.y, qs[c], rec.z * acc[c]);
+        float2 *p = reinterpret_cast<float2 *>(y + 6 * s);
+        p[0] = make_float2(out[0], out[1]);
+        p[1] = make_float2(out[2], out[3]);
+        p[2] = make_float2(out[4], out[5]);
+    }
+};
+
+__global__ void __launch_bounds__(kEndThreads, DPF_END_MIN_BLOCKS) end_hvp_kernel(EndGraph G, const float *q, float *y) {
+    EndHvpEpi epi{y};
+    for_ends<true>(G, q, epi);
+}
+
+// One thread per incidence k of site s (site-major): the end record of bond
+// v = inc_bond[k] (v >= 0: s is its i end; ~v: its j end).
+struct EndPackArgs {
+    int64_t n_inc;
+    const int32_t *inc_bond;
+    const int64_t *edges;
+    const float4 *t0, *t1, *t2, *t3;  // tangent records (n, kn), (ri, ks), (rj, kb), (kt, -, -, -)
+    float alpha;
+    float4 *e0, *e1, *e2;
+};
+
+__global__ void __launch_bounds__(kThreads) pack_ends_kernel(EndPackArgs a) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= a.n_inc) return;
+    const int v = a.inc_bond[k];
+    const bool at_i = v >= 0;
+    const int64_t b = at_i ? v : ~v;
+    const float4 n = a.t0[b], ri = a.t1[b], rj = a.t2[b], g = a.t3[b];
+    const float L = (ri.x - rj.x) * n.x + (ri.y - rj.y) * n.y + (ri.z - rj.z) * n.z;
+    const longlong2 e = reinterpret_cast<const longlong2 *>(a.edges)[b];
+    const int other = (int)(at_i ? e.y : e.x);
+    const float sg = at_i ? 1.0f : -1.0f;
+    const float4 r = at_i ? ri : rj;
+    a.e0[k] = make_float4(sg * n.x, sg * n.y, sg * n.z, r.x);
+    a.e1[k] = make_float4(r.y, r.z, L, a.alpha * n.w);
+    a.e2[k] = make_float4(a.alpha * ri.w, a.alpha * rj.w, a.alpha * g.x, __int_as_float(other));
+}
+
 // ---- tiled elastic PCG (single-reduction form: two grid barriers per iteration) ----
 //
 // Same equations and stopping rule as the reference loop: after iteration k's
@@ -492,8 +786,9 @@ __device__ __forceinline__ void sym_mv6(const float P[21], const float x[6], flo
 
 struct PcgArgs {
     int64_t n;
-    TileGraph G;
+    TileGraph G;  // tiled operator
     Layout L;
+    EndGraph E;   // bond-end operator
     const uint8_t *fixed;
     const float4 *P24;
     const float *block, *units32;
@@ -530,12 +825,14 @@ __device__ __forceinline__ void mv36(const float *B, const float x[6], float y[6
     }
 }
 
-__global__ void __launch_bounds__(kTileThreadsMax, DPF_TILE_MIN_BLOCKS) tiled_pcg_kernel(PcgArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+// kTiles: w = A u by the tiled sweep, else by the bond-end sweep.
+template <bool kTiles>
+__device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const float zero6[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-    Pipe P = pipe_init(smem, a.L);
+    Pipe P;
+    if (kTiles) P = pipe_init(smem, a.L, ((int)blockDim.x - 64) / 32);
     // r0 = B (units v) with fixed rows zero, u0 = P r0, x = p = s = 0
     float pf = 0.0f;
     for (int64_t s = tid; s < a.n; s += stride) {
@@ -572,7 +869,11 @@ __global__ void __launch_bounds__(kTileThreadsMax, DPF_TILE_MIN_BLOCKS) tiled_pc
     for (; it < a.max_it; ++it) {
         // w = A u over the tiles of this block, delta partial (w, u)
         PcgEpi epi{a, 0.0f};
-        const bool ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
+        bool ok = true;
+        if (kTiles)
+            ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
+        else
+            for_ends<false>(a.E, a.u, epi);
         part = block_sum((double)epi.dot);
         if (threadIdx.x == 0) a.part_a[blockIdx.x] = part;
         if (!ok) return;
@@ -636,6 +937,13 @@ __global__ void __launch_bounds__(kTileThreadsMax, DPF_TILE_MIN_BLOCKS) tiled_pc
     if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
 }
 
+__global__ void __launch_bounds__(kTileThreadsMax + 64, DPF_TILE_MIN_BLOCKS) tiled_pcg_kernel(PcgArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    pcg_body<true>(a, smem);
+}
+
+__global__ void __launch_bounds__(kEndThreads, DPF_END_MIN_BLOCKS) end_pcg_kernel(PcgArgs a) { pcg_body<false>(a, nullptr); }
+
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
 
 }  // namespace tiles
@@ -671,28 +979,27 @@ Layout layout_of(const dpf_tiles *t, int stages) {
     L.qhalo = L.qown + (uint32_t)round16(24 * (size_t)t->max_sites + 16);
     L.site = L.qhalo + (uint32_t)round16(24 * (size_t)(t->max_halo > 0 ? t->max_halo : 1));
     L.meta = L.site + 16u * (uint32_t)t->max_sites;
-    L.size = L.meta + 4u * (uint32_t)t->max_meta_words;
+    L.head = (uint32_t)round16(L.meta + 4u * (uint32_t)t->max_meta_words);
+    L.size = L.head + 32u;
     L.stages = stages;
     return L;
 }
 
-size_t smem_bytes(const Layout &L) { return (size_t)L.stages * L.size + 8 * (size_t)L.stages; }
+size_t smem_bytes(const Layout &L) { return (size_t)L.stages * L.size + 24 * (size_t)L.stages; }
 
-// A ring of `stages` buffers (2..4); 0 picks the deepest within the cap.
+// A ring of `stages` buffers (3..4); 0 picks the deepest within the cap.
 Layout pick_layout(const dpf_tiles *t, int stages) {
-    if (stages >= 2) return layout_of(t, stages);
-    for (stages = 4; stages > 2; --stages) {
-        const Layout L = layout_of(t, stages);
-        if (smem_bytes(L) <= kMaxTileSmem) return L;
-    }
-    return layout_of(t, 2);
+    if (stages >= 3) return layout_of(t, stages);
+    const Layout L = layout_of(t, 4);
+    return smem_bytes(L) <= kMaxTileSmem ? L : layout_of(t, 3);
 }
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
 
 // Launch checks shared by the tiled kernels; returns the dynamic shared memory.
 int tile_launch_check(const dpf_tiles *t, int threads, int stages, size_t &smem) {
-    if (threads < 64 || threads > kTileThreadsMax || threads % 32 || stages < 0 || stages == 1 || stages > 4)
+    if (threads < 64 || threads > kTileThreadsMax || threads % 32 || stages < 0 || stages == 1 || stages == 2 ||
+        stages > 4)
         return DPF_ERR_ARGUMENT;
     if (t->max_entries > kPer * threads) return DPF_ERR_TOO_LARGE;
     smem = smem_bytes(pick_layout(t, stages));
@@ -711,7 +1018,7 @@ struct GridKey {
 };
 
 template <class K>
-int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t cap, int &grid) {
+int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t cap, int &grid, bool tiled = true) {
     static GridKey keys[64];
     static int values[64];
     static int used = 0;
@@ -725,10 +1032,12 @@ int persistent_grid(K kernel, int threads, size_t smem, int64_t n_tiles, int64_t
             keys[k].smem == smem)
             per_grid = values[k];
     if (per_grid == 0) {
-        // the attribute is the cap (not this shape's size): any cached shape stays launchable
-        if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxTileSmem) !=
-                cudaSuccess ||
-            cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess) {
+        // the attribute is the cap (not this shape's size): any cached shape stays
+        // launchable; the bond-end sweep uses no shared memory and prefers L1
+        if ((tiled && cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxTileSmem) !=
+                          cudaSuccess) ||
+            cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, tiled ? 100 : 0) !=
+                cudaSuccess) {
             cudaGetLastError();
             return DPF_ERR_CUDA;
         }
@@ -938,10 +1247,10 @@ int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, 
     int rc = tile_launch_check(t, threads, stages, smem);
     if (rc) return rc;
     int grid = 0;
-    rc = persistent_grid(tiled_hvp_kernel, threads, smem, t->n_tiles, INT32_MAX, grid);
+    rc = persistent_grid(tiled_hvp_kernel, threads + 64, smem, t->n_tiles, INT32_MAX, grid);
     if (rc) return rc;
     HvpArgs a{tile_graph(t, entries, site4), pick_layout(t, stages), q, y, status};
-    tiled_hvp_kernel<<<grid, threads, smem, (cudaStream_t)stream>>>(a);
+    tiled_hvp_kernel<<<grid, threads + 64, smem, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
@@ -961,7 +1270,7 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
     int rc = tile_launch_check(t, threads, stages, smem);
     if (rc) return rc;
     int grid = 0;
-    rc = persistent_grid(tiled_pcg_kernel, threads, smem, t->n_tiles, kMaxPcgBlocksTiled, grid);
+    rc = persistent_grid(tiled_pcg_kernel, threads + 64, smem, t->n_tiles, kMaxPcgBlocksTiled, grid);
     if (rc) return rc;
     const int64_t n6 = 6 * g->n_sites;
     PcgArgs a{};
@@ -988,7 +1297,7 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
     a.barrier = barrier;
     a.status = status;
     void *args[] = {&a};
-    if (cudaLaunchCooperativeKernel((const void *)tiled_pcg_kernel, grid, threads, args, smem,
+    if (cudaLaunchCooperativeKernel((const void *)tiled_pcg_kernel, grid, threads + 64, args, smem,
                                     (cudaStream_t)stream) != cudaSuccess) {
         cudaGetLastError();  // report it here, not at the next caller's launch check
         return DPF_ERR_CUDA;
@@ -997,5 +1306,90 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
 }
 
 int64_t dpf_tiled_partials_doubles(void) { return 2 * kMaxPcgBlocksTiled; }
+
+int64_t dpf_end_floats(int64_t n_bonds) { return n_bonds < 0 ? 0 : 24 * n_bonds; }
+
+int dpf_end_pack(const dpf_graph *g, const float *bond_data, double alpha, const float *P36, const float *mass32,
+                 const uint8_t *fixed, float *ends, float *P24, float *site4, void *stream) {
+    if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!g->edges || !g->inc_bond || !bond_data || !ends ||
+                                                                !aligned16(bond_data) || !aligned16(ends))) ||
+        (P24 && (!P36 || !aligned16(P24))) || (site4 && (!mass32 || !fixed || !aligned16(site4))))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t m = g->n_bonds, n_inc = 2 * m;
+    if (m) {
+        const float4 *base = reinterpret_cast<const float4 *>(bond_data);
+        float4 *e = reinterpret_cast<float4 *>(ends);
+        EndPackArgs a{n_inc, g->inc_bond, g->edges, base + 7 * m, base + 8 * m, base + 9 * m, base + 10 * m,
+                      (float)alpha, e, e + n_inc, e + 2 * n_inc};
+        pack_ends_kernel<<<blocks_for(n_inc, kThreads), kThreads, 0, st>>>(a);
+    }
+    if (P24 || site4)
+        pack_sites_kernel<<<blocks_for(g->n_sites, kThreads), kThreads, 0, st>>>(
+            g->n_sites, P36, mass32, fixed, reinterpret_cast<float4 *>(P24), reinterpret_cast<float4 *>(site4));
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+static EndGraph end_graph(const dpf_graph *g, const float *ends, const float *site4) {
+    const float4 *e = reinterpret_cast<const float4 *>(ends);
+    const int64_t n_inc = 2 * g->n_bonds;
+    return EndGraph{g->n_sites, g->inc_ptr, e, e + n_inc, e + 2 * n_inc, reinterpret_cast<const float4 *>(site4)};
+}
+
+int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, void *stream) {
+    if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!ends || !aligned16(ends))) || !site4 ||
+        !aligned16(site4) || !q || !y || ((uintptr_t)q & 7u) || ((uintptr_t)y & 7u))
+        return DPF_ERR_ARGUMENT;
+    int grid = 0;
+    const int rc = persistent_grid(end_hvp_kernel, kEndThreads, 0, INT32_MAX, INT32_MAX, grid, false);
+    if (rc) return rc;
+    end_hvp_kernel<<<grid, kEndThreads, 0, (cudaStream_t)stream>>>(end_graph(g, ends, site4), q, y);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
+                         const float *block32, const float *P24, const float *units32, const double *vector,
+                         double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
+                         double *partials, unsigned *barrier, int *status, void *stream) {
+    if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!ends || !aligned16(ends))) || !site4 || !fixed ||
+        !block32 || !P24 || !units32 || !vector || !out || !iterations || !workspace || !partials || !barrier ||
+        !status || max_iterations < 1 || !aligned16(workspace) || !aligned16(P24) || !aligned16(site4))
+        return DPF_ERR_ARGUMENT;
+    int grid = 0;
+    int rc = persistent_grid(end_pcg_kernel, kEndThreads, 0, INT32_MAX, kMaxPcgBlocksTiled, grid, false);
+    if (rc) return rc;
+    const int64_t n6 = 6 * g->n_sites;
+    PcgArgs a{};
+    a.n = g->n_sites;
+    a.E = end_graph(g, ends, site4);
+    a.fixed = fixed;
+    a.P24 = reinterpret_cast<const float4 *>(P24);
+    a.block = block32;
+    a.units32 = units32;
+    a.vector = vector;
+    a.tol2 = tolerance * tolerance;
+    a.max_it = max_iterations;
+    a.out = out;
+    a.iterations = iterations;
+    a.x = workspace;
+    a.r = workspace + n6;
+    a.u = workspace + 2 * n6;
+    a.p = workspace + 3 * n6;
+    a.s = workspace + 4 * n6;
+    a.w = workspace + 5 * n6;
+    a.part_a = partials;
+    a.part_b = partials + kMaxPcgBlocksTiled;
+    a.barrier = barrier;
+    a.status = status;
+    void *args[] = {&a};
+    if (cudaLaunchCooperativeKernel((const void *)end_pcg_kernel, grid, kEndThreads, args, 0, (cudaStream_t)stream) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return DPF_ERR_CUDA;
+    }
+    return DPF_OK;
+}
 
 }  // extern "C"

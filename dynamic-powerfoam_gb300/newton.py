@@ -953,9 +953,12 @@ class MixedNewtonBonds(NewtonBonds):
     # Steps between float64 rebuilds of the bond records and committed loads
     # (in between they are advanced by the commit's float32 increments).
     refresh_interval = 32
-    # Elastic PCG on site tiles (shared-memory HVP, two grid barriers per
-    # iteration); the tile size and CTA width are autotuned at the first use.
-    tiled = True
+    # Operator sweep of the elastic PCG (one cooperative launch, two grid
+    # barriers per iteration): 'ends' -- bond ends over the site-sorted
+    # incidence CSR, lanes of a site sum in registers; 'tiles' -- site tiles
+    # staged in shared memory (tile size and CTA width autotuned at the first
+    # use); 'bonds' -- a bond pass and a site gather through HBM per iteration.
+    sweep = 'ends'
 
     def step(self, dt, external, tolerance=2e-7, max_iterations=12, *, pose_tolerance=2e-6, backend='fgmres',
              linear_tolerance=1e-6, preconditioning='elastic'):
@@ -987,21 +990,46 @@ class MixedNewtonBonds(NewtonBonds):
         self._init_tiles()
 
     def _init_tiles(self):
-        n, dev = self.n_sites, self.device
         self._tiles = None
+        self._ends = None
+        self._sweep_ready = False
         self.tile_timings = {}
-        if not self.tiled:
+        self._packed = None
+
+    def _sweep_buffers(self):
+        """Packed block inverses, site records and PCG workspace of the 'ends' and
+        'tiles' sweeps (allocated at the first use)."""
+        if self._sweep_ready:
             return
-        lib = self._lib
+        n, dev, lib = self.n_sites, self.device, self._lib
         self._site4 = torch.empty((n, 4), dtype=torch.float32, device=dev)
         self._p24 = torch.empty(24*n, dtype=torch.float32, device=dev)
         self._tiled_workspace = torch.empty(lib.dpf_tiled_workspace_floats(n), dtype=torch.float32, device=dev)
         self._tiled_partials = torch.zeros(lib.dpf_tiled_partials_doubles(), dtype=F64, device=dev)
         self._tune_iterations = torch.zeros(1, dtype=torch.int32, device=dev)
-        self._packed = None
+        self._sweep_ready = True
+
+    def _pack_ends(self, dt):
+        """End records (alpha = dt^2/4 folded in), packed P and site records."""
+        self._sweep_buffers()
+        if self._ends is None:
+            self._ends = torch.empty(max(4, self._lib.dpf_end_floats(self.n_bonds)), dtype=torch.float32,
+                                     device=self.device)
+        self._call('dpf_end_pack', ctypes.byref(self._graph), self._bond_data.data_ptr(), .25*dt*dt,
+                   self._p32.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), self._ends.data_ptr(),
+                   self._p24.data_ptr(), self._site4.data_ptr(), self._stream())
+        self._packed = ('ends', dt)
+
+    def _end_pcg(self, vector, out, tolerance, max_iterations, iterations):
+        self._call('dpf_end_precondition', ctypes.byref(self._graph), self._ends.data_ptr(), self._site4.data_ptr(),
+                   self.fixed.data_ptr(), self._block32.data_ptr(), self._p24.data_ptr(), self._units32.data_ptr(),
+                   vector.data_ptr(), float(tolerance), int(max_iterations), out.data_ptr(), iterations.data_ptr(),
+                   self._tiled_workspace.data_ptr(), self._tiled_partials.data_ptr(), self._barrier.data_ptr(),
+                   self._status.data_ptr(), self._stream())
 
     def _pack_tiles(self, tiles, dt):
         """Entry records (alpha = dt^2/4 folded in), packed P and site records for ``tiles``."""
+        self._sweep_buffers()
         self._call('dpf_tile_pack', ctypes.byref(tiles.struct), self._bond_data.data_ptr(), self.n_bonds,
                    .25*dt*dt, self._p32.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), self.n_sites,
                    tiles.entries.data_ptr(), self._p24.data_ptr(), self._site4.data_ptr(), self._stream())
@@ -1094,8 +1122,7 @@ class MixedNewtonBonds(NewtonBonds):
         if status:
             raise guard_error(status)
         self.units = self._units
-        if self.tiled:
-            self._packed = None  # new tangent: repack before the next tiled PCG
+        self._packed = None  # new tangent: repack before the next swept PCG
         return scaled, norms
 
     def _newton_operator(self, y, dt, external):
@@ -1119,7 +1146,12 @@ class MixedNewtonBonds(NewtonBonds):
         def precondition(vector, tolerance=.03, max_iterations=80):
             vector = self._vec(vector)
             out = torch.empty_like(vector)
-            if self.tiled:
+            if self.sweep == 'ends':
+                if self._packed != ('ends', dt):
+                    self._pack_ends(dt)
+                self._timed('pcg', lambda: self._end_pcg(vector, out, tolerance, max_iterations, self._inner))
+                return out
+            if self.sweep == 'tiles':
                 self._ensure_tiles(dt, vector, tolerance, max_iterations)
                 self._timed('pcg', lambda: self._tiled_pcg(self._tiles, vector, out, tolerance, max_iterations,
                                                            self._inner))

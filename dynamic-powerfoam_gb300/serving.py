@@ -282,7 +282,7 @@ class Pool:
 class Batch(MixedNewtonBonds):
     """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
 
-    tiled = False
+    sweep = 'bonds'
     _active_mask = None
 
     def __init__(self, parts, pool=None):

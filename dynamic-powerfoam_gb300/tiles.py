@@ -15,10 +15,10 @@ import torch
 
 from . import _lib
 
-# Candidate (max entries per tile, threads per CTA, tile buffers per CTA) of
+# Candidate (max entries per tile, consumer threads per CTA, tile buffers per CTA) of
 # the autotuner; a CTA handles at most two entries per thread.
-CANDIDATES = ((256, 128, 2), (384, 192, 2), (384, 192, 3), (512, 256, 2), (768, 384, 2))
-DEFAULT = (512, 256, 2)
+CANDIDATES = ((256, 128, 3), (256, 128, 4), (320, 160, 3), (384, 192, 3), (384, 192, 4))
+DEFAULT = (384, 192, 3)
 
 
 def host_tiles(edges, inc_ptr, inc_bond, n_sites, max_entries=DEFAULT[0], max_stage=65535):

@@ -495,11 +495,12 @@ int dpf_tile_pack(const dpf_tiles *t, const float *bond_data, int64_t n_bonds, d
 /* y = (diag M + alpha K) q in float32 with identity rows on fixed sites;
  * q, y float32 (N, 6), 16-byte aligned; site4 the site records of
  * dpf_tile_pack.  Persistent
- * CTAs of `threads` (<= 384, >= max_entries / 2) walk their tiles through a
- * ring of `stages` shared-memory buffers (2..4; 0 = the deepest that fits)
- * filled by TMA bulk copies (records, metadata, own-site q) and cp.async
- * (halo q); a wait past its time limit sets DPF_ERR_BARRIER_TIMEOUT in
- * *status. */
+ * CTAs of `threads` consumer threads (<= 192, >= max_entries / 2) plus a
+ * bulk-copy warp and a halo-gather warp walk their tiles through a ring of
+ * `stages` shared-memory buffers (3 or 4; 0 = the deepest that fits): TMA
+ * bulk copies (records, metadata, own-site q) and cp.async (halo q) stream
+ * up to stages - 1 tiles ahead of the consumers; a wait past its time limit
+ * sets DPF_ERR_BARRIER_TIMEOUT in *status. */
 int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4, const float *q,
                   float *y, int *status, int threads, int stages, void *stream);
 
@@ -510,6 +511,37 @@ int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, 
  * buffers per CTA (2..4; 0 = the deepest that fits). */
 int64_t dpf_tiled_workspace_floats(int64_t n_sites);
 int64_t dpf_tiled_partials_doubles(void);
+
+/* ---- Bond-end sweep: the same float32 operator over the site-sorted
+ * incidence CSR ----
+ * One end record per incidence (bond seen from one of its sites, in the
+ * CSR's order): 3 float4 (n', r_s.x) (r_s.y, r_s.z, L, a kn)
+ * (a ks, a kb, a kt, other site) with n' pointing from the site to the other
+ * end; a group of lanes per site sums its ends' wrenches in registers and a
+ * fixed shuffle tree adds the lanes (no shared memory, no atomics).
+ * Replaces the same operator as dpf_tiled_hvp
+ * (experiments/bonded_dem_linear_gpu.py:42-52, 74-77). */
+
+/* Floats of the end records of a graph with n_bonds bonds (24 n_bonds). */
+int64_t dpf_end_floats(int64_t n_bonds);
+
+/* End records from the float32 tangent of dpf_mixed_residual (bond_data)
+ * with alpha folded into the stiffnesses; optionally P24 and site4 as
+ * dpf_tile_pack. */
+int dpf_end_pack(const dpf_graph *g, const float *bond_data, double alpha, const float *P36, const float *mass32,
+                 const uint8_t *fixed, float *ends, float *P24, float *site4, void *stream);
+
+/* y = (diag M + alpha K) q in float32 from the end records; q, y (N, 6)
+ * float32, 8-byte aligned. */
+int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, void *stream);
+
+/* dpf_tiled_precondition on the bond-end operator (one cooperative launch;
+ * workspace dpf_tiled_workspace_floats(N), partials
+ * dpf_tiled_partials_doubles()). */
+int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
+                         const float *block32, const float *P24, const float *units32, const double *vector,
+                         double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
+                         double *partials, unsigned *barrier, int *status, void *stream);
 int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4,
                            const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
                            const double *vector, double tolerance, int max_iterations, double *out, int *iterations,

@@ -1,5 +1,6 @@
-"""Tiled float32 HVP and elastic PCG against float64 products and the
-untiled float32 PCG on the same tangent."""
+"""The float32 operator sweeps (site tiles, bond ends) and their elastic
+PCGs against float64 products and the bond-pass float32 PCG on the same
+tangent."""
 import ctypes
 
 import numpy as np
@@ -45,7 +46,7 @@ def _direct_operator(s, alpha, q):
     return y
 
 
-@pytest.mark.parametrize('max_entries,threads,stages', [(256, 128, 2), (384, 192, 3), (512, 256, 4)])
+@pytest.mark.parametrize('max_entries,threads,stages', [(256, 128, 3), (320, 160, 4), (384, 192, 3)])
 def test_tiled_hvp_matches_float64_product(max_entries, threads, stages):
     import torch
     from dpf_gb300 import _lib
@@ -66,33 +67,57 @@ def test_tiled_hvp_matches_float64_product(max_entries, threads, stages):
     assert float(err) < 2e-6
 
 
-def test_tiled_pcg_matches_untiled_pcg():
+def test_end_hvp_matches_float64_product():
+    import torch
+    from dpf_gb300 import _lib
+    s, dt = _solver(m=9, seed=4)
+    s._pack_ends(dt)
+    q = torch.randn((s.n_sites, 6), dtype=torch.float64, device='cuda')
+    q32 = q.float().contiguous()
+    y = torch.empty_like(q32)
+    _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q32.data_ptr(),
+              y.data_ptr(), s._stream())
+    ref = _direct_operator(s, .25*dt*dt, q32.double())
+    err = (y.double() - ref).norm()/ref.norm()
+    assert float(err) < 2e-6
+    # bitwise reproducible: fixed lane split and shuffle tree, no atomics
+    y2 = torch.empty_like(q32)
+    _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q32.data_ptr(),
+              y2.data_ptr(), s._stream())
+    assert torch.equal(y, y2)
+
+
+@pytest.mark.parametrize('sweep', ['ends', 'tiles'])
+def test_swept_pcg_matches_bond_pass_pcg(sweep):
     import torch
     s, dt = _solver()
     v = torch.randn((s.n_sites, 6), dtype=torch.float64, device='cuda')
     pre = s._newton_preconditioner(dt)
-    s.tiled = True
+    s.sweep = sweep
     a = pre(v, tolerance=1e-7, max_iterations=2000)
-    from dpf_gb300.tiles import _TUNED
-    assert s._tiles is not None and (s.n_sites, s.n_bonds) in _TUNED, 'autotuner did not run'
-    s.tiled = False
+    if sweep == 'tiles':
+        from dpf_gb300.tiles import _TUNED
+        assert s._tiles is not None and (s.n_sites, s.n_bonds) in _TUNED, 'autotuner did not run'
+    s.sweep = 'bonds'
     b = pre(v, tolerance=1e-7, max_iterations=2000)
     rel = float((a - b).norm()/b.norm())
     assert rel < 1e-4, rel
     # the reference tolerance: comparable iteration counts
-    s.tiled = True
+    s.sweep = sweep
     s.inner_iterations = 0
     pre(v)
-    tiled_its = s.inner_iterations
-    s.tiled = False
+    swept_its = s.inner_iterations
+    s.sweep = 'bonds'
     s.inner_iterations = 0
     pre(v)
-    assert abs(tiled_its - s.inner_iterations) <= max(2, .2*s.inner_iterations)
+    assert abs(swept_its - s.inner_iterations) <= max(2, .2*s.inner_iterations)
 
 
-def test_tiled_pcg_is_deterministic():
+@pytest.mark.parametrize('sweep', ['ends', 'tiles'])
+def test_swept_pcg_is_deterministic(sweep):
     import torch
     s, dt = _solver(m=10, seed=3)
+    s.sweep = sweep
     v = torch.randn((s.n_sites, 6), dtype=torch.float64, device='cuda')
     pre = s._newton_preconditioner(dt)
     a = pre(v).clone()
