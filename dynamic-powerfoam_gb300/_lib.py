@@ -118,7 +118,8 @@ SIGNATURES = {
     'dpf_end_floats': (i64, [i64]),
     'dpf_end_pack': (i32, [P(Graph), vp, f64, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_end_hvp': (i32, [P(Graph), vp, vp, vp, vp, vp]),
-    'dpf_end_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_end_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, vp, vp,
+                                   vp]),
     'dpf_tiled_partials_doubles': (i64, []),
     'dpf_tiled_precondition': (i32, [P(Graph), P(Tiles), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp,
                                      i32, i32, vp]),

@@ -616,6 +616,8 @@ struct EndGraph {
     const int32_t *ptr;           // incidence CSR pointers (n + 1)
     const float4 *e0, *e1, *e2;   // end records in incidence order
     const float4 *site;           // per site (mass, inertia, 1 free / 0 fixed, -); fixed sites (1, 1, 0, -)
+    const int32_t *seg;           // optional per-site segment (a request of a batch) ...
+    const uint8_t *active;        // ... and per-segment flag: sites of inactive segments skip their ends
 };
 
 __device__ __forceinline__ void end_wrench(float4 a, float4 b, float4 c, const float qs[6], const float qo[6],
@@ -700,8 +702,8 @@ __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi 
         const int64_t s = (warp + r * warps) * kSites + lane32 / kEndLanes;
         const bool valid = s < G.n;
         float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, qs[6];
-        if (valid) {
-            load_q<kConst>(q, s, qs);
+        if (valid) load_q<kConst>(q, s, qs);
+        if (valid && !(G.active && !G.active[G.seg[s]])) {
             const int k1 = G.ptr[s + 1];
             // two ends per step: both ends' records, then both gathers, are in
             // flight together
@@ -1331,10 +1333,12 @@ int dpf_end_pack(const dpf_graph *g, const float *bond_data, double alpha, const
     return DPF_OK;
 }
 
-static EndGraph end_graph(const dpf_graph *g, const float *ends, const float *site4) {
+static EndGraph end_graph(const dpf_graph *g, const float *ends, const float *site4,
+                          const int32_t *seg_site = nullptr, const uint8_t *active = nullptr) {
     const float4 *e = reinterpret_cast<const float4 *>(ends);
     const int64_t n_inc = 2 * g->n_bonds;
-    return EndGraph{g->n_sites, g->inc_ptr, e, e + n_inc, e + 2 * n_inc, reinterpret_cast<const float4 *>(site4)};
+    return EndGraph{g->n_sites, g->inc_ptr, e, e + n_inc, e + 2 * n_inc, reinterpret_cast<const float4 *>(site4),
+                    seg_site, active};
 }
 
 int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, void *stream) {
@@ -1352,10 +1356,12 @@ int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const
 int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
                          const float *block32, const float *P24, const float *units32, const double *vector,
                          double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
-                         double *partials, unsigned *barrier, int *status, void *stream) {
+                         double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
+                         const uint8_t *active, void *stream) {
     if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!ends || !aligned16(ends))) || !site4 || !fixed ||
         !block32 || !P24 || !units32 || !vector || !out || !iterations || !workspace || !partials || !barrier ||
-        !status || max_iterations < 1 || !aligned16(workspace) || !aligned16(P24) || !aligned16(site4))
+        !status || max_iterations < 1 || !aligned16(workspace) || !aligned16(P24) || !aligned16(site4) ||
+        (active && !seg_site))
         return DPF_ERR_ARGUMENT;
     int grid = 0;
     int rc = persistent_grid(end_pcg_kernel, kEndThreads, 0, INT32_MAX, kMaxPcgBlocksTiled, grid, false);
@@ -1363,7 +1369,7 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
     const int64_t n6 = 6 * g->n_sites;
     PcgArgs a{};
     a.n = g->n_sites;
-    a.E = end_graph(g, ends, site4);
+    a.E = end_graph(g, ends, site4, seg_site, active);
     a.fixed = fixed;
     a.P24 = reinterpret_cast<const float4 *>(P24);
     a.block = block32;

@@ -1025,7 +1025,12 @@ class MixedNewtonBonds(NewtonBonds):
                    self.fixed.data_ptr(), self._block32.data_ptr(), self._p24.data_ptr(), self._units32.data_ptr(),
                    vector.data_ptr(), float(tolerance), int(max_iterations), out.data_ptr(), iterations.data_ptr(),
                    self._tiled_workspace.data_ptr(), self._tiled_partials.data_ptr(), self._barrier.data_ptr(),
-                   self._status.data_ptr(), self._stream())
+                   self._status.data_ptr(), *self._site_mask(), self._stream())
+
+    def _site_mask(self):
+        """(per-site segment, per-segment active flag) device pointers that let the
+        bond-end sweep skip sites of finished segments; (None, None) here."""
+        return None, None
 
     def _pack_tiles(self, tiles, dt):
         """Entry records (alpha = dt^2/4 folded in), packed P and site records for ``tiles``."""

@@ -260,7 +260,9 @@ class Pool:
         n, m = self.max_sites, self.max_bonds
         self.f64 = torch.empty(9*m + 3*6*n + 65*6*n + 1024, dtype=F64, device=device)
         self.f32 = torch.empty(lib.dpf_mixed_bond_floats(m) + 9*m + 2*36*n + 3*6*n +
-                               lib.dpf_mixed_workspace_floats(n, m) + 1024, dtype=torch.float32, device=device)
+                               lib.dpf_mixed_workspace_floats(n, m) + lib.dpf_end_floats(m) +
+                               (4 + 24)*n + lib.dpf_tiled_workspace_floats(n) + 4096,
+                               dtype=torch.float32, device=device)
 
     def carve(self, n, m):
         if n > self.max_sites or m > self.max_bonds:
@@ -282,7 +284,6 @@ class Pool:
 class Batch(MixedNewtonBonds):
     """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
 
-    sweep = 'bonds'
     _active_mask = None
 
     def __init__(self, parts, pool=None):
@@ -365,6 +366,17 @@ class Batch(MixedNewtonBonds):
         self._y32 = take32(6*n, (n, 6))
         self._d32 = take32(6*n, (n, 6))
         self._mixed_workspace = take32(lib.dpf_mixed_workspace_floats(n, m))
+        # bond-end sweep of the elastic PCG
+        self._ends = take32(max(4, lib.dpf_end_floats(m)))
+        self._site4 = take32(4*n, (n, 4))
+        self._p24 = take32(24*n)
+        self._tiled_workspace = take32(lib.dpf_tiled_workspace_floats(n))
+        self._tiled_partials = torch.zeros(lib.dpf_tiled_partials_doubles(), dtype=F64, device=dev)
+        self._tune_iterations = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._sweep_ready = True
+        self._packed = None
+        self._tiles = None
+        self.tile_timings = {}
         self._cached = None
         self._loads = take64(6*n, (n, 6))
         self._token = None
@@ -434,6 +446,11 @@ class Batch(MixedNewtonBonds):
             return None, None
         return self.seg_bond.data_ptr(), self._active_mask.data_ptr()
 
+    def _site_mask(self):
+        if self._active_mask is None:
+            return None, None
+        return self.seg_site.data_ptr(), self._active_mask.data_ptr()
+
     def _set_active(self, requests):
         """Bond passes of the following launches skip every request not in
         ``requests`` (their sites' rows of those passes are not read)."""
@@ -482,6 +499,7 @@ class Batch(MixedNewtonBonds):
                        self._mass32.data_ptr(), self.fixed.data_ptr(), self.radii.data_ptr(), dt,
                        self._block32.data_ptr(), self._p32.data_ptr(), self._units.data_ptr(),
                        self._units32.data_ptr(), stream)
+            self._packed = None  # new tangent and blocks: repack the end records before the PCG
             scaled = torch.empty_like(r)
             self._call('dpf_mixed_scale_residual', self.n_sites, self._p32.data_ptr(), self._units32.data_ptr(),
                        r.data_ptr(), scaled.data_ptr(), None, None, stream)
@@ -645,8 +663,9 @@ def footprint_bytes(sites, bonds):
 
     Per site: positions, reference points, velocity, rotation, mass (float64
     and float32), radius, flag and incidence pointer; per bond: edges, tangent,
-    stiffnesses, history and two incidence entries.  Batch scratch comes from
-    the service's pool, counted once.
+    stiffnesses, history and two incidence entries.  Batch scratch (Krylov
+    basis, float32 records, bond-end records, CG vectors) comes from the
+    service's pool, counted once.
     """
     per_site = 8*(3 + 3 + 6 + 9 + 6 + 1) + 4*6 + 1 + 4
     per_bond = 16 + 8*(3*3 + 4 + 3*2 + 2 + 3*2) + 8

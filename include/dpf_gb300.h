@@ -537,11 +537,14 @@ int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const
 
 /* dpf_tiled_precondition on the bond-end operator (one cooperative launch;
  * workspace dpf_tiled_workspace_floats(N), partials
- * dpf_tiled_partials_doubles()). */
+ * dpf_tiled_partials_doubles()).  seg_site/active (optional, for batches):
+ * a site s with active[seg_site[s]] == 0 skips its ends (its request's
+ * vector is zero, so its rows stay zero). */
 int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
                          const float *block32, const float *P24, const float *units32, const double *vector,
                          double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
-                         double *partials, unsigned *barrier, int *status, void *stream);
+                         double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
+                         const uint8_t *active, void *stream);
 int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4,
                            const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
                            const double *vector, double tolerance, int max_iterations, double *out, int *iterations,
