@@ -847,10 +847,11 @@ class NewtonBonds(FiniteBonds):
                            self._partials.data_ptr(), stream)
                 if len(y):
                     self._scalars[2:3].copy_(torch.linalg.vector_norm(y[:, 3:], dim=1).max().reshape(1))
-                (work, _, max_rotation), _ = self._fetch(3)
+                self._scalars[3:4].copy_(self._inner)   # the device CG count rides along
+                (work, _, max_rotation, inner), _ = self._fetch(4)
                 return work, dict(nonlinear_iterations=iteration, nonlinear_relative_residual=relative,
                                   local_pose_defect=local, krylov_iterations=krylov,
-                                  cg_iterations=self.inner_iterations, residual_trace=residual_trace,
+                                  cg_iterations=self._inner_host + int(inner), residual_trace=residual_trace,
                                   max_step_rotation=max_rotation)
             if iteration == max_iterations:
                 break
