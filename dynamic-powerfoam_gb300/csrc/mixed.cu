@@ -376,7 +376,7 @@ __device__ __forceinline__ void matvec6f(const float *P, const float x[6], float
 // Scaled residual in float32 from a float64 residual: s = P r / units;
 // returns max |s| and accumulates |s|^2.
 __device__ __forceinline__ float scale_site(const float *P, const float *units32, const double r[6], double *scaled,
-                                            float &sum_s) {
+                                            double &sum_s) {
     float rf[6], sf[6];
 #pragma unroll
     for (int c = 0; c < 6; ++c) rf[c] = (float)r[c];
@@ -387,7 +387,7 @@ __device__ __forceinline__ float scale_site(const float *P, const float *units32
         const float v = sf[c] / units32[c];
         if (scaled) scaled[c] = v;
         mx = fmaxf(mx, fabsf(v));
-        sum_s = fmaf(v, v, sum_s);
+        sum_s += (double)v * (double)v;  // float64: |s| equals the norm of the float64 copy
     }
     return mx;
 }
@@ -418,7 +418,8 @@ __device__ __forceinline__ void finish_norms(double sum_r, double max_s, double 
 
 __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
     double sum_r = 0.0;
-    float max_s = 0.0f, sum_s = 0.0f;
+    float max_s = 0.0f;
+    double sum_s = 0.0;
     int flags = 0;
     const int lane = threadIdx.x & (kGroupJ - 1);
     const int64_t groups = (int64_t)gridDim.x * blockDim.x / kGroupJ;
@@ -459,7 +460,8 @@ __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const flo
                                                             const double *r, double *scaled, double *norms,
                                                             double *partials) {
     double sum_r = 0.0;
-    float max_s = 0.0f, sum_s = 0.0f;
+    float max_s = 0.0f;
+    double sum_s = 0.0;
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
         double rr[6];
 #pragma unroll

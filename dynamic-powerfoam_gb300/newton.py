@@ -518,7 +518,7 @@ class _Krylov:
 
 
 def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iterations=256, *, workspace=None,
-           strict=True):
+           strict=True, rhs_norm=None):
     """Right-preconditioned flexible GMRES with CGS2 Arnoldi on CUDA tensors.
 
     Same signature, iteration and stopping rules as the reference
@@ -527,7 +527,8 @@ def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iteratio
     the (restart+1) x restart Hessenberg/Givens recurrence stays on the host,
     read back once per Arnoldi step as in the reference.  ``strict=False``
     returns the last iterate (with ``converged=False`` in the info) instead of
-    raising when the iteration budget runs out.
+    raising when the iteration budget runs out.  ``rhs_norm``: the float64
+    2-norm of ``rhs`` when the caller already holds it (saves one device read).
     """
     lib = _lib.load()
     device = rhs.device
@@ -543,7 +544,7 @@ def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iteratio
                    'dpf_dot_norm')
         return float(scal[1])
 
-    norm = norm_of(b)
+    norm = norm_of(b) if rhs_norm is None else float(rhs_norm)
     x = torch.zeros_like(b)
     if norm == 0:
         return x.reshape(shape), dict(iterations=0, relative_residual=0.)
@@ -880,8 +881,9 @@ class NewtonBonds(FiniteBonds):
                     self._krylov = _Krylov(n6, 32, self.device)
                 rhs = torch.empty_like(scaled)
                 self._call('dpf_axpby', n6, -1., scaled.data_ptr(), 0., scaled.data_ptr(), rhs.data_ptr(), stream)
+                # rhs = -scaled, whose float64 norm the residual pass returned (merit)
                 delta, metrics = fgmres(operator, rhs, precondition, tolerance=linear_tolerance,
-                                        workspace=self._krylov)
+                                        workspace=self._krylov, rhs_norm=merit)
                 krylov += metrics['iterations']
             else:
                 raise ValueError(backend)
