@@ -680,7 +680,9 @@ class Service:
     device) once it has arrived, admitted when its footprint fits the budget
     and the batch has room, and solved by batched Newton steps together with
     every other admitted request.  Requests that arrive while a batch step is
-    running join at the next step boundary.  Latency = completion - arrival.
+    running are set up meanwhile (a collector thread builds them as groups on a
+    side stream) and join at the next step boundary.  Latency = completion -
+    arrival.
     """
 
     def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=4_000_000, tolerance=1e-6):
@@ -697,16 +699,24 @@ class Service:
     def run(self, requests, clock=time.perf_counter):
         pending = sorted(requests)
         waiting, active, finished = [], [], []
+        ready = []           # (requests, group, event): admitted and set up, not yet in a batch
         if self.pool is None:
             largest = max((r.bonds for r in requests), default=1)
             max_bonds = int(self.max_batch_sites*max(r.bonds/max(r.sites, 1) for r in requests)*1.05) + largest
             self.pool = Pool(self.device, self.max_batch_sites + max(r.sites for r in requests), max_bonds)
             self.in_use += self.pool.f64.numel()*8 + self.pool.f32.numel()*4
+            # Reserve half of the rest of the budget in the caching allocator up
+            # front, so request state is carved from it instead of waiting on
+            # device allocations while batches run.
+            free = torch.cuda.mem_get_info(self.device)[0]
+            spare = int(min(.5*(self.hbm_budget - self.in_use), .5*free))
+            if spare > 0:
+                block = torch.empty(spare, dtype=torch.uint8, device=self.device)
+                del block
         t0 = clock()
         now = lambda: clock() - t0
         batch, members = None, []
         side = torch.cuda.Stream(device=self.device)
-        prefetch = None      # (requests, future of their group state) being set up on the side stream
 
         def build(reqs):
             with torch.cuda.stream(side):
@@ -718,46 +728,67 @@ class Service:
                 r.device_load = group.external[int(a):int(b)]
             return group, event
 
-        while pending or waiting or active:
+        def admit(room, first_free):
+            """Arrived requests in arrival order that fit the HBM budget and ``room``
+            sites (the first one regardless of ``room`` when ``first_free``)."""
             while pending and pending[0].arrival <= now():
                 waiting.append(pending.pop(0))
-            admitted = []
-            sites = sum(r.sites for r in active)
-            if prefetch is not None:
-                # requests already being set up are admitted first, as one group
-                admitted = prefetch[0]
-                sites += sum(r.sites for r in admitted)
-            while waiting and prefetch is None:
+            taken, sites = [], 0
+            while waiting:
                 req = waiting[0]
                 need = footprint_bytes(req.sites, req.bonds)
-                if self.in_use + need > self.hbm_budget or ((active or admitted) and
-                                                              sites + req.sites > self.max_batch_sites):
+                if self.in_use + need > self.hbm_budget or \
+                        (sites + req.sites > room and not (first_free and not taken)):
                     break
                 waiting.pop(0)
                 self.in_use += need
                 req.started = now()
-                admitted.append(req)
+                taken.append(req)
                 sites += req.sites
-            if not active and not admitted:
+            return taken
+
+        def collect(stop, room, first_free):
+            """While a batch step runs: set up the requests that arrive, as groups on
+            the side stream, so they join at the next step boundary ready to go."""
+            built = []
+            while not stop.is_set():
+                taken = admit(room, first_free and not built)
+                if taken:
+                    room -= sum(r.sites for r in taken)
+                    built.append((taken, *build(taken)))
+                    continue
+                wait = pending[0].arrival - now() if pending else .005
+                stop.wait(max(2e-4, min(wait, .005)))
+            return built
+
+        while pending or waiting or active or ready:
+            if not active and not ready:
+                # nothing to run: set up what has arrived here (otherwise the
+                # collector takes it during the next step)
+                taken = admit(self.max_batch_sites, True)
+                if taken:
+                    t1 = clock()
+                    ready.append((taken, *build(taken)))
+                    self.timers['setup'] += clock() - t1
+            if not active and not ready:
                 if pending:
                     time.sleep(max(0., min(pending[0].arrival - now(), .001)))
                 continue
-            if admitted or batch is None:
-                # staying requests keep their resident state; the admitted ones are
-                # set up together on the device (one upload, one setup, one sort)
+            if ready or batch is None:
+                # staying requests keep their resident state; the admitted ones join
+                # as the groups they were set up in
                 t1 = clock()
                 parts = [r.part for r in active]
-                if admitted:
-                    if prefetch is not None:
-                        group, event = prefetch[1].result()
-                        torch.cuda.current_stream(self.device).wait_event(event)
-                        prefetch = None
-                    else:
-                        group, event = build(admitted)
-                        torch.cuda.current_stream(self.device).wait_event(event)
+                stream = torch.cuda.current_stream(self.device)
+                for reqs, group, event in ready:
+                    stream.wait_event(event)
+                    for value in vars(group).values():   # set up on the side stream, used here
+                        if torch.is_tensor(value) and value.is_cuda:
+                            value.record_stream(stream)
                     parts.append(group)
+                    active += reqs
+                ready = []
                 t2 = clock()
-                active += admitted
                 members = list(active)
                 batch = Batch(parts, pool=self.pool)
                 ext = parts[0].external if len(parts) == 1 and isinstance(parts[0], RequestState) else \
@@ -765,25 +796,16 @@ class Service:
                 t3 = clock()
                 self.timers['setup'] += t2 - t1
                 self.timers['batch'] += t3 - t2
-            # set up the next group (requests waiting now) while this batch solves
-            if prefetch is None and waiting:
-                nxt, cap = [], 0
-                budget = self.in_use
-                while waiting:
-                    req = waiting[0]
-                    need = footprint_bytes(req.sites, req.bonds)
-                    if budget + need > self.hbm_budget or (nxt and cap + req.sites > self.max_batch_sites):
-                        break
-                    waiting.pop(0)
-                    budget += need
-                    self.in_use += need
-                    req.started = now()
-                    nxt.append(req)
-                    cap += req.sites
-                if nxt:
-                    prefetch = (nxt, _PREFETCH.submit(build, nxt))
+            # requests arriving during this step are set up meanwhile
+            staying = sum(r.sites for r in members if r.done_steps + 1 < r.steps)
+            stop = threading.Event()
+            future = _PREFETCH.submit(collect, stop, self.max_batch_sites - staying, not staying)
             t4 = clock()
-            results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
+            try:
+                results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
+            finally:
+                stop.set()
+                ready += future.result()
             self.timers['solve'] += clock() - t4
             self.batch_sizes.append([len(members), batch.n_sites])
             self.batches += 1
@@ -797,7 +819,7 @@ class Service:
                 req.done_steps += 1
                 if req.done_steps >= req.steps:
                     leaving.append(req)
-            if leaving or waiting or prefetch is not None or (pending and pending[0].arrival <= now()):
+            if leaving or ready or waiting or (pending and pending[0].arrival <= now()):
                 stamp = now()
                 for k, req in enumerate(members):
                     if req in leaving:
