@@ -67,6 +67,11 @@ def parse():
     p.add_argument('--adjoint-steps', type=int, default=50)
     p.add_argument('--adjoint-fd', type=int, default=4, help='bonds checked against central differences')
     p.add_argument('--served', type=int, default=512, help='requests of the served mixed-size stream (0: skip)')
+    p.add_argument('--large-mix', type=int, default=0,
+                   help='lattice size of the large served mix (128: one 128^3 foam for 10 steps with '
+                        '--large-mix-count requests of 32^3 sites; 0: skip)')
+    p.add_argument('--large-mix-count', type=int, default=64)
+    p.add_argument('--large-mix-small', type=int, default=32)
     p.add_argument('--served-plain', type=int, default=64,
                    help='requests of the same stream solved one at a time by the plain float64 solver')
     p.add_argument('--served-rate', type=float, default=4000., help='Poisson arrival rate of the stream (1/s)')
@@ -260,6 +265,47 @@ def run_adjoint(args, device):
                 rows.append([int(b), g, fd])
         out.update(fd_bonds=len(bonds), fd_h=h, fd_max_relative_error=float(max(errs)),
                    fd_median_relative_error=float(np.median(errs)), fd_samples=rows[:8])
+    return out
+
+
+def run_large_mix(args, device, peak, peaks):
+    """The large served mix: one jittered ``L^3`` foam under gravity (10 implicit
+    steps at dt = 1e-3) served together with requests of 32^3 sites (randomized
+    material, box and top load, one step each), all arriving at t = 0, under a
+    150 GB budget; then the bond-end HVP on the large foam alone."""
+    import torch
+    import dpf_gb300
+    from dpf_gb300 import serving
+    t = time.time()
+    reqs = serving.large_mix(big=args.large_mix, small=args.large_mix_small, count=args.large_mix_count,
+                             seed=args.seed)
+    build_s = time.time() - t
+    sites = sum(r.sites for r in reqs)
+    service = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=max(8_000_000, sites))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    finished = service.run(reqs)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ok = [r for r in finished if r.error is None]
+    solves = sum(r.done_steps for r in ok)
+    lat = np.array([r.finished - r.arrival for r in ok])
+    big = reqs[0]
+    out = dict(workload=f'{args.large_mix}^3 foam x 10 steps + {args.large_mix_count} x {args.large_mix_small}^3 '
+                        'requests, all at t = 0, 150 GB budget', requests=len(reqs), failed=len(reqs) - len(ok),
+               big_sites=big.sites, big_bonds=big.bonds, sites=sites, solves=solves, wall_s=wall,
+               solves_per_s=solves/wall, p50_ms=1e3*float(np.percentile(lat, 50)),
+               p99_ms=1e3*float(np.percentile(lat, 99)), batched_steps=service.batches,
+               phase_s={k: round(v, 4) for k, v in service.timers.items()}, foam_build_s=build_s,
+               max_relative_residual=float(max(i['nonlinear_relative_residual'] for r in ok for i in r.infos)))
+    del service, finished, ok
+    f = big.foam
+    s = dpf_gb300.MixedNewtonBonds(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
+                                   young=f['young'], shear=f['shear'], device=device)
+    s.step(big.dt, s.tensor(big.load), tolerance=args.tolerance)
+    out['hvp'] = run_hvp(s, big.dt, peak, peaks, launches=20)
+    del s
+    torch.cuda.empty_cache()
     return out
 
 
@@ -535,6 +581,7 @@ def run_ours(args):
         torch.cuda.synchronize()
     served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None
     adjoint = run_adjoint(args, device) if args.adjoint_lattice > 0 and world == 1 else None
+    large = run_large_mix(args, device, peak, peaks) if args.large_mix > 0 and world == 1 else None
     if rank != 0:
         return
     cpu = None
@@ -559,7 +606,7 @@ def run_ours(args):
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
                 gpu_launches=launches, kernels=kernels, roofline=roof, hvp=hvp, cpu_baseline=cpu, plain_f64=plain,
-                served=served, adjoint=adjoint,
+                served=served, adjoint=adjoint, large_mix=large,
                 relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)

@@ -821,15 +821,16 @@ class Service:
                     leaving.append(req)
             if leaving or ready or waiting or (pending and pending[0].arrival <= now()):
                 stamp = now()
+                gone = {id(r) for r in leaving}      # identity: requests compare by arrival time
                 for k, req in enumerate(members):
-                    if req in leaving:
+                    if id(req) in gone:
                         req.state = batch.request_state(k)
                         req.finished = stamp
-                        active.remove(req)
                         finished.append(req)
                         self.in_use -= footprint_bytes(req.sites, req.bonds)
                     else:
                         req.part = Slice(batch, k)
+                active = [r for r in active if id(r) not in gone]
                 batch = None
         return finished
 
@@ -882,6 +883,22 @@ def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, st
     if top.any():
         load[top, 2] -= young*strain*aspect[0]*aspect[1]/top.sum()
     return foam, load
+
+
+def large_mix(big=128, small=32, count=64, seed=0, big_steps=10, dt=1e-3):
+    """The large served mix: one jittered ``big^3`` foam under gravity with its
+    bottom layer fixed (``big_steps`` implicit steps of ``dt``) and ``count``
+    requests of ``small^3`` sites with randomized E, nu, box and top load as in
+    ``synthetic_stream`` (one step each), all arriving at t = 0."""
+    from .foam import gravity_load, jittered_lattice_foam
+    rng = np.random.default_rng(seed)
+    foam = jittered_lattice_foam(big, seed=seed)
+    foam['contacts'] = None
+    out = [Request(arrival=0., rid=0, foam=foam, load=gravity_load(foam), dt=dt, steps=big_steps)]
+    for rid in range(1, count + 1):
+        f, load = compressed_foam_request(small, rng, seed=seed + 1)
+        out.append(Request(arrival=0., rid=rid, foam=f, load=load, dt=dt, steps=1))
+    return out
 
 
 def synthetic_stream(count, seed=0, sites=(1024, 131072), rate=None, buckets=8, steps=1):

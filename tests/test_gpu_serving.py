@@ -107,3 +107,22 @@ def test_group_state_matches_solver_setup():
         assert torch.allclose(group.mass[site0:site0 + s.n_sites], s.mass, rtol=1e-14, atol=0)
         site0 += s.n_sites
         bond0 += s.n_bonds
+
+
+def test_large_mix_small_scale():
+    """The large served mix at small sizes: a multi-step foam served together
+    with single-step requests; each result agrees with its request solved alone."""
+    from dpf_gb300 import serving
+    reqs = serving.large_mix(big=12, small=6, count=5, seed=2, big_steps=4)
+    service = serving.Service(hbm_budget=8e9, max_batch_sites=20000)
+    finished = service.run(reqs)
+    assert len(finished) == 6 and all(r.error is None for r in finished)
+    by_id = {r.rid: r for r in finished}
+    assert by_id[0].done_steps == 4 and all(by_id[k].done_steps == 1 for k in range(1, 6))
+    # the single-step requests leave after the first batch step; the foam continues alone
+    assert service.batch_sizes[0][0] == 6 and service.batch_sizes[-1][0] == 1
+    for rid, steps in ((0, 4), (1, 1), (5, 1)):
+        req = by_id[rid]
+        alone, x0 = _alone(req, steps)
+        err = float(torch.linalg.vector_norm(req.state['x'] - alone.x)/torch.linalg.vector_norm(alone.x - x0))
+        assert err < 1e-5, (rid, err)
