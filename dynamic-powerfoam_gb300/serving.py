@@ -681,8 +681,10 @@ class Service:
     and the batch has room, and solved by batched Newton steps together with
     every other admitted request.  Requests that arrive while a batch step is
     running are set up meanwhile (a collector thread builds them as groups on a
-    side stream) and join at the next step boundary.  Latency = completion -
-    arrival.
+    side stream) and join at the next step boundary.  A batch steps all its
+    requests with one dt: admission is in arrival order and stops at a request
+    with another dt, which starts the next batch once the current one drains.
+    Latency = completion - arrival.
     """
 
     def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=4_000_000, tolerance=1e-6):
@@ -728,9 +730,11 @@ class Service:
                 r.device_load = group.external[int(a):int(b)]
             return group, event
 
-        def admit(room, first_free):
+        def admit(room, first_free, dt=None):
             """Arrived requests in arrival order that fit the HBM budget and ``room``
-            sites (the first one regardless of ``room`` when ``first_free``)."""
+            sites (the first one regardless of ``room`` when ``first_free``) and step
+            with ``dt`` (a batch steps all its requests with one dt; None: the
+            first one's)."""
             while pending and pending[0].arrival <= now():
                 waiting.append(pending.pop(0))
             taken, sites = [], 0
@@ -738,7 +742,8 @@ class Service:
                 req = waiting[0]
                 need = footprint_bytes(req.sites, req.bonds)
                 if self.in_use + need > self.hbm_budget or \
-                        (sites + req.sites > room and not (first_free and not taken)):
+                        (sites + req.sites > room and not (first_free and not taken)) or \
+                        (dt is not None and req.dt != dt) or (taken and req.dt != taken[0].dt):
                     break
                 waiting.pop(0)
                 self.in_use += need
@@ -747,12 +752,12 @@ class Service:
                 sites += req.sites
             return taken
 
-        def collect(stop, room, first_free):
+        def collect(stop, room, first_free, dt):
             """While a batch step runs: set up the requests that arrive, as groups on
             the side stream, so they join at the next step boundary ready to go."""
             built = []
             while not stop.is_set():
-                taken = admit(room, first_free and not built)
+                taken = admit(room, first_free and not built, dt)
                 if taken:
                     room -= sum(r.sites for r in taken)
                     built.append((taken, *build(taken)))
@@ -799,7 +804,7 @@ class Service:
             # requests arriving during this step are set up meanwhile
             staying = sum(r.sites for r in members if r.done_steps + 1 < r.steps)
             stop = threading.Event()
-            future = _PREFETCH.submit(collect, stop, self.max_batch_sites - staying, not staying)
+            future = _PREFETCH.submit(collect, stop, self.max_batch_sites - staying, not staying, members[0].dt)
             t4 = clock()
             try:
                 results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)

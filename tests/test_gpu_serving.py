@@ -126,3 +126,18 @@ def test_large_mix_small_scale():
         alone, x0 = _alone(req, steps)
         err = float(torch.linalg.vector_norm(req.state['x'] - alone.x)/torch.linalg.vector_norm(alone.x - x0))
         assert err < 1e-5, (rid, err)
+
+
+def test_requests_with_other_dt_get_their_own_batch():
+    """A batch steps with one dt: a request with another dt waits for its own batch."""
+    from dpf_gb300 import serving
+    reqs = serving.synthetic_stream(3, seed=13, sites=(600, 2000))
+    reqs[1].dt = 2e-3
+    service = serving.Service(hbm_budget=8e9, max_batch_sites=20000)
+    finished = service.run(reqs)
+    assert len(finished) == 3 and all(r.error is None for r in finished)
+    assert service.batches >= 2
+    for req in finished:
+        alone, x0 = _alone(req, 1)
+        err = float(torch.linalg.vector_norm(req.state['x'] - alone.x)/torch.linalg.vector_norm(alone.x - x0))
+        assert err < 1e-5, (req.rid, err)
