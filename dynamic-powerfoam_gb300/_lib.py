@@ -105,7 +105,8 @@ SIGNATURES = {
     'dpf_mixed_begin': (i32, [i64, vp, vp, vp, vp, vp, f64, vp, vp, vp, vp]),
     'dpf_mixed_residual_segmented': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp,
                                            vp, vp, vp, vp]),
-    'dpf_segment_norms': (i32, [i32, vp, vp, vp, i32, vp, vp, vp]),
+    'dpf_segment_partials_doubles': (i64, [i32]),
+    'dpf_segment_norms': (i32, [i32, vp, vp, vp, i32, vp, vp, vp, vp]),
     'dpf_segment_axpy': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_segment_select': (i32, [i64, vp, vp, vp, vp, vp, vp]),
     'dpf_static_max_bonds': (i64, []),
@@ -146,7 +147,7 @@ KERNELS = {
     'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
     'dpf_stiffness_apply_static': 2, 'dpf_mixed_setup': 2, 'dpf_mixed_residual': 2, 'dpf_mixed_scaling': 1,
     'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 3, 'dpf_mixed_stiffness_apply': 2,
-    'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 1,
+    'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 2,
     'dpf_segment_axpy': 1, 'dpf_segment_select': 1,
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
     'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_end_pack': 2, 'dpf_end_hvp': 1,

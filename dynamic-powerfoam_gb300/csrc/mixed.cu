@@ -1206,15 +1206,21 @@ __global__ void __launch_bounds__(kThreads) begin_sites(BeginArgs a) {
 // stored as contiguous site ranges [seg_ptr[r], seg_ptr[r+1]).
 
 // out[r] = [|a|_2, max|a|, |b|_2 or a.b] over the segment's 6-vectors,
-// skipping masked sites (mask[s] != 0) when mask is given.  One block per
-// segment, fixed order: deterministic and independent of the other segments.
+// skipping masked sites (mask[s] != 0) when mask is given.  kSegChunks blocks
+// per segment (blockIdx.x), each over a fixed slice of it, write partials; a
+// second pass adds a segment's partials in slice order: deterministic and
+// independent of the other segments.
+constexpr int kSegChunks = 16;
+
 __global__ void __launch_bounds__(kThreads) segment_norms_kernel(const int64_t *seg_ptr, const double *a,
                                                                  const double *b, int b_dot, const uint8_t *mask,
-                                                                 double *out) {
-    const int r = blockIdx.x;
-    const int64_t e0 = 6 * seg_ptr[r], e1 = 6 * seg_ptr[r + 1];
+                                                                 double *partials) {
+    const int r = blockIdx.y, c = blockIdx.x;
+    const int64_t s0 = seg_ptr[r], s1 = seg_ptr[r + 1];
+    const int64_t per = (s1 - s0 + kSegChunks - 1) / kSegChunks;
+    const int64_t lo = s0 + c * per < s1 ? s0 + c * per : s1, hi = lo + per < s1 ? lo + per : s1;
     double s2 = 0.0, mx = 0.0, t = 0.0;
-    for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
+    for (int64_t e = 6 * lo + threadIdx.x; e < 6 * hi; e += blockDim.x) {
         if (mask && mask[e / 6]) continue;
         const double v = a[e];
         s2 = fma(v, v, s2);
@@ -1225,10 +1231,26 @@ __global__ void __launch_bounds__(kThreads) segment_norms_kernel(const int64_t *
     mx = block_max(mx);
     t = block_sum(t);
     if (threadIdx.x == 0) {
-        out[3 * r] = sqrt(s2);
-        out[3 * r + 1] = mx;
-        out[3 * r + 2] = b_dot ? t : sqrt(t);
+        double *p = partials + 3 * ((int64_t)r * kSegChunks + c);
+        p[0] = s2;
+        p[1] = mx;
+        p[2] = t;
     }
+}
+
+__global__ void segment_finish_kernel(int n_segments, const double *partials, int b_dot, double *out) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_segments) return;
+    double s2 = 0.0, mx = 0.0, t = 0.0;
+    for (int c = 0; c < kSegChunks; ++c) {
+        const double *p = partials + 3 * ((int64_t)r * kSegChunks + c);
+        s2 += p[0];
+        mx = fmax(mx, p[1]);
+        t += p[2];
+    }
+    out[3 * r] = sqrt(s2);
+    out[3 * r + 1] = mx;
+    out[3 * r + 2] = b_dot ? t : sqrt(t);
 }
 
 // out = a + factor[seg[s]] * c on every site (factor 0 leaves a).
@@ -1493,10 +1515,14 @@ int dpf_mixed_begin(int64_t n_sites, const double *loads, const double *mass, co
     return DPF_OK;
 }
 
+int64_t dpf_segment_partials_doubles(int n_segments) { return n_segments < 0 ? 0 : 3LL * kSegChunks * n_segments; }
+
 int dpf_segment_norms(int n_segments, const int64_t *seg_ptr, const double *a, const double *b, int b_dot,
-                      const uint8_t *mask, double *out, void *stream) {
-    if (n_segments <= 0 || !seg_ptr || !a || !out) return DPF_ERR_ARGUMENT;
-    segment_norms_kernel<<<n_segments, kThreads, 0, (cudaStream_t)stream>>>(seg_ptr, a, b, b_dot, mask, out);
+                      const uint8_t *mask, double *out, double *partials, void *stream) {
+    if (n_segments <= 0 || n_segments > 65535 || !seg_ptr || !a || !out || !partials) return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    segment_norms_kernel<<<dim3(kSegChunks, n_segments), kThreads, 0, st>>>(seg_ptr, a, b, b_dot, mask, partials);
+    segment_finish_kernel<<<(n_segments + 127) / 128, 128, 0, st>>>(n_segments, partials, b_dot, out);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

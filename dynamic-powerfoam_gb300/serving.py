@@ -383,6 +383,7 @@ class Batch(MixedNewtonBonds):
         self._since_refresh = 0
         self._seg_norms = torch.zeros((R, 3), dtype=F64, device=dev)
         self._seg_norms2 = torch.zeros((R, 3), dtype=F64, device=dev)
+        self._seg_partials = torch.empty(max(1, lib.dpf_segment_partials_doubles(R)), dtype=F64, device=dev)
         self._host_seg = torch.zeros((2, R, 3), dtype=F64).pin_memory()
         self._host_seg_status = torch.zeros(R, dtype=torch.int32).pin_memory()
 
@@ -415,7 +416,7 @@ class Batch(MixedNewtonBonds):
         out = self._seg_norms if out is None else out
         self._call('dpf_segment_norms', self.n_segments, self.site_ptr.data_ptr(), a.data_ptr(),
                    None if b is None else b.data_ptr(), int(b_dot), None if mask is None else mask.data_ptr(),
-                   out.data_ptr(), self._stream())
+                   out.data_ptr(), self._seg_partials.data_ptr(), self._stream())
         return out
 
     def _fetch_segments(self, second=False, status=False):

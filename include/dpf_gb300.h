@@ -387,9 +387,13 @@ int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const dou
 
 /* Per-request [|a|_2, max|a|, |b|_2] (or [.., .., a.b] with b_dot) over the
  * 6-vectors of sites seg_ptr[r] .. seg_ptr[r+1]-1, skipping sites with mask
- * != 0 when mask is given; out: 3 doubles per request (device). */
+ * != 0 when mask is given; out: 3 doubles per request (device); partials:
+ * dpf_segment_partials_doubles(n_segments) doubles of scratch (at most 65,535
+ * requests).  Each request is split into fixed slices whose partials are added
+ * in slice order (deterministic). */
+int64_t dpf_segment_partials_doubles(int n_segments);
 int dpf_segment_norms(int n_segments, const int64_t *seg_ptr, const double *a, const double *b,
-                      int b_dot, const uint8_t *mask, double *out, void *stream);
+                      int b_dot, const uint8_t *mask, double *out, double *partials, void *stream);
 
 /* out = a + factor[seg[s]] * c for every site's 6-vector (factor: device doubles). */
 int dpf_segment_axpy(int64_t n_sites, const int32_t *seg, const double *factor, const double *a,
