@@ -661,21 +661,10 @@ __device__ __forceinline__ void load_q(const float *q, int64_t s, float v[6]) {
     v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
 }
 
-#ifndef DPF_END_PREFETCH
-#define DPF_END_PREFETCH 0
-#endif
-constexpr int kEndPrefetch = DPF_END_PREFETCH;  // rounds of L2 prefetch ahead of the loads (0: none)
-
-// L2 prefetch of [p, p + bytes) (fire and forget; 16-byte aligned, multiple of 16 bytes).
-__device__ __forceinline__ void prefetch_l2(const void *p, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
 // For every site s: epi(s, q_s, site record, acc) with acc the alpha K q sum.
 // Warp w of the grid takes the chunks w, w + W, ... of 32 / kEndLanes
-// consecutive sites (W warps in the grid); with kEndPrefetch > 0 lane 0
-// prefetches the end records of the chunk kEndPrefetch rounds ahead into L2.
-// The round count is the same for every warp, so the shuffles see full warps.
+// consecutive sites (W warps in the grid).  The round count is the same for
+// every warp, so the shuffles see full warps.
 template <bool kConst, class Epi>
 __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi &epi) {
     constexpr int kSites = 32 / kEndLanes;  // sites per warp and round
@@ -684,21 +673,7 @@ __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi 
     const int lane32 = (int)threadIdx.x & 31, lane = lane32 & (kEndLanes - 1);
     const int64_t chunks = (G.n + kSites - 1) / kSites;
     const int64_t rounds = (chunks + warps - 1) / warps;
-    auto prefetch = [&](int64_t chunk) {
-        if (chunk >= chunks) return;
-        const int64_t s0 = chunk * kSites, s1 = s0 + kSites < G.n ? s0 + kSites : G.n;
-        const int k0 = G.ptr[s0], k1 = G.ptr[s1];
-        if (k1 > k0) {
-            const uint32_t bytes = 16u * (uint32_t)(k1 - k0);
-            prefetch_l2(G.e0 + k0, bytes);
-            prefetch_l2(G.e1 + k0, bytes);
-            prefetch_l2(G.e2 + k0, bytes);
-        }
-    };
-    if (kEndPrefetch > 0 && lane32 == 0)
-        for (int d = 0; d < kEndPrefetch; ++d) prefetch(warp + d * warps);
     for (int64_t r = 0; r < rounds; ++r) {
-        if (kEndPrefetch > 0 && lane32 == 0) prefetch(warp + (r + kEndPrefetch) * warps);
         const int64_t s = (warp + r * warps) * kSites + lane32 / kEndLanes;
         const bool valid = s < G.n;
         float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, qs[6];
