@@ -608,8 +608,14 @@ __device__ __forceinline__ void sym_mv6(const float P[21], const float x[6], flo
 #ifndef DPF_END_MIN_BLOCKS
 #define DPF_END_MIN_BLOCKS 4
 #endif
+#ifndef DPF_END_PCG_THREADS
+#define DPF_END_PCG_THREADS 256
+#endif
 constexpr int kEndLanes = DPF_END_LANES;
 constexpr int kEndThreads = 256;
+// CTA width of the bond-end PCG: 32 warps per SM in all, fewer and wider CTAs
+// make its grid barriers and partial sums cheaper
+constexpr int kEndPcgThreads = DPF_END_PCG_THREADS;
 
 struct EndGraph {
     int64_t n;
@@ -802,6 +808,37 @@ __device__ __forceinline__ void mv36(const float *B, const float x[6], float y[6
     }
 }
 
+// One site of the single-reduction update: p = u + beta p, x += alpha p,
+// s = w + beta s, r -= alpha s, u = P r; returns (r, u).  Every load of the
+// site comes before any store.
+__device__ __forceinline__ float update_site(const PcgArgs &a, int64_t s, float fa, float fb) {
+    float uv[6], pv[6], xv[6], wv[6], sv[6], rv[6], Pm[21];
+    ld6(a.u + 6 * s, uv);
+    ld6(a.p + 6 * s, pv);
+    ld6(a.x + 6 * s, xv);
+    ld6(a.w + 6 * s, wv);
+    ld6(a.s + 6 * s, sv);
+    ld6(a.r + 6 * s, rv);
+    sym6(a.P24 + 6 * s, Pm);
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        pv[c] = fmaf(fb, pv[c], uv[c]);
+        xv[c] = fmaf(fa, pv[c], xv[c]);
+        sv[c] = fmaf(fb, sv[c], wv[c]);
+        rv[c] = fmaf(-fa, sv[c], rv[c]);
+    }
+    sym_mv6(Pm, rv, uv);
+    st6(a.p + 6 * s, pv);
+    st6(a.x + 6 * s, xv);
+    st6(a.s + 6 * s, sv);
+    st6(a.r + 6 * s, rv);
+    st6(a.u + 6 * s, uv);
+    float dot = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) dot = fmaf(rv[c], uv[c], dot);
+    return dot;
+}
+
 // kTiles: w = A u by the tiled sweep, else by the bond-end sweep.
 template <bool kTiles>
 __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
@@ -866,36 +903,7 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
         }
         const float fa = (float)alpha, fb = (float)beta;
         pf = 0.0f;
-        for (int64_t s = tid; s < a.n; s += stride) {
-            float pv[6], tv[6], rv[6];
-            // p = u + beta p ; x += alpha p
-            ld6(a.u + 6 * s, tv);
-            ld6(a.p + 6 * s, pv);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) pv[c] = fmaf(fb, pv[c], tv[c]);
-            st6(a.p + 6 * s, pv);
-            ld6(a.x + 6 * s, tv);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) tv[c] = fmaf(fa, pv[c], tv[c]);
-            st6(a.x + 6 * s, tv);
-            // s = w + beta s ; r -= alpha s
-            ld6(a.w + 6 * s, tv);
-            ld6(a.s + 6 * s, pv);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) pv[c] = fmaf(fb, pv[c], tv[c]);
-            st6(a.s + 6 * s, pv);
-            ld6(a.r + 6 * s, rv);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) rv[c] = fmaf(-fa, pv[c], rv[c]);
-            st6(a.r + 6 * s, rv);
-            // u = P r
-            float Pm[21];
-            sym6(a.P24 + 6 * s, Pm);
-            sym_mv6(Pm, rv, tv);
-            st6(a.u + 6 * s, tv);
-#pragma unroll
-            for (int c = 0; c < 6; ++c) pf = fmaf(rv[c], tv[c], pf);
-        }
+        for (int64_t s = tid; s < a.n; s += stride) pf += update_site(a, s, fa, fb);
         part = block_sum((double)pf);
         if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
         if (!grid_barrier(a.barrier, a.status)) return;
@@ -919,7 +927,9 @@ __global__ void __launch_bounds__(kTileThreadsMax + 64, DPF_TILE_MIN_BLOCKS) til
     pcg_body<true>(a, smem);
 }
 
-__global__ void __launch_bounds__(kEndThreads, DPF_END_MIN_BLOCKS) end_pcg_kernel(PcgArgs a) { pcg_body<false>(a, nullptr); }
+__global__ void __launch_bounds__(kEndPcgThreads, 1024 / kEndPcgThreads) end_pcg_kernel(PcgArgs a) {
+    pcg_body<false>(a, nullptr);
+}
 
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
 
@@ -1339,7 +1349,7 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
         (active && !seg_site))
         return DPF_ERR_ARGUMENT;
     int grid = 0;
-    int rc = persistent_grid(end_pcg_kernel, kEndThreads, 0, INT32_MAX, kMaxPcgBlocksTiled, grid, false);
+    int rc = persistent_grid(end_pcg_kernel, kEndPcgThreads, 0, INT32_MAX, kMaxPcgBlocksTiled, grid, false);
     if (rc) return rc;
     const int64_t n6 = 6 * g->n_sites;
     PcgArgs a{};
@@ -1365,7 +1375,8 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
     a.barrier = barrier;
     a.status = status;
     void *args[] = {&a};
-    if (cudaLaunchCooperativeKernel((const void *)end_pcg_kernel, grid, kEndThreads, args, 0, (cudaStream_t)stream) !=
+    if (cudaLaunchCooperativeKernel((const void *)end_pcg_kernel, grid, kEndPcgThreads, args, 0,
+                                    (cudaStream_t)stream) !=
         cudaSuccess) {
         cudaGetLastError();
         return DPF_ERR_CUDA;
