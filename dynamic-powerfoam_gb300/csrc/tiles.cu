@@ -839,47 +839,6 @@ __device__ __forceinline__ float update_site(const PcgArgs &a, int64_t s, float 
     return dot;
 }
 
-// Float64 work is scarce on this GPU (a small fraction of the float32 rate),
-// so the PCG's scalar work runs once per block instead of once per thread:
-// block partials are summed in float64 by one warp, global sums over the
-// block partials by one warp, and the recurrence's divisions by thread 0.
-
-// Widest CTA of the two PCG kernels.
-constexpr int kPcgThreadsMax = kTileThreadsMax + 64 > kEndPcgThreads ? kTileThreadsMax + 64 : kEndPcgThreads;
-
-// Sum over the block of one float per thread, in float64, fixed order.
-__device__ __forceinline__ double block_sum_float(float v) {
-    __shared__ float vals[kPcgThreadsMax];
-    __shared__ double total;
-    vals[threadIdx.x] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double t = 0.0;
-        for (int k = (int)threadIdx.x; k < (int)blockDim.x; k += 32) t += (double)vals[k];
-        t = warp_sum(t);
-        if (threadIdx.x == 0) total = t;
-    }
-    __syncthreads();
-    const double out = total;
-    __syncthreads();
-    return out;
-}
-
-// Sum of count float64 partials (one warp, fixed order), returned to every thread.
-__device__ __forceinline__ double block_total(const double *p, int count) {
-    __shared__ double total;
-    if (threadIdx.x < 32) {
-        double t = 0.0;
-        for (int k = (int)threadIdx.x; k < count; k += 32) t += p[k];
-        t = warp_sum(t);
-        if (threadIdx.x == 0) total = t;
-    }
-    __syncthreads();
-    const double out = total;
-    __syncthreads();
-    return out;
-}
-
 // kTiles: w = A u by the tiled sweep, else by the bond-end sweep.
 template <bool kTiles>
 __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
@@ -910,12 +869,11 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
 #pragma unroll
         for (int c = 0; c < 6; ++c) pf = fmaf(rr[c], zz[c], pf);
     }
-    double part = block_sum_float(pf);
+    double part = block_sum((double)pf);
     if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
     if (!grid_barrier(a.barrier, a.status)) return;
-    double gamma = block_total(a.part_b, gridDim.x);
+    double gamma = block_sum_array(a.part_b, gridDim.x);
     const double initial = gamma;
-    __shared__ double coef[3];  // alpha, and alpha / beta as float32, from thread 0
     if (initial == 0.0) {
         for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = 0.0;
         return;
@@ -930,33 +888,26 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
             ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
         else
             for_ends<false>(a.E, a.u, epi);
-        part = block_sum_float(epi.dot);
+        part = block_sum((double)epi.dot);
         if (threadIdx.x == 0) a.part_a[blockIdx.x] = part;
         if (!ok) return;
         if (!grid_barrier(a.barrier, a.status)) return;
-        const double delta = block_total(a.part_a, gridDim.x);
-        if (threadIdx.x == 0) {
-            double beta, alpha;
-            if (it == 0) {
-                beta = 0.0;
-                alpha = gamma / delta;
-            } else {
-                beta = gamma / gamma_prev;
-                alpha = gamma / (delta - beta * gamma / alpha_prev);
-            }
-            coef[0] = alpha;
-            coef[1] = (double)(float)alpha;
-            coef[2] = (double)(float)beta;
+        const double delta = block_sum_array(a.part_a, gridDim.x);
+        double beta, alpha;
+        if (it == 0) {
+            beta = 0.0;
+            alpha = gamma / delta;
+        } else {
+            beta = gamma / gamma_prev;
+            alpha = gamma / (delta - beta * gamma / alpha_prev);
         }
-        __syncthreads();
-        const double alpha = coef[0];
-        const float fa = (float)coef[1], fb = (float)coef[2];
+        const float fa = (float)alpha, fb = (float)beta;
         pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) pf += update_site(a, s, fa, fb);
-        part = block_sum_float(pf);  // (its barriers also keep coef until every thread has read it)
+        part = block_sum((double)pf);
         if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
         if (!grid_barrier(a.barrier, a.status)) return;
-        const double following = block_total(a.part_b, gridDim.x);
+        const double following = block_sum_array(a.part_b, gridDim.x);
         if (it % 5 == 0 && following <= a.tol2 * initial) break;
         gamma_prev = gamma;
         gamma = following;
