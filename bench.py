@@ -232,6 +232,8 @@ def run_adjoint(args, device):
     from dpf_gb300.adjoint import inverse_fit_problem
     model, theta0, loss = inverse_fit_problem(args.adjoint_lattice, 4, device, steps, dt, 10, 1e-12)
     theta = theta0.clone().requires_grad_(True)
+    with torch.no_grad():
+        loss(theta0)       # warm-up rollout (allocations, first launches), not timed
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     value = loss(theta)
