@@ -507,7 +507,7 @@ def run_ours(args):
         dist.all_reduce(times, op=dist.ReduceOp.MAX)
     ms, e_ms = times.tolist()
 
-    # the plain float64 solver on the same foam, one-at-a-time (spec comparator)
+    # the plain float64 solver on the same foam, one step at a time (the comparator of the mixed and served forms)
     plain = None
     if args.precision == 'mixed' and args.plain_steps > 0:
         p64 = dpf_gb300.NewtonBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
