@@ -385,6 +385,19 @@ def _reference_worker_step(args):
     return time.perf_counter() - t0
 
 
+def replica_rates(ms, e_ms, steps, world, device='cpu'):
+    """Whole-job rates of ``world`` replicas that each timed ``steps`` solves: the
+    slowest rank's device and end-to-end times (all-reduce MAX over the process
+    group when world > 1) and ``world * steps`` solves over those times."""
+    import torch
+    times = torch.tensor([ms, e_ms], dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(times, op=dist.ReduceOp.MAX)
+    ms, e_ms = times.tolist()
+    return ms, e_ms, world*steps/(ms*1e-3), world*steps/(e_ms*1e-3)
+
+
 def run_reference(args):
     """The reference algorithm (NumPy restatement) on all host cores: one worker
     process per core, each advancing its own copy of the one-eighth corner
@@ -502,10 +515,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     profile, s.profile = s.profile, None
 
-    times = torch.tensor([ms, e_ms], dtype=torch.float64, device=device)
-    if world > 1:
-        dist.all_reduce(times, op=dist.ReduceOp.MAX)
-    ms, e_ms = times.tolist()
+    ms, e_ms, value, e2e = replica_rates(ms, e_ms, args.steps, world, device)
 
     # the plain float64 solver on the same foam, one step at a time (the comparator of the mixed and served forms)
     plain = None
@@ -590,8 +600,6 @@ def run_ours(args):
     if not args.no_cpu_baseline and world == 1:
         rate, sample = oracle_rate(foam, load, args.dt, args.tolerance, steps=1, warmup=0, budget_s=30.)
         cpu = dict(value=rate, unit=UNIT, cores=1, kind='port', sample=sample)
-    value = world*args.steps/(ms*1e-3)
-    e2e = world*args.steps/(e_ms*1e-3)
     mean = lambda k: sum(i[k] for i in infos)/len(infos)
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
                 ms_per_step=ms/args.steps, higher_is_better=True, scaling='weak', vs_baseline=None,
