@@ -5,8 +5,10 @@ autotuner that picks the tile size and CTA width per graph.
 The tiled kernels compute ``(diag M + dt^2/4 K) q`` -- the operator of
 ``LinearBondsGPU._operator`` (``experiments/bonded_dem_linear_gpu.py:74-77``)
 inside ``NewtonBonds.elastic_precondition``
-(``experiments/bonded_dem_newton.py:107-130``) -- one CTA per tile with the
-tile's site vectors and bond wrenches in shared memory.
+(``experiments/bonded_dem_newton.py:107-130``) -- persistent CTAs stream the
+tiles through a ring of shared-memory buffers (a bulk-copy warp, a halo-gather
+warp, consumer warps).  ``MixedNewtonBonds`` uses them with ``sweep = 'tiles'``;
+its default is the bond-end sweep, which needs no tiling.
 """
 import ctypes
 
