@@ -10,7 +10,6 @@ are evaluated by one CUDA bond pass and a deterministic incidence gather.
 """
 import ctypes
 
-import numpy as np
 import torch
 
 from . import _lib

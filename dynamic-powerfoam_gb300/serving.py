@@ -34,8 +34,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .newton import (MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64, bond_setup,
-                     classical_contacts, incidence)
+from .newton import MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64, incidence
 
 _PER_SITE = ('p', 'mass', 'fixed', 'radii', 'x', 'v', 'rotation', '_mass32')
 _PER_BOND = ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')

@@ -29,7 +29,6 @@ def test_energy_and_forces_match_reference(name):
 def test_forces_are_energy_gradients():
     """-dE/dx and -dE/d(world rotation) by central differences of the GPU energy
     (rotation perturbed as q <- quat(exp(eps w)) q)."""
-    import torch
     g = golden('energy_foam5')
     model = _model(g)
     rng = np.random.default_rng(5)

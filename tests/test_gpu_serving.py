@@ -3,7 +3,6 @@ continuous-batching service.  A request's result must agree alone and in the
 mix within the solve tolerance: both runs satisfy the float64-accurate relative
 residual 1e-6 of their own request, and positions agree to 1e-5 of the step's
 displacement."""
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu

@@ -3,7 +3,6 @@ PCGs against float64 products and the bond-pass float32 PCG on the same
 tangent."""
 import ctypes
 
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
