@@ -136,6 +136,18 @@ SIGNATURES = {
     'dpf_adjoint_apply_jt': (i32, [P(Graph), vp, vp, vp, f64, vp, vp, vp, vp]),
     'dpf_adjoint_bond_vjp': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, f64, vp, i32, vp, vp, vp, vp, vp,
                                    vp]),
+    'dpf_operator_apply': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, f64, vp, vp, vp, vp]),
+    'dpf_block_inverse': (i32, [i64, vp, vp, vp, f64, vp, vp, vp]),
+    'dpf_block_pcg_workspace_doubles': (i64, [i64]),
+    'dpf_block_pcg': (i32, [P(Graph), P(Stiffness), P(Tangent), vp, vp, vp, vp, vp, f64, f64, i32, i32, i32, vp, vp,
+                            vp, vp, vp, vp, vp]),
+    'dpf_linear_midpoint_rhs': (i32, [i64, vp, vp, vp, vp, f64, vp, vp, vp]),
+    'dpf_linear_midpoint_advance': (i32, [i64, vp, f64, vp, vp, vp]),
+    'dpf_small_partials_doubles': (i64, []),
+    'dpf_linear_sums': (i32, [i64, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_anderson_gram': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, vp, vp, vp, vp]),
+    'dpf_anderson_mix': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, P(ctypes.c_double), vp, vp, vp]),
+    'dpf_barrier_selftest': (i32, [i32, i64, i32, vp, vp, vp, vp]),
 }
 
 
@@ -152,6 +164,8 @@ KERNELS = {
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
     'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_end_pack': 2, 'dpf_end_hvp': 1,
     'dpf_end_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
+    'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
+    'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
 }
 LAUNCHES = {'count': 0}
 

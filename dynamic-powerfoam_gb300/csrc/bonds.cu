@@ -5,7 +5,6 @@
 // doubles [F, T_i, T_j] (endpoint i receives (F, T_i), endpoint j (-F, T_j));
 // a site pass walks the site's incidence list in the reference's index_add_
 // order and sums them.  Results are deterministic run to run.
-#include <mutex>
 
 #include "common.cuh"
 
@@ -23,30 +22,6 @@ __device__ __forceinline__ void store_wrench(double *w, int64_t b, d3 f, d3 ti, 
     st3(p, f);
     st3(p + 3, ti);
     st3(p + 6, tj);
-}
-
-// acc += contributions of all bonds incident to site s.
-__device__ __forceinline__ void gather_wrench(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
-                                              const double *__restrict__ w, int64_t s, double acc[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) acc[c] = 0.0;
-    const int e1 = ptr[s + 1];
-    for (int e = ptr[s]; e < e1; ++e) {
-        const int v = inc[e];
-        if (v >= 0) {
-            const double *p = w + 9 * (int64_t)v;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) acc[c] += p[c];
-        } else {
-            const double *p = w + 9 * (int64_t)(~v);
-            acc[0] -= p[0];
-            acc[1] -= p[1];
-            acc[2] -= p[2];
-            acc[3] += p[6];
-            acc[4] += p[7];
-            acc[5] += p[8];
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -448,64 +423,6 @@ __device__ __forceinline__ void site_diagonal(const int32_t *ptr, const int32_t 
     }
 }
 
-// Inverse of a symmetric positive definite 6x6 matrix via Cholesky
-// (A = L L^T, A^-1 = L^-T L^-1), fully unrolled into registers: every loop
-// has a constant trip count so all indices fold.
-__device__ __forceinline__ void spd_inverse6(const double A[36], double P[36]) {
-    double L[36];
-#pragma unroll
-    for (int c = 0; c < 36; ++c) L[c] = 0.0;
-#pragma unroll
-    for (int jj = 0; jj < 6; ++jj) {
-        double s = A[6 * jj + jj];
-#pragma unroll
-        for (int kk = 0; kk < 6; ++kk)
-            if (kk < jj) s -= L[6 * jj + kk] * L[6 * jj + kk];
-        const double ljj = sqrt(s);
-        L[6 * jj + jj] = ljj;
-        const double inv = 1.0 / ljj;
-#pragma unroll
-        for (int ii = 0; ii < 6; ++ii) {
-            if (ii > jj) {
-                double v = A[6 * ii + jj];
-#pragma unroll
-                for (int kk = 0; kk < 6; ++kk)
-                    if (kk < jj) v -= L[6 * ii + kk] * L[6 * jj + kk];
-                L[6 * ii + jj] = v * inv;
-            }
-        }
-    }
-    double W[36];  // W = L^-1 (lower triangular)
-#pragma unroll
-    for (int c = 0; c < 36; ++c) W[c] = 0.0;
-#pragma unroll
-    for (int ii = 0; ii < 6; ++ii) {
-        W[6 * ii + ii] = 1.0 / L[6 * ii + ii];
-#pragma unroll
-        for (int jj = 0; jj < 6; ++jj) {
-            if (jj < ii) {
-                double v = 0.0;
-#pragma unroll
-                for (int kk = 0; kk < 6; ++kk)
-                    if (kk >= jj && kk < ii) v += L[6 * ii + kk] * W[6 * kk + jj];
-                W[6 * ii + jj] = -v * W[6 * ii + ii];
-            }
-        }
-    }
-#pragma unroll
-    for (int ii = 0; ii < 6; ++ii)
-#pragma unroll
-        for (int jj = 0; jj < 6; ++jj) {
-            if (jj <= ii) {
-                double v = 0.0;
-#pragma unroll
-                for (int kk = 0; kk < 6; ++kk)
-                    if (kk >= ii) v += W[6 * kk + ii] * W[6 * kk + jj];
-                P[6 * ii + jj] = v;
-                P[6 * jj + ii] = v;
-            }
-        }
-}
 
 struct ScalingArgs {
     int64_t n;
@@ -598,29 +515,35 @@ struct BondSetupArgs {
     double *n, *ri, *rj, *kn, *ks, *kb, *kt, *offset;
 };
 
+// One-time setup arithmetic, written with correctly rounded divisions and no
+// fused multiply-adds so that it gives the bits of the reference's host
+// formulas (n = d / |d|, c = (p_i + p_j)/2 + (r_i - r_j)/2 n, k = E A / L, ..).
 __global__ void __launch_bounds__(kThreads) bond_setup_kernel(BondSetupArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
     int64_t i, j;
     edge(a.edges, b, i, j);
     const d3 pi = ld3(a.points, i), pj = ld3(a.points, j);
-    const d3 d = pj - pi;
-    const double length = norm(d);
-    const d3 n = d / length;
-    const d3 classical = 0.5 * (pi + pj) + (0.5 * (a.radii[i] - a.radii[j])) * n;
+    const d3 d = mk(__dsub_rn(pj.x, pi.x), __dsub_rn(pj.y, pi.y), __dsub_rn(pj.z, pi.z));
+    const double length = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(d.x, d.x), __dmul_rn(d.y, d.y)), __dmul_rn(d.z, d.z)));
+    const d3 n = mk(__ddiv_rn(d.x, length), __ddiv_rn(d.y, length), __ddiv_rn(d.z, length));
+    const double half = __dmul_rn(0.5, __dsub_rn(a.radii[i], a.radii[j]));
+    const d3 classical = mk(__dadd_rn(__dmul_rn(0.5, __dadd_rn(pi.x, pj.x)), __dmul_rn(half, n.x)),
+                            __dadd_rn(__dmul_rn(0.5, __dadd_rn(pi.y, pj.y)), __dmul_rn(half, n.y)),
+                            __dadd_rn(__dmul_rn(0.5, __dadd_rn(pi.z, pj.z)), __dmul_rn(half, n.z)));
     const d3 c = a.contacts ? ld3(a.contacts, b) : classical;
     st3(a.n, b, n);
-    st3(a.ri, b, c - pi);
-    st3(a.rj, b, c - pj);
-    if (a.offset) st3(a.offset, b, c - classical);
+    st3(a.ri, b, mk(__dsub_rn(c.x, pi.x), __dsub_rn(c.y, pi.y), __dsub_rn(c.z, pi.z)));
+    st3(a.rj, b, mk(__dsub_rn(c.x, pj.x), __dsub_rn(c.y, pj.y), __dsub_rn(c.z, pj.z)));
+    if (a.offset)
+        st3(a.offset, b, mk(__dsub_rn(c.x, classical.x), __dsub_rn(c.y, classical.y), __dsub_rn(c.z, classical.z)));
     const double area = a.areas[b];
-    const double second = area * area / (4.0 * 3.14159265358979323846);
-    const double inv = 1.0 / length;
+    const double second = __ddiv_rn(__dmul_rn(area, area), 4.0 * 3.14159265358979323846);
     const double E = a.young_b ? a.young_b[b] : a.young, G = a.shear_b ? a.shear_b[b] : a.shear;
-    a.kn[b] = E * area * inv;
-    a.ks[b] = G * area * inv;
-    a.kb[b] = E * second * inv;
-    a.kt[b] = G * (2.0 * second) * inv;
+    a.kn[b] = __ddiv_rn(__dmul_rn(E, area), length);
+    a.ks[b] = __ddiv_rn(__dmul_rn(G, area), length);
+    a.kb[b] = __ddiv_rn(__dmul_rn(E, second), length);
+    a.kt[b] = __ddiv_rn(__dmul_rn(G, __dmul_rn(2.0, second)), length);
 }
 
 __global__ void __launch_bounds__(kThreads) site_mass_kernel(int64_t n, const double *masses, const double *radii,
@@ -628,7 +551,7 @@ __global__ void __launch_bounds__(kThreads) site_mass_kernel(int64_t n, const do
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= n) return;
     const double m = masses[s], r = radii[s];
-    const double inertia = 0.4 * m * r * r;
+    const double inertia = __dmul_rn(__dmul_rn(__dmul_rn(0.4, m), r), r);
 #pragma unroll
     for (int c = 0; c < 6; ++c) mass6[6 * s + c] = c < 3 ? m : inertia;
 }
@@ -839,23 +762,18 @@ namespace {
 
 __device__ __align__(256) double g_static_wrench[9 * DPF_STATIC_MAX_BONDS];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_static_mutex;
-double *g_static_wrench_ptr[kMaxDevices] = {};
-
 // Device address of g_static_wrench on the current device.  The host-side
-// name is only a stand-in for the device symbol, so it is resolved once per
-// device with cudaGetSymbolAddress while that device is current.
+// name is only a stand-in for the device symbol, so the address is looked up
+// with cudaGetSymbolAddress while the device is current.  It is looked up on
+// every call (cheap once the module is loaded) rather than cached, so a
+// device reset or a re-created primary context never leaves a stale address.
 int static_wrench(double **out) {
-    int dev = -1;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return DPF_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_wrench_ptr[dev]) {
-        void *ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_static_wrench) != cudaSuccess || !ptr) return DPF_ERR_CUDA;
-        g_static_wrench_ptr[dev] = static_cast<double *>(ptr);
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_static_wrench) != cudaSuccess || !ptr) {
+        cudaGetLastError();
+        return DPF_ERR_CUDA;
     }
-    *out = g_static_wrench_ptr[dev];
+    *out = static_cast<double *>(ptr);
     return DPF_OK;
 }
 

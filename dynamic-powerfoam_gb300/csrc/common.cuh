@@ -76,6 +76,90 @@ __device__ __forceinline__ d3 apply(const Transport &t, d3 v) {
     return t.c * out + t.s * cross(t.n1, out) + ((1.0 - t.c) * dot(t.n1, out)) * t.n1;
 }
 
+// Sum over the incidences of site s of the bond wrenches [F, T_i, T_j]
+// (nine doubles per bond; the j end receives (-F, T_j)), in incidence order.
+__device__ __forceinline__ void gather_wrench(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
+                                              const double *__restrict__ w, int64_t s, double acc[6]) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) acc[c] = 0.0;
+    const int e1 = ptr[s + 1];
+    for (int e = ptr[s]; e < e1; ++e) {
+        const int v = inc[e];
+        if (v >= 0) {
+            const double *p = w + 9 * (int64_t)v;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) acc[c] += p[c];
+        } else {
+            const double *p = w + 9 * (int64_t)(~v);
+            acc[0] -= p[0];
+            acc[1] -= p[1];
+            acc[2] -= p[2];
+            acc[3] += p[6];
+            acc[4] += p[7];
+            acc[5] += p[8];
+        }
+    }
+}
+
+// Inverse of a symmetric positive definite 6x6 matrix via Cholesky
+// (A = L L^T, A^-1 = L^-T L^-1), fully unrolled into registers: every loop
+// has a constant trip count so all indices fold.
+__device__ __forceinline__ void spd_inverse6(const double A[36], double P[36]) {
+    double L[36];
+#pragma unroll
+    for (int c = 0; c < 36; ++c) L[c] = 0.0;
+#pragma unroll
+    for (int jj = 0; jj < 6; ++jj) {
+        double s = A[6 * jj + jj];
+#pragma unroll
+        for (int kk = 0; kk < 6; ++kk)
+            if (kk < jj) s -= L[6 * jj + kk] * L[6 * jj + kk];
+        const double ljj = sqrt(s);
+        L[6 * jj + jj] = ljj;
+        const double inv = 1.0 / ljj;
+#pragma unroll
+        for (int ii = 0; ii < 6; ++ii) {
+            if (ii > jj) {
+                double v = A[6 * ii + jj];
+#pragma unroll
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk < jj) v -= L[6 * ii + kk] * L[6 * jj + kk];
+                L[6 * ii + jj] = v * inv;
+            }
+        }
+    }
+    double W[36];  // W = L^-1 (lower triangular)
+#pragma unroll
+    for (int c = 0; c < 36; ++c) W[c] = 0.0;
+#pragma unroll
+    for (int ii = 0; ii < 6; ++ii) {
+        W[6 * ii + ii] = 1.0 / L[6 * ii + ii];
+#pragma unroll
+        for (int jj = 0; jj < 6; ++jj) {
+            if (jj < ii) {
+                double v = 0.0;
+#pragma unroll
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk >= jj && kk < ii) v += L[6 * ii + kk] * W[6 * kk + jj];
+                W[6 * ii + jj] = -v * W[6 * ii + ii];
+            }
+        }
+    }
+#pragma unroll
+    for (int ii = 0; ii < 6; ++ii)
+#pragma unroll
+        for (int jj = 0; jj < 6; ++jj) {
+            if (jj <= ii) {
+                double v = 0.0;
+#pragma unroll
+                for (int kk = 0; kk < 6; ++kk)
+                    if (kk >= ii) v += W[6 * kk + ii] * W[6 * kk + jj];
+                P[6 * ii + jj] = v;
+                P[6 * jj + ii] = v;
+            }
+        }
+}
+
 // ---- reductions -----------------------------------------------------------
 
 __device__ __forceinline__ double warp_sum(double v) {
@@ -170,8 +254,11 @@ __device__ __forceinline__ unsigned long long global_ns() {
 }
 
 // barrier[0] = arrival count, barrier[1] = generation.  Returns false when the
-// wait ran past kBarrierTimeoutNs (the status word then carries the error).
-__device__ __forceinline__ bool grid_barrier(unsigned *barrier, int *status) {
+// wait ran past timeout_ns (the status word then carries the error).  parties:
+// arrivals that release the barrier (0 = every block of the grid).
+__device__ __forceinline__ bool grid_barrier(unsigned *barrier, int *status,
+                                             unsigned long long timeout_ns = kBarrierTimeoutNs,
+                                             unsigned parties = 0) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -179,14 +266,14 @@ __device__ __forceinline__ bool grid_barrier(unsigned *barrier, int *status) {
         const unsigned gen = ld_acquire(barrier + 1);
         __threadfence();
         const unsigned arrived = atomicAdd(barrier, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == (parties ? parties : gridDim.x) - 1) {
             atomicExch(barrier, 0u);
             __threadfence();
             atomicAdd(barrier + 1, 1u);
         } else {
             const unsigned long long t0 = global_ns();
             while (ld_acquire(barrier + 1) == gen) {
-                if (global_ns() - t0 > kBarrierTimeoutNs) {
+                if (global_ns() - t0 > timeout_ns) {
                     atomicOr(status, DPF_ERR_BARRIER_TIMEOUT);
                     ok = 0;
                     break;

@@ -22,29 +22,6 @@ __device__ __forceinline__ unsigned *counter_slot(double *partials, int slot) {
     return reinterpret_cast<unsigned *>(partials) + slot;
 }
 
-__device__ __forceinline__ void gather_wrench(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
-                                              const double *__restrict__ w, int64_t s, double acc[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) acc[c] = 0.0;
-    const int e1 = ptr[s + 1];
-    for (int e = ptr[s]; e < e1; ++e) {
-        const int v = inc[e];
-        if (v >= 0) {
-            const double *p = w + 9 * (int64_t)v;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) acc[c] += p[c];
-        } else {
-            const double *p = w + 9 * (int64_t)(~v);
-            acc[0] -= p[0];
-            acc[1] -= p[1];
-            acc[2] -= p[2];
-            acc[3] += p[6];
-            acc[4] += p[7];
-            acc[5] += p[8];
-        }
-    }
-}
-
 __device__ __forceinline__ void matvec6(const double *P, const double x[6], double y[6]) {
 #pragma unroll
     for (int row = 0; row < 6; ++row) {

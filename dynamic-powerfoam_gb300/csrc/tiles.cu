@@ -1283,6 +1283,11 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
     a.part_b = partials + kMaxPcgBlocksTiled;
     a.barrier = barrier;
     a.status = status;
+    // a wait that timed out in an earlier launch leaves a partial arrival count
+    if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), (cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();
+        return DPF_ERR_CUDA;
+    }
     void *args[] = {&a};
     if (cudaLaunchCooperativeKernel((const void *)tiled_pcg_kernel, grid, threads + 64, args, smem,
                                     (cudaStream_t)stream) != cudaSuccess) {
@@ -1374,6 +1379,11 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
     a.part_b = partials + kMaxPcgBlocksTiled;
     a.barrier = barrier;
     a.status = status;
+    // a wait that timed out in an earlier launch leaves a partial arrival count
+    if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), (cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();
+        return DPF_ERR_CUDA;
+    }
     void *args[] = {&a};
     if (cudaLaunchCooperativeKernel((const void *)end_pcg_kernel, grid, kEndPcgThreads, args, 0,
                                     (cudaStream_t)stream) !=

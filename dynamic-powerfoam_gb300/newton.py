@@ -15,6 +15,7 @@ A method the caller replaces on an instance (``s.jacobian_vector = f`` as
 through the reference's generic code path.
 """
 import ctypes
+import threading
 
 import numpy as np
 import torch
@@ -66,6 +67,32 @@ def incidence(edges, n_sites):
     return ptr.astype(np.int32), value[order].astype(np.int32)
 
 
+def device_incidence(edges, n_sites):
+    """``incidence`` built on the device by one stable sort of the endpoint sites
+    (int32 pointers and entries)."""
+    m = edges.shape[0]
+    site = torch.cat((edges[:, 0], edges[:, 1]))
+    ids = torch.arange(m, dtype=torch.int64, device=edges.device)
+    value = torch.cat((ids, -ids - 1))
+    order = torch.sort(site, stable=True).indices
+    ptr = torch.zeros(n_sites + 1, dtype=torch.int64, device=edges.device)
+    ptr[1:] = torch.cumsum(torch.bincount(site, minlength=n_sites), 0)
+    return ptr.to(torch.int32).contiguous(), value[order].to(torch.int32).contiguous()
+
+
+_PINNED = threading.local()
+
+
+def _pinned_buffers():
+    """Pinned host buffers for device-scalar reads, one set per host thread and
+    shared by every solver of that thread (a read copies, syncs and consumes
+    them at once), so constructing a solver allocates no pinned memory."""
+    if not hasattr(_PINNED, 'buffers'):
+        _PINNED.buffers = (torch.zeros(1, dtype=torch.int32).pin_memory(), torch.zeros(64, dtype=F64).pin_memory(),
+                           torch.zeros(64, dtype=F64).pin_memory())
+    return _PINNED.buffers
+
+
 def bond_setup(points, radii, pairs, areas, contacts, masses, young, shear):
     """Host-side setup arithmetic of ``LinearBondsGPU.__init__``
     (``experiments/bonded_dem_linear_gpu.py:15-40``): bond normals, contact
@@ -114,20 +141,9 @@ class LinearBonds:
             self.device = torch.device('cuda', torch.cuda.current_device())
         self._lib = _lib.load()
         self.tensor = lambda x: torch.as_tensor(x, dtype=F64, device=self.device)
-        # Setup arithmetic (bonded_dem_linear_gpu.py:15-40) on the host, once.
-        h = bond_setup(points, radii, pairs, areas, contacts, masses, young, shear)
-        p, edges = h['p'], h['edges']
-        self.p = self.tensor(p)
-        self.edges = torch.as_tensor(edges, dtype=torch.long, device=self.device).contiguous()
-        self.i, self.j = self.edges.T
-        self.n, self.ri, self.rj = self.tensor(h['n']), self.tensor(h['ri']), self.tensor(h['rj'])
-        self.kn, self.ks, self.kb, self.kt = (self.tensor(h[k]) for k in ('kn', 'ks', 'kb', 'kt'))
-        self.mass = self.tensor(h['mass'])
-        self.fixed = torch.as_tensor(np.asarray(fixed, dtype=bool), device=self.device)
-        ptr, inc = incidence(edges, len(p))
-        self._inc_ptr = torch.as_tensor(ptr, device=self.device)
-        self._inc_bond = torch.as_tensor(inc, device=self.device)
-        n_sites, n_bonds = len(p), len(edges)
+        self._offset = self._setup(points, radii, pairs, areas, contacts, masses, fixed, young, shear)
+        n_sites, n_bonds = self.p.shape[0], self.edges.shape[0]
+        self._inc_ptr, self._inc_bond = device_incidence(self.edges, n_sites)
         self._graph = _lib.Graph(n_sites, n_bonds, self.edges.data_ptr() if n_bonds else None,
                                  self._inc_ptr.data_ptr(), self._inc_bond.data_ptr())
         self._wrench = torch.empty(max(1, self._lib.dpf_wrench_scratch_doubles(n_bonds)), dtype=F64,
@@ -135,13 +151,50 @@ class LinearBonds:
         self._partials = torch.zeros(self._lib.dpf_partials_doubles(), dtype=F64, device=self.device)
         self._status = torch.zeros(1, dtype=torch.int32, device=self.device)
         self._scalars = torch.zeros(8, dtype=F64, device=self.device)
-        self._host_status = torch.zeros(1, dtype=torch.int32).pin_memory()
-        self._host_scalars = torch.zeros(64, dtype=F64).pin_memory()
+        self._host_status, self._host_scalars, _ = _pinned_buffers()
         self.q, self.v = torch.zeros_like(self.mass), torch.zeros_like(self.mass)
         self.kq = torch.zeros_like(self.mass)
         self.diagonal = self._diagonal_blocks()
         self.preconditioner = None
         self.preconditioner_dt = None
+
+    def _setup(self, points, radii, pairs, areas, contacts, masses, fixed, young, shear):
+        """Setup arithmetic of ``LinearBondsGPU.__init__`` (``bonded_dem_linear_gpu.py:15-40``)
+        in one device pass over the bonds and one over the sites (``dpf_bond_setup``):
+        normals, contact levers (classical ball contacts when ``contacts`` is
+        None), kn = E A/L, ks = G A/L, kb = E I/L, kt = 2 G I/L with I = A^2/(4 pi),
+        and the (N, 6) mass [m, m, m, 0.4 m r^2 x 3].  Returns the contact offsets
+        (contacts - classical)."""
+        p = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(p)
+        edges = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+        m = len(edges)
+        if m and (edges.min() < 0 or edges.max() >= n):
+            raise ValueError('Invalid endpoint index')
+        r = np.broadcast_to(np.asarray(radii, dtype=np.float64), (n,))
+        mass = np.broadcast_to(np.asarray(masses, dtype=np.float64), (n,))
+        if np.any(mass <= 0) or np.any(.4*mass*r*r <= 0):
+            raise ValueError('Only positive-mass bodies can enter this solver')
+        area = np.broadcast_to(np.asarray(areas, dtype=np.float64), (m,))
+        dev = self.device
+        self.p = self.tensor(p)
+        self.edges = torch.as_tensor(edges, device=dev).contiguous()
+        self.i, self.j = self.edges.T
+        self._site_radii = self.tensor(np.ascontiguousarray(r))
+        mass_d = self.tensor(np.ascontiguousarray(mass))
+        area_d = self.tensor(np.ascontiguousarray(area))
+        contacts_d = None if contacts is None else self.tensor(np.asarray(contacts, dtype=np.float64).reshape(-1, 3))
+        e = lambda *shape: torch.empty(shape, dtype=F64, device=dev)
+        self.n, self.ri, self.rj, offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
+        self.kn, self.ks, self.kb, self.kt = e(m), e(m), e(m), e(m)
+        self.mass = e(n, 6)
+        self._call('dpf_bond_setup', n, m, self.edges.data_ptr() if m else None, self.p.data_ptr(),
+                   self._site_radii.data_ptr(), area_d.data_ptr(), _addr(contacts_d), mass_d.data_ptr(),
+                   float(young), float(shear), None, None, self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr(),
+                   self.kn.data_ptr(), self.ks.data_ptr(), self.kb.data_ptr(), self.kt.data_ptr(), offset.data_ptr(),
+                   self.mass.data_ptr(), self._stream())
+        self.fixed = torch.as_tensor(np.ascontiguousarray(fixed, dtype=bool), device=dev)
+        return offset
 
     # ---- plumbing ---------------------------------------------------------
     @property
@@ -208,57 +261,113 @@ class LinearBonds:
 
     def _operator(self, q, alpha):
         """(diag M + alpha K) q, identity rows on fixed sites (``bonded_dem_linear_gpu.py:74-77``)."""
-        out = self.mass*q + alpha*self.stiffness(q)
-        out[self.fixed] = q[self.fixed]
+        q = self._vec(q)
+        if 'stiffness' in self.__dict__:       # an instance plug-in supplies K q
+            return torch.where(self.fixed[:, None], q, torch.addcmul(alpha*self.stiffness(q), self.mass, q))
+        out = torch.empty_like(q)
+        self._call('dpf_operator_apply', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(), float(alpha),
+                   q.data_ptr(), out.data_ptr(), self._wrench.data_ptr(), self._stream())
         return out
+
+    # ---- linear solves on the library's cooperative block PCG ----------------
+    def _solver_buffers(self):
+        """Workspace, barrier, info and reduction partials of the library PCG and sums."""
+        if getattr(self, '_lin', None) is None:
+            lib, dev = self._lib, self.device
+            self._lin = dict(work=torch.empty(lib.dpf_block_pcg_workspace_doubles(self.n_sites), dtype=F64, device=dev),
+                             barrier=torch.zeros(2, dtype=torch.int32, device=dev),
+                             aux=torch.zeros(64, dtype=F64, device=dev),
+                             flag=torch.zeros(1, dtype=torch.int32, device=dev),
+                             partials=torch.zeros(lib.dpf_small_partials_doubles(), dtype=F64, device=dev))
+        self._lin['host'] = _pinned_buffers()[2]
+        return self._lin
+
+    def _read_aux(self, count, status=False):
+        """aux[:count] (and the status word) on the host after one stream sync."""
+        buf = self._solver_buffers()
+        buf['host'][:count].copy_(buf['aux'][:count], non_blocking=True)
+        if status:
+            self._host_status.copy_(self._status[:1], non_blocking=True)
+        torch.cuda.current_stream(self.device).synchronize()
+        return buf['host'][:count].tolist(), int(self._host_status[0]) if status else 0
+
+    def _block_inverse(self, alpha):
+        """(diag M + alpha D)^-1 per site from ``self.diagonal`` (identity on fixed sites)."""
+        out = torch.empty((self.n_sites, 6, 6), dtype=F64, device=self.device)
+        diagonal = self.diagonal.to(F64).contiguous()
+        self._call('dpf_block_inverse', self.n_sites, self.mass.data_ptr(), self.fixed.data_ptr(),
+                   diagonal.data_ptr(), float(alpha), None, out.data_ptr(), self._stream())
+        return out
+
+    def _block_pcg(self, rhs, alpha, tolerance, max_iterations, mode, x, use_guess, scale=None, info_at=0):
+        """Launch the library PCG (mode 0: linear test, 1: balanced test); its
+        [iterations, relative, state, |rhs|] land in aux[info_at:info_at+4]."""
+        buf = self._solver_buffers()
+        self._call('dpf_block_pcg', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(),
+                   self.preconditioner.data_ptr(), _addr(scale), rhs.data_ptr(), float(alpha), float(tolerance),
+                   int(max_iterations), int(mode), int(use_guess), x.data_ptr(), buf['aux'][info_at:].data_ptr(),
+                   self._wrench.data_ptr(), buf['work'].data_ptr(), buf['barrier'].data_ptr(), self._status.data_ptr(),
+                   self._stream())
 
     @torch.no_grad()
     def solve_increment(self, rhs, dt, guess=None, tolerance=2e-8, max_iterations=1000):
-        """Block-Jacobi PCG of the linear model (``bonded_dem_linear_gpu.py:79-112``)."""
-        alpha = dt*dt/4
+        """Block-Jacobi PCG of the linear model (``bonded_dem_linear_gpu.py:79-112``):
+        one cooperative launch with the reference's stopping test, then one read
+        of its iteration count and true residual."""
+        alpha = .25*dt*dt
         if self.preconditioner_dt != dt:
-            diagonal = torch.diag_embed(self.mass) + alpha*self.diagonal
-            diagonal[self.fixed] = torch.eye(6, device=self.device, dtype=F64)
-            self.preconditioner = torch.linalg.inv(diagonal)
+            self.preconditioner = self._block_inverse(alpha)
             self.preconditioner_dt = dt
-        rhs = rhs.clone(); rhs[self.fixed] = 0
-        norm = float(torch.linalg.vector_norm(rhs))
+        x = torch.zeros_like(self.mass) if guess is None else self._vec(guess).clone()
+        return x, self._linear_result(self._vec(rhs), alpha, x, guess is not None, tolerance, max_iterations)
+
+    def _linear_result(self, rhs, alpha, x, use_guess, tolerance, max_iterations):
+        self._block_pcg(rhs, alpha, tolerance, max_iterations, 0, x, use_guess)
+        (iterations, relative, state, norm), _ = self._read_aux(4)
         if norm < 1e-30:
-            return torch.zeros_like(rhs), dict(iterations=0, relative_residual=0.)
-        x = torch.zeros_like(rhs) if guess is None else guess.clone()
-        x[self.fixed] = 0
-        residual = rhs - self._operator(x, alpha)
-        z = torch.einsum('nij,nj->ni', self.preconditioner, residual)
-        direction = z.clone(); rz = (residual*z).sum()
-        for iteration in range(max_iterations):
-            ad = self._operator(direction, alpha)
-            step = rz/(direction*ad).sum()
-            x += step*direction; residual -= step*ad
-            if iteration % 10 == 0:
-                relative = float(torch.linalg.vector_norm(residual))/norm
-                if relative < tolerance:
-                    break
-                if not np.isfinite(relative):
-                    raise RuntimeError('Nonfinite conjugate-gradient residual')
-            z = torch.einsum('nij,nj->ni', self.preconditioner, residual)
-            next_rz = (residual*z).sum()
-            direction = z + (next_rz/rz)*direction; rz = next_rz
-        actual = float(torch.linalg.vector_norm(rhs - self._operator(x, alpha)))/norm
-        if actual > 5*tolerance or not np.isfinite(actual):
-            raise RuntimeError(f'Linear solve failed after {iteration+1} iterations: {actual}')
-        return x, dict(iterations=iteration+1, relative_residual=actual)
+            return dict(iterations=0, relative_residual=0.)
+        if state == 2:
+            raise RuntimeError('Nonfinite conjugate-gradient residual')
+        if not relative <= 5*tolerance:
+            raise RuntimeError(f'Linear solve failed after {int(iterations)} iterations: {relative}')
+        return dict(iterations=int(iterations), relative_residual=relative)
 
     @torch.no_grad()
     def step(self, dt, external):
-        """Linear implicit midpoint (``bonded_dem_linear_gpu.py:114-121``)."""
-        rhs = dt*self.mass*self.v + .5*dt*dt*(external - self.kq)
-        dq, metrics = self.solve_increment(rhs, dt, guess=dt*self.v)
-        self.v = 2*dq/dt - self.v
-        self.q += dq; self.kq = self.stiffness(self.q)
-        return float((external*dq).sum()), metrics
+        """Linear implicit midpoint (``bonded_dem_linear_gpu.py:114-121``): the
+        right-hand side and the dt v guess in one kernel, the library PCG, then
+        the velocity/displacement update, K q and the work on the device."""
+        external, v, kq = self._vec(external), self._vec(self.v).clone(), self._vec(self.kq)
+        rhs, dq = torch.empty_like(v), torch.empty_like(v)
+        n, stream = self.n_sites, self._stream()
+        self._call('dpf_linear_midpoint_rhs', n, self.mass.data_ptr(), v.data_ptr(), external.data_ptr(),
+                   kq.data_ptr(), float(dt), rhs.data_ptr(), dq.data_ptr(), stream)
+        alpha = .25*dt*dt
+        if self.preconditioner_dt != dt:
+            self.preconditioner = self._block_inverse(alpha)
+            self.preconditioner_dt = dt
+        metrics = self._linear_result(rhs, alpha, dq, True, 2e-8, 1000)   # a vanishing rhs leaves dq = 0
+        self.q = self._vec(self.q)
+        self._call('dpf_linear_midpoint_advance', n, dq.data_ptr(), float(dt), v.data_ptr(), self.q.data_ptr(), stream)
+        self.v = v
+        self.kq = self.stiffness(self.q)
+        buf = self._solver_buffers()
+        self._call('dpf_linear_sums', n, external.data_ptr(), dq.data_ptr(), None, None, None, None,
+                   buf['aux'].data_ptr(), buf['partials'].data_ptr(), stream)
+        (work,), _ = self._read_aux(1)
+        return work, metrics
 
+    @torch.no_grad()
     def energy(self):
-        return float(.5*((self.mass*self.v*self.v).sum() + (self.q*self.kq).sum()))
+        """(sum m v^2 + q . K q) / 2 (``bonded_dem_linear_gpu.py:123-124``)."""
+        buf = self._solver_buffers()
+        v, q, kq = self._vec(self.v), self._vec(self.q), self._vec(self.kq)
+        self._call('dpf_linear_sums', self.n_sites, None, None, self.mass.data_ptr(), v.data_ptr(), q.data_ptr(),
+                   kq.data_ptr(), buf['aux'].data_ptr(), buf['partials'].data_ptr(), self._stream())
+        (_, value), _ = self._read_aux(2)
+        return value
 
 
 class FiniteBonds(LinearBonds):
@@ -269,17 +378,12 @@ class FiniteBonds(LinearBonds):
 
     def __init__(self, points, radii, pairs, areas, masses, fixed, contacts=None,
                  young=1200., shear=480., device='cuda'):
-        p = np.asarray(points, dtype=np.float64)
-        radii_a = np.broadcast_to(np.asarray(radii, dtype=np.float64), (len(p),))
-        classical = classical_contacts(p, radii_a, pairs)
-        if contacts is None:
-            contacts = classical
-        contacts = np.asarray(contacts, dtype=np.float64)
-        super().__init__(p, radii_a, pairs, areas, contacts, masses, fixed, young, shear, device)
+        # contacts=None: classical ball contacts, computed with the levers on the device
+        super().__init__(points, radii, pairs, areas, contacts, masses, fixed, young, shear, device)
         self.x = self.p.clone()
-        self.radii = self.tensor(np.array(radii_a))
+        self.radii = self._site_radii
         self.normal = self.n.clone()
-        self.offset = self.tensor(contacts - classical)
+        self.offset = self._offset
         self.fn, self.mt = torch.zeros_like(self.kn), torch.zeros_like(self.kn)
         self.fs, self.mb = torch.zeros_like(self.n), torch.zeros_like(self.n)
         self.rotation = torch.eye(3, dtype=F64, device=self.device).repeat(self.n_sites, 1, 1)
@@ -369,142 +473,237 @@ class FiniteBonds(LinearBonds):
         values, _ = self._fetch(1)
         return values[0]
 
+    def _pose_scale(self):
+        """Per-DOF scale of the pose defect: [r, r, r, 1, 1, 1] (``bonded_dem_finite_gpu.py:129-130``)."""
+        scale = torch.ones_like(self.mass)
+        scale[:, :3] = self._vec(self.radii)[:, None]
+        return scale
+
+    @torch.no_grad()
     def local_defect(self, residual):
-        """Max block-scaled pose defect (``bonded_dem_finite_gpu.py:127-131``)."""
-        correction = torch.einsum('nij,nj->ni', self.preconditioner, residual)
-        scale = torch.ones_like(correction)
-        scale[:, :3] = self.radii[:, None]
-        return float((correction/scale).abs().max())
+        """Max block-scaled pose defect max |P r / scale| (``bonded_dem_finite_gpu.py:127-131``)."""
+        buf = self._solver_buffers()
+        r = self._vec(residual)
+        self._call('dpf_scale_residual', self.n_sites, self.preconditioner.data_ptr(), self._pose_scale().data_ptr(),
+                   r.data_ptr(), None, buf['aux'].data_ptr(), self._partials.data_ptr(), self._stream())
+        (_, value), _ = self._read_aux(2)
+        return value
+
+    def _balanced_solve(self, rhs, dt, tolerance, max_iterations, scale, info_at=0):
+        """Launch the balanced PCG of the previous solver on the blocks of
+        ``self.diagonal`` (the preconditioner is rebuilt every call, as the
+        reference does); nothing is read back here."""
+        alpha = .25*dt*dt
+        self.preconditioner = self._block_inverse(alpha)
+        x = torch.empty_like(self.mass)
+        self._block_pcg(rhs, alpha, tolerance, max_iterations, 1, x, False, scale=scale, info_at=info_at)
+        return x
+
+    @staticmethod
+    def _balanced_outcome(info):
+        iterations, _, state, norm = info
+        if norm < 1e-40:
+            return 0
+        if state == 2:
+            raise RuntimeError('Nonfinite PCG residual')
+        if state != 0:
+            raise SubdivideError('Subdivide: balanced PCG did not converge')
+        return int(iterations)
 
     @torch.no_grad()
     def solve_increment(self, rhs, dt, tolerance=2e-7, max_iterations=1600):
-        """Block-Jacobi PCG with local and global checks (``bonded_dem_finite_gpu.py:133-167``).
+        """Block-Jacobi PCG with the local pose-defect and global residual tests
+        and a true-residual exit check (``bonded_dem_finite_gpu.py:133-167``),
+        one cooperative launch."""
+        x = self._balanced_solve(self._vec(rhs), dt, tolerance, max_iterations, self._pose_scale())
+        info, _ = self._read_aux(4)
+        return x, dict(iterations=self._balanced_outcome(info))
 
-        The blocks and their inverse come from the library (``dpf_prepare_scaling``);
-        K q from ``dpf_stiffness_apply``; the short vector recurrences are torch ops.
-        """
-        n = self.n_sites
-        block = torch.empty((n, 6, 6), dtype=F64, device=self.device)
-        preconditioner = torch.empty_like(block)
-        units = torch.empty_like(self.mass)
-        self._call('dpf_prepare_scaling', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
-                   ctypes.byref(self._tangent_struct()), self.mass.data_ptr(), self.fixed.data_ptr(),
-                   self.radii.data_ptr(), float(dt), None, block.data_ptr(), preconditioner.data_ptr(),
-                   units.data_ptr(), self._stream())
-        self.preconditioner = preconditioner
-        rhs = rhs.clone(); rhs[self.fixed] = 0
-        norm = float(torch.linalg.vector_norm(rhs))
-        if norm < 1e-40:
-            return torch.zeros_like(rhs), dict(iterations=0)
-        x, residual = torch.zeros_like(rhs), rhs.clone()
-        z = torch.einsum('nij,nj->ni', preconditioner, residual)
-        direction = z.clone(); rz = (residual*z).sum()
-        alpha = dt*dt/4
-        for iteration in range(max_iterations):
-            ad = LinearBonds._operator(self, direction, alpha)
-            step = rz/(direction*ad).sum()
-            x += step*direction; residual -= step*ad
-            if iteration % 10 == 0:
-                relative = float(torch.linalg.vector_norm(residual))/norm
-                if relative < tolerance and self.local_defect(residual) < 2e-8:
-                    actual = rhs - LinearBonds._operator(self, x, alpha)
-                    if (float(torch.linalg.vector_norm(actual))/norm < 5*tolerance
-                            and self.local_defect(actual) < 1e-7):
-                        return x, dict(iterations=iteration+1)
-                if not np.isfinite(relative):
-                    raise RuntimeError('Nonfinite PCG residual')
-            z = torch.einsum('nij,nj->ni', preconditioner, residual)
-            next_rz = (residual*z).sum()
-            direction = z + (next_rz/rz)*direction; rz = next_rz
-        raise SubdivideError('Subdivide: balanced PCG did not converge')
+    def _previous_residual(self, y, dt, external, v, preconditioner, scale, tangent=None):
+        """Midpoint residual at y (fixed rows y = 0) with [|r|, max |P r / scale|]
+        in aux[0:2] and the trial guards in the status word; returns r."""
+        r = torch.empty_like(y)
+        self._status.zero_()
+        use_p = preconditioner is not None
+        self._call('dpf_residual', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
+                   ctypes.byref(self._history_struct()), y.data_ptr(), v.data_ptr(), external.data_ptr(),
+                   self.mass.data_ptr(), self.fixed.data_ptr(), float(dt),
+                   ctypes.byref(self._trial_struct(tangent, end=False)) if tangent else None,
+                   preconditioner.data_ptr() if use_p else None, scale.data_ptr() if use_p else None, r.data_ptr(),
+                   None, self._solver_buffers()['aux'].data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(),
+                   self._status.data_ptr(), self._stream())
+        return r
 
     @torch.no_grad()
     def step(self, dt, external, tolerance=2e-7, max_iterations=18):
-        """Anderson-accelerated nonlinear implicit midpoint, the reference's
-        previous solver (``bonded_dem_finite_gpu.py:169-250``)."""
+        """The reference's previous solver (``bonded_dem_finite_gpu.py:169-250``):
+        nonlinear implicit midpoint by block-PCG corrections, type-II Anderson
+        mixing over the last six iterates and merit backtracking.  Every bond
+        sweep, solve, mixing reduction and norm runs in library kernels; the host
+        reads a few scalars per iteration and solves the at most 5 x 5 mixing
+        system."""
         if not np.isfinite(dt) or dt <= 0:
             raise ValueError('Positive finite dt required')
-        external = self._vec(external)
+        dt = float(dt)
+        external, v = self._vec(external), self._vec(self.v)
+        n, stream, buf = self.n_sites, self._stream(), self._solver_buffers()
+        self._call('dpf_rhs_scale', n, self.mass.data_ptr(), v.data_ptr(), external.data_ptr(),
+                   self.loads().data_ptr(), self.fixed.data_ptr(), dt, buf['aux'][8:].data_ptr(),
+                   self._partials.data_ptr(), stream)
+        scale = self._pose_scale()
+        mixing = _Mixing(self, 6)
         y = torch.zeros_like(self.mass)
-        v = self._vec(self.v)
-        rhs_scale = float(torch.linalg.vector_norm(dt*self.mass*v + .5*dt*dt*external))
-        rhs_scale = max(rhs_scale, .5*dt*dt*float(torch.linalg.vector_norm(self.loads()[~self.fixed])), 1e-30)
-        cg_total = 0
-        iterates, corrections = [], []
-        units = torch.ones_like(self.mass)
-        units[:, 3:] = self.radii[:, None]
+        m = self.n_bonds
+        tangent = {k: torch.empty((m, 3), dtype=F64, device=self.device) for k in ('n', 'ri', 'rj')}
+        tangent['force'] = None
+        solved = 0
         relative = float('nan')
+        rhs_scale = None
         for iteration in range(max_iterations):
-            trial = self.trial(y)
-            residual = self.mass*(y - dt*v) - .5*dt*dt*(trial['force'] + external)
-            residual[self.fixed] = 0
-            relative = float(torch.linalg.vector_norm(residual))/rhs_scale
-            local = self.local_defect(residual) if iteration else (0. if relative == 0 else float('inf'))
+            r = self._previous_residual(y, dt, external, v, self.preconditioner if iteration else None, scale, tangent)
+            values, status = self._read_aux(10, status=True)
+            if rhs_scale is None:
+                rhs_scale = max(values[8], .5*dt*dt*values[9], 1e-30)
+            if status:
+                raise guard_error(status)
+            relative = values[0]/rhs_scale
+            local = values[1] if iteration else (0. if relative == 0 else float('inf'))
             if relative < tolerance and local < 2e-6:
-                velocity = 2*y/dt - v
-                rotation = self._vec(self.rotation).clone()
-                self._call('dpf_accept_step', self.n_sites, y.data_ptr(), float(dt), v.clone().data_ptr(),
-                           rotation.data_ptr(), self._stream())
-                self.commit(trial)
-                self.v, self.rotation = velocity, rotation
-                self.time += dt
-                return float((external*y).sum()), dict(
-                    nonlinear_iterations=iteration, nonlinear_relative_residual=relative, cg_iterations=cg_total,
-                    local_pose_defect=local,
-                    max_step_rotation=float(torch.linalg.vector_norm(y[:, 3:], dim=1).max()))
-            self.n, self.ri, self.rj = trial['n'], trial['ri'], trial['rj']
+                return self._accept_previous(y, dt, external, v, dict(
+                    nonlinear_iterations=iteration, nonlinear_relative_residual=relative, cg_iterations=solved,
+                    local_pose_defect=local))
+            # frozen tangent of this iterate, its blocks, the balanced correction
+            self.n, self.ri, self.rj = tangent['n'], tangent['ri'], tangent['rj']
+            tangent = {k: torch.empty((m, 3), dtype=F64, device=self.device) for k in ('n', 'ri', 'rj')}
+            tangent['force'] = None
             self.diagonal = self._diagonal_blocks()
             self.preconditioner_dt = None
-            correction, cg = self.solve_increment(-residual, dt)
-            cg_total += cg['iterations']
-            merit = max(relative/tolerance, self.local_defect(residual)/2e-6)
-            iterates.append(y.clone()); corrections.append(correction.clone())
-            iterates, corrections = iterates[-6:], corrections[-6:]
+            rhs = torch.empty_like(r)
+            self._call('dpf_axpby', 6*n, -1., r.data_ptr(), 0., r.data_ptr(), rhs.data_ptr(), stream)
+            correction = self._balanced_solve(rhs, dt, 2e-7, 1600, scale, info_at=4)
+            self._call('dpf_scale_residual', n, self.preconditioner.data_ptr(), scale.data_ptr(), r.data_ptr(), None,
+                       buf['aux'][1:].data_ptr(), self._partials.data_ptr(), stream)
+            mixing.push(y, correction)
+            terms = mixing.reduce(buf['aux'][16:])
+            values, _ = self._read_aux(16 + terms)
+            solved += self._balanced_outcome(values[4:8])
+            merit = max(relative/tolerance, values[2]/2e-6)
             directions = []
-            if len(corrections) > 1:
-                dc = torch.stack([b - a for a, b in zip(corrections[:-1], corrections[1:])])
-                dg = torch.stack([b + db - a - da for a, b, da, db in
-                                  zip(iterates[:-1], iterates[1:], corrections[:-1], corrections[1:])])
-                weighted = (dc*units).flatten(1)
-                gram = weighted@weighted.T
-                ridge = 1e-10*torch.trace(gram).clamp_min(1e-40)
-                coefficients = torch.linalg.solve(gram + ridge*torch.eye(len(gram), dtype=F64, device=self.device),
-                                                  weighted@(correction*units).flatten())
-                accelerated = correction - torch.einsum('h,hij->ij', coefficients, dg)
-                if bool(torch.isfinite(accelerated).all()):
-                    directions.append(accelerated)
+            accelerated = mixing.mix(values[16:16 + terms])
+            if accelerated is not None:
+                directions.append(accelerated)
             directions.append(correction)
-            accepted = False
-            for direction in directions:
-                for factor in (1., .5, .25, .125, .0625):
-                    candidate = y + factor*direction
-                    try:
-                        state = self.trial(candidate)
-                    except RuntimeError:
-                        continue
-                    r = self.mass*(candidate - dt*v) - .5*dt*dt*(state['force'] + external)
-                    r[self.fixed] = 0
-                    candidate_merit = max(float(torch.linalg.vector_norm(r))/rhs_scale/tolerance,
-                                          self.local_defect(r)/2e-6)
-                    if candidate_merit < merit:
-                        y = candidate; accepted = True; break
-                if accepted:
-                    break
-            if not accepted:
-                raise SubdivideError('Subdivide: nonlinear line search failed')
+            y = self._backtrack(y, directions, merit, dt, external, v, scale, rhs_scale, tolerance)
         raise SubdivideError(f'Subdivide: nonlinear residual {relative} did not converge')
 
+    def _backtrack(self, y, directions, merit, dt, external, v, scale, rhs_scale, tolerance):
+        """First candidate y + f d (d in order, f = 1, 1/2, .., 1/16) whose trial
+        passes every guard and whose merit max(|r|/scale/tol, defect/2e-6) is
+        below the iterate's (``bonded_dem_finite_gpu.py:231-249``)."""
+        candidate = torch.empty_like(y)
+        for direction in directions:
+            for halvings in range(5):
+                self._call('dpf_axpby', 6*self.n_sites, 1., y.data_ptr(), 2.**-halvings, direction.data_ptr(),
+                           candidate.data_ptr(), self._stream())
+                self._previous_residual(candidate, dt, external, v, self.preconditioner, scale)
+                (norm, defect), status = self._read_aux(2, status=True)
+                if not status and max(norm/rhs_scale/tolerance, defect/2e-6) < merit:
+                    return candidate
+        raise SubdivideError('Subdivide: nonlinear line search failed')
+
+    def _accept_previous(self, y, dt, external, v, info):
+        """Commit the trial at y, v <- 2 y/dt - v, R <- exp(y_w) R; work = external . y."""
+        state = self.trial(y)
+        velocity, rotation = v.clone(), self._vec(self.rotation).clone()
+        self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, velocity.data_ptr(), rotation.data_ptr(),
+                   self._stream())
+        buf = self._solver_buffers()
+        self._call('dpf_linear_sums', self.n_sites, external.data_ptr(), y.data_ptr(), None, None, None, None,
+                   buf['aux'].data_ptr(), buf['partials'].data_ptr(), self._stream())
+        buf['aux'][1:2].copy_(torch.linalg.vector_norm(y[:, 3:], dim=1).max().reshape(1) if len(y) else
+                              torch.zeros(1, dtype=F64, device=self.device))
+        (work, turn), _ = self._read_aux(2)
+        self.commit(state)
+        self.v, self.rotation = velocity, rotation
+        self.time += dt
+        return work, dict(info, max_step_rotation=turn)
+
     def advance_interval(self, dt, force_at_time, depth=0):
-        """Recursive dt bisection on 'Subdivide:' (``bonded_dem_finite_gpu.py:252-261``)."""
-        try:
-            work, info = self.step(dt, force_at_time(self.time + .5*dt))
-            return work, [dict(dt=dt, subdivision_depth=depth, **info)]
-        except RuntimeError as error:
-            if depth >= 8 or 'Subdivide:' not in str(error):
-                raise
-            a, ia = self.advance_interval(.5*dt, force_at_time, depth+1)
-            b, ib = self.advance_interval(.5*dt, force_at_time, depth+1)
-            return a+b, ia+ib
+        """Advance by dt; an interval whose step fails with 'Subdivide:' is
+        replaced by its two halves, down to depth 8 (``bonded_dem_finite_gpu.py:252-261``).
+        The halves are walked depth first from an explicit stack; records come
+        out in time order."""
+        work, records = 0., []
+        pending = [(float(dt), depth)]
+        while pending:
+            h, level = pending.pop()
+            try:
+                value, info = self.step(h, force_at_time(self.time + .5*h))
+            except RuntimeError as error:
+                if level >= 8 or 'Subdivide:' not in str(error):
+                    raise
+                pending += [(.5*h, level + 1), (.5*h, level + 1)]
+                continue
+            work += value
+            records.append(dict(dt=h, subdivision_depth=level, **info))
+        return work, records
+
+
+class _Mixing:
+    """Type-II Anderson mixing of the previous solver over device slots holding
+    the last ``depth`` (iterate, correction) pairs (``bonded_dem_finite_gpu.py:215-229``):
+    one kernel reduces the weighted Gram system of the correction differences,
+    the host solves it (at most 5 x 5, ridge 1e-10 trace), one kernel forms
+    c - sum_h a_h (dy_h + dc_h)."""
+
+    def __init__(self, solver, depth):
+        self.solver, self.depth = solver, depth
+        shape = (depth, solver.n_sites, 6)
+        self.y = torch.empty(shape, dtype=F64, device=solver.device)
+        self.c = torch.empty(shape, dtype=F64, device=solver.device)
+        self.slots = []       # oldest first
+
+    def push(self, y, correction):
+        slot = self.slots.pop(0) if len(self.slots) == self.depth else len(self.slots)
+        self.y[slot].copy_(y)
+        self.c[slot].copy_(correction)
+        self.slots.append(slot)
+
+    def _order(self):
+        return (ctypes.c_int32*len(self.slots))(*self.slots)
+
+    def reduce(self, out):
+        """Launch the Gram reduction into ``out``; returns the number of terms (0: nothing to mix)."""
+        count = len(self.slots)
+        if count < 2:
+            return 0
+        s = self.solver
+        s._call('dpf_anderson_gram', s.n_sites, self.y.data_ptr(), self.c.data_ptr(), self.depth, self._order(), count,
+                s._vec(s.radii).data_ptr(), out.data_ptr(), s._solver_buffers()['partials'].data_ptr(), s._stream())
+        return (count - 1)*count//2 + count - 1
+
+    def mix(self, terms):
+        """Mixed direction from the reduced terms, or None when it is not finite."""
+        count = len(self.slots)
+        if count < 2:
+            return None
+        k = count - 1
+        gram = np.zeros((k, k))
+        upper = iter(terms[:k*(k + 1)//2])
+        for h in range(k):
+            for l in range(h, k):
+                gram[h, l] = gram[l, h] = next(upper)
+        proj = np.asarray(terms[k*(k + 1)//2:k*(k + 1)//2 + k])
+        ridge = 1e-10*max(np.trace(gram), 1e-40)
+        coefficients = np.ascontiguousarray(np.linalg.solve(gram + ridge*np.eye(k), proj), dtype=np.float64)
+        s = self.solver
+        out = torch.empty_like(s.mass)
+        flag = s._solver_buffers()['flag']
+        flag.zero_()
+        s._call('dpf_anderson_mix', s.n_sites, self.y.data_ptr(), self.c.data_ptr(), self.depth, self._order(), count,
+                coefficients.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), out.data_ptr(), flag.data_ptr(),
+                s._stream())
+        return None if int(flag.item()) else out
 
 
 class _Krylov:
@@ -726,23 +925,33 @@ class NewtonBonds(FiniteBonds):
         return out
 
     def _elastic_precondition_generic(self, vector, dt, tolerance, max_iterations):
-        rhs = torch.einsum('nij,nj->ni', self.block, self.units*vector)
-        rhs[self.fixed] = 0
-        x = torch.zeros_like(rhs); r = rhs.clone()
-        z = torch.einsum('nij,nj->ni', self.preconditioner, r)
-        direction = z.clone(); rz = (r*z).sum(); initial = float(rz)
-        if initial == 0:
+        """The elastic PCG with K q from an instance ``stiffness`` plug-in: the
+        recurrence and stopping rule of the library kernel, driven from the
+        host with one plug-in K q per iteration."""
+        def blocks(matrices, v):
+            return (matrices @ v.unsqueeze(-1)).squeeze(-1)
+
+        def inner(a, b):
+            return torch.dot(a.reshape(-1), b.reshape(-1))
+        b = torch.where(self.fixed[:, None], 0., blocks(self.block, self.units*vector))
+        x = torch.zeros_like(b)
+        r, z = b, blocks(self.preconditioner, b)
+        p, gamma = z, inner(b, z)
+        gamma0 = float(gamma)
+        if gamma0 == 0:
             return x
-        for iteration in range(max_iterations):
-            ad = self._operator(direction, .25*dt*dt)
-            alpha = rz/(direction*ad).sum()
-            x += alpha*direction; r -= alpha*ad
-            z = torch.einsum('nij,nj->ni', self.preconditioner, r)
-            following = (r*z).sum()
-            if iteration % 5 == 0 and float(following) <= tolerance*tolerance*initial:
+        done = max_iterations
+        for k in range(max_iterations):
+            w = self._operator(p, .25*dt*dt)
+            step = gamma/inner(p, w)
+            x, r = x + step*p, r - step*w
+            z = blocks(self.preconditioner, r)
+            gamma_next = inner(r, z)
+            if k % 5 == 0 and float(gamma_next) <= tolerance*tolerance*gamma0:
+                done = k + 1
                 break
-            direction = z + (following/rz)*direction; rz = following
-        self._inner_host += iteration+1
+            p, gamma = z + (gamma_next/gamma)*p, gamma_next
+        self._inner_host += done
         return x/self.units
 
     # ---- the Newton step ---------------------------------------------------
@@ -815,6 +1024,26 @@ class NewtonBonds(FiniteBonds):
         self.commit(state)
         self.v, self.rotation = self._v, rotation
 
+    def _dense_direction(self, operator, scaled):
+        """Newton direction of the 'dense' backend (``bonded_dem_newton.py:163-175``):
+        the scaled Jacobian restricted to the free DOFs is built one unit
+        column at a time through ``operator`` and solved by LU."""
+        free = (~self.fixed)[:, None].expand(-1, 6).reshape(-1)
+        index = free.nonzero().reshape(-1)
+        size = int(index.numel())
+        if size > 400:
+            raise ValueError('Dense reference limited to 400 free DOFs')
+        n6 = 6*self.n_sites
+        jacobian = torch.empty((size, size), dtype=F64, device=self.device)
+        unit = torch.zeros(n6, dtype=F64, device=self.device)
+        for column, dof in enumerate(index.tolist()):
+            unit[dof] = 1.
+            jacobian[:, column] = operator(unit.view(-1, 6)).reshape(-1).index_select(0, index)
+            unit[dof] = 0.
+        delta = torch.zeros(n6, dtype=F64, device=self.device)
+        delta.index_copy_(0, index, torch.linalg.solve(jacobian, -scaled.reshape(-1).index_select(0, index)))
+        return delta.view(-1, 6)
+
     @torch.no_grad()
     def step(self, dt, external, tolerance=2e-7, max_iterations=12, *,
              pose_tolerance=2e-6, backend='fgmres', linear_tolerance=1e-6,
@@ -858,18 +1087,7 @@ class NewtonBonds(FiniteBonds):
                 break
             operator = self._newton_operator(y, dt, external)
             if backend == 'dense':
-                free = torch.nonzero(~self.fixed.repeat_interleave(6)).flatten()
-                if len(free) > 400:
-                    raise ValueError('Dense reference limited to 400 free DOFs')
-                eye = torch.eye(len(free), dtype=F64, device=self.device)
-                columns = []
-                for col in eye:
-                    direction = torch.zeros_like(y).flatten(); direction[free] = col
-                    columns.append(operator(direction.reshape_as(y)).flatten()[free])
-                jac = torch.stack(columns, dim=1)
-                delta = torch.zeros_like(y).flatten()
-                delta[free] = torch.linalg.solve(jac, -scaled.flatten()[free])
-                delta = delta.reshape_as(y)
+                delta = self._dense_direction(operator, scaled)
             elif backend == 'fgmres':
                 if preconditioning == 'elastic':
                     precondition = self._newton_preconditioner(dt)
@@ -911,7 +1129,15 @@ FastNewtonBonds = NewtonBonds
 
 
 class AdaptiveIntervals:
-    """Remember a successful subdivision depth (``experiments/bonded_dem_adaptive.py:4-23``)."""
+    """Interval controller that keeps the subdivision depth which last worked
+    (``experiments/bonded_dem_adaptive.py:4-23``): an interval is advanced as
+    2^depth equal pieces, each bisected further on demand; the deepest piece
+    sets the next depth, and after ``coarsen_after`` consecutive easy
+    intervals (no piece needed more than ``easy_newton`` Newton iterations)
+    the depth drops by one."""
+
+    coarsen_after = 8
+    easy_newton = 3
 
     def __init__(self, solver):
         self.solver = solver
@@ -919,19 +1145,18 @@ class AdaptiveIntervals:
         self.easy_intervals = 0
 
     def advance(self, dt, load):
-        work, records = 0., []
-        for _ in range(2**self.depth):
-            value, info = self.solver.advance_interval(dt/(2**self.depth), load, depth=self.depth)
-            work += value; records.extend(info)
-        self.depth = max(item['subdivision_depth'] for item in records)
-        if max(item['nonlinear_iterations'] for item in records) <= 3:
-            self.easy_intervals += 1
-        else:
-            self.easy_intervals = 0
-        if self.easy_intervals >= 8 and self.depth:
-            self.depth -= 1
-            self.easy_intervals = 0
-        return work, records
+        pieces = 1 << self.depth
+        results = [self.solver.advance_interval(dt/pieces, load, depth=self.depth) for _ in range(pieces)]
+        records = [record for _, part in results for record in part]
+        self._remember(records)
+        return sum(value for value, _ in results), records
+
+    def _remember(self, records):
+        self.depth = max(record['subdivision_depth'] for record in records)
+        easy = all(record['nonlinear_iterations'] <= self.easy_newton for record in records)
+        self.easy_intervals = self.easy_intervals + 1 if easy else 0
+        if self.depth and self.easy_intervals >= self.coarsen_after:
+            self.depth, self.easy_intervals = self.depth - 1, 0
 
 
 class MixedNewtonBonds(NewtonBonds):

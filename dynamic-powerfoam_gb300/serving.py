@@ -34,7 +34,8 @@ import numpy as np
 import torch
 
 from . import _lib
-from .newton import MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64, incidence
+from .newton import (MixedNewtonBonds, NewtonBonds, SubdivideError, guard_error, _Krylov, fgmres, F64, incidence,
+                     device_incidence)
 
 _PER_SITE = ('p', 'mass', 'fixed', 'radii', 'x', 'v', 'rotation', '_mass32')
 _PER_BOND = ('n', 'ri', 'rj', 'kn', 'ks', 'kb', 'kt', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
@@ -89,18 +90,6 @@ def _staging():
     if not hasattr(_LOCAL, 'staging'):
         _LOCAL.staging = Staging()
     return _LOCAL.staging
-
-
-def device_incidence(edges, n_sites):
-    """Incidence CSR of ``incidence`` built on the device (stable sort by site)."""
-    m = edges.shape[0]
-    site = torch.cat((edges[:, 0], edges[:, 1]))
-    ids = torch.arange(m, dtype=torch.int64, device=edges.device)
-    value = torch.cat((ids, -ids - 1))
-    order = torch.sort(site, stable=True).indices
-    ptr = torch.zeros(n_sites + 1, dtype=torch.int64, device=edges.device)
-    ptr[1:] = torch.cumsum(torch.bincount(site, minlength=n_sites), 0)
-    return ptr.to(torch.int32).contiguous(), value[order].to(torch.int32).contiguous()
 
 
 # Device copies of request bond graphs, keyed by the host pairs array (many
@@ -862,17 +851,19 @@ def _unit_foam(m, seed):
     return _UNIT_FOAMS[key]
 
 
-def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, strain=None, seed=0, density=1000.):
+def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, strain=None, seed=0, density=1000.,
+                            base=None):
     """A jittered ``m^3`` foam stretched by box aspect ratios, with its material and top load.
 
-    The bond graph is that of the unit-cube foam (computed once per lattice
-    size); positions, cross sections, masses and lever radii follow the
-    stretched box.  The top layer (unit z > 0.95) carries a compressive force
-    equivalent to the nominal strain ``strain``: E * strain * (top area) spread
-    over the top sites; gravity acts on every free site.
+    The bond graph is that of the unit-cube foam ``base`` (default: the cached
+    foam of lattice size ``m`` and ``seed``); positions, cross sections, masses
+    and lever radii follow the stretched box.  The top layer (unit z > 0.95)
+    carries a compressive force equivalent to the nominal strain ``strain``:
+    E * strain * (top area) spread over the top sites; gravity acts on every
+    free site.
     """
     from .foam import gravity_load
-    base = _unit_foam(m, seed)
+    base = _unit_foam(m, seed) if base is None else base
     aspect = rng.uniform(.5, 2., 3) if aspect is None else np.asarray(aspect, dtype=float)
     young = float(np.exp(rng.uniform(np.log(1e4), np.log(1e6)))) if young is None else young
     poisson = float(rng.uniform(.2, .4)) if poisson is None else poisson
@@ -888,6 +879,38 @@ def compressed_foam_request(m, rng, *, aspect=None, young=None, poisson=None, st
     if top.any():
         load[top, 2] -= young*strain*aspect[0]*aspect[1]/top.sum()
     return foam, load
+
+
+def stream_plan(count, seed=0, sites=(1024, 131072), rate=None):
+    """Per-request parameters of a mixed-size stream in which every request has
+    its own foam: lattice size m (m^3 log-uniform in ``sites``, rounded to the
+    nearest lattice), foam seed, box aspect ratios U[0.5, 2], E log-uniform
+    [1e4, 1e6], nu U[0.2, 0.4], top strain U[1%, 10%] and a Poisson arrival
+    time at ``rate`` per second (None: all at t = 0).  The foams themselves
+    (the expensive part) are built from the plan by ``planned_stream``."""
+    rng = np.random.default_rng(seed)
+    arrival, plan = 0., []
+    for rid in range(count):
+        target = np.exp(rng.uniform(np.log(sites[0]), np.log(sites[1])))
+        m = max(2, int(round(target**(1/3))))
+        if rate:
+            arrival += float(rng.exponential(1./rate))
+        plan.append(dict(rid=rid, m=m, foam_seed=int(rng.integers(1 << 31)), aspect=rng.uniform(.5, 2., 3),
+                         young=float(np.exp(rng.uniform(np.log(1e4), np.log(1e6)))), poisson=float(rng.uniform(.2, .4)),
+                         strain=float(rng.uniform(.01, .1)), area_seed=int(rng.integers(1 << 31)), arrival=arrival))
+    return plan
+
+
+def planned_stream(plan, bases, steps=1):
+    """Requests of a ``stream_plan`` from their unit-cube foams ``bases``
+    (``bases[k]`` = ``jittered_lattice_foam(plan[k]['m'], seed=plan[k]['foam_seed'])``)."""
+    out = []
+    for spec, base in zip(plan, bases):
+        foam, load = compressed_foam_request(spec['m'], np.random.default_rng(spec['area_seed']), aspect=spec['aspect'],
+                                             young=spec['young'], poisson=spec['poisson'], strain=spec['strain'],
+                                             base=base)
+        out.append(Request(arrival=spec['arrival'], rid=spec['rid'], foam=foam, load=load, steps=steps))
+    return out
 
 
 def large_mix(big=128, small=32, count=64, seed=0, big_steps=10, dt=1e-3):

@@ -112,11 +112,12 @@ int dpf_stiffness_apply(const dpf_graph *g, const dpf_stiffness *k, const dpf_ta
  * 9 * DPF_STATIC_MAX_BONDS doubles (4.5 MiB) that every GPU which loads the
  * library holds until the process exits.  Graphs with more than
  * DPF_STATIC_MAX_BONDS bonds are rejected with DPF_ERR_TOO_LARGE before any
- * launch.  The first call on a device looks up the array's device address for
- * that device (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls on a device share the one array: calls whose work
- * overlaps on the GPU (concurrent streams, several host threads) race on it,
- * so serialise them.  The array keeps the last call's contents; every value a
+ * launch.  Every call looks up the array's device address on the current
+ * device (cudaGetSymbolAddress; the first lookup on a device loads the
+ * module there, so make the first call before any stream capture).  All
+ * calls on a device share the one array: calls whose work overlaps on the
+ * GPU (concurrent streams, several host threads) race on it, so serialise
+ * them.  The array keeps the last call's contents; every value a
  * call reads from it is written earlier in the same call, so nothing needs
  * clearing.  The function allocates nothing and frees nothing. */
 int dpf_stiffness_apply_static(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t,
@@ -262,6 +263,89 @@ int dpf_rhs_scale(int64_t n_sites, const double *mass, const double *v, const do
  * NewtonBonds.step (experiments/bonded_dem_newton.py:186-187). */
 int dpf_masked_scale(int64_t n_sites, const double *a, const double *units, const uint8_t *fixed,
                      double *out, void *stream);
+
+/* ---- Linear model and the previous solver (float64) ----
+ * out = (diag M + alpha K) q with identity rows on fixed sites; the operator
+ * of LinearBondsGPU._operator (experiments/bonded_dem_linear_gpu.py:74-77).
+ * wrench: dpf_wrench_scratch_doubles(M) doubles. */
+int dpf_operator_apply(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t, const double *mass,
+                       const uint8_t *fixed, double alpha, const double *q, double *out, double *wrench,
+                       void *stream);
+
+/* Block preconditioner of the linear solves: block = diag M + alpha diagonal
+ * per site (the identity on fixed sites; optional output) and
+ * preconditioner = block^-1, both (N, 6, 6) doubles; diagonal (N, 6, 6) are
+ * the K blocks.  Replaces the inverse in LinearBondsGPU.solve_increment
+ * (experiments/bonded_dem_linear_gpu.py:82-86) and
+ * FiniteBondsGPU.solve_increment (experiments/bonded_dem_finite_gpu.py:141-143). */
+int dpf_block_inverse(int64_t n_sites, const double *mass, const uint8_t *fixed, const double *diagonal, double alpha,
+                      double *block, double *preconditioner, void *stream);
+
+/* Doubles of the workspace of dpf_block_pcg for N sites. */
+int64_t dpf_block_pcg_workspace_doubles(int64_t n_sites);
+
+/* Block-Jacobi PCG on (diag M + alpha K) x = rhs (identity rows on fixed
+ * sites, rhs rows of fixed sites read as zero) in one cooperative launch.
+ * preconditioner: (N, 6, 6) block inverse.  mode 0 replaces
+ * LinearBondsGPU.solve_increment (experiments/bonded_dem_linear_gpu.py:79-112):
+ * starts from x (use_guess != 0; fixed rows zeroed) or zero, stops at the
+ * first 10th iteration with |r|/|rhs| < tolerance, and returns the true
+ * residual |rhs - A x|/|rhs|.  mode 1 replaces FiniteBondsGPU.solve_increment
+ * (experiments/bonded_dem_finite_gpu.py:133-167): starts from zero and, every
+ * 10th iteration with |r|/|rhs| < tolerance and max|P r / scale| < 2e-8,
+ * accepts when the true residual a satisfies |a|/|rhs| < 5 tolerance and
+ * max|P a / scale| < 1e-7 (scale (N, 6) required).  x (N, 6): guess in,
+ * solution out.  info (device, 4 doubles): [iterations, relative residual,
+ * state (0 converged, 1 iteration cap, 2 non-finite residual at a test),
+ * |rhs|]; a right-hand side below 1e-30 (mode 0) or 1e-40 (mode 1) gives
+ * x = 0 and 0 iterations.  workspace: dpf_block_pcg_workspace_doubles(N);
+ * barrier: 2 unsigned ints (device), zeroed by the call on its stream. */
+int dpf_block_pcg(const dpf_graph *g, const dpf_stiffness *k, const dpf_tangent *t, const double *mass,
+                  const uint8_t *fixed, const double *preconditioner, const double *scale, const double *rhs,
+                  double alpha, double tolerance, int max_iterations, int mode, int use_guess, double *x,
+                  double *info, double *wrench, double *workspace, unsigned *barrier, int *status, void *stream);
+
+/* Linear implicit midpoint (experiments/bonded_dem_linear_gpu.py:114-121):
+ * rhs = dt M v + dt^2/2 (external - kq) and guess = dt v; then, with the
+ * increment dq, v <- 2 dq/dt - v and q <- q + dq.  All (N, 6) doubles. */
+int dpf_linear_midpoint_rhs(int64_t n_sites, const double *mass, const double *v, const double *external,
+                            const double *kq, double dt, double *rhs, double *guess, void *stream);
+int dpf_linear_midpoint_advance(int64_t n_sites, const double *dq, double dt, double *v, double *q, void *stream);
+
+/* Doubles of the partials buffer of dpf_linear_sums and dpf_anderson_gram
+ * (zeroed once before first use; the kernels leave their counters at zero). */
+int64_t dpf_small_partials_doubles(void);
+
+/* out[0] = sum a.b (when a is given), out[1] = (sum m v^2 + sum q kq) / 2
+ * (when mass is given): the step work and LinearBondsGPU.energy
+ * (experiments/bonded_dem_linear_gpu.py:121, 123-124).  Device doubles. */
+int dpf_linear_sums(int64_t n_sites, const double *a, const double *b, const double *mass, const double *v,
+                    const double *q, const double *kq, double *out, double *partials, void *stream);
+
+/* Anderson mixing of the previous solver (experiments/bonded_dem_finite_gpu.py:215-229)
+ * over device history slots: iterates and corrections are (slots, N, 6)
+ * doubles, order[0..count) (host ints) lists the slots oldest first
+ * (2 <= count <= slots <= 8).  With dc_h = c_{h+1} - c_h and weights
+ * u = [1, 1, 1, radius x 3], dpf_anderson_gram writes the upper triangle of
+ * gram[h][l] = (u dc_h).(u dc_l) row by row, then proj[h] = (u dc_h).(u c_last)
+ * (device doubles); dpf_anderson_mix writes out = c_last - sum_h coef_h
+ * (dy_h + dc_h) and ORs 1 into *flag (device int) if an entry is not finite. */
+int dpf_anderson_gram(int64_t n_sites, const double *iterates, const double *corrections, int slots,
+                      const int32_t *order, int count, const double *radii, double *out, double *partials,
+                      void *stream);
+int dpf_anderson_mix(int64_t n_sites, const double *iterates, const double *corrections, int slots,
+                     const int32_t *order, int count, const double *coefficients, double *out, int *flag,
+                     void *stream);
+
+/* Self-test of the time-limited grid barrier every cooperative kernel here
+ * uses (no reference counterpart).  `blocks` blocks (1..64) each wait for
+ * blocks + missing arrivals: with missing = 0 they pass and add their count
+ * to *passed; with missing > 0 nobody can release the barrier, every wait
+ * gives up after timeout_ns (<= 2 s) and DPF_ERR_BARRIER_TIMEOUT is ORed
+ * into *status, and the kernel returns.  barrier (2 unsigned ints, zeroed
+ * by the call), status and passed are device memory. */
+int dpf_barrier_selftest(int blocks, int64_t timeout_ns, int missing, unsigned *barrier, int *status, int *passed,
+                         void *stream);
 
 /* ---- Mixed precision: float32 bond sweeps, float64 reductions and residual ----
  * One step of NewtonBonds.step (experiments/bonded_dem_newton.py:132-201) in
@@ -511,7 +595,8 @@ int dpf_tiled_hvp(const dpf_graph *g, const dpf_tiles *t, const float *entries, 
 /* Elastic PCG of dpf_mixed_precondition on the tiled operator, two grid
  * barriers per iteration (single-reduction recurrence); same stopping rule
  * and iteration accounting.  workspace: dpf_tiled_workspace_floats(N)
- * floats; partials: dpf_tiled_partials_doubles() doubles.  stages: tile
+ * floats; partials: dpf_tiled_partials_doubles() doubles; barrier: 2
+ * unsigned ints (device), zeroed by the call on its stream.  stages: tile
  * buffers per CTA (2..4; 0 = the deepest that fits). */
 int64_t dpf_tiled_workspace_floats(int64_t n_sites);
 int64_t dpf_tiled_partials_doubles(void);
@@ -541,7 +626,8 @@ int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const
 
 /* dpf_tiled_precondition on the bond-end operator (one cooperative launch;
  * workspace dpf_tiled_workspace_floats(N), partials
- * dpf_tiled_partials_doubles()).  seg_site/active (optional, for batches):
+ * dpf_tiled_partials_doubles(); barrier: 2 unsigned ints (device), zeroed
+ * by the call on its stream).  seg_site/active (optional, for batches):
  * a site s with active[seg_site[s]] == 0 skips its ends (its request's
  * vector is zero, so its rows stay zero). */
 int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,

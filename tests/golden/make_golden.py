@@ -3,7 +3,7 @@
 Run from the repository root in a container that has the reference checked
 out (read-only) and torch/numpy/scipy installed:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/reference [--only-linear-step]
 
 It imports ``experiments.bonded_dem_*`` from the reference with
 ``device='cpu'``, builds the fixtures of the reference's own check scripts
@@ -351,7 +351,51 @@ def main(reference):
     out['iterations'] = np.array(infos)
     np.savez_compressed(HERE/'lattice8.npz', **out)
     print('lattice8', infos)
+    linear_step(reference)
+
+
+def linear_step(reference):
+    """The linear implicit-midpoint step of ``bonded_dem_linear_gpu.checks``
+    (seed 217: 12 random points, complete graph, site 0 fixed, random load,
+    dt = 0.03), run by the reference's LinearBondsGPU on the CPU, with the
+    check's independent dense solve of the same step."""
+    sys.path.insert(0, str(reference))
+    import torch
+    torch.set_num_threads(1)
+    from experiments.bonded_dem_core import ParallelBonds
+    from experiments.bonded_dem_dynamics import reference_stiffness
+    from experiments.bonded_dem_linear_gpu import LinearBondsGPU
+    rng = np.random.default_rng(217)
+    p = rng.normal(size=(12, 3))
+    pairs = np.array([(i, j) for i in range(len(p)) for j in range(i+1, len(p))])
+    r = rng.uniform(.8, 1.2, len(p))
+    lengths = np.linalg.norm(p[pairs[:, 1]]-p[pairs[:, 0]], axis=1)
+    cpu = ParallelBonds(p, pairs, r, .12, 1200/lengths, 480/lengths)
+    k = reference_stiffness(cpu).toarray()
+    contacts = cpu.geometry(p)[1]
+    gpu = LinearBondsGPU(p, r, pairs, cpu.area, contacts, np.ones(len(p)), np.zeros(len(p), bool), device='cpu')
+    rng.normal(size=(len(p), 6))      # the K q probe vector of the check
+    gpu.fixed[0] = True
+    mass = gpu.mass.cpu().numpy().ravel()
+    free = np.arange(6, len(mass))
+    force = rng.normal(size=(len(p), 6))
+    force[0] = 0
+    dt = .03
+    dense = np.zeros(len(mass))
+    dense[free] = np.linalg.solve(np.diag(mass[free]) + dt*dt*k[np.ix_(free, free)]/4, .5*dt*dt*force.ravel()[free])
+    work, metrics = gpu.step(dt, gpu.tensor(force))
+    np.savez_compressed(HERE/'linear_step_217.npz', points=p, pairs=pairs, radii=r, areas=cpu.area, contacts=contacts,
+                        fixed=gpu.fixed.numpy(), force=force, dt=dt, dense_q=dense.reshape(-1, 6),
+                        step_q=gpu.q.numpy(), step_v=gpu.v.numpy(), step_kq=gpu.kq.numpy(), step_work=work,
+                        step_energy=gpu.energy(), step_iterations=metrics['iterations'],
+                        step_relative=metrics['relative_residual'])
+    print('linear_step_217', metrics, work)
 
 
 if __name__ == '__main__':
-    main(Path(sys.argv[1] if len(sys.argv) > 1 else os.environ['DPF_REFERENCE']))
+    args = [a for a in sys.argv[1:] if not a.startswith('--')]
+    where = Path(args[0] if args else os.environ['DPF_REFERENCE'])
+    if '--only-linear-step' in sys.argv:
+        linear_step(where)
+    else:
+        main(where)

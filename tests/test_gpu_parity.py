@@ -104,6 +104,34 @@ def test_tangent_81_and_linear_217():
     assert np.abs(host(s.diagonal) - g['diagonal']).max() < 1e-10
 
 
+def test_linear_step_217_matches_reference_and_dense_solve():
+    """LinearBonds.step (library PCG, linear stopping test) against the
+    reference's own step and the check's dense midpoint solve: positions
+    1e-6 of the dense solve and work = energy to 1e-6, as
+    bonded_dem_linear_gpu.py:144-155 asserts; the reference's step to 1e-10."""
+    import dpf_gb300
+    g = golden('linear_step_217')
+    p = g['points']
+    s = dpf_gb300.LinearBonds(p, g['radii'], g['pairs'], g['areas'], g['contacts'], np.ones(len(p)), g['fixed'])
+    work, metrics = s.step(float(g['dt']), s.tensor(g['force']))
+    assert rel(s.q, g['dense_q']) < 1e-6
+    assert rel(s.q, g['step_q']) < 1e-10
+    assert rel(s.v, g['step_v']) < 1e-10
+    assert rel(s.kq, g['step_kq']) < 1e-10
+    assert abs(work - float(g['step_work'])) <= 1e-10*abs(float(g['step_work']))
+    assert abs(s.energy() - work)/work < 1e-6
+    assert abs(metrics['iterations'] - int(g['step_iterations'])) <= 10
+    assert metrics['relative_residual'] < 5*2e-8
+    # the operator and the solve on their own: (diag M + a K) x = b
+    alpha = .25*float(g['dt'])**2
+    b = s.tensor(np.random.default_rng(1).normal(size=(len(p), 6)))
+    x, info = s.solve_increment(b, float(g['dt']))
+    r = s._operator(x, alpha) - b
+    r[s.fixed] = 0
+    assert float(torch.linalg.vector_norm(r)/torch.linalg.vector_norm(b[~s.fixed])) < 5*2e-8
+    assert info['relative_residual'] < 5*2e-8
+
+
 def test_finite_history_953_matches_parallel_bonds():
     import dpf_gb300
     g = golden('finite_953')

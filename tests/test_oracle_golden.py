@@ -76,6 +76,20 @@ def test_linear_217_against_dense_k():
     assert np.abs(k - g['dense_k']).max() < 1e-10
 
 
+def test_linear_step_217_matches_reference_and_dense_solve():
+    """The oracle's linear implicit-midpoint step against the reference's own
+    step and the dense solve of ``bonded_dem_linear_gpu.checks`` (1e-6 bar)."""
+    g = golden('linear_step_217')
+    p = g['points']
+    s = dem.LinearBonds(p, g['radii'], g['pairs'], g['areas'], g['contacts'], np.ones(len(p)), g['fixed'])
+    work, metrics = s.step(float(g['dt']), g['force'])
+    assert rel(s.q, g['step_q']) < 1e-12
+    assert rel(s.q, g['dense_q']) < 1e-6
+    assert abs(work - float(g['step_work'])) <= 1e-12*abs(float(g['step_work']))
+    assert abs(s.energy() - work)/work < 1e-6
+    assert metrics['iterations'] == int(g['step_iterations'])
+
+
 def test_tangent_81():
     g = golden('tangent_81')
     s = dem.LinearBonds(g['points'], np.ones(50), g['pairs'], np.ones(len(g['pairs'])), g['contacts'],
