@@ -5,20 +5,30 @@ Workload (one "step" = one Newton solve of one implicit-midpoint time step,
 ``NewtonBonds.step`` at relative residual 1e-6): a 64^3 jittered-lattice foam
 (262,144 sites, ~1.95M bonds; seeded synthetic input, generator in
 ``dynamic-powerfoam_gb300/foam.py``) with density 1000, gravity -9.81 z,
-bottom layer fixed, dt = 1e-3, successive steps of one trajectory.
+bottom layer fixed, dt = 1e-3, successive steps of one trajectory, solved by
+the mixed-precision form (float32 bond sweeps, float64 reductions and
+residual).
 
 Prints one JSON line.  ``value`` is solves/s with the load already in HBM;
 ``e2e`` is the same through the public API with the load copied from pinned
 host memory and the new positions copied back every step.  The working set
 (about 0.5 GB of bond state) is larger than L2, so no flush is needed.
+``accuracy`` holds every timed step's error against a float64 solve of the
+same inputs; ``served`` the mixed-size request stream (every request its own
+foam) against the plain float64 solver over the same requests; ``large_mix``
+the 128^3 foam served with 64 requests of 32^3 sites; ``adjoint`` the inverse
+material fit.  The foams of the served workloads are triangulated on the
+host in spawned worker processes (lowest priority) while the GPU measures
+the rest; every timed region starts after its inputs exist.
 
 ``--impl reference`` times the reference algorithm on the host CPU instead
-(the NumPy restatement in ``oracle/``, the reference code itself does not
-travel), on a bounded sample of the same workload.
+(the NumPy restatement in ``oracle/``; the reference code itself does not
+travel) on the same full foam, one solver process per host core.
 Multi-GPU (torchrun): independent replicas, one foam per rank, no collective
 on the data path; rank 0 prints the aggregate.
 """
 import argparse
+import importlib.util
 import json
 import os
 import statistics
@@ -32,11 +42,11 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture on
-# the 64^3 bench foam, profiles/end_pcg_hvp_64cube.txt): a bond-end PCG launch
-# of exactly 20 iterations, and one bond-end HVP launch.
-PCG_DRAM_BYTES_PER_ITERATION_64 = (4027809536 + 134359296)/20
-HVP_DRAM_BYTES_PER_LAUNCH_64 = 199288576 + 3624960
+# DRAM bytes per algorithmic byte of the bond-end PCG and HVP launches, from
+# one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 64^3
+# bench foam; applied to the algorithmic bytes of the measured size.
+PCG_TRAFFIC_PER_ALGORITHMIC_BYTE = 0.932
+HVP_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.537
 
 METRIC = 'implicit Newton solves/s at rel. residual 1e-6 (64^3 jittered foam, 262k sites, ~1.95M bonds)'
 UNIT = 'solves/s'
@@ -59,24 +69,66 @@ def parse():
     p.add_argument('--precision', default='mixed', choices=('mixed', 'f64'))
     p.add_argument('--plain-steps', type=int, default=3,
                    help='solves of the plain float64 solver timed beside the mixed one (0: skip)')
+    p.add_argument('--accuracy', type=int, default=1, help='check every timed step against float64 solves (0: skip)')
     p.add_argument('--hvp-launches', type=int, default=50, help='timed launches of the standalone HVP (0: skip)')
     p.add_argument('--profile-pcg', type=int, default=0,
                    help='run one elastic PCG launch of exactly this many iterations in an NVTX range "profile_pcg" '
                         '(for an ncu capture of its DRAM traffic)')
     p.add_argument('--adjoint-lattice', type=int, default=32, help='lattice size of the inverse-fit workload (0: skip)')
     p.add_argument('--adjoint-steps', type=int, default=50)
-    p.add_argument('--adjoint-fd', type=int, default=4, help='bonds checked against central differences')
+    p.add_argument('--adjoint-fd', type=int, default=16, help='bonds checked against central differences')
     p.add_argument('--served', type=int, default=512, help='requests of the served mixed-size stream (0: skip)')
-    p.add_argument('--large-mix', type=int, default=0,
+    p.add_argument('--served-plain', type=int, default=-1,
+                   help='requests of the same stream solved one at a time by the plain float64 solver (-1: all)')
+    p.add_argument('--served-accuracy', type=int, default=16,
+                   help='served requests checked against a float64 solve of the same request')
+    p.add_argument('--served-rate', type=float, default=4000., help='Poisson arrival rate of the stream (1/s)')
+    p.add_argument('--served-batch-sites', type=int, default=8_000_000, help='site capacity of one batch')
+    p.add_argument('--large-mix', type=int, default=128,
                    help='lattice size of the large served mix (128: one 128^3 foam for 10 steps with '
                         '--large-mix-count requests of 32^3 sites; 0: skip)')
     p.add_argument('--large-mix-count', type=int, default=64)
     p.add_argument('--large-mix-small', type=int, default=32)
-    p.add_argument('--served-plain', type=int, default=64,
-                   help='requests of the same stream solved one at a time by the plain float64 solver')
-    p.add_argument('--served-rate', type=float, default=4000., help='Poisson arrival rate of the stream (1/s)')
-    p.add_argument('--served-batch-sites', type=int, default=8_000_000, help='site capacity of one batch')
+    p.add_argument('--foam-workers', type=int, default=0, help='host processes triangulating foams (0: cores - 1)')
     return p.parse_args()
+
+
+def _foam_module():
+    """The foam generator alone (NumPy/SciPy), without the package or torch."""
+    spec = importlib.util.spec_from_file_location('_dpf_foam', os.path.join(ROOT, 'dynamic-powerfoam_gb300', 'foam.py'))
+    module = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(module)
+    return module
+
+
+def _foam_worker_init():
+    try:
+        os.nice(19)
+    except OSError:
+        pass
+
+
+def _foam_job(m, seed):
+    return _foam_module().jittered_lattice_foam(m, seed=seed)
+
+
+class FoamPool:
+    """Jittered-lattice foams triangulated on the host in spawned worker
+    processes at the lowest priority, so that the SciPy regular triangulation
+    of the served workloads runs while the GPU measures the others."""
+
+    def __init__(self, workers):
+        import multiprocessing
+        from concurrent.futures import ProcessPoolExecutor
+        self.workers = workers
+        self.executor = ProcessPoolExecutor(workers, mp_context=multiprocessing.get_context('spawn'),
+                                            initializer=_foam_worker_init)
+
+    def submit(self, m, seed):
+        return self.executor.submit(_foam_job, m, seed)
+
+    def close(self):
+        self.executor.shutdown(wait=True, cancel_futures=True)
 
 
 def foam_and_load(m, seed):
@@ -85,41 +137,54 @@ def foam_and_load(m, seed):
     return foam, dpf_gb300.gravity_load(foam)
 
 
-def corner_subfoam(foam, load):
-    """Sites with all unit coordinates < 1/2 (one eighth of the foam, same spacing)."""
-    keep = np.all(foam['unit'] < .5, axis=1)
-    index = -np.ones(len(keep), dtype=np.int64)
-    index[keep] = np.arange(keep.sum())
-    pairs = foam['pairs']
-    both = keep[pairs[:, 0]] & keep[pairs[:, 1]]
-    sub = dict(points=foam['points'][keep], radii=foam['radii'][keep], pairs=index[pairs[both]],
-               areas=foam['areas'][both], masses=foam['masses'][keep], fixed=foam['fixed'][keep],
-               young=foam['young'], shear=foam['shear'])
-    return sub, load[keep]
+def _single_thread_env():
+    for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
+        os.environ[var] = '1'
 
 
-def oracle_rate(foam, load, dt, tol, steps, warmup, budget_s):
-    """Solves/s of the NumPy reference restatement on the one-eighth corner sub-foam,
-    scaled to the full foam by bond count."""
+_WORKER = {}
+
+
+def _reference_worker_init(foam, load):
+    """Process-pool initializer: one NumPy reference solver of the full foam per worker."""
     from oracle import dem
-    sub, sload = corner_subfoam(foam, load)
-    s = dem.NewtonBonds(sub['points'], sub['radii'], sub['pairs'], sub['areas'], sub['masses'], sub['fixed'],
-                        young=sub['young'], shear=sub['shear'])
-    for _ in range(warmup):
-        s.step(dt, sload, tolerance=tol)
+    _WORKER['s'] = dem.NewtonBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
+                                   foam['fixed'], young=foam['young'], shear=foam['shear'])
+    _WORKER['load'] = load
+
+
+def _reference_worker_step(args):
+    """One Newton solve of the worker's own trajectory: (seconds, Newton, Krylov, CG)."""
+    dt, tol = args
     t0 = time.perf_counter()
-    done = 0
-    while done < steps:
-        s.step(dt, sload, tolerance=tol)
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
-            break
-    elapsed = time.perf_counter() - t0
-    scale = len(sub['pairs'])/len(foam['pairs'])
-    sample = (f'{done} Newton step(s) of the NumPy float64 restatement of NewtonBonds.step on the one-eighth '
-              f'corner sub-foam ({len(sub["points"])} sites, {len(sub["pairs"])} bonds, same spacing), '
-              f'{elapsed:.1f} s, solves/s scaled by the bond-count ratio {scale:.4f}')
-    return done/elapsed*scale, sample
+    _, info = _WORKER['s'].step(dt, _WORKER['load'], tolerance=tol)
+    return (time.perf_counter() - t0, info['nonlinear_iterations'], info['krylov_iterations'],
+            info['cg_iterations'])
+
+
+def reference_rate(foam, load, dt, tol, workers, warmup, steps):
+    """Solves/s of the NumPy restatement of ``NewtonBonds.step`` on the full
+    foam: ``workers`` spawned processes (one thread each) each advance their
+    own copy of the trajectory; ``warmup`` untimed solves, then ``steps`` timed
+    solves spread over the processes.  Returns (rate, per-solve iteration
+    means, sample text)."""
+    import multiprocessing
+    _single_thread_env()
+    with multiprocessing.get_context('spawn').Pool(workers, initializer=_reference_worker_init,
+                                                   initargs=(foam, load)) as pool:
+        if warmup:
+            pool.map(_reference_worker_step, [(dt, tol)]*min(warmup, workers), chunksize=1)
+        t0 = time.perf_counter()
+        rows = pool.map(_reference_worker_step, [(dt, tol)]*steps, chunksize=1)
+        elapsed = time.perf_counter() - t0
+    rows = np.array(rows)
+    iterations = dict(newton_per_solve=float(rows[:, 1].mean()), krylov_per_solve=float(rows[:, 2].mean()),
+                      cg_per_solve=float(rows[:, 3].mean()), seconds_per_solve=float(rows[:, 0].mean()))
+    sample = (f'{steps} Newton solve(s) of the NumPy float64 restatement of NewtonBonds.step on the full '
+              f'{len(foam["points"])}-site, {len(foam["pairs"])}-bond foam, {workers} single-threaded process(es) '
+              f'each advancing its own trajectory, {min(warmup, workers) if warmup else 0} untimed warm-up solve(s), '
+              f'{elapsed:.1f} s')
+    return steps/elapsed, iterations, sample
 
 
 class ClockSampler:
@@ -177,8 +242,7 @@ def run_hvp(s, dt, peak, peaks, launches=50):
     """Bond-HVPs/s of the float32 operator y = (diag M + dt^2/4 K) q of the
     elastic PCG (the bond-end sweep) on the bench foam: each launch timed
     alone with CUDA events on the launching stream, L2 flushed (a 256 MB
-    write) between launches; also back to back (the end records, 188 MB, are
-    larger than L2)."""
+    write) between launches; also back to back."""
     import ctypes
     import torch
     from dpf_gb300 import _lib
@@ -216,24 +280,25 @@ def run_hvp(s, dt, peak, peaks, launches=50):
     alg = 60*m + 56*n
     achieved = alg/(mean*1e-3)/1e9
     return dict(kernel='end_hvp_kernel', bond_hvps_per_s=m/(mean*1e-3), mean_ms=mean, min_ms=min(ms),
-                launches=len(ms), algorithmic_bytes=alg, traffic=HVP_DRAM_BYTES_PER_LAUNCH_64 if n == 262144 else None,
-                achieved=achieved, peak=peak, unit='GB/s',
-                frac=achieved/peak, peak_source='measured' if peaks else 'fallback', l2='flushed between launches',
+                launches=len(ms), algorithmic_bytes=alg, traffic=HVP_TRAFFIC_PER_ALGORITHMIC_BYTE*alg,
+                achieved=achieved, peak=peak, unit='GB/s', frac=achieved/peak,
+                peak_source='measured' if peaks else 'fallback', l2='flushed between launches',
                 back_to_back_ms=back_to_back, back_to_back_frac=alg/(back_to_back*1e-3)/1e9/peak,
                 end_records_bytes=int(s._ends.numel())*4)
 
 
 def run_adjoint(args, device):
     """Gradient of the inverse-fit loss by the adjoint (implicit-function
-    theorem, checkpoints every 10 steps), timed; checked against central
-    differences (h = 1e-4) of the loss in ``args.adjoint_fd`` random bonds."""
+    theorem, checkpoints every 10 steps), timed after one untimed forward and
+    backward pass; checked against central differences (h = 1e-4) of the loss
+    on ``args.adjoint_fd`` bonds (half uniformly drawn, half the largest
+    gradients)."""
     import torch
     steps, dt = args.adjoint_steps, 2e-3
     from dpf_gb300.adjoint import inverse_fit_problem
     model, theta0, loss = inverse_fit_problem(args.adjoint_lattice, 4, device, steps, dt, 10, 1e-12)
     theta = theta0.clone().requires_grad_(True)
-    with torch.no_grad():
-        loss(theta0)       # warm-up rollout (allocations, first launches), not timed
+    torch.autograd.grad(loss(theta), [theta])       # warm-up forward and backward, not timed
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     value = loss(theta)
@@ -248,15 +313,14 @@ def run_adjoint(args, device):
                         '(l=0.2, mean log 1e5, std 0.5), MSE of positions; adjoint with checkpoints every 10 steps',
                loss=float(value), forward_s=t1 - t0, backward_s=t2 - t1, forward_ms_per_step=1e3*(t1 - t0)/steps,
                backward_ms_per_step=1e3*(t2 - t1)/steps, gradient_norm=float(grad.norm()),
-               newton_tolerance=1e-12)
+               newton_tolerance=1e-12, warmup='one forward and backward pass')
     if args.adjoint_fd > 0:
         rng = np.random.default_rng(5)
-        # bonds with the largest gradients are the ones the loss sees best; mix
-        # them with uniformly random bonds
         bonds = np.unique(np.concatenate([rng.choice(len(theta0), args.adjoint_fd//2, replace=False),
                                           torch.topk(grad.abs(), args.adjoint_fd - args.adjoint_fd//2)
                                           .indices.cpu().numpy()]))
         h, errs, rows = 1e-4, [], []
+        t3 = time.perf_counter()
         with torch.no_grad():
             for b in bonds:
                 e = torch.zeros_like(theta0)
@@ -266,66 +330,27 @@ def run_adjoint(args, device):
                 errs.append(abs(fd - g)/max(abs(fd), 1e-300))
                 rows.append([int(b), g, fd])
         out.update(fd_bonds=len(bonds), fd_h=h, fd_max_relative_error=float(max(errs)),
-                   fd_median_relative_error=float(np.median(errs)), fd_samples=rows[:8])
+                   fd_median_relative_error=float(np.median(errs)), fd_samples=rows[:8],
+                   fd_seconds=time.perf_counter() - t3)
     return out
 
 
-def run_large_mix(args, device, peak, peaks):
-    """The large served mix: one jittered ``L^3`` foam under gravity (10 implicit
-    steps at dt = 1e-3) served together with requests of 32^3 sites (randomized
-    material, box and top load, one step each), all arriving at t = 0, under a
-    150 GB budget; then the bond-end HVP on the large foam alone."""
-    import torch
-    import dpf_gb300
-    from dpf_gb300 import serving
-    t = time.time()
-    reqs = serving.large_mix(big=args.large_mix, small=args.large_mix_small, count=args.large_mix_count,
-                             seed=args.seed)
-    build_s = time.time() - t
-    sites = sum(r.sites for r in reqs)
-    service = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=max(8_000_000, sites))
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    finished = service.run(reqs)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    ok = [r for r in finished if r.error is None]
-    solves = sum(r.done_steps for r in ok)
-    lat = np.array([r.finished - r.arrival for r in ok])
-    big = reqs[0]
-    out = dict(workload=f'{args.large_mix}^3 foam x 10 steps + {args.large_mix_count} x {args.large_mix_small}^3 '
-                        'requests, all at t = 0, 150 GB budget', requests=len(reqs), failed=len(reqs) - len(ok),
-               big_sites=big.sites, big_bonds=big.bonds, sites=sites, solves=solves, wall_s=wall,
-               solves_per_s=solves/wall, p50_ms=1e3*float(np.percentile(lat, 50)),
-               p99_ms=1e3*float(np.percentile(lat, 99)), batched_steps=service.batches,
-               phase_s={k: round(v, 4) for k, v in service.timers.items()}, foam_build_s=build_s,
-               max_relative_residual=float(max(i['nonlinear_relative_residual'] for r in ok for i in r.infos)))
-    del service, finished, ok
-    f = big.foam
-    s = dpf_gb300.MixedNewtonBonds(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
-                                   young=f['young'], shear=f['shear'], device=device)
-    s.step(big.dt, s.tensor(big.load), tolerance=args.tolerance)
-    out['hvp'] = run_hvp(s, big.dt, peak, peaks, launches=20)
-    del s
-    torch.cuda.empty_cache()
-    return out
-
-
-def run_served(args, device):
+def run_served(args, device, stream):
     """Served stream vs the plain float64 solver (one request at a time).
 
-    Stream: ``args.served`` requests, site counts log-uniform 1,024-131,072,
-    box aspect U[0.5, 2], E log-uniform [1e4, 1e6], nu U[0.2, 0.4], top strain
-    U[1%, 10%] (as a top load), Poisson arrivals; one implicit Newton solve per
-    request at relative residual 1e-6.  Served: continuous batching of mixed-
-    precision batched Newton steps under a 150 GB HBM budget.  Plain: float64
-    ``NewtonBonds`` constructed and solved per request in arrival order.
-    Latency = completion - arrival, request construction included in both arms.
+    Stream: ``args.served`` requests, each its own seeded jittered-lattice
+    foam with m^3 sites log-uniform in 1,024-131,072, box aspect U[0.5, 2],
+    E log-uniform [1e4, 1e6], nu U[0.2, 0.4], top strain U[1%, 10%] (as a top
+    load), Poisson arrivals; one implicit Newton solve per request at
+    relative residual 1e-6.  Served: continuous batching of mixed-precision
+    batched Newton steps under a 150 GB HBM budget.  Plain: float64
+    ``NewtonBonds`` constructed (on the device) and solved per request, in
+    arrival order, over the same requests.  Latency = completion - arrival.
     """
     import torch
     import dpf_gb300
     from dpf_gb300 import serving
-    stream = serving.synthetic_stream(args.served, seed=11, sites=(1024, 131072), rate=args.served_rate)
+    from dpf_gb300.accuracy import served_accuracy
     warm = serving.synthetic_stream(4, seed=12, sites=(1024, 4096))
     serving.Service(device=device).run(warm)
     torch.cuda.synchronize()
@@ -339,50 +364,87 @@ def run_served(args, device):
     served = dict(requests=len(stream), solved=len(ok), failed=len(stream) - len(ok), wall_s=wall,
                   solves_per_s=len(ok)/wall, p50_ms=1e3*stats['p50'], p99_ms=1e3*stats['p99'],
                   batched_steps=service.batches, sites=int(sum(r.sites for r in stream)),
+                  distinct_foams=len({id(r.foam['pairs']) for r in stream}),
                   phase_s={k: round(v, 4) for k, v in service.timers.items()},
                   batch_sizes=service.batch_sizes,
                   newton_per_solve=float(np.mean([r.infos[0]['nonlinear_iterations'] for r in ok])),
                   max_relative_residual=float(max(r.infos[0]['nonlinear_relative_residual'] for r in ok)))
-    del finished, ok, stream
+    served['accuracy'] = served_accuracy(finished, args.served_accuracy, device)
+    del finished, ok
     plain = None
-    if args.served_plain > 0:
-        stream = serving.synthetic_stream(args.served_plain, seed=11, sites=(1024, 131072), rate=args.served_rate)
-        lat = []
+    count = len(stream) if args.served_plain < 0 else min(args.served_plain, len(stream))
+    if count > 0:
+        requests = sorted(stream)[:count]
+        lat, build, solve = [], 0., 0.
         t0 = time.perf_counter()
-        for req in stream:
+        for req in requests:
             wait = req.arrival - (time.perf_counter() - t0)
             if wait > 0:
                 time.sleep(wait)
             f = req.foam
+            t1 = time.perf_counter()
             s = dpf_gb300.NewtonBonds(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
                                       young=f['young'], shear=f['shear'], device=device)
-            s.step(req.dt, s.tensor(req.load), tolerance=args.tolerance)
-            lat.append(time.perf_counter() - t0 - req.arrival)
+            ext = s.tensor(req.load)
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+            s.step(req.dt, ext, tolerance=args.tolerance)
+            t3 = time.perf_counter()
+            build += t2 - t1
+            solve += t3 - t2
+            lat.append(t3 - t0 - req.arrival)
+            del s, ext
         torch.cuda.synchronize()
         pwall = time.perf_counter() - t0
-        plain = dict(requests=len(stream), solves_per_s=len(stream)/pwall, p50_ms=1e3*float(np.percentile(lat, 50)),
-                     p99_ms=1e3*float(np.percentile(lat, 99)), dtype='f64', sample='first requests of the same stream')
+        plain = dict(requests=count, solves_per_s=count/pwall, p50_ms=1e3*float(np.percentile(lat, 50)),
+                     p99_ms=1e3*float(np.percentile(lat, 99)), dtype='f64', construction_s=build, solve_s=solve,
+                     solve_only_solves_per_s=count/solve,
+                     sample='every request of the same stream' if count == len(stream) else
+                     f'the first {count} requests of the same stream')
         served['speedup_vs_plain'] = served['solves_per_s']/plain['solves_per_s']
+        served['speedup_vs_plain_solve_only'] = served['solves_per_s']/plain['solve_only_solves_per_s']
     served['plain_f64'] = plain
     return served
 
 
-_WORKER = {}
-
-
-def _reference_worker_init(sub, sload):
-    """Process-pool initializer: one NumPy reference solver per worker process."""
-    from oracle import dem
-    _WORKER['s'] = dem.NewtonBonds(sub['points'], sub['radii'], sub['pairs'], sub['areas'], sub['masses'],
-                                   sub['fixed'], young=sub['young'], shear=sub['shear'])
-    _WORKER['load'] = sload
-
-
-def _reference_worker_step(args):
-    dt, tol = args
+def run_large_mix(args, device, peak, peaks, requests, build_s):
+    """The large served mix: one jittered ``L^3`` foam under gravity (10 implicit
+    steps at dt = 1e-3) served together with requests of 32^3 sites (each its
+    own foam; randomized material, box and top load, one step each), all
+    arriving at t = 0, under a 150 GB budget; then the bond-end HVP on the
+    large foam alone."""
+    import torch
+    import dpf_gb300
+    from dpf_gb300 import serving
+    from dpf_gb300.accuracy import served_accuracy
+    sites = sum(r.sites for r in requests)
+    service = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=max(8_000_000, sites))
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    _WORKER['s'].step(dt, _WORKER['load'], tolerance=tol)
-    return time.perf_counter() - t0
+    finished = service.run(requests)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ok = [r for r in finished if r.error is None]
+    solves = sum(r.done_steps for r in ok)
+    lat = np.array([r.finished - r.arrival for r in ok])
+    big = requests[0]
+    out = dict(workload=f'{args.large_mix}^3 foam x 10 steps + {args.large_mix_count} x {args.large_mix_small}^3 '
+                        'requests (each its own foam), all at t = 0, 150 GB budget', requests=len(requests),
+               failed=len(requests) - len(ok), big_sites=big.sites, big_bonds=big.bonds, sites=sites, solves=solves,
+               wall_s=wall, solves_per_s=solves/wall, p50_ms=1e3*float(np.percentile(lat, 50)),
+               p99_ms=1e3*float(np.percentile(lat, 99)), batched_steps=service.batches,
+               phase_s={k: round(v, 4) for k, v in service.timers.items()}, foam_build_s=build_s,
+               max_relative_residual=float(max(i['nonlinear_relative_residual'] for r in ok for i in r.infos)))
+    out['accuracy'] = served_accuracy(finished, 8, device)
+    del service, finished, ok
+    f = big.foam
+    s = dpf_gb300.MixedNewtonBonds(f['points'], f['radii'], f['pairs'], f['areas'], f['masses'], f['fixed'],
+                                   young=f['young'], shear=f['shear'], device=device)
+    s.step(big.dt, s.tensor(big.load), tolerance=args.tolerance)
+    out['hvp'] = run_hvp(s, big.dt, peak, peaks, launches=20)
+    del s
+    torch.cuda.empty_cache()
+    return out
 
 
 def replica_rates(ms, e_ms, steps, world, device='cpu'):
@@ -399,55 +461,65 @@ def replica_rates(ms, e_ms, steps, world, device='cpu'):
 
 
 def run_reference(args):
-    """The reference algorithm (NumPy restatement) on all host cores: one worker
-    process per core, each advancing its own copy of the one-eighth corner
-    sub-foam; a step is one Newton solve in every worker, solves/s scaled to
-    the full foam by bond count."""
-    import multiprocessing
+    """The reference algorithm (NumPy restatement of ``NewtonBonds.step``) on
+    all host cores, on the same full foam and solver settings as our arm:
+    one single-threaded process per core, each advancing its own copy of the
+    trajectory; K timed solves spread over the processes."""
     rank = int(os.environ.get('RANK', '0'))
     if rank != 0:
         return
     foam, load = foam_and_load(args.lattice, args.seed)
-    sub, sload = corner_subfoam(foam, load)
     cores = os.cpu_count() or 1
-    for var in ('OMP_NUM_THREADS', 'OPENBLAS_NUM_THREADS', 'MKL_NUM_THREADS'):
-        os.environ[var] = '1'
-    scale = len(sub['pairs'])/len(foam['pairs'])
-    with multiprocessing.get_context('spawn').Pool(cores, initializer=_reference_worker_init,
-                                                   initargs=(sub, sload)) as pool:
-        task = [(args.dt, args.tolerance)]*cores
-        for _ in range(max(1, min(args.warmup, 1))):
-            pool.map(_reference_worker_step, task)
-        t0 = time.perf_counter()
-        for _ in range(max(1, args.steps)):
-            pool.map(_reference_worker_step, task)
-        elapsed = time.perf_counter() - t0
     steps = max(1, args.steps)
-    rate = cores*steps/elapsed*scale
-    sample = (f'{steps} step(s) x {cores} worker processes, each one Newton step of the NumPy float64 '
-              f'restatement of NewtonBonds.step on the one-eighth corner sub-foam ({len(sub["points"])} sites, '
-              f'{len(sub["pairs"])} bonds, same spacing), {elapsed:.1f} s, solves/s scaled by the bond-count '
-              f'ratio {scale:.4f}')
+    rate, iterations, sample = reference_rate(foam, load, args.dt, args.tolerance, cores, args.warmup, steps)
     line = dict(impl='reference', metric=METRIC, value=rate, unit=UNIT, n_gpus=args.gpus, steps=args.steps,
                 warmup=args.warmup, ms_per_step=1e3/rate if rate else None, higher_is_better=True,
-                scaling='weak', vs_baseline=None, dtype='f64', data='synthetic',
-                config=dict(workload=f'{args.lattice}^3 jittered-lattice foam, gravity, bottom fixed, '
-                                     f'dt={args.dt}, NewtonBonds.step tol={args.tolerance}', lattice=args.lattice,
-                            sites=len(foam['points']), bonds=len(foam['pairs'])),
+                scaling='weak', vs_baseline=None, dtype='f64',
+                data='synthetic (seeded jittered-lattice foam; no dataset)',
+                config=_config(args, len(foam['points']), len(foam['pairs']), int(os.environ.get('WORLD_SIZE', '1'))),
+                iterations=iterations,
                 cpu_baseline=dict(value=rate, unit=UNIT, cores=cores, kind='port', sample=sample),
                 e2e=dict(value=rate, unit=UNIT, h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
 
 
+def _config(args, sites, bonds, world):
+    """The workload description, identical in both arms (each arm reports its
+    own iteration counts beside it)."""
+    return dict(workload=f'{args.lattice}^3 jittered-lattice foam, gravity, bottom fixed, dt={args.dt}, '
+                         f'NewtonBonds.step tol={args.tolerance}, fgmres+elastic PCG',
+                lattice=args.lattice, sites=sites, bonds=bonds, dt=args.dt, tolerance=args.tolerance,
+                parallelism=f'replicas{world}', l2='working set > L2 (no flush)')
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
-    import dpf_gb300
-    from dpf_gb300 import _lib
 
     world = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
+
+    # host triangulation of the served workloads starts first (largest first)
+    pool, large_jobs, served_jobs, plan = None, [], [], None
+    if world == 1 and (args.served > 0 or args.large_mix > 0) and args.precision == 'mixed':
+        from dpf_gb300 import serving
+        cores = os.cpu_count() or 2
+        pool = FoamPool(args.foam_workers or max(1, cores - 1))
+        t_pool = time.time()
+        if args.large_mix > 0:
+            large_jobs.append(pool.submit(args.large_mix, args.seed))
+            for k in range(args.large_mix_count):
+                large_jobs.append(pool.submit(args.large_mix_small, args.seed + 1 + k))
+        if args.served > 0:
+            plan = serving.stream_plan(args.served, seed=11, sites=(1024, 131072), rate=args.served_rate)
+            order = sorted(range(len(plan)), key=lambda k: -plan[k]['m'])
+            futures = {k: pool.submit(plan[k]['m'], plan[k]['foam_seed']) for k in order}
+            served_jobs = [futures[k] for k in range(len(plan))]
+
+    import dpf_gb300
+    from dpf_gb300 import _lib
+    from dpf_gb300.accuracy import restore, snapshot_state, trajectory_accuracy
     torch.cuda.set_device(local)
     device = torch.device('cuda', local)
     if world > 1:
@@ -474,9 +546,8 @@ def run_ours(args):
     host_load = torch.from_numpy(load).pin_memory()
     host_x = torch.empty((n_sites, 3), dtype=torch.float64).pin_memory()
     dev_load = torch.empty_like(ext)
-    # the end-to-end run below replays the same K steps from the same state
-    snapshot = {name: getattr(s, name).clone() for name in s.PHYSICAL_STATE}
-    snapshot_time = s.time
+    # the end-to-end run and the accuracy check replay the same K steps from the same state
+    snapshot = snapshot_state(s)
     with ClockSampler(local) as clocks:
         clocks.ready()
         barrier()
@@ -490,9 +561,7 @@ def run_ours(args):
         launches = _lib.LAUNCHES['count'] - launches0
 
         # end to end through the public API: pinned host load in, positions out, every step
-        for name, value in snapshot.items():
-            setattr(s, name, value.clone())
-        s.time = snapshot_time
+        restore(s, *snapshot)
         barrier()
         torch.cuda.synchronize()
         e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -510,12 +579,17 @@ def run_ours(args):
 
     # launch timing of the hot kernels: the same steps again with CUDA events
     # around every launch (kept out of the timed regions above)
+    restore(s, *snapshot)
     s.profile = {}
     profiled = [s.step(args.dt, ext, tolerance=args.tolerance)[1] for _ in range(args.steps)]
     torch.cuda.synchronize()
     profile, s.profile = s.profile, None
 
     ms, e_ms, value, e2e = replica_rates(ms, e_ms, args.steps, world, device)
+
+    accuracy = None
+    if args.accuracy and args.precision == 'mixed':
+        accuracy = trajectory_accuracy(s, foam, ext, args.dt, args.tolerance, args.steps, snapshot, device)
 
     # the plain float64 solver on the same foam, one step at a time (the comparator of the mixed and served forms)
     plain = None
@@ -570,12 +644,11 @@ def run_ours(args):
     if dominant:
         achieved = alg[dominant]/(kernels[dominant]['mean_ms']*1e-3)/1e9
         traffic = None
-        if dominant == 'pcg' and args.precision == 'mixed' and args.lattice == 64 and args.seed == 0 and \
-                PCG_DRAM_BYTES_PER_ITERATION_64:
-            traffic = PCG_DRAM_BYTES_PER_ITERATION_64*cg/pcg_launches
+        if dominant == 'pcg' and args.precision == 'mixed' and s.sweep == 'ends':
+            traffic = PCG_TRAFFIC_PER_ALGORITHMIC_BYTE*alg[dominant]
         roof = dict(bound='hbm', kernel=dominant, achieved=achieved, peak=peak, unit='GB/s', frac=achieved/peak,
                     traffic=traffic, algorithmic_bytes=alg[dominant],
-                    traffic_source='ncu capture of this workload, scaled by CG iterations per launch'
+                    traffic_source='ncu DRAM bytes per algorithmic byte of this launch on the 64^3 foam'
                     if traffic else None, peak_source='measured' if peaks else 'fallback',
                     launches=kernels[dominant]['launches'], mean_ms=kernels[dominant]['mean_ms'])
 
@@ -591,32 +664,47 @@ def run_ours(args):
         s._end_pcg(vec, out, 0.0, args.profile_pcg, its)
         torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
-    served = run_served(args, device) if args.served > 0 and args.precision == 'mixed' else None
+    del s
+    torch.cuda.empty_cache()
+    served = None
+    if served_jobs:
+        from dpf_gb300 import serving
+        bases = [job.result() for job in served_jobs]
+        stream = serving.planned_stream(plan, bases)
+        served = run_served(args, device, stream)
+        served['foam_pool_s'] = time.time() - t_pool
+        del stream, bases
     adjoint = run_adjoint(args, device) if args.adjoint_lattice > 0 and world == 1 else None
-    large = run_large_mix(args, device, peak, peaks) if args.large_mix > 0 and world == 1 else None
+    large = None
+    if large_jobs:
+        from dpf_gb300 import serving
+        foams = [job.result() for job in large_jobs]
+        build_s = time.time() - t_pool
+        requests = serving.large_mix_requests(foams[0], foams[1:], seed=args.seed)
+        large = run_large_mix(args, device, peak, peaks, requests, build_s)
+        del foams, requests
+    if pool is not None:
+        pool.close()
     if rank != 0:
         return
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        rate, sample = oracle_rate(foam, load, args.dt, args.tolerance, steps=1, warmup=0, budget_s=30.)
-        cpu = dict(value=rate, unit=UNIT, cores=1, kind='port', sample=sample)
+        rate, iterations, sample = reference_rate(foam, load, args.dt, args.tolerance, 1, 0, 1)
+        cpu = dict(value=rate, unit=UNIT, cores=1, kind='port', sample=sample, **iterations)
     mean = lambda k: sum(i[k] for i in infos)/len(infos)
+    iterations = dict(newton_per_solve=mean('nonlinear_iterations'), krylov_per_solve=mean('krylov_iterations'),
+                      cg_per_solve=mean('cg_iterations'))
+    config = _config(args, n_sites, n_bonds, world)
     line = dict(metric=METRIC, value=value, unit=UNIT, n_gpus=world, steps=args.steps, warmup=args.warmup,
                 ms_per_step=ms/args.steps, higher_is_better=True, scaling='weak', vs_baseline=None,
                 dtype='f32+f64' if args.precision == 'mixed' else 'f64',
-                data='synthetic (seeded jittered-lattice foam; no dataset)',
-                config=dict(workload=f'{args.lattice}^3 jittered-lattice foam, gravity, bottom fixed, dt={args.dt}, '
-                                     f'NewtonBonds.step tol={args.tolerance}, fgmres+elastic PCG, '
-                                     + ('float32 bond sweeps + float64 reductions/residual'
-                                        if args.precision == 'mixed' else 'float64'),
-                            lattice=args.lattice, sites=n_sites, bonds=n_bonds, parallelism=f'replicas{world}',
-                            l2='working set > L2 (no flush)',
-                            newton_per_solve=mean('nonlinear_iterations'),
-                            krylov_per_solve=mean('krylov_iterations'), cg_per_solve=mean('cg_iterations')),
+                data='synthetic (seeded jittered-lattice foam; no dataset)', config=config, iterations=iterations,
+                precision='float32 bond sweeps + float64 reductions/residual' if args.precision == 'mixed'
+                else 'float64',
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
                 gpu_launches=launches, kernels=kernels, roofline=roof, hvp=hvp, cpu_baseline=cpu, plain_f64=plain,
-                served=served, adjoint=adjoint, large_mix=large,
+                accuracy=accuracy, served=served, adjoint=adjoint, large_mix=large,
                 relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)

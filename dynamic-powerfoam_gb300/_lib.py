@@ -130,6 +130,7 @@ SIGNATURES = {
                                    P(ParallelState), vp, vp, vp, vp]),
     'dpf_parallel_loads': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_bond_energy': (i32, [P(Graph), vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_energy_tangent': (i32, [P(Graph), vp, vp, i64, vp, vp, vp, vp, vp, vp]),
     'dpf_adjoint_jacobian_doubles': (i64, [i64]),
     'dpf_adjoint_slot_doubles': (i64, [i64]),
     'dpf_adjoint_local_jacobian': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp]),
@@ -164,7 +165,7 @@ KERNELS = {
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
     'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_end_pack': 2, 'dpf_end_hvp': 1,
     'dpf_end_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
-    'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
+    'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
 }
 LAUNCHES = {'count': 0}

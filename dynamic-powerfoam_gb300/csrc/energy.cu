@@ -128,6 +128,40 @@ __global__ void __launch_bounds__(kThreads) site_forces_kernel(int64_t n, const 
         for (int c = 0; c < 3; ++c) torque[3 * s + c] = t[c];
 }
 
+// Frozen tangent of the bond potential at the current configuration, for
+// the Newton direction of the energy-law solver: the bond axis
+// n = (x_j - x_i) / |x_j - x_i|, the current contact point c (the mean of the
+// two body-attached contact points x_i + R_i r_i and x_j + R_j r_j), levers
+// c - x_i and c - x_j (so that r_i - r_j = L n exactly), and the bond
+// stiffnesses; written as the float32 tangent records (n, kn) (r_i, ks)
+// (r_j, kb) (kt, 0, 0, 0) that the bond-end sweep and the 6x6 block scaling
+// read.  At the reference configuration this is the stiffness of
+// LinearBondsGPU, the exact Hessian of the potential there.
+__global__ void __launch_bounds__(kThreads) energy_tangent_kernel(int64_t m, const int64_t *edges, const double *base,
+                                                                  const double *theta, int64_t theta_stride,
+                                                                  const double *x, const double *q, const double *ri0,
+                                                                  const double *rj0, float4 *t0, float4 *t1, float4 *t2,
+                                                                  float4 *t3) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= m) return;
+    int64_t i, j;
+    edge(edges, b, i, j);
+    const d3 xi = ld3(x, i), xj = ld3(x, j);
+    const M3 Ri = quat_matrix(q + 4 * i), Rj = quat_matrix(q + 4 * j);
+    const d3 c = 0.5 * ((xi + mul(Ri, ld3(ri0, b))) + (xj + mul(Rj, ld3(rj0, b))));
+    const d3 d = xj - xi;
+    const d3 n = d / norm(d);
+    const d3 ri = c - xi, rj = c - xj;
+    const double *ti = theta + theta_stride * i, *tj = theta + theta_stride * j;
+    const double *k0 = base + 4 * b;
+    const float kn = (float)(k0[0] * exp(0.5 * (ti[0] + tj[0]))), ks = (float)(k0[1] * exp(0.5 * (ti[1] + tj[1])));
+    const float kb = (float)(k0[2] * exp(0.5 * (ti[2] + tj[2]))), kt = (float)(k0[3] * exp(0.5 * (ti[3] + tj[3])));
+    t0[b] = make_float4((float)n.x, (float)n.y, (float)n.z, kn);
+    t1[b] = make_float4((float)ri.x, (float)ri.y, (float)ri.z, ks);
+    t2[b] = make_float4((float)rj.x, (float)rj.y, (float)rj.z, kb);
+    t3[b] = make_float4(kt, 0.0f, 0.0f, 0.0f);
+}
+
 }  // namespace energy
 }  // namespace dpf
 
@@ -162,6 +196,23 @@ int dpf_bond_energy(const dpf_graph *g, const double *base, const double *theta,
     if (want_forces)
         site_forces_kernel<<<(int)((g->n_sites + kThreads - 1) / kThreads), kThreads, 0, st>>>(
             g->n_sites, g->inc_ptr, g->inc_bond, wrench, force, torque);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_energy_tangent(const dpf_graph *g, const double *base, const double *theta, int64_t theta_stride,
+                       const double *x, const double *q, const double *ri0, const double *rj0, float *bond_data,
+                       void *stream) {
+    if (!g || g->n_sites <= 0 || g->n_bonds < 0 || !x || !q || theta_stride < 4 ||
+        (g->n_bonds && (!g->edges || !base || !theta || !ri0 || !rj0 || !bond_data)) ||
+        ((uintptr_t)bond_data & 15u))
+        return DPF_ERR_ARGUMENT;
+    const int64_t m = g->n_bonds;
+    if (m) {
+        float4 *p = reinterpret_cast<float4 *>(bond_data);
+        energy_tangent_kernel<<<(int)((m + kThreads - 1) / kThreads), kThreads, 0, (cudaStream_t)stream>>>(
+            m, g->edges, base, theta, theta_stride, x, q, ri0, rj0, p + 7 * m, p + 8 * m, p + 9 * m, p + 10 * m);
+    }
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -75,3 +75,224 @@ class EnergyFoam:
         """-dE/dx and -dE/d(world rotation), (n_sites, 3) each."""
         f, tau, _ = self._run(theta, x, q, True, False)
         return f, tau
+
+
+# ---------------------------------------------------------------------------
+# Line-searched Newton on the bond potential: static equilibrium and implicit
+# Euler steps.
+
+def rotation_quaternion(theta):
+    """Unit quaternions (w, x, y, z) of rotation vectors (N, 3)."""
+    angle = torch.linalg.vector_norm(theta, dim=1, keepdim=True)
+    half = .5*angle
+    # sin(t/2)/t, with its series below 1e-4
+    scale = torch.where(angle > 1e-4, torch.sin(half)/angle.clamp_min(1e-300), .5 - angle*angle/48)
+    return torch.cat((torch.cos(half), scale*theta), 1)
+
+
+def quaternion_product(a, b):
+    """Hamilton product a b of (N, 4) quaternions (w, x, y, z)."""
+    aw, ax, ay, az = a.unbind(1)
+    bw, bx, by, bz = b.unbind(1)
+    return torch.stack((aw*bw - ax*bx - ay*by - az*bz, aw*bx + ax*bw + ay*bz - az*by,
+                        aw*by - ax*bz + ay*bw + az*bx, aw*bz + ax*by - ay*bx + az*bw), 1)
+
+
+def left_jacobian_transpose_apply(theta, v):
+    """J_l(theta)^T v for the left Jacobian of SO(3), exp(theta + e) = exp(J_l e) exp(theta):
+    J_l^T v = v - a theta x v + b theta x (theta x v), a = (1 - cos t)/t^2,
+    b = (t - sin t)/t^3 (series below t = 1e-3)."""
+    t = torch.linalg.vector_norm(theta, dim=1, keepdim=True)
+    small = t < 1e-3
+    tt = t.clamp_min(1e-300)
+    a = torch.where(small, .5 - t*t/24, (1 - torch.cos(t))/(tt*tt))
+    b = torch.where(small, 1/6 - t*t/120, (t - torch.sin(t))/(tt*tt*tt))
+    c = torch.linalg.cross(theta, v, dim=1)
+    return v - a*c + b*torch.linalg.cross(theta, c, dim=1)
+
+
+class EnergyNewton:
+    """Line-searched Newton on the bond potential of ``EnergyFoam``
+    (``volume=False, kinematics='small'``: ``foam_dem_energy.py:303-315,
+    405-421, 797-811``) for static equilibrium and implicit-Euler steps.
+
+    Unknowns per site: a displacement u and a rotation vector t of the body
+    rotation relative to the start of the solve (q = exp(t) q_0).  Potentials:
+
+    * static: ``Pi(u, t) = E_b(X + u, exp(t) q_0) - f . u - tau . t``;
+    * implicit Euler (dt): ``Phi = sum m |u - dt v|^2 / (2 dt^2) +
+      sum I |t - dt w|^2 / (2 dt^2) + Pi``, after which v = u / dt, w = t / dt.
+
+    Sites flagged ``fixed`` are held (static: at ``prescribed`` displacements,
+    rotation held); their rows are removed from the gradient.  Each Newton
+    direction solves ``(M/dt^2 + K) d = -g`` (static: ``K d = -g``) by the
+    float32 block-Jacobi PCG over the bond-end sweep, with K the frozen tangent
+    of the potential at the current configuration (``dpf_energy_tangent``; at
+    the reference configuration K is the exact Hessian).  The step length
+    follows an Armijo backtracking search on the float64 potential; the
+    gradient (float64 forces and torques, ``dpf_bond_energy``; the rotation
+    rows ``-J_l(t)^T tau``) decides convergence: ``|g| <= tolerance * scale``
+    with scale the larger of the first gradient norm and |external load|.
+    """
+
+    def __init__(self, geometry, young=1200., shear=480., device='cuda', theta=None, inner_tolerance=1e-2,
+                 inner_iterations=200):
+        self.law = EnergyFoam(geometry, volume=False, young=young, shear=shear, device=device)
+        b = self.law._bonds
+        self.device, self._lib = b.device, b._lib
+        n, m = b.n_sites, b.n_bonds
+        self.n_sites, self.n_bonds = n, m
+        f64, f32, dev = F64, torch.float32, self.device
+        self.theta = torch.zeros((n, 4), dtype=f64, device=dev) if theta is None else \
+            torch.as_tensor(theta, dtype=f64, device=dev).contiguous()
+        self.X = self.law.X
+        self.x = self.X.clone()
+        self.q = torch.zeros((n, 4), dtype=f64, device=dev)
+        self.q[:, 0] = 1.
+        self.v = torch.zeros((n, 3), dtype=f64, device=dev)
+        self.w = torch.zeros((n, 3), dtype=f64, device=dev)
+        self.fixed = b.fixed
+        self.mass, self.inertia = self.law.mass, self.law.inertia
+        self.inner_tolerance, self.inner_iterations = inner_tolerance, inner_iterations
+        lib = self._lib
+        self._bond_data = torch.zeros(max(4, lib.dpf_mixed_bond_floats(m)), dtype=f32, device=dev)
+        self._ends = torch.empty(max(4, lib.dpf_end_floats(m)), dtype=f32, device=dev)
+        self._mass32 = torch.cat((self.mass[:, None].expand(n, 3), self.inertia[:, None].expand(n, 3)), 1).float()
+        self._zero32 = torch.zeros((n, 6), dtype=f32, device=dev)
+        eye = torch.eye(6, dtype=f32, device=dev)
+        self._identity32 = eye.expand(n, 6, 6).contiguous()
+        self._ones32 = torch.ones((n, 6), dtype=f32, device=dev)
+        self._block32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
+        self._p32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
+        self._units = torch.empty((n, 6), dtype=f64, device=dev)
+        self._units32 = torch.empty((n, 6), dtype=f32, device=dev)
+        self._site4 = torch.empty((n, 4), dtype=f32, device=dev)
+        self._p24 = torch.empty(24*n, dtype=f32, device=dev)
+        self._workspace = torch.empty(lib.dpf_tiled_workspace_floats(n), dtype=f32, device=dev)
+        self._partials = torch.zeros(lib.dpf_tiled_partials_doubles(), dtype=f64, device=dev)
+        self._cg = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._barrier = torch.zeros(2, dtype=torch.int32, device=dev)
+        self._status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.time = 0.
+
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _evaluate(self, x0, q0, u, t, load, inertia):
+        """Potential and its gradient (N, 6) at (u, t); fixed rows of the gradient zeroed."""
+        law = self.law
+        x = x0 + u
+        q = quaternion_product(rotation_quaternion(t), q0)
+        f, tau, e = law._run(self.theta, x, q, True, True)
+        g = torch.cat((-f - load[:, :3], -left_jacobian_transpose_apply(t, tau) - load[:, 3:]), 1)
+        phi = e[0] - (load[:, :3]*u).sum() - (load[:, 3:]*t).sum()
+        if inertia is not None:
+            dt, v, w = inertia
+            du, dw = u - dt*v, t - dt*w
+            g[:, :3] += self.mass[:, None]*du/(dt*dt)
+            g[:, 3:] += self.inertia[:, None]*dw/(dt*dt)
+            phi = phi + .5*((self.mass[:, None]*du*du).sum() + (self.inertia[:, None]*dw*dw).sum())/(dt*dt)
+        g[self.fixed] = 0.
+        return float(phi), g, x, q
+
+    def _direction(self, x, q, g, inertia):
+        """d with (M/dt^2 + K) d = -g (static: K d = -g) by the float32 bond-end PCG."""
+        b = self.law._bonds
+        stream = self._stream()
+        _lib.check(self._lib.dpf_energy_tangent(ctypes.byref(b._graph), self.law.base.data_ptr(),
+                                                self.theta.data_ptr(), self.theta.shape[1], x.data_ptr(),
+                                                q.data_ptr(), self.law.ri.data_ptr(), self.law.rj.data_ptr(),
+                                                self._bond_data.data_ptr(), stream), 'dpf_energy_tangent')
+        # operator diag(mass32) + alpha K: alpha = dt^2 (the system times dt^2) or 1 (static)
+        if inertia is None:
+            mass32, alpha, rhs = self._zero32, 1., -g
+        else:
+            dt = inertia[0]
+            mass32, alpha, rhs = self._mass32, dt*dt, -(dt*dt)*g
+        # dpf_mixed_scaling takes the midpoint step: its alpha is dt'^2/4
+        _lib.check(self._lib.dpf_mixed_scaling(ctypes.byref(b._graph), self._bond_data.data_ptr(), mass32.data_ptr(),
+                                               self.fixed.data_ptr(), b._site_radii.data_ptr(), 2.*alpha**.5,
+                                               self._block32.data_ptr(), self._p32.data_ptr(), self._units.data_ptr(),
+                                               self._units32.data_ptr(), stream), 'dpf_mixed_scaling')
+        _lib.check(self._lib.dpf_end_pack(ctypes.byref(b._graph), self._bond_data.data_ptr(), alpha,
+                                          self._p32.data_ptr(), mass32.data_ptr(), self.fixed.data_ptr(),
+                                          self._ends.data_ptr(), self._p24.data_ptr(), self._site4.data_ptr(),
+                                          stream), 'dpf_end_pack')
+        rhs = rhs.contiguous()
+        out = torch.empty_like(rhs)
+        _lib.check(self._lib.dpf_end_precondition(
+            ctypes.byref(b._graph), self._ends.data_ptr(), self._site4.data_ptr(), self.fixed.data_ptr(),
+            self._identity32.data_ptr(), self._p24.data_ptr(), self._ones32.data_ptr(), rhs.data_ptr(),
+            float(self.inner_tolerance), int(self.inner_iterations), out.data_ptr(), self._cg.data_ptr(),
+            self._workspace.data_ptr(), self._partials.data_ptr(), self._barrier.data_ptr(), self._status.data_ptr(),
+            None, None, stream), 'dpf_end_precondition')
+        out[self.fixed] = 0.
+        return out
+
+    def _minimize(self, load, prescribed, inertia, tolerance, max_iterations):
+        load = torch.as_tensor(load, dtype=F64, device=self.device).reshape(self.n_sites, 6)
+        load = load.masked_fill(self.fixed[:, None], 0.)
+        x0, q0 = self.x, self.q
+        u = torch.zeros_like(x0)
+        if prescribed is not None:
+            prescribed = torch.as_tensor(prescribed, dtype=F64, device=self.device).reshape(self.n_sites, 3)
+            u = torch.where(self.fixed[:, None], prescribed, u)
+        t = torch.zeros_like(x0)
+        self._cg.zero_()
+        self._status.zero_()
+        phi, g, x, q = self._evaluate(x0, q0, u, t, load, inertia)
+        gnorm = float(torch.linalg.vector_norm(g))
+        scale = max(gnorm, float(torch.linalg.vector_norm(load)), 1e-300)
+        trace = [gnorm/scale]
+        for iteration in range(max_iterations + 1):
+            if gnorm <= tolerance*scale:
+                return u, t, x, q, dict(newton_iterations=iteration, relative_gradient=gnorm/scale,
+                                        cg_iterations=int(self._cg.item()), gradient_trace=trace, energy=phi)
+            if iteration == max_iterations:
+                break
+            d = self._direction(x, q, g, inertia)
+            slope = float((g*d).sum())
+            if not slope < 0:                      # not a descent direction: precondition the gradient only
+                d = -g
+                slope = -gnorm*gnorm
+            du, dtheta = d[:, :3], d[:, 3:]
+            step, accepted = 1., False
+            for _ in range(30):
+                cand = self._evaluate(x0, q0, u + step*du, t + step*dtheta, load, inertia)
+                cnorm = float(torch.linalg.vector_norm(cand[1]))
+                drop = cand[0] - phi
+                if drop <= 1e-4*step*slope or (abs(drop) <= 1e-13*max(abs(phi), 1.) and cnorm < gnorm):
+                    accepted = True
+                    break
+                step *= .5
+            if not accepted:
+                raise RuntimeError(f'energy Newton line search failed at relative gradient {gnorm/scale:g}')
+            u, t = u + step*du, t + step*dtheta
+            phi, g, x, q = cand
+            gnorm = cnorm
+            trace.append(gnorm/scale)
+        if int(self._status.item()):
+            raise RuntimeError(f'device status {int(self._status.item()):#x}')
+        raise RuntimeError(f'energy Newton did not converge ({gnorm/scale:g})')
+
+    @torch.no_grad()
+    def solve(self, load=None, prescribed=None, tolerance=1e-10, max_iterations=60):
+        """Static equilibrium under ``load`` (N, 6) [force, torque] with the
+        fixed sites held at ``prescribed`` (N, 3) displacements from the
+        current positions (rows of free sites ignored; None: held in place);
+        the state moves to the equilibrium.  Returns info."""
+        load = torch.zeros((self.n_sites, 6), dtype=F64, device=self.device) if load is None else load
+        u, t, x, q, info = self._minimize(load, prescribed, None, tolerance, max_iterations)
+        self.x, self.q = x, q
+        return info
+
+    @torch.no_grad()
+    def step(self, dt, load, tolerance=1e-10, max_iterations=40):
+        """One implicit-Euler step of length dt under ``load`` (N, 6); returns info."""
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('Positive finite dt required')
+        u, t, x, q, info = self._minimize(load, None, (float(dt), self.v, self.w), tolerance, max_iterations)
+        self.v, self.w = u/dt, t/dt
+        self.x, self.q = x, q
+        self.time += dt
+        return info

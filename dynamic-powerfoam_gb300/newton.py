@@ -165,25 +165,25 @@ class LinearBonds:
         None), kn = E A/L, ks = G A/L, kb = E I/L, kt = 2 G I/L with I = A^2/(4 pi),
         and the (N, 6) mass [m, m, m, 0.4 m r^2 x 3].  Returns the contact offsets
         (contacts - classical)."""
-        p = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        p = np.array(points, dtype=np.float64).reshape(-1, 3)
         n = len(p)
-        edges = np.ascontiguousarray(pairs, dtype=np.int64).reshape(-1, 2)
+        edges = np.array(pairs, dtype=np.int64).reshape(-1, 2)
         m = len(edges)
         if m and (edges.min() < 0 or edges.max() >= n):
             raise ValueError('Invalid endpoint index')
-        r = np.broadcast_to(np.asarray(radii, dtype=np.float64), (n,))
-        mass = np.broadcast_to(np.asarray(masses, dtype=np.float64), (n,))
+        r = np.array(np.broadcast_to(np.asarray(radii, dtype=np.float64), (n,)))
+        mass = np.array(np.broadcast_to(np.asarray(masses, dtype=np.float64), (n,)))
         if np.any(mass <= 0) or np.any(.4*mass*r*r <= 0):
             raise ValueError('Only positive-mass bodies can enter this solver')
-        area = np.broadcast_to(np.asarray(areas, dtype=np.float64), (m,))
+        area = np.array(np.broadcast_to(np.asarray(areas, dtype=np.float64), (m,)))
         dev = self.device
         self.p = self.tensor(p)
         self.edges = torch.as_tensor(edges, device=dev).contiguous()
         self.i, self.j = self.edges.T
-        self._site_radii = self.tensor(np.ascontiguousarray(r))
-        mass_d = self.tensor(np.ascontiguousarray(mass))
-        area_d = self.tensor(np.ascontiguousarray(area))
-        contacts_d = None if contacts is None else self.tensor(np.asarray(contacts, dtype=np.float64).reshape(-1, 3))
+        self._site_radii = self.tensor(r)
+        mass_d = self.tensor(mass)
+        area_d = self.tensor(area)
+        contacts_d = None if contacts is None else self.tensor(np.array(contacts, dtype=np.float64).reshape(-1, 3))
         e = lambda *shape: torch.empty(shape, dtype=F64, device=dev)
         self.n, self.ri, self.rj, offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)
         self.kn, self.ks, self.kb, self.kt = e(m), e(m), e(m), e(m)
@@ -193,7 +193,7 @@ class LinearBonds:
                    float(young), float(shear), None, None, self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr(),
                    self.kn.data_ptr(), self.ks.data_ptr(), self.kb.data_ptr(), self.kt.data_ptr(), offset.data_ptr(),
                    self.mass.data_ptr(), self._stream())
-        self.fixed = torch.as_tensor(np.ascontiguousarray(fixed, dtype=bool), device=dev)
+        self.fixed = torch.as_tensor(np.array(fixed, dtype=bool), device=dev)
         return offset
 
     # ---- plumbing ---------------------------------------------------------

@@ -929,6 +929,23 @@ def large_mix(big=128, small=32, count=64, seed=0, big_steps=10, dt=1e-3):
     return out
 
 
+def large_mix_requests(big_foam, small_bases, seed=0, big_steps=10, dt=1e-3):
+    """The large served mix from prepared foams: ``big_foam`` (a jittered
+    lattice foam) under gravity with its bottom layer fixed for ``big_steps``
+    implicit steps, and one request per unit-cube foam of ``small_bases``
+    (each its own foam; randomized E, nu, box and top load as in
+    ``stream_plan``, one step each), all arriving at t = 0."""
+    from .foam import gravity_load
+    rng = np.random.default_rng(seed)
+    big_foam = dict(big_foam, contacts=None)
+    out = [Request(arrival=0., rid=0, foam=big_foam, load=gravity_load(big_foam), dt=dt, steps=big_steps)]
+    for rid, base in enumerate(small_bases, 1):
+        m = round(len(base['points'])**(1/3))
+        f, load = compressed_foam_request(m, rng, base=base)
+        out.append(Request(arrival=0., rid=rid, foam=f, load=load, dt=dt, steps=1))
+    return out
+
+
 def synthetic_stream(count, seed=0, sites=(1024, 131072), rate=None, buckets=8, steps=1):
     """Mixed-size requests: site counts log-uniform in ``sites`` (rounded to
     ``buckets`` lattice sizes so that bond graphs are generated once per size),

@@ -657,6 +657,18 @@ int dpf_bond_energy(const dpf_graph *g, const double *base, const double *theta,
                     double *force, double *torque, double *energy, double *wrench, double *partials,
                     void *stream);
 
+/* Frozen tangent of the bond potential at the configuration (x, q) for the
+ * Newton direction of the energy-law solver (no reference counterpart; at the
+ * reference configuration it is the LinearBondsGPU stiffness, the exact
+ * Hessian there, foam_dem_energy.py:14-16): bond axis n = (x_j - x_i)/L,
+ * contact point c = ((x_i + R_i ri0) + (x_j + R_j rj0))/2, levers c - x_i,
+ * c - x_j, stiffness base * exp((theta_i + theta_j)/2); written into the
+ * float32 tangent part of bond_data (dpf_mixed_bond_floats(M) floats,
+ * 16-byte aligned) that dpf_mixed_scaling and dpf_end_pack read. */
+int dpf_energy_tangent(const dpf_graph *g, const double *base, const double *theta, int64_t theta_stride,
+                       const double *x, const double *q, const double *ri0, const double *rj0, float *bond_data,
+                       void *stream);
+
 /* ---- Parallel-bond component with brittle failure ----
  * Replaces ParallelBonds.advance / loads (experiments/bonded_dem_core.py:132-208).
  * Per bond: stiffnesses kn = kbar_n A, ks = kbar_s A, kb = kbar_n I, kt = kbar_s J,

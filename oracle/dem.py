@@ -902,3 +902,151 @@ class ParallelBonds:
         self.time += dt
         return dict(newly_broken=int(broken.sum()), energy=float(self.elastic_energy_per_bond().sum()),
                     removed_bond_energy=float(self.break_energy.sum()))
+
+
+# ---------------------------------------------------------------------------
+# Line-searched Newton on the bond potential (static equilibrium and implicit
+# Euler).  The reference integrates EnergyFoam explicitly; these minimisations
+# of its bond potential (foam_dem_energy.py:303-315, 405-421, 797-811) are
+# restated here in NumPy with exact sparse solves so that the CUDA solver's
+# minimiser can be checked.  Unknowns per site: displacement u and rotation
+# vector t with q = exp(t) q0.
+
+def rotation_quaternion(t):
+    """Unit quaternions (w, x, y, z) of rotation vectors (N, 3)."""
+    angle = np.linalg.norm(t, axis=1, keepdims=True)
+    with np.errstate(invalid='ignore', divide='ignore'):
+        scale = np.where(angle > 1e-4, np.sin(.5*angle)/np.where(angle > 0, angle, 1.), .5 - angle*angle/48)
+    return np.concatenate((np.cos(.5*angle), scale*t), 1)
+
+
+def quaternion_product(a, b):
+    """Hamilton product of (N, 4) quaternions (w, x, y, z)."""
+    aw, ax, ay, az = a.T
+    bw, bx, by, bz = b.T
+    return np.stack((aw*bw - ax*bx - ay*by - az*bz, aw*bx + ax*bw + ay*bz - az*by,
+                     aw*by - ax*bz + ay*bw + az*bx, aw*bz + ax*by - ay*bx + az*bw), 1)
+
+
+def left_jacobian_transpose_apply(t, v):
+    """J_l(t)^T v, exp(t + e) = exp(J_l(t) e) exp(t)."""
+    a_ = np.linalg.norm(t, axis=1, keepdims=True)
+    small = a_ < 1e-3
+    s = np.where(small, 1., a_)
+    a = np.where(small, .5 - a_*a_/24, (1 - np.cos(a_))/(s*s))
+    b = np.where(small, 1/6 - a_*a_/120, (a_ - np.sin(a_))/(s*s*s))
+    c = cross(t, v)
+    return v - a*c + b*cross(t, c)
+
+
+def bond_blocks(n, ri, rj, kn, ks, kb, kt):
+    """Per-bond 12 x 12 stiffness B^T D B + A^T H A (bonded_dem_dynamics.py:22-47)."""
+    count = len(n)
+    b, a = np.zeros((count, 3, 12)), np.zeros((count, 3, 12))
+    b[:, :, :3], b[:, :, 3:6] = -np.eye(3), skew(ri)
+    b[:, :, 6:9], b[:, :, 9:12] = np.eye(3), -skew(rj)
+    a[:, :, 3:6], a[:, :, 9:12] = -np.eye(3), np.eye(3)
+    nn = n[:, :, None]*n[:, None, :]
+    dd = ks[:, None, None]*np.eye(3) + (kn-ks)[:, None, None]*nn
+    hh = kb[:, None, None]*np.eye(3) + (kt-kb)[:, None, None]*nn
+    return np.einsum('eai,eab,ebj->eij', b, dd, b) + np.einsum('eai,eab,ebj->eij', a, hh, a)
+
+
+def sparse_stiffness(n_sites, pairs, n, ri, rj, kn, ks, kb, kt):
+    """The 6N x 6N stiffness of ``bond_blocks`` as a SciPy CSR matrix."""
+    import scipy.sparse as sp
+    i, j = np.asarray(pairs).T
+    local = bond_blocks(n, ri, rj, kn, ks, kb, kt)
+    idx = np.concatenate((6*i[:, None] + np.arange(6), 6*j[:, None] + np.arange(6)), 1)
+    rows = np.repeat(idx, 12, axis=1).ravel()
+    cols = np.tile(idx, (1, 12)).ravel()
+    return sp.coo_matrix((local.ravel(), (rows, cols)), shape=(6*n_sites, 6*n_sites)).tocsr()
+
+
+def energy_tangent(bonds, theta, x, q):
+    """Frozen tangent of the bond potential at (x, q): axis n = (x_j - x_i)/L,
+    contact point c = ((x_i + R_i r_i) + (x_j + R_j r_j))/2, levers c - x_i,
+    c - x_j, stiffness base exp((theta_i + theta_j)/2)."""
+    R = quat_matrix(q)
+    i, j = bonds.i, bonds.j
+    ci = x[i] + np.einsum('bij,bj->bi', R[i], bonds.ri)
+    cj = x[j] + np.einsum('bij,bj->bi', R[j], bonds.rj)
+    c = .5*(ci + cj)
+    d = x[j] - x[i]
+    n = d/np.linalg.norm(d, axis=1)[:, None]
+    k = bonds.base*np.exp(.5*(theta[i, :4] + theta[j, :4]))
+    return n, c - x[i], c - x[j], k
+
+
+def energy_newton(bonds, theta, x0, q0, load, fixed, prescribed=None, inertia=None, tolerance=1e-10,
+                  max_iterations=60):
+    """Minimise the bond potential over (u, t) (static: E_b - f . u - tau . t;
+    implicit Euler with inertia = (dt, v, w): plus sum m |u - dt v|^2/(2 dt^2)
+    + sum I |t - dt w|^2/(2 dt^2)).  Fixed sites are held at ``prescribed``
+    displacements with their rotation held.  Newton directions solve the
+    frozen-tangent system exactly (sparse LU on the free DOFs); Armijo
+    backtracking on the potential; stop at |g| <= tolerance * scale, scale the
+    largest of the first gradient norm, |load| and the roundoff level of the
+    bond forces divided by the tolerance.  Returns (u, t, info)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    n_sites = len(x0)
+    fixed = np.asarray(fixed, dtype=bool)
+    load = np.where(fixed[:, None], 0., np.asarray(load, dtype=np.float64))
+    free = np.flatnonzero(~np.repeat(fixed, 6))
+    u = np.zeros((n_sites, 3))
+    if prescribed is not None:
+        u[fixed] = np.asarray(prescribed, dtype=np.float64)[fixed]
+    t = np.zeros((n_sites, 3))
+
+    def evaluate(u, t):
+        x = x0 + u
+        q = quaternion_product(rotation_quaternion(t), q0)
+        e = bonds.energy(theta, x, q)
+        f, tau = bonds.forces(theta, x, q)
+        g = np.concatenate((-f - load[:, :3], -left_jacobian_transpose_apply(t, tau) - load[:, 3:]), 1)
+        phi = e - (load[:, :3]*u).sum() - (load[:, 3:]*t).sum()
+        if inertia is not None:
+            dt, v, w = inertia
+            du, dw = u - dt*v, t - dt*w
+            g[:, :3] += bonds.mass[:, None]*du/(dt*dt)
+            g[:, 3:] += bonds.inertia[:, None]*dw/(dt*dt)
+            phi += .5*((bonds.mass[:, None]*du*du).sum() + (bonds.inertia[:, None]*dw*dw).sum())/(dt*dt)
+        g[fixed] = 0.
+        return phi, g, x, q
+
+    phi, g, x, q = evaluate(u, t)
+    gnorm = np.linalg.norm(g)
+    # floor: the roundoff level of bond forces (1e-13 of the stiffest bond times the largest coordinate)
+    floor = 1e-13*float(bonds.base[:, 0].max(initial=0.))*float(np.abs(x0).max(initial=1.))/max(tolerance, 1e-300)
+    scale = max(gnorm, np.linalg.norm(load), floor, 1e-300)
+    for iteration in range(max_iterations + 1):
+        if gnorm <= tolerance*scale:
+            return u, t, dict(newton_iterations=iteration, relative_gradient=gnorm/scale, energy=phi)
+        if iteration == max_iterations:
+            break
+        n, ri, rj, k = energy_tangent(bonds, theta, x, q)
+        h = sparse_stiffness(n_sites, np.stack((bonds.i, bonds.j), 1), n, ri, rj, *k.T)
+        if inertia is not None:
+            dt = inertia[0]
+            h = h + sp.diags(np.repeat(np.stack((bonds.mass, bonds.inertia), 1), 3, axis=1).ravel()/(dt*dt))
+        d = np.zeros(6*n_sites)
+        d[free] = spla.spsolve(h[free][:, free].tocsc(), -g.ravel()[free])
+        d = d.reshape(-1, 6)
+        slope = float((g*d).sum())
+        if not slope < 0:
+            d, slope = -g, -gnorm*gnorm
+        step = 1.
+        for _ in range(30):
+            cand = evaluate(u + step*d[:, :3], t + step*d[:, 3:])
+            cnorm = np.linalg.norm(cand[1])
+            drop = cand[0] - phi
+            if drop <= 1e-4*step*slope or (abs(drop) <= 1e-13*max(abs(phi), 1.) and cnorm < gnorm):
+                break
+            step *= .5
+        else:
+            raise RuntimeError('energy Newton line search failed')
+        u, t = u + step*d[:, :3], t + step*d[:, 3:]
+        phi, g, x, q = cand
+        gnorm = cnorm
+    raise RuntimeError(f'energy Newton did not converge ({gnorm/scale:g})')

@@ -148,3 +148,24 @@ def test_incremental_loads_match_float64_rebuild():
     assert err < 1e-6, err
     dx = float(torch.linalg.vector_norm(a.x - b.x)/torch.linalg.vector_norm(b.x - a.p))
     assert dx < 1e-6, dx
+
+
+def test_mixed_32cube_meets_float64_bars():
+    """The mixed-precision form on a 32^3 foam (32,768 sites, ~243k bonds) under
+    gravity, bottom fixed, dt = 1e-3, at relative residual 1e-6: every step's
+    float64 force residual and displacement error against a float64 solve of
+    the same state (tolerance 1e-10) are at most 1e-6 (the spec bars,
+    which apply to each result); over the 4-step trajectory the per-step errors
+    add up, so the trajectory is held to 4e-6 of its displacement."""
+    import dpf_gb300
+    from dpf_gb300.accuracy import snapshot_state, trajectory_accuracy
+    foam = dpf_gb300.jittered_lattice_foam(32, seed=0)
+    load = dpf_gb300.gravity_load(foam)
+    s = dpf_gb300.MixedNewtonBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], foam['masses'],
+                                   foam['fixed'], young=foam['young'], shear=foam['shear'])
+    ext = s.tensor(load)
+    s.step(1e-3, ext, tolerance=1e-6)          # start from a moving state
+    report = trajectory_accuracy(s, foam, ext, 1e-3, 1e-6, 4, snapshot_state(s), 'cuda')
+    assert report['force_residual_rel_max'] <= 1e-6, report
+    assert report['displacement_rel_max'] <= 1e-6, report
+    assert report['trajectory_displacement_rel'] <= 4e-6, report
