@@ -90,6 +90,8 @@ def parse():
     p.add_argument('--large-mix-count', type=int, default=64)
     p.add_argument('--large-mix-small', type=int, default=32)
     p.add_argument('--foam-workers', type=int, default=0, help='host processes triangulating foams (0: cores - 1)')
+    p.add_argument('--static-lattice', type=int, default=16,
+                   help='lattice of the static energy-law configuration (bottom held, top pushed 5%%; 0: skip)')
     return p.parse_args()
 
 
@@ -447,6 +449,75 @@ def run_large_mix(args, device, peak, peaks, requests, build_s):
     return out
 
 
+def _platen_problem(m, seed=0):
+    """The static configuration: jittered m^3 foam, bottom lattice layer held,
+    top layer pushed down by 5% of its height (whole sites held: a clamped
+    platen)."""
+    import dpf_gb300
+    foam = dpf_gb300.jittered_lattice_foam(m, seed=seed)
+    unit, h = foam['unit'], 1./m
+    bottom, top = unit[:, 2] < h, unit[:, 2] > 1 - h
+    prescribed = np.zeros((len(unit), 3))
+    prescribed[top, 2] = -.05*foam['points'][top, 2]
+    geometry = dict(points=foam['points'], radii=foam['radii'], pairs=foam['pairs'], areas=foam['areas'],
+                    contacts=None, masses=foam['masses'], fixed=bottom | top)
+    return foam, geometry, prescribed
+
+
+def _static_oracle_job(m):
+    """One static solve of the NumPy restatement (single thread, own process): (seconds, info, u)."""
+    import dpf_gb300
+    from oracle import dem
+    foam, geometry, prescribed = _platen_problem(m)
+    contacts = dpf_gb300.newton.classical_contacts(foam['points'], foam['radii'], foam['pairs'])
+    b = dem.EnergyBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], contacts, foam['masses'],
+                        geometry['fixed'], foam['young'], foam['shear'])
+    n = len(foam['points'])
+    q0 = np.zeros((n, 4))
+    q0[:, 0] = 1
+    t0 = time.perf_counter()
+    u, _, info = dem.energy_newton(b, np.zeros((n, 4)), foam['points'], q0, np.zeros((n, 6)), geometry['fixed'],
+                                   prescribed, tolerance=1e-10)
+    return time.perf_counter() - t0, {k: float(v) for k, v in info.items()}, u
+
+
+def run_static(args, device):
+    """The static configuration on the energy law: line-searched Newton to a
+    relative gradient of 1e-10, timed on the GPU (CUDA events, after one
+    untimed solve), beside one solve of the NumPy restatement on one host
+    core; displacements compared."""
+    import multiprocessing
+    import torch
+    import dpf_gb300
+    foam, geometry, prescribed = _platen_problem(args.static_lattice)
+    times, infos = [], []
+    for k in range(4):
+        solver = dpf_gb300.EnergyNewton(geometry, young=foam['young'], shear=foam['shear'], device=device)
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        info = solver.solve(prescribed=prescribed, tolerance=1e-10)
+        end.record()
+        torch.cuda.synchronize()
+        if k:
+            times.append(start.elapsed_time(end))
+            infos.append(info)
+    u = (solver.x - solver.X).cpu().numpy()
+    _single_thread_env()
+    with multiprocessing.get_context('spawn').Pool(1) as pool:
+        cpu_s, cpu_info, u_ref = pool.apply(_static_oracle_job, (args.static_lattice,))
+    ms = float(np.mean(times))
+    return dict(workload=f'{args.static_lattice}^3 jittered foam, energy law (EnergyFoam bond potential), bottom '
+                         'layer held, top layer pushed down 5% (clamped platen), static equilibrium to relative '
+                         'gradient 1e-10', sites=solver.n_sites, bonds=solver.n_bonds, solves_per_s=1e3/ms,
+                ms_per_solve=ms, newton_iterations=infos[-1]['newton_iterations'],
+                cg_iterations=infos[-1]['cg_iterations'], relative_gradient=infos[-1]['relative_gradient'],
+                cpu=dict(kind='port', cores=1, seconds_per_solve=cpu_s, solves_per_s=1./cpu_s,
+                         newton_iterations=cpu_info['newton_iterations'],
+                         sample='one solve of the NumPy restatement (block-Jacobi CG Newton directions)'),
+                displacement_rel_vs_cpu=float(np.linalg.norm(u - u_ref)/np.linalg.norm(u_ref)))
+
+
 def replica_rates(ms, e_ms, steps, world, device='cpu'):
     """Whole-job rates of ``world`` replicas that each timed ``steps`` solves: the
     slowest rank's device and end-to-end times (all-reduce MAX over the process
@@ -685,6 +756,7 @@ def run_ours(args):
         del foams, requests
     if pool is not None:
         pool.close()
+    static = run_static(args, device) if args.static_lattice > 0 and world == 1 else None
     if rank != 0:
         return
     cpu = None
@@ -704,7 +776,7 @@ def run_ours(args):
                 e2e=dict(value=e2e, unit=UNIT, h2d_bytes_per_step=int(load.nbytes),
                          d2h_bytes_per_step=int(n_sites*3*8)),
                 gpu_launches=launches, kernels=kernels, roofline=roof, hvp=hvp, cpu_baseline=cpu, plain_f64=plain,
-                accuracy=accuracy, served=served, adjoint=adjoint, large_mix=large,
+                accuracy=accuracy, served=served, adjoint=adjoint, large_mix=large, static=static,
                 relative_residual_max=max(i['nonlinear_relative_residual'] for i in infos),
                 clocks=dict(sm_mhz=clock['sm_mhz'], sm_max_mhz=clock['sm_max_mhz'], reasons=clock['reasons']))
     print(json.dumps(line), flush=True)

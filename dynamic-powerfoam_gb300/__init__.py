@@ -9,7 +9,7 @@ from .foam import jittered_lattice_foam, gravity_load, regular_edges, morton_ord
 from .newton import (LinearBonds, FiniteBonds, NewtonBonds, FastNewtonBonds, MixedNewtonBonds, AdaptiveIntervals,
                      SubdivideError, fgmres, incidence, guard_error)
 from .adjoint import DifferentiableBonds
-from .energy import EnergyFoam
+from .energy import EnergyFoam, EnergyNewton
 from .core import ParallelBonds
 from .static import reference_stiffness, solve_prescribed
 
@@ -20,4 +20,4 @@ FiniteBondsGPU = FiniteBonds
 __all__ = ['jittered_lattice_foam', 'gravity_load', 'regular_edges', 'morton_order', 'LinearBonds',
            'FiniteBonds', 'NewtonBonds', 'FastNewtonBonds', 'MixedNewtonBonds', 'LinearBondsGPU', 'FiniteBondsGPU',
            'AdaptiveIntervals', 'SubdivideError', 'fgmres', 'incidence', 'guard_error', 'DifferentiableBonds',
-           'EnergyFoam', 'ParallelBonds', 'reference_stiffness', 'solve_prescribed']
+           'EnergyFoam', 'EnergyNewton', 'ParallelBonds', 'reference_stiffness', 'solve_prescribed']

@@ -10,6 +10,7 @@ are evaluated by one CUDA bond pass and a deterministic incidence gather.
 """
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -132,7 +133,8 @@ class EnergyNewton:
     follows an Armijo backtracking search on the float64 potential; the
     gradient (float64 forces and torques, ``dpf_bond_energy``; the rotation
     rows ``-J_l(t)^T tau``) decides convergence: ``|g| <= tolerance * scale``
-    with scale the larger of the first gradient norm and |external load|.
+    with scale the largest of the first gradient norm, |external load| and
+    the roundoff level of the bond forces divided by the tolerance.
     """
 
     def __init__(self, geometry, young=1200., shear=480., device='cuda', theta=None, inner_tolerance=1e-2,
@@ -242,7 +244,10 @@ class EnergyNewton:
         self._status.zero_()
         phi, g, x, q = self._evaluate(x0, q0, u, t, load, inertia)
         gnorm = float(torch.linalg.vector_norm(g))
-        scale = max(gnorm, float(torch.linalg.vector_norm(load)), 1e-300)
+        # floor: the roundoff level of bond forces (1e-13 of the stiffest bond times the largest coordinate)
+        floor = 1e-13*float(self.law.base[:, 0].max())*float(x0.abs().max())/max(tolerance, 1e-300) \
+            if self.n_bonds else 0.
+        scale = max(gnorm, float(torch.linalg.vector_norm(load)), floor, 1e-300)
         trace = [gnorm/scale]
         for iteration in range(max_iterations + 1):
             if gnorm <= tolerance*scale:

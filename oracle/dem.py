@@ -978,13 +978,36 @@ def energy_tangent(bonds, theta, x, q):
     return n, c - x[i], c - x[j], k
 
 
+def _block_jacobi_cg(a, b, tolerance):
+    """Solve a x = b (SPD, rows in whole sites of 6) by CG preconditioned with
+    the inverse 6 x 6 diagonal blocks, to |r| <= tolerance |b|."""
+    import scipy.sparse.linalg as spla
+    n = a.shape[0]//6
+    blocks = np.stack([a[6*k:6*k + 6, 6*k:6*k + 6].toarray() for k in range(n)]) if n < 64 else \
+        a.tobsr(blocksize=(6, 6)).data[_diagonal_block_index(a.tobsr(blocksize=(6, 6)))]
+    inverse = np.linalg.inv(blocks)
+    precondition = spla.LinearOperator(a.shape, matvec=lambda v: np.einsum('kij,kj->ki', inverse,
+                                                                           v.reshape(-1, 6)).ravel())
+    x, info = spla.cg(a, b, rtol=tolerance, atol=0., maxiter=20*n + 200, M=precondition)
+    if info != 0:
+        raise RuntimeError(f'energy Newton: inner CG did not converge ({info})')
+    return x
+
+
+def _diagonal_block_index(bsr):
+    """Positions of the diagonal blocks in a BSR matrix's data (every block row has one)."""
+    rows = np.repeat(np.arange(bsr.shape[0]//6), np.diff(bsr.indptr))
+    where = np.flatnonzero(bsr.indices == rows)
+    return where[np.argsort(rows[where], kind='stable')]
+
+
 def energy_newton(bonds, theta, x0, q0, load, fixed, prescribed=None, inertia=None, tolerance=1e-10,
                   max_iterations=60):
     """Minimise the bond potential over (u, t) (static: E_b - f . u - tau . t;
     implicit Euler with inertia = (dt, v, w): plus sum m |u - dt v|^2/(2 dt^2)
     + sum I |t - dt w|^2/(2 dt^2)).  Fixed sites are held at ``prescribed``
     displacements with their rotation held.  Newton directions solve the
-    frozen-tangent system exactly (sparse LU on the free DOFs); Armijo
+    frozen-tangent system on the free DOFs by block-Jacobi CG to 1e-10; Armijo
     backtracking on the potential; stop at |g| <= tolerance * scale, scale the
     largest of the first gradient norm, |load| and the roundoff level of the
     bond forces divided by the tolerance.  Returns (u, t, info)."""
@@ -1031,7 +1054,7 @@ def energy_newton(bonds, theta, x0, q0, load, fixed, prescribed=None, inertia=No
             dt = inertia[0]
             h = h + sp.diags(np.repeat(np.stack((bonds.mass, bonds.inertia), 1), 3, axis=1).ravel()/(dt*dt))
         d = np.zeros(6*n_sites)
-        d[free] = spla.spsolve(h[free][:, free].tocsc(), -g.ravel()[free])
+        d[free] = _block_jacobi_cg(h[free][:, free].tocsr(), -g.ravel()[free], 1e-10)
         d = d.reshape(-1, 6)
         slope = float((g*d).sum())
         if not slope < 0:

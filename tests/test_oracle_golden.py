@@ -209,3 +209,68 @@ def test_static_equilibrium_matches_reference():
     q, residual = dem.solve_prescribed(k, g['prescribed'], g['values'], g['load'])
     assert np.abs(q.reshape(-1, 6) - g['q']).max() <= 1e-9*np.abs(g['q']).max()
     assert residual < 1e-8
+
+
+def _platen_foam(m, seed=0):
+    """A jittered m^3 foam with its bottom lattice layer held and its top layer
+    pushed down by 5% of its height (the static configuration's boundary
+    conditions on whole sites: a clamped platen)."""
+    import dpf_gb300
+    foam = dpf_gb300.jittered_lattice_foam(m, seed=seed)
+    unit, h = foam['unit'], 1./m
+    bottom, top = unit[:, 2] < h, unit[:, 2] > 1 - h
+    n = len(unit)
+    prescribed = np.zeros((n, 3))
+    prescribed[top, 2] = -.05*foam['points'][top, 2]
+    contacts = dpf_gb300.newton.classical_contacts(foam['points'], foam['radii'], foam['pairs'])
+    return foam, contacts, bottom | top, prescribed
+
+
+def test_energy_newton_linear_limit_matches_reference_stiffness():
+    """For a vanishing platen displacement the minimiser of the bond potential
+    is the linear static solution of the reference stiffness (the reference
+    Hessian of the potential, foam_dem_energy.py:14-16, assembled as in
+    bonded_dem_dynamics.py:22-47)."""
+    foam, contacts, fixed, prescribed = _platen_foam(5)
+    b = dem.EnergyBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], contacts, foam['masses'],
+                        fixed, foam['young'], foam['shear'])
+    n = len(foam['points'])
+    eps = 1e-6
+    q0 = np.zeros((n, 4))
+    q0[:, 0] = 1
+    u, t, info = dem.energy_newton(b, np.zeros((n, 4)), foam['points'], q0, np.zeros((n, 6)), fixed,
+                                   eps*prescribed, tolerance=1e-12)
+    assert info['relative_gradient'] <= 1e-12
+    k = dem.reference_stiffness(foam['points'], foam['pairs'], contacts, b.base[:, 0], b.base[:, 1], b.base[:, 2],
+                                b.base[:, 3])
+    mask = np.repeat(fixed, 6)
+    values = np.zeros((n, 6))
+    values[:, :3] = eps*prescribed
+    q, _ = dem.solve_prescribed(k, mask, values)
+    q = q.reshape(n, 6)
+    assert np.linalg.norm(np.c_[u, t] - q)/np.linalg.norm(q) < 1e-5
+
+
+def test_energy_newton_minimises_the_potential():
+    """The oracle's static minimiser: relative gradient below the tolerance, and
+    the potential grows along random admissible perturbations."""
+    foam, contacts, fixed, prescribed = _platen_foam(6, seed=1)
+    b = dem.EnergyBonds(foam['points'], foam['radii'], foam['pairs'], foam['areas'], contacts, foam['masses'],
+                        fixed, foam['young'], foam['shear'])
+    n = len(foam['points'])
+    q0 = np.zeros((n, 4))
+    q0[:, 0] = 1
+    theta = np.zeros((n, 4))
+    u, t, info = dem.energy_newton(b, theta, foam['points'], q0, np.zeros((n, 6)), fixed, prescribed,
+                                   tolerance=1e-11)
+    assert info['relative_gradient'] <= 1e-11
+
+    def energy(du, dt):
+        q = dem.quaternion_product(dem.rotation_quaternion(t + dt), q0)
+        return b.energy(theta, foam['points'] + u + du, q)
+    e0 = energy(0., 0.)
+    rng = np.random.default_rng(3)
+    for _ in range(3):
+        d = rng.normal(size=(n, 6))*1e-4
+        d[fixed] = 0
+        assert energy(d[:, :3], d[:, 3:]) > e0
