@@ -249,6 +249,7 @@ def run_hvp(s, dt, peak, peaks, launches=50):
     import torch
     from dpf_gb300 import _lib
     s._pack_ends(dt)
+    variant = s._end_variant or 0
     stream = torch.cuda.current_stream()
     n, m = s.n_sites, s.n_bonds
     q = torch.randn((n, 6), dtype=torch.float32, device=s.device)
@@ -257,7 +258,7 @@ def run_hvp(s, dt, peak, peaks, launches=50):
 
     def launch():
         _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q.data_ptr(),
-                  y.data_ptr(), stream.cuda_stream)
+                  y.data_ptr(), variant, stream.cuda_stream)
     for _ in range(3):
         launch()
     times = []
@@ -286,7 +287,7 @@ def run_hvp(s, dt, peak, peaks, launches=50):
                 achieved=achieved, peak=peak, unit='GB/s', frac=achieved/peak,
                 peak_source='measured' if peaks else 'fallback', l2='flushed between launches',
                 back_to_back_ms=back_to_back, back_to_back_frac=alg/(back_to_back*1e-3)/1e9/peak,
-                end_records_bytes=int(s._ends.numel())*4)
+                end_records_bytes=int(s._ends.numel())*4, variant=_end_shape(variant))
 
 
 def run_adjoint(args, device):
@@ -447,6 +448,16 @@ def run_large_mix(args, device, peak, peaks, requests, build_s):
     del s
     torch.cuda.empty_cache()
     return out
+
+
+def _end_shape(variant):
+    """(lanes per site, CTAs per SM) of a bond-end sweep variant."""
+    import ctypes
+    from dpf_gb300 import _lib
+    lanes, blocks = ctypes.c_int(), ctypes.c_int()
+    _lib.check(_lib.load().dpf_end_variant_shape(int(variant), ctypes.byref(lanes), ctypes.byref(blocks)),
+               'dpf_end_variant_shape')
+    return dict(variant=int(variant), lanes_per_site=lanes.value, ctas_per_sm=blocks.value)
 
 
 def _platen_problem(m, seed=0):

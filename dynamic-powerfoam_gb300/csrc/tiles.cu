@@ -596,26 +596,22 @@ __device__ __forceinline__ void sym_mv6(const float P[21], const float x[6], flo
 //   f = ks du + (kn - ks)(du.n') n',  m = kb dw + (kt - kb)(dw.n') n',
 //   F_s = -f,  T_s = -(r_s x f) - m
 // (for the i end this is the bond's wrench on i; for the j end n' = -n and the
-// same formula gives the wrench on j).  A group of kEndLanes lanes owns a
-// site, each lane sums the ends k = start + lane, start + lane + kEndLanes, ..
+// same formula gives the wrench on j).  A group of L lanes owns a site, each
+// lane sums the ends k = start + lane, start + lane + L, ..
 // in registers and a fixed xor-shuffle tree adds the lanes: no shared
 // memory, no atomics, bitwise reproducible.  Records stream from HBM once per
 // sweep (evict-first); q of the other ends is gathered from L2.
 
-#ifndef DPF_END_LANES
-#define DPF_END_LANES 8
-#endif
-#ifndef DPF_END_MIN_BLOCKS
-#define DPF_END_MIN_BLOCKS 4
-#endif
-#ifndef DPF_END_PCG_THREADS
-#define DPF_END_PCG_THREADS 256
-#endif
-constexpr int kEndLanes = DPF_END_LANES;
+// Launch shapes of the bond-end sweep: L lanes per site (4, 8 or 16) and B
+// resident 256-thread CTAs per SM (the register budget: 64 registers at 4,
+// 80 at 3, 128 at 2).  The variants are compiled side by side; callers pick
+// one per graph size (dpf_end_variant_shape lists them; variant 0 is 8 lanes,
+// 4 CTAs per SM).
 constexpr int kEndThreads = 256;
-// CTA width of the bond-end PCG: 32 warps per SM in all, fewer and wider CTAs
-// make its grid barriers and partial sums cheaper
-constexpr int kEndPcgThreads = DPF_END_PCG_THREADS;
+constexpr int kEndPcgThreads = 256;
+constexpr int kEndVariants = 6;
+constexpr int kEndVariantLanes[kEndVariants] = {8, 4, 16, 8, 4, 8};
+constexpr int kEndVariantBlocks[kEndVariants] = {4, 4, 4, 3, 2, 2};
 
 struct EndGraph {
     int64_t n;
@@ -668,19 +664,19 @@ __device__ __forceinline__ void load_q(const float *q, int64_t s, float v[6]) {
 }
 
 // For every site s: epi(s, q_s, site record, acc) with acc the alpha K q sum.
-// Warp w of the grid takes the chunks w, w + W, ... of 32 / kEndLanes
+// Warp w of the grid takes the chunks w, w + W, ... of 32 / L
 // consecutive sites (W warps in the grid).  The round count is the same for
 // every warp, so the shuffles see full warps.
-template <bool kConst, class Epi>
+template <int L, bool kConst, class Epi>
 __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi &epi) {
-    constexpr int kSites = 32 / kEndLanes;  // sites per warp and round
+    constexpr int kSites = 32 / L;  // sites per warp and round
     const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-    const int lane32 = (int)threadIdx.x & 31, lane = lane32 & (kEndLanes - 1);
+    const int lane32 = (int)threadIdx.x & 31, lane = lane32 & (L - 1);
     const int64_t chunks = (G.n + kSites - 1) / kSites;
     const int64_t rounds = (chunks + warps - 1) / warps;
     for (int64_t r = 0; r < rounds; ++r) {
-        const int64_t s = (warp + r * warps) * kSites + lane32 / kEndLanes;
+        const int64_t s = (warp + r * warps) * kSites + lane32 / L;
         const bool valid = s < G.n;
         float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, qs[6];
         if (valid) load_q<kConst>(q, s, qs);
@@ -688,8 +684,8 @@ __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi 
             const int k1 = G.ptr[s + 1];
             // two ends per step: both ends' records, then both gathers, are in
             // flight together
-            for (int k = G.ptr[s] + lane; k < k1; k += 2 * kEndLanes) {
-                const int k2 = k + kEndLanes;
+            for (int k = G.ptr[s] + lane; k < k1; k += 2 * L) {
+                const int k2 = k + L;
                 const bool two = k2 < k1;
                 const float4 a = __ldcs(G.e0 + k), b = __ldcs(G.e1 + k), c = __ldcs(G.e2 + k);
                 float4 a2 = a, b2 = b, c2 = c;
@@ -706,7 +702,7 @@ __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi 
             }
         }
 #pragma unroll
-        for (int o = 1; o < kEndLanes; o <<= 1)
+        for (int o = 1; o < L; o <<= 1)
 #pragma unroll
             for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
         if (valid && lane == 0) epi(s, qs, G.site[s], acc);
@@ -726,9 +722,10 @@ struct EndHvpEpi {
     }
 };
 
-__global__ void __launch_bounds__(kEndThreads, DPF_END_MIN_BLOCKS) end_hvp_kernel(EndGraph G, const float *q, float *y) {
+template <int L, int B>
+__global__ void __launch_bounds__(kEndThreads, B) end_hvp_kernel(EndGraph G, const float *q, float *y) {
     EndHvpEpi epi{y};
-    for_ends<true>(G, q, epi);
+    for_ends<L, true>(G, q, epi);
 }
 
 // One thread per incidence k of site s (site-major): the end record of bond
@@ -840,7 +837,7 @@ __device__ __forceinline__ float update_site(const PcgArgs &a, int64_t s, float 
 }
 
 // kTiles: w = A u by the tiled sweep, else by the bond-end sweep.
-template <bool kTiles>
+template <bool kTiles, int L>
 __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -887,7 +884,7 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
         if (kTiles)
             ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
         else
-            for_ends<false>(a.E, a.u, epi);
+            for_ends<L, false>(a.E, a.u, epi);
         part = block_sum((double)epi.dot);
         if (threadIdx.x == 0) a.part_a[blockIdx.x] = part;
         if (!ok) return;
@@ -924,11 +921,36 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
 
 __global__ void __launch_bounds__(kTileThreadsMax + 64, DPF_TILE_MIN_BLOCKS) tiled_pcg_kernel(PcgArgs a) {
     extern __shared__ __align__(16) unsigned char smem[];
-    pcg_body<true>(a, smem);
+    pcg_body<true, 8>(a, smem);
 }
 
-__global__ void __launch_bounds__(kEndPcgThreads, 1024 / kEndPcgThreads) end_pcg_kernel(PcgArgs a) {
-    pcg_body<false>(a, nullptr);
+template <int L, int B>
+__global__ void __launch_bounds__(kEndPcgThreads, B) end_pcg_kernel(PcgArgs a) {
+    pcg_body<false, L>(a, nullptr);
+}
+
+// The kernels of variant v (0 <= v < kEndVariants).
+using EndHvpKernel = void (*)(EndGraph, const float *, float *);
+using EndPcgKernel = void (*)(PcgArgs);
+inline EndHvpKernel end_hvp_variant(int v) {
+    switch (v) {
+    case 1: return end_hvp_kernel<4, 4>;
+    case 2: return end_hvp_kernel<16, 4>;
+    case 3: return end_hvp_kernel<8, 3>;
+    case 4: return end_hvp_kernel<4, 2>;
+    case 5: return end_hvp_kernel<8, 2>;
+    default: return end_hvp_kernel<8, 4>;
+    }
+}
+inline EndPcgKernel end_pcg_variant(int v) {
+    switch (v) {
+    case 1: return end_pcg_kernel<4, 4>;
+    case 2: return end_pcg_kernel<16, 4>;
+    case 3: return end_pcg_kernel<8, 3>;
+    case 4: return end_pcg_kernel<4, 2>;
+    case 5: return end_pcg_kernel<8, 2>;
+    default: return end_pcg_kernel<8, 4>;
+    }
 }
 
 inline int blocks_for(int64_t n, int threads) { return (int)((n + threads - 1) / threads); }
@@ -1331,14 +1353,24 @@ static EndGraph end_graph(const dpf_graph *g, const float *ends, const float *si
                     seg_site, active};
 }
 
-int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, void *stream) {
+int dpf_end_variant_shape(int variant, int *lanes, int *blocks_per_sm) {
+    if (variant < 0 || variant >= kEndVariants) return DPF_ERR_ARGUMENT;
+    if (lanes) *lanes = kEndVariantLanes[variant];
+    if (blocks_per_sm) *blocks_per_sm = kEndVariantBlocks[variant];
+    return DPF_OK;
+}
+
+int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, int variant,
+                void *stream) {
     if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!ends || !aligned16(ends))) || !site4 ||
-        !aligned16(site4) || !q || !y || ((uintptr_t)q & 7u) || ((uintptr_t)y & 7u))
+        !aligned16(site4) || !q || !y || ((uintptr_t)q & 7u) || ((uintptr_t)y & 7u) || variant < 0 ||
+        variant >= kEndVariants)
         return DPF_ERR_ARGUMENT;
     int grid = 0;
-    const int rc = persistent_grid(end_hvp_kernel, kEndThreads, 0, INT32_MAX, INT32_MAX, grid, false);
+    const EndHvpKernel kernel = end_hvp_variant(variant);
+    const int rc = persistent_grid(kernel, kEndThreads, 0, INT32_MAX, INT32_MAX, grid, false);
     if (rc) return rc;
-    end_hvp_kernel<<<grid, kEndThreads, 0, (cudaStream_t)stream>>>(end_graph(g, ends, site4), q, y);
+    kernel<<<grid, kEndThreads, 0, (cudaStream_t)stream>>>(end_graph(g, ends, site4), q, y);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
@@ -1347,14 +1379,15 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
                          const float *block32, const float *P24, const float *units32, const double *vector,
                          double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
                          double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
-                         const uint8_t *active, void *stream) {
+                         const uint8_t *active, int variant, void *stream) {
     if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!ends || !aligned16(ends))) || !site4 || !fixed ||
         !block32 || !P24 || !units32 || !vector || !out || !iterations || !workspace || !partials || !barrier ||
         !status || max_iterations < 1 || !aligned16(workspace) || !aligned16(P24) || !aligned16(site4) ||
-        (active && !seg_site))
+        (active && !seg_site) || variant < 0 || variant >= kEndVariants)
         return DPF_ERR_ARGUMENT;
     int grid = 0;
-    int rc = persistent_grid(end_pcg_kernel, kEndPcgThreads, 0, INT32_MAX, kMaxPcgBlocksTiled, grid, false);
+    const EndPcgKernel kernel = end_pcg_variant(variant);
+    int rc = persistent_grid(kernel, kEndPcgThreads, 0, INT32_MAX, kMaxPcgBlocksTiled, grid, false);
     if (rc) return rc;
     const int64_t n6 = 6 * g->n_sites;
     PcgArgs a{};
@@ -1385,7 +1418,7 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
         return DPF_ERR_CUDA;
     }
     void *args[] = {&a};
-    if (cudaLaunchCooperativeKernel((const void *)end_pcg_kernel, grid, kEndPcgThreads, args, 0,
+    if (cudaLaunchCooperativeKernel((const void *)kernel, grid, kEndPcgThreads, args, 0,
                                     (cudaStream_t)stream) !=
         cudaSuccess) {
         cudaGetLastError();

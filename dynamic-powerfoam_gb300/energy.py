@@ -227,7 +227,7 @@ class EnergyNewton:
             self._identity32.data_ptr(), self._p24.data_ptr(), self._ones32.data_ptr(), rhs.data_ptr(),
             float(self.inner_tolerance), int(self.inner_iterations), out.data_ptr(), self._cg.data_ptr(),
             self._workspace.data_ptr(), self._partials.data_ptr(), self._barrier.data_ptr(), self._status.data_ptr(),
-            None, None, stream), 'dpf_end_precondition')
+            None, None, 0, stream), 'dpf_end_precondition')
         out[self.fixed] = 0.
         return out
 

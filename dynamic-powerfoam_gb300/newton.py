@@ -1220,6 +1220,7 @@ class MixedNewtonBonds(NewtonBonds):
     def _init_tiles(self):
         self._tiles = None
         self._ends = None
+        self._end_variant = None       # launch shape of the bond-end sweep (autotuned at the first PCG)
         self._sweep_ready = False
         self.tile_timings = {}
         self._packed = None
@@ -1248,12 +1249,17 @@ class MixedNewtonBonds(NewtonBonds):
                    self._p24.data_ptr(), self._site4.data_ptr(), self._stream())
         self._packed = ('ends', dt)
 
-    def _end_pcg(self, vector, out, tolerance, max_iterations, iterations):
+    def _end_pcg(self, vector, out, tolerance, max_iterations, iterations, variant=None):
+        if variant is None:
+            if self._end_variant is None:
+                from .tiles import tune_end_sweep
+                self._end_variant = tune_end_sweep(self, vector)
+            variant = self._end_variant
         self._call('dpf_end_precondition', ctypes.byref(self._graph), self._ends.data_ptr(), self._site4.data_ptr(),
                    self.fixed.data_ptr(), self._block32.data_ptr(), self._p24.data_ptr(), self._units32.data_ptr(),
                    vector.data_ptr(), float(tolerance), int(max_iterations), out.data_ptr(), iterations.data_ptr(),
                    self._tiled_workspace.data_ptr(), self._tiled_partials.data_ptr(), self._barrier.data_ptr(),
-                   self._status.data_ptr(), *self._site_mask(), self._stream())
+                   self._status.data_ptr(), *self._site_mask(), int(variant), self._stream())
 
     def _site_mask(self):
         """(per-site segment, per-segment active flag) device pointers that let the

@@ -151,3 +151,42 @@ def autotune(solver, run, candidates=CANDIDATES, repeats=3):
     best = min(timings, key=timings.get)
     _TUNED[key] = best
     return Tiles(built[best[0]], solver.device, best[1], best[2]), timings
+
+
+# Launch shape of the bond-end sweep per (device, size class): the autotuner
+# times each compiled variant (lanes per site x CTAs per SM, see
+# dpf_end_variant_shape) on the first elastic PCG of a graph of that size
+# class and keeps the fastest for every later graph of the class.
+END_VARIANTS = 6
+_END_TUNED = {}
+
+
+def end_size_class(n_sites, n_bonds):
+    """Size class of a graph for the bond-end sweep: log2 of its incidences."""
+    return int(np.log2(max(2*n_bonds, 1)))
+
+
+def tune_end_sweep(solver, vector, iterations=5):
+    """Variant index of the bond-end PCG for ``solver``'s graph: cached per
+    (device, size class); otherwise each variant runs an elastic PCG of exactly
+    ``iterations`` iterations on the solver's own packed records and
+    ``vector`` (tolerance 0), once to warm up and once timed with CUDA events
+    on the current stream, and the fastest is kept."""
+    key = (solver.device.index, end_size_class(solver.n_sites, solver.n_bonds))
+    if key in _END_TUNED:
+        return _END_TUNED[key][0]
+    scratch = torch.empty_like(vector)
+    count = torch.zeros(1, dtype=torch.int32, device=solver.device)
+    stream = torch.cuda.current_stream(solver.device)
+    times = {}
+    for variant in range(END_VARIANTS):
+        solver._end_pcg(vector, scratch, 0., iterations, count, variant=variant)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record(stream)
+        solver._end_pcg(vector, scratch, 0., iterations, count, variant=variant)
+        end.record(stream)
+        end.synchronize()
+        times[variant] = start.elapsed_time(end)
+    best = min(times, key=times.get)
+    _END_TUNED[key] = (best, times)
+    return best

@@ -620,26 +620,64 @@ int64_t dpf_end_floats(int64_t n_bonds);
 int dpf_end_pack(const dpf_graph *g, const float *bond_data, double alpha, const float *P36, const float *mass32,
                  const uint8_t *fixed, float *ends, float *P24, float *site4, void *stream);
 
+/* Launch shape of bond-end sweep variant `variant` (0 .. 5): lanes per site
+ * (4, 8 or 16) and resident 256-thread CTAs per SM (2, 3 or 4; fewer CTAs
+ * leave more registers per thread).  Variant 0 (8 lanes, 4 CTAs) is the
+ * default; an autotuner may pick another per graph size. */
+int dpf_end_variant_shape(int variant, int *lanes, int *blocks_per_sm);
+
 /* y = (diag M + alpha K) q in float32 from the end records; q, y (N, 6)
- * float32, 8-byte aligned. */
-int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, void *stream);
+ * float32, 8-byte aligned; variant as dpf_end_variant_shape. */
+int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const float *q, float *y, int variant,
+                void *stream);
 
 /* dpf_tiled_precondition on the bond-end operator (one cooperative launch;
  * workspace dpf_tiled_workspace_floats(N), partials
  * dpf_tiled_partials_doubles(); barrier: 2 unsigned ints (device), zeroed
  * by the call on its stream).  seg_site/active (optional, for batches):
  * a site s with active[seg_site[s]] == 0 skips its ends (its request's
- * vector is zero, so its rows stay zero). */
+ * vector is zero, so its rows stay zero).  variant: the sweep's launch
+ * shape (dpf_end_variant_shape); every variant gives the same iterates up
+ * to float32 rounding of the lane sums. */
 int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
                          const float *block32, const float *P24, const float *units32, const double *vector,
                          double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
                          double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
-                         const uint8_t *active, void *stream);
+                         const uint8_t *active, int variant, void *stream);
 int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4,
                            const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
                            const double *vector, double tolerance, int max_iterations, double *out, int *iterations,
                            float *workspace, double *partials, unsigned *barrier, int *status, int threads,
                            int stages, void *stream);
+
+/* ---- Per-request Arnoldi over a served batch (no reference counterpart:
+ * each request of a batch follows its own FGMRES of
+ * experiments/bonded_dem_newton.py:13-60) ----
+ * Segments are contiguous site ranges seg_ptr[r] .. seg_ptr[r+1] (int64,
+ * R + 1 entries); seg (N) int32 gives each site's segment; active (R, uint8,
+ * optional) skips segments (their results are 0).  Vectors are (N, 6)
+ * doubles; a basis is `count` (<= 40) rows of ld doubles.  Sums are per
+ * (segment, chunk) then over chunks in a fixed order (deterministic).
+ * partials: dpf_segment_krylov_partials_doubles(R, count) doubles. */
+int64_t dpf_segment_krylov_partials_doubles(int n_segments, int count);
+
+/* out (R, count): out[r][k] = basis_k . w over segment r. */
+int dpf_segment_dots(int n_segments, const int64_t *seg_ptr, const uint8_t *active, const double *basis, int64_t ld,
+                     int count, const double *w, double *out, double *partials, void *stream);
+
+/* w -= sum_k h[r][k] basis_k on each active segment r (h (R, count));
+ * norm2 (R) = |w|^2 per segment afterwards. */
+int dpf_segment_project(int n_segments, const int64_t *seg_ptr, const uint8_t *active, const double *basis,
+                        int64_t ld, int count, const double *h, double *w, double *norm2, double *partials,
+                        void *stream);
+
+/* out = scale[seg] * a on active segments, 0 on the others (scale (R)). */
+int dpf_segment_scale(int64_t n_sites, const int32_t *seg, const uint8_t *active, const double *scale,
+                      const double *a, double *out, void *stream);
+
+/* x += sum_k y[seg][k] rows_k (y (R, count), zero past a segment's own length). */
+int dpf_segment_combine(int64_t n_sites, const int32_t *seg, const double *rows, int64_t ld, int count,
+                        const double *y, double *x, void *stream);
 
 /* ---- Energy law (bond part of EnergyFoam with volume=False, kinematics='small') ----
  * Replaces EnergyFoam._bond_kinematics / energy / forces

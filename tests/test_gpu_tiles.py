@@ -75,15 +75,25 @@ def test_end_hvp_matches_float64_product():
     q32 = q.float().contiguous()
     y = torch.empty_like(q32)
     _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q32.data_ptr(),
-              y.data_ptr(), s._stream())
+              y.data_ptr(), 0, s._stream())
     ref = _direct_operator(s, .25*dt*dt, q32.double())
     err = (y.double() - ref).norm()/ref.norm()
     assert float(err) < 2e-6
     # bitwise reproducible: fixed lane split and shuffle tree, no atomics
     y2 = torch.empty_like(q32)
     _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q32.data_ptr(),
-              y2.data_ptr(), s._stream())
+              y2.data_ptr(), 0, s._stream())
     assert torch.equal(y, y2)
+    # every launch shape gives the same operator
+    lib = _lib.load()
+    for variant in range(1, 6):
+        lanes, blocks = ctypes.c_int(), ctypes.c_int()
+        assert lib.dpf_end_variant_shape(variant, ctypes.byref(lanes), ctypes.byref(blocks)) == 0
+        y3 = torch.empty_like(q32)
+        _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q32.data_ptr(),
+                  y3.data_ptr(), variant, s._stream())
+        err = (y3.double() - ref).norm()/ref.norm()
+        assert float(err) < 2e-6, (variant, lanes.value, blocks.value)
 
 
 @pytest.mark.parametrize('sweep', ['ends', 'tiles'])
