@@ -150,11 +150,6 @@ SIGNATURES = {
     'dpf_anderson_gram': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, vp, vp, vp, vp]),
     'dpf_anderson_mix': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, P(ctypes.c_double), vp, vp, vp]),
     'dpf_barrier_selftest': (i32, [i32, i64, i32, vp, vp, vp, vp]),
-    'dpf_segment_krylov_partials_doubles': (i64, [i32, i32]),
-    'dpf_segment_dots': (i32, [i32, vp, vp, vp, i64, i32, vp, vp, vp, vp]),
-    'dpf_segment_project': (i32, [i32, vp, vp, vp, i64, i32, vp, vp, vp, vp, vp]),
-    'dpf_segment_scale': (i32, [i64, vp, vp, vp, vp, vp, vp]),
-    'dpf_segment_combine': (i32, [i64, vp, vp, i64, i32, vp, vp, vp]),
 }
 
 
@@ -173,7 +168,6 @@ KERNELS = {
     'dpf_end_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
     'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
-    'dpf_segment_dots': 2, 'dpf_segment_project': 2, 'dpf_segment_scale': 1, 'dpf_segment_combine': 1,
 }
 LAUNCHES = {'count': 0}
 

@@ -92,33 +92,6 @@ def _staging():
     return _LOCAL.staging
 
 
-# Device copies of request bond graphs, keyed by the host pairs array (many
-# requests share one graph, e.g. one per lattice size): edges (m, 2) int32 and
-# the incidence CSR, uploaded and sorted once.  The cache keeps the host array
-# alive, so its id is not reused while the entry exists.
-_GRAPHS = {}
-_GRAPHS_LOCK = threading.Lock()
-_GRAPHS_MAX = 64
-
-
-def _device_graph(pairs, n_sites, device):
-    key = (id(pairs), n_sites, str(device))
-    with _GRAPHS_LOCK:
-        hit = _GRAPHS.get(key)
-        if hit is not None and hit[0] is pairs:
-            return hit[1:]
-    fp = np.asarray(pairs)
-    if len(fp) and (fp.min() < 0 or fp.max() >= n_sites):
-        raise ValueError('Invalid endpoint index')
-    edges = torch.as_tensor(np.ascontiguousarray(fp, dtype=np.int32), device=device).reshape(-1, 2)
-    ptr, inc = device_incidence(edges.to(torch.int64), n_sites)
-    with _GRAPHS_LOCK:
-        if len(_GRAPHS) >= _GRAPHS_MAX:
-            _GRAPHS.pop(next(iter(_GRAPHS)))
-        _GRAPHS[key] = (pairs, edges, ptr, inc)
-    return edges, ptr, inc
-
-
 class RequestState:
     """Resident state of one or several requests: exactly what a ``Batch``
     concatenates (the attributes of fresh ``MixedNewtonBonds`` solvers, without
@@ -159,8 +132,11 @@ class RequestState:
         n_load = 6*n if loads is not None else 0
         f64 = staging.host('f8', 5*n + m + n_load)
         u8 = staging.host('u1', n)
+        i32 = staging.host('i4', 2*m)
         pts, rad, mas, are = f64[:3*n].reshape(n, 3), f64[3*n:4*n], f64[4*n:5*n], f64[5*n:5*n + m]
         ext = f64[5*n + m:5*n + m + n_load].reshape(-1, 6)
+        ends = i32.reshape(-1, 2)
+        bad = []
 
         def copy(k):
             f = foams[k]
@@ -172,27 +148,26 @@ class RequestState:
             u8[a:b] = np.asarray(f['fixed'], dtype=bool)
             if n_load:
                 ext[a:b] = loads[k]
+            # the request's bonds with group-wide site ids (int32)
+            pairs = np.asarray(f['pairs']).reshape(-1, 2)
+            if len(pairs) and (pairs.min() < 0 or pairs.max() >= sites[k]):
+                bad.append(k)
+            np.add(pairs, a, out=ends[c:d], casting='unsafe')
         # numpy releases the GIL for these copies: spread the requests over threads
         list(_COPIERS.map(copy, range(len(foams))))
+        if bad:
+            raise ValueError('Invalid endpoint index')
         if np.any(mas <= 0):
             raise ValueError('Only positive-mass bodies can enter this solver')
-        # bond graphs from the device cache, concatenated with site and bond offsets
-        graphs = [_device_graph(f['pairs'], sites[k], self.device) for k, f in enumerate(foams)]
         dev64 = staging.send('f8', 5*n + m + n_load, self.device)
+        # one upload of the group's bonds and one device sort for its incidence CSR
+        edges = staging.send('i4', 2*m, self.device).view(-1, 2).to(torch.int64).contiguous()
+        inc_ptr, inc_bond = device_incidence(edges, n)
         self.external = dev64[5*n + m:].view(n, 6) if n_load else None
         self.fixed = staging.send('u1', n, self.device).view(torch.bool)
         self.p = dev64[:3*n].view(n, 3)
         self.radii = dev64[3*n:4*n]
         masses_d, areas_d = dev64[4*n:5*n], dev64[5*n:5*n + m]
-        if len(foams) == 1:
-            edges = graphs[0][0].to(torch.int64).contiguous()
-            inc_ptr, inc_bond = graphs[0][1], graphs[0][2]
-        else:
-            edges = torch.cat([g[0].to(torch.int64) + int(so[k]) for k, g in enumerate(graphs)]).contiguous()
-            inc_ptr = torch.cat([g[1][:-1] + 2*int(bo[k]) for k, g in enumerate(graphs)] +
-                                [torch.full((1,), 2*m, dtype=torch.int32, device=self.device)]).contiguous()
-            inc_bond = torch.cat([torch.where(g[2] >= 0, g[2] + int(bo[k]), g[2] - int(bo[k]))
-                                  for k, g in enumerate(graphs)]).contiguous()
         self.n_sites, self.n_bonds = n, m
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         self.n, self.ri, self.rj, self.offset = e(m, 3), e(m, 3), e(m, 3), e(m, 3)

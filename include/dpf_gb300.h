@@ -650,35 +650,6 @@ int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *
                            float *workspace, double *partials, unsigned *barrier, int *status, int threads,
                            int stages, void *stream);
 
-/* ---- Per-request Arnoldi over a served batch (no reference counterpart:
- * each request of a batch follows its own FGMRES of
- * experiments/bonded_dem_newton.py:13-60) ----
- * Segments are contiguous site ranges seg_ptr[r] .. seg_ptr[r+1] (int64,
- * R + 1 entries); seg (N) int32 gives each site's segment; active (R, uint8,
- * optional) skips segments (their results are 0).  Vectors are (N, 6)
- * doubles; a basis is `count` (<= 40) rows of ld doubles.  Sums are per
- * (segment, chunk) then over chunks in a fixed order (deterministic).
- * partials: dpf_segment_krylov_partials_doubles(R, count) doubles. */
-int64_t dpf_segment_krylov_partials_doubles(int n_segments, int count);
-
-/* out (R, count): out[r][k] = basis_k . w over segment r. */
-int dpf_segment_dots(int n_segments, const int64_t *seg_ptr, const uint8_t *active, const double *basis, int64_t ld,
-                     int count, const double *w, double *out, double *partials, void *stream);
-
-/* w -= sum_k h[r][k] basis_k on each active segment r (h (R, count));
- * norm2 (R) = |w|^2 per segment afterwards. */
-int dpf_segment_project(int n_segments, const int64_t *seg_ptr, const uint8_t *active, const double *basis,
-                        int64_t ld, int count, const double *h, double *w, double *norm2, double *partials,
-                        void *stream);
-
-/* out = scale[seg] * a on active segments, 0 on the others (scale (R)). */
-int dpf_segment_scale(int64_t n_sites, const int32_t *seg, const uint8_t *active, const double *scale,
-                      const double *a, double *out, void *stream);
-
-/* x += sum_k y[seg][k] rows_k (y (R, count), zero past a segment's own length). */
-int dpf_segment_combine(int64_t n_sites, const int32_t *seg, const double *rows, int64_t ld, int count,
-                        const double *y, double *x, void *stream);
-
 /* ---- Energy law (bond part of EnergyFoam with volume=False, kinematics='small') ----
  * Replaces EnergyFoam._bond_kinematics / energy / forces
  * (experiments/foam_dem_energy.py:303-315, 405-421, 797-811).  base (M, 4):
