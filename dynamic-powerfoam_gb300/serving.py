@@ -339,6 +339,7 @@ class Batch(MixedNewtonBonds):
         self._sweep_ready = True
         self._packed = None
         self._tiles = None
+        self._end_variant = None       # bond-end sweep launch shape, from the autotuner's size-class cache
         self.tile_timings = {}
         self._cached = None
         self._loads = take64(6*n, (n, 6))

@@ -154,10 +154,9 @@ def autotune(solver, run, candidates=CANDIDATES, repeats=3):
 
 
 # Launch shape of the bond-end sweep per (device, size class): the autotuner
-# times each compiled variant (lanes per site x CTAs per SM, see
-# dpf_end_variant_shape) on the first elastic PCG of a graph of that size
+# times each compiled variant (lanes per site x CTAs per SM x record
+# look-ahead, see dpf_end_variant_shape) on the first elastic PCG of a graph of that size
 # class and keeps the fastest for every later graph of the class.
-END_VARIANTS = 6
 _END_TUNED = {}
 
 
@@ -179,7 +178,7 @@ def tune_end_sweep(solver, vector, iterations=5):
     count = torch.zeros(1, dtype=torch.int32, device=solver.device)
     stream = torch.cuda.current_stream(solver.device)
     times = {}
-    for variant in range(END_VARIANTS):
+    for variant in range(_lib.load().dpf_end_variant_count()):
         solver._end_pcg(vector, scratch, 0., iterations, count, variant=variant)
         start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         start.record(stream)
