@@ -458,11 +458,10 @@ def _end_shape(variant):
     """(lanes per site, CTAs per SM) of a bond-end sweep variant."""
     import ctypes
     from dpf_gb300 import _lib
-    lanes, blocks, ahead = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
-    _lib.check(_lib.load().dpf_end_variant_shape(int(variant), ctypes.byref(lanes), ctypes.byref(blocks),
-                                                 ctypes.byref(ahead)), 'dpf_end_variant_shape')
-    return dict(variant=int(variant), lanes_per_site=lanes.value, ctas_per_sm=blocks.value,
-                records_one_round_ahead=bool(ahead.value))
+    lanes, blocks = ctypes.c_int(), ctypes.c_int()
+    _lib.check(_lib.load().dpf_end_variant_shape(int(variant), ctypes.byref(lanes), ctypes.byref(blocks)),
+               'dpf_end_variant_shape')
+    return dict(variant=int(variant), lanes_per_site=lanes.value, ctas_per_sm=blocks.value)
 
 
 def _platen_problem(m, seed=0):

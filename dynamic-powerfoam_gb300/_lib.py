@@ -119,7 +119,7 @@ SIGNATURES = {
     'dpf_end_floats': (i64, [i64]),
     'dpf_end_pack': (i32, [P(Graph), vp, f64, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_end_variant_count': (i32, []),
-    'dpf_end_variant_shape': (i32, [i32, P(ctypes.c_int), P(ctypes.c_int), P(ctypes.c_int)]),
+    'dpf_end_variant_shape': (i32, [i32, P(ctypes.c_int), P(ctypes.c_int)]),
     'dpf_end_hvp': (i32, [P(Graph), vp, vp, vp, vp, i32, vp]),
     'dpf_end_precondition': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, vp, vp,
                                    i32, vp]),

@@ -609,11 +609,9 @@ __device__ __forceinline__ void sym_mv6(const float P[21], const float x[6], flo
 // 4 CTAs per SM).
 constexpr int kEndThreads = 256;
 constexpr int kEndPcgThreads = 256;
-constexpr int kEndVariants = 9;
-constexpr int kEndVariantLanes[kEndVariants] = {8, 4, 16, 8, 4, 8, 8, 8, 4};
-constexpr int kEndVariantBlocks[kEndVariants] = {4, 4, 4, 3, 2, 2, 2, 3, 2};
-// variants 6-8 load each lane's next-round end records one round ahead
-constexpr bool kEndVariantAhead[kEndVariants] = {false, false, false, false, false, false, true, true, true};
+constexpr int kEndVariants = 6;
+constexpr int kEndVariantLanes[kEndVariants] = {8, 4, 16, 8, 4, 8};
+constexpr int kEndVariantBlocks[kEndVariants] = {4, 4, 4, 3, 2, 2};
 
 struct EndGraph {
     int64_t n;
@@ -711,96 +709,6 @@ __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi 
     }
 }
 
-// for_ends with the first step's end records (and CSR bounds) of each
-// lane's next site loaded one round ahead, so that their DRAM latency
-// overlaps the current round's gathers and arithmetic.  Same sums in the same
-// order as for_ends.
-template <int L, bool kConst, class Epi>
-__device__ __forceinline__ void for_ends_ahead(const EndGraph &G, const float *q, Epi &epi) {
-    constexpr int kSites = 32 / L;
-    const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
-    const int lane32 = (int)threadIdx.x & 31, lane = lane32 & (L - 1);
-    const int64_t chunks = (G.n + kSites - 1) / kSites;
-    const int64_t rounds = (chunks + warps - 1) / warps;
-    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    // the first step of round r: ends k, k + L of site s (if below k1)
-    auto bounds = [&](int64_t r, int &k, int &k1) {
-        const int64_t s = (warp + r * warps) * kSites + lane32 / L;
-        k = k1 = 0;
-        if (r < rounds && s < G.n && !(G.active && !G.active[G.seg[s]])) {
-            k = G.ptr[s] + lane;
-            k1 = G.ptr[s + 1];
-        }
-    };
-    int k = 0, k1 = 0;
-    bounds(0, k, k1);
-    float4 a = zero, b = zero, c = zero, a2 = zero, b2 = zero, c2 = zero;
-    if (k < k1) {
-        a = __ldcs(G.e0 + k);
-        b = __ldcs(G.e1 + k);
-        c = __ldcs(G.e2 + k);
-        if (k + L < k1) {
-            a2 = __ldcs(G.e0 + k + L);
-            b2 = __ldcs(G.e1 + k + L);
-            c2 = __ldcs(G.e2 + k + L);
-        }
-    }
-    for (int64_t r = 0; r < rounds; ++r) {
-        const int64_t s = (warp + r * warps) * kSites + lane32 / L;
-        const bool valid = s < G.n;
-        // next round's bounds and first records, in flight during this round
-        int nk, nk1;
-        bounds(r + 1, nk, nk1);
-        float4 na = zero, nb = zero, nc = zero, na2 = zero, nb2 = zero, nc2 = zero;
-        if (nk < nk1) {
-            na = __ldcs(G.e0 + nk);
-            nb = __ldcs(G.e1 + nk);
-            nc = __ldcs(G.e2 + nk);
-            if (nk + L < nk1) {
-                na2 = __ldcs(G.e0 + nk + L);
-                nb2 = __ldcs(G.e1 + nk + L);
-                nc2 = __ldcs(G.e2 + nk + L);
-            }
-        }
-        float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, qs[6];
-        if (valid) load_q<kConst>(q, s, qs);
-        if (k < k1) {
-            const bool two = k + L < k1;
-            float qo[6], qo2[6];
-            load_q<kConst>(q, (int64_t)__float_as_int(c.w), qo);
-            if (two) load_q<kConst>(q, (int64_t)__float_as_int(c2.w), qo2);
-            end_wrench(a, b, c, qs, qo, acc);
-            if (two) end_wrench(a2, b2, c2, qs, qo2, acc);
-            // the site's further ends, loaded in the round as for_ends does
-            for (int kk = k + 2 * L; kk < k1; kk += 2 * L) {
-                const int kk2 = kk + L;
-                const bool two2 = kk2 < k1;
-                const float4 ea = __ldcs(G.e0 + kk), eb = __ldcs(G.e1 + kk), ec = __ldcs(G.e2 + kk);
-                float4 ea2 = ea, eb2 = eb, ec2 = ec;
-                if (two2) {
-                    ea2 = __ldcs(G.e0 + kk2);
-                    eb2 = __ldcs(G.e1 + kk2);
-                    ec2 = __ldcs(G.e2 + kk2);
-                }
-                float po[6], po2[6];
-                load_q<kConst>(q, (int64_t)__float_as_int(ec.w), po);
-                load_q<kConst>(q, (int64_t)__float_as_int(ec2.w), po2);
-                end_wrench(ea, eb, ec, qs, po, acc);
-                if (two2) end_wrench(ea2, eb2, ec2, qs, po2, acc);
-            }
-        }
-#pragma unroll
-        for (int o = 1; o < L; o <<= 1)
-#pragma unroll
-            for (int cc = 0; cc < 6; ++cc) acc[cc] += __shfl_xor_sync(0xffffffffu, acc[cc], o);
-        if (valid && lane == 0) epi(s, qs, G.site[s], acc);
-        k = nk;
-        k1 = nk1;
-        a = na, b = nb, c = nc, a2 = na2, b2 = nb2, c2 = nc2;
-    }
-}
-
 struct EndHvpEpi {
     float *y;
     __device__ __forceinline__ void operator()(int64_t s, const float *qs, float4 rec, const float acc[6]) const {
@@ -814,13 +722,10 @@ struct EndHvpEpi {
     }
 };
 
-template <int L, int B, bool A>
+template <int L, int B>
 __global__ void __launch_bounds__(kEndThreads, B) end_hvp_kernel(EndGraph G, const float *q, float *y) {
     EndHvpEpi epi{y};
-    if (A)
-        for_ends_ahead<L, true>(G, q, epi);
-    else
-        for_ends<L, true>(G, q, epi);
+    for_ends<L, true>(G, q, epi);
 }
 
 // One thread per incidence k of site s (site-major): the end record of bond
@@ -932,7 +837,7 @@ __device__ __forceinline__ float update_site(const PcgArgs &a, int64_t s, float 
 }
 
 // kTiles: w = A u by the tiled sweep, else by the bond-end sweep.
-template <bool kTiles, int L, bool A = false>
+template <bool kTiles, int L>
 __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -978,8 +883,6 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
         bool ok = true;
         if (kTiles)
             ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
-        else if (A)
-            for_ends_ahead<L, false>(a.E, a.u, epi);
         else
             for_ends<L, false>(a.E, a.u, epi);
         part = block_sum((double)epi.dot);
@@ -1021,9 +924,9 @@ __global__ void __launch_bounds__(kTileThreadsMax + 64, DPF_TILE_MIN_BLOCKS) til
     pcg_body<true, 8>(a, smem);
 }
 
-template <int L, int B, bool A>
+template <int L, int B>
 __global__ void __launch_bounds__(kEndPcgThreads, B) end_pcg_kernel(PcgArgs a) {
-    pcg_body<false, L, A>(a, nullptr);
+    pcg_body<false, L>(a, nullptr);
 }
 
 // The kernels of variant v (0 <= v < kEndVariants).
@@ -1031,28 +934,22 @@ using EndHvpKernel = void (*)(EndGraph, const float *, float *);
 using EndPcgKernel = void (*)(PcgArgs);
 inline EndHvpKernel end_hvp_variant(int v) {
     switch (v) {
-    case 1: return end_hvp_kernel<4, 4, false>;
-    case 2: return end_hvp_kernel<16, 4, false>;
-    case 3: return end_hvp_kernel<8, 3, false>;
-    case 4: return end_hvp_kernel<4, 2, false>;
-    case 5: return end_hvp_kernel<8, 2, false>;
-    case 6: return end_hvp_kernel<8, 2, true>;
-    case 7: return end_hvp_kernel<8, 3, true>;
-    case 8: return end_hvp_kernel<4, 2, true>;
-    default: return end_hvp_kernel<8, 4, false>;
+    case 1: return end_hvp_kernel<4, 4>;
+    case 2: return end_hvp_kernel<16, 4>;
+    case 3: return end_hvp_kernel<8, 3>;
+    case 4: return end_hvp_kernel<4, 2>;
+    case 5: return end_hvp_kernel<8, 2>;
+    default: return end_hvp_kernel<8, 4>;
     }
 }
 inline EndPcgKernel end_pcg_variant(int v) {
     switch (v) {
-    case 1: return end_pcg_kernel<4, 4, false>;
-    case 2: return end_pcg_kernel<16, 4, false>;
-    case 3: return end_pcg_kernel<8, 3, false>;
-    case 4: return end_pcg_kernel<4, 2, false>;
-    case 5: return end_pcg_kernel<8, 2, false>;
-    case 6: return end_pcg_kernel<8, 2, true>;
-    case 7: return end_pcg_kernel<8, 3, true>;
-    case 8: return end_pcg_kernel<4, 2, true>;
-    default: return end_pcg_kernel<8, 4, false>;
+    case 1: return end_pcg_kernel<4, 4>;
+    case 2: return end_pcg_kernel<16, 4>;
+    case 3: return end_pcg_kernel<8, 3>;
+    case 4: return end_pcg_kernel<4, 2>;
+    case 5: return end_pcg_kernel<8, 2>;
+    default: return end_pcg_kernel<8, 4>;
     }
 }
 
@@ -1458,11 +1355,10 @@ static EndGraph end_graph(const dpf_graph *g, const float *ends, const float *si
 
 int dpf_end_variant_count(void) { return kEndVariants; }
 
-int dpf_end_variant_shape(int variant, int *lanes, int *blocks_per_sm, int *lookahead) {
+int dpf_end_variant_shape(int variant, int *lanes, int *blocks_per_sm) {
     if (variant < 0 || variant >= kEndVariants) return DPF_ERR_ARGUMENT;
     if (lanes) *lanes = kEndVariantLanes[variant];
     if (blocks_per_sm) *blocks_per_sm = kEndVariantBlocks[variant];
-    if (lookahead) *lookahead = kEndVariantAhead[variant] ? 1 : 0;
     return DPF_OK;
 }
 

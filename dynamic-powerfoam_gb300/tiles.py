@@ -154,8 +154,8 @@ def autotune(solver, run, candidates=CANDIDATES, repeats=3):
 
 
 # Launch shape of the bond-end sweep per (device, size class): the autotuner
-# times each compiled variant (lanes per site x CTAs per SM x record
-# look-ahead, see dpf_end_variant_shape) on the first elastic PCG of a graph of that size
+# times each compiled variant (lanes per site x CTAs per SM, see
+# dpf_end_variant_shape) on the first elastic PCG of a graph of that size
 # class and keeps the fastest for every later graph of the class.
 _END_TUNED = {}
 

@@ -621,14 +621,12 @@ int dpf_end_pack(const dpf_graph *g, const float *bond_data, double alpha, const
                  const uint8_t *fixed, float *ends, float *P24, float *site4, void *stream);
 
 /* Number of bond-end sweep variants, and the launch shape of variant
- * `variant` (0 .. count - 1): lanes per site (4, 8 or 16), resident
+ * `variant` (0 .. count - 1): lanes per site (4, 8 or 16) and resident
  * 256-thread CTAs per SM (2, 3 or 4; fewer CTAs leave more registers per
- * thread) and whether each lane loads its next site's end records one round
- * ahead (1) or in the round (0).  Variant 0 (8 lanes, 4 CTAs, in the round)
- * is the default; an autotuner may pick another per graph size.  Any output
- * pointer may be NULL. */
+ * thread).  Variant 0 (8 lanes, 4 CTAs) is the default; an autotuner may
+ * pick another per graph size.  Output pointers may be NULL. */
 int dpf_end_variant_count(void);
-int dpf_end_variant_shape(int variant, int *lanes, int *blocks_per_sm, int *lookahead);
+int dpf_end_variant_shape(int variant, int *lanes, int *blocks_per_sm);
 
 /* y = (diag M + alpha K) q in float32 from the end records; q, y (N, 6)
  * float32, 8-byte aligned; variant as dpf_end_variant_shape. */

@@ -88,7 +88,7 @@ def test_end_hvp_matches_float64_product():
     lib = _lib.load()
     for variant in range(1, lib.dpf_end_variant_count()):
         lanes, blocks = ctypes.c_int(), ctypes.c_int()
-        assert lib.dpf_end_variant_shape(variant, ctypes.byref(lanes), ctypes.byref(blocks), None) == 0
+        assert lib.dpf_end_variant_shape(variant, ctypes.byref(lanes), ctypes.byref(blocks)) == 0
         y3 = torch.empty_like(q32)
         _lib.call('dpf_end_hvp', ctypes.byref(s._graph), s._ends.data_ptr(), s._site4.data_ptr(), q32.data_ptr(),
                   y3.data_ptr(), variant, s._stream())
