@@ -697,8 +697,10 @@ def run_ours(args):
 
     # roofline of the dominant launch
     kernels = {}
-    for key, pairs in profile.items():
-        durations = [a.elapsed_time(b) for a, b in pairs]
+    for key, entries in profile.items():
+        # (start, end) CUDA events of the Python control path, or milliseconds
+        # per launch measured by the library's step driver
+        durations = [e if isinstance(e, float) else e[0].elapsed_time(e[1]) for e in entries]
         kernels[key] = dict(launches=len(durations), total_ms=sum(durations),
                             mean_ms=sum(durations)/len(durations))
     cg = sum(i['cg_iterations'] for i in profiled)

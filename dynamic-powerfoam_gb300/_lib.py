@@ -62,6 +62,43 @@ class Tiles(ctypes.Structure):
                 ('entry_ends', vp), ('tile_desc', vp), ('tile_meta', vp)]
 
 
+class MixedNewton(ctypes.Structure):
+    """dpf_mixed_newton: buffers of a MixedNewtonBonds solver for the native step driver."""
+    _fields_ = ([('graph', vp), ('stiffness', Stiffness)] +
+                [(k, vp) for k in ('radii', 'mass', 'mass32', 'fixed', 'bond_data', 'r0', 'loads', 'scales',
+                                   'wrench64', 'partials', 'scalars', 'status', 'y32', 'd32', 'wrench32', 'block32',
+                                   'p32', 'units', 'units32', 'ends', 'site4', 'p24', 'end_workspace',
+                                   'end_partials', 'barrier', 'inner', 'basis', 'transformed', 'h')] +
+                [('krylov_width', i32)] +
+                [(k, vp) for k in ('krylov_partials', 'krylov_scalars', 'vectors', 'host')] +
+                [('end_variant', i32)])
+
+
+class NewtonStep(ctypes.Structure):
+    """dpf_newton_step: one step's inputs and end-state outputs."""
+    _fields_ = ([('dt', f64), ('external', vp), ('v', vp), ('rotation', vp), ('history', History)] +
+                [(k, vp) for k in ('x_end', 'normal_end', 'offset_end', 'fn_end', 'fs_end', 'mt_end', 'mb_end')] +
+                [('tolerance', f64), ('pose_tolerance', f64), ('linear_tolerance', f64),
+                 ('max_iterations', i32), ('refresh', i32), ('timing', i32)])
+
+
+NEWTON_VECTORS = 11
+NEWTON_HOST_DOUBLES = 128
+NEWTON_TRACE = 32
+NEWTON_TIMERS = ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit')
+(NEWTON_CONVERGED, NEWTON_GUARD, NEWTON_NONFINITE, NEWTON_SINGULAR, NEWTON_KRYLOV, NEWTON_LINE_SEARCH,
+ NEWTON_DIVERGED) = range(7)
+
+
+class NewtonInfo(ctypes.Structure):
+    """dpf_newton_info: outcome, iteration counts, norms, trace and launch times of a step."""
+    _fields_ = ([(k, i32) for k in ('outcome', 'guard', 'nonlinear_iterations', 'krylov_iterations',
+                                    'cg_iterations', 'launches')] +
+                [(k, f64) for k in ('relative', 'local', 'work', 'max_rotation', 'krylov_relative')] +
+                [('trace_len', i32), ('trace', f64*(2*NEWTON_TRACE)), ('time_ms', f64*len(NEWTON_TIMERS)),
+                 ('timed_launches', i32*len(NEWTON_TIMERS))])
+
+
 P = ctypes.POINTER
 SIGNATURES = {
     'dpf_wrench_scratch_doubles': (i64, [i64]),
@@ -151,6 +188,8 @@ SIGNATURES = {
     'dpf_anderson_gram': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, vp, vp, vp, vp]),
     'dpf_anderson_mix': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, P(ctypes.c_double), vp, vp, vp]),
     'dpf_barrier_selftest': (i32, [i32, i64, i32, vp, vp, vp, vp]),
+    'dpf_mixed_newton_step': (i32, [P(MixedNewton), P(NewtonStep), P(NewtonInfo), vp]),
+    'dpf_newton_struct_sizes': (i32, [P(ctypes.c_int64)]),
 }
 
 

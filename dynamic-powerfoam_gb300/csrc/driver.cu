@@ -1,0 +1,457 @@
+// Native step driver of the mixed-precision Newton solver: the control flow of
+// NewtonBonds.step and fgmres (experiments/bonded_dem_newton.py:13-60,
+// 132-201) as host code that launches this library's entry points directly.
+//
+// The Python control path (MixedNewtonBonds.step) and this driver issue the
+// same entry points in the same order with the same arguments, and take the
+// same host decisions in float64 (Givens rotations with hypot, back
+// substitution, convergence tests, Armijo line search), so a step gives
+// bit-identical results either way.  What changes is the host cost between
+// launches: a few microseconds of C++ instead of Python, which matters after
+// each of the step's small device reads (the FGMRES Hessenberg column, the
+// residual norms), when the GPU idles until the next launch arrives.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "dpf_gb300.h"
+
+namespace dpf {
+namespace driver {
+
+// max over sites of |y_w| (the rotation part of the increment); non-negative
+// doubles order like their bit patterns, so an integer atomicMax is exact.
+__global__ void max_rotation_kernel(int64_t n, const double *y, unsigned long long *out) {
+    double best = 0.0;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const double *w = y + 6 * s + 3;
+        const double v = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        best = v > best ? v : best;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        const double other = __shfl_xor_sync(0xffffffffu, best, o);
+        best = other > best ? other : best;
+    }
+    if ((threadIdx.x & 31) == 0 && best > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
+}
+
+enum Timer { kSetup = 0, kResidual, kScaling, kPcg, kJvp, kCommit };
+
+// CUDA events around the hot launches (only with step->timing), created for
+// the call and destroyed before it returns.
+struct Timing {
+    bool on = false;
+    cudaStream_t stream = nullptr;
+    std::vector<int> keys;
+    std::vector<cudaEvent_t> events;
+    void record(bool opening, int key) {
+        if (!on) return;
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) != cudaSuccess) {
+            on = false;  // no timing rather than a failed step
+            return;
+        }
+        if (opening) keys.push_back(key);
+        events.push_back(e);
+        cudaEventRecord(e, stream);
+    }
+    void begin(int key) { record(true, key); }
+    void end() { record(false, 0); }
+    // after the stream has been synchronised
+    void collect(dpf_newton_info *info) {
+        for (size_t k = 0; k < keys.size() && 2 * k + 1 < events.size(); ++k) {
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, events[2 * k], events[2 * k + 1]) == cudaSuccess) {
+                info->time_ms[keys[k]] += ms;
+                info->timed_launches[keys[k]] += 1;
+            }
+        }
+    }
+    ~Timing() {
+        for (cudaEvent_t e : events) cudaEventDestroy(e);
+    }
+};
+
+struct Step {
+    const dpf_mixed_newton *s;
+    const dpf_newton_step *a;
+    dpf_newton_info *info;
+    cudaStream_t st;
+    int64_t n, n6;
+    double *y, *cand, *r, *r_cand, *scaled, *rhs, *x, *res, *w, *corr, *ax;
+    double *host;     // pinned: [0..8) scalars, [8..10) scales, [16..16+72) h column
+    int *host_int;    // pinned ints after the doubles: [0] status, [1] inner
+    Timing timing;
+    bool packed = false;
+    double rhs_scale = -1.0;
+
+    int launched(int count) {
+        info->launches += count;
+        return DPF_OK;
+    }
+
+    // copy `count` device scalars (and optionally the status word and the
+    // step's scales) to pinned memory, then wait for the stream
+    int fetch(int count, bool status, bool scales) {
+        if (count && cudaMemcpyAsync(host, s->scalars, count * sizeof(double), cudaMemcpyDeviceToHost, st))
+            return DPF_ERR_CUDA;
+        if (status && cudaMemcpyAsync(host_int, s->status, sizeof(int), cudaMemcpyDeviceToHost, st))
+            return DPF_ERR_CUDA;
+        if (scales && cudaMemcpyAsync(host + 8, s->scales, 2 * sizeof(double), cudaMemcpyDeviceToHost, st))
+            return DPF_ERR_CUDA;
+        return cudaStreamSynchronize(st) == cudaSuccess ? DPF_OK : DPF_ERR_CUDA;
+    }
+
+    int residual(const double *yy, double *out, bool use_p) {
+        int rc = dpf_to_float(n6, yy, s->y32, st);
+        if (rc) return rc;
+        launched(1);
+        if (cudaMemsetAsync(s->status, 0, sizeof(int), st)) return DPF_ERR_CUDA;
+        timing.begin(kResidual);
+        rc = dpf_mixed_residual(s->graph, s->bond_data, yy, s->y32, s->mass, s->fixed, a->dt, s->r0, 1,
+                                use_p ? s->p32 : nullptr, use_p ? s->units32 : nullptr, out, nullptr,
+                                use_p ? s->scalars : nullptr, s->wrench32, s->partials, s->status, st);
+        timing.end();
+        return rc ? rc : launched(s->graph->n_bonds ? 2 : 1);
+    }
+
+    // norms of the iterate's residual r: [|r|, max |s|, |s|] into s->scalars
+    int iteration_norms() {
+        timing.begin(kScaling);
+        int rc = dpf_mixed_scaling(s->graph, s->bond_data, s->mass32, s->fixed, s->radii, a->dt, s->block32, s->p32,
+                                   s->units, s->units32, st);
+        timing.end();
+        if (rc) return rc;
+        launched(1);
+        rc = dpf_mixed_scale_residual(n, s->p32, s->units32, r, scaled, s->scalars, s->partials, st);
+        return rc ? rc : launched(1);
+    }
+
+    int precondition(const double *vector, double *out) {
+        int rc;
+        if (!packed) {
+            rc = dpf_end_pack(s->graph, s->bond_data, 0.25 * a->dt * a->dt, s->p32, s->mass32, s->fixed, s->ends,
+                              s->p24, s->site4, st);
+            if (rc) return rc;
+            launched(2);
+            packed = true;
+        }
+        timing.begin(kPcg);
+        rc = dpf_end_precondition(s->graph, s->ends, s->site4, s->fixed, s->block32, s->p24, s->units32, vector, 0.03,
+                                  80, out, s->inner, s->end_workspace, s->end_partials, s->barrier, s->status,
+                                  nullptr, nullptr, s->end_variant, st);
+        timing.end();
+        return rc ? rc : launched(1);
+    }
+
+    int jvp(const double *direction, double *out) {
+        timing.begin(kJvp);
+        const int rc = dpf_mixed_jacobian_vector(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
+                                                 a->dt, s->units32, s->p32, out, s->d32, s->wrench32, nullptr,
+                                                 nullptr, st);
+        timing.end();
+        return rc ? rc : launched(s->graph->n_bonds ? 3 : 2);
+    }
+
+    int norm_of(const double *v, double *out) {
+        int rc = dpf_dot_norm(n6, v, nullptr, s->krylov_scalars, s->krylov_partials, st);
+        if (rc) return rc;
+        launched(1);
+        if (cudaMemcpyAsync(host + 12, s->krylov_scalars + 1, sizeof(double), cudaMemcpyDeviceToHost, st) ||
+            cudaStreamSynchronize(st))
+            return DPF_ERR_CUDA;
+        *out = host[12];
+        return DPF_OK;
+    }
+
+    // Right-preconditioned FGMRES with CGS2 Arnoldi (fgmres in newton.py):
+    // solves J delta = b with b = rhs, |b| = norm; x = delta.  Sets *ok.
+    int fgmres(double norm, double tolerance, int restart, int max_iterations, bool *ok, int *krylov) {
+        *ok = false;
+        *krylov = 0;
+        if (cudaMemsetAsync(x, 0, n6 * sizeof(double), st)) return DPF_ERR_CUDA;
+        if (norm == 0.0) {
+            *ok = true;
+            return DPF_OK;
+        }
+        int iterations = 0;
+        double relative = NAN;
+        double residual_norm = norm;
+        bool first = true;
+        double H[64 * 63];
+        double cs[64], sn[64], g[65], coef[64];
+        while (iterations < max_iterations) {
+            const int width = restart < max_iterations - iterations ? restart : max_iterations - iterations;
+            if (width > s->krylov_width) return DPF_ERR_ARGUMENT;
+            const int ldh = width;  // H is (width + 1) x width, row-major
+            std::memset(H, 0, sizeof(double) * (width + 1) * width);
+            std::memset(cs, 0, sizeof(double) * width);
+            std::memset(sn, 0, sizeof(double) * width);
+            std::memset(g, 0, sizeof(double) * (width + 1));
+            if (first) {
+                g[0] = residual_norm;
+            } else {
+                const int rc = norm_of(res, &g[0]);
+                if (rc) return rc;
+            }
+            const double *start = first ? rhs : res;
+            first = false;
+            int rc = dpf_axpby(n6, 1.0 / g[0], start, 0.0, start, s->basis, st);
+            if (rc) return rc;
+            launched(1);
+            for (int j = 0; j < width; ++j) {
+                double *bj = s->basis + (int64_t)j * n6;
+                double *tj = s->transformed + (int64_t)j * n6;
+                rc = precondition(bj, tj);
+                if (rc) return rc;
+                rc = jvp(tj, w);
+                if (rc) return rc;
+                rc = dpf_arnoldi_cgs2(n6, s->basis, n6, j, w, s->h, s->krylov_partials, st);
+                if (rc) return rc;
+                launched(4);
+                double *column = host + 16;
+                if (cudaMemcpyAsync(column, s->h, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st) ||
+                    cudaStreamSynchronize(st))
+                    return DPF_ERR_CUDA;
+                for (int k = 0; k <= j + 1; ++k) H[k * ldh + j] = column[k];
+                const bool breakdown = H[(j + 1) * ldh + j] < 1e-14;
+                for (int k = 0; k < j; ++k) {
+                    const double hk = H[k * ldh + j], hk1 = H[(k + 1) * ldh + j];
+                    H[k * ldh + j] = cs[k] * hk + sn[k] * hk1;
+                    H[(k + 1) * ldh + j] = -sn[k] * hk + cs[k] * hk1;
+                }
+                const double denominator = std::hypot(H[j * ldh + j], H[(j + 1) * ldh + j]);
+                if (denominator == 0.0) {
+                    info->outcome = DPF_NEWTON_SINGULAR;
+                    return DPF_OK;
+                }
+                cs[j] = H[j * ldh + j] / denominator;
+                sn[j] = H[(j + 1) * ldh + j] / denominator;
+                H[j * ldh + j] = denominator;
+                H[(j + 1) * ldh + j] = 0.0;
+                const double gj = g[j];
+                g[j + 1] = -sn[j] * gj;
+                g[j] = cs[j] * gj;
+                iterations += 1;
+                if (std::fabs(g[j + 1]) <= tolerance * norm || breakdown || j + 1 == width) {
+                    // back substitution of the (j+1) x (j+1) upper triangle
+                    const int k = j + 1;
+                    for (int i = k - 1; i >= 0; --i) {
+                        double acc = g[i];
+                        for (int c = i + 1; c < k; ++c) acc -= H[i * ldh + c] * coef[c];
+                        coef[i] = acc / H[i * ldh + i];
+                    }
+                    rc = dpf_combine_rows(n6, s->transformed, n6, k, coef, x, st);
+                    if (rc) return rc;
+                    launched(1);
+                    rc = jvp(x, ax);
+                    if (rc) return rc;
+                    rc = dpf_axpby(n6, 1.0, rhs, -1.0, ax, res, st);
+                    if (rc) return rc;
+                    launched(1);
+                    double rn;
+                    rc = norm_of(res, &rn);
+                    if (rc) return rc;
+                    relative = rn / norm;
+                    if (relative <= 1.05 * tolerance) {
+                        *ok = true;
+                        *krylov = iterations;
+                        info->krylov_relative = relative;
+                        return DPF_OK;
+                    }
+                    break;
+                }
+            }
+        }
+        *krylov = iterations;
+        info->krylov_relative = relative;
+        return DPF_OK;
+    }
+
+    int accept() {
+        int rc = dpf_to_float(n6, y, s->y32, st);
+        if (rc) return rc;
+        launched(1);
+        const dpf_history &h = a->history;
+        timing.begin(kCommit);
+        rc = dpf_mixed_commit(s->graph, s->bond_data, &h, y, s->y32, a->x_end, a->normal_end, a->offset_end, a->fn_end,
+                              a->fs_end, a->mt_end, a->mb_end, s->wrench32, s->loads, st);
+        timing.end();
+        if (rc) return rc;
+        launched(s->graph->n_bonds ? 2 : 1);
+        rc = dpf_accept_step(n, y, a->dt, a->v, a->rotation, st);
+        if (rc) return rc;
+        launched(1);
+        rc = dpf_dot_norm(n6, a->external, y, s->scalars, s->partials, st);
+        if (rc) return rc;
+        launched(1);
+        if (cudaMemsetAsync(s->scalars + 2, 0, sizeof(double), st)) return DPF_ERR_CUDA;
+        const int grid = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+        max_rotation_kernel<<<grid, 256, 0, st>>>(n, y, reinterpret_cast<unsigned long long *>(s->scalars + 2));
+        if (cudaGetLastError() != cudaSuccess) return DPF_ERR_CUDA;
+        launched(1);
+        if (cudaMemcpyAsync(host_int + 1, s->inner, sizeof(int), cudaMemcpyDeviceToHost, st)) return DPF_ERR_CUDA;
+        rc = fetch(3, false, false);
+        if (rc) return rc;
+        info->work = host[0];
+        info->max_rotation = host[2];
+        info->cg_iterations = host_int[1];
+        return DPF_OK;
+    }
+
+    int run() {
+        if (cudaMemsetAsync(s->inner, 0, sizeof(int), st) || cudaMemsetAsync(s->status, 0, sizeof(int), st) ||
+            cudaMemsetAsync(y, 0, n6 * sizeof(double), st))
+            return DPF_ERR_CUDA;
+        int rc;
+        timing.begin(kSetup);
+        if (a->refresh) {
+            const dpf_history &h = a->history;
+            rc = dpf_mixed_setup(s->graph, &s->stiffness, &h, s->mass, a->v, a->external, s->fixed, a->dt,
+                                 s->bond_data, s->r0, s->loads, s->scales, s->wrench64, s->partials, s->status, st);
+            if (!rc) launched(s->graph->n_bonds ? 2 : 1);
+        } else {
+            rc = dpf_mixed_begin(n, s->loads, s->mass, a->v, a->external, s->fixed, a->dt, s->r0, s->scales,
+                                 s->partials, st);
+            if (!rc) launched(1);
+        }
+        timing.end();
+        if (rc) return rc;
+        bool cached = false;
+        const double dt = a->dt;
+        for (int iteration = 0; iteration <= a->max_iterations; ++iteration) {
+            if (!cached) {
+                rc = residual(y, r, false);
+                if (rc) return rc;
+            }
+            rc = iteration_norms();
+            if (rc) return rc;
+            const bool first = rhs_scale < 0.0;
+            rc = fetch(3, !cached, first);
+            if (rc) return rc;
+            const int status = cached ? 0 : host_int[0];
+            if (status) {
+                info->outcome = DPF_NEWTON_GUARD;
+                info->guard = status;
+                return DPF_OK;
+            }
+            cached = false;
+            packed = false;
+            const double rnorm = host[0], local = host[1], merit = host[2];
+            if (first) {
+                const double sa = host[8], sl = host[9];
+                double v = sa;
+                if (0.5 * dt * dt * sl > v) v = 0.5 * dt * dt * sl;
+                if (1e-30 > v) v = 1e-30;
+                rhs_scale = v;
+            }
+            const double relative = rnorm / rhs_scale;
+            info->relative = relative;
+            info->local = local;
+            info->nonlinear_iterations = iteration;
+            if (!std::isfinite(relative) || !std::isfinite(local)) {
+                info->outcome = DPF_NEWTON_NONFINITE;
+                return DPF_OK;
+            }
+            if (info->trace_len < DPF_NEWTON_TRACE) {
+                info->trace[2 * info->trace_len] = relative;
+                info->trace[2 * info->trace_len + 1] = local;
+                info->trace_len += 1;
+            }
+            if (relative < a->tolerance && local < a->pose_tolerance) {
+                rc = accept();
+                if (rc) return rc;
+                info->outcome = DPF_NEWTON_CONVERGED;
+                return DPF_OK;
+            }
+            if (iteration == a->max_iterations) break;
+            rc = dpf_axpby(n6, -1.0, scaled, 0.0, scaled, rhs, st);
+            if (rc) return rc;
+            launched(1);
+            bool ok;
+            int krylov;
+            rc = fgmres(merit, a->linear_tolerance, 32, 256, &ok, &krylov);
+            if (rc) return rc;
+            if (info->outcome == DPF_NEWTON_SINGULAR) return DPF_OK;
+            if (!ok) {
+                info->outcome = DPF_NEWTON_KRYLOV;
+                return DPF_OK;
+            }
+            info->krylov_iterations += krylov;
+            rc = dpf_masked_scale(n, x, s->units, s->fixed, corr, st);
+            if (rc) return rc;
+            launched(1);
+            bool accepted = false;
+            for (int power = 0; power < 10; ++power) {
+                const double factor = std::ldexp(1.0, -power);
+                rc = dpf_axpby(n6, 1.0, y, factor, corr, cand, st);
+                if (rc) return rc;
+                launched(1);
+                rc = residual(cand, r_cand, true);
+                if (rc) return rc;
+                rc = fetch(3, true, false);
+                if (rc) return rc;
+                if (host_int[0]) continue;
+                if (host[2] < (1.0 - 1e-4 * factor) * merit) {
+                    double *t = y;
+                    y = cand;
+                    cand = t;
+                    t = r;
+                    r = r_cand;
+                    r_cand = t;
+                    cached = true;
+                    accepted = true;
+                    break;
+                }
+            }
+            if (!accepted) {
+                info->outcome = DPF_NEWTON_LINE_SEARCH;
+                return DPF_OK;
+            }
+        }
+        info->outcome = DPF_NEWTON_DIVERGED;
+        return DPF_OK;
+    }
+};
+
+}  // namespace driver
+}  // namespace dpf
+
+extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_newton_step *step,
+                                     dpf_newton_info *info, void *stream) {
+    using dpf::driver::Step;
+    if (!solver || !step || !info || !solver->graph || solver->graph->n_sites <= 0 || !solver->vectors ||
+        !solver->host || !solver->basis || !solver->transformed || !solver->h || solver->krylov_width < 1 ||
+        solver->krylov_width > 62 || !step->external || !step->v || !step->rotation || !(step->dt > 0.0) ||
+        step->max_iterations < 0 || ((uintptr_t)solver->vectors & 15u))
+        return DPF_ERR_ARGUMENT;
+    std::memset(info, 0, sizeof(*info));
+    Step run;
+    run.s = solver;
+    run.a = step;
+    run.info = info;
+    run.st = (cudaStream_t)stream;
+    run.n = solver->graph->n_sites;
+    run.n6 = 6 * run.n;
+    double *v = solver->vectors;
+    double **slots[DPF_NEWTON_VECTORS] = {&run.y, &run.cand, &run.r, &run.r_cand, &run.scaled, &run.rhs,
+                                          &run.x, &run.res, &run.w, &run.corr, &run.ax};
+    for (int k = 0; k < DPF_NEWTON_VECTORS; ++k) *slots[k] = v + (int64_t)k * run.n6;
+    run.host = solver->host;
+    run.host_int = reinterpret_cast<int *>(solver->host + 96);
+    run.timing.on = step->timing != 0;
+    run.timing.stream = run.st;
+    const int rc = run.run();
+    if (!run.timing.events.empty() && cudaStreamSynchronize(run.st) == cudaSuccess) run.timing.collect(info);
+    return rc;
+}
+
+extern "C" int dpf_newton_struct_sizes(int64_t *out) {
+    if (!out) return DPF_ERR_ARGUMENT;
+    out[0] = (int64_t)sizeof(dpf_mixed_newton);
+    out[1] = (int64_t)sizeof(dpf_newton_step);
+    out[2] = (int64_t)sizeof(dpf_newton_info);
+    return DPF_OK;
+}

@@ -373,25 +373,6 @@ __device__ __forceinline__ void matvec6f(const float *P, const float x[6], float
     }
 }
 
-// Scaled residual in float32 from a float64 residual: s = P r / units;
-// returns max |s| and accumulates |s|^2.
-__device__ __forceinline__ float scale_site(const float *P, const float *units32, const double r[6], double *scaled,
-                                            double &sum_s) {
-    float rf[6], sf[6];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) rf[c] = (float)r[c];
-    matvec6f(P, rf, sf);
-    float mx = 0.0f;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        const float v = sf[c] / units32[c];
-        if (scaled) scaled[c] = v;
-        mx = fmaxf(mx, fabsf(v));
-        sum_s += (double)v * (double)v;  // float64: |s| equals the norm of the float64 copy
-    }
-    return mx;
-}
-
 __device__ __forceinline__ void finish_norms(double sum_r, double max_s, double sum_s, double *partials, int slot,
                                              double *norms, int *status) {
     sum_r = block_sum(sum_r);
@@ -416,7 +397,27 @@ __device__ __forceinline__ void finish_norms(double sum_r, double max_s, double 
     }
 }
 
+// One scaled row of a site: (P r)_row / units_row in float32 (the fmaf order
+// of matvec6f), from the float32 copy rf of the site's residual.
+__device__ __forceinline__ float scale_row(const float *P, const float rf[6], int row, float unit) {
+    const float2 *p = reinterpret_cast<const float2 *>(P + 6 * row);
+    const float2 p01 = p[0], p23 = p[1], p45 = p[2];
+    float v = 0.0f;
+    v = fmaf(p01.x, rf[0], v);
+    v = fmaf(p01.y, rf[1], v);
+    v = fmaf(p23.x, rf[2], v);
+    v = fmaf(p23.y, rf[3], v);
+    v = fmaf(p45.x, rf[4], v);
+    v = fmaf(p45.y, rf[5], v);
+    return v / unit;
+}
+
+// A group of kGroupJ = 4 lanes per site: the lanes gather the site's bond
+// wrench, lanes 0-2 then form two residual components each (16-byte loads and
+// stores), the group exchanges them by shuffles, and with a preconditioner
+// lane l scales rows l and l + 4.
 __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
+    static_assert(kGroupJ == 4, "two residual components per lane on lanes 0-2, scaled rows l and l + 4");
     double sum_r = 0.0;
     float max_s = 0.0f;
     double sum_s = 0.0;
@@ -428,48 +429,81 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
         const bool valid = s < a.n;
         float hi[6], lo[6];
         group_gather9c_j(a.ptr, a.inc, a.wrench, s, valid, lane, hi, lo);
-        if (!valid || lane != 0) continue;
-        double r[6];
-        const double *ys = a.y + 6 * s;
-        const float w0 = (float)ys[3], w1 = (float)ys[4], w2 = (float)ys[5];
-        if (sqrtf(w0 * w0 + w1 * w1 + w2 * w2) > 0.25f) {
-            if (a.seg)
-                atomicOr(a.status + a.seg[s], DPF_ERR_ROTATION);
-            else
-                flags |= DPF_ERR_ROTATION;
+        double r0v = 0.0, r1v = 0.0;
+        if (valid && lane < 3) {
+            const float h0 = lane == 0 ? hi[0] : (lane == 1 ? hi[2] : hi[4]);
+            const float l0 = lane == 0 ? lo[0] : (lane == 1 ? lo[2] : lo[4]);
+            const float h1 = lane == 0 ? hi[1] : (lane == 1 ? hi[3] : hi[5]);
+            const float l1 = lane == 0 ? lo[1] : (lane == 1 ? lo[3] : lo[5]);
+            const int64_t e = 6 * s + 2 * lane;
+            const double2 yv = *reinterpret_cast<const double2 *>(a.y + e);
+            const double2 mv = *reinterpret_cast<const double2 *>(a.mass + e);
+            const double2 rv = *reinterpret_cast<const double2 *>(a.r0 + e);
+            const bool fx = a.fixed[s] != 0;
+            r0v = fx ? yv.x : fma(mv.x, yv.x, rv.x) - a.half_dt2 * ((double)h0 + (double)l0);
+            r1v = fx ? yv.y : fma(mv.y, yv.y, rv.y) - a.half_dt2 * ((double)h1 + (double)l1);
+            *reinterpret_cast<double2 *>(a.residual + e) = make_double2(r0v, r1v);
+            sum_r = fma(r0v, r0v, sum_r);
+            sum_r = fma(r1v, r1v, sum_r);
         }
-        const bool fx = a.fixed[s] != 0;
+        if (valid && lane == 0) {
+            const double *ys = a.y + 6 * s;
+            const float w0 = (float)ys[3], w1 = (float)ys[4], w2 = (float)ys[5];
+            if (sqrtf(w0 * w0 + w1 * w1 + w2 * w2) > 0.25f) {
+                if (a.seg)
+                    atomicOr(a.status + a.seg[s], DPF_ERR_ROTATION);
+                else
+                    flags |= DPF_ERR_ROTATION;
+            }
+        }
+        if (a.P) {  // uniform over the grid: every lane takes part in the shuffles
+            float rf[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const double acc = (double)hi[c] + (double)lo[c];
-            const double val = fma(a.mass[6 * s + c], ys[c], a.r0[6 * s + c]) - a.half_dt2 * acc;
-            r[c] = fx ? ys[c] : val;
-            a.residual[6 * s + c] = r[c];
-            sum_r = fma(r[c], r[c], sum_r);
+            for (int k = 0; k < 3; ++k) {
+                rf[2 * k] = (float)__shfl_sync(0xffffffffu, r0v, k, kGroupJ);
+                rf[2 * k + 1] = (float)__shfl_sync(0xffffffffu, r1v, k, kGroupJ);
+            }
+            if (valid) {
+                const float *P = a.P + 36 * s;
+                const float *u = a.units32 + 6 * s;
+#pragma unroll
+                for (int k = 0; k < 2; ++k) {
+                    const int row = lane + 4 * k;
+                    if (row < 6) {
+                        const float v = scale_row(P, rf, row, u[row]);
+                        if (a.scaled) a.scaled[6 * s + row] = v;
+                        max_s = fmaxf(max_s, fabsf(v));
+                        sum_s += (double)v * (double)v;  // float64: |s| equals the norm of the float64 copy
+                    }
+                }
+            }
         }
-        if (a.P)
-            max_s = fmaxf(max_s, scale_site(a.P + 36 * s, a.units32 + 6 * s, r, a.scaled ? a.scaled + 6 * s : nullptr,
-                                            sum_s));
     }
     if (flags) atomicOr(a.status, flags);
     if (!a.norms) return;
     finish_norms(sum_r, max_s, sum_s, a.partials, 6, a.norms, a.status);
 }
 
+// One thread per scaled row (6 per site): the site's six residual entries are
+// read by its six threads (one cache line), each thread its 24-byte row of P.
 __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const float *P, const float *units32,
                                                             const double *r, double *scaled, double *norms,
                                                             double *partials) {
     double sum_r = 0.0;
     float max_s = 0.0f;
     double sum_s = 0.0;
-    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-        double rr[6];
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 6 * n; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t s = e / 6;
+        const int row = (int)(e - 6 * s);
+        float rf[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            rr[c] = r[6 * s + c];
-            sum_r = fma(rr[c], rr[c], sum_r);
-        }
-        max_s = fmaxf(max_s, scale_site(P + 36 * s, units32 + 6 * s, rr, scaled ? scaled + 6 * s : nullptr, sum_s));
+        for (int c = 0; c < 6; ++c) rf[c] = (float)r[6 * s + c];
+        const double own = r[e];
+        sum_r = fma(own, own, sum_r);
+        const float v = scale_row(P + 36 * s, rf, row, units32[e]);
+        if (scaled) scaled[e] = v;
+        max_s = fmaxf(max_s, fabsf(v));
+        sum_s += (double)v * (double)v;
     }
     if (!norms) return;
     finish_norms(sum_r, max_s, sum_s, partials, 7, norms, nullptr);
@@ -1101,7 +1135,7 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     const double *yi = a.y + 6 * (int64_t)B.i, *yj = a.y + 6 * (int64_t)B.j;
     const d3 de = (ld3(a.h.x, B.j) + ld3(yj)) - (ld3(a.h.x, B.i) + ld3(yi));
     const double le64 = norm(de);
-    const d3 ne = de / le64;
+    const d3 ne = (1.0 / le64) * de;
     st3(a.normal_end, b, ne);
     const V3<float> nx = lift3<float>(B.n0) + lift3<float>(B.dn0);
     float le;
@@ -1335,6 +1369,10 @@ int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const dou
     if (!mixed_graph_ok(g) || !bond_data || !y || !y32 || !mass || !fixed || !r0 || !residual || !status ||
         (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units32) || (active && !seg_bond))
         return DPF_ERR_ARGUMENT;
+    // the site pass moves y, mass, r0 and the residual in 16-byte pairs and P in 8-byte pairs
+    if ((((uintptr_t)y | (uintptr_t)mass | (uintptr_t)r0 | (uintptr_t)residual) & 15u) ||
+        ((uintptr_t)preconditioner & 7u))
+        return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
         ResidualBondArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, want_tangent, wrench, status,
@@ -1362,9 +1400,11 @@ int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32,
 
 int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const float *units32,
                              const double *residual, double *scaled, double *norms, double *partials, void *stream) {
-    if (n_sites <= 0 || !preconditioner || !units32 || !residual || (norms && !partials)) return DPF_ERR_ARGUMENT;
-    scale_sites_f32<<<reduce_grid(n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units32,
-                                                                                  residual, scaled, norms, partials);
+    if (n_sites <= 0 || !preconditioner || !units32 || !residual || (norms && !partials) ||
+        ((uintptr_t)preconditioner & 7u))
+        return DPF_ERR_ARGUMENT;
+    scale_sites_f32<<<reduce_grid(6 * n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units32,
+                                                                                      residual, scaled, norms, partials);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -214,7 +214,9 @@ __global__ void __launch_bounds__(kThreads) arnoldi_normalize(int64_t len, doubl
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     double *row = basis + (int64_t)(j + 1) * ld;
-    for (int64_t e = tid; e < len; e += stride) row[e] = w[e] / nrm;
+    // one float64 division per block, then products (float64 divides are slow on this part)
+    const double inv = 1.0 / nrm;
+    for (int64_t e = tid; e < len; e += stride) row[e] = w[e] * inv;
 }
 
 struct Coefficients {
@@ -316,9 +318,33 @@ __global__ void __launch_bounds__(kThreads) accept_kernel(int64_t n, const doubl
 #pragma unroll
     for (int c = 0; c < 6; ++c) v[6 * s + c] = 2.0 * y[6 * s + c] / dt - v[6 * s + c];
     const d3 w = ld3(y + 6 * s + 3);
-    const double angle = norm(w);
-    double A = 1.0, B = 0.5;
-    if (angle > 0.0) {
+    // Rodrigues coefficients A = sin(a)/a and B = (1 - cos a)/a^2 of a = |w|.
+    // Both are even in a: for a^2 < 1/4 (every step the rotation guard lets
+    // through has a <= 0.25) their Maclaurin series in a^2, 8 terms each,
+    // are exact to a few 1e-17 and need no float64 transcendental, which is
+    // slow on this part.  Larger angles take the closed form.
+    const double theta = w.x * w.x + w.y * w.y + w.z * w.z;
+    double A, B;
+    if (theta < 0.25) {
+        // Horner in theta: A = sum (-theta)^k/(2k+1)!, B = sum (-theta)^k/(2k+2)!, k = 0..7
+        A = 1.0 / 1307674368000.0;                 // 1/15!
+        A = fma(-theta, A, 1.0 / 6227020800.0);    // 1/13!
+        A = fma(-theta, A, 1.0 / 39916800.0);      // 1/11!
+        A = fma(-theta, A, 1.0 / 362880.0);        // 1/9!
+        A = fma(-theta, A, 1.0 / 5040.0);          // 1/7!
+        A = fma(-theta, A, 1.0 / 120.0);           // 1/5!
+        A = fma(-theta, A, 1.0 / 6.0);             // 1/3!
+        A = fma(-theta, A, 1.0);
+        B = 1.0 / 20922789888000.0;                // 1/16!
+        B = fma(-theta, B, 1.0 / 87178291200.0);   // 1/14!
+        B = fma(-theta, B, 1.0 / 479001600.0);     // 1/12!
+        B = fma(-theta, B, 1.0 / 3628800.0);       // 1/10!
+        B = fma(-theta, B, 1.0 / 40320.0);         // 1/8!
+        B = fma(-theta, B, 1.0 / 720.0);           // 1/6!
+        B = fma(-theta, B, 1.0 / 24.0);            // 1/4!
+        B = fma(-theta, B, 0.5);
+    } else {
+        const double angle = sqrt(theta);
         double sh, ch;
         sincos(0.5 * angle, &sh, &ch);
         A = sin(angle) / angle;

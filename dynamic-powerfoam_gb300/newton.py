@@ -716,6 +716,19 @@ class _Krylov:
         self.h = torch.zeros(72, dtype=F64, device=device)
 
 
+def _back_substitute(h, g, k):
+    """Solve the k x k upper-triangular h[:k, :k] c = g[:k] (the Givens-reduced
+    Hessenberg system) row by row from the bottom, float64 operation for
+    operation as the library's step driver does."""
+    c = np.zeros(k)
+    for i in range(k-1, -1, -1):
+        acc = g[i]
+        for col in range(i+1, k):
+            acc -= h[i, col]*c[col]
+        c[i] = acc/h[i, i]
+    return c
+
+
 def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iterations=256, *, workspace=None,
            strict=True, rhs_norm=None):
     """Right-preconditioned flexible GMRES with CGS2 Arnoldi on CUDA tensors.
@@ -782,7 +795,7 @@ def fgmres(operator, rhs, precondition, tolerance=1e-6, restart=32, max_iteratio
             g[j+1], g[j] = -sn[j]*g[j], cs[j]*g[j]
             iterations += 1
             if abs(g[j+1]) <= tolerance*norm or breakdown or j+1 == width:
-                coefficients = np.ascontiguousarray(np.linalg.solve(h[:j+1, :j+1], g[:j+1]), dtype=np.float64)
+                coefficients = _back_substitute(h, g, j+1)
                 _lib.check(lib.dpf_combine_rows(length, ws.transformed.data_ptr(), length, j+1,
                                                 coefficients.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                                 x.data_ptr(), stream), 'dpf_combine_rows')
@@ -1188,11 +1201,136 @@ class MixedNewtonBonds(NewtonBonds):
     # use); 'bonds' -- a bond pass and a site gather through HBM per iteration.
     sweep = 'ends'
 
+    # Drive eligible steps (bond-end sweep, FGMRES, elastic preconditioning, no
+    # overridden hook) from the library's host step driver: the same launches
+    # and decisions as the Python control path, bit for bit, without Python
+    # between the launches.  False keeps every step on the Python path.
+    native = True
+
+    # the hooks the native driver replaces; a subclass that overrides one keeps the Python path
+    _NATIVE_HOOKS = ('_step_begin', '_iteration_residual', '_mixed_residual', '_newton_operator',
+                     '_newton_preconditioner', '_line_merit', '_accept', '_bond_mask', '_site_mask', '_end_pcg',
+                     '_pack_ends', 'step', '_native_step')
+
     def step(self, dt, external, tolerance=2e-7, max_iterations=12, *, pose_tolerance=2e-6, backend='fgmres',
              linear_tolerance=1e-6, preconditioning='elastic'):
+        linear_tolerance = max(linear_tolerance, self.min_linear_tolerance)
+        if self._native_ready(backend, preconditioning):
+            return self._native_step(dt, external, tolerance, max_iterations, pose_tolerance, linear_tolerance)
         return super().step(dt, external, tolerance, max_iterations, pose_tolerance=pose_tolerance, backend=backend,
-                            linear_tolerance=max(linear_tolerance, self.min_linear_tolerance),
-                            preconditioning=preconditioning)
+                            linear_tolerance=linear_tolerance, preconditioning=preconditioning)
+
+    def _native_ready(self, backend, preconditioning):
+        if not (self.native and backend == 'fgmres' and preconditioning == 'elastic' and self.sweep == 'ends'):
+            return False
+        if self._end_variant is None or self._ends is None or not self._sweep_ready:
+            return False        # the first step runs in Python: it autotunes the sweep's launch shape
+        cls = type(self)
+        return all(getattr(cls, name) is getattr(MixedNewtonBonds, name) for name in self._NATIVE_HOOKS)
+
+    def _native_buffers(self):
+        """Descriptor of this solver's buffers for ``dpf_mixed_newton_step`` (cached
+        while the tensors it points to stay the same)."""
+        key = tuple(t.data_ptr() for t in (self.mass, self.fixed, self.radii, self.kn, self.ks, self.kb, self.kt,
+                                           self._ends)) + (self._end_variant,)
+        cached = getattr(self, '_native_desc', None)
+        if cached is not None and cached[0] == key:
+            return cached[1]
+        n, dev, lib = self.n_sites, self.device, self._lib
+        if self._krylov is None or self._krylov.length != 6*n:
+            self._krylov = _Krylov(6*n, 32, dev)
+        if getattr(self, '_native_vectors', None) is None:
+            self._native_vectors = torch.empty((_lib.NEWTON_VECTORS, n, 6), dtype=F64, device=dev)
+            self._native_partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=dev)
+            self._native_scalars = torch.zeros(2, dtype=F64, device=dev)
+            self._native_host = torch.zeros(_lib.NEWTON_HOST_DOUBLES, dtype=F64).pin_memory()
+        for name in ('mass', 'fixed', 'radii'):
+            t = getattr(self, name)
+            if not t.is_contiguous():
+                setattr(self, name, t.contiguous())
+        ptr = lambda t: t.data_ptr()
+        desc = _lib.MixedNewton(
+            graph=ctypes.addressof(self._graph), stiffness=self._stiffness_struct(), radii=ptr(self.radii),
+            mass=ptr(self.mass), mass32=ptr(self._mass32), fixed=ptr(self.fixed), bond_data=ptr(self._bond_data),
+            r0=ptr(self._r0), loads=ptr(self._loads), scales=ptr(self._begin_scales), wrench64=ptr(self._wrench),
+            partials=ptr(self._partials), scalars=ptr(self._scalars), status=ptr(self._status), y32=ptr(self._y32),
+            d32=ptr(self._d32), wrench32=ptr(self._wrench32), block32=ptr(self._block32), p32=ptr(self._p32),
+            units=ptr(self._units), units32=ptr(self._units32), ends=ptr(self._ends), site4=ptr(self._site4),
+            p24=ptr(self._p24), end_workspace=ptr(self._tiled_workspace), end_partials=ptr(self._tiled_partials),
+            barrier=ptr(self._barrier), inner=ptr(self._inner), basis=ptr(self._krylov.basis),
+            transformed=ptr(self._krylov.transformed), h=ptr(self._krylov.h), krylov_width=self._krylov.width,
+            krylov_partials=ptr(self._native_partials), krylov_scalars=ptr(self._native_scalars),
+            vectors=ptr(self._native_vectors), host=ptr(self._native_host), end_variant=int(self._end_variant))
+        # the descriptor holds only addresses: keep what they point into alive with it
+        self._native_desc = (key, desc, self._krylov)
+        return desc
+
+    @torch.no_grad()
+    def _native_step(self, dt, external, tolerance, max_iterations, pose_tolerance, linear_tolerance):
+        """``step`` through ``dpf_mixed_newton_step``: one library call per step."""
+        if not np.isfinite(dt) or dt <= 0:
+            raise ValueError('Positive finite dt required')
+        dt = float(dt)
+        external = self._vec(external)
+        self._v = self._vec(self.v).clone()
+        rotation = self._vec(self.rotation).clone()
+        if getattr(self, '_begin_scales', None) is None:
+            self._begin_scales = torch.zeros(2, dtype=F64, device=self.device)
+        self._cached = None
+        refresh = not (self._token is not None and self._token == self._state_token() and
+                       self._since_refresh < self.refresh_interval)
+        if refresh:
+            self._since_refresh = 0
+        history = self._history_struct()
+        desc = self._native_buffers()
+        m, n = self.n_bonds, self.n_sites
+        e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
+        state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
+        timing = self.profile is not None
+        args = _lib.NewtonStep(dt=dt, external=external.data_ptr(), v=self._v.data_ptr(),
+                               rotation=rotation.data_ptr(), history=history,
+                               x_end=state['x'].data_ptr(), normal_end=state['normal'].data_ptr(),
+                               offset_end=state['offset'].data_ptr(), fn_end=state['fn'].data_ptr(),
+                               fs_end=state['fs'].data_ptr(), mt_end=state['mt'].data_ptr(),
+                               mb_end=state['mb'].data_ptr(), tolerance=float(tolerance),
+                               pose_tolerance=float(pose_tolerance), linear_tolerance=float(linear_tolerance),
+                               max_iterations=int(max_iterations), refresh=int(refresh), timing=int(timing))
+        info = _lib.NewtonInfo()
+        self._inner_host = 0
+        self._call('dpf_mixed_newton_step', ctypes.byref(desc), ctypes.byref(args), ctypes.byref(info),
+                   self._stream())
+        _lib.LAUNCHES['count'] += info.launches
+        self.units = self._units
+        self._packed = None
+        if timing:
+            for k, key in enumerate(_lib.NEWTON_TIMERS):
+                count = info.timed_launches[k]
+                if count:
+                    self.profile.setdefault(key, []).extend([info.time_ms[k]/count]*count)
+        relative, local = info.relative, info.local
+        outcome = info.outcome
+        if outcome == _lib.NEWTON_GUARD:
+            raise guard_error(info.guard)
+        if outcome == _lib.NEWTON_NONFINITE:
+            raise SubdivideError(f'Subdivide: non-finite Newton residual ({relative:g}, {local:g})')
+        if outcome == _lib.NEWTON_SINGULAR:
+            raise SubdivideError('Subdivide: singular Newton linear system')
+        if outcome == _lib.NEWTON_KRYLOV:
+            raise SubdivideError(f'Subdivide: FGMRES did not converge ({info.krylov_relative:g})')
+        if outcome == _lib.NEWTON_LINE_SEARCH:
+            raise SubdivideError('Subdivide: Newton line search failed')
+        if outcome != _lib.NEWTON_CONVERGED:
+            raise SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
+        self.commit(state)
+        self.v, self.rotation = self._v, rotation
+        self._token = self._state_token()
+        self._since_refresh += 1
+        self.time += dt
+        trace = [[info.trace[2*k], info.trace[2*k + 1]] for k in range(info.trace_len)]
+        return info.work, dict(nonlinear_iterations=info.nonlinear_iterations, nonlinear_relative_residual=relative,
+                               local_pose_defect=local, krylov_iterations=info.krylov_iterations,
+                               cg_iterations=info.cg_iterations, residual_trace=trace,
+                               max_step_rotation=info.max_rotation)
 
     def __init__(self, *args, **kwargs):
         super().__init__(*args, **kwargs)

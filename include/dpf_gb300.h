@@ -378,6 +378,8 @@ int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_histor
 /* Residual at increment y with every trial guard (status bits as dpf_trial);
  * want_tangent stores the midpoint tangent for dpf_mixed_scaling and K q;
  * preconditioner (float32 (N, 6, 6)) / units / scaled / norms as in dpf_residual.
+ * y, mass, r0 and residual are 16-byte aligned, preconditioner 8-byte aligned
+ * (DPF_ERR_ARGUMENT otherwise).
  * Replaces NewtonBonds.residual + scale_residual (experiments/bonded_dem_newton.py:83-86, 104-105). */
 int dpf_mixed_residual(const dpf_graph *g, float *bond_data, const double *y, const float *y32,
                        const double *mass, const uint8_t *fixed, double dt, const double *r0,
@@ -718,6 +720,101 @@ int dpf_parallel_advance(const dpf_graph *g, const dpf_parallel_params *p, const
 int dpf_parallel_loads(const dpf_graph *g, const double *radii, const double *x, const double *fn, const double *fs,
                        const double *mt, const double *mb, double *force, double *torque, double *wrench,
                        int *status, void *stream);
+
+/* ---- native step driver of the mixed-precision Newton solver -------------
+ * One implicit step of MixedNewtonBonds.step (bond-end PCG, FGMRES, elastic
+ * preconditioning) driven from host code in this library: the same entry
+ * points, in the same order, with the same arguments and the same host
+ * decisions (convergence tests, Givens rotations, triangular solve, line
+ * search) as the Python control path, so both give bit-identical results.
+ * Replaces the control flow of NewtonBonds.step and fgmres
+ * (experiments/bonded_dem_newton.py:13-60, 132-201).
+ *
+ * Device pointers unless noted; float64 vectors are (N, 6) = 6 N doubles. */
+#define DPF_NEWTON_VECTORS 11      /* scratch vectors of 6 N doubles in `vectors` */
+#define DPF_NEWTON_HOST_DOUBLES 128 /* pinned host doubles in `host` */
+#define DPF_NEWTON_TRACE 32         /* residual trace entries kept */
+#define DPF_NEWTON_TIMERS 6         /* setup, residual, scaling, pcg, jvp, commit */
+
+typedef struct dpf_mixed_newton {
+    const dpf_graph *graph;        /* host struct */
+    dpf_stiffness stiffness;       /* float64 stiffnesses (the float64 setup) */
+    const double *radii;           /* (N) */
+    const double *mass;            /* (N, 6) diagonal mass */
+    const float *mass32;           /* (N, 6) */
+    const uint8_t *fixed;          /* (N) */
+    float *bond_data;              /* dpf_mixed_bond_floats(M) */
+    double *r0, *loads;            /* (N, 6) */
+    double *scales;                /* 2: the rhs scale terms of the step */
+    double *wrench64;              /* 9 M doubles (float64 setup) */
+    double *partials;              /* dpf_partials_doubles() */
+    double *scalars;               /* >= 4 */
+    int *status;                   /* guard bits */
+    float *y32, *d32, *wrench32;   /* (N, 6), (N, 6), 9 M */
+    float *block32, *p32;          /* (N, 6, 6) */
+    double *units;                 /* (N, 6) */
+    float *units32;                /* (N, 6) */
+    float *ends, *site4, *p24;     /* dpf_end_pack outputs */
+    float *end_workspace;          /* dpf_tiled_workspace_floats(N) */
+    double *end_partials;          /* dpf_tiled_partials_doubles() */
+    unsigned *barrier;             /* 2 words */
+    int *inner;                    /* CG iteration counter (added to) */
+    double *basis, *transformed;   /* (width + 1, 6 N), (width, 6 N) */
+    double *h;                     /* >= width + 2 */
+    int krylov_width;              /* FGMRES restart length, <= 62 */
+    double *krylov_partials;       /* dpf_partials_doubles() */
+    double *krylov_scalars;        /* 2 */
+    double *vectors;               /* DPF_NEWTON_VECTORS x 6 N, 16-byte aligned */
+    double *host;                  /* pinned host memory, DPF_NEWTON_HOST_DOUBLES */
+    int end_variant;               /* launch shape of the bond-end sweep */
+} dpf_mixed_newton;
+
+typedef struct dpf_newton_step {
+    double dt;
+    const double *external;        /* (N, 6) */
+    double *v;                     /* (N, 6) velocity, advanced on convergence */
+    double *rotation;              /* (N, 3, 3), advanced on convergence */
+    dpf_history history;           /* committed state */
+    double *x_end, *normal_end, *offset_end, *fn_end, *fs_end, *mt_end, *mb_end;  /* end state */
+    double tolerance, pose_tolerance, linear_tolerance;
+    int max_iterations;            /* Newton iterations */
+    int refresh;                   /* 1: float64 setup of the records; 0: begin from the maintained loads */
+    int timing;                    /* 1: CUDA-event times of the hot launches into the info */
+} dpf_newton_step;
+
+/* outcome of a step */
+enum {
+    DPF_NEWTON_CONVERGED = 0,
+    DPF_NEWTON_GUARD = 1,          /* a trial guard fired (bits in guard) */
+    DPF_NEWTON_NONFINITE = 2,      /* non-finite Newton residual */
+    DPF_NEWTON_SINGULAR = 3,       /* zero Givens denominator */
+    DPF_NEWTON_KRYLOV = 4,         /* FGMRES iteration budget spent (krylov_relative) */
+    DPF_NEWTON_LINE_SEARCH = 5,    /* no admissible step length */
+    DPF_NEWTON_DIVERGED = 6        /* Newton iteration budget spent */
+};
+
+typedef struct dpf_newton_info {
+    int outcome, guard;
+    int nonlinear_iterations, krylov_iterations, cg_iterations;
+    int launches;                  /* kernels launched by the step */
+    double relative, local;        /* last relative residual and pose defect */
+    double work, max_rotation;     /* on convergence: external . y, max |y_w| */
+    double krylov_relative;
+    int trace_len;
+    double trace[2 * DPF_NEWTON_TRACE];          /* [relative, local] per Newton iteration */
+    double time_ms[DPF_NEWTON_TIMERS];
+    int timed_launches[DPF_NEWTON_TIMERS];
+} dpf_newton_info;
+
+/* Returns DPF_OK with the outcome in info (DPF_NEWTON_CONVERGED: the end state
+ * is in the step's outputs, v and rotation advanced), or the error code of a
+ * failed entry point (DPF_ERR_ARGUMENT / DPF_ERR_CUDA). */
+int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_newton_step *step, dpf_newton_info *info,
+                          void *stream);
+
+/* sizeof(dpf_mixed_newton), sizeof(dpf_newton_step), sizeof(dpf_newton_info)
+ * into out[0..3): lets a binding check its struct layouts (host only). */
+int dpf_newton_struct_sizes(int64_t *out);
 
 #ifdef __cplusplus
 }

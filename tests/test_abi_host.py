@@ -39,6 +39,15 @@ def test_binding_covers_header():
     assert set(_lib.KERNELS) <= set(_lib.SIGNATURES)
 
 
+def test_step_driver_struct_layouts_match_the_binding(library):
+    from dpf_gb300 import _lib
+    out = (ctypes.c_int64*3)()
+    library.dpf_newton_struct_sizes.argtypes = [ctypes.POINTER(ctypes.c_int64)]
+    assert library.dpf_newton_struct_sizes(out) == 0
+    assert list(out) == [ctypes.sizeof(_lib.MixedNewton), ctypes.sizeof(_lib.NewtonStep),
+                         ctypes.sizeof(_lib.NewtonInfo)]
+
+
 def test_size_queries(library):
     library.dpf_wrench_scratch_doubles.restype = ctypes.c_int64
     library.dpf_wrench_scratch_doubles.argtypes = [ctypes.c_int64]
