@@ -121,8 +121,15 @@ __device__ __forceinline__ void gather9f(const int32_t *__restrict__ ptr, const 
 }
 
 // Segmented site sum by groups of kGroupJ lanes (xor-shuffle reduction),
-// compensated: used by the residual and JVP site passes.
-constexpr int kGroupJ = 4;
+// compensated: used by the residual, JVP and commit site passes.  The group
+// width is a launch-shape choice (4, 8 or 16 lanes; the build may set it):
+// on the 64^3 foam 4 lanes measured fastest (residual 157 / 186 / 258 us,
+// JVP 169 / 176 / 205 us for 4 / 8 / 16 lanes).
+#ifndef DPF_SITE_LANES
+#define DPF_SITE_LANES 4
+#endif
+constexpr int kGroupJ = DPF_SITE_LANES;
+static_assert(kGroupJ == 4 || kGroupJ == 8 || kGroupJ == 16, "site groups of 4, 8 or 16 lanes");
 
 __device__ __forceinline__ void group_gather9c_j(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
                                                  const float *__restrict__ w, int64_t s, bool valid, int lane,
@@ -412,12 +419,11 @@ __device__ __forceinline__ float scale_row(const float *P, const float rf[6], in
     return v / unit;
 }
 
-// A group of kGroupJ = 4 lanes per site: the lanes gather the site's bond
+// A group of kGroupJ lanes per site: the lanes gather the site's bond
 // wrench, lanes 0-2 then form two residual components each (16-byte loads and
 // stores), the group exchanges them by shuffles, and with a preconditioner
-// lane l scales rows l and l + 4.
+// lane l scales rows l, l + kGroupJ, ... of the six.
 __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
-    static_assert(kGroupJ == 4, "two residual components per lane on lanes 0-2, scaled rows l and l + 4");
     double sum_r = 0.0;
     float max_s = 0.0f;
     double sum_s = 0.0;
@@ -467,8 +473,8 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
                 const float *P = a.P + 36 * s;
                 const float *u = a.units32 + 6 * s;
 #pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const int row = lane + 4 * k;
+                for (int k = 0; k < (6 + kGroupJ - 1) / kGroupJ; ++k) {
+                    const int row = lane + kGroupJ * k;
                     if (row < 6) {
                         const float v = scale_row(P, rf, row, u[row]);
                         if (a.scaled) a.scaled[6 * s + row] = v;
@@ -534,7 +540,21 @@ __global__ void __launch_bounds__(kThreads) prepare_direction(int64_t count, con
     d32[e] = units32 ? d * units32[e] : d;
 }
 
-__global__ void __launch_bounds__(kThreads) jvp_bonds_mixed(JvpArgs a) {
+// Resident 256-thread blocks per SM the JVP bond pass is compiled for (the
+// dual-number increment is register heavy); 0 leaves the register count to
+// the compiler (99 registers, 2 blocks).  3 blocks (80 registers, 88 bytes of
+// spills) measured 156 us per JVP on the 64^3 foam against 168 us for 2 and
+// 164 us for 4 (64 registers).  The build may set it.
+#ifndef DPF_JVP_BLOCKS_PER_SM
+#define DPF_JVP_BLOCKS_PER_SM 3
+#endif
+#if DPF_JVP_BLOCKS_PER_SM > 0
+#define DPF_JVP_BOUNDS __launch_bounds__(kThreads, DPF_JVP_BLOCKS_PER_SM)
+#else
+#define DPF_JVP_BOUNDS __launch_bounds__(kThreads)
+#endif
+
+__global__ void DPF_JVP_BOUNDS jvp_bonds_mixed(JvpArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
     if (a.active && !a.active[a.seg[b]]) {
@@ -567,7 +587,9 @@ __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
     const bool valid = g < a.n;
     float hi[6], lo[6], r[6];
     group_gather9c_j(a.ptr, a.inc, a.wrench, g, valid, lane, hi, lo);
-    if (!valid || lane != 0) return;
+    if (!valid) return;
+    // every lane of the group holds the sums: each forms the six entries of
+    // r (the site's d and mass are one cache line) and writes its rows
     const int64_t s = g;
     const bool fx = a.fixed[s] != 0;
 #pragma unroll
@@ -578,14 +600,17 @@ __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
         const float e = fmaf(m, d, -p) - fmaf(a.half_dt2, hi[c], -q) - a.half_dt2 * lo[c];
         r[c] = fx ? d : (p - q) + e;
     }
-    if (a.P) {
-        float o[6];
-        matvec6f(a.P + 36 * s, r, o);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)(o[c] / a.units32[6 * s + c]);
-    } else {
-#pragma unroll
-        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)r[c];
+    for (int k = 0; k < (6 + kGroupJ - 1) / kGroupJ; ++k) {
+        const int row = lane + kGroupJ * k;
+        if (row < 6) {
+            float v;
+            if (a.P)
+                v = scale_row(a.P + 36 * s, r, row, a.units32[6 * s + row]);
+            else
+                v = row == 0 ? r[0] : row == 1 ? r[1] : row == 2 ? r[2] : row == 3 ? r[3] : row == 4 ? r[4] : r[5];
+            a.out[6 * s + row] = (double)v;
+        }
     }
 }
 
@@ -1414,7 +1439,8 @@ int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float 
                               const float *preconditioner, double *out, float *d32, float *wrench,
                               const int32_t *seg_bond, const uint8_t *active, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !y32 || !direction || !mass32 || !fixed || !out || !d32 ||
-        (g->n_bonds && !wrench) || (preconditioner && !units32) || (active && !seg_bond))
+        (g->n_bonds && !wrench) || (preconditioner && !units32) || (active && !seg_bond) ||
+        ((uintptr_t)preconditioner & 7u))  // rows of P are read in 8-byte pairs
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n6 = 6 * g->n_sites;

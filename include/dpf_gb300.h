@@ -406,6 +406,7 @@ int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const
  * same options as dpf_jacobian_vector (units, float32 preconditioner).
  * seg_bond/active (optional, for batches): a bond b with active[seg_bond[b]]
  * == 0 contributes nothing (the rows of its request's sites are not read).
+ * The preconditioner is 8-byte aligned (DPF_ERR_ARGUMENT otherwise).
  * Replaces NewtonBonds.jacobian_vector (experiments/bonded_dem_newton.py:88-92). */
 int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float *y32,
                               const double *direction, const float *mass32, const uint8_t *fixed,
