@@ -68,7 +68,7 @@ class MixedNewton(ctypes.Structure):
                 [(k, vp) for k in ('radii', 'mass', 'mass32', 'fixed', 'bond_data', 'r0', 'loads', 'scales',
                                    'wrench64', 'partials', 'scalars', 'status', 'y32', 'd32', 'wrench32', 'block32',
                                    'p32', 'units', 'units32', 'ends', 'site4', 'p24', 'end_workspace',
-                                   'end_partials', 'barrier', 'inner', 'basis', 'transformed', 'h')] +
+                                   'end_partials', 'barrier', 'inner', 'basis', 'transformed', 'w32', 'h')] +
                 [('krylov_width', i32)] +
                 [(k, vp) for k in ('krylov_partials', 'krylov_scalars', 'vectors', 'host')] +
                 [('end_variant', i32)])
@@ -82,7 +82,7 @@ class NewtonStep(ctypes.Structure):
                  ('max_iterations', i32), ('refresh', i32), ('timing', i32)])
 
 
-NEWTON_VECTORS = 11
+NEWTON_VECTORS = 10
 NEWTON_HOST_DOUBLES = 128
 NEWTON_TRACE = 32
 NEWTON_TIMERS = ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit')
@@ -189,6 +189,12 @@ SIGNATURES = {
     'dpf_anderson_mix': (i32, [i64, vp, vp, i32, P(ctypes.c_int32), i32, P(ctypes.c_double), vp, vp, vp]),
     'dpf_barrier_selftest': (i32, [i32, i64, i32, vp, vp, vp, vp]),
     'dpf_mixed_newton_step': (i32, [P(MixedNewton), P(NewtonStep), P(NewtonInfo), vp]),
+    'dpf_end_precondition_f32': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, i32,
+                                       vp]),
+    'dpf_mixed_jacobian_vector_f32': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp]),
+    'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp]),
+    'dpf_combine_rows_f32': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
+    'dpf_scale_to_float': (i32, [i64, f64, vp, vp, vp]),
     'dpf_newton_struct_sizes': (i32, [P(ctypes.c_int64)]),
 }
 
@@ -201,13 +207,15 @@ KERNELS = {
     'dpf_dot_norm': 1, 'dpf_axpby': 1, 'dpf_rhs_scale': 1, 'dpf_masked_scale': 1,
     'dpf_stiffness_apply_static': 2, 'dpf_mixed_setup': 2, 'dpf_mixed_residual': 2, 'dpf_mixed_scaling': 1,
     'dpf_mixed_scale_residual': 1, 'dpf_mixed_jacobian_vector': 3, 'dpf_mixed_stiffness_apply': 2,
-    'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 2, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 2,
+    'dpf_to_float': 1, 'dpf_mixed_precondition': 1, 'dpf_mixed_commit': 3, 'dpf_mixed_begin': 1, 'dpf_mixed_residual_segmented': 2, 'dpf_segment_norms': 2,
     'dpf_segment_axpy': 1, 'dpf_segment_select': 1,
     'dpf_adjoint_local_jacobian': 1, 'dpf_adjoint_apply_jt': 2, 'dpf_adjoint_bond_vjp': 2,
     'dpf_tile_pack': 2, 'dpf_tiled_hvp': 1, 'dpf_tiled_precondition': 1, 'dpf_end_pack': 2, 'dpf_end_hvp': 1,
     'dpf_end_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
     'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
+    'dpf_end_precondition_f32': 1, 'dpf_mixed_jacobian_vector_f32': 3, 'dpf_arnoldi_cgs2_f32': 4,
+    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1,
 }
 LAUNCHES = {'count': 0}
 

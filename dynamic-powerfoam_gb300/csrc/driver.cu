@@ -80,7 +80,7 @@ struct Step {
     dpf_newton_info *info;
     cudaStream_t st;
     int64_t n, n6;
-    double *y, *cand, *r, *r_cand, *scaled, *rhs, *x, *res, *w, *corr, *ax;
+    double *y, *cand, *r, *r_cand, *scaled, *rhs, *x, *res, *corr, *ax;
     double *host;     // pinned: [0..8) scalars, [8..10) scales, [16..16+72) h column
     int *host_int;    // pinned ints after the doubles: [0] status, [1] inner
     Timing timing;
@@ -129,7 +129,8 @@ struct Step {
         return rc ? rc : launched(1);
     }
 
-    int precondition(const double *vector, double *out) {
+    // the elastic PCG on a float32 Krylov vector
+    int precondition(const float *vector, float *out) {
         int rc;
         if (!packed) {
             rc = dpf_end_pack(s->graph, s->bond_data, 0.25 * a->dt * a->dt, s->p32, s->mass32, s->fixed, s->ends,
@@ -139,13 +140,23 @@ struct Step {
             packed = true;
         }
         timing.begin(kPcg);
-        rc = dpf_end_precondition(s->graph, s->ends, s->site4, s->fixed, s->block32, s->p24, s->units32, vector, 0.03,
-                                  80, out, s->inner, s->end_workspace, s->end_partials, s->barrier, s->status,
-                                  nullptr, nullptr, s->end_variant, st);
+        rc = dpf_end_precondition_f32(s->graph, s->ends, s->site4, s->fixed, s->block32, s->p24, s->units32, vector,
+                                      0.03, 80, out, s->inner, s->end_workspace, s->end_partials, s->barrier,
+                                      s->status, s->end_variant, st);
         timing.end();
         return rc ? rc : launched(1);
     }
 
+    // J d on float32 Krylov vectors
+    int jvp32(const float *direction, float *out) {
+        timing.begin(kJvp);
+        const int rc = dpf_mixed_jacobian_vector_f32(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
+                                                     a->dt, s->units32, s->p32, out, s->d32, s->wrench32, st);
+        timing.end();
+        return rc ? rc : launched(s->graph->n_bonds ? 3 : 2);
+    }
+
+    // J d on a float64 vector (the Newton direction)
     int jvp(const double *direction, double *out) {
         timing.begin(kJvp);
         const int rc = dpf_mixed_jacobian_vector(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
@@ -166,8 +177,11 @@ struct Step {
         return DPF_OK;
     }
 
-    // Right-preconditioned FGMRES with CGS2 Arnoldi (fgmres in newton.py):
-    // solves J delta = b with b = rhs, |b| = norm; x = delta.  Sets *ok.
+    // Right-preconditioned FGMRES with CGS2 Arnoldi (MixedNewtonBonds._fgmres32
+    // in newton.py): solves J delta = b with b = rhs, |b| = norm; x = delta.
+    // The Krylov vectors are float32 (the PCG and JVP outputs carry float32
+    // precision), their sums exact float32 pairs; x, b and the true residual
+    // are float64.  Sets *ok.
     int fgmres(double norm, double tolerance, int restart, int max_iterations, bool *ok, int *krylov) {
         *ok = false;
         *krylov = 0;
@@ -198,17 +212,17 @@ struct Step {
             }
             const double *start = first ? rhs : res;
             first = false;
-            int rc = dpf_axpby(n6, 1.0 / g[0], start, 0.0, start, s->basis, st);
+            int rc = dpf_scale_to_float(n6, 1.0 / g[0], start, s->basis, st);
             if (rc) return rc;
             launched(1);
             for (int j = 0; j < width; ++j) {
-                double *bj = s->basis + (int64_t)j * n6;
-                double *tj = s->transformed + (int64_t)j * n6;
+                float *bj = s->basis + (int64_t)j * n6;
+                float *tj = s->transformed + (int64_t)j * n6;
                 rc = precondition(bj, tj);
                 if (rc) return rc;
-                rc = jvp(tj, w);
+                rc = jvp32(tj, s->w32);
                 if (rc) return rc;
-                rc = dpf_arnoldi_cgs2(n6, s->basis, n6, j, w, s->h, s->krylov_partials, st);
+                rc = dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, s->w32, s->h, s->krylov_partials, st);
                 if (rc) return rc;
                 launched(4);
                 double *column = host + 16;
@@ -243,7 +257,7 @@ struct Step {
                         for (int c = i + 1; c < k; ++c) acc -= H[i * ldh + c] * coef[c];
                         coef[i] = acc / H[i * ldh + i];
                     }
-                    rc = dpf_combine_rows(n6, s->transformed, n6, k, coef, x, st);
+                    rc = dpf_combine_rows_f32(n6, s->transformed, n6, k, coef, x, st);
                     if (rc) return rc;
                     launched(1);
                     rc = jvp(x, ax);
@@ -280,7 +294,7 @@ struct Step {
                               a->fs_end, a->mt_end, a->mb_end, s->wrench32, s->loads, st);
         timing.end();
         if (rc) return rc;
-        launched(s->graph->n_bonds ? 2 : 1);
+        launched(s->graph->n_bonds ? 3 : 1);
         rc = dpf_accept_step(n, y, a->dt, a->v, a->rotation, st);
         if (rc) return rc;
         launched(1);
@@ -423,7 +437,8 @@ extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_n
                                      dpf_newton_info *info, void *stream) {
     using dpf::driver::Step;
     if (!solver || !step || !info || !solver->graph || solver->graph->n_sites <= 0 || !solver->vectors ||
-        !solver->host || !solver->basis || !solver->transformed || !solver->h || solver->krylov_width < 1 ||
+        !solver->host || !solver->basis || !solver->transformed || !solver->w32 || !solver->h ||
+        solver->krylov_width < 1 ||
         solver->krylov_width > 62 || !step->external || !step->v || !step->rotation || !(step->dt > 0.0) ||
         step->max_iterations < 0 || ((uintptr_t)solver->vectors & 15u))
         return DPF_ERR_ARGUMENT;
@@ -436,8 +451,8 @@ extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_n
     run.n = solver->graph->n_sites;
     run.n6 = 6 * run.n;
     double *v = solver->vectors;
-    double **slots[DPF_NEWTON_VECTORS] = {&run.y, &run.cand, &run.r, &run.r_cand, &run.scaled, &run.rhs,
-                                          &run.x, &run.res, &run.w, &run.corr, &run.ax};
+    double **slots[DPF_NEWTON_VECTORS] = {&run.y, &run.cand, &run.r, &run.r_cand, &run.scaled,
+                                          &run.rhs, &run.x, &run.res, &run.corr, &run.ax};
     for (int k = 0; k < DPF_NEWTON_VECTORS; ++k) *slots[k] = v + (int64_t)k * run.n6;
     run.host = solver->host;
     run.host_int = reinterpret_cast<int *>(solver->host + 96);

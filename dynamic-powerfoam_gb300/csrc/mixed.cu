@@ -419,6 +419,16 @@ __device__ __forceinline__ float scale_row(const float *P, const float rf[6], in
     return v / unit;
 }
 
+// (hi, lo) += v^2 without rounding error beyond float32 pairs: the square by
+// FMA (TwoProd) and the sum by TwoSum.  Keeps |s|^2 to about 48 bits without
+// float64 arithmetic per entry (float64 is scarce on this part).
+__device__ __forceinline__ void add_square(float &hi, float &lo, float v) {
+    const float p = v * v;
+    const float e = fmaf(v, v, -p);
+    two_sum(hi, lo, p);
+    lo += e;
+}
+
 // A group of kGroupJ lanes per site: the lanes gather the site's bond
 // wrench, lanes 0-2 then form two residual components each (16-byte loads and
 // stores), the group exchanges them by shuffles, and with a preconditioner
@@ -426,7 +436,7 @@ __device__ __forceinline__ float scale_row(const float *P, const float rf[6], in
 __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
     double sum_r = 0.0;
     float max_s = 0.0f;
-    double sum_s = 0.0;
+    float s_hi = 0.0f, s_lo = 0.0f;
     int flags = 0;
     const int lane = threadIdx.x & (kGroupJ - 1);
     const int64_t groups = (int64_t)gridDim.x * blockDim.x / kGroupJ;
@@ -463,11 +473,13 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
             }
         }
         if (a.P) {  // uniform over the grid: every lane takes part in the shuffles
+            // lanes 0-2 round their two entries to float32, the group shares them
+            const float f0 = (float)r0v, f1 = (float)r1v;
             float rf[6];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                rf[2 * k] = (float)__shfl_sync(0xffffffffu, r0v, k, kGroupJ);
-                rf[2 * k + 1] = (float)__shfl_sync(0xffffffffu, r1v, k, kGroupJ);
+                rf[2 * k] = __shfl_sync(0xffffffffu, f0, k, kGroupJ);
+                rf[2 * k + 1] = __shfl_sync(0xffffffffu, f1, k, kGroupJ);
             }
             if (valid) {
                 const float *P = a.P + 36 * s;
@@ -479,7 +491,7 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
                         const float v = scale_row(P, rf, row, u[row]);
                         if (a.scaled) a.scaled[6 * s + row] = v;
                         max_s = fmaxf(max_s, fabsf(v));
-                        sum_s += (double)v * (double)v;  // float64: |s| equals the norm of the float64 copy
+                        add_square(s_hi, s_lo, v);
                     }
                 }
             }
@@ -487,32 +499,60 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
     }
     if (flags) atomicOr(a.status, flags);
     if (!a.norms) return;
-    finish_norms(sum_r, max_s, sum_s, a.partials, 6, a.norms, a.status);
+    finish_norms(sum_r, max_s, (double)s_hi + (double)s_lo, a.partials, 6, a.norms, a.status);
 }
 
-// One thread per scaled row (6 per site): the site's six residual entries are
-// read by its six threads (one cache line), each thread its 24-byte row of P.
+// One thread per site, 16-byte loads: the six residual entries (rounded to
+// float32 once), the 36-float P block, the six units; s = P r / units.
 __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const float *P, const float *units32,
                                                             const double *r, double *scaled, double *norms,
                                                             double *partials) {
     double sum_r = 0.0;
     float max_s = 0.0f;
-    double sum_s = 0.0;
-    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < 6 * n; e += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t s = e / 6;
-        const int row = (int)(e - 6 * s);
+    float s_hi = 0.0f, s_lo = 0.0f;
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const double2 *rp = reinterpret_cast<const double2 *>(r + 6 * s);
+        const double2 a0 = rp[0], a1 = rp[1], a2 = rp[2];
+        const double rr[6] = {a0.x, a0.y, a1.x, a1.y, a2.x, a2.y};
         float rf[6];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) rf[c] = (float)r[6 * s + c];
-        const double own = r[e];
-        sum_r = fma(own, own, sum_r);
-        const float v = scale_row(P + 36 * s, rf, row, units32[e]);
-        if (scaled) scaled[e] = v;
-        max_s = fmaxf(max_s, fabsf(v));
-        sum_s += (double)v * (double)v;
+        for (int c = 0; c < 6; ++c) {
+            sum_r = fma(rr[c], rr[c], sum_r);
+            rf[c] = (float)rr[c];
+        }
+        const float4 *pp = reinterpret_cast<const float4 *>(P + 36 * s);
+        float pm[36];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            const float4 q = pp[k];
+            pm[4 * k] = q.x;
+            pm[4 * k + 1] = q.y;
+            pm[4 * k + 2] = q.z;
+            pm[4 * k + 3] = q.w;
+        }
+        const float2 *up = reinterpret_cast<const float2 *>(units32 + 6 * s);
+        const float2 u0 = up[0], u1 = up[1], u2 = up[2];
+        const float un[6] = {u0.x, u0.y, u1.x, u1.y, u2.x, u2.y};
+        double out[6];
+#pragma unroll
+        for (int row = 0; row < 6; ++row) {
+            float v = 0.0f;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) v = fmaf(pm[6 * row + c], rf[c], v);
+            v = v / un[row];
+            max_s = fmaxf(max_s, fabsf(v));
+            add_square(s_hi, s_lo, v);
+            out[row] = (double)v;
+        }
+        if (scaled) {
+            double2 *sp = reinterpret_cast<double2 *>(scaled + 6 * s);
+            sp[0] = make_double2(out[0], out[1]);
+            sp[1] = make_double2(out[2], out[3]);
+            sp[2] = make_double2(out[4], out[5]);
+        }
     }
     if (!norms) return;
-    finish_norms(sum_r, max_s, sum_s, partials, 7, norms, nullptr);
+    finish_norms(sum_r, max_s, (double)s_hi + (double)s_lo, partials, 7, norms, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -531,12 +571,14 @@ __device__ __forceinline__ V3<Dual> dual3(V3<float> v, V3<float> d) {
     return {{v.x, d.x}, {v.y, d.y}, {v.z, d.z}};
 }
 
-// d32 = units * direction in float32 (one conversion per entry).
+// d32 = units * direction in float32 (one conversion per entry; a float32
+// direction is taken as it is).
 __global__ void __launch_bounds__(kThreads) prepare_direction(int64_t count, const double *direction,
-                                                              const float *units32, float *d32) {
+                                                              const float *direction32, const float *units32,
+                                                              float *d32) {
     const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (e >= count) return;
-    const float d = (float)direction[e];
+    const float d = direction32 ? direction32[e] : (float)direction[e];
     d32[e] = units32 ? d * units32[e] : d;
 }
 
@@ -579,6 +621,7 @@ struct JvpSiteArgs {
     const uint8_t *fixed;
     float half_dt2;
     double *out;
+    float *out32;  // float32 output instead of out (one of the two)
 };
 
 __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
@@ -609,7 +652,10 @@ __global__ void __launch_bounds__(kThreads) jvp_sites_mixed(JvpSiteArgs a) {
                 v = scale_row(a.P + 36 * s, r, row, a.units32[6 * s + row]);
             else
                 v = row == 0 ? r[0] : row == 1 ? r[1] : row == 2 ? r[2] : row == 3 ? r[3] : row == 4 ? r[4] : r[5];
-            a.out[6 * s + row] = (double)v;
+            if (a.out32)
+                a.out32[6 * s + row] = v;
+            else
+                a.out[6 * s + row] = (double)v;
         }
     }
 }
@@ -1136,15 +1182,24 @@ struct CommitArgs {
     BondData bd;
     dpf_history h;
     const float *y32;
-    const double *y;
+    const double *x_end;  // end positions x + y, formed first by end_positions
     double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
     float *dloads;  // optional: increment of the committed loads (9 floats per bond)
 };
 
+// x_end = x + u per site, before the bond pass reads it.
+__global__ void __launch_bounds__(kThreads) end_positions(int64_t n, const double *x, const double *y, double *x_end) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= 3 * n) return;
+    const int64_t s = e / 3;
+    x_end[e] = x[e] + y[6 * s + (e - 3 * s)];
+}
+
 // End state of the accepted increment; with dloads it also rewrites the bond
 // records for the next step in place (the bond's own record only) and emits
 // loads(x_end) - loads(x) per bond as float32 increments.
-__global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
+// 3 resident blocks per SM (80 registers) rather than 2 (88 registers).
+__global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
     const Bond B = load_bond(a.bd.rec, b);
@@ -1156,11 +1211,14 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     const double fn_end = a.h.fn[b] + (double)dfn, mt_end = a.h.mt[b] + (double)dmt;
     a.fn_end[b] = fn_end;
     a.mt_end[b] = mt_end;
-    // end normal in float64 from the end positions (geometry(end))
-    const double *yi = a.y + 6 * (int64_t)B.i, *yj = a.y + 6 * (int64_t)B.j;
-    const d3 de = (ld3(a.h.x, B.j) + ld3(yj)) - (ld3(a.h.x, B.i) + ld3(yi));
-    const double le64 = norm(de);
-    const d3 ne = (1.0 / le64) * de;
+    // end normal in float64 from the end positions (geometry(end)); one
+    // reciprocal square root instead of a square root and a division (float64
+    // arithmetic is scarce on this part)
+    const d3 de = ld3(a.x_end, B.j) - ld3(a.x_end, B.i);
+    const double l2 = dot(de, de);
+    const double inv = rsqrt(l2);
+    const double le64 = l2 * inv;
+    const d3 ne = inv * de;
     st3(a.normal_end, b, ne);
     const V3<float> nx = lift3<float>(B.n0) + lift3<float>(B.dn0);
     float le;
@@ -1205,22 +1263,18 @@ __global__ void __launch_bounds__(kThreads) commit_bonds(CommitArgs a) {
     a.bd.rec.r5[b] = make_float4(offr.x, offr.y, offr.z, B.ks);
 }
 
-// x_end = x + u; with dloads, loads += site sum of the load increments.
+// loads += site sum of the load increments.
 __global__ void __launch_bounds__(kThreads) commit_sites(int64_t n, const int32_t *ptr, const int32_t *inc,
-                                                         const double *x, const double *y, double *x_end,
                                                          const float *dloads, double *loads) {
     const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kGroupJ;
     const int lane = threadIdx.x & (kGroupJ - 1);
     const bool valid = g < n;
-    if (dloads) {
-        float hi[6], lo[6];
-        group_gather9c_j(ptr, inc, dloads, g, valid, lane, hi, lo);
-        if (valid && lane == 0) {
+    float hi[6], lo[6];
+    group_gather9c_j(ptr, inc, dloads, g, valid, lane, hi, lo);
+    if (valid && lane == 0) {
 #pragma unroll
-            for (int c = 0; c < 6; ++c) loads[6 * g + c] += (double)hi[c] + (double)lo[c];
-        }
+        for (int c = 0; c < 6; ++c) loads[6 * g + c] += (double)hi[c] + (double)lo[c];
     }
-    if (valid && lane == 0) st3(x_end, g, ld3(x, g) + ld3(y + 6 * g));
 }
 
 // Per-step constants from maintained loads: r0 and the rhs scale terms.
@@ -1425,11 +1479,36 @@ int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32,
 
 int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const float *units32,
                              const double *residual, double *scaled, double *norms, double *partials, void *stream) {
+    // P in 16-byte quads, units in 8-byte pairs, residual and scaled in 16-byte pairs
     if (n_sites <= 0 || !preconditioner || !units32 || !residual || (norms && !partials) ||
-        ((uintptr_t)preconditioner & 7u))
+        ((uintptr_t)preconditioner & 15u) || ((uintptr_t)units32 & 7u) || ((uintptr_t)residual & 15u) ||
+        ((uintptr_t)scaled & 15u))
         return DPF_ERR_ARGUMENT;
-    scale_sites_f32<<<reduce_grid(6 * n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units32,
-                                                                                      residual, scaled, norms, partials);
+    scale_sites_f32<<<reduce_grid(n_sites), kThreads, 0, (cudaStream_t)stream>>>(n_sites, preconditioner, units32,
+                                                                                  residual, scaled, norms, partials);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+static int mixed_jvp(const dpf_graph *g, float *bond_data, const float *y32, const double *direction,
+                     const float *direction32, const float *mass32, const uint8_t *fixed, double dt,
+                     const float *units32, const float *preconditioner, double *out, float *out32, float *d32,
+                     float *wrench, const int32_t *seg_bond, const uint8_t *active, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !y32 || (!direction && !direction32) || !mass32 || !fixed ||
+        (!out && !out32) || !d32 || (g->n_bonds && !wrench) || (preconditioner && !units32) ||
+        (active && !seg_bond) || ((uintptr_t)preconditioner & 7u))  // rows of P are read in 8-byte pairs
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int64_t n6 = 6 * g->n_sites;
+    prepare_direction<<<blocks_for(n6, kThreads), kThreads, 0, st>>>(n6, direction32 ? nullptr : direction,
+                                                                     direction32, units32, d32);
+    if (g->n_bonds) {
+        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, d32, wrench, seg_bond, active};
+        jvp_bonds_mixed<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+    }
+    JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, d32, mass32, preconditioner, units32, fixed,
+                  (float)(0.5 * dt * dt), out32 ? nullptr : out, out32};
+    jvp_sites_mixed<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(s);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
@@ -1438,22 +1517,17 @@ int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float 
                               const float *mass32, const uint8_t *fixed, double dt, const float *units32,
                               const float *preconditioner, double *out, float *d32, float *wrench,
                               const int32_t *seg_bond, const uint8_t *active, void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !y32 || !direction || !mass32 || !fixed || !out || !d32 ||
-        (g->n_bonds && !wrench) || (preconditioner && !units32) || (active && !seg_bond) ||
-        ((uintptr_t)preconditioner & 7u))  // rows of P are read in 8-byte pairs
-        return DPF_ERR_ARGUMENT;
-    cudaStream_t st = (cudaStream_t)stream;
-    const int64_t n6 = 6 * g->n_sites;
-    prepare_direction<<<blocks_for(n6, kThreads), kThreads, 0, st>>>(n6, direction, units32, d32);
-    if (g->n_bonds) {
-        JvpArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), y32, d32, wrench, seg_bond, active};
-        jvp_bonds_mixed<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
-    }
-    JvpSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, d32, mass32, preconditioner, units32, fixed,
-                  (float)(0.5 * dt * dt), out};
-    jvp_sites_mixed<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(s);
-    DPF_CHECK_LAUNCH();
-    return DPF_OK;
+    if (!direction || !out) return DPF_ERR_ARGUMENT;
+    return mixed_jvp(g, bond_data, y32, direction, nullptr, mass32, fixed, dt, units32, preconditioner, out, nullptr,
+                     d32, wrench, seg_bond, active, stream);
+}
+
+int dpf_mixed_jacobian_vector_f32(const dpf_graph *g, float *bond_data, const float *y32, const float *direction,
+                                  const float *mass32, const uint8_t *fixed, double dt, const float *units32,
+                                  const float *preconditioner, float *out, float *d32, float *wrench, void *stream) {
+    if (!direction || !out) return DPF_ERR_ARGUMENT;
+    return mixed_jvp(g, bond_data, y32, nullptr, direction, mass32, fixed, dt, units32, preconditioner, nullptr, out,
+                     d32, wrench, nullptr, nullptr, stream);
 }
 
 int dpf_mixed_stiffness_apply(const dpf_graph *g, float *bond_data, const float *q, double *out, float *wrench,
@@ -1560,13 +1634,15 @@ int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h,
         ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
+    end_positions<<<blocks_for(3 * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, h->x, y, x_end);
     if (g->n_bonds) {
-        CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y32, y, normal_end, offset_end, fs_end,
-                     mb_end, fn_end, mt_end, dloads};
+        CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y32, x_end, normal_end, offset_end,
+                     fs_end, mb_end, fn_end, mt_end, dloads};
         commit_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+        if (dloads)
+            commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(
+                g->n_sites, g->inc_ptr, g->inc_bond, dloads, loads);
     }
-    commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(
-        g->n_sites, g->inc_ptr, g->inc_bond, h->x, y, x_end, g->n_bonds ? dloads : nullptr, loads);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -455,6 +455,141 @@ static DeviceInfo &device_info() {
 
 using namespace dpf;
 
+namespace dpf {
+
+// ---------------------------------------------------------------------------
+// Krylov vectors in float32 with exactly accumulated float32 pairs.  The
+// mixed Newton path's Krylov inputs (PCG and JVP outputs, the scaled residual)
+// carry float32 precision; storing the basis in float32 and forming dot
+// products and updates as float32 pairs (TwoProd by FMA, TwoSum) gives
+// float64-quality sums without float64 arithmetic per entry, which is scarce
+// on this part (the float64 form of these kernels ran at 77-82% of the FP64
+// pipe).  Block partials and the Hessenberg entries stay float64.
+
+__device__ __forceinline__ void ff_two_sum(float &s, float &e, float b) {
+    const float t = s + b;
+    const float bp = t - s;
+    e += (s - (t - bp)) + (b - bp);
+    s = t;
+}
+
+// (hi, lo) += a b exactly up to the pair's precision
+__device__ __forceinline__ void ff_add_product(float &hi, float &lo, float a, float b) {
+    const float p = a * b;
+    const float e = fmaf(a, b, -p);
+    ff_two_sum(hi, lo, p);
+    lo += e;
+}
+
+__device__ __forceinline__ double ff_value(float hi, float lo) { return (double)hi + (double)lo; }
+
+// float64 value v as hi + lo float32 (lo the rounded remainder)
+__device__ __forceinline__ void ff_split(double v, float &hi, float &lo) {
+    hi = (float)v;
+    lo = (float)(v - (double)hi);
+}
+
+__global__ void __launch_bounds__(kThreads) arnoldi32_dots(int64_t len, const float *basis, int64_t ld, int count,
+                                                           const float *w, double *part) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int k = 0; k < count; ++k) {
+        const float *row = basis + k * ld;
+        float hi = 0.0f, lo = 0.0f;
+        for (int64_t e = tid; e < len; e += stride) ff_add_product(hi, lo, row[e], w[e]);
+        const double p = block_sum(ff_value(hi, lo));
+        if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = p;
+    }
+}
+
+// values_k = sum of part_in; h[k] (=|+=) values_k; w -= sum_k values_k basis_k
+// (the projection as a float32 pair, w rounded once); then the next pass's
+// partial dots (want_dots) or |w|^2 (part_out[blk]).
+__global__ void __launch_bounds__(kThreads) arnoldi32_update(int64_t len, const float *basis, int64_t ld, int count,
+                                                             float *w, const double *part_in, double *h,
+                                                             int accumulate, double *part_out, int want_dots) {
+    __shared__ double values[kMaxArnoldi];
+    __shared__ float vhi[kMaxArnoldi], vlo[kMaxArnoldi];
+    for (int k = 0; k < count; ++k) {
+        const double v = block_sum_array(part_in + k * gridDim.x, gridDim.x);
+        if (threadIdx.x == 0) {
+            values[k] = v;
+            ff_split(v, vhi[k], vlo[k]);
+        }
+    }
+    __syncthreads();
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (int k = 0; k < count; ++k) h[k] = accumulate ? h[k] + values[k] : values[k];
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    float sq_hi = 0.0f, sq_lo = 0.0f;
+    for (int64_t e = tid; e < len; e += stride) {
+        float ph = 0.0f, pl = 0.0f;
+        for (int k = 0; k < count; ++k) {
+            const float b = basis[k * ld + e];
+            ff_add_product(ph, pl, vhi[k], b);
+            pl = fmaf(vlo[k], b, pl);
+        }
+        // w - (ph + pl): the difference w - ph exactly (TwoSum), then the rest
+        float d = w[e], err = 0.0f;
+        ff_two_sum(d, err, -ph);
+        const float wv = d + (err - pl);
+        w[e] = wv;
+        ff_add_product(sq_hi, sq_lo, wv, wv);
+    }
+    if (want_dots) {
+        for (int k = 0; k < count; ++k) {
+            const float *row = basis + k * ld;
+            float hi = 0.0f, lo = 0.0f;
+            for (int64_t e = tid; e < len; e += stride) ff_add_product(hi, lo, row[e], w[e]);
+            const double p = block_sum(ff_value(hi, lo));
+            if (threadIdx.x == 0) part_out[k * gridDim.x + blockIdx.x] = p;
+        }
+    } else {
+        const double sq = block_sum(ff_value(sq_hi, sq_lo));
+        if (threadIdx.x == 0) part_out[blockIdx.x] = sq;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) arnoldi32_normalize(int64_t len, float *basis, int64_t ld, int j,
+                                                                const float *w, const double *part, double *h) {
+    const double nrm = sqrt(block_sum_array(part, gridDim.x));
+    if (blockIdx.x == 0 && threadIdx.x == 0) h[j + 1] = nrm;
+    if (!(nrm >= 1e-14)) return;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    float *row = basis + (int64_t)(j + 1) * ld;
+    const float inv = (float)(1.0 / nrm);
+    for (int64_t e = tid; e < len; e += stride) row[e] = w[e] * inv;
+}
+
+// x += sum_k c_k rows_k, the sum as a float32 pair, added to float64 x
+__global__ void __launch_bounds__(kThreads) combine32_kernel(int64_t len, const float *rows, int64_t ld, int count,
+                                                             Coefficients coef, double *x) {
+    __shared__ float chi[kMaxArnoldi], clo[kMaxArnoldi];
+    if (threadIdx.x < count) ff_split(coef.c[threadIdx.x], chi[threadIdx.x], clo[threadIdx.x]);
+    __syncthreads();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < len; e += stride) {
+        float hi = 0.0f, lo = 0.0f;
+        for (int k = 0; k < count; ++k) {
+            const float r = rows[k * ld + e];
+            ff_add_product(hi, lo, chi[k], r);
+            lo = fmaf(clo[k], r, lo);
+        }
+        x[e] += ff_value(hi, lo);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) scale_to_float_kernel(int64_t len, double alpha, const double *a,
+                                                                  float *out) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < len; e += stride)
+        out[e] = (float)(alpha * a[e]);
+}
+
+}  // namespace dpf
+
 extern "C" {
 
 int64_t dpf_elastic_workspace_doubles(int64_t n_sites) { return 30 * n_sites + 2 * (int64_t)kMaxPcgBlocks; }
@@ -528,6 +663,41 @@ int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w
     arnoldi_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pa, h, 0, pb, 1);
     arnoldi_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pb, h, 1, pa, 0);
     arnoldi_normalize<<<grid, kThreads, 0, st>>>(length, basis, ld, j, w, pa, h);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, float *w, double *h, double *partials,
+                         void *stream) {
+    if (length <= 0 || !basis || !w || !h || !partials || j < 0 || j + 1 >= kMaxArnoldi || ld < length)
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int grid = reduce_grid(length);
+    const int count = j + 1;
+    double *pa = partials + kPartialsOffset;
+    double *pb = pa + (int64_t)kMaxArnoldi * kMaxReduceBlocks;
+    arnoldi32_dots<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pa);
+    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pa, h, 0, pb, 1);
+    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pb, h, 1, pa, 0);
+    arnoldi32_normalize<<<grid, kThreads, 0, st>>>(length, basis, ld, j, w, pa, h);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_combine_rows_f32(int64_t length, const float *rows, int64_t ld, int count, const double *coefficients,
+                         double *x, void *stream) {
+    if (length <= 0 || !rows || !x || count < 0 || count > kMaxArnoldi || (count && !coefficients))
+        return DPF_ERR_ARGUMENT;
+    Coefficients c{};
+    for (int k = 0; k < count; ++k) c.c[k] = coefficients[k];
+    combine32_kernel<<<reduce_grid(length), kThreads, 0, (cudaStream_t)stream>>>(length, rows, ld, count, c, x);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_scale_to_float(int64_t length, double alpha, const double *a, float *out, void *stream) {
+    if (length <= 0 || !a || !out) return DPF_ERR_ARGUMENT;
+    scale_to_float_kernel<<<reduce_grid(length), kThreads, 0, (cudaStream_t)stream>>>(length, alpha, a, out);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

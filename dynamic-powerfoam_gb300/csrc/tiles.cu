@@ -773,9 +773,11 @@ struct PcgArgs {
     const float4 *P24;
     const float *block, *units32;
     const double *vector;
+    const float *vector32;  // float32 input instead of vector (one of the two)
     double tol2;
     int max_it;
     double *out;
+    float *out32;           // float32 output instead of out (one of the two)
     int *iterations;
     float *x, *r, *u, *p, *s, *w;  // (N, 6) each
     double *part_a, *part_b;
@@ -849,7 +851,8 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
     for (int64_t s = tid; s < a.n; s += stride) {
         float v[6], rr[6], zz[6], Pm[21];
 #pragma unroll
-        for (int c = 0; c < 6; ++c) v[c] = a.units32[6 * s + c] * (float)a.vector[6 * s + c];
+        for (int c = 0; c < 6; ++c)
+            v[c] = a.units32[6 * s + c] * (a.vector32 ? a.vector32[6 * s + c] : (float)a.vector[6 * s + c]);
         if (a.fixed[s]) {
 #pragma unroll
             for (int c = 0; c < 6; ++c) rr[c] = 0.0f;
@@ -872,7 +875,12 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
     double gamma = block_sum_array(a.part_b, gridDim.x);
     const double initial = gamma;
     if (initial == 0.0) {
-        for (int64_t e = tid; e < 6 * a.n; e += stride) a.out[e] = 0.0;
+        for (int64_t e = tid; e < 6 * a.n; e += stride) {
+            if (a.out32)
+                a.out32[e] = 0.0f;
+            else
+                a.out[e] = 0.0;
+        }
         return;
     }
     double alpha_prev = 1.0, gamma_prev = 1.0;
@@ -914,7 +922,13 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
         float xv[6];
         ld6(a.x + 6 * s, xv);
 #pragma unroll
-        for (int c = 0; c < 6; ++c) a.out[6 * s + c] = (double)(xv[c] / a.units32[6 * s + c]);
+        for (int c = 0; c < 6; ++c) {
+            const float v = xv[c] / a.units32[6 * s + c];
+            if (a.out32)
+                a.out32[6 * s + c] = v;
+            else
+                a.out[6 * s + c] = (double)v;
+        }
     }
     if (tid == 0) atomicAdd(a.iterations, it < a.max_it ? it + 1 : a.max_it);
 }
@@ -1377,15 +1391,15 @@ int dpf_end_hvp(const dpf_graph *g, const float *ends, const float *site4, const
     return DPF_OK;
 }
 
-int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
-                         const float *block32, const float *P24, const float *units32, const double *vector,
-                         double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
-                         double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
-                         const uint8_t *active, int variant, void *stream) {
+static int end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
+                            const float *block32, const float *P24, const float *units32, const double *vector,
+                            const float *vector32, double tolerance, int max_iterations, double *out, float *out32,
+                            int *iterations, float *workspace, double *partials, unsigned *barrier, int *status,
+                            const int32_t *seg_site, const uint8_t *active, int variant, void *stream) {
     if (!g || g->n_sites <= 0 || !g->inc_ptr || (g->n_bonds && (!ends || !aligned16(ends))) || !site4 || !fixed ||
-        !block32 || !P24 || !units32 || !vector || !out || !iterations || !workspace || !partials || !barrier ||
-        !status || max_iterations < 1 || !aligned16(workspace) || !aligned16(P24) || !aligned16(site4) ||
-        (active && !seg_site) || variant < 0 || variant >= kEndVariants)
+        !block32 || !P24 || !units32 || (!vector && !vector32) || (!out && !out32) || !iterations || !workspace ||
+        !partials || !barrier || !status || max_iterations < 1 || !aligned16(workspace) || !aligned16(P24) ||
+        !aligned16(site4) || (active && !seg_site) || variant < 0 || variant >= kEndVariants)
         return DPF_ERR_ARGUMENT;
     int grid = 0;
     const EndPcgKernel kernel = end_pcg_variant(variant);
@@ -1399,10 +1413,12 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
     a.P24 = reinterpret_cast<const float4 *>(P24);
     a.block = block32;
     a.units32 = units32;
-    a.vector = vector;
+    a.vector = vector32 ? nullptr : vector;
+    a.vector32 = vector32;
     a.tol2 = tolerance * tolerance;
     a.max_it = max_iterations;
-    a.out = out;
+    a.out = out32 ? nullptr : out;
+    a.out32 = out32;
     a.iterations = iterations;
     a.x = workspace;
     a.r = workspace + n6;
@@ -1427,6 +1443,27 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
         return DPF_ERR_CUDA;
     }
     return DPF_OK;
+}
+
+int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
+                         const float *block32, const float *P24, const float *units32, const double *vector,
+                         double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
+                         double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
+                         const uint8_t *active, int variant, void *stream) {
+    if (!vector || !out) return DPF_ERR_ARGUMENT;
+    return end_precondition(g, ends, site4, fixed, block32, P24, units32, vector, nullptr, tolerance, max_iterations,
+                            out, nullptr, iterations, workspace, partials, barrier, status, seg_site, active, variant,
+                            stream);
+}
+
+int dpf_end_precondition_f32(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
+                             const float *block32, const float *P24, const float *units32, const float *vector,
+                             double tolerance, int max_iterations, float *out, int *iterations, float *workspace,
+                             double *partials, unsigned *barrier, int *status, int variant, void *stream) {
+    if (!vector || !out) return DPF_ERR_ARGUMENT;
+    return end_precondition(g, ends, site4, fixed, block32, P24, units32, nullptr, vector, tolerance, max_iterations,
+                            nullptr, out, iterations, workspace, partials, barrier, status, nullptr, nullptr, variant,
+                            stream);
 }
 
 }  // extern "C"

@@ -716,6 +716,24 @@ class _Krylov:
         self.h = torch.zeros(72, dtype=F64, device=device)
 
 
+class _Krylov32:
+    """Float32 Krylov vectors of the mixed Newton path's FGMRES (basis,
+    transformed rows, the Arnoldi vector) with its float64 h column, partials
+    and vectors (x, true residual)."""
+
+    def __init__(self, length, width, device):
+        self.length, self.width = length, width
+        f32 = torch.float32
+        self.basis = torch.empty((width+1, length), dtype=f32, device=device)
+        self.transformed = torch.empty((width, length), dtype=f32, device=device)
+        self.w = torch.empty(length, dtype=f32, device=device)
+        self.h = torch.zeros(72, dtype=F64, device=device)
+        self.partials = torch.zeros(_lib.load().dpf_partials_doubles(), dtype=F64, device=device)
+        self.scalars = torch.zeros(2, dtype=F64, device=device)
+        self.x = torch.empty(length, dtype=F64, device=device)
+        self.residual = torch.empty(length, dtype=F64, device=device)
+
+
 def _back_substitute(h, g, k):
     """Solve the k x k upper-triangular h[:k, :k] c = g[:k] (the Givens-reduced
     Hessenberg system) row by row from the bottom, float64 operation for
@@ -1037,6 +1055,10 @@ class NewtonBonds(FiniteBonds):
         self.commit(state)
         self.v, self.rotation = self._v, rotation
 
+    def _krylov_solve(self, operator, rhs, precondition, tolerance, rhs_norm, dt):
+        """FGMRES on the scaled Newton system (``bonded_dem_newton.py:160-162``)."""
+        return fgmres(operator, rhs, precondition, tolerance=tolerance, workspace=self._krylov, rhs_norm=rhs_norm)
+
     def _dense_direction(self, operator, scaled):
         """Newton direction of the 'dense' backend (``bonded_dem_newton.py:163-175``):
         the scaled Jacobian restricted to the free DOFs is built one unit
@@ -1113,8 +1135,7 @@ class NewtonBonds(FiniteBonds):
                 rhs = torch.empty_like(scaled)
                 self._call('dpf_axpby', n6, -1., scaled.data_ptr(), 0., scaled.data_ptr(), rhs.data_ptr(), stream)
                 # rhs = -scaled, whose float64 norm the residual pass returned (merit)
-                delta, metrics = fgmres(operator, rhs, precondition, tolerance=linear_tolerance,
-                                        workspace=self._krylov, rhs_norm=merit)
+                delta, metrics = self._krylov_solve(operator, rhs, precondition, linear_tolerance, merit, dt)
                 krylov += metrics['iterations']
             else:
                 raise ValueError(backend)
@@ -1237,8 +1258,7 @@ class MixedNewtonBonds(NewtonBonds):
         if cached is not None and cached[0] == key:
             return cached[1]
         n, dev, lib = self.n_sites, self.device, self._lib
-        if self._krylov is None or self._krylov.length != 6*n:
-            self._krylov = _Krylov(6*n, 32, dev)
+        ws = self._krylov_workspace32()
         if getattr(self, '_native_vectors', None) is None:
             self._native_vectors = torch.empty((_lib.NEWTON_VECTORS, n, 6), dtype=F64, device=dev)
             self._native_partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=dev)
@@ -1257,13 +1277,102 @@ class MixedNewtonBonds(NewtonBonds):
             d32=ptr(self._d32), wrench32=ptr(self._wrench32), block32=ptr(self._block32), p32=ptr(self._p32),
             units=ptr(self._units), units32=ptr(self._units32), ends=ptr(self._ends), site4=ptr(self._site4),
             p24=ptr(self._p24), end_workspace=ptr(self._tiled_workspace), end_partials=ptr(self._tiled_partials),
-            barrier=ptr(self._barrier), inner=ptr(self._inner), basis=ptr(self._krylov.basis),
-            transformed=ptr(self._krylov.transformed), h=ptr(self._krylov.h), krylov_width=self._krylov.width,
+            barrier=ptr(self._barrier), inner=ptr(self._inner), basis=ptr(ws.basis),
+            transformed=ptr(ws.transformed), w32=ptr(ws.w), h=ptr(ws.h), krylov_width=ws.width,
             krylov_partials=ptr(self._native_partials), krylov_scalars=ptr(self._native_scalars),
             vectors=ptr(self._native_vectors), host=ptr(self._native_host), end_variant=int(self._end_variant))
         # the descriptor holds only addresses: keep what they point into alive with it
-        self._native_desc = (key, desc, self._krylov)
+        self._native_desc = (key, desc, ws)
         return desc
+
+    def _krylov_workspace32(self):
+        ws = getattr(self, '_krylov32', None)
+        if ws is None or ws.length != 6*self.n_sites:
+            ws = self._krylov32 = _Krylov32(6*self.n_sites, 32, self.device)
+        return ws
+
+    def _krylov_solve(self, operator, rhs, precondition, tolerance, rhs_norm, dt):
+        cls = type(self)
+        if self.sweep == 'ends' and cls._newton_operator is MixedNewtonBonds._newton_operator and \
+                cls._newton_preconditioner is MixedNewtonBonds._newton_preconditioner:
+            return self._fgmres32(operator, rhs, tolerance, rhs_norm, dt)
+        return super()._krylov_solve(operator, rhs, precondition, tolerance, rhs_norm, dt)
+
+    def _fgmres32(self, operator, b, tolerance, norm, dt, restart=32, max_iterations=256):
+        """``fgmres`` with float32 Krylov vectors: the elastic PCG and the JVP read
+        and write float32 rows (their values carry float32 precision either
+        way), the Arnoldi sums are exact float32 pairs with float64 partials
+        and h, and x, b and the true residual stay float64.  The Hessenberg
+        recurrence, stopping rules and restarts are those of ``fgmres``
+        (``bonded_dem_newton.py:13-60``); the library's step driver runs the
+        same launches."""
+        lib, stream = self._lib, self._stream()
+        n6 = 6*self.n_sites
+        ws = self._krylov_workspace32()
+        b = b.reshape(-1)
+        x, res = ws.x, ws.residual
+        x.zero_()
+        if norm == 0:
+            return x.view(-1, 6), dict(iterations=0, relative_residual=0.)
+
+        def norm_of(v):
+            self._call('dpf_dot_norm', n6, v.data_ptr(), None, ws.scalars.data_ptr(), ws.partials.data_ptr(),
+                       stream)
+            return float(ws.scalars[1])
+
+        iterations, relative, first = 0, float('nan'), True
+        while iterations < max_iterations:
+            width = min(restart, max_iterations - iterations)
+            h = np.zeros((width+1, width)); cs, sn = np.zeros(width), np.zeros(width)
+            g = np.zeros(width+1)
+            g[0] = norm if first else norm_of(res)
+            start = b if first else res
+            first = False
+            self._call('dpf_scale_to_float', n6, 1./g[0], start.data_ptr(), ws.basis[0].data_ptr(), stream)
+            for j in range(width):
+                bj, tj = ws.basis[j], ws.transformed[j]
+                if self._packed != ('ends', dt):     # at the first PCG of a tangent, as the step driver does
+                    self._pack_ends(dt)
+                if self._end_variant is None:
+                    from .tiles import tune_end_sweep
+                    self._end_variant = tune_end_sweep(self, b.view(-1, 6))
+                self._timed('pcg', lambda: self._call(
+                    'dpf_end_precondition_f32', ctypes.byref(self._graph), self._ends.data_ptr(),
+                    self._site4.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p24.data_ptr(),
+                    self._units32.data_ptr(), bj.data_ptr(), .03, 80, tj.data_ptr(), self._inner.data_ptr(),
+                    self._tiled_workspace.data_ptr(), self._tiled_partials.data_ptr(), self._barrier.data_ptr(),
+                    self._status.data_ptr(), int(self._end_variant), stream))
+                self._timed('jvp', lambda: self._call(
+                    'dpf_mixed_jacobian_vector_f32', ctypes.byref(self._graph), self._bond_data.data_ptr(),
+                    self._y32.data_ptr(), tj.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), dt,
+                    self._units32.data_ptr(), self._p32.data_ptr(), ws.w.data_ptr(), self._d32.data_ptr(),
+                    self._wrench32.data_ptr(), stream))
+                self._call('dpf_arnoldi_cgs2_f32', n6, ws.basis.data_ptr(), n6, j, ws.w.data_ptr(), ws.h.data_ptr(),
+                           ws.partials.data_ptr(), stream)
+                column = ws.h[:j+2].cpu().numpy()
+                h[:j+1, j] = column[:j+1]
+                h[j+1, j] = column[j+1]
+                breakdown = h[j+1, j] < 1e-14
+                for k in range(j):
+                    h[k, j], h[k+1, j] = cs[k]*h[k, j] + sn[k]*h[k+1, j], -sn[k]*h[k, j] + cs[k]*h[k+1, j]
+                denominator = np.hypot(h[j, j], h[j+1, j])
+                if denominator == 0:
+                    raise SubdivideError('Subdivide: singular Newton linear system')
+                cs[j], sn[j] = h[j, j]/denominator, h[j+1, j]/denominator
+                h[j, j], h[j+1, j] = denominator, 0.
+                g[j+1], g[j] = -sn[j]*g[j], cs[j]*g[j]
+                iterations += 1
+                if abs(g[j+1]) <= tolerance*norm or breakdown or j+1 == width:
+                    coefficients = _back_substitute(h, g, j+1)
+                    self._call('dpf_combine_rows_f32', n6, ws.transformed.data_ptr(), n6, j+1,
+                               coefficients.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), x.data_ptr(), stream)
+                    ax = operator(x.view(-1, 6)).reshape(-1)
+                    self._call('dpf_axpby', n6, 1., b.data_ptr(), -1., ax.data_ptr(), res.data_ptr(), stream)
+                    relative = norm_of(res)/norm
+                    if relative <= 1.05*tolerance:
+                        return x.view(-1, 6), dict(iterations=iterations, relative_residual=relative)
+                    break
+        raise SubdivideError(f'Subdivide: FGMRES did not converge ({relative:g})')
 
     @torch.no_grad()
     def _native_step(self, dt, external, tolerance, max_iterations, pose_tolerance, linear_tolerance):

@@ -239,10 +239,25 @@ int64_t dpf_partials_doubles(void);
 int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w, double *h,
                      double *partials, void *stream);
 
+/* dpf_arnoldi_cgs2 on float32 vectors (basis rows and w): dot products and
+ * the projection are summed exactly as float32 pairs (TwoProd by FMA and
+ * TwoSum), block partials and h in float64, w and the new row rounded to
+ * float32 once.  partials: dpf_partials_doubles(). */
+int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, float *w, double *h,
+                         double *partials, void *stream);
+
 /* x += sum_{k<count} coefficients[k] * rows[k]  (coefficients on the host, count <= 64).
  * Replaces `x += transformed[:j+1].T @ coefficients` (experiments/bonded_dem_newton.py:54). */
 int dpf_combine_rows(int64_t length, const double *rows, int64_t ld, int count,
                      const double *coefficients, double *x, void *stream);
+
+/* x += sum_k coefficients[k] rows[k] for float32 rows into float64 x (the
+ * sum as a float32 pair). */
+int dpf_combine_rows_f32(int64_t length, const float *rows, int64_t ld, int count,
+                         const double *coefficients, double *x, void *stream);
+
+/* out = (float)(alpha a) */
+int dpf_scale_to_float(int64_t length, double alpha, const double *a, float *out, void *stream);
 
 /* result[0] = sum a*b and result[1] = sqrt(sum a*a) over `length` doubles (device). */
 int dpf_dot_norm(int64_t length, const double *a, const double *b, double *result,
@@ -396,7 +411,8 @@ int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32,
                       double *units, float *units32, void *stream);
 
 /* Scaled residual with the float32 block inverse: s = P r / units and
- * norms = [|r|, max|s|, |s|] (float64).
+ * norms = [|r|, max|s|, |s|] (float64; |s|^2 is summed exactly in float32
+ * pairs).  P and residual/scaled are 16-byte aligned, units32 8-byte aligned.
  * Replaces NewtonBonds.scale_residual (experiments/bonded_dem_newton.py:104-105). */
 int dpf_mixed_scale_residual(int64_t n_sites, const float *preconditioner, const float *units32,
                              const double *residual, double *scaled, double *norms, double *partials,
@@ -413,6 +429,13 @@ int dpf_mixed_jacobian_vector(const dpf_graph *g, float *bond_data, const float 
                               double dt, const float *units32, const float *preconditioner,
                               double *out, float *d32, float *wrench, const int32_t *seg_bond,
                               const uint8_t *active, void *stream);
+
+/* dpf_mixed_jacobian_vector with a float32 direction and float32 output (the
+ * float32 Krylov vectors of the mixed Newton path); no batch masks. */
+int dpf_mixed_jacobian_vector_f32(const dpf_graph *g, float *bond_data, const float *y32,
+                                  const float *direction, const float *mass32, const uint8_t *fixed,
+                                  double dt, const float *units32, const float *preconditioner,
+                                  float *out, float *d32, float *wrench, void *stream);
 
 /* K q in float32 from the stored tangent; q float32 (N, 6), out float64 (N, 6).
  * Replaces LinearBondsGPU.stiffness (experiments/bonded_dem_linear_gpu.py:42-52). */
@@ -649,6 +672,13 @@ int dpf_end_precondition(const dpf_graph *g, const float *ends, const float *sit
                          double tolerance, int max_iterations, double *out, int *iterations, float *workspace,
                          double *partials, unsigned *barrier, int *status, const int32_t *seg_site,
                          const uint8_t *active, int variant, void *stream);
+
+/* dpf_end_precondition with a float32 input vector and float32 output (the
+ * float32 Krylov vectors of the mixed Newton path); no batch masks. */
+int dpf_end_precondition_f32(const dpf_graph *g, const float *ends, const float *site4, const uint8_t *fixed,
+                             const float *block32, const float *P24, const float *units32, const float *vector,
+                             double tolerance, int max_iterations, float *out, int *iterations, float *workspace,
+                             double *partials, unsigned *barrier, int *status, int variant, void *stream);
 int dpf_tiled_precondition(const dpf_graph *g, const dpf_tiles *t, const float *entries, const float *site4,
                            const uint8_t *fixed, const float *block32, const float *P24, const float *units32,
                            const double *vector, double tolerance, int max_iterations, double *out, int *iterations,
@@ -732,7 +762,7 @@ int dpf_parallel_loads(const dpf_graph *g, const double *radii, const double *x,
  * (experiments/bonded_dem_newton.py:13-60, 132-201).
  *
  * Device pointers unless noted; float64 vectors are (N, 6) = 6 N doubles. */
-#define DPF_NEWTON_VECTORS 11      /* scratch vectors of 6 N doubles in `vectors` */
+#define DPF_NEWTON_VECTORS 10      /* scratch vectors of 6 N doubles in `vectors` */
 #define DPF_NEWTON_HOST_DOUBLES 128 /* pinned host doubles in `host` */
 #define DPF_NEWTON_TRACE 32         /* residual trace entries kept */
 #define DPF_NEWTON_TIMERS 6         /* setup, residual, scaling, pcg, jvp, commit */
@@ -760,7 +790,8 @@ typedef struct dpf_mixed_newton {
     double *end_partials;          /* dpf_tiled_partials_doubles() */
     unsigned *barrier;             /* 2 words */
     int *inner;                    /* CG iteration counter (added to) */
-    double *basis, *transformed;   /* (width + 1, 6 N), (width, 6 N) */
+    float *basis, *transformed;    /* float32 Krylov vectors (width + 1, 6 N), (width, 6 N) */
+    float *w32;                    /* 6 N floats */
     double *h;                     /* >= width + 2 */
     int krylov_width;              /* FGMRES restart length, <= 62 */
     double *krylov_partials;       /* dpf_partials_doubles() */
