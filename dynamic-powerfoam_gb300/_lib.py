@@ -68,10 +68,11 @@ class MixedNewton(ctypes.Structure):
                 [(k, vp) for k in ('radii', 'mass', 'mass32', 'fixed', 'bond_data', 'r0', 'loads', 'scales',
                                    'wrench64', 'partials', 'scalars', 'status', 'y32', 'd32', 'wrench32', 'block32',
                                    'p32', 'units', 'units32', 'ends', 'site4', 'p24', 'end_workspace',
-                                   'end_partials', 'barrier', 'inner', 'basis', 'transformed', 'w32', 'h')] +
+                                   'end_partials', 'barrier', 'inner', 'basis', 'transformed', 'products', 'w32',
+                                   'h')] +
                 [('krylov_width', i32)] +
                 [(k, vp) for k in ('krylov_partials', 'krylov_scalars', 'vectors', 'host')] +
-                [('end_variant', i32)])
+                [('end_variant', i32), ('history_increments', vp)])
 
 
 class NewtonStep(ctypes.Structure):
@@ -85,7 +86,7 @@ class NewtonStep(ctypes.Structure):
 NEWTON_VECTORS = 10
 NEWTON_HOST_DOUBLES = 128
 NEWTON_TRACE = 32
-NEWTON_TIMERS = ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit')
+NEWTON_TIMERS = ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit', 'pack', 'krylov', 'norms', 'vector', 'accept')
 (NEWTON_CONVERGED, NEWTON_GUARD, NEWTON_NONFINITE, NEWTON_SINGULAR, NEWTON_KRYLOV, NEWTON_LINE_SEARCH,
  NEWTON_DIVERGED) = range(7)
 
@@ -192,9 +193,12 @@ SIGNATURES = {
     'dpf_end_precondition_f32': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, i32,
                                        vp]),
     'dpf_mixed_jacobian_vector_f32': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp]),
-    'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp]),
+    'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp, vp]),
     'dpf_combine_rows_f32': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
     'dpf_scale_to_float': (i32, [i64, f64, vp, vp, vp]),
+    'dpf_history_increment_floats': (i64, [i64]),
+    'dpf_mixed_commit_lazy': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_fold_history': (i32, [P(Graph), P(History), vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_newton_struct_sizes': (i32, [P(ctypes.c_int64)]),
 }
 
@@ -215,7 +219,7 @@ KERNELS = {
     'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
     'dpf_end_precondition_f32': 1, 'dpf_mixed_jacobian_vector_f32': 3, 'dpf_arnoldi_cgs2_f32': 4,
-    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1,
+    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1, 'dpf_mixed_commit_lazy': 3, 'dpf_mixed_fold_history': 1,
 }
 LAUNCHES = {'count': 0}
 

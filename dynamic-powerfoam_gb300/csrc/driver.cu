@@ -37,10 +37,24 @@ __global__ void max_rotation_kernel(int64_t n, const double *y, unsigned long lo
     if ((threadIdx.x & 31) == 0 && best > 0.0) atomicMax(out, (unsigned long long)__double_as_longlong(best));
 }
 
-enum Timer { kSetup = 0, kResidual, kScaling, kPcg, kJvp, kCommit };
+// launch categories timed with step->timing (the order of DPF_NEWTON_TIMERS)
+enum Timer {
+    kSetup = 0,  // float64 setup or the per-step begin
+    kResidual,   // residual bond and site passes
+    kScaling,    // 6x6 blocks and their inverses
+    kPcg,        // the elastic PCG
+    kJvp,        // J d
+    kCommit,     // end state of the accepted increment
+    kPack,       // bond-end records of a tangent
+    kKrylov,     // Arnoldi, row combination, Krylov norms and scaling
+    kNorms,      // scaled residual and its norms
+    kVector,     // float64 vector updates (rhs, correction, candidates, float32 copies)
+    kAccept      // velocity, rotation, work and step statistics
+};
+static_assert(kAccept + 1 == DPF_NEWTON_TIMERS, "one timer per category");
 
-// CUDA events around the hot launches (only with step->timing), created for
-// the call and destroyed before it returns.
+// CUDA events around the launches (only with step->timing), created for the
+// call and destroyed before it returns.
 struct Timing {
     bool on = false;
     cudaStream_t stream = nullptr;
@@ -57,8 +71,6 @@ struct Timing {
         events.push_back(e);
         cudaEventRecord(e, stream);
     }
-    void begin(int key) { record(true, key); }
-    void end() { record(false, 0); }
     // after the stream has been synchronised
     void collect(dpf_newton_info *info) {
         for (size_t k = 0; k < keys.size() && 2 * k + 1 < events.size(); ++k) {
@@ -79,17 +91,22 @@ struct Step {
     const dpf_newton_step *a;
     dpf_newton_info *info;
     cudaStream_t st;
-    int64_t n, n6;
+    int64_t n, n6, m;
     double *y, *cand, *r, *r_cand, *scaled, *rhs, *x, *res, *corr, *ax;
-    double *host;     // pinned: [0..8) scalars, [8..10) scales, [16..16+72) h column
+    double *host;     // pinned: [0..8) scalars, [8..10) scales, [12] a norm, [16..80) h column
     int *host_int;    // pinned ints after the doubles: [0] status, [1] inner
     Timing timing;
     bool packed = false;
     double rhs_scale = -1.0;
 
-    int launched(int count) {
-        info->launches += count;
-        return DPF_OK;
+    // one library call of `kernels` launches, timed under `key`
+    template <class F>
+    int call(int key, int kernels, F &&f) {
+        timing.record(true, key);
+        const int rc = f();
+        timing.record(false, key);
+        if (!rc) info->launches += kernels;
+        return rc;
     }
 
     // copy `count` device scalars (and optionally the status word and the
@@ -105,71 +122,66 @@ struct Step {
     }
 
     int residual(const double *yy, double *out, bool use_p) {
-        int rc = dpf_to_float(n6, yy, s->y32, st);
+        int rc = call(kVector, 1, [&] { return dpf_to_float(n6, yy, s->y32, st); });
         if (rc) return rc;
-        launched(1);
         if (cudaMemsetAsync(s->status, 0, sizeof(int), st)) return DPF_ERR_CUDA;
-        timing.begin(kResidual);
-        rc = dpf_mixed_residual(s->graph, s->bond_data, yy, s->y32, s->mass, s->fixed, a->dt, s->r0, 1,
-                                use_p ? s->p32 : nullptr, use_p ? s->units32 : nullptr, out, nullptr,
-                                use_p ? s->scalars : nullptr, s->wrench32, s->partials, s->status, st);
-        timing.end();
-        return rc ? rc : launched(s->graph->n_bonds ? 2 : 1);
+        return call(kResidual, m ? 2 : 1, [&] {
+            return dpf_mixed_residual(s->graph, s->bond_data, yy, s->y32, s->mass, s->fixed, a->dt, s->r0, 1,
+                                      use_p ? s->p32 : nullptr, use_p ? s->units32 : nullptr, out, nullptr,
+                                      use_p ? s->scalars : nullptr, s->wrench32, s->partials, s->status, st);
+        });
     }
 
     // norms of the iterate's residual r: [|r|, max |s|, |s|] into s->scalars
     int iteration_norms() {
-        timing.begin(kScaling);
-        int rc = dpf_mixed_scaling(s->graph, s->bond_data, s->mass32, s->fixed, s->radii, a->dt, s->block32, s->p32,
-                                   s->units, s->units32, st);
-        timing.end();
+        int rc = call(kScaling, 1, [&] {
+            return dpf_mixed_scaling(s->graph, s->bond_data, s->mass32, s->fixed, s->radii, a->dt, s->block32,
+                                     s->p32, s->units, s->units32, st);
+        });
         if (rc) return rc;
-        launched(1);
-        rc = dpf_mixed_scale_residual(n, s->p32, s->units32, r, scaled, s->scalars, s->partials, st);
-        return rc ? rc : launched(1);
+        return call(kNorms, 1, [&] {
+            return dpf_mixed_scale_residual(n, s->p32, s->units32, r, scaled, s->scalars, s->partials, st);
+        });
     }
 
     // the elastic PCG on a float32 Krylov vector
     int precondition(const float *vector, float *out) {
-        int rc;
         if (!packed) {
-            rc = dpf_end_pack(s->graph, s->bond_data, 0.25 * a->dt * a->dt, s->p32, s->mass32, s->fixed, s->ends,
-                              s->p24, s->site4, st);
+            const int rc = call(kPack, 2, [&] {
+                return dpf_end_pack(s->graph, s->bond_data, 0.25 * a->dt * a->dt, s->p32, s->mass32, s->fixed,
+                                    s->ends, s->p24, s->site4, st);
+            });
             if (rc) return rc;
-            launched(2);
             packed = true;
         }
-        timing.begin(kPcg);
-        rc = dpf_end_precondition_f32(s->graph, s->ends, s->site4, s->fixed, s->block32, s->p24, s->units32, vector,
-                                      0.03, 80, out, s->inner, s->end_workspace, s->end_partials, s->barrier,
-                                      s->status, s->end_variant, st);
-        timing.end();
-        return rc ? rc : launched(1);
+        return call(kPcg, 1, [&] {
+            return dpf_end_precondition_f32(s->graph, s->ends, s->site4, s->fixed, s->block32, s->p24, s->units32,
+                                            vector, 0.03, 80, out, s->inner, s->end_workspace, s->end_partials,
+                                            s->barrier, s->status, s->end_variant, st);
+        });
     }
 
     // J d on float32 Krylov vectors
     int jvp32(const float *direction, float *out) {
-        timing.begin(kJvp);
-        const int rc = dpf_mixed_jacobian_vector_f32(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
-                                                     a->dt, s->units32, s->p32, out, s->d32, s->wrench32, st);
-        timing.end();
-        return rc ? rc : launched(s->graph->n_bonds ? 3 : 2);
+        return call(kJvp, m ? 3 : 2, [&] {
+            return dpf_mixed_jacobian_vector_f32(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
+                                                 a->dt, s->units32, s->p32, out, s->d32, s->wrench32, st);
+        });
     }
 
     // J d on a float64 vector (the Newton direction)
     int jvp(const double *direction, double *out) {
-        timing.begin(kJvp);
-        const int rc = dpf_mixed_jacobian_vector(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
-                                                 a->dt, s->units32, s->p32, out, s->d32, s->wrench32, nullptr,
-                                                 nullptr, st);
-        timing.end();
-        return rc ? rc : launched(s->graph->n_bonds ? 3 : 2);
+        return call(kJvp, m ? 3 : 2, [&] {
+            return dpf_mixed_jacobian_vector(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed, a->dt,
+                                             s->units32, s->p32, out, s->d32, s->wrench32, nullptr, nullptr, st);
+        });
     }
 
     int norm_of(const double *v, double *out) {
-        int rc = dpf_dot_norm(n6, v, nullptr, s->krylov_scalars, s->krylov_partials, st);
+        const int rc = call(kKrylov, 1, [&] {
+            return dpf_dot_norm(n6, v, nullptr, s->krylov_scalars, s->krylov_partials, st);
+        });
         if (rc) return rc;
-        launched(1);
         if (cudaMemcpyAsync(host + 12, s->krylov_scalars + 1, sizeof(double), cudaMemcpyDeviceToHost, st) ||
             cudaStreamSynchronize(st))
             return DPF_ERR_CUDA;
@@ -181,7 +193,8 @@ struct Step {
     // in newton.py): solves J delta = b with b = rhs, |b| = norm; x = delta.
     // The Krylov vectors are float32 (the PCG and JVP outputs carry float32
     // precision), their sums exact float32 pairs; x, b and the true residual
-    // are float64.  Sets *ok.
+    // are float64, the residual's J x formed from the kept products J z_k.
+    // Sets *ok.
     int fgmres(double norm, double tolerance, int restart, int max_iterations, bool *ok, int *krylov) {
         *ok = false;
         *krylov = 0;
@@ -212,19 +225,20 @@ struct Step {
             }
             const double *start = first ? rhs : res;
             first = false;
-            int rc = dpf_scale_to_float(n6, 1.0 / g[0], start, s->basis, st);
+            int rc = call(kKrylov, 1, [&] { return dpf_scale_to_float(n6, 1.0 / g[0], start, s->basis, st); });
             if (rc) return rc;
-            launched(1);
             for (int j = 0; j < width; ++j) {
                 float *bj = s->basis + (int64_t)j * n6;
                 float *tj = s->transformed + (int64_t)j * n6;
+                float *pj = s->products + (int64_t)j * n6;
                 rc = precondition(bj, tj);
                 if (rc) return rc;
-                rc = jvp32(tj, s->w32);
+                rc = jvp32(tj, pj);
                 if (rc) return rc;
-                rc = dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, s->w32, s->h, s->krylov_partials, st);
+                rc = call(kKrylov, 4, [&] {
+                    return dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, pj, s->w32, s->h, s->krylov_partials, st);
+                });
                 if (rc) return rc;
-                launched(4);
                 double *column = host + 16;
                 if (cudaMemcpyAsync(column, s->h, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st) ||
                     cudaStreamSynchronize(st))
@@ -257,14 +271,14 @@ struct Step {
                         for (int c = i + 1; c < k; ++c) acc -= H[i * ldh + c] * coef[c];
                         coef[i] = acc / H[i * ldh + i];
                     }
-                    rc = dpf_combine_rows_f32(n6, s->transformed, n6, k, coef, x, st);
+                    rc = call(kKrylov, 1, [&] { return dpf_combine_rows_f32(n6, s->transformed, n6, k, coef, x, st); });
                     if (rc) return rc;
-                    launched(1);
-                    rc = jvp(x, ax);
+                    // J x = sum_k c_k J z_k from the stored products (J is linear)
+                    if (cudaMemsetAsync(ax, 0, n6 * sizeof(double), st)) return DPF_ERR_CUDA;
+                    rc = call(kKrylov, 1, [&] { return dpf_combine_rows_f32(n6, s->products, n6, k, coef, ax, st); });
                     if (rc) return rc;
-                    rc = dpf_axpby(n6, 1.0, rhs, -1.0, ax, res, st);
+                    rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, rhs, -1.0, ax, res, st); });
                     if (rc) return rc;
-                    launched(1);
                     double rn;
                     rc = norm_of(res, &rn);
                     if (rc) return rc;
@@ -285,27 +299,28 @@ struct Step {
     }
 
     int accept() {
-        int rc = dpf_to_float(n6, y, s->y32, st);
+        int rc = call(kVector, 1, [&] { return dpf_to_float(n6, y, s->y32, st); });
         if (rc) return rc;
-        launched(1);
         const dpf_history &h = a->history;
-        timing.begin(kCommit);
-        rc = dpf_mixed_commit(s->graph, s->bond_data, &h, y, s->y32, a->x_end, a->normal_end, a->offset_end, a->fn_end,
-                              a->fs_end, a->mt_end, a->mb_end, s->wrench32, s->loads, st);
-        timing.end();
+        rc = call(kCommit, m ? 3 : 1, [&] {
+            if (s->history_increments)
+                return dpf_mixed_commit_lazy(s->graph, s->bond_data, h.x, y, s->y32, a->x_end, s->history_increments,
+                                             s->wrench32, s->loads, st);
+            return dpf_mixed_commit(s->graph, s->bond_data, &h, y, s->y32, a->x_end, a->normal_end, a->offset_end,
+                                    a->fn_end, a->fs_end, a->mt_end, a->mb_end, s->wrench32, s->loads, st);
+        });
         if (rc) return rc;
-        launched(s->graph->n_bonds ? 3 : 1);
-        rc = dpf_accept_step(n, y, a->dt, a->v, a->rotation, st);
+        rc = call(kAccept, 1, [&] { return dpf_accept_step(n, y, a->dt, a->v, a->rotation, st); });
         if (rc) return rc;
-        launched(1);
-        rc = dpf_dot_norm(n6, a->external, y, s->scalars, s->partials, st);
+        rc = call(kAccept, 1, [&] { return dpf_dot_norm(n6, a->external, y, s->scalars, s->partials, st); });
         if (rc) return rc;
-        launched(1);
         if (cudaMemsetAsync(s->scalars + 2, 0, sizeof(double), st)) return DPF_ERR_CUDA;
-        const int grid = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
-        max_rotation_kernel<<<grid, 256, 0, st>>>(n, y, reinterpret_cast<unsigned long long *>(s->scalars + 2));
-        if (cudaGetLastError() != cudaSuccess) return DPF_ERR_CUDA;
-        launched(1);
+        rc = call(kAccept, 1, [&] {
+            const int grid = (int)((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024);
+            max_rotation_kernel<<<grid, 256, 0, st>>>(n, y, reinterpret_cast<unsigned long long *>(s->scalars + 2));
+            return cudaGetLastError() == cudaSuccess ? DPF_OK : DPF_ERR_CUDA;
+        });
+        if (rc) return rc;
         if (cudaMemcpyAsync(host_int + 1, s->inner, sizeof(int), cudaMemcpyDeviceToHost, st)) return DPF_ERR_CUDA;
         rc = fetch(3, false, false);
         if (rc) return rc;
@@ -320,18 +335,19 @@ struct Step {
             cudaMemsetAsync(y, 0, n6 * sizeof(double), st))
             return DPF_ERR_CUDA;
         int rc;
-        timing.begin(kSetup);
         if (a->refresh) {
             const dpf_history &h = a->history;
-            rc = dpf_mixed_setup(s->graph, &s->stiffness, &h, s->mass, a->v, a->external, s->fixed, a->dt,
-                                 s->bond_data, s->r0, s->loads, s->scales, s->wrench64, s->partials, s->status, st);
-            if (!rc) launched(s->graph->n_bonds ? 2 : 1);
+            rc = call(kSetup, m ? 2 : 1, [&] {
+                return dpf_mixed_setup(s->graph, &s->stiffness, &h, s->mass, a->v, a->external, s->fixed, a->dt,
+                                       s->bond_data, s->r0, s->loads, s->scales, s->wrench64, s->partials, s->status,
+                                       st);
+            });
         } else {
-            rc = dpf_mixed_begin(n, s->loads, s->mass, a->v, a->external, s->fixed, a->dt, s->r0, s->scales,
-                                 s->partials, st);
-            if (!rc) launched(1);
+            rc = call(kSetup, 1, [&] {
+                return dpf_mixed_begin(n, s->loads, s->mass, a->v, a->external, s->fixed, a->dt, s->r0, s->scales,
+                                       s->partials, st);
+            });
         }
-        timing.end();
         if (rc) return rc;
         bool cached = false;
         const double dt = a->dt;
@@ -381,9 +397,8 @@ struct Step {
                 return DPF_OK;
             }
             if (iteration == a->max_iterations) break;
-            rc = dpf_axpby(n6, -1.0, scaled, 0.0, scaled, rhs, st);
+            rc = call(kVector, 1, [&] { return dpf_axpby(n6, -1.0, scaled, 0.0, scaled, rhs, st); });
             if (rc) return rc;
-            launched(1);
             bool ok;
             int krylov;
             rc = fgmres(merit, a->linear_tolerance, 32, 256, &ok, &krylov);
@@ -394,15 +409,13 @@ struct Step {
                 return DPF_OK;
             }
             info->krylov_iterations += krylov;
-            rc = dpf_masked_scale(n, x, s->units, s->fixed, corr, st);
+            rc = call(kVector, 1, [&] { return dpf_masked_scale(n, x, s->units, s->fixed, corr, st); });
             if (rc) return rc;
-            launched(1);
             bool accepted = false;
             for (int power = 0; power < 10; ++power) {
                 const double factor = std::ldexp(1.0, -power);
-                rc = dpf_axpby(n6, 1.0, y, factor, corr, cand, st);
+                rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, y, factor, corr, cand, st); });
                 if (rc) return rc;
-                launched(1);
                 rc = residual(cand, r_cand, true);
                 if (rc) return rc;
                 rc = fetch(3, true, false);
@@ -437,7 +450,7 @@ extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_n
                                      dpf_newton_info *info, void *stream) {
     using dpf::driver::Step;
     if (!solver || !step || !info || !solver->graph || solver->graph->n_sites <= 0 || !solver->vectors ||
-        !solver->host || !solver->basis || !solver->transformed || !solver->w32 || !solver->h ||
+        !solver->host || !solver->basis || !solver->transformed || !solver->products || !solver->w32 || !solver->h ||
         solver->krylov_width < 1 ||
         solver->krylov_width > 62 || !step->external || !step->v || !step->rotation || !(step->dt > 0.0) ||
         step->max_iterations < 0 || ((uintptr_t)solver->vectors & 15u))
@@ -450,6 +463,7 @@ extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_n
     run.st = (cudaStream_t)stream;
     run.n = solver->graph->n_sites;
     run.n6 = 6 * run.n;
+    run.m = solver->graph->n_bonds;
     double *v = solver->vectors;
     double **slots[DPF_NEWTON_VECTORS] = {&run.y, &run.cand, &run.r, &run.r_cand, &run.scaled,
                                           &run.rhs, &run.x, &run.res, &run.corr, &run.ax};

@@ -858,10 +858,14 @@ __global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
         for (int e = a.ptr[s]; e < e1; ++e) {
             const int v = a.inc[e];
             const int64_t b = v >= 0 ? v : ~v;
-            const float4 t0 = __ldg(a.bd.t0 + b), tr = __ldg((v >= 0 ? a.bd.t1 : a.bd.t2) + b);
-            const float4 t1w = __ldg(a.bd.t1 + b), t2w = __ldg(a.bd.t2 + b);
-            const float kt = __ldg(a.bd.t3 + b).x;
-            add_block_sym(D, {t0.x, t0.y, t0.z}, {tr.x, tr.y, tr.z}, t0.w, t1w.w, t2w.w, kt);
+            // (n, kn), this end's (lever, ks or kb), the other stiffness and kt:
+            // two 16-byte and two 4-byte loads
+            const bool at_i = v >= 0;
+            const float4 t0 = __ldg(a.bd.t0 + b), tr = __ldg((at_i ? a.bd.t1 : a.bd.t2) + b);
+            const float other_k = __ldg(reinterpret_cast<const float *>((at_i ? a.bd.t2 : a.bd.t1) + b) + 3);
+            const float kt = __ldg(reinterpret_cast<const float *>(a.bd.t3 + b));
+            const float ks = at_i ? tr.w : other_k, kb = at_i ? other_k : tr.w;
+            add_block_sym(D, {t0.x, t0.y, t0.z}, {tr.x, tr.y, tr.z}, t0.w, ks, kb, kt);
         }
     }
     if (!valid) return;
@@ -1185,7 +1189,22 @@ struct CommitArgs {
     const double *x_end;  // end positions x + y, formed first by end_positions
     double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
     float *dloads;  // optional: increment of the committed loads (9 floats per bond)
+    float4 *inc;    // lazy form: history increments since the last fold (6 float4 arrays of m)
 };
+
+// History increments since the last fold, per bond as float32 pairs: arrays
+// k = 0, 1, 2 hold the high parts (fs, fn), (mb, mt), (offset, 0) and
+// k = 3, 4, 5 the low parts.  hi + lo is the exact sum of the float32
+// increments (TwoSum), so a fold adds it to the float64 history with one
+// rounding instead of one per step.
+constexpr int kIncArrays = 6;
+
+__device__ __forceinline__ void accumulate4(float4 &hi, float4 &lo, float x, float y, float z, float w) {
+    two_sum(hi.x, lo.x, x);
+    two_sum(hi.y, lo.y, y);
+    two_sum(hi.z, lo.z, z);
+    two_sum(hi.w, lo.w, w);
+}
 
 // x_end = x + u per site, before the bond pass reads it.
 __global__ void __launch_bounds__(kThreads) end_positions(int64_t n, const double *x, const double *y, double *x_end) {
@@ -1199,6 +1218,20 @@ __global__ void __launch_bounds__(kThreads) end_positions(int64_t n, const doubl
 // records for the next step in place (the bond's own record only) and emits
 // loads(x_end) - loads(x) per bond as float32 increments.
 // 3 resident blocks per SM (80 registers) rather than 2 (88 registers).
+// end normal and length in float64 from the end positions (geometry(end));
+// one reciprocal square root instead of a square root and a division (float64
+// arithmetic is scarce on this part).  The fold of the lazy form uses it too.
+__device__ __forceinline__ d3 end_normal(const double *x, int64_t i, int64_t j, double &length) {
+    const d3 de = ld3(x, j) - ld3(x, i);
+    const double l2 = dot(de, de);
+    const double inv = rsqrt(l2);
+    length = l2 * inv;
+    return inv * de;
+}
+
+// kLazy: the float64 end state is not written; the increments accumulate in
+// a.inc until dpf_mixed_fold_history adds them.
+template <bool kLazy>
 __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
@@ -1208,18 +1241,13 @@ __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     load_y(a.y32, B.j, uj, wj);
     const BondIncrement<float> o = bond_increment<float>(B, ui, wi, uj, wj);
     const float dfn = B.kn * value(o.dn), dmt = B.kt * value(o.tw);
-    const double fn_end = a.h.fn[b] + (double)dfn, mt_end = a.h.mt[b] + (double)dmt;
-    a.fn_end[b] = fn_end;
-    a.mt_end[b] = mt_end;
-    // end normal in float64 from the end positions (geometry(end)); one
-    // reciprocal square root instead of a square root and a division (float64
-    // arithmetic is scarce on this part)
-    const d3 de = ld3(a.x_end, B.j) - ld3(a.x_end, B.i);
-    const double l2 = dot(de, de);
-    const double inv = rsqrt(l2);
-    const double le64 = l2 * inv;
-    const d3 ne = inv * de;
-    st3(a.normal_end, b, ne);
+    if (!kLazy) {
+        a.fn_end[b] = a.h.fn[b] + (double)dfn;
+        a.mt_end[b] = a.h.mt[b] + (double)dmt;
+    }
+    double le64;
+    const d3 ne = end_normal(a.x_end, B.i, B.j, le64);
+    if (!kLazy) st3(a.normal_end, b, ne);
     const V3<float> nx = lift3<float>(B.n0) + lift3<float>(B.dn0);
     float le;
     const V3<float> dnx_e = normal_change(B.L0, nx, uj - ui, le);
@@ -1230,12 +1258,25 @@ __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     const V3<float> dfs = o.dfs1 + t2.apply(fs1);
     const V3<float> dmb = o.dmb1 + t2.apply(mb1);
     const V3<float> doff = o.doff + t2.apply(off1);
-    const d3 fs_end = ld3(a.h.fs, b) + mk(dfs.x, dfs.y, dfs.z);
-    const d3 mb_end = ld3(a.h.mb, b) + mk(dmb.x, dmb.y, dmb.z);
-    const d3 off_end = ld3(a.h.offset, b) + mk(doff.x, doff.y, doff.z);
-    st3(a.fs_end, b, fs_end);
-    st3(a.mb_end, b, mb_end);
-    st3(a.offset_end, b, off_end);
+    if (kLazy) {
+        float4 *A = a.inc;
+        const int64_t m = a.m;
+        float4 h0 = A[b], h1 = A[m + b], h2 = A[2 * m + b];
+        float4 l0 = A[3 * m + b], l1 = A[4 * m + b], l2 = A[5 * m + b];
+        accumulate4(h0, l0, dfs.x, dfs.y, dfs.z, dfn);
+        accumulate4(h1, l1, dmb.x, dmb.y, dmb.z, dmt);
+        accumulate4(h2, l2, doff.x, doff.y, doff.z, 0.0f);
+        A[b] = h0;
+        A[m + b] = h1;
+        A[2 * m + b] = h2;
+        A[3 * m + b] = l0;
+        A[4 * m + b] = l1;
+        A[5 * m + b] = l2;
+    } else {
+        st3(a.fs_end, b, ld3(a.h.fs, b) + mk(dfs.x, dfs.y, dfs.z));
+        st3(a.mb_end, b, ld3(a.h.mb, b) + mk(dmb.x, dmb.y, dmb.z));
+        st3(a.offset_end, b, ld3(a.h.offset, b) + mk(doff.x, doff.y, doff.z));
+    }
     if (!a.dloads) return;
     // loads(x_end) - loads(x) of this bond from the small increments
     const V3<float> ne32 = nx + dnx_e;
@@ -1275,6 +1316,36 @@ __global__ void __launch_bounds__(kThreads) commit_sites(int64_t n, const int32_
 #pragma unroll
         for (int c = 0; c < 6; ++c) loads[6 * g + c] += (double)hi[c] + (double)lo[c];
     }
+}
+
+// history += the accumulated increments (out of place), normal = geometry(x),
+// increments zeroed.
+struct FoldArgs {
+    int64_t m;
+    const int64_t *edges;
+    dpf_history in;
+    float4 *inc;
+    double *normal, *offset, *fn, *fs, *mt, *mb;
+};
+
+__global__ void __launch_bounds__(kThreads) fold_history(FoldArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    double length;
+    st3(a.normal, b, end_normal(a.in.x, a.edges[2 * b], a.edges[2 * b + 1], length));
+    float4 *A = a.inc;
+    const int64_t m = a.m;
+    const float4 h0 = A[b], h1 = A[m + b], h2 = A[2 * m + b];
+    const float4 l0 = A[3 * m + b], l1 = A[4 * m + b], l2 = A[5 * m + b];
+    const auto pair = [](float hi, float lo) { return (double)hi + (double)lo; };
+    a.fn[b] = a.in.fn[b] + pair(h0.w, l0.w);
+    a.mt[b] = a.in.mt[b] + pair(h1.w, l1.w);
+    st3(a.fs, b, ld3(a.in.fs, b) + mk(pair(h0.x, l0.x), pair(h0.y, l0.y), pair(h0.z, l0.z)));
+    st3(a.mb, b, ld3(a.in.mb, b) + mk(pair(h1.x, l1.x), pair(h1.y, l1.y), pair(h1.z, l1.z)));
+    st3(a.offset, b, ld3(a.in.offset, b) + mk(pair(h2.x, l2.x), pair(h2.y, l2.y), pair(h2.z, l2.z)));
+    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < kIncArrays; ++k) A[k * m + b] = zero;
 }
 
 // Per-step constants from maintained loads: r0 and the rhs scale terms.
@@ -1637,12 +1708,48 @@ int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h,
     end_positions<<<blocks_for(3 * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, h->x, y, x_end);
     if (g->n_bonds) {
         CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), *h, y32, x_end, normal_end, offset_end,
-                     fs_end, mb_end, fn_end, mt_end, dloads};
-        commit_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+                     fs_end, mb_end, fn_end, mt_end, dloads, nullptr};
+        commit_bonds<false><<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
         if (dloads)
             commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(
                 g->n_sites, g->inc_ptr, g->inc_bond, dloads, loads);
     }
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int64_t dpf_history_increment_floats(int64_t n_bonds) { return n_bonds < 0 ? 0 : 4 * kIncArrays * n_bonds; }
+
+int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x, const double *y, const float *y32,
+                          double *x_end, float *increments, float *dloads, double *loads, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !x || !y || !y32 || !x_end || (g->n_bonds && (!increments || !dloads ||
+        !loads || ((uintptr_t)increments & 15u))))
+        return DPF_ERR_ARGUMENT;
+    cudaStream_t st = (cudaStream_t)stream;
+    end_positions<<<blocks_for(3 * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, x, y, x_end);
+    if (g->n_bonds) {
+        dpf_history h{};
+        h.x = x;
+        CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), h, y32, x_end, nullptr, nullptr, nullptr,
+                     nullptr, nullptr, nullptr, dloads, reinterpret_cast<float4 *>(increments)};
+        commit_bonds<true><<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
+        commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, g->inc_ptr,
+                                                                                       g->inc_bond, dloads, loads);
+    }
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_fold_history(const dpf_graph *g, const dpf_history *in, float *increments, double *normal,
+                           double *offset, double *fn, double *fs, double *mt, double *mb, void *stream) {
+    if (!mixed_graph_ok(g) || !in || !in->x || !g->edges)
+        return DPF_ERR_ARGUMENT;
+    if (!g->n_bonds) return DPF_OK;
+    if (!in->normal || !in->offset || !in->fn || !in->fs || !in->mt || !in->mb || !increments || !normal ||
+        !offset || !fn || !fs || !mt || !mb || ((uintptr_t)increments & 15u))
+        return DPF_ERR_ARGUMENT;
+    FoldArgs a{g->n_bonds, g->edges, *in, reinterpret_cast<float4 *>(increments), normal, offset, fn, fs, mt, mb};
+    fold_history<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

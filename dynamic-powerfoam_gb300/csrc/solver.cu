@@ -315,8 +315,9 @@ __global__ void __launch_bounds__(kThreads) accept_kernel(int64_t n, const doubl
                                                           double *rotation) {
     const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (s >= n) return;
+    const double two_over_dt = 2.0 / dt;  // one float64 division per site, not six
 #pragma unroll
-    for (int c = 0; c < 6; ++c) v[6 * s + c] = 2.0 * y[6 * s + c] / dt - v[6 * s + c];
+    for (int c = 0; c < 6; ++c) v[6 * s + c] = two_over_dt * y[6 * s + c] - v[6 * s + c];
     const d3 w = ld3(y + 6 * s + 3);
     // Rodrigues coefficients A = sin(a)/a and B = (1 - cos a)/a^2 of a = |w|.
     // Both are even in a: for a^2 < 1/4 (every step the rotation guard lets
@@ -502,12 +503,13 @@ __global__ void __launch_bounds__(kThreads) arnoldi32_dots(int64_t len, const fl
     }
 }
 
-// values_k = sum of part_in; h[k] (=|+=) values_k; w -= sum_k values_k basis_k
-// (the projection as a float32 pair, w rounded once); then the next pass's
-// partial dots (want_dots) or |w|^2 (part_out[blk]).
+// values_k = sum of part_in; h[k] (=|+=) values_k; w = in - sum_k values_k basis_k
+// (the projection as a float32 pair, w rounded once; in may be w); then the
+// next pass's partial dots (want_dots) or |w|^2 (part_out[blk]).
 __global__ void __launch_bounds__(kThreads) arnoldi32_update(int64_t len, const float *basis, int64_t ld, int count,
-                                                             float *w, const double *part_in, double *h,
-                                                             int accumulate, double *part_out, int want_dots) {
+                                                             const float *in, float *w, const double *part_in,
+                                                             double *h, int accumulate, double *part_out,
+                                                             int want_dots) {
     __shared__ double values[kMaxArnoldi];
     __shared__ float vhi[kMaxArnoldi], vlo[kMaxArnoldi];
     for (int k = 0; k < count; ++k) {
@@ -530,8 +532,8 @@ __global__ void __launch_bounds__(kThreads) arnoldi32_update(int64_t len, const 
             ff_add_product(ph, pl, vhi[k], b);
             pl = fmaf(vlo[k], b, pl);
         }
-        // w - (ph + pl): the difference w - ph exactly (TwoSum), then the rest
-        float d = w[e], err = 0.0f;
+        // in - (ph + pl): the difference in - ph exactly (TwoSum), then the rest
+        float d = in[e], err = 0.0f;
         ff_two_sum(d, err, -ph);
         const float wv = d + (err - pl);
         w[e] = wv;
@@ -667,18 +669,18 @@ int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w
     return DPF_OK;
 }
 
-int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, float *w, double *h, double *partials,
-                         void *stream) {
-    if (length <= 0 || !basis || !w || !h || !partials || j < 0 || j + 1 >= kMaxArnoldi || ld < length)
+int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, const float *v, float *w, double *h,
+                         double *partials, void *stream) {
+    if (length <= 0 || !basis || !v || !w || !h || !partials || j < 0 || j + 1 >= kMaxArnoldi || ld < length)
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     const int grid = reduce_grid(length);
     const int count = j + 1;
     double *pa = partials + kPartialsOffset;
     double *pb = pa + (int64_t)kMaxArnoldi * kMaxReduceBlocks;
-    arnoldi32_dots<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pa);
-    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pa, h, 0, pb, 1);
-    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, pb, h, 1, pa, 0);
+    arnoldi32_dots<<<grid, kThreads, 0, st>>>(length, basis, ld, count, v, pa);
+    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, v, w, pa, h, 0, pb, 1);
+    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, w, pb, h, 1, pa, 0);
     arnoldi32_normalize<<<grid, kThreads, 0, st>>>(length, basis, ld, j, w, pa, h);
     DPF_CHECK_LAUNCH();
     return DPF_OK;

@@ -726,11 +726,13 @@ class _Krylov32:
         f32 = torch.float32
         self.basis = torch.empty((width+1, length), dtype=f32, device=device)
         self.transformed = torch.empty((width, length), dtype=f32, device=device)
+        self.products = torch.empty((width, length), dtype=f32, device=device)   # J z_k
         self.w = torch.empty(length, dtype=f32, device=device)
         self.h = torch.zeros(72, dtype=F64, device=device)
         self.partials = torch.zeros(_lib.load().dpf_partials_doubles(), dtype=F64, device=device)
         self.scalars = torch.zeros(2, dtype=F64, device=device)
         self.x = torch.empty(length, dtype=F64, device=device)
+        self.product = torch.empty(length, dtype=F64, device=device)    # J x
         self.residual = torch.empty(length, dtype=F64, device=device)
 
 
@@ -1162,6 +1164,24 @@ class NewtonBonds(FiniteBonds):
 FastNewtonBonds = NewtonBonds
 
 
+_HISTORY = ('x', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')
+
+
+def _history_property(name):
+    key = '_h_' + name
+
+    def get(self):
+        if name != 'x' and self.__dict__.get('_pending_fold'):
+            self._fold_history()
+        return self.__dict__[key]
+
+    def put(self, value):
+        if self.__dict__.get('_pending_fold'):
+            self._fold_history()
+        self.__dict__[key] = value
+    return property(get, put, doc=f'Committed {name} (float64; pending step increments are folded in on access).')
+
+
 class AdaptiveIntervals:
     """Interval controller that keeps the subdivision depth which last worked
     (``experiments/bonded_dem_adaptive.py:4-23``): an interval is advanced as
@@ -1253,7 +1273,7 @@ class MixedNewtonBonds(NewtonBonds):
         """Descriptor of this solver's buffers for ``dpf_mixed_newton_step`` (cached
         while the tensors it points to stay the same)."""
         key = tuple(t.data_ptr() for t in (self.mass, self.fixed, self.radii, self.kn, self.ks, self.kb, self.kt,
-                                           self._ends)) + (self._end_variant,)
+                                           self._ends)) + (self._end_variant, self.lazy_history)
         cached = getattr(self, '_native_desc', None)
         if cached is not None and cached[0] == key:
             return cached[1]
@@ -1278,9 +1298,11 @@ class MixedNewtonBonds(NewtonBonds):
             units=ptr(self._units), units32=ptr(self._units32), ends=ptr(self._ends), site4=ptr(self._site4),
             p24=ptr(self._p24), end_workspace=ptr(self._tiled_workspace), end_partials=ptr(self._tiled_partials),
             barrier=ptr(self._barrier), inner=ptr(self._inner), basis=ptr(ws.basis),
-            transformed=ptr(ws.transformed), w32=ptr(ws.w), h=ptr(ws.h), krylov_width=ws.width,
+            transformed=ptr(ws.transformed), products=ptr(ws.products), w32=ptr(ws.w), h=ptr(ws.h),
+            krylov_width=ws.width,
             krylov_partials=ptr(self._native_partials), krylov_scalars=ptr(self._native_scalars),
-            vectors=ptr(self._native_vectors), host=ptr(self._native_host), end_variant=int(self._end_variant))
+            vectors=ptr(self._native_vectors), host=ptr(self._native_host), end_variant=int(self._end_variant),
+            history_increments=ptr(self._history_increments()) if self.lazy_history else None)
         # the descriptor holds only addresses: keep what they point into alive with it
         self._native_desc = (key, desc, ws)
         return desc
@@ -1295,17 +1317,19 @@ class MixedNewtonBonds(NewtonBonds):
         cls = type(self)
         if self.sweep == 'ends' and cls._newton_operator is MixedNewtonBonds._newton_operator and \
                 cls._newton_preconditioner is MixedNewtonBonds._newton_preconditioner:
-            return self._fgmres32(operator, rhs, tolerance, rhs_norm, dt)
+            return self._fgmres32(rhs, tolerance, rhs_norm, dt)
         return super()._krylov_solve(operator, rhs, precondition, tolerance, rhs_norm, dt)
 
-    def _fgmres32(self, operator, b, tolerance, norm, dt, restart=32, max_iterations=256):
+    def _fgmres32(self, b, tolerance, norm, dt, restart=32, max_iterations=256):
         """``fgmres`` with float32 Krylov vectors: the elastic PCG and the JVP read
         and write float32 rows (their values carry float32 precision either
         way), the Arnoldi sums are exact float32 pairs with float64 partials
         and h, and x, b and the true residual stay float64.  The Hessenberg
         recurrence, stopping rules and restarts are those of ``fgmres``
-        (``bonded_dem_newton.py:13-60``); the library's step driver runs the
-        same launches."""
+        (``bonded_dem_newton.py:13-60``), except that the true residual's J x
+        is sum_k c_k J z_k from the kept products (J is linear; the reference
+        applies the operator to x once more, a fourth JVP per two Arnoldi
+        steps).  The library's step driver runs the same launches."""
         lib, stream = self._lib, self._stream()
         n6 = 6*self.n_sites
         ws = self._krylov_workspace32()
@@ -1330,7 +1354,7 @@ class MixedNewtonBonds(NewtonBonds):
             first = False
             self._call('dpf_scale_to_float', n6, 1./g[0], start.data_ptr(), ws.basis[0].data_ptr(), stream)
             for j in range(width):
-                bj, tj = ws.basis[j], ws.transformed[j]
+                bj, tj, pj = ws.basis[j], ws.transformed[j], ws.products[j]
                 if self._packed != ('ends', dt):     # at the first PCG of a tangent, as the step driver does
                     self._pack_ends(dt)
                 if self._end_variant is None:
@@ -1345,10 +1369,10 @@ class MixedNewtonBonds(NewtonBonds):
                 self._timed('jvp', lambda: self._call(
                     'dpf_mixed_jacobian_vector_f32', ctypes.byref(self._graph), self._bond_data.data_ptr(),
                     self._y32.data_ptr(), tj.data_ptr(), self._mass32.data_ptr(), self.fixed.data_ptr(), dt,
-                    self._units32.data_ptr(), self._p32.data_ptr(), ws.w.data_ptr(), self._d32.data_ptr(),
+                    self._units32.data_ptr(), self._p32.data_ptr(), pj.data_ptr(), self._d32.data_ptr(),
                     self._wrench32.data_ptr(), stream))
-                self._call('dpf_arnoldi_cgs2_f32', n6, ws.basis.data_ptr(), n6, j, ws.w.data_ptr(), ws.h.data_ptr(),
-                           ws.partials.data_ptr(), stream)
+                self._call('dpf_arnoldi_cgs2_f32', n6, ws.basis.data_ptr(), n6, j, pj.data_ptr(), ws.w.data_ptr(),
+                           ws.h.data_ptr(), ws.partials.data_ptr(), stream)
                 column = ws.h[:j+2].cpu().numpy()
                 h[:j+1, j] = column[:j+1]
                 h[j+1, j] = column[j+1]
@@ -1364,9 +1388,12 @@ class MixedNewtonBonds(NewtonBonds):
                 iterations += 1
                 if abs(g[j+1]) <= tolerance*norm or breakdown or j+1 == width:
                     coefficients = _back_substitute(h, g, j+1)
-                    self._call('dpf_combine_rows_f32', n6, ws.transformed.data_ptr(), n6, j+1,
-                               coefficients.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), x.data_ptr(), stream)
-                    ax = operator(x.view(-1, 6)).reshape(-1)
+                    c = coefficients.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+                    self._call('dpf_combine_rows_f32', n6, ws.transformed.data_ptr(), n6, j+1, c, x.data_ptr(),
+                               stream)
+                    ax = ws.product
+                    ax.zero_()
+                    self._call('dpf_combine_rows_f32', n6, ws.products.data_ptr(), n6, j+1, c, ax.data_ptr(), stream)
                     self._call('dpf_axpby', n6, 1., b.data_ptr(), -1., ax.data_ptr(), res.data_ptr(), stream)
                     relative = norm_of(res)/norm
                     if relative <= 1.05*tolerance:
@@ -1390,11 +1417,16 @@ class MixedNewtonBonds(NewtonBonds):
                        self._since_refresh < self.refresh_interval)
         if refresh:
             self._since_refresh = 0
-        history = self._history_struct()
+        # a float64 setup reads the whole (folded) history; the lazy commit only x
+        history = self._history_struct() if (refresh or not self.lazy_history) else self._stored_history()
         desc = self._native_buffers()
         m, n = self.n_bonds, self.n_sites
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
-        state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
+        if self.lazy_history:
+            state = dict(x=e(n, 3))
+            state.update({name: state['x'][:0] for name in ('normal', 'offset', 'fn', 'fs', 'mt', 'mb')})
+        else:
+            state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
         timing = self.profile is not None
         args = _lib.NewtonStep(dt=dt, external=external.data_ptr(), v=self._v.data_ptr(),
                                rotation=rotation.data_ptr(), history=history,
@@ -1430,7 +1462,10 @@ class MixedNewtonBonds(NewtonBonds):
             raise SubdivideError('Subdivide: Newton line search failed')
         if outcome != _lib.NEWTON_CONVERGED:
             raise SubdivideError(f'Subdivide: Newton did not converge ({relative:g}, {local:g})')
-        self.commit(state)
+        if self.lazy_history:
+            self._commit_lazy(state['x'])
+        else:
+            self.commit(state)
         self.v, self.rotation = self._v, rotation
         self._token = self._state_token()
         self._since_refresh += 1
@@ -1543,9 +1578,55 @@ class MixedNewtonBonds(NewtonBonds):
             self._pack_tiles(self._tiles, dt)
 
     def _state_token(self):
-        # identity and in-place version of every committed tensor the records depend on
-        return tuple((t.data_ptr(), t._version) for t in (self.x, self.normal, self.offset, self.fn, self.fs,
-                                                           self.mt, self.mb, self.radii))
+        # identity and in-place version of every committed tensor the records
+        # depend on (the stored tensors: reading the history would fold it)
+        d = self.__dict__
+        return tuple((t.data_ptr(), t._version) for t in [d['_h_' + name] for name in _HISTORY] + [self.radii])
+
+    # ---- lazily folded float64 history -------------------------------------
+    # The accepted step adds float32 increments of fn, mt, fs, mb and offset to
+    # per-bond float32 pairs (exact sums) instead of rewriting the float64
+    # history; reading a history attribute (or a float64 setup, every
+    # refresh_interval steps) first folds them in with one float64 rounding,
+    # into new tensors, with normal = geometry(x) as the eager commit forms it.
+    # Between folds nothing float64 is written per bond.
+    lazy_history = True
+
+    def _history_increments(self):
+        inc = getattr(self, '_history_inc', None)
+        if inc is None or inc.numel() != max(4, self._lib.dpf_history_increment_floats(self.n_bonds)):
+            inc = self._history_inc = torch.zeros(max(4, self._lib.dpf_history_increment_floats(self.n_bonds)),
+                                                  dtype=torch.float32, device=self.device)
+        return inc
+
+    def _stored_history(self):
+        """History struct of the stored tensors (no fold: only x is read by the lazy commit)."""
+        d = self.__dict__
+        return _lib.History(*(d['_h_' + name].data_ptr() if name != 'radii' else self.radii.data_ptr()
+                              for name in ('x', 'radii', 'normal', 'offset', 'fn', 'fs', 'mt', 'mb')))
+
+    def _fold_history(self):
+        d = self.__dict__
+        d['_pending_fold'] = False
+        valid = self._token is not None and self._token == self._state_token()
+        for name in _HISTORY:
+            t = d['_h_' + name]
+            if not (t.is_contiguous() and t.dtype == F64):
+                d['_h_' + name] = t.to(F64).contiguous()
+        out = {name: torch.empty_like(d['_h_' + name]) for name in _HISTORY if name != 'x'}
+        self._call('dpf_mixed_fold_history', ctypes.byref(self._graph), ctypes.byref(self._stored_history()),
+                   self._history_increments().data_ptr(), out['normal'].data_ptr(), out['offset'].data_ptr(),
+                   out['fn'].data_ptr(), out['fs'].data_ptr(), out['mt'].data_ptr(), out['mb'].data_ptr(),
+                   self._stream())
+        for name, t in out.items():
+            d['_h_' + name] = t
+        if valid:                  # the records describe the folded state as well
+            self._token = self._state_token()
+
+    def _commit_lazy(self, x_end):
+        """Adopt the end positions of a lazily committed step."""
+        self.__dict__['_h_x'] = x_end
+        self.__dict__['_pending_fold'] = self.n_bonds > 0
 
     def _to_y32(self, y):
         self._call('dpf_to_float', 6*self.n_sites, y.data_ptr(), self._y32.data_ptr(), self._stream())
@@ -1553,7 +1634,6 @@ class MixedNewtonBonds(NewtonBonds):
     def _step_begin(self, dt, external):
         self._cached = None
         self._status.zero_()
-        history = self._history_struct()
         if getattr(self, '_begin_scales', None) is None:
             self._begin_scales = torch.zeros(2, dtype=F64, device=self.device)
         scales = self._begin_scales
@@ -1565,6 +1645,7 @@ class MixedNewtonBonds(NewtonBonds):
                 self._partials.data_ptr(), self._stream()))
         else:
             self._since_refresh = 0
+            history = self._history_struct()     # folds pending increments
             self._timed('setup', lambda: self._call(
                 'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                 ctypes.byref(history), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
@@ -1662,19 +1743,34 @@ class MixedNewtonBonds(NewtonBonds):
     def _accept(self, y, dt):
         m, n = self.n_bonds, self.n_sites
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
-        state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
         self._to_y32(y)
-        history = self._history_struct()
-        self._timed('commit', lambda: self._call(
-            'dpf_mixed_commit', ctypes.byref(self._graph), self._bond_data.data_ptr(), ctypes.byref(history),
-            y.data_ptr(), self._y32.data_ptr(), state['x'].data_ptr(), state['normal'].data_ptr(),
-            state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(), state['mt'].data_ptr(),
-            state['mb'].data_ptr(), self._wrench32.data_ptr(), self._loads.data_ptr(), self._stream()))
+        if self.lazy_history:
+            x_end = e(n, 3)
+            x = self.__dict__['_h_x']
+            self._timed('commit', lambda: self._call(
+                'dpf_mixed_commit_lazy', ctypes.byref(self._graph), self._bond_data.data_ptr(), x.data_ptr(),
+                y.data_ptr(), self._y32.data_ptr(), x_end.data_ptr(), self._history_increments().data_ptr(),
+                self._wrench32.data_ptr(), self._loads.data_ptr(), self._stream()))
+        else:
+            state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
+            history = self._history_struct()
+            self._timed('commit', lambda: self._call(
+                'dpf_mixed_commit', ctypes.byref(self._graph), self._bond_data.data_ptr(), ctypes.byref(history),
+                y.data_ptr(), self._y32.data_ptr(), state['x'].data_ptr(), state['normal'].data_ptr(),
+                state['offset'].data_ptr(), state['fn'].data_ptr(), state['fs'].data_ptr(), state['mt'].data_ptr(),
+                state['mb'].data_ptr(), self._wrench32.data_ptr(), self._loads.data_ptr(), self._stream()))
         rotation = self._vec(self.rotation).clone()
         self._call('dpf_accept_step', self.n_sites, y.data_ptr(), dt, self._v.data_ptr(), rotation.data_ptr(),
                    self._stream())
-        self.commit(state)
+        if self.lazy_history:
+            self._commit_lazy(x_end)
+        else:
+            self.commit(state)
         self.v, self.rotation = self._v, rotation
         self._cached = None
         self._token = self._state_token()
         self._since_refresh += 1
+
+
+for _name in _HISTORY:
+    setattr(MixedNewtonBonds, _name, _history_property(_name))

@@ -239,11 +239,12 @@ int64_t dpf_partials_doubles(void);
 int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w, double *h,
                      double *partials, void *stream);
 
-/* dpf_arnoldi_cgs2 on float32 vectors (basis rows and w): dot products and
- * the projection are summed exactly as float32 pairs (TwoProd by FMA and
- * TwoSum), block partials and h in float64, w and the new row rounded to
- * float32 once.  partials: dpf_partials_doubles(). */
-int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, float *w, double *h,
+/* dpf_arnoldi_cgs2 on float32 vectors: orthogonalises v (kept unchanged; v
+ * may be w) against basis rows 0..j into w and writes row j+1 = w/|w|.  Dot
+ * products and the projection are summed exactly as float32 pairs (TwoProd
+ * by FMA and TwoSum), block partials and h in float64, w and the new row
+ * rounded to float32 once.  partials: dpf_partials_doubles(). */
+int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, const float *v, float *w, double *h,
                          double *partials, void *stream);
 
 /* x += sum_{k<count} coefficients[k] * rows[k]  (coefficients on the host, count <= 64).
@@ -379,6 +380,23 @@ int64_t dpf_mixed_bond_floats(int64_t n_bonds);
 /* Float workspace of dpf_mixed_precondition for N sites and M bonds
  * (16-byte aligned; holds the padded work vectors and the bond wrench). */
 int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds);
+
+/* Lazy commit of the accepted increment y: x_end = x + y (N, 3), the bond
+ * records and loads advanced as dpf_mixed_commit does (dloads: 9 M floats),
+ * and the float32 increments of fn, mt, fs, mb and offset added exactly, as
+ * float32 pairs, to `increments` (dpf_history_increment_floats(M) floats,
+ * 16-byte aligned, zero after a fold) instead of writing the float64 end
+ * state.  dpf_mixed_fold_history adds them to a history later. */
+int64_t dpf_history_increment_floats(int64_t n_bonds);
+int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x, const double *y, const float *y32,
+                          double *x_end, float *increments, float *dloads, double *loads, void *stream);
+
+/* out = in + increments for offset, fn, fs, mt, mb (one float64 rounding per
+ * entry), normal = the unit vector from x_i to x_j of in->x (as
+ * dpf_mixed_commit forms normal_end), and the increments zeroed.  The
+ * outputs are distinct from the inputs. */
+int dpf_mixed_fold_history(const dpf_graph *g, const dpf_history *in, float *increments, double *normal,
+                           double *offset, double *fn, double *fs, double *mt, double *mb, void *stream);
 
 /* Per-step float64 setup: bond records from the committed state, r0 (N, 6),
  * optionally loads(x) (N, 6), and scales[0..1] = [|dt M v + dt^2/2 ext|,
@@ -765,7 +783,7 @@ int dpf_parallel_loads(const dpf_graph *g, const double *radii, const double *x,
 #define DPF_NEWTON_VECTORS 10      /* scratch vectors of 6 N doubles in `vectors` */
 #define DPF_NEWTON_HOST_DOUBLES 128 /* pinned host doubles in `host` */
 #define DPF_NEWTON_TRACE 32         /* residual trace entries kept */
-#define DPF_NEWTON_TIMERS 6         /* setup, residual, scaling, pcg, jvp, commit */
+#define DPF_NEWTON_TIMERS 11        /* setup, residual, scaling, pcg, jvp, commit, pack, krylov, norms, vector, accept */
 
 typedef struct dpf_mixed_newton {
     const dpf_graph *graph;        /* host struct */
@@ -791,6 +809,7 @@ typedef struct dpf_mixed_newton {
     unsigned *barrier;             /* 2 words */
     int *inner;                    /* CG iteration counter (added to) */
     float *basis, *transformed;    /* float32 Krylov vectors (width + 1, 6 N), (width, 6 N) */
+    float *products;               /* float32 J z_k of the transformed rows, (width, 6 N) */
     float *w32;                    /* 6 N floats */
     double *h;                     /* >= width + 2 */
     int krylov_width;              /* FGMRES restart length, <= 62 */
@@ -799,6 +818,10 @@ typedef struct dpf_mixed_newton {
     double *vectors;               /* DPF_NEWTON_VECTORS x 6 N, 16-byte aligned */
     double *host;                  /* pinned host memory, DPF_NEWTON_HOST_DOUBLES */
     int end_variant;               /* launch shape of the bond-end sweep */
+    float *history_increments;     /* dpf_history_increment_floats(M), or NULL: with it the accepted
+                                      step is committed lazily (dpf_mixed_commit_lazy: x_end only,
+                                      the history's increments accumulate for dpf_mixed_fold_history);
+                                      without it the float64 end state goes to the step's outputs */
 } dpf_mixed_newton;
 
 typedef struct dpf_newton_step {

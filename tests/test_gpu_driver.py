@@ -77,7 +77,8 @@ def test_driver_timing_fills_the_profile():
     native.profile = {}
     native.step(1e-3, native.tensor(load), tolerance=1e-6)
     profile, native.profile = native.profile, None
-    for key in ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit'):
+    for key in ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit', 'pack', 'krylov', 'norms', 'vector',
+                'accept'):
         assert key in profile and all(isinstance(v, float) and v > 0 for v in profile[key]), key
 
 
@@ -106,3 +107,33 @@ def test_driver_reports_the_same_failures():
     assert wp == wn
     assert_same_info(ip, inn)
     assert_same_state(python, native)
+
+
+def test_lazy_history_matches_eager_commit():
+    """Committing steps as exact float32-pair increments and folding them into
+    the float64 history on access (or at a refresh) agrees with writing the
+    float64 end state every step: bit for bit until the first float64 refresh
+    (the records advance the same way), to float64 rounding afterwards."""
+    import dpf_gb300
+    foam, lazy, eager = pair(m=10, seed=5, refresh=4)
+    eager.lazy_history = False
+    load = dpf_gb300.gravity_load(foam)*4.0
+    for step in range(9):      # the history is read only after the loop: 9 steps, refreshes at 4 and 8
+        lazy.step(2e-3, lazy.tensor(load), tolerance=1e-6)
+        eager.step(2e-3, eager.tensor(load), tolerance=1e-6)
+        if step < 4:
+            assert torch.equal(lazy.x, eager.x) and torch.equal(lazy.v, eager.v)
+        scale = float(torch.linalg.vector_norm(eager.x - torch.as_tensor(foam['points'], device=eager.x.device)))
+        assert float(torch.linalg.vector_norm(lazy.x - eager.x)) <= 1e-12*scale
+    assert lazy._pending_fold
+    for k in ('fn', 'fs', 'mt', 'mb', 'offset', 'normal'):
+        a, b = getattr(lazy, k), getattr(eager, k)
+        assert float(torch.linalg.vector_norm(a - b)) <= 1e-12*max(float(torch.linalg.vector_norm(b)), 1e-300), k
+    assert not lazy._pending_fold
+    # a fold leaves nothing pending and new tensors behind: an old reference keeps its values
+    fn_before = lazy.fn.clone()
+    held = lazy.fn
+    lazy.step(2e-3, lazy.tensor(load), tolerance=1e-6)
+    assert torch.equal(held, fn_before)
+    assert not torch.equal(lazy.fn, fn_before)
+    assert lazy.fn is lazy.fn
