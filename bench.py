@@ -586,13 +586,18 @@ def run_ours(args):
     rank = int(os.environ.get('RANK', '0'))
     local = int(os.environ.get('LOCAL_RANK', '0'))
 
-    # host triangulation of the served workloads starts first (largest first)
+    # host triangulation of the served workloads (largest first), in worker
+    # processes that start only after the main leg's timed regions: the step
+    # driver's host side must not share the cores with them while it is timed
     pool, large_jobs, served_jobs, plan = None, [], [], None
-    if world == 1 and (args.served > 0 or args.large_mix > 0) and args.precision == 'mixed':
+
+    def start_pool():
+        nonlocal pool, plan
+        if not (world == 1 and (args.served > 0 or args.large_mix > 0) and args.precision == 'mixed'):
+            return None
         from dpf_gb300 import serving
         cores = os.cpu_count() or 2
         pool = FoamPool(args.foam_workers or max(1, cores - 1))
-        t_pool = time.time()
         if args.large_mix > 0:
             large_jobs.append(pool.submit(args.large_mix, args.seed))
             for k in range(args.large_mix_count):
@@ -601,7 +606,8 @@ def run_ours(args):
             plan = serving.stream_plan(args.served, seed=11, sites=(1024, 131072), rate=args.served_rate)
             order = sorted(range(len(plan)), key=lambda k: -plan[k]['m'])
             futures = {k: pool.submit(plan[k]['m'], plan[k]['foam_seed']) for k in order}
-            served_jobs = [futures[k] for k in range(len(plan))]
+            served_jobs.extend(futures[k] for k in range(len(plan)))
+        return time.time()
 
     import dpf_gb300
     from dpf_gb300 import _lib
@@ -672,6 +678,7 @@ def run_ours(args):
     profile, s.profile = s.profile, None
 
     ms, e_ms, value, e2e = replica_rates(ms, e_ms, args.steps, world, device)
+    t_pool = start_pool()
 
     accuracy = None
     if args.accuracy and args.precision == 'mixed':
