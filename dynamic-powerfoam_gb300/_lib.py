@@ -193,7 +193,7 @@ SIGNATURES = {
     'dpf_end_precondition_f32': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, f64, i32, vp, vp, vp, vp, vp, vp, i32,
                                        vp]),
     'dpf_mixed_jacobian_vector_f32': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp]),
-    'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp, vp]),
+    'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_combine_rows_f32': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
     'dpf_scale_to_float': (i32, [i64, f64, vp, vp, vp]),
     'dpf_history_increment_floats': (i64, [i64]),
@@ -218,7 +218,7 @@ KERNELS = {
     'dpf_end_precondition': 1, 'dpf_bond_energy': 3, 'dpf_parallel_advance': 2, 'dpf_parallel_loads': 2,
     'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
-    'dpf_end_precondition_f32': 1, 'dpf_mixed_jacobian_vector_f32': 3, 'dpf_arnoldi_cgs2_f32': 4,
+    'dpf_end_precondition_f32': 1, 'dpf_mixed_jacobian_vector_f32': 3, 'dpf_arnoldi_cgs2_f32': 1,
     'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1, 'dpf_mixed_commit_lazy': 3, 'dpf_mixed_fold_history': 1,
 }
 LAUNCHES = {'count': 0}

@@ -235,8 +235,9 @@ struct Step {
                 if (rc) return rc;
                 rc = jvp32(tj, pj);
                 if (rc) return rc;
-                rc = call(kKrylov, 4, [&] {
-                    return dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, pj, s->w32, s->h, s->krylov_partials, st);
+                rc = call(kKrylov, 1, [&] {
+                    return dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, pj, s->w32, s->h, s->krylov_partials,
+                                                s->barrier, s->status, st);
                 });
                 if (rc) return rc;
                 double *column = host + 16;

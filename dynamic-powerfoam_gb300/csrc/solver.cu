@@ -490,81 +490,6 @@ __device__ __forceinline__ void ff_split(double v, float &hi, float &lo) {
     lo = (float)(v - (double)hi);
 }
 
-__global__ void __launch_bounds__(kThreads) arnoldi32_dots(int64_t len, const float *basis, int64_t ld, int count,
-                                                           const float *w, double *part) {
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int k = 0; k < count; ++k) {
-        const float *row = basis + k * ld;
-        float hi = 0.0f, lo = 0.0f;
-        for (int64_t e = tid; e < len; e += stride) ff_add_product(hi, lo, row[e], w[e]);
-        const double p = block_sum(ff_value(hi, lo));
-        if (threadIdx.x == 0) part[k * gridDim.x + blockIdx.x] = p;
-    }
-}
-
-// values_k = sum of part_in; h[k] (=|+=) values_k; w = in - sum_k values_k basis_k
-// (the projection as a float32 pair, w rounded once; in may be w); then the
-// next pass's partial dots (want_dots) or |w|^2 (part_out[blk]).
-__global__ void __launch_bounds__(kThreads) arnoldi32_update(int64_t len, const float *basis, int64_t ld, int count,
-                                                             const float *in, float *w, const double *part_in,
-                                                             double *h, int accumulate, double *part_out,
-                                                             int want_dots) {
-    __shared__ double values[kMaxArnoldi];
-    __shared__ float vhi[kMaxArnoldi], vlo[kMaxArnoldi];
-    for (int k = 0; k < count; ++k) {
-        const double v = block_sum_array(part_in + k * gridDim.x, gridDim.x);
-        if (threadIdx.x == 0) {
-            values[k] = v;
-            ff_split(v, vhi[k], vlo[k]);
-        }
-    }
-    __syncthreads();
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        for (int k = 0; k < count; ++k) h[k] = accumulate ? h[k] + values[k] : values[k];
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    float sq_hi = 0.0f, sq_lo = 0.0f;
-    for (int64_t e = tid; e < len; e += stride) {
-        float ph = 0.0f, pl = 0.0f;
-        for (int k = 0; k < count; ++k) {
-            const float b = basis[k * ld + e];
-            ff_add_product(ph, pl, vhi[k], b);
-            pl = fmaf(vlo[k], b, pl);
-        }
-        // in - (ph + pl): the difference in - ph exactly (TwoSum), then the rest
-        float d = in[e], err = 0.0f;
-        ff_two_sum(d, err, -ph);
-        const float wv = d + (err - pl);
-        w[e] = wv;
-        ff_add_product(sq_hi, sq_lo, wv, wv);
-    }
-    if (want_dots) {
-        for (int k = 0; k < count; ++k) {
-            const float *row = basis + k * ld;
-            float hi = 0.0f, lo = 0.0f;
-            for (int64_t e = tid; e < len; e += stride) ff_add_product(hi, lo, row[e], w[e]);
-            const double p = block_sum(ff_value(hi, lo));
-            if (threadIdx.x == 0) part_out[k * gridDim.x + blockIdx.x] = p;
-        }
-    } else {
-        const double sq = block_sum(ff_value(sq_hi, sq_lo));
-        if (threadIdx.x == 0) part_out[blockIdx.x] = sq;
-    }
-}
-
-__global__ void __launch_bounds__(kThreads) arnoldi32_normalize(int64_t len, float *basis, int64_t ld, int j,
-                                                                const float *w, const double *part, double *h) {
-    const double nrm = sqrt(block_sum_array(part, gridDim.x));
-    if (blockIdx.x == 0 && threadIdx.x == 0) h[j + 1] = nrm;
-    if (!(nrm >= 1e-14)) return;
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    float *row = basis + (int64_t)(j + 1) * ld;
-    const float inv = (float)(1.0 / nrm);
-    for (int64_t e = tid; e < len; e += stride) row[e] = w[e] * inv;
-}
-
 // x += sum_k c_k rows_k, the sum as a float32 pair, added to float64 x
 __global__ void __launch_bounds__(kThreads) combine32_kernel(int64_t len, const float *rows, int64_t ld, int count,
                                                              Coefficients coef, double *x) {
@@ -580,6 +505,111 @@ __global__ void __launch_bounds__(kThreads) combine32_kernel(int64_t len, const 
             lo = fmaf(clo[k], r, lo);
         }
         x[e] += ff_value(hi, lo);
+    }
+}
+
+// CGS2 of one Arnoldi step in one cooperative launch: the four passes of
+// arnoldi32_* with grid barriers between them, pairs of floats per access.
+// Every block sums the per-block partials of a phase in the same order, so
+// all take the same values.  Partials: part1 = count x grid, part2 = count x
+// grid, part3 = grid doubles.
+struct Arnoldi32Args {
+    int64_t half;        // length / 2 (the length is even: 6 per site)
+    const float2 *basis;  // rows of ld2 float2
+    float2 *next;         // row count (written)
+    int64_t ld2;
+    int count;
+    const float2 *v;
+    float2 *w;
+    double *h, *part1, *part2, *part3;
+    unsigned *barrier;
+    int *status;
+};
+
+// per-thread float32-pair dots of rows 0..count-1 with x, reduced per block
+// into part[k * gridDim.x + blockIdx.x]
+__device__ __forceinline__ void arnoldi_dots_pass(const Arnoldi32Args &a, const float2 *x, double *part) {
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int k0 = 0; k0 < a.count; k0 += 4) {
+        float hi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, lo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const int kn = a.count - k0 < 4 ? a.count - k0 : 4;
+        for (int64_t e = tid; e < a.half; e += stride) {
+            const float2 xv = x[e];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q < kn) {
+                    const float2 b = a.basis[(k0 + q) * a.ld2 + e];
+                    ff_add_product(hi[q], lo[q], b.x, xv.x);
+                    ff_add_product(hi[q], lo[q], b.y, xv.y);
+                }
+            }
+        }
+        for (int q = 0; q < kn; ++q) {
+            const double p = block_sum(ff_value(hi[q], lo[q]));
+            if (threadIdx.x == 0) part[(k0 + q) * gridDim.x + blockIdx.x] = p;
+        }
+    }
+}
+
+// w = in - sum_k values_k basis_k (values from the partials of the last pass),
+// the projection as float32 pairs; returns this thread's |w|^2 pair
+__device__ __forceinline__ void arnoldi_project(const Arnoldi32Args &a, const float2 *in, const double *part,
+                                               bool second, float &sq_hi, float &sq_lo) {
+    __shared__ float vhi[kMaxArnoldi], vlo[kMaxArnoldi];
+    for (int k = 0; k < a.count; ++k) {
+        const double v = block_sum_array(part + k * gridDim.x, gridDim.x);
+        if (threadIdx.x == 0) {
+            ff_split(v, vhi[k], vlo[k]);
+            if (blockIdx.x == 0) a.h[k] = second ? a.h[k] + v : v;
+        }
+    }
+    __syncthreads();
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = tid; e < a.half; e += stride) {
+        float2 ph = make_float2(0.0f, 0.0f), pl = make_float2(0.0f, 0.0f);
+        for (int k = 0; k < a.count; ++k) {
+            const float2 b = a.basis[k * a.ld2 + e];
+            ff_add_product(ph.x, pl.x, vhi[k], b.x);
+            ff_add_product(ph.y, pl.y, vhi[k], b.y);
+            pl.x = fmaf(vlo[k], b.x, pl.x);
+            pl.y = fmaf(vlo[k], b.y, pl.y);
+        }
+        const float2 iv = in[e];
+        float dx = iv.x, ex = 0.0f, dy = iv.y, ey = 0.0f;
+        ff_two_sum(dx, ex, -ph.x);
+        ff_two_sum(dy, ey, -ph.y);
+        const float2 wv = make_float2(dx + (ex - pl.x), dy + (ey - pl.y));
+        a.w[e] = wv;
+        ff_add_product(sq_hi, sq_lo, wv.x, wv.x);
+        ff_add_product(sq_hi, sq_lo, wv.y, wv.y);
+    }
+}
+
+__global__ void __launch_bounds__(kThreads) arnoldi32_fused_kernel(Arnoldi32Args a) {
+    arnoldi_dots_pass(a, a.v, a.part1);
+    if (!grid_barrier(a.barrier, a.status)) return;
+    float sh = 0.0f, sl = 0.0f;
+    arnoldi_project(a, a.v, a.part1, false, sh, sl);
+    // the second pass reads w only after every block has written it
+    if (!grid_barrier(a.barrier, a.status)) return;
+    arnoldi_dots_pass(a, a.w, a.part2);
+    if (!grid_barrier(a.barrier, a.status)) return;
+    sh = sl = 0.0f;
+    arnoldi_project(a, a.w, a.part2, true, sh, sl);
+    const double sq = block_sum(ff_value(sh, sl));
+    if (threadIdx.x == 0) a.part3[blockIdx.x] = sq;
+    if (!grid_barrier(a.barrier, a.status)) return;
+    const double nrm = sqrt(block_sum_array(a.part3, gridDim.x));
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.h[a.count] = nrm;
+    if (!(nrm >= 1e-14)) return;
+    const float inv = (float)(1.0 / nrm);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t e = tid; e < a.half; e += stride) {
+        const float2 wv = a.w[e];
+        a.next[e] = make_float2(wv.x * inv, wv.y * inv);
     }
 }
 
@@ -670,19 +700,48 @@ int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w
 }
 
 int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, const float *v, float *w, double *h,
-                         double *partials, void *stream) {
-    if (length <= 0 || !basis || !v || !w || !h || !partials || j < 0 || j + 1 >= kMaxArnoldi || ld < length)
+                         double *partials, unsigned *barrier, int *status, void *stream) {
+    if (length <= 0 || (length & 1) || (ld & 1) || !basis || !v || !w || !h || !partials || !barrier || !status ||
+        j < 0 || j + 1 >= kMaxArnoldi || ld < length || (((uintptr_t)basis | (uintptr_t)v | (uintptr_t)w) & 7u))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
-    const int grid = reduce_grid(length);
-    const int count = j + 1;
-    double *pa = partials + kPartialsOffset;
-    double *pb = pa + (int64_t)kMaxArnoldi * kMaxReduceBlocks;
-    arnoldi32_dots<<<grid, kThreads, 0, st>>>(length, basis, ld, count, v, pa);
-    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, v, w, pa, h, 0, pb, 1);
-    arnoldi32_update<<<grid, kThreads, 0, st>>>(length, basis, ld, count, w, w, pb, h, 1, pa, 0);
-    arnoldi32_normalize<<<grid, kThreads, 0, st>>>(length, basis, ld, j, w, pa, h);
-    DPF_CHECK_LAUNCH();
+    static int per_sm[64] = {0}, sms[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (per_sm[dev & 63] == 0) {
+        cudaDeviceGetAttribute(&sms[dev & 63], cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm[dev & 63], arnoldi32_fused_kernel, kThreads, 0);
+    }
+    int grid = sms[dev & 63] * (per_sm[dev & 63] < 4 ? per_sm[dev & 63] : 4);
+    const int64_t need = (length / 2 + kThreads - 1) / kThreads;
+    if (grid > need) grid = (int)need;
+    if (grid > kMaxReduceBlocks) grid = kMaxReduceBlocks;
+    if (grid < 1) return DPF_ERR_CUDA;
+    Arnoldi32Args a;
+    a.half = length / 2;
+    a.basis = reinterpret_cast<const float2 *>(basis);
+    a.ld2 = ld / 2;
+    a.next = reinterpret_cast<float2 *>(basis + (int64_t)(j + 1) * ld);
+    a.count = j + 1;
+    a.v = reinterpret_cast<const float2 *>(v);
+    a.w = reinterpret_cast<float2 *>(w);
+    a.h = h;
+    a.part1 = partials + kPartialsOffset;
+    a.part2 = a.part1 + (int64_t)kMaxArnoldi * kMaxReduceBlocks;
+    a.part3 = a.part2 + (int64_t)(kMaxArnoldi - 1) * kMaxReduceBlocks;
+    a.barrier = barrier;
+    a.status = status;
+    // a wait that timed out in an earlier launch leaves a partial arrival count
+    if (cudaMemsetAsync(barrier, 0, 2 * sizeof(unsigned), st) != cudaSuccess) {
+        cudaGetLastError();
+        return DPF_ERR_CUDA;
+    }
+    void *args[] = {&a};
+    if (cudaLaunchCooperativeKernel((const void *)arnoldi32_fused_kernel, grid, kThreads, args, 0, st) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return DPF_ERR_CUDA;
+    }
     return DPF_OK;
 }
 

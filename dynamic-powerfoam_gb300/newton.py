@@ -1372,7 +1372,8 @@ class MixedNewtonBonds(NewtonBonds):
                     self._units32.data_ptr(), self._p32.data_ptr(), pj.data_ptr(), self._d32.data_ptr(),
                     self._wrench32.data_ptr(), stream))
                 self._call('dpf_arnoldi_cgs2_f32', n6, ws.basis.data_ptr(), n6, j, pj.data_ptr(), ws.w.data_ptr(),
-                           ws.h.data_ptr(), ws.partials.data_ptr(), stream)
+                           ws.h.data_ptr(), ws.partials.data_ptr(), self._barrier.data_ptr(),
+                           self._status.data_ptr(), stream)
                 column = ws.h[:j+2].cpu().numpy()
                 h[:j+1, j] = column[:j+1]
                 h[j+1, j] = column[j+1]

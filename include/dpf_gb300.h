@@ -239,13 +239,16 @@ int64_t dpf_partials_doubles(void);
 int dpf_arnoldi_cgs2(int64_t length, double *basis, int64_t ld, int j, double *w, double *h,
                      double *partials, void *stream);
 
-/* dpf_arnoldi_cgs2 on float32 vectors: orthogonalises v (kept unchanged; v
- * may be w) against basis rows 0..j into w and writes row j+1 = w/|w|.  Dot
- * products and the projection are summed exactly as float32 pairs (TwoProd
- * by FMA and TwoSum), block partials and h in float64, w and the new row
- * rounded to float32 once.  partials: dpf_partials_doubles(). */
+/* dpf_arnoldi_cgs2 on float32 vectors in one cooperative launch (three grid
+ * barriers): orthogonalises v (kept unchanged) against basis rows 0..j into
+ * w and writes row j+1 = w/|w|.  Dot products and the projection are summed
+ * exactly as float32 pairs (TwoProd by FMA and TwoSum), block partials and h
+ * in float64, w and the new row rounded to float32 once.  length and ld are
+ * even, the vectors 8-byte aligned; partials: dpf_partials_doubles();
+ * barrier: 2 words (reset by the call); a barrier wait that runs out sets
+ * DPF_ERR_BARRIER_TIMEOUT in *status. */
 int dpf_arnoldi_cgs2_f32(int64_t length, float *basis, int64_t ld, int j, const float *v, float *w, double *h,
-                         double *partials, void *stream);
+                         double *partials, unsigned *barrier, int *status, void *stream);
 
 /* x += sum_{k<count} coefficients[k] * rows[k]  (coefficients on the host, count <= 64).
  * Replaces `x += transformed[:j+1].T @ coefficients` (experiments/bonded_dem_newton.py:54). */
