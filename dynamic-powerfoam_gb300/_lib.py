@@ -80,7 +80,7 @@ class NewtonStep(ctypes.Structure):
     _fields_ = ([('dt', f64), ('external', vp), ('v', vp), ('rotation', vp), ('history', History)] +
                 [(k, vp) for k in ('x_end', 'normal_end', 'offset_end', 'fn_end', 'fs_end', 'mt_end', 'mb_end')] +
                 [('tolerance', f64), ('pose_tolerance', f64), ('linear_tolerance', f64),
-                 ('max_iterations', i32), ('refresh', i32), ('timing', i32)])
+                 ('max_iterations', i32), ('refresh', i32), ('timing', i32), ('v_in', vp), ('rotation_in', vp)])
 
 
 NEWTON_VECTORS = 10

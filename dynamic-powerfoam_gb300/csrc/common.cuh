@@ -222,6 +222,17 @@ __device__ __forceinline__ double block_max_array(const double *p, int count, in
     return block_max(v);
 }
 
+// a / b formed by thread 0 and shared with the block: one float64 division
+// per block instead of one per thread (float64 division is slow on this
+// part).  Every thread of the block calls it, with the same a and b.
+__device__ __forceinline__ double block_divide(double a, double b) {
+    __shared__ double quotient;
+    __syncthreads();  // the previous quotient has been read
+    if (threadIdx.x == 0) quotient = a / b;
+    __syncthreads();
+    return quotient;
+}
+
 // "Last block finishes" protocol: every block has written its partial(s);
 // returns true in exactly one block, after all partials are visible.  The
 // counter lives in device memory, starts at zero and is reset by the last block.

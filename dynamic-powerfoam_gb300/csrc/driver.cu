@@ -335,6 +335,10 @@ struct Step {
         if (cudaMemsetAsync(s->inner, 0, sizeof(int), st) || cudaMemsetAsync(s->status, 0, sizeof(int), st) ||
             cudaMemsetAsync(y, 0, n6 * sizeof(double), st))
             return DPF_ERR_CUDA;
+        if ((a->v_in && cudaMemcpyAsync(a->v, a->v_in, n6 * sizeof(double), cudaMemcpyDeviceToDevice, st)) ||
+            (a->rotation_in &&
+             cudaMemcpyAsync(a->rotation, a->rotation_in, 9 * n * sizeof(double), cudaMemcpyDeviceToDevice, st)))
+            return DPF_ERR_CUDA;
         int rc;
         if (a->refresh) {
             const dpf_history &h = a->history;

@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(kThreads) block_pcg_kernel(BlockPcgArgs a) {
             }
         }
         if (!reduce(dad, 0.0, 0.0, a.barrier, a.status, tot)) return;
-        const double step = rz / tot[0];
+        const double step = block_divide(rz, tot[0]);
         // x += step d, r -= step ad, z = P r; (r, z), |r|^2, max |z / scale|
         double rz1 = 0.0, rr2 = 0.0, zmax = 0.0;
         for (int64_t s = tid; s < n; s += stride) {
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(kThreads) block_pcg_kernel(BlockPcgArgs a) {
                 break;
             }
         }
-        const double beta = rz1 / rz;
+        const double beta = block_divide(rz1, rz);
         for (int64_t e = tid; e < 6 * n; e += stride) a.d[e] = a.z[e] + beta * a.d[e];
         rz = rz1;
         if (!grid_barrier(a.barrier, a.status)) return;

@@ -1140,7 +1140,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
         p = block_sum((double)pf);
         if (threadIdx.x == 0) a.part_a[blockIdx.x] = p;
         if (!grid_barrier(a.barrier, a.status)) return;
-        const float alpha = (float)(rz / block_sum_array(a.part_a, gridDim.x));
+        const float alpha = (float)block_divide(rz, block_sum_array(a.part_a, gridDim.x));
         pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) {
             float xv[6], rv[6], dv[6], av[6], zz[6];
@@ -1165,7 +1165,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_kernel_f32(PcgArgs a) {
         if (!grid_barrier(a.barrier, a.status)) return;
         const double following = block_sum_array(a.part_b, gridDim.x);
         if (it % 5 == 0 && following <= a.tol2 * initial) break;
-        beta = (float)(following / rz);
+        beta = (float)block_divide(following, rz);
         rz = following;
     }
     for (int64_t s = tid; s < a.n; s += stride) {

@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs a) {
         p = block_sum(p);
         if (threadIdx.x == 0) a.part_a[blockIdx.x] = p;
         if (!grid_barrier(a.barrier, a.status)) return;
-        const double alpha = rz / block_sum_array(a.part_a, gridDim.x);
+        const double alpha = block_divide(rz, block_sum_array(a.part_a, gridDim.x));
         p = 0.0;
         for (int64_t s = tid; s < a.n; s += stride) {
             double rr[6], zz[6];
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(kThreads) pcg_kernel(PcgArgs a) {
         if (!grid_barrier(a.barrier, a.status)) return;
         const double following = block_sum_array(a.part_b, gridDim.x);
         if (it % 5 == 0 && following <= a.tol2 * initial) break;
-        const double beta = following / rz;
+        const double beta = block_divide(following, rz);
         for (int64_t e = tid; e < 6 * a.n; e += stride) a.d[e] = a.z[e] + beta * a.d[e];
         rz = following;
         if (!grid_barrier(a.barrier, a.status)) return;

@@ -898,14 +898,23 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
         if (!ok) return;
         if (!grid_barrier(a.barrier, a.status)) return;
         const double delta = block_sum_array(a.part_a, gridDim.x);
-        double beta, alpha;
-        if (it == 0) {
-            beta = 0.0;
-            alpha = gamma / delta;
-        } else {
-            beta = gamma / gamma_prev;
-            alpha = gamma / (delta - beta * gamma / alpha_prev);
+        // the recurrence's three float64 divisions once per block (thread 0),
+        // not once per thread: float64 division is slow on this part
+        __shared__ double shared_ab[2];
+        if (threadIdx.x == 0) {
+            double beta, alpha;
+            if (it == 0) {
+                beta = 0.0;
+                alpha = gamma / delta;
+            } else {
+                beta = gamma / gamma_prev;
+                alpha = gamma / (delta - beta * gamma / alpha_prev);
+            }
+            shared_ab[0] = alpha;
+            shared_ab[1] = beta;
         }
+        __syncthreads();
+        const double alpha = shared_ab[0], beta = shared_ab[1];
         const float fa = (float)alpha, fb = (float)beta;
         pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) pf += update_site(a, s, fa, fb);

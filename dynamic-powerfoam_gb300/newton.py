@@ -1404,18 +1404,19 @@ class MixedNewtonBonds(NewtonBonds):
 
     @torch.no_grad()
     def _native_step(self, dt, external, tolerance, max_iterations, pose_tolerance, linear_tolerance):
-        """``step`` through ``dpf_mixed_newton_step``: one library call per step."""
-        if not np.isfinite(dt) or dt <= 0:
+        """``step`` through ``dpf_mixed_newton_step``: one library call per step
+        (the host work around it is kept small: the GPU idles meanwhile)."""
+        if not (dt > 0 and np.isfinite(dt)):
             raise ValueError('Positive finite dt required')
         dt = float(dt)
         external = self._vec(external)
-        self._v = self._vec(self.v).clone()
-        rotation = self._vec(self.rotation).clone()
+        v0, r0 = self._vec(self.v), self._vec(self.rotation)
+        self._v, rotation = torch.empty_like(v0), torch.empty_like(r0)   # the driver copies the start values in
         if getattr(self, '_begin_scales', None) is None:
             self._begin_scales = torch.zeros(2, dtype=F64, device=self.device)
         self._cached = None
-        refresh = not (self._token is not None and self._token == self._state_token() and
-                       self._since_refresh < self.refresh_interval)
+        refresh = not (self._token is not None and self._since_refresh < self.refresh_interval and
+                       self._token == self._state_token())
         if refresh:
             self._since_refresh = 0
         # a float64 setup reads the whole (folded) history; the lazy commit only x
@@ -1425,19 +1426,24 @@ class MixedNewtonBonds(NewtonBonds):
         e = lambda *shape: torch.empty(shape, dtype=F64, device=self.device)
         if self.lazy_history:
             state = dict(x=e(n, 3))
-            state.update({name: state['x'][:0] for name in ('normal', 'offset', 'fn', 'fs', 'mt', 'mb')})
+            ends = (None,)*6
         else:
             state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))
+            ends = tuple(state[k].data_ptr() for k in ('normal', 'offset', 'fn', 'fs', 'mt', 'mb'))
         timing = self.profile is not None
-        args = _lib.NewtonStep(dt=dt, external=external.data_ptr(), v=self._v.data_ptr(),
-                               rotation=rotation.data_ptr(), history=history,
-                               x_end=state['x'].data_ptr(), normal_end=state['normal'].data_ptr(),
-                               offset_end=state['offset'].data_ptr(), fn_end=state['fn'].data_ptr(),
-                               fs_end=state['fs'].data_ptr(), mt_end=state['mt'].data_ptr(),
-                               mb_end=state['mb'].data_ptr(), tolerance=float(tolerance),
-                               pose_tolerance=float(pose_tolerance), linear_tolerance=float(linear_tolerance),
-                               max_iterations=int(max_iterations), refresh=int(refresh), timing=int(timing))
-        info = _lib.NewtonInfo()
+        args = self.__dict__.get('_native_args')
+        if args is None:
+            args = self._native_args = _lib.NewtonStep()
+            self._native_info = _lib.NewtonInfo()
+        args.dt, args.external, args.v, args.rotation, args.history = \
+            dt, external.data_ptr(), self._v.data_ptr(), rotation.data_ptr(), history
+        args.x_end = state['x'].data_ptr()
+        args.normal_end, args.offset_end, args.fn_end, args.fs_end, args.mt_end, args.mb_end = ends
+        args.tolerance, args.pose_tolerance, args.linear_tolerance = float(tolerance), float(pose_tolerance), \
+            float(linear_tolerance)
+        args.max_iterations, args.refresh, args.timing = int(max_iterations), int(refresh), int(timing)
+        args.v_in, args.rotation_in = v0.data_ptr(), r0.data_ptr()
+        info = self._native_info
         self._inner_host = 0
         self._call('dpf_mixed_newton_step', ctypes.byref(desc), ctypes.byref(args), ctypes.byref(info),
                    self._stream())

@@ -838,6 +838,8 @@ typedef struct dpf_newton_step {
     int max_iterations;            /* Newton iterations */
     int refresh;                   /* 1: float64 setup of the records; 0: begin from the maintained loads */
     int timing;                    /* 1: CUDA-event times of the hot launches into the info */
+    const double *v_in;            /* optional: the step's start velocity, copied into v first */
+    const double *rotation_in;     /* optional: the start rotations, copied into rotation first */
 } dpf_newton_step;
 
 /* outcome of a step */
