@@ -222,6 +222,84 @@ __device__ __forceinline__ double block_max_array(const double *p, int count, in
     return block_max(v);
 }
 
+// ---- sums as float32 pairs ---------------------------------------------------
+// A float32 pair (hi, lo) carries a sum to about 48 bits with float32
+// arithmetic only (TwoSum); float64 arithmetic is scarce on this part, and a
+// block reduction of doubles costs every thread a float64 add per shuffle
+// level.  TwoSum's error term is exact whatever the order of its operands,
+// so an xor-shuffle tree leaves the same pair in every lane.
+
+__device__ __forceinline__ void pair_add(float &hi, float &lo, float h, float l) {
+    const float t = hi + h;
+    const float hp = t - hi;
+    lo += ((hi - (t - hp)) + (h - hp)) + l;
+    hi = t;
+}
+
+__device__ __forceinline__ void warp_pair_sum(float &hi, float &lo) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float h = __shfl_xor_sync(0xffffffffu, hi, o), l = __shfl_xor_sync(0xffffffffu, lo, o);
+        pair_add(hi, lo, h, l);
+    }
+}
+
+// Block sum of per-thread pairs; every thread gets the total pair.
+__device__ __forceinline__ float2 block_pair_sum(float hi, float lo) {
+    __shared__ float2 buf[32];
+    __shared__ float2 total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    warp_pair_sum(hi, lo);
+    __syncthreads();
+    if (lane == 0) buf[warp] = make_float2(hi, lo);
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        float h = lane < nw ? buf[lane].x : 0.0f, l = lane < nw ? buf[lane].y : 0.0f;
+        warp_pair_sum(h, l);
+        if (lane == 0) total = make_float2(h, l);
+    }
+    __syncthreads();
+    return total;
+}
+
+__device__ __forceinline__ float block_max_float(float v) {
+    __shared__ float buf[32];
+    __shared__ float total;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __syncthreads();
+    if (lane == 0) buf[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        float m = lane < nw ? buf[lane] : -INFINITY;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) total = m;
+    }
+    __syncthreads();
+    return total;
+}
+
+// The block's partial of a per-thread float32 value, as a pair, into part[blockIdx.x].
+__device__ __forceinline__ void block_pair_partial(float v, float2 *part) {
+    const float2 t = block_pair_sum(v, 0.0f);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// Sum of `count` block partial pairs, in float64, the same in every block.
+__device__ __forceinline__ double pair_total(const float2 *part, int count) {
+    float hi = 0.0f, lo = 0.0f;
+    for (int k = threadIdx.x; k < count; k += blockDim.x) {
+        const float2 p = part[k];
+        pair_add(hi, lo, p.x, p.y);
+    }
+    const float2 t = block_pair_sum(hi, lo);
+    return (double)t.x + (double)t.y;
+}
+
 // a / b formed by thread 0 and shared with the block: one float64 division
 // per block instead of one per thread (float64 division is slow on this
 // part).  Every thread of the block calls it, with the same a and b.

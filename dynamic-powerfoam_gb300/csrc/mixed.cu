@@ -380,16 +380,22 @@ __device__ __forceinline__ void matvec6f(const float *P, const float x[6], float
     }
 }
 
-__device__ __forceinline__ void finish_norms(double sum_r, double max_s, double sum_s, double *partials, int slot,
-                                             double *norms, int *status) {
-    sum_r = block_sum(sum_r);
-    max_s = block_max(max_s);
-    sum_s = block_sum(sum_s);
+// Block partials of [|r|^2, max |s|, |s|^2] from per-thread float64 |r|^2,
+// float32 max |s| and the float32 pair |s|^2, reduced as float32 pairs
+// (float64 is scarce on this part: three float64 operations per thread
+// instead of a float64 add per shuffle level), then in the last block the
+// grid totals.
+__device__ __forceinline__ void finish_norms(double sum_r, float max_s, float s_hi, float s_lo, double *partials,
+                                             int slot, double *norms, int *status) {
+    const float r_hi = (float)sum_r, r_lo = (float)(sum_r - (double)r_hi);
+    const float2 r2 = block_pair_sum(r_hi, r_lo);
+    const float mx = block_max_float(max_s);
+    const float2 s2 = block_pair_sum(s_hi, s_lo);
     double *part = partials + kPartialsOffset;
     if (threadIdx.x == 0) {
-        part[3 * blockIdx.x] = sum_r;
-        part[3 * blockIdx.x + 1] = max_s;
-        part[3 * blockIdx.x + 2] = sum_s;
+        part[3 * blockIdx.x] = (double)r2.x + (double)r2.y;
+        part[3 * blockIdx.x + 1] = mx;
+        part[3 * blockIdx.x + 2] = (double)s2.x + (double)s2.y;
     }
     if (last_block(counter_slot(partials, slot))) {
         const double r2 = block_sum_array(part, gridDim.x, 3);
@@ -499,7 +505,7 @@ __global__ void __launch_bounds__(kThreads) residual_sites(ResidualSiteArgs a) {
     }
     if (flags) atomicOr(a.status, flags);
     if (!a.norms) return;
-    finish_norms(sum_r, max_s, (double)s_hi + (double)s_lo, a.partials, 6, a.norms, a.status);
+    finish_norms(sum_r, max_s, s_hi, s_lo, a.partials, 6, a.norms, a.status);
 }
 
 // One thread per site, 16-byte loads: the six residual entries (rounded to
@@ -552,7 +558,7 @@ __global__ void __launch_bounds__(kThreads) scale_sites_f32(int64_t n, const flo
         }
     }
     if (!norms) return;
-    finish_norms(sum_r, max_s, (double)s_hi + (double)s_lo, partials, 7, norms, nullptr);
+    finish_norms(sum_r, max_s, s_hi, s_lo, partials, 7, norms, nullptr);
 }
 
 // ---------------------------------------------------------------------------

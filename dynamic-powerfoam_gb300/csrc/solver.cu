@@ -508,11 +508,11 @@ __global__ void __launch_bounds__(kThreads) combine32_kernel(int64_t len, const 
     }
 }
 
-// CGS2 of one Arnoldi step in one cooperative launch: the four passes of
-// arnoldi32_* with grid barriers between them, pairs of floats per access.
-// Every block sums the per-block partials of a phase in the same order, so
-// all take the same values.  Partials: part1 = count x grid, part2 = count x
-// grid, part3 = grid doubles.
+// CGS2 of one Arnoldi step in one cooperative launch: dots, projection,
+// dots, projection and norm, normalisation, with grid barriers between them
+// and pairs of floats per access.  Block partials are float32 pairs; every
+// block sums them in the same order, so all take the same values.  Partials:
+// part1 = count x grid, part2 = count x grid, part3 = grid pairs.
 struct Arnoldi32Args {
     int64_t half;        // length / 2 (the length is even: 6 per site)
     const float2 *basis;  // rows of ld2 float2
@@ -546,8 +546,8 @@ __device__ __forceinline__ void arnoldi_dots_pass(const Arnoldi32Args &a, const 
             }
         }
         for (int q = 0; q < kn; ++q) {
-            const double p = block_sum(ff_value(hi[q], lo[q]));
-            if (threadIdx.x == 0) part[(k0 + q) * gridDim.x + blockIdx.x] = p;
+            const float2 p = block_pair_sum(hi[q], lo[q]);
+            if (threadIdx.x == 0) reinterpret_cast<float2 *>(part)[(k0 + q) * gridDim.x + blockIdx.x] = p;
         }
     }
 }
@@ -558,7 +558,7 @@ __device__ __forceinline__ void arnoldi_project(const Arnoldi32Args &a, const fl
                                                bool second, float &sq_hi, float &sq_lo) {
     __shared__ float vhi[kMaxArnoldi], vlo[kMaxArnoldi];
     for (int k = 0; k < a.count; ++k) {
-        const double v = block_sum_array(part + k * gridDim.x, gridDim.x);
+        const double v = pair_total(reinterpret_cast<const float2 *>(part) + k * gridDim.x, gridDim.x);
         if (threadIdx.x == 0) {
             ff_split(v, vhi[k], vlo[k]);
             if (blockIdx.x == 0) a.h[k] = second ? a.h[k] + v : v;
@@ -598,10 +598,10 @@ __global__ void __launch_bounds__(kThreads) arnoldi32_fused_kernel(Arnoldi32Args
     if (!grid_barrier(a.barrier, a.status)) return;
     sh = sl = 0.0f;
     arnoldi_project(a, a.w, a.part2, true, sh, sl);
-    const double sq = block_sum(ff_value(sh, sl));
-    if (threadIdx.x == 0) a.part3[blockIdx.x] = sq;
+    const float2 sq = block_pair_sum(sh, sl);
+    if (threadIdx.x == 0) reinterpret_cast<float2 *>(a.part3)[blockIdx.x] = sq;
     if (!grid_barrier(a.barrier, a.status)) return;
-    const double nrm = sqrt(block_sum_array(a.part3, gridDim.x));
+    const double nrm = sqrt(pair_total(reinterpret_cast<const float2 *>(a.part3), gridDim.x));
     if (blockIdx.x == 0 && threadIdx.x == 0) a.h[a.count] = nrm;
     if (!(nrm >= 1e-14)) return;
     const float inv = (float)(1.0 / nrm);

@@ -869,10 +869,11 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
 #pragma unroll
         for (int c = 0; c < 6; ++c) pf = fmaf(rr[c], zz[c], pf);
     }
-    double part = block_sum((double)pf);
-    if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
+    // CG scalars as float32-pair block partials (no float64 per thread)
+    float2 *part_a = reinterpret_cast<float2 *>(a.part_a), *part_b = reinterpret_cast<float2 *>(a.part_b);
+    block_pair_partial(pf, part_b);
     if (!grid_barrier(a.barrier, a.status)) return;
-    double gamma = block_sum_array(a.part_b, gridDim.x);
+    double gamma = pair_total(part_b, gridDim.x);
     const double initial = gamma;
     if (initial == 0.0) {
         for (int64_t e = tid; e < 6 * a.n; e += stride) {
@@ -893,11 +894,10 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
             ok = for_tiles(a.G, a.L, P, a.u, a.status, epi);
         else
             for_ends<L, false>(a.E, a.u, epi);
-        part = block_sum((double)epi.dot);
-        if (threadIdx.x == 0) a.part_a[blockIdx.x] = part;
+        block_pair_partial(epi.dot, part_a);
         if (!ok) return;
         if (!grid_barrier(a.barrier, a.status)) return;
-        const double delta = block_sum_array(a.part_a, gridDim.x);
+        const double delta = pair_total(part_a, gridDim.x);
         // the recurrence's three float64 divisions once per block (thread 0),
         // not once per thread: float64 division is slow on this part
         __shared__ double shared_ab[2];
@@ -918,10 +918,9 @@ __device__ __forceinline__ void pcg_body(PcgArgs &a, unsigned char *smem) {
         const float fa = (float)alpha, fb = (float)beta;
         pf = 0.0f;
         for (int64_t s = tid; s < a.n; s += stride) pf += update_site(a, s, fa, fb);
-        part = block_sum((double)pf);
-        if (threadIdx.x == 0) a.part_b[blockIdx.x] = part;
+        block_pair_partial(pf, part_b);
         if (!grid_barrier(a.barrier, a.status)) return;
-        const double following = block_sum_array(a.part_b, gridDim.x);
+        const double following = pair_total(part_b, gridDim.x);
         if (it % 5 == 0 && following <= a.tol2 * initial) break;
         gamma_prev = gamma;
         gamma = following;
