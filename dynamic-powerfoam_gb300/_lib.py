@@ -72,7 +72,7 @@ class MixedNewton(ctypes.Structure):
                                    'h')] +
                 [('krylov_width', i32)] +
                 [(k, vp) for k in ('krylov_partials', 'krylov_scalars', 'vectors', 'host')] +
-                [('end_variant', i32), ('history_increments', vp)])
+                [('end_variant', i32), ('history_corrections', vp)])
 
 
 class NewtonStep(ctypes.Structure):
@@ -196,9 +196,10 @@ SIGNATURES = {
     'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_combine_rows_f32': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
     'dpf_scale_to_float': (i32, [i64, f64, vp, vp, vp]),
-    'dpf_history_increment_floats': (i64, [i64]),
+    'dpf_history_correction_floats': (i64, [i64]),
+    'dpf_mixed_history_corrections': (i32, [P(Graph), P(History), vp, vp, vp]),
     'dpf_mixed_commit_lazy': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp]),
-    'dpf_mixed_fold_history': (i32, [P(Graph), P(History), vp, vp, vp, vp, vp, vp, vp, vp]),
+    'dpf_mixed_fold_history': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_newton_struct_sizes': (i32, [P(ctypes.c_int64)]),
 }
 
@@ -219,7 +220,7 @@ KERNELS = {
     'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
     'dpf_end_precondition_f32': 1, 'dpf_mixed_jacobian_vector_f32': 3, 'dpf_arnoldi_cgs2_f32': 1,
-    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1, 'dpf_mixed_commit_lazy': 3, 'dpf_mixed_fold_history': 1,
+    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1, 'dpf_mixed_commit_lazy': 3, 'dpf_mixed_fold_history': 1, 'dpf_mixed_history_corrections': 1,
 }
 LAUNCHES = {'count': 0}
 

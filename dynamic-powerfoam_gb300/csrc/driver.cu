@@ -304,8 +304,8 @@ struct Step {
         if (rc) return rc;
         const dpf_history &h = a->history;
         rc = call(kCommit, m ? 3 : 1, [&] {
-            if (s->history_increments)
-                return dpf_mixed_commit_lazy(s->graph, s->bond_data, h.x, y, s->y32, a->x_end, s->history_increments,
+            if (s->history_corrections)
+                return dpf_mixed_commit_lazy(s->graph, s->bond_data, h.x, y, s->y32, a->x_end, s->history_corrections,
                                              s->wrench32, s->loads, st);
             return dpf_mixed_commit(s->graph, s->bond_data, &h, y, s->y32, a->x_end, a->normal_end, a->offset_end,
                                     a->fn_end, a->fs_end, a->mt_end, a->mb_end, s->wrench32, s->loads, st);
@@ -347,6 +347,10 @@ struct Step {
                                        s->bond_data, s->r0, s->loads, s->scales, s->wrench64, s->partials, s->status,
                                        st);
             });
+            if (!rc && s->history_corrections)
+                rc = call(kSetup, m ? 1 : 0, [&] {
+                    return dpf_mixed_history_corrections(s->graph, &h, s->bond_data, s->history_corrections, st);
+                });
         } else {
             rc = call(kSetup, 1, [&] {
                 return dpf_mixed_begin(n, s->loads, s->mass, a->v, a->external, s->fixed, a->dt, s->r0, s->scales,

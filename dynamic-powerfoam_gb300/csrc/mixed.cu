@@ -851,17 +851,21 @@ __device__ __forceinline__ void add_block_sym(float D[21], V3<float> n, V3<float
         }
 }
 
-// One thread per site: the 6x6 inverse dominates, so lane groups would idle.
+// kScalingLanes lanes per site sum the incident bonds' blocks (more loads in
+// flight than one thread walking the site's ~15 incidences), an xor-shuffle
+// tree adds the lanes' sums, and lane 0 inverts.
+constexpr int kScalingLanes = 4;
+
 __global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
-    const int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) / kScalingLanes;
+    const int lane = threadIdx.x & (kScalingLanes - 1);
     const bool valid = s < a.n;
     float D[21];
 #pragma unroll
     for (int c = 0; c < 21; ++c) D[c] = 0.0f;
     if (valid) {
         const int e1 = a.ptr[s + 1];
-#pragma unroll 2
-        for (int e = a.ptr[s]; e < e1; ++e) {
+        for (int e = a.ptr[s] + lane; e < e1; e += kScalingLanes) {
             const int v = a.inc[e];
             const int64_t b = v >= 0 ? v : ~v;
             // (n, kn), this end's (lever, ks or kb), the other stiffness and kt:
@@ -874,7 +878,11 @@ __global__ void __launch_bounds__(128) scaling_sites_f32(ScalingArgs a) {
             add_block_sym(D, {t0.x, t0.y, t0.z}, {tr.x, tr.y, tr.z}, t0.w, ks, kb, kt);
         }
     }
-    if (!valid) return;
+#pragma unroll
+    for (int o = 1; o < kScalingLanes; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < 21; ++c) D[c] += __shfl_xor_sync(0xffffffffu, D[c], o);
+    if (!valid || lane != 0) return;
     const bool fx = a.fixed[s] != 0;
     float B[36];
 #pragma unroll
@@ -1195,21 +1203,23 @@ struct CommitArgs {
     const double *x_end;  // end positions x + y, formed first by end_positions
     double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
     float *dloads;  // optional: increment of the committed loads (9 floats per bond)
-    float4 *inc;    // lazy form: history increments since the last fold (6 float4 arrays of m)
+    float4 *corr;   // lazy form: corrections of the records' float32 state (3 float4 arrays of m)
 };
 
-// History increments since the last fold, per bond as float32 pairs: arrays
-// k = 0, 1, 2 hold the high parts (fs, fn), (mb, mt), (offset, 0) and
-// k = 3, 4, 5 the low parts.  hi + lo is the exact sum of the float32
-// increments (TwoSum), so a fold adds it to the float64 history with one
-// rounding instead of one per step.
-constexpr int kIncArrays = 6;
+// Lazy float64 history: the bond records carry fn, mt, fs, mb and offset in
+// float32 and advance them every step; per bond three float4 corrections
+// (fs, fn), (mb, mt), (offset, -) hold what float32 rounding dropped, so that
+// (double)record + (double)correction is the float64 history (to about 48
+// bits).  A float64 setup writes the records and their corrections from the
+// history; each lazy commit adds the exact rounding error of each record
+// update (TwoSum) to the correction; a fold forms the history from both.
+constexpr int kCorrArrays = 3;
 
-__device__ __forceinline__ void accumulate4(float4 &hi, float4 &lo, float x, float y, float z, float w) {
-    two_sum(hi.x, lo.x, x);
-    two_sum(hi.y, lo.y, y);
-    two_sum(hi.z, lo.z, z);
-    two_sum(hi.w, lo.w, w);
+// s = a + b rounded as the record update rounds it; returns the exact error
+// a + b - s (Knuth's TwoSum)
+__device__ __forceinline__ float sum_error(float a, float b, float s) {
+    const float bp = s - a;
+    return (a - (s - bp)) + (b - bp);
 }
 
 // x_end = x + u per site, before the bond pass reads it.
@@ -1235,8 +1245,8 @@ __device__ __forceinline__ d3 end_normal(const double *x, int64_t i, int64_t j, 
     return inv * de;
 }
 
-// kLazy: the float64 end state is not written; the increments accumulate in
-// a.inc until dpf_mixed_fold_history adds them.
+// kLazy: the float64 end state is not written; the records' rounding errors
+// go to the corrections a.corr (dpf_mixed_fold_history forms the history).
 template <bool kLazy>
 __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -1264,21 +1274,7 @@ __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     const V3<float> dfs = o.dfs1 + t2.apply(fs1);
     const V3<float> dmb = o.dmb1 + t2.apply(mb1);
     const V3<float> doff = o.doff + t2.apply(off1);
-    if (kLazy) {
-        float4 *A = a.inc;
-        const int64_t m = a.m;
-        float4 h0 = A[b], h1 = A[m + b], h2 = A[2 * m + b];
-        float4 l0 = A[3 * m + b], l1 = A[4 * m + b], l2 = A[5 * m + b];
-        accumulate4(h0, l0, dfs.x, dfs.y, dfs.z, dfn);
-        accumulate4(h1, l1, dmb.x, dmb.y, dmb.z, dmt);
-        accumulate4(h2, l2, doff.x, doff.y, doff.z, 0.0f);
-        A[b] = h0;
-        A[m + b] = h1;
-        A[2 * m + b] = h2;
-        A[3 * m + b] = l0;
-        A[4 * m + b] = l1;
-        A[5 * m + b] = l2;
-    } else {
+    if (!kLazy) {
         st3(a.fs_end, b, ld3(a.h.fs, b) + mk(dfs.x, dfs.y, dfs.z));
         st3(a.mb_end, b, ld3(a.h.mb, b) + mk(dmb.x, dmb.y, dmb.z));
         st3(a.offset_end, b, ld3(a.h.offset, b) + mk(doff.x, doff.y, doff.z));
@@ -1302,10 +1298,30 @@ __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     const V3<float> nef = {ne32f.x, ne32f.y, ne32f.z};
     const V3<float> ri_end = (0.5f * le32) * nef + B.rh * nef + (lift3<float>(B.off) + doff);
     const V3<float> fsr = lift3<float>(B.fs) + dfs, mbr = lift3<float>(B.mb) + dmb, offr = lift3<float>(B.off) + doff;
+    const float fnr = B.fn + dfn, mtr = B.mt + dmt;
+    if (kLazy) {
+        float4 *C = a.corr;
+        const int64_t m = a.m;
+        float4 c0 = C[b], c1 = C[m + b], c2 = C[2 * m + b];
+        c0.x += sum_error(B.fs.x, dfs.x, fsr.x);
+        c0.y += sum_error(B.fs.y, dfs.y, fsr.y);
+        c0.z += sum_error(B.fs.z, dfs.z, fsr.z);
+        c0.w += sum_error(B.fn, dfn, fnr);
+        c1.x += sum_error(B.mb.x, dmb.x, mbr.x);
+        c1.y += sum_error(B.mb.y, dmb.y, mbr.y);
+        c1.z += sum_error(B.mb.z, dmb.z, mbr.z);
+        c1.w += sum_error(B.mt, dmt, mtr);
+        c2.x += sum_error(B.off.x, doff.x, offr.x);
+        c2.y += sum_error(B.off.y, doff.y, offr.y);
+        c2.z += sum_error(B.off.z, doff.z, offr.z);
+        C[b] = c0;
+        C[m + b] = c1;
+        C[2 * m + b] = c2;
+    }
     a.bd.rec.r0[b] = make_float4(ne32f.x, ne32f.y, ne32f.z, le32);
     a.bd.rec.r1[b] = make_float4(0.0f, 0.0f, 0.0f, B.rh);
-    a.bd.rec.r2[b] = make_float4(ri_end.x, ri_end.y, ri_end.z, B.fn + dfn);
-    a.bd.rec.r3[b] = make_float4(fsr.x, fsr.y, fsr.z, B.mt + dmt);
+    a.bd.rec.r2[b] = make_float4(ri_end.x, ri_end.y, ri_end.z, fnr);
+    a.bd.rec.r3[b] = make_float4(fsr.x, fsr.y, fsr.z, mtr);
     a.bd.rec.r4[b] = make_float4(mbr.x, mbr.y, mbr.z, B.kn);
     a.bd.rec.r5[b] = make_float4(offr.x, offr.y, offr.z, B.ks);
 }
@@ -1324,34 +1340,50 @@ __global__ void __launch_bounds__(kThreads) commit_sites(int64_t n, const int32_
     }
 }
 
-// history += the accumulated increments (out of place), normal = geometry(x),
-// increments zeroed.
 struct FoldArgs {
     int64_t m;
     const int64_t *edges;
-    dpf_history in;
-    float4 *inc;
+    const double *x;
+    Records rec;
+    const float4 *corr;
     double *normal, *offset, *fn, *fs, *mt, *mb;
 };
 
+// history = (double)record + (double)correction, normal = geometry(x)
 __global__ void __launch_bounds__(kThreads) fold_history(FoldArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
     double length;
-    st3(a.normal, b, end_normal(a.in.x, a.edges[2 * b], a.edges[2 * b + 1], length));
-    float4 *A = a.inc;
+    st3(a.normal, b, end_normal(a.x, a.edges[2 * b], a.edges[2 * b + 1], length));
     const int64_t m = a.m;
-    const float4 h0 = A[b], h1 = A[m + b], h2 = A[2 * m + b];
-    const float4 l0 = A[3 * m + b], l1 = A[4 * m + b], l2 = A[5 * m + b];
-    const auto pair = [](float hi, float lo) { return (double)hi + (double)lo; };
-    a.fn[b] = a.in.fn[b] + pair(h0.w, l0.w);
-    a.mt[b] = a.in.mt[b] + pair(h1.w, l1.w);
-    st3(a.fs, b, ld3(a.in.fs, b) + mk(pair(h0.x, l0.x), pair(h0.y, l0.y), pair(h0.z, l0.z)));
-    st3(a.mb, b, ld3(a.in.mb, b) + mk(pair(h1.x, l1.x), pair(h1.y, l1.y), pair(h1.z, l1.z)));
-    st3(a.offset, b, ld3(a.in.offset, b) + mk(pair(h2.x, l2.x), pair(h2.y, l2.y), pair(h2.z, l2.z)));
-    const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll
-    for (int k = 0; k < kIncArrays; ++k) A[k * m + b] = zero;
+    const float4 c0 = a.corr[b], c1 = a.corr[m + b], c2 = a.corr[2 * m + b];
+    const float4 r2 = a.rec.r2[b], r3 = a.rec.r3[b], r4 = a.rec.r4[b], r5 = a.rec.r5[b];
+    const auto pair = [](float v, float c) { return (double)v + (double)c; };
+    a.fn[b] = pair(r2.w, c0.w);
+    a.mt[b] = pair(r3.w, c1.w);
+    st3(a.fs, b, mk(pair(r3.x, c0.x), pair(r3.y, c0.y), pair(r3.z, c0.z)));
+    st3(a.mb, b, mk(pair(r4.x, c1.x), pair(r4.y, c1.y), pair(r4.z, c1.z)));
+    st3(a.offset, b, mk(pair(r5.x, c2.x), pair(r5.y, c2.y), pair(r5.z, c2.z)));
+}
+
+// corrections = history - (double)record after a float64 setup wrote the records
+struct CorrArgs {
+    int64_t m;
+    dpf_history h;
+    Records rec;
+    float4 *corr;
+};
+
+__global__ void __launch_bounds__(kThreads) history_corrections(CorrArgs a) {
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= a.m) return;
+    const float4 r2 = a.rec.r2[b], r3 = a.rec.r3[b], r4 = a.rec.r4[b], r5 = a.rec.r5[b];
+    const auto gap = [](double h, float v) { return (float)(h - (double)v); };
+    const d3 fs = ld3(a.h.fs, b), mb = ld3(a.h.mb, b), off = ld3(a.h.offset, b);
+    const int64_t m = a.m;
+    a.corr[b] = make_float4(gap(fs.x, r3.x), gap(fs.y, r3.y), gap(fs.z, r3.z), gap(a.h.fn[b], r2.w));
+    a.corr[m + b] = make_float4(gap(mb.x, r4.x), gap(mb.y, r4.y), gap(mb.z, r4.z), gap(a.h.mt[b], r3.w));
+    a.corr[2 * m + b] = make_float4(gap(off.x, r5.x), gap(off.y, r5.y), gap(off.z, r5.z), 0.0f);
 }
 
 // Per-step constants from maintained loads: r0 and the rhs scale terms.
@@ -1549,7 +1581,7 @@ int dpf_mixed_scaling(const dpf_graph *g, float *bond_data, const float *mass32,
         return DPF_ERR_ARGUMENT;
     ScalingArgs a{g->n_sites, g->inc_ptr, g->inc_bond, split_bond_data(bond_data, g->n_bonds), mass32, radii, fixed,
                   (float)(0.25 * dt * dt), block, preconditioner, units32, units};
-    scaling_sites_f32<<<blocks_for(g->n_sites, 128), 128, 0, (cudaStream_t)stream>>>(a);
+    scaling_sites_f32<<<blocks_for(kScalingLanes * g->n_sites, 128), 128, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }
@@ -1724,12 +1756,25 @@ int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h,
     return DPF_OK;
 }
 
-int64_t dpf_history_increment_floats(int64_t n_bonds) { return n_bonds < 0 ? 0 : 4 * kIncArrays * n_bonds; }
+int64_t dpf_history_correction_floats(int64_t n_bonds) { return n_bonds < 0 ? 0 : 4 * kCorrArrays * n_bonds; }
+
+int dpf_mixed_history_corrections(const dpf_graph *g, const dpf_history *h, const float *bond_data,
+                                  float *corrections, void *stream) {
+    if (!mixed_graph_ok(g) || !h || !bond_data) return DPF_ERR_ARGUMENT;
+    if (!g->n_bonds) return DPF_OK;
+    if (!h->fn || !h->fs || !h->mt || !h->mb || !h->offset || !corrections || ((uintptr_t)corrections & 15u))
+        return DPF_ERR_ARGUMENT;
+    CorrArgs a{g->n_bonds, *h, split_bond_data(const_cast<float *>(bond_data), g->n_bonds).rec,
+               reinterpret_cast<float4 *>(corrections)};
+    history_corrections<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, (cudaStream_t)stream>>>(a);
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
 
 int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x, const double *y, const float *y32,
-                          double *x_end, float *increments, float *dloads, double *loads, void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !x || !y || !y32 || !x_end || (g->n_bonds && (!increments || !dloads ||
-        !loads || ((uintptr_t)increments & 15u))))
+                          double *x_end, float *corrections, float *dloads, double *loads, void *stream) {
+    if (!mixed_graph_ok(g) || !bond_data || !x || !y || !y32 || !x_end || (g->n_bonds && (!corrections || !dloads ||
+        !loads || ((uintptr_t)corrections & 15u))))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     end_positions<<<blocks_for(3 * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, x, y, x_end);
@@ -1737,7 +1782,7 @@ int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x,
         dpf_history h{};
         h.x = x;
         CommitArgs a{g->n_bonds, split_bond_data(bond_data, g->n_bonds), h, y32, x_end, nullptr, nullptr, nullptr,
-                     nullptr, nullptr, nullptr, dloads, reinterpret_cast<float4 *>(increments)};
+                     nullptr, nullptr, nullptr, dloads, reinterpret_cast<float4 *>(corrections)};
         commit_bonds<true><<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
         commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, g->inc_ptr,
                                                                                        g->inc_bond, dloads, loads);
@@ -1746,15 +1791,16 @@ int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x,
     return DPF_OK;
 }
 
-int dpf_mixed_fold_history(const dpf_graph *g, const dpf_history *in, float *increments, double *normal,
-                           double *offset, double *fn, double *fs, double *mt, double *mb, void *stream) {
-    if (!mixed_graph_ok(g) || !in || !in->x || !g->edges)
+int dpf_mixed_fold_history(const dpf_graph *g, const double *x, const float *bond_data, const float *corrections,
+                           double *normal, double *offset, double *fn, double *fs, double *mt, double *mb,
+                           void *stream) {
+    if (!mixed_graph_ok(g) || !x || !g->edges || !bond_data)
         return DPF_ERR_ARGUMENT;
     if (!g->n_bonds) return DPF_OK;
-    if (!in->normal || !in->offset || !in->fn || !in->fs || !in->mt || !in->mb || !increments || !normal ||
-        !offset || !fn || !fs || !mt || !mb || ((uintptr_t)increments & 15u))
+    if (!corrections || !normal || !offset || !fn || !fs || !mt || !mb || ((uintptr_t)corrections & 15u))
         return DPF_ERR_ARGUMENT;
-    FoldArgs a{g->n_bonds, g->edges, *in, reinterpret_cast<float4 *>(increments), normal, offset, fn, fs, mt, mb};
+    FoldArgs a{g->n_bonds, g->edges, x, split_bond_data(const_cast<float *>(bond_data), g->n_bonds).rec,
+               reinterpret_cast<const float4 *>(corrections), normal, offset, fn, fs, mt, mb};
     fold_history<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, (cudaStream_t)stream>>>(a);
     DPF_CHECK_LAUNCH();
     return DPF_OK;

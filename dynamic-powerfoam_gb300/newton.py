@@ -1302,7 +1302,7 @@ class MixedNewtonBonds(NewtonBonds):
             krylov_width=ws.width,
             krylov_partials=ptr(self._native_partials), krylov_scalars=ptr(self._native_scalars),
             vectors=ptr(self._native_vectors), host=ptr(self._native_host), end_variant=int(self._end_variant),
-            history_increments=ptr(self._history_increments()) if self.lazy_history else None)
+            history_corrections=ptr(self._history_corrections()) if self.lazy_history else None)
         # the descriptor holds only addresses: keep what they point into alive with it
         self._native_desc = (key, desc, ws)
         return desc
@@ -1591,20 +1591,22 @@ class MixedNewtonBonds(NewtonBonds):
         return tuple((t.data_ptr(), t._version) for t in [d['_h_' + name] for name in _HISTORY] + [self.radii])
 
     # ---- lazily folded float64 history -------------------------------------
-    # The accepted step adds float32 increments of fn, mt, fs, mb and offset to
-    # per-bond float32 pairs (exact sums) instead of rewriting the float64
-    # history; reading a history attribute (or a float64 setup, every
-    # refresh_interval steps) first folds them in with one float64 rounding,
-    # into new tensors, with normal = geometry(x) as the eager commit forms it.
-    # Between folds nothing float64 is written per bond.
+    # The bond records carry fn, mt, fs, mb and offset in float32 and every
+    # accepted step advances them; a per-bond float32 correction keeps what
+    # float32 rounding dropped (the exact TwoSum error of each update), so
+    # record + correction is the float64 history.  An accepted step therefore
+    # writes no float64 per bond; reading a history attribute (or a float64
+    # setup, every refresh_interval steps) first folds records and corrections
+    # into new float64 tensors, with normal = geometry(x) as the eager commit
+    # forms it.
     lazy_history = True
 
-    def _history_increments(self):
-        inc = getattr(self, '_history_inc', None)
-        if inc is None or inc.numel() != max(4, self._lib.dpf_history_increment_floats(self.n_bonds)):
-            inc = self._history_inc = torch.zeros(max(4, self._lib.dpf_history_increment_floats(self.n_bonds)),
-                                                  dtype=torch.float32, device=self.device)
-        return inc
+    def _history_corrections(self):
+        size = max(4, self._lib.dpf_history_correction_floats(self.n_bonds))
+        corr = getattr(self, '_history_corr', None)
+        if corr is None or corr.numel() != size:
+            corr = self._history_corr = torch.zeros(size, dtype=torch.float32, device=self.device)
+        return corr
 
     def _stored_history(self):
         """History struct of the stored tensors (no fold: only x is read by the lazy commit)."""
@@ -1621,10 +1623,10 @@ class MixedNewtonBonds(NewtonBonds):
             if not (t.is_contiguous() and t.dtype == F64):
                 d['_h_' + name] = t.to(F64).contiguous()
         out = {name: torch.empty_like(d['_h_' + name]) for name in _HISTORY if name != 'x'}
-        self._call('dpf_mixed_fold_history', ctypes.byref(self._graph), ctypes.byref(self._stored_history()),
-                   self._history_increments().data_ptr(), out['normal'].data_ptr(), out['offset'].data_ptr(),
-                   out['fn'].data_ptr(), out['fs'].data_ptr(), out['mt'].data_ptr(), out['mb'].data_ptr(),
-                   self._stream())
+        self._call('dpf_mixed_fold_history', ctypes.byref(self._graph), d['_h_x'].data_ptr(),
+                   self._bond_data.data_ptr(), self._history_corrections().data_ptr(), out['normal'].data_ptr(),
+                   out['offset'].data_ptr(), out['fn'].data_ptr(), out['fs'].data_ptr(), out['mt'].data_ptr(),
+                   out['mb'].data_ptr(), self._stream())
         for name, t in out.items():
             d['_h_' + name] = t
         if valid:                  # the records describe the folded state as well
@@ -1652,13 +1654,16 @@ class MixedNewtonBonds(NewtonBonds):
                 self._partials.data_ptr(), self._stream()))
         else:
             self._since_refresh = 0
-            history = self._history_struct()     # folds pending increments
+            history = self._history_struct()     # folds a lazily committed history first
             self._timed('setup', lambda: self._call(
                 'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                 ctypes.byref(history), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
                 self.fixed.data_ptr(), dt, self._bond_data.data_ptr(), self._r0.data_ptr(), self._loads.data_ptr(),
                 scales.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(),
                 self._status.data_ptr(), self._stream()))
+            if self.lazy_history:
+                self._call('dpf_mixed_history_corrections', ctypes.byref(self._graph), ctypes.byref(history),
+                           self._bond_data.data_ptr(), self._history_corrections().data_ptr(), self._stream())
         # the scales reach the host with the first residual's fetch (one sync
         # less per step); a setup guard is raised by that residual's own trial
         self._deferred_scale = scales
@@ -1756,7 +1761,7 @@ class MixedNewtonBonds(NewtonBonds):
             x = self.__dict__['_h_x']
             self._timed('commit', lambda: self._call(
                 'dpf_mixed_commit_lazy', ctypes.byref(self._graph), self._bond_data.data_ptr(), x.data_ptr(),
-                y.data_ptr(), self._y32.data_ptr(), x_end.data_ptr(), self._history_increments().data_ptr(),
+                y.data_ptr(), self._y32.data_ptr(), x_end.data_ptr(), self._history_corrections().data_ptr(),
                 self._wrench32.data_ptr(), self._loads.data_ptr(), self._stream()))
         else:
             state = dict(x=e(n, 3), normal=e(m, 3), offset=e(m, 3), fn=e(m), fs=e(m, 3), mt=e(m), mb=e(m, 3))

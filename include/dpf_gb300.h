@@ -384,22 +384,28 @@ int64_t dpf_mixed_bond_floats(int64_t n_bonds);
  * (16-byte aligned; holds the padded work vectors and the bond wrench). */
 int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds);
 
-/* Lazy commit of the accepted increment y: x_end = x + y (N, 3), the bond
- * records and loads advanced as dpf_mixed_commit does (dloads: 9 M floats),
- * and the float32 increments of fn, mt, fs, mb and offset added exactly, as
- * float32 pairs, to `increments` (dpf_history_increment_floats(M) floats,
- * 16-byte aligned, zero after a fold) instead of writing the float64 end
- * state.  dpf_mixed_fold_history adds them to a history later. */
-int64_t dpf_history_increment_floats(int64_t n_bonds);
+/* Lazy float64 history.  The bond records (bond_data) carry fn, mt, fs, mb
+ * and offset in float32 and every commit advances them; `corrections`
+ * (dpf_history_correction_floats(M) floats, 16-byte aligned) hold per bond
+ * what float32 rounding dropped, so that record + correction is the float64
+ * history to about 48 bits.
+ * dpf_mixed_history_corrections: corrections = h - record, right after a
+ * float64 dpf_mixed_setup wrote the records from h.
+ * dpf_mixed_commit_lazy: the accepted increment y as dpf_mixed_commit
+ * applies it (x_end = x + y (N, 3), records and loads advanced; dloads: 9 M
+ * floats) with the exact rounding error of each record update added to the
+ * corrections, and no float64 end state written.
+ * dpf_mixed_fold_history: the float64 history from the records and
+ * corrections, normal = the unit vector from x_i to x_j (as dpf_mixed_commit
+ * forms normal_end). */
+int64_t dpf_history_correction_floats(int64_t n_bonds);
+int dpf_mixed_history_corrections(const dpf_graph *g, const dpf_history *h, const float *bond_data,
+                                  float *corrections, void *stream);
 int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x, const double *y, const float *y32,
-                          double *x_end, float *increments, float *dloads, double *loads, void *stream);
-
-/* out = in + increments for offset, fn, fs, mt, mb (one float64 rounding per
- * entry), normal = the unit vector from x_i to x_j of in->x (as
- * dpf_mixed_commit forms normal_end), and the increments zeroed.  The
- * outputs are distinct from the inputs. */
-int dpf_mixed_fold_history(const dpf_graph *g, const dpf_history *in, float *increments, double *normal,
-                           double *offset, double *fn, double *fs, double *mt, double *mb, void *stream);
+                          double *x_end, float *corrections, float *dloads, double *loads, void *stream);
+int dpf_mixed_fold_history(const dpf_graph *g, const double *x, const float *bond_data, const float *corrections,
+                           double *normal, double *offset, double *fn, double *fs, double *mt, double *mb,
+                           void *stream);
 
 /* Per-step float64 setup: bond records from the committed state, r0 (N, 6),
  * optionally loads(x) (N, 6), and scales[0..1] = [|dt M v + dt^2/2 ext|,
@@ -821,10 +827,10 @@ typedef struct dpf_mixed_newton {
     double *vectors;               /* DPF_NEWTON_VECTORS x 6 N, 16-byte aligned */
     double *host;                  /* pinned host memory, DPF_NEWTON_HOST_DOUBLES */
     int end_variant;               /* launch shape of the bond-end sweep */
-    float *history_increments;     /* dpf_history_increment_floats(M), or NULL: with it the accepted
-                                      step is committed lazily (dpf_mixed_commit_lazy: x_end only,
-                                      the history's increments accumulate for dpf_mixed_fold_history);
-                                      without it the float64 end state goes to the step's outputs */
+    float *history_corrections;    /* dpf_history_correction_floats(M), or NULL: with it the accepted
+                                      step is committed lazily (dpf_mixed_commit_lazy: x_end only;
+                                      a float64 refresh also writes the corrections); without it the
+                                      float64 end state goes to the step's outputs */
 } dpf_mixed_newton;
 
 typedef struct dpf_newton_step {
