@@ -80,7 +80,8 @@ class NewtonStep(ctypes.Structure):
     _fields_ = ([('dt', f64), ('external', vp), ('v', vp), ('rotation', vp), ('history', History)] +
                 [(k, vp) for k in ('x_end', 'normal_end', 'offset_end', 'fn_end', 'fs_end', 'mt_end', 'mb_end')] +
                 [('tolerance', f64), ('pose_tolerance', f64), ('linear_tolerance', f64),
-                 ('max_iterations', i32), ('refresh', i32), ('timing', i32), ('v_in', vp), ('rotation_in', vp)])
+                 ('max_iterations', i32), ('refresh', i32), ('timing', i32), ('v_in', vp), ('rotation_in', vp),
+                 ('committed_start', i32)])
 
 
 NEWTON_VECTORS = 10
@@ -196,6 +197,7 @@ SIGNATURES = {
     'dpf_arnoldi_cgs2_f32': (i32, [i64, vp, i64, i32, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_combine_rows_f32': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
     'dpf_scale_to_float': (i32, [i64, f64, vp, vp, vp]),
+    'dpf_mixed_initial_residual': (i32, [i64, vp, vp, vp, vp, vp]),
     'dpf_history_correction_floats': (i64, [i64]),
     'dpf_mixed_history_corrections': (i32, [P(Graph), P(History), vp, vp, vp]),
     'dpf_mixed_commit_lazy': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp]),
@@ -220,7 +222,7 @@ KERNELS = {
     'dpf_energy_tangent': 1, 'dpf_operator_apply': 2, 'dpf_block_inverse': 1, 'dpf_block_pcg': 1, 'dpf_linear_midpoint_rhs': 1, 'dpf_linear_midpoint_advance': 1,
     'dpf_linear_sums': 1, 'dpf_anderson_gram': 1, 'dpf_anderson_mix': 1, 'dpf_barrier_selftest': 1,
     'dpf_end_precondition_f32': 1, 'dpf_mixed_jacobian_vector_f32': 3, 'dpf_arnoldi_cgs2_f32': 1,
-    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1, 'dpf_mixed_commit_lazy': 3, 'dpf_mixed_fold_history': 1, 'dpf_mixed_history_corrections': 1,
+    'dpf_combine_rows_f32': 1, 'dpf_scale_to_float': 1, 'dpf_mixed_commit_lazy': 3, 'dpf_mixed_fold_history': 1, 'dpf_mixed_history_corrections': 1, 'dpf_mixed_initial_residual': 1,
 }
 LAUNCHES = {'count': 0}
 

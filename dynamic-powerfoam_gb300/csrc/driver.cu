@@ -361,7 +361,11 @@ struct Step {
         bool cached = false;
         const double dt = a->dt;
         for (int iteration = 0; iteration <= a->max_iterations; ++iteration) {
-            if (!cached) {
+            if (iteration == 0 && a->committed_start && !a->refresh) {
+                if (cudaMemsetAsync(s->status, 0, sizeof(int), st)) return DPF_ERR_CUDA;
+                rc = call(kResidual, 1, [&] { return dpf_mixed_initial_residual(n, s->r0, s->fixed, s->y32, r, st); });
+                if (rc) return rc;
+            } else if (!cached) {
                 rc = residual(y, r, false);
                 if (rc) return rc;
             }

@@ -1321,6 +1321,12 @@ __global__ void __launch_bounds__(kThreads, 3) commit_bonds(CommitArgs a) {
     a.bd.rec.r0[b] = make_float4(ne32f.x, ne32f.y, ne32f.z, le32);
     a.bd.rec.r1[b] = make_float4(0.0f, 0.0f, 0.0f, B.rh);
     a.bd.rec.r2[b] = make_float4(ri_end.x, ri_end.y, ri_end.z, fnr);
+    // the next step's tangent at y = 0 (dn0 = 0: n = n0, ri = ri_x, rj = ri_x - L0 n0,
+    // what the residual pass forms there), so that its first residual needs no bond pass
+    const V3<float> rj_end = ri_end - le32 * nef;
+    a.bd.t0[b] = make_float4(nef.x, nef.y, nef.z, B.kn);
+    a.bd.t1[b] = make_float4(ri_end.x, ri_end.y, ri_end.z, B.ks);
+    a.bd.t2[b] = make_float4(rj_end.x, rj_end.y, rj_end.z, B.kb);
     a.bd.rec.r3[b] = make_float4(fsr.x, fsr.y, fsr.z, mtr);
     a.bd.rec.r4[b] = make_float4(mbr.x, mbr.y, mbr.z, B.kn);
     a.bd.rec.r5[b] = make_float4(offr.x, offr.y, offr.z, B.ks);
@@ -1384,6 +1390,16 @@ __global__ void __launch_bounds__(kThreads) history_corrections(CorrArgs a) {
     a.corr[b] = make_float4(gap(fs.x, r3.x), gap(fs.y, r3.y), gap(fs.z, r3.z), gap(a.h.fn[b], r2.w));
     a.corr[m + b] = make_float4(gap(mb.x, r4.x), gap(mb.y, r4.y), gap(mb.z, r4.z), gap(a.h.mt[b], r3.w));
     a.corr[2 * m + b] = make_float4(gap(off.x, r5.x), gap(off.y, r5.y), gap(off.z, r5.z), 0.0f);
+}
+
+// Residual at y = 0 after a commit: the records' increments vanish there, so
+// r = r0 on free sites and 0 (= y) on fixed ones; y32 = 0.
+__global__ void __launch_bounds__(kThreads) initial_residual(int64_t n, const double *r0, const uint8_t *fixed,
+                                                             float *y32, double *residual) {
+    const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (e >= 6 * n) return;
+    residual[e] = fixed[e / 6] ? 0.0 : r0[e];
+    y32[e] = 0.0f;
 }
 
 // Per-step constants from maintained loads: r0 and the rhs scale terms.
@@ -1752,6 +1768,15 @@ int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h,
             commit_sites<<<blocks_for(kGroupJ * g->n_sites, kThreads), kThreads, 0, st>>>(
                 g->n_sites, g->inc_ptr, g->inc_bond, dloads, loads);
     }
+    DPF_CHECK_LAUNCH();
+    return DPF_OK;
+}
+
+int dpf_mixed_initial_residual(int64_t n_sites, const double *r0, const uint8_t *fixed, float *y32, double *residual,
+                               void *stream) {
+    if (n_sites <= 0 || !r0 || !fixed || !y32 || !residual) return DPF_ERR_ARGUMENT;
+    initial_residual<<<blocks_for(6 * n_sites, kThreads), kThreads, 0, (cudaStream_t)stream>>>(n_sites, r0, fixed,
+                                                                                              y32, residual);
     DPF_CHECK_LAUNCH();
     return DPF_OK;
 }

@@ -1443,6 +1443,8 @@ class MixedNewtonBonds(NewtonBonds):
             float(linear_tolerance)
         args.max_iterations, args.refresh, args.timing = int(max_iterations), int(refresh), int(timing)
         args.v_in, args.rotation_in = v0.data_ptr(), r0.data_ptr()
+        args.committed_start = int(self.__dict__.get('_committed_start', False) and not refresh)
+        self._committed_start = False      # until this step commits
         info = self._native_info
         self._inner_host = 0
         self._call('dpf_mixed_newton_step', ctypes.byref(desc), ctypes.byref(args), ctypes.byref(info),
@@ -1474,6 +1476,7 @@ class MixedNewtonBonds(NewtonBonds):
         else:
             self.commit(state)
         self.v, self.rotation = self._v, rotation
+        self._committed_start = True
         self._token = self._state_token()
         self._since_refresh += 1
         self.time += dt
@@ -1646,14 +1649,17 @@ class MixedNewtonBonds(NewtonBonds):
         if getattr(self, '_begin_scales', None) is None:
             self._begin_scales = torch.zeros(2, dtype=F64, device=self.device)
         scales = self._begin_scales
+        self._zero_start = False
         if self._token is not None and self._token == self._state_token() and \
                 self._since_refresh < self.refresh_interval:
+            self._zero_start = self.__dict__.get('_committed_start', False)
             self._timed('setup', lambda: self._call(
                 'dpf_mixed_begin', self.n_sites, self._loads.data_ptr(), self.mass.data_ptr(), self._v.data_ptr(),
                 external.data_ptr(), self.fixed.data_ptr(), dt, self._r0.data_ptr(), scales.data_ptr(),
                 self._partials.data_ptr(), self._stream()))
         else:
             self._since_refresh = 0
+            self._committed_start = False
             history = self._history_struct()     # folds a lazily committed history first
             self._timed('setup', lambda: self._call(
                 'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
@@ -1674,6 +1680,7 @@ class MixedNewtonBonds(NewtonBonds):
         return rhs_scale
 
     def _mixed_residual(self, y, dt, want_tangent, use_p, scaled=None):
+        self._committed_start = False      # the tangent is no longer the one the last commit stored
         r = torch.empty_like(y)
         self._to_y32(y)
         self._status.zero_()
@@ -1687,7 +1694,16 @@ class MixedNewtonBonds(NewtonBonds):
 
     def _iteration_residual(self, y, dt, external):
         reuse = self._cached is not None and self._cached[0] is y
-        r = self._cached[1] if reuse else self._mixed_residual(y, dt, want_tangent=True, use_p=False)
+        if self.__dict__.get('_zero_start'):
+            # y = 0 on records and tangent from the last commit: r = r0 (0 on fixed sites)
+            self._zero_start = False
+            r = torch.empty_like(y)
+            self._status.zero_()
+            self._timed('residual', lambda: self._call(
+                'dpf_mixed_initial_residual', self.n_sites, self._r0.data_ptr(), self.fixed.data_ptr(),
+                self._y32.data_ptr(), r.data_ptr(), self._stream()))
+        else:
+            r = self._cached[1] if reuse else self._mixed_residual(y, dt, want_tangent=True, use_p=False)
         self._cached = None
         self._timed('scaling', lambda: self._call(
             'dpf_mixed_scaling', ctypes.byref(self._graph), self._bond_data.data_ptr(), self._mass32.data_ptr(),
@@ -1779,6 +1795,7 @@ class MixedNewtonBonds(NewtonBonds):
         else:
             self.commit(state)
         self.v, self.rotation = self._v, rotation
+        self._committed_start = True       # records and the tangent at y = 0 of the next step
         self._cached = None
         self._token = self._state_token()
         self._since_refresh += 1

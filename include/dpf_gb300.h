@@ -384,6 +384,15 @@ int64_t dpf_mixed_bond_floats(int64_t n_bonds);
  * (16-byte aligned; holds the padded work vectors and the bond wrench). */
 int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds);
 
+/* The residual at y = 0 of a step whose records a commit wrote (dpf_mixed_commit
+ * with dloads, or dpf_mixed_commit_lazy): every bond increment vanishes there,
+ * so residual = r0 on free sites and 0 on fixed ones, y32 = 0, and the commit
+ * already stored the tangent at y = 0 in bond_data.  Equal to
+ * dpf_mixed_residual(y = 0) without its bond pass and site gather; not valid
+ * after a float64 setup (its records carry dn0 != 0). */
+int dpf_mixed_initial_residual(int64_t n_sites, const double *r0, const uint8_t *fixed, float *y32, double *residual,
+                               void *stream);
+
 /* Lazy float64 history.  The bond records (bond_data) carry fn, mt, fs, mb
  * and offset in float32 and every commit advances them; `corrections`
  * (dpf_history_correction_floats(M) floats, 16-byte aligned) hold per bond
@@ -846,6 +855,8 @@ typedef struct dpf_newton_step {
     int timing;                    /* 1: CUDA-event times of the hot launches into the info */
     const double *v_in;            /* optional: the step's start velocity, copied into v first */
     const double *rotation_in;     /* optional: the start rotations, copied into rotation first */
+    int committed_start;           /* 1: the records and the tangent at y = 0 come from the last commit
+                                      (dpf_mixed_initial_residual replaces the first residual pass) */
 } dpf_newton_step;
 
 /* outcome of a step */

@@ -137,3 +137,28 @@ def test_lazy_history_matches_eager_commit():
     assert torch.equal(held, fn_before)
     assert not torch.equal(lazy.fn, fn_before)
     assert lazy.fn is lazy.fn
+
+
+def test_committed_start_equals_the_full_first_residual():
+    """After a commit the first residual of the next step is r0 (0 on fixed
+    sites) and the tangent the commit stored equals the one the residual pass
+    forms at y = 0."""
+    import dpf_gb300
+    foam, s, _ = pair(m=10, seed=7)
+    load = dpf_gb300.gravity_load(foam)*4.0
+    for _ in range(2):
+        s.step(2e-3, s.tensor(load), tolerance=1e-6)
+    assert s._committed_start
+    m, dt = s.n_bonds, 2e-3
+    stored = s._bond_data[7*4*m:10*4*m].clone()
+    s._v = s._vec(s.v).clone()
+    s._step_begin(dt, s.tensor(load))
+    assert s._zero_start
+    y = torch.zeros_like(s._v)
+    quick = torch.empty_like(y)
+    s._call('dpf_mixed_initial_residual', s.n_sites, s._r0.data_ptr(), s.fixed.data_ptr(), s._y32.data_ptr(),
+            quick.data_ptr(), s._stream())
+    full = s._mixed_residual(y, dt, want_tangent=True, use_p=False)
+    assert torch.equal(quick, full)
+    recomputed = s._bond_data[7*4*m:10*4*m]
+    assert torch.allclose(stored, recomputed, rtol=2e-7, atol=0)
