@@ -198,6 +198,7 @@ SIGNATURES = {
     'dpf_combine_rows_f32': (i32, [i64, vp, i64, i32, P(ctypes.c_double), vp, vp]),
     'dpf_scale_to_float': (i32, [i64, f64, vp, vp, vp]),
     'dpf_mixed_initial_residual': (i32, [i64, vp, vp, vp, vp, vp]),
+    'dpf_mixed_wrench_floats': (i64, [i64]),
     'dpf_history_correction_floats': (i64, [i64]),
     'dpf_mixed_history_corrections': (i32, [P(Graph), P(History), vp, vp, vp]),
     'dpf_mixed_commit_lazy': (i32, [P(Graph), vp, vp, vp, vp, vp, vp, vp, vp, vp]),

@@ -56,11 +56,32 @@ __device__ __forceinline__ V3<float> f3(const double *p) {
 }
 __device__ __forceinline__ float3 tof3(d3 a) { return make_float3((float)a.x, (float)a.y, (float)a.z); }
 
+// Float32 bond wrench record [F, T_i, T_j] in 12 floats (48 B, 16-byte
+// aligned): (F.x F.y F.z Ti.x) (Ti.y Ti.z Tj.x Tj.y) (Tj.z 0 0 0), so that a
+// site pass reads an end's six numbers with two or three 16-byte loads.
+constexpr int kWrenchFloats = 12;
+
 __device__ __forceinline__ void store9(float *w, int64_t b, V3<float> f, V3<float> ti, V3<float> tj) {
-    float *p = w + 9 * b;
-    p[0] = f.x; p[1] = f.y; p[2] = f.z;
-    p[3] = ti.x; p[4] = ti.y; p[5] = ti.z;
-    p[6] = tj.x; p[7] = tj.y; p[8] = tj.z;
+    float4 *p = reinterpret_cast<float4 *>(w + kWrenchFloats * b);
+    p[0] = make_float4(f.x, f.y, f.z, ti.x);
+    p[1] = make_float4(ti.y, ti.z, tj.x, tj.y);
+    p[2] = make_float4(tj.z, 0.0f, 0.0f, 0.0f);
+}
+
+// The signed share of incidence v (v >= 0: the i end, F and T_i; ~v: the j
+// end, -F and T_j) of a wrench record.
+__device__ __forceinline__ void end_share(const float *__restrict__ w, int v, float out[6]) {
+    const bool at_i = v >= 0;
+    const float4 *p = reinterpret_cast<const float4 *>(w + kWrenchFloats * (int64_t)(at_i ? v : ~v));
+    const float4 q0 = p[0], q1 = p[1];
+    if (at_i) {
+        out[0] = q0.x; out[1] = q0.y; out[2] = q0.z;
+        out[3] = q0.w; out[4] = q1.x; out[5] = q1.y;
+    } else {
+        const float tz = reinterpret_cast<const float *>(p)[8];
+        out[0] = -q0.x; out[1] = -q0.y; out[2] = -q0.z;
+        out[3] = q1.z; out[4] = q1.w; out[5] = tz;
+    }
 }
 
 // Error-free sum a + b = s + e (Knuth's TwoSum), float32.
@@ -71,54 +92,6 @@ __device__ __forceinline__ void two_sum(float &s, float &e, float b) {
     s = t;
 }
 
-// Compensated float32 site sum of a float32 bond wrench: hi + lo carries the
-// sum to about float64 accuracy without float64 arithmetic per incidence.
-__device__ __forceinline__ void gather9c(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
-                                         const float *__restrict__ w, int64_t s, float hi[6], float lo[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) hi[c] = lo[c] = 0.0f;
-    const int e1 = ptr[s + 1];
-    for (int e = ptr[s]; e < e1; ++e) {
-        const int v = inc[e];
-        if (v >= 0) {
-            const float *p = w + 9 * (int64_t)v;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], p[c]);
-        } else {
-            const float *p = w + 9 * (int64_t)(~v);
-            two_sum(hi[0], lo[0], -p[0]);
-            two_sum(hi[1], lo[1], -p[1]);
-            two_sum(hi[2], lo[2], -p[2]);
-            two_sum(hi[3], lo[3], p[6]);
-            two_sum(hi[4], lo[4], p[7]);
-            two_sum(hi[5], lo[5], p[8]);
-        }
-    }
-}
-
-// Plain float32 site sum.
-__device__ __forceinline__ void gather9f(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
-                                         const float *__restrict__ w, int64_t s, float acc[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
-    const int e1 = ptr[s + 1];
-    for (int e = ptr[s]; e < e1; ++e) {
-        const int v = inc[e];
-        if (v >= 0) {
-            const float *p = w + 9 * (int64_t)v;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) acc[c] += p[c];
-        } else {
-            const float *p = w + 9 * (int64_t)(~v);
-            acc[0] -= p[0];
-            acc[1] -= p[1];
-            acc[2] -= p[2];
-            acc[3] += p[6];
-            acc[4] += p[7];
-            acc[5] += p[8];
-        }
-    }
-}
 
 // Segmented site sum by groups of kGroupJ lanes (xor-shuffle reduction),
 // compensated: used by the residual, JVP and commit site passes.  The group
@@ -139,20 +112,10 @@ __device__ __forceinline__ void group_gather9c_j(const int32_t *__restrict__ ptr
     if (valid) {
         const int e1 = ptr[s + 1];
         for (int e = ptr[s] + lane; e < e1; e += kGroupJ) {
-            const int v = inc[e];
-            if (v >= 0) {
-                const float *p = w + 9 * (int64_t)v;
+            float sh[6];
+            end_share(w, inc[e], sh);
 #pragma unroll
-                for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], p[c]);
-            } else {
-                const float *p = w + 9 * (int64_t)(~v);
-                two_sum(hi[0], lo[0], -p[0]);
-                two_sum(hi[1], lo[1], -p[1]);
-                two_sum(hi[2], lo[2], -p[2]);
-                two_sum(hi[3], lo[3], p[6]);
-                two_sum(hi[4], lo[4], p[7]);
-                two_sum(hi[5], lo[5], p[8]);
-            }
+            for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], sh[c]);
         }
     }
 #pragma unroll
@@ -173,20 +136,10 @@ __device__ __forceinline__ void gather9(const int32_t *__restrict__ ptr, const i
     for (int c = 0; c < 6; ++c) acc[c] = 0.0;
     const int e1 = ptr[s + 1];
     for (int e = ptr[s]; e < e1; ++e) {
-        const int v = inc[e];
-        if (v >= 0) {
-            const float *p = w + 9 * (int64_t)v;
+        float sh[6];
+        end_share(w, inc[e], sh);
 #pragma unroll
-            for (int c = 0; c < 6; ++c) acc[c] += (double)p[c];
-        } else {
-            const float *p = w + 9 * (int64_t)(~v);
-            acc[0] -= (double)p[0];
-            acc[1] -= (double)p[1];
-            acc[2] -= (double)p[2];
-            acc[3] += (double)p[6];
-            acc[4] += (double)p[7];
-            acc[5] += (double)p[8];
-        }
+        for (int c = 0; c < 6; ++c) acc[c] += (double)sh[c];
     }
 }
 
@@ -321,9 +274,8 @@ __device__ __forceinline__ void load_y(const float *y, int s, V3<float> &u, V3<f
 }
 
 __device__ __forceinline__ void store_zero9(float *w, int64_t b) {
-    float *p = w + 9 * b;
-#pragma unroll
-    for (int c = 0; c < 9; ++c) p[c] = 0.0f;
+    float4 *p = reinterpret_cast<float4 *>(w + kWrenchFloats * b);
+    p[0] = p[1] = p[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 __global__ void __launch_bounds__(kThreads) residual_bonds(ResidualBondArgs a) {
@@ -922,70 +874,7 @@ __device__ __forceinline__ void mv6(const float *P, const float x[6], float y[6]
     }
 }
 
-__device__ __forceinline__ void group_gather9f(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
-                                               const float *__restrict__ w, int64_t s, bool valid, int lane,
-                                               float acc[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) acc[c] = 0.0f;
-    if (valid) {
-        const int e1 = ptr[s + 1];
-        for (int e = ptr[s] + lane; e < e1; e += kGroup) {
-            const int v = inc[e];
-            if (v >= 0) {
-                const float *p = w + 9 * (int64_t)v;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) acc[c] += p[c];
-            } else {
-                const float *p = w + 9 * (int64_t)(~v);
-                acc[0] -= p[0];
-                acc[1] -= p[1];
-                acc[2] -= p[2];
-                acc[3] += p[6];
-                acc[4] += p[7];
-                acc[5] += p[8];
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 1; o < kGroup; o <<= 1)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-}
 
-__device__ __forceinline__ void group_gather9c(const int32_t *__restrict__ ptr, const int32_t *__restrict__ inc,
-                                               const float *__restrict__ w, int64_t s, bool valid, int lane,
-                                               float hi[6], float lo[6]) {
-#pragma unroll
-    for (int c = 0; c < 6; ++c) hi[c] = lo[c] = 0.0f;
-    if (valid) {
-        const int e1 = ptr[s + 1];
-        for (int e = ptr[s] + lane; e < e1; e += kGroup) {
-            const int v = inc[e];
-            if (v >= 0) {
-                const float *p = w + 9 * (int64_t)v;
-#pragma unroll
-                for (int c = 0; c < 6; ++c) two_sum(hi[c], lo[c], p[c]);
-            } else {
-                const float *p = w + 9 * (int64_t)(~v);
-                two_sum(hi[0], lo[0], -p[0]);
-                two_sum(hi[1], lo[1], -p[1]);
-                two_sum(hi[2], lo[2], -p[2]);
-                two_sum(hi[3], lo[3], p[6]);
-                two_sum(hi[4], lo[4], p[7]);
-                two_sum(hi[5], lo[5], p[8]);
-            }
-        }
-    }
-#pragma unroll
-    for (int o = 1; o < kGroup; o <<= 1)
-#pragma unroll
-        for (int c = 0; c < 6; ++c) {
-            const float h = __shfl_xor_sync(0xffffffffu, hi[c], o);
-            const float l = __shfl_xor_sync(0xffffffffu, lo[c], o);
-            two_sum(hi[c], lo[c], h);
-            lo[c] += l;
-        }
-}
 
 // Elastic PCG in float32 with float64 dot products, one cooperative launch
 // (experiments/bonded_dem_newton.py:107-130).  Three grid barriers per
@@ -1202,7 +1091,7 @@ struct CommitArgs {
     const float *y32;
     const double *x_end;  // end positions x + y, formed first by end_positions
     double *normal_end, *offset_end, *fs_end, *mb_end, *fn_end, *mt_end;
-    float *dloads;  // optional: increment of the committed loads (9 floats per bond)
+    float *dloads;  // optional: increment of the committed loads (a wrench record per bond)
     float4 *corr;   // lazy form: corrections of the records' float32 state (3 float4 arrays of m)
 };
 
@@ -1518,6 +1407,10 @@ extern "C" {
 
 int64_t dpf_mixed_bond_floats(int64_t n_bonds) { return 4 * 11 * n_bonds; }
 
+int64_t dpf_mixed_wrench_floats(int64_t n_bonds) { return n_bonds < 0 ? 0 : kWrenchFloats * n_bonds; }
+
+static bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
 int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds) {
     return 40 * n_sites + 12 * n_bonds + 4 * (int64_t)kMaxPcgBlocks;
 }
@@ -1573,9 +1466,10 @@ int dpf_mixed_residual_segmented(const dpf_graph *g, float *bond_data, const dou
     if (!mixed_graph_ok(g) || !bond_data || !y || !y32 || !mass || !fixed || !r0 || !residual || !status ||
         (g->n_bonds && !wrench) || (norms && !partials) || (preconditioner && !units32) || (active && !seg_bond))
         return DPF_ERR_ARGUMENT;
-    // the site pass moves y, mass, r0 and the residual in 16-byte pairs and P in 8-byte pairs
+    // the site pass moves y, mass, r0 and the residual in 16-byte pairs and P in 8-byte pairs;
+    // wrench records are 16-byte quads
     if ((((uintptr_t)y | (uintptr_t)mass | (uintptr_t)r0 | (uintptr_t)residual) & 15u) ||
-        ((uintptr_t)preconditioner & 7u))
+        ((uintptr_t)preconditioner & 7u) || !aligned16(wrench))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
@@ -1621,7 +1515,8 @@ static int mixed_jvp(const dpf_graph *g, float *bond_data, const float *y32, con
                      float *wrench, const int32_t *seg_bond, const uint8_t *active, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !y32 || (!direction && !direction32) || !mass32 || !fixed ||
         (!out && !out32) || !d32 || (g->n_bonds && !wrench) || (preconditioner && !units32) ||
-        (active && !seg_bond) || ((uintptr_t)preconditioner & 7u))  // rows of P are read in 8-byte pairs
+        (active && !seg_bond) || ((uintptr_t)preconditioner & 7u) ||  // rows of P are read in 8-byte pairs
+        !aligned16(wrench))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     const int64_t n6 = 6 * g->n_sites;
@@ -1657,7 +1552,8 @@ int dpf_mixed_jacobian_vector_f32(const dpf_graph *g, float *bond_data, const fl
 
 int dpf_mixed_stiffness_apply(const dpf_graph *g, float *bond_data, const float *q, double *out, float *wrench,
                               void *stream) {
-    if (!mixed_graph_ok(g) || !bond_data || !q || !out || (g->n_bonds && !wrench)) return DPF_ERR_ARGUMENT;
+    if (!mixed_graph_ok(g) || !bond_data || !q || !out || (g->n_bonds && !wrench) || !aligned16(wrench))
+        return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds)
         stiffness_bonds_f32<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(
@@ -1755,7 +1651,7 @@ int dpf_mixed_commit(const dpf_graph *g, float *bond_data, const dpf_history *h,
                      double *mt_end, double *mb_end, float *dloads, double *loads, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !h || !h->x ||
         (g->n_bonds && (!h->fn || !h->fs || !h->mt || !h->mb || !h->offset)) || !y || !y32 || !x_end ||
-        (dloads && !loads) ||
+        (dloads && (!loads || !aligned16(dloads))) ||
         ((g->n_bonds) && (!normal_end || !offset_end || !fn_end || !fs_end || !mt_end || !mb_end)))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
@@ -1799,7 +1695,7 @@ int dpf_mixed_history_corrections(const dpf_graph *g, const dpf_history *h, cons
 int dpf_mixed_commit_lazy(const dpf_graph *g, float *bond_data, const double *x, const double *y, const float *y32,
                           double *x_end, float *corrections, float *dloads, double *loads, void *stream) {
     if (!mixed_graph_ok(g) || !bond_data || !x || !y || !y32 || !x_end || (g->n_bonds && (!corrections || !dloads ||
-        !loads || ((uintptr_t)corrections & 15u))))
+        !loads || ((uintptr_t)corrections & 15u) || !aligned16(dloads))))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     end_positions<<<blocks_for(3 * g->n_sites, kThreads), kThreads, 0, st>>>(g->n_sites, x, y, x_end);

@@ -1492,7 +1492,7 @@ class MixedNewtonBonds(NewtonBonds):
         dev = self.device
         f32 = torch.float32
         self._bond_data = torch.empty(max(4, lib.dpf_mixed_bond_floats(m)), dtype=f32, device=dev)
-        self._wrench32 = torch.empty(max(1, 9*m), dtype=f32, device=dev)
+        self._wrench32 = torch.empty(max(4, lib.dpf_mixed_wrench_floats(m)), dtype=f32, device=dev)
         self._r0 = torch.empty((n, 6), dtype=F64, device=dev)
         self._block32 = torch.empty((n, 6, 6), dtype=f32, device=dev)
         self._p32 = torch.empty((n, 6, 6), dtype=f32, device=dev)

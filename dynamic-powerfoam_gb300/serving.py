@@ -222,7 +222,7 @@ class Pool:
         self.max_sites, self.max_bonds = int(max_sites), int(max_bonds)
         n, m = self.max_sites, self.max_bonds
         self.f64 = torch.empty(9*m + 3*6*n + 65*6*n + 1024, dtype=F64, device=device)
-        self.f32 = torch.empty(lib.dpf_mixed_bond_floats(m) + 9*m + 2*36*n + 3*6*n +
+        self.f32 = torch.empty(lib.dpf_mixed_bond_floats(m) + lib.dpf_mixed_wrench_floats(m) + 2*36*n + 3*6*n +
                                lib.dpf_mixed_workspace_floats(n, m) + lib.dpf_end_floats(m) +
                                (4 + 24)*n + lib.dpf_tiled_workspace_floats(n) + 4096,
                                dtype=torch.float32, device=device)
@@ -320,7 +320,7 @@ class Batch(MixedNewtonBonds):
         self.block = self.units = None
         self.profile = None
         self._bond_data = take32(max(4, lib.dpf_mixed_bond_floats(m)))
-        self._wrench32 = take32(max(1, 9*m))
+        self._wrench32 = take32(max(4, lib.dpf_mixed_wrench_floats(m)))
         self._r0 = take64(6*n, (n, 6))
         self._block32 = take32(36*n, (n, 6, 6))
         self._p32 = take32(36*n, (n, 6, 6))

@@ -374,7 +374,8 @@ int dpf_barrier_selftest(int blocks, int64_t timeout_ns, int missing, unsigned *
  * increments f_mid(y) - f_mid(0), evaluated from small quantities only and
  * summed per site in compensated float32 (about float64 accuracy).
  * bond_data: dpf_mixed_bond_floats(M) floats (float4 records + float32
- * tangent, 16-byte aligned); wrench: 9 M floats.  The *32 arguments are
+ * tangent, 16-byte aligned); wrench: dpf_mixed_wrench_floats(M) floats, 16-byte
+ * aligned (one 48-byte record [F, T_i, T_j] per bond).  The *32 arguments are
  * float32 copies of the float64 arrays of the same name (y32 of the increment,
  * mass32 of the (N, 6) mass, units32 of the units written by
  * dpf_mixed_scaling); d32 is a float32 (N, 6) scratch. */
@@ -383,6 +384,9 @@ int64_t dpf_mixed_bond_floats(int64_t n_bonds);
 /* Float workspace of dpf_mixed_precondition for N sites and M bonds
  * (16-byte aligned; holds the padded work vectors and the bond wrench). */
 int64_t dpf_mixed_workspace_floats(int64_t n_sites, int64_t n_bonds);
+
+/* Size in floats of the float32 bond wrench of the mixed passes (12 M). */
+int64_t dpf_mixed_wrench_floats(int64_t n_bonds);
 
 /* The residual at y = 0 of a step whose records a commit wrote (dpf_mixed_commit
  * with dloads, or dpf_mixed_commit_lazy): every bond increment vanishes there,
@@ -817,7 +821,7 @@ typedef struct dpf_mixed_newton {
     double *partials;              /* dpf_partials_doubles() */
     double *scalars;               /* >= 4 */
     int *status;                   /* guard bits */
-    float *y32, *d32, *wrench32;   /* (N, 6), (N, 6), 9 M */
+    float *y32, *d32, *wrench32;   /* (N, 6), (N, 6), dpf_mixed_wrench_floats(M) */
     float *block32, *p32;          /* (N, 6, 6) */
     double *units;                 /* (N, 6) */
     float *units32;                /* (N, 6) */
