@@ -40,6 +40,39 @@ __device__ __forceinline__ void dsincos(Dual a, Dual &s, Dual &c) {
     c = {cv, -sv * a.d};
 }
 __device__ __forceinline__ void dsincos(float a, float &s, float &c) { sincosf(a, &s, &c); }
+
+// sin t and 1 - cos t (= 2 sin^2(t/2), without cancellation).  For |t| < 1/2
+// (every spin increment the rotation guards admit) from their Maclaurin
+// series in t^2, five terms each (truncation below 3e-11 relative), instead of
+// two sincos evaluations; larger |t| through sincos of t and t/2.
+__device__ __forceinline__ void sin_omc(float t, float &s, float &omc) {
+    const float t2 = t * t;
+    if (t2 < 0.25f) {
+        float p = 1.0f / 362880.0f;               // 1/9!
+        p = fmaf(p, t2, -1.0f / 5040.0f);         // 1/7!
+        p = fmaf(p, t2, 1.0f / 120.0f);           // 1/5!
+        p = fmaf(p, t2, -1.0f / 6.0f);            // 1/3!
+        p = fmaf(p, t2, 1.0f);
+        s = t * p;
+        float q = 1.0f / 3628800.0f;              // 1/10!
+        q = fmaf(q, t2, -1.0f / 40320.0f);        // 1/8!
+        q = fmaf(q, t2, 1.0f / 720.0f);           // 1/6!
+        q = fmaf(q, t2, -1.0f / 24.0f);           // 1/4!
+        q = fmaf(q, t2, 0.5f);                    // 1/2!
+        omc = t2 * q;
+    } else {
+        float sh, ch, c;
+        sincosf(0.5f * t, &sh, &ch);
+        sincosf(t, &s, &c);
+        omc = 2.0f * sh * sh;
+    }
+}
+__device__ __forceinline__ void sin_omc(Dual t, Dual &s, Dual &omc) {
+    float sv, ov;
+    sin_omc(t.v, sv, ov);
+    s = {sv, (1.0f - ov) * t.d};   // d sin = cos dt
+    omc = {ov, sv * t.d};          // d (1 - cos) = sin dt
+}
 __device__ __forceinline__ float value(float a) { return a; }
 __device__ __forceinline__ float value(Dual a) { return a.v; }
 __device__ __forceinline__ float deriv(Dual a) { return a.d; }
@@ -158,11 +191,7 @@ __device__ __forceinline__ TransportInc<T> make_transport_inc(V3<T> n0, V3<T> dn
     const T bl = dsqrt(dot(bv, bv));
     const V3<T> b = bv / bl;
     const T theta = dot(hs, b);
-    T sh, ch;
-    dsincos(0.5f * theta, sh, ch);
-    T c;
-    dsincos(theta, t.s, c);
-    t.omc = 2.0f * sh * sh;
+    sin_omc(theta, t.s, t.omc);
     return t;
 }
 
