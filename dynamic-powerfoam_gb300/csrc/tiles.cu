@@ -645,22 +645,56 @@ __device__ __forceinline__ void end_wrench(float4 a, float4 b, float4 c, const f
     acc[5] -= (rx * fy - ry * fx) + mz;
 }
 
+// ---- L2 residency of the PCG's per-site vectors ----------------------------
+// Every CG iteration streams the end records (about 190 MB at 64^3, loaded
+// evict-first) through L2 and reads the site vectors u, p, x, w, s, r and the
+// block inverses (about 65 MB) again.  Their loads and stores carry an L2
+// evict-last policy so that the record stream does not push them out.
+__device__ __forceinline__ uint64_t keep_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ float2 ld2_keep(const float2 *p, uint64_t pol) {
+    float2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.f32 {%0, %1}, [%2], %3;" : "=f"(v.x), "=f"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float4 ld4_keep(const float4 *p, uint64_t pol) {
+    float4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.f32 {%0, %1, %2, %3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st2_keep(float2 *p, float2 v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;" ::"l"(p), "f"(v.x), "f"(v.y), "l"(pol)
+                 : "memory");
+}
+__device__ __forceinline__ void ld6_keep(const float *p, float v[6], uint64_t pol) {
+    const float2 *q = reinterpret_cast<const float2 *>(p);
+    const float2 a = ld2_keep(q, pol), b = ld2_keep(q + 1, pol), c = ld2_keep(q + 2, pol);
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
+}
+__device__ __forceinline__ void st6_keep(float *p, const float v[6], uint64_t pol) {
+    float2 *q = reinterpret_cast<float2 *>(p);
+    st2_keep(q, make_float2(v[0], v[1]), pol);
+    st2_keep(q + 1, make_float2(v[2], v[3]), pol);
+    st2_keep(q + 2, make_float2(v[4], v[5]), pol);
+}
+
 // q of a site: read-only for the whole launch (kConst) through the
-// non-coherent path, else with plain loads (a PCG updates q between sweeps).
+// non-coherent path, else (a PCG updates q between sweeps) with plain loads
+// under the evict-last policy.
 template <bool kConst>
 __device__ __forceinline__ void load_q(const float *q, int64_t s, float v[6]) {
-    const float2 *p = reinterpret_cast<const float2 *>(q + 6 * s);
-    float2 a, b, c;
     if (kConst) {
-        a = __ldg(p);
-        b = __ldg(p + 1);
-        c = __ldg(p + 2);
+        const float2 *p = reinterpret_cast<const float2 *>(q + 6 * s);
+        const float2 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
     } else {
-        a = p[0];
-        b = p[1];
-        c = p[2];
+        ld6_keep(q + 6 * s, v, keep_policy());
     }
-    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y;
 }
 
 // For every site s: epi(s, q_s, site record, acc) with acc the alpha K q sum.
@@ -793,7 +827,7 @@ struct PcgEpi {
         operator_row(rec, qs, acc, wv);
 #pragma unroll
         for (int c = 0; c < 6; ++c) dot = fmaf(wv[c], qs[c], dot);
-        st6(a.w + 6 * s, wv);
+        st6_keep(a.w + 6 * s, wv, keep_policy());
     }
 };
 
@@ -812,13 +846,26 @@ __device__ __forceinline__ void mv36(const float *B, const float x[6], float y[6
 // site comes before any store.
 __device__ __forceinline__ float update_site(const PcgArgs &a, int64_t s, float fa, float fb) {
     float uv[6], pv[6], xv[6], wv[6], sv[6], rv[6], Pm[21];
-    ld6(a.u + 6 * s, uv);
-    ld6(a.p + 6 * s, pv);
-    ld6(a.x + 6 * s, xv);
-    ld6(a.w + 6 * s, wv);
-    ld6(a.s + 6 * s, sv);
-    ld6(a.r + 6 * s, rv);
-    sym6(a.P24 + 6 * s, Pm);
+    const uint64_t pol = keep_policy();
+    ld6_keep(a.u + 6 * s, uv, pol);
+    ld6_keep(a.p + 6 * s, pv, pol);
+    ld6_keep(a.x + 6 * s, xv, pol);
+    ld6_keep(a.w + 6 * s, wv, pol);
+    ld6_keep(a.s + 6 * s, sv, pol);
+    ld6_keep(a.r + 6 * s, rv, pol);
+    {
+        float q24[24];
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const float4 v = ld4_keep(a.P24 + 6 * s + k, pol);
+            q24[4 * k] = v.x;
+            q24[4 * k + 1] = v.y;
+            q24[4 * k + 2] = v.z;
+            q24[4 * k + 3] = v.w;
+        }
+#pragma unroll
+        for (int k = 0; k < 21; ++k) Pm[k] = q24[k];
+    }
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
         pv[c] = fmaf(fb, pv[c], uv[c]);
@@ -827,11 +874,11 @@ __device__ __forceinline__ float update_site(const PcgArgs &a, int64_t s, float 
         rv[c] = fmaf(-fa, sv[c], rv[c]);
     }
     sym_mv6(Pm, rv, uv);
-    st6(a.p + 6 * s, pv);
-    st6(a.x + 6 * s, xv);
-    st6(a.s + 6 * s, sv);
-    st6(a.r + 6 * s, rv);
-    st6(a.u + 6 * s, uv);
+    st6_keep(a.p + 6 * s, pv, pol);
+    st6_keep(a.x + 6 * s, xv, pol);
+    st6_keep(a.s + 6 * s, sv, pol);
+    st6_keep(a.r + 6 * s, rv, pol);
+    st6_keep(a.u + 6 * s, uv, pol);
     float dot = 0.0f;
 #pragma unroll
     for (int c = 0; c < 6; ++c) dot = fmaf(rv[c], uv[c], dot);
