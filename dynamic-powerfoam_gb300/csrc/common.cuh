@@ -289,15 +289,22 @@ __device__ __forceinline__ void block_pair_partial(float v, float2 *part) {
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-// Sum of `count` block partial pairs, in float64, the same in every block.
+// Sum of `count` block partial pairs, in float64, the same in every block
+// (one warp adds them in a fixed order; the others wait at the block barrier).
 __device__ __forceinline__ double pair_total(const float2 *part, int count) {
-    float hi = 0.0f, lo = 0.0f;
-    for (int k = threadIdx.x; k < count; k += blockDim.x) {
-        const float2 p = part[k];
-        pair_add(hi, lo, p.x, p.y);
+    __shared__ double total;
+    __syncthreads();  // the previous total has been read
+    if (threadIdx.x < 32) {
+        float hi = 0.0f, lo = 0.0f;
+        for (int k = threadIdx.x; k < count; k += 32) {
+            const float2 p = part[k];
+            pair_add(hi, lo, p.x, p.y);
+        }
+        warp_pair_sum(hi, lo);
+        if (threadIdx.x == 0) total = (double)hi + (double)lo;
     }
-    const float2 t = block_pair_sum(hi, lo);
-    return (double)t.x + (double)t.y;
+    __syncthreads();
+    return total;
 }
 
 // a / b formed by thread 0 and shared with the block: one float64 division
@@ -342,9 +349,15 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// barrier[0] = arrival count, barrier[1] = generation.  Returns false when the
-// wait ran past timeout_ns (the status word then carries the error).  parties:
-// arrivals that release the barrier (0 = every block of the grid).
+// One atomic per block and barrier: block 0 adds 2^31 - (parties - 1), every
+// other block 1, so the top bit of barrier[0] flips exactly when all parties
+// have arrived (and the low bits return to where they were); a block waits
+// until the bit differs from the value its own add returned.  Release add and
+// acquire loads order the blocks' writes before and after the barrier.
+// barrier[0] starts at 0 (the launching entry point clears it); barrier[1] is
+// unused.  Returns false when the wait ran past timeout_ns (the status word
+// then carries the error).  parties: arrivals that release the barrier (0 =
+// every block of the grid).
 __device__ __forceinline__ bool grid_barrier(unsigned *barrier, int *status,
                                              unsigned long long timeout_ns = kBarrierTimeoutNs,
                                              unsigned parties = 0) {
@@ -352,25 +365,19 @@ __device__ __forceinline__ bool grid_barrier(unsigned *barrier, int *status,
     __syncthreads();
     if (threadIdx.x == 0) {
         ok = 1;
-        const unsigned gen = ld_acquire(barrier + 1);
-        __threadfence();
-        const unsigned arrived = atomicAdd(barrier, 1u);
-        if (arrived == (parties ? parties : gridDim.x) - 1) {
-            atomicExch(barrier, 0u);
-            __threadfence();
-            atomicAdd(barrier + 1, 1u);
-        } else {
-            const unsigned long long t0 = global_ns();
-            while (ld_acquire(barrier + 1) == gen) {
-                if (global_ns() - t0 > timeout_ns) {
-                    atomicOr(status, DPF_ERR_BARRIER_TIMEOUT);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(64);
+        const unsigned n = parties ? parties : gridDim.x;
+        const unsigned add = blockIdx.x == 0 ? 0x80000000u - (n - 1) : 1u;
+        unsigned old;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;" : "=r"(old) : "l"(barrier), "r"(add) : "memory");
+        unsigned polls = 0;
+        const unsigned long long t0 = global_ns();
+        while (((ld_acquire(barrier) ^ old) & 0x80000000u) == 0) {
+            if ((++polls & 63u) == 0 && global_ns() - t0 > timeout_ns) {
+                atomicOr(status, DPF_ERR_BARRIER_TIMEOUT);
+                ok = 0;
+                break;
             }
         }
-        __threadfence();
     }
     __syncthreads();
     return ok != 0;

@@ -48,7 +48,9 @@ def test_barrier_wait_runs_out_and_reports(lib):
     assert rc == 0
     assert status & _lib.DPF_ERR_BARRIER_TIMEOUT
     assert passed == 0
-    assert barrier[0] == 8          # the arrivals stay behind in the barrier word
+    # the arrivals stay behind in the barrier word: block 0 added 2^31 - 8 (nine
+    # parties), the seven others 1 each, so the top bit never flipped
+    assert barrier[0] == 0x7FFFFFFF
     assert elapsed < 2.0
     # the context still works
     x = torch.arange(10, dtype=torch.float64, device='cuda')
