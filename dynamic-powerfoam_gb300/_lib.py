@@ -67,7 +67,8 @@ class MixedNewton(ctypes.Structure):
     _fields_ = ([('graph', vp), ('stiffness', Stiffness)] +
                 [(k, vp) for k in ('radii', 'mass', 'mass32', 'fixed', 'bond_data', 'r0', 'loads', 'scales',
                                    'wrench64', 'partials', 'scalars', 'status', 'y32', 'd32', 'wrench32', 'block32',
-                                   'p32', 'units', 'units32', 'ends', 'site4', 'p24', 'end_workspace',
+                                   'p32', 'units', 'units32', 'block32_b', 'p32_b', 'units_b', 'units32_b', 'ends',
+                                   'site4', 'p24', 'end_workspace',
                                    'end_partials', 'barrier', 'inner', 'basis', 'transformed', 'products', 'w32',
                                    'h')] +
                 [('krylov_width', i32)] +
@@ -94,7 +95,7 @@ NEWTON_TIMERS = ('setup', 'residual', 'scaling', 'pcg', 'jvp', 'commit', 'pack',
 
 class NewtonInfo(ctypes.Structure):
     """dpf_newton_info: outcome, iteration counts, norms, trace and launch times of a step."""
-    _fields_ = ([(k, i32) for k in ('outcome', 'guard', 'nonlinear_iterations', 'krylov_iterations',
+    _fields_ = ([(k, i32) for k in ('outcome', 'guard', 'scaling_alternate', 'nonlinear_iterations', 'krylov_iterations',
                                     'cg_iterations', 'launches')] +
                 [(k, f64) for k in ('relative', 'local', 'work', 'max_rotation', 'krylov_relative')] +
                 [('trace_len', i32), ('trace', f64*(2*NEWTON_TRACE)), ('time_ms', f64*len(NEWTON_TIMERS)),

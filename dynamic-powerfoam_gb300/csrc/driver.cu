@@ -98,6 +98,12 @@ struct Step {
     Timing timing;
     bool packed = false;
     double rhs_scale = -1.0;
+    // the iterate's 6x6 blocks, their inverses and units, and the other set,
+    // which the speculative scaling of a line-search candidate writes
+    struct Scaling {
+        float *block32, *p32, *units32;
+        double *units;
+    } cur, alt;
 
     // one library call of `kernels` launches, timed under `key`
     template <class F>
@@ -127,20 +133,21 @@ struct Step {
         if (cudaMemsetAsync(s->status, 0, sizeof(int), st)) return DPF_ERR_CUDA;
         return call(kResidual, m ? 2 : 1, [&] {
             return dpf_mixed_residual(s->graph, s->bond_data, yy, s->y32, s->mass, s->fixed, a->dt, s->r0, 1,
-                                      use_p ? s->p32 : nullptr, use_p ? s->units32 : nullptr, out, nullptr,
+                                      use_p ? cur.p32 : nullptr, use_p ? cur.units32 : nullptr, out, nullptr,
                                       use_p ? s->scalars : nullptr, s->wrench32, s->partials, s->status, st);
         });
     }
 
-    // norms of the iterate's residual r: [|r|, max |s|, |s|] into s->scalars
-    int iteration_norms() {
+    // blocks and scaling of the tangent in bond_data into `into`, then the
+    // scaled residual of rr and its norms [|r|, max |s|, |s|] into norms
+    int scaling_norms(const Scaling &into, const double *rr, double *norms) {
         int rc = call(kScaling, 1, [&] {
-            return dpf_mixed_scaling(s->graph, s->bond_data, s->mass32, s->fixed, s->radii, a->dt, s->block32,
-                                     s->p32, s->units, s->units32, st);
+            return dpf_mixed_scaling(s->graph, s->bond_data, s->mass32, s->fixed, s->radii, a->dt, into.block32,
+                                     into.p32, into.units, into.units32, st);
         });
         if (rc) return rc;
         return call(kNorms, 1, [&] {
-            return dpf_mixed_scale_residual(n, s->p32, s->units32, r, scaled, s->scalars, s->partials, st);
+            return dpf_mixed_scale_residual(n, into.p32, into.units32, rr, scaled, norms, s->partials, st);
         });
     }
 
@@ -148,14 +155,14 @@ struct Step {
     int precondition(const float *vector, float *out) {
         if (!packed) {
             const int rc = call(kPack, 2, [&] {
-                return dpf_end_pack(s->graph, s->bond_data, 0.25 * a->dt * a->dt, s->p32, s->mass32, s->fixed,
+                return dpf_end_pack(s->graph, s->bond_data, 0.25 * a->dt * a->dt, cur.p32, s->mass32, s->fixed,
                                     s->ends, s->p24, s->site4, st);
             });
             if (rc) return rc;
             packed = true;
         }
         return call(kPcg, 1, [&] {
-            return dpf_end_precondition_f32(s->graph, s->ends, s->site4, s->fixed, s->block32, s->p24, s->units32,
+            return dpf_end_precondition_f32(s->graph, s->ends, s->site4, s->fixed, cur.block32, s->p24, cur.units32,
                                             vector, 0.03, 80, out, s->inner, s->end_workspace, s->end_partials,
                                             s->barrier, s->status, s->end_variant, st);
         });
@@ -165,7 +172,7 @@ struct Step {
     int jvp32(const float *direction, float *out) {
         return call(kJvp, m ? 3 : 2, [&] {
             return dpf_mixed_jacobian_vector_f32(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed,
-                                                 a->dt, s->units32, s->p32, out, s->d32, s->wrench32, st);
+                                                 a->dt, cur.units32, cur.p32, out, s->d32, s->wrench32, st);
         });
     }
 
@@ -173,129 +180,91 @@ struct Step {
     int jvp(const double *direction, double *out) {
         return call(kJvp, m ? 3 : 2, [&] {
             return dpf_mixed_jacobian_vector(s->graph, s->bond_data, s->y32, direction, s->mass32, s->fixed, a->dt,
-                                             s->units32, s->p32, out, s->d32, s->wrench32, nullptr, nullptr, st);
+                                             cur.units32, cur.p32, out, s->d32, s->wrench32, nullptr, nullptr, st);
         });
     }
 
-    int norm_of(const double *v, double *out) {
-        const int rc = call(kKrylov, 1, [&] {
-            return dpf_dot_norm(n6, v, nullptr, s->krylov_scalars, s->krylov_partials, st);
-        });
-        if (rc) return rc;
-        if (cudaMemcpyAsync(host + 12, s->krylov_scalars + 1, sizeof(double), cudaMemcpyDeviceToHost, st) ||
-            cudaStreamSynchronize(st))
-            return DPF_ERR_CUDA;
-        *out = host[12];
-        return DPF_OK;
-    }
-
-    // Right-preconditioned FGMRES with CGS2 Arnoldi (MixedNewtonBonds._fgmres32
-    // in newton.py): solves J delta = b with b = rhs, |b| = norm; x = delta.
-    // The Krylov vectors are float32 (the PCG and JVP outputs carry float32
-    // precision), their sums exact float32 pairs; x, b and the true residual
-    // are float64, the residual's J x formed from the kept products J z_k.
-    // Sets *ok.
-    int fgmres(double norm, double tolerance, int restart, int max_iterations, bool *ok, int *krylov) {
-        *ok = false;
-        *krylov = 0;
-        if (cudaMemsetAsync(x, 0, n6 * sizeof(double), st)) return DPF_ERR_CUDA;
-        if (norm == 0.0) {
-            *ok = true;
-            return DPF_OK;
-        }
-        int iterations = 0;
-        double relative = NAN;
-        double residual_norm = norm;
-        bool first = true;
+    // One restart cycle of the right-preconditioned FGMRES with CGS2 Arnoldi
+    // (MixedNewtonBonds._fgmres32 in newton.py) from `start` with |start| = g0:
+    // x += the cycle's correction, then J x (from the kept products J z_k), the
+    // true residual res = rhs - J x and its norm (krylov_scalars[1]) are
+    // enqueued but not read: the caller fetches that norm together with the
+    // speculative line-search values.  The Krylov vectors are float32 (the PCG
+    // and JVP outputs carry float32 precision), their sums exact float32
+    // pairs; x, rhs and the true residual are float64.  *krylov counts the
+    // Arnoldi steps; *singular reports a zero Givens denominator.
+    int fgmres_cycle(const double *start, double g0, double norm, double tolerance, int width, int *krylov,
+                     bool *singular) {
+        *singular = false;
+        if (width > s->krylov_width) return DPF_ERR_ARGUMENT;
+        const int ldh = width;  // H is (width + 1) x width, row-major
         double H[64 * 63];
         double cs[64], sn[64], g[65], coef[64];
-        while (iterations < max_iterations) {
-            const int width = restart < max_iterations - iterations ? restart : max_iterations - iterations;
-            if (width > s->krylov_width) return DPF_ERR_ARGUMENT;
-            const int ldh = width;  // H is (width + 1) x width, row-major
-            std::memset(H, 0, sizeof(double) * (width + 1) * width);
-            std::memset(cs, 0, sizeof(double) * width);
-            std::memset(sn, 0, sizeof(double) * width);
-            std::memset(g, 0, sizeof(double) * (width + 1));
-            if (first) {
-                g[0] = residual_norm;
-            } else {
-                const int rc = norm_of(res, &g[0]);
-                if (rc) return rc;
-            }
-            const double *start = first ? rhs : res;
-            first = false;
-            int rc = call(kKrylov, 1, [&] { return dpf_scale_to_float(n6, 1.0 / g[0], start, s->basis, st); });
+        std::memset(H, 0, sizeof(double) * (width + 1) * width);
+        std::memset(cs, 0, sizeof(double) * width);
+        std::memset(sn, 0, sizeof(double) * width);
+        std::memset(g, 0, sizeof(double) * (width + 1));
+        g[0] = g0;
+        int rc = call(kKrylov, 1, [&] { return dpf_scale_to_float(n6, 1.0 / g[0], start, s->basis, st); });
+        if (rc) return rc;
+        for (int j = 0; j < width; ++j) {
+            float *bj = s->basis + (int64_t)j * n6;
+            float *tj = s->transformed + (int64_t)j * n6;
+            float *pj = s->products + (int64_t)j * n6;
+            rc = precondition(bj, tj);
             if (rc) return rc;
-            for (int j = 0; j < width; ++j) {
-                float *bj = s->basis + (int64_t)j * n6;
-                float *tj = s->transformed + (int64_t)j * n6;
-                float *pj = s->products + (int64_t)j * n6;
-                rc = precondition(bj, tj);
+            rc = jvp32(tj, pj);
+            if (rc) return rc;
+            rc = call(kKrylov, 1, [&] {
+                return dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, pj, s->w32, s->h, s->krylov_partials, s->barrier,
+                                            s->status, st);
+            });
+            if (rc) return rc;
+            double *column = host + 16;
+            if (cudaMemcpyAsync(column, s->h, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st) ||
+                cudaStreamSynchronize(st))
+                return DPF_ERR_CUDA;
+            for (int k = 0; k <= j + 1; ++k) H[k * ldh + j] = column[k];
+            const bool breakdown = H[(j + 1) * ldh + j] < 1e-14;
+            for (int k = 0; k < j; ++k) {
+                const double hk = H[k * ldh + j], hk1 = H[(k + 1) * ldh + j];
+                H[k * ldh + j] = cs[k] * hk + sn[k] * hk1;
+                H[(k + 1) * ldh + j] = -sn[k] * hk + cs[k] * hk1;
+            }
+            const double denominator = std::hypot(H[j * ldh + j], H[(j + 1) * ldh + j]);
+            if (denominator == 0.0) {
+                *singular = true;
+                return DPF_OK;
+            }
+            cs[j] = H[j * ldh + j] / denominator;
+            sn[j] = H[(j + 1) * ldh + j] / denominator;
+            H[j * ldh + j] = denominator;
+            H[(j + 1) * ldh + j] = 0.0;
+            const double gj = g[j];
+            g[j + 1] = -sn[j] * gj;
+            g[j] = cs[j] * gj;
+            *krylov += 1;
+            if (std::fabs(g[j + 1]) <= tolerance * norm || breakdown || j + 1 == width) {
+                // back substitution of the (j+1) x (j+1) upper triangle
+                const int k = j + 1;
+                for (int i = k - 1; i >= 0; --i) {
+                    double acc = g[i];
+                    for (int c = i + 1; c < k; ++c) acc -= H[i * ldh + c] * coef[c];
+                    coef[i] = acc / H[i * ldh + i];
+                }
+                rc = call(kKrylov, 1, [&] { return dpf_combine_rows_f32(n6, s->transformed, n6, k, coef, x, st); });
                 if (rc) return rc;
-                rc = jvp32(tj, pj);
+                // J x = sum_k c_k J z_k from the stored products (J is linear)
+                if (cudaMemsetAsync(ax, 0, n6 * sizeof(double), st)) return DPF_ERR_CUDA;
+                rc = call(kKrylov, 1, [&] { return dpf_combine_rows_f32(n6, s->products, n6, k, coef, ax, st); });
                 if (rc) return rc;
-                rc = call(kKrylov, 1, [&] {
-                    return dpf_arnoldi_cgs2_f32(n6, s->basis, n6, j, pj, s->w32, s->h, s->krylov_partials,
-                                                s->barrier, s->status, st);
+                rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, rhs, -1.0, ax, res, st); });
+                if (rc) return rc;
+                return call(kKrylov, 1, [&] {
+                    return dpf_dot_norm(n6, res, nullptr, s->krylov_scalars, s->krylov_partials, st);
                 });
-                if (rc) return rc;
-                double *column = host + 16;
-                if (cudaMemcpyAsync(column, s->h, (j + 2) * sizeof(double), cudaMemcpyDeviceToHost, st) ||
-                    cudaStreamSynchronize(st))
-                    return DPF_ERR_CUDA;
-                for (int k = 0; k <= j + 1; ++k) H[k * ldh + j] = column[k];
-                const bool breakdown = H[(j + 1) * ldh + j] < 1e-14;
-                for (int k = 0; k < j; ++k) {
-                    const double hk = H[k * ldh + j], hk1 = H[(k + 1) * ldh + j];
-                    H[k * ldh + j] = cs[k] * hk + sn[k] * hk1;
-                    H[(k + 1) * ldh + j] = -sn[k] * hk + cs[k] * hk1;
-                }
-                const double denominator = std::hypot(H[j * ldh + j], H[(j + 1) * ldh + j]);
-                if (denominator == 0.0) {
-                    info->outcome = DPF_NEWTON_SINGULAR;
-                    return DPF_OK;
-                }
-                cs[j] = H[j * ldh + j] / denominator;
-                sn[j] = H[(j + 1) * ldh + j] / denominator;
-                H[j * ldh + j] = denominator;
-                H[(j + 1) * ldh + j] = 0.0;
-                const double gj = g[j];
-                g[j + 1] = -sn[j] * gj;
-                g[j] = cs[j] * gj;
-                iterations += 1;
-                if (std::fabs(g[j + 1]) <= tolerance * norm || breakdown || j + 1 == width) {
-                    // back substitution of the (j+1) x (j+1) upper triangle
-                    const int k = j + 1;
-                    for (int i = k - 1; i >= 0; --i) {
-                        double acc = g[i];
-                        for (int c = i + 1; c < k; ++c) acc -= H[i * ldh + c] * coef[c];
-                        coef[i] = acc / H[i * ldh + i];
-                    }
-                    rc = call(kKrylov, 1, [&] { return dpf_combine_rows_f32(n6, s->transformed, n6, k, coef, x, st); });
-                    if (rc) return rc;
-                    // J x = sum_k c_k J z_k from the stored products (J is linear)
-                    if (cudaMemsetAsync(ax, 0, n6 * sizeof(double), st)) return DPF_ERR_CUDA;
-                    rc = call(kKrylov, 1, [&] { return dpf_combine_rows_f32(n6, s->products, n6, k, coef, ax, st); });
-                    if (rc) return rc;
-                    rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, rhs, -1.0, ax, res, st); });
-                    if (rc) return rc;
-                    double rn;
-                    rc = norm_of(res, &rn);
-                    if (rc) return rc;
-                    relative = rn / norm;
-                    if (relative <= 1.05 * tolerance) {
-                        *ok = true;
-                        *krylov = iterations;
-                        info->krylov_relative = relative;
-                        return DPF_OK;
-                    }
-                    break;
-                }
             }
         }
-        *krylov = iterations;
-        info->krylov_relative = relative;
         return DPF_OK;
     }
 
@@ -358,31 +327,44 @@ struct Step {
             });
         }
         if (rc) return rc;
-        bool cached = false;
+        bool cached = false, prefetched = false;
+        double pre[3] = {0.0, 0.0, 0.0};
         const double dt = a->dt;
         for (int iteration = 0; iteration <= a->max_iterations; ++iteration) {
-            if (iteration == 0 && a->committed_start && !a->refresh) {
-                if (cudaMemsetAsync(s->status, 0, sizeof(int), st)) return DPF_ERR_CUDA;
-                rc = call(kResidual, 1, [&] { return dpf_mixed_initial_residual(n, s->r0, s->fixed, s->y32, r, st); });
-                if (rc) return rc;
-            } else if (!cached) {
-                rc = residual(y, r, false);
-                if (rc) return rc;
-            }
-            rc = iteration_norms();
-            if (rc) return rc;
+            double rnorm, local, merit;
             const bool first = rhs_scale < 0.0;
-            rc = fetch(3, !cached, first);
-            if (rc) return rc;
-            const int status = cached ? 0 : host_int[0];
-            if (status) {
-                info->outcome = DPF_NEWTON_GUARD;
-                info->guard = status;
-                return DPF_OK;
+            if (prefetched) {
+                // the accepted candidate's norms came with the line-search fetch
+                rnorm = pre[0];
+                local = pre[1];
+                merit = pre[2];
+            } else {
+                if (iteration == 0 && a->committed_start && !a->refresh) {
+                    if (cudaMemsetAsync(s->status, 0, sizeof(int), st)) return DPF_ERR_CUDA;
+                    rc = call(kResidual, 1,
+                              [&] { return dpf_mixed_initial_residual(n, s->r0, s->fixed, s->y32, r, st); });
+                    if (rc) return rc;
+                } else if (!cached) {
+                    rc = residual(y, r, false);
+                    if (rc) return rc;
+                }
+                rc = scaling_norms(cur, r, s->scalars);
+                if (rc) return rc;
+                rc = fetch(3, !cached, first);
+                if (rc) return rc;
+                const int status = cached ? 0 : host_int[0];
+                if (status) {
+                    info->outcome = DPF_NEWTON_GUARD;
+                    info->guard = status;
+                    return DPF_OK;
+                }
+                rnorm = host[0];
+                local = host[1];
+                merit = host[2];
             }
             cached = false;
+            prefetched = false;
             packed = false;
-            const double rnorm = host[0], local = host[1], merit = host[2];
             if (first) {
                 const double sa = host[8], sl = host[9];
                 double v = sa;
@@ -412,27 +394,72 @@ struct Step {
             if (iteration == a->max_iterations) break;
             rc = call(kVector, 1, [&] { return dpf_axpby(n6, -1.0, scaled, 0.0, scaled, rhs, st); });
             if (rc) return rc;
-            bool ok;
-            int krylov;
-            rc = fgmres(merit, a->linear_tolerance, 32, 256, &ok, &krylov);
-            if (rc) return rc;
-            if (info->outcome == DPF_NEWTON_SINGULAR) return DPF_OK;
-            if (!ok) {
-                info->outcome = DPF_NEWTON_KRYLOV;
-                return DPF_OK;
-            }
-            info->krylov_iterations += krylov;
-            rc = call(kVector, 1, [&] { return dpf_masked_scale(n, x, s->units, s->fixed, corr, st); });
-            if (rc) return rc;
-            bool accepted = false;
-            for (int power = 0; power < 10; ++power) {
-                const double factor = std::ldexp(1.0, -power);
-                rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, y, factor, corr, cand, st); });
+            // FGMRES cycles (restart 32, at most 256 Arnoldi steps).  Each cycle's
+            // true-residual norm is fetched together with a speculative first
+            // line-search step (factor 1) and the scaling and norms of that
+            // candidate, which the next iteration starts from if it is accepted:
+            // one wait instead of three.  A failed guess costs work, not results:
+            // the iterate's scaling stays in `cur`, and y32 is restored before a
+            // restart's JVPs.
+            if (cudaMemsetAsync(x, 0, n6 * sizeof(double), st)) return DPF_ERR_CUDA;
+            int krylov = 0;
+            const double *start = rhs;
+            double g0 = merit;
+            bool speculated = false;
+            for (;;) {
+                if (merit != 0.0) {
+                    const int width = 256 - krylov < 32 ? 256 - krylov : 32;
+                    bool singular;
+                    rc = fgmres_cycle(start, g0, merit, a->linear_tolerance, width, &krylov, &singular);
+                    if (rc) return rc;
+                    if (singular) {
+                        info->outcome = DPF_NEWTON_SINGULAR;
+                        return DPF_OK;
+                    }
+                }
+                rc = call(kVector, 1, [&] { return dpf_masked_scale(n, x, cur.units, s->fixed, corr, st); });
+                if (rc) return rc;
+                rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, y, 1.0, corr, cand, st); });
                 if (rc) return rc;
                 rc = residual(cand, r_cand, true);
                 if (rc) return rc;
+                rc = scaling_norms(alt, r_cand, s->scalars + 4);
+                if (rc) return rc;
+                if (merit != 0.0 &&
+                    cudaMemcpyAsync(host + 12, s->krylov_scalars + 1, sizeof(double), cudaMemcpyDeviceToHost, st))
+                    return DPF_ERR_CUDA;
+                if (cudaMemcpyAsync(host + 4, s->scalars + 4, 3 * sizeof(double), cudaMemcpyDeviceToHost, st))
+                    return DPF_ERR_CUDA;
                 rc = fetch(3, true, false);
                 if (rc) return rc;
+                const double krylov_relative = merit != 0.0 ? host[12] / merit : 0.0;
+                info->krylov_relative = krylov_relative;
+                if (krylov_relative <= 1.05 * a->linear_tolerance) {
+                    speculated = true;
+                    break;
+                }
+                if (krylov >= 256) {
+                    info->outcome = DPF_NEWTON_KRYLOV;
+                    return DPF_OK;
+                }
+                // restart from the true residual; the JVPs need the iterate's y32 again
+                rc = call(kVector, 1, [&] { return dpf_to_float(n6, y, s->y32, st); });
+                if (rc) return rc;
+                start = res;
+                g0 = host[12];
+            }
+            info->krylov_iterations += krylov;
+            bool accepted = false;
+            for (int power = 0; power < 10; ++power) {
+                const double factor = std::ldexp(1.0, -power);
+                if (power > 0 || !speculated) {
+                    rc = call(kVector, 1, [&] { return dpf_axpby(n6, 1.0, y, factor, corr, cand, st); });
+                    if (rc) return rc;
+                    rc = residual(cand, r_cand, true);
+                    if (rc) return rc;
+                    rc = fetch(3, true, false);
+                    if (rc) return rc;
+                }
                 if (host_int[0]) continue;
                 if (host[2] < (1.0 - 1e-4 * factor) * merit) {
                     double *t = y;
@@ -441,7 +468,19 @@ struct Step {
                     t = r;
                     r = r_cand;
                     r_cand = t;
-                    cached = true;
+                    if (power == 0) {
+                        // the next iteration's scaling is the candidate's: swap the sets
+                        const Scaling keep = cur;
+                        cur = alt;
+                        alt = keep;
+                        info->scaling_alternate ^= 1;
+                        prefetched = true;
+                        pre[0] = host[4];
+                        pre[1] = host[5];
+                        pre[2] = host[6];
+                    } else {
+                        cached = true;
+                    }
                     accepted = true;
                     break;
                 }
@@ -464,6 +503,7 @@ extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_n
     using dpf::driver::Step;
     if (!solver || !step || !info || !solver->graph || solver->graph->n_sites <= 0 || !solver->vectors ||
         !solver->host || !solver->basis || !solver->transformed || !solver->products || !solver->w32 || !solver->h ||
+        !solver->block32_b || !solver->p32_b || !solver->units_b || !solver->units32_b ||
         solver->krylov_width < 1 ||
         solver->krylov_width > 62 || !step->external || !step->v || !step->rotation || !(step->dt > 0.0) ||
         step->max_iterations < 0 || ((uintptr_t)solver->vectors & 15u))
@@ -483,6 +523,8 @@ extern "C" int dpf_mixed_newton_step(const dpf_mixed_newton *solver, const dpf_n
     for (int k = 0; k < DPF_NEWTON_VECTORS; ++k) *slots[k] = v + (int64_t)k * run.n6;
     run.host = solver->host;
     run.host_int = reinterpret_cast<int *>(solver->host + 96);
+    run.cur = {solver->block32, solver->p32, solver->units32, solver->units};
+    run.alt = {solver->block32_b, solver->p32_b, solver->units32_b, solver->units_b};
     run.timing.on = step->timing != 0;
     run.timing.stream = run.st;
     const int rc = run.run();

@@ -1273,13 +1273,16 @@ class MixedNewtonBonds(NewtonBonds):
         """Descriptor of this solver's buffers for ``dpf_mixed_newton_step`` (cached
         while the tensors it points to stay the same)."""
         key = tuple(t.data_ptr() for t in (self.mass, self.fixed, self.radii, self.kn, self.ks, self.kb, self.kt,
-                                           self._ends)) + (self._end_variant, self.lazy_history)
+                                           self._ends, self._p32)) + (self._end_variant, self.lazy_history)
         cached = getattr(self, '_native_desc', None)
         if cached is not None and cached[0] == key:
             return cached[1]
         n, dev, lib = self.n_sites, self.device, self._lib
         ws = self._krylov_workspace32()
         if getattr(self, '_native_vectors', None) is None:
+            # the second scaling set (a line-search candidate's blocks, inverses and units)
+            self._scaling_b = (torch.empty_like(self._block32), torch.empty_like(self._p32),
+                               torch.empty_like(self._units), torch.empty_like(self._units32))
             self._native_vectors = torch.empty((_lib.NEWTON_VECTORS, n, 6), dtype=F64, device=dev)
             self._native_partials = torch.zeros(lib.dpf_partials_doubles(), dtype=F64, device=dev)
             self._native_scalars = torch.zeros(2, dtype=F64, device=dev)
@@ -1295,7 +1298,9 @@ class MixedNewtonBonds(NewtonBonds):
             r0=ptr(self._r0), loads=ptr(self._loads), scales=ptr(self._begin_scales), wrench64=ptr(self._wrench),
             partials=ptr(self._partials), scalars=ptr(self._scalars), status=ptr(self._status), y32=ptr(self._y32),
             d32=ptr(self._d32), wrench32=ptr(self._wrench32), block32=ptr(self._block32), p32=ptr(self._p32),
-            units=ptr(self._units), units32=ptr(self._units32), ends=ptr(self._ends), site4=ptr(self._site4),
+            units=ptr(self._units), units32=ptr(self._units32), block32_b=ptr(self._scaling_b[0]),
+            p32_b=ptr(self._scaling_b[1]), units_b=ptr(self._scaling_b[2]), units32_b=ptr(self._scaling_b[3]),
+            ends=ptr(self._ends), site4=ptr(self._site4),
             p24=ptr(self._p24), end_workspace=ptr(self._tiled_workspace), end_partials=ptr(self._tiled_partials),
             barrier=ptr(self._barrier), inner=ptr(self._inner), basis=ptr(ws.basis),
             transformed=ptr(ws.transformed), products=ptr(ws.products), w32=ptr(ws.w), h=ptr(ws.h),
@@ -1450,6 +1455,10 @@ class MixedNewtonBonds(NewtonBonds):
         self._call('dpf_mixed_newton_step', ctypes.byref(desc), ctypes.byref(args), ctypes.byref(info),
                    self._stream())
         _lib.LAUNCHES['count'] += info.launches
+        if info.scaling_alternate:      # the last scaling went to the second set: it is now the first
+            b = self._scaling_b
+            self._scaling_b = (self._block32, self._p32, self._units, self._units32)
+            self._block32, self._p32, self._units, self._units32 = b
         self.units = self._units
         self._packed = None
         if timing:

@@ -819,12 +819,15 @@ typedef struct dpf_mixed_newton {
     double *scales;                /* 2: the rhs scale terms of the step */
     double *wrench64;              /* 9 M doubles (float64 setup) */
     double *partials;              /* dpf_partials_doubles() */
-    double *scalars;               /* >= 4 */
+    double *scalars;               /* >= 8 */
     int *status;                   /* guard bits */
     float *y32, *d32, *wrench32;   /* (N, 6), (N, 6), dpf_mixed_wrench_floats(M) */
     float *block32, *p32;          /* (N, 6, 6) */
     double *units;                 /* (N, 6) */
     float *units32;                /* (N, 6) */
+    float *block32_b, *p32_b;      /* a second set of the four scaling arrays: the scaling of a */
+    double *units_b;               /* line-search candidate goes there until it is accepted */
+    float *units32_b;
     float *ends, *site4, *p24;     /* dpf_end_pack outputs */
     float *end_workspace;          /* dpf_tiled_workspace_floats(N) */
     double *end_partials;          /* dpf_tiled_partials_doubles() */
@@ -876,6 +879,7 @@ enum {
 
 typedef struct dpf_newton_info {
     int outcome, guard;
+    int scaling_alternate;         /* 1: the last scaling is in the *_b arrays (the caller swaps its sets) */
     int nonlinear_iterations, krylov_iterations, cg_iterations;
     int launches;                  /* kernels launched by the step */
     double relative, local;        /* last relative residual and pose defect */
