@@ -45,8 +45,8 @@ import numpy as np  # noqa: E402
 # DRAM bytes per algorithmic byte of the bond-end PCG and HVP launches, from
 # one ncu capture (dram__bytes_read.sum + dram__bytes_write.sum) of the 64^3
 # bench foam; applied to the algorithmic bytes of the measured size.
-PCG_TRAFFIC_PER_ALGORITHMIC_BYTE = 0.909
-HVP_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.542
+PCG_TRAFFIC_PER_ALGORITHMIC_BYTE = 0.921
+HVP_TRAFFIC_PER_ALGORITHMIC_BYTE = 1.545
 
 METRIC = 'implicit Newton solves/s at rel. residual 1e-6 (64^3 jittered foam, 262k sites, ~1.95M bonds)'
 UNIT = 'solves/s'
