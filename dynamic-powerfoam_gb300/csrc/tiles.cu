@@ -700,25 +700,42 @@ __device__ __forceinline__ void load_q(const float *q, int64_t s, float v[6]) {
 // For every site s: epi(s, q_s, site record, acc) with acc the alpha K q sum.
 // Warp w of the grid takes the chunks w, w + W, ... of 32 / L
 // consecutive sites (W warps in the grid).  The round count is the same for
-// every warp, so the shuffles see full warps.
+// every warp, so the shuffles see full warps.  A round is a chain of
+// dependent loads (CSR bounds, end records, gathers of q_o, site record); the
+// next round's CSR bounds are loaded at the start of this one and the site
+// record before the shuffle tree, so a round waits on the records and the
+// gathers only.  (An L2 prefetch of the next round's records as well made
+// the PCG slower: 1.40 vs 1.32 ms per 20 iterations at 64^3.)
 template <int L, bool kConst, class Epi>
 __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi &epi) {
     constexpr int kSites = 32 / L;  // sites per warp and round
-    const int64_t warps = (int64_t)gridDim.x * blockDim.x / 32;
-    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    const int warps = (int)((int64_t)gridDim.x * blockDim.x / 32);
+    const int warp = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32);
     const int lane32 = (int)threadIdx.x & 31, lane = lane32 & (L - 1);
+    const int n = (int)G.n;  // callers bound the site count by 2^31 - 1
     const int64_t chunks = (G.n + kSites - 1) / kSites;
     const int64_t rounds = (chunks + warps - 1) / warps;
+    const int step = warps * kSites;  // site stride between rounds (< 2^31: a grid of at most 2^26 warps)
+    int s = warp * kSites + lane32 / L;
+    int k0 = 0, k1 = 0;
+    if (s < n) {
+        k0 = G.ptr[s];
+        k1 = G.ptr[s + 1];
+    }
     for (int64_t r = 0; r < rounds; ++r) {
-        const int64_t s = (warp + r * warps) * kSites + lane32 / L;
-        const bool valid = s < G.n;
+        const bool valid = s < n;
+        const int following = s < n - step ? s + step : n;  // the next round's site (n: none)
+        int n0 = 0, n1 = 0;
+        if (following < n) {
+            n0 = G.ptr[following];
+            n1 = G.ptr[following + 1];
+        }
         float acc[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f}, qs[6];
         if (valid) load_q<kConst>(q, s, qs);
         if (valid && !(G.active && !G.active[G.seg[s]])) {
-            const int k1 = G.ptr[s + 1];
             // two ends per step: both ends' records, then both gathers, are in
             // flight together
-            for (int k = G.ptr[s] + lane; k < k1; k += 2 * L) {
+            for (int k = k0 + lane; k < k1; k += 2 * L) {
                 const int k2 = k + L;
                 const bool two = k2 < k1;
                 const float4 a = __ldcs(G.e0 + k), b = __ldcs(G.e1 + k), c = __ldcs(G.e2 + k);
@@ -735,11 +752,16 @@ __device__ __forceinline__ void for_ends(const EndGraph &G, const float *q, Epi 
                 if (two) end_wrench(a2, b2, c2, qs, qo2, acc);
             }
         }
+        float4 rec = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (valid && lane == 0) rec = G.site[s];
 #pragma unroll
         for (int o = 1; o < L; o <<= 1)
 #pragma unroll
             for (int c = 0; c < 6; ++c) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], o);
-        if (valid && lane == 0) epi(s, qs, G.site[s], acc);
+        if (valid && lane == 0) epi((int64_t)s, qs, rec, acc);
+        s = following;
+        k0 = n0;
+        k1 = n1;
     }
 }
 
