@@ -1364,7 +1364,7 @@ class MixedNewtonBonds(NewtonBonds):
                     self._pack_ends(dt)
                 if self._end_variant is None:
                     from .tiles import tune_end_sweep
-                    self._end_variant = tune_end_sweep(self, b.view(-1, 6))
+                    self._end_variant = tune_end_sweep(self, b.view(-1, 6), nearest=self._tune_nearest)
                 self._timed('pcg', lambda: self._call(
                     'dpf_end_precondition_f32', ctypes.byref(self._graph), self._ends.data_ptr(),
                     self._site4.data_ptr(), self.fixed.data_ptr(), self._block32.data_ptr(), self._p24.data_ptr(),
@@ -1550,11 +1550,14 @@ class MixedNewtonBonds(NewtonBonds):
                    self._p24.data_ptr(), self._site4.data_ptr(), self._stream())
         self._packed = ('ends', dt)
 
+    # size classes an untuned graph may borrow the launch shape from (0: time the shapes)
+    _tune_nearest = 0
+
     def _end_pcg(self, vector, out, tolerance, max_iterations, iterations, variant=None):
         if variant is None:
             if self._end_variant is None:
                 from .tiles import tune_end_sweep
-                self._end_variant = tune_end_sweep(self, vector)
+                self._end_variant = tune_end_sweep(self, vector, nearest=self._tune_nearest)
             variant = self._end_variant
         self._call('dpf_end_precondition', ctypes.byref(self._graph), self._ends.data_ptr(), self._site4.data_ptr(),
                    self.fixed.data_ptr(), self._block32.data_ptr(), self._p24.data_ptr(), self._units32.data_ptr(),

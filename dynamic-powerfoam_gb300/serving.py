@@ -248,6 +248,10 @@ class Batch(MixedNewtonBonds):
     """Union of resident ``MixedNewtonBonds`` requests (no host-side rebuild)."""
 
     _active_mask = None
+    # a batch of a size class not yet tuned takes the launch shape of a tuned
+    # class up to two classes (4x in incidences) away: batch sizes follow the
+    # arrivals, and timing the shapes inside a step costs more than it saves
+    _tune_nearest = 2
 
     def __init__(self, parts, pool=None):
         if not parts:

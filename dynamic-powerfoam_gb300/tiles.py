@@ -165,15 +165,24 @@ def end_size_class(n_sites, n_bonds):
     return int(np.log2(max(2*n_bonds, 1)))
 
 
-def tune_end_sweep(solver, vector, iterations=5):
+def tune_end_sweep(solver, vector, iterations=5, nearest=0):
     """Variant index of the bond-end PCG for ``solver``'s graph: cached per
     (device, size class); otherwise each variant runs an elastic PCG of exactly
     ``iterations`` iterations on the solver's own packed records and
     ``vector`` (tolerance 0), once to warm up and once timed with CUDA events
-    on the current stream, and the fastest is kept."""
-    key = (solver.device.index, end_size_class(solver.n_sites, solver.n_bonds))
+    on the current stream, and the fastest is kept.  With ``nearest`` > 0 an
+    untuned class takes the choice of the closest tuned class at most
+    ``nearest`` classes away (the larger on a tie) instead of timing the
+    variants: a served batch of a new size meets the timing's dozen launches
+    (tens of ms at millions of sites) inside its step otherwise."""
+    device, size = solver.device.index, end_size_class(solver.n_sites, solver.n_bonds)
+    key = (device, size)
     if key in _END_TUNED:
         return _END_TUNED[key][0]
+    for distance in range(1, nearest + 1):
+        for near in (size + distance, size - distance):
+            if (device, near) in _END_TUNED:
+                return _END_TUNED[(device, near)][0]
     scratch = torch.empty_like(vector)
     count = torch.zeros(1, dtype=torch.int32, device=solver.device)
     stream = torch.cuda.current_stream(solver.device)

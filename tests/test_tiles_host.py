@@ -147,3 +147,27 @@ def test_tiled_operator_semantics_match_direct_product():
                 acc += w[:6] if kk < mid[s - a] else np.concatenate([-w[:3], w[6:]])
             y[s] = q[s] if fixed[s] else np.repeat(mass[s], 3)*q[s] + acc
     assert np.abs(y - direct).max() <= 1e-12*np.abs(direct).max()
+
+
+def test_end_sweep_tuner_borrows_the_nearest_tuned_class():
+    """An untuned size class takes the launch shape of the closest tuned class
+    within ``nearest`` classes (the larger one on a tie); the cache is keyed by
+    (device, log2 of incidences)."""
+    from types import SimpleNamespace
+    from dpf_gb300 import tiles
+    saved = dict(tiles._END_TUNED)
+    try:
+        tiles._END_TUNED.clear()
+        tiles._END_TUNED[(0, 20)] = (3, {})
+        tiles._END_TUNED[(0, 24)] = (5, {})
+        tiles._END_TUNED[(1, 22)] = (1, {})
+        solver = lambda bonds: SimpleNamespace(device=SimpleNamespace(index=0), n_sites=1, n_bonds=bonds)
+        assert tiles.end_size_class(1, 1 << 20) == 21
+        assert tiles.tune_end_sweep(solver(1 << 19), None, nearest=0) == 3       # class 20 itself
+        assert tiles.tune_end_sweep(solver(1 << 20), None, nearest=2) == 3       # 21: 20 is one away
+        assert tiles.tune_end_sweep(solver(1 << 21), None, nearest=2) == 5       # 22: 20 and 24 tie, larger wins
+        assert tiles.tune_end_sweep(solver(1 << 24), None, nearest=1) == 5       # 25: 24 is one away
+        assert (0, 22) not in tiles._END_TUNED                                   # borrowed, not cached
+    finally:
+        tiles._END_TUNED.clear()
+        tiles._END_TUNED.update(saved)
