@@ -132,7 +132,7 @@ SIGNATURES = {
     'dpf_mixed_bond_floats': (i64, [i64]),
     'dpf_mixed_workspace_floats': (i64, [i64, i64]),
     'dpf_mixed_setup': (i32, [P(Graph), P(Stiffness), P(History), vp, vp, vp, vp, f64, vp, vp, vp, vp, vp, vp, vp,
-                              vp]),
+                              vp, vp]),
     'dpf_mixed_residual': (i32, [P(Graph), vp, vp, vp, vp, vp, f64, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
     'dpf_mixed_scaling': (i32, [P(Graph), vp, vp, vp, vp, f64, vp, vp, vp, vp, vp]),
     'dpf_mixed_scale_residual': (i32, [i64, vp, vp, vp, vp, vp, vp, vp]),

@@ -313,13 +313,9 @@ struct Step {
             const dpf_history &h = a->history;
             rc = call(kSetup, m ? 2 : 1, [&] {
                 return dpf_mixed_setup(s->graph, &s->stiffness, &h, s->mass, a->v, a->external, s->fixed, a->dt,
-                                       s->bond_data, s->r0, s->loads, s->scales, s->wrench64, s->partials, s->status,
-                                       st);
+                                       s->bond_data, s->r0, s->loads, s->scales, s->wrench64,
+                                       s->history_corrections, s->partials, s->status, st);
             });
-            if (!rc && s->history_corrections)
-                rc = call(kSetup, m ? 1 : 0, [&] {
-                    return dpf_mixed_history_corrections(s->graph, &h, s->bond_data, s->history_corrections, st);
-                });
         } else {
             rc = call(kSetup, 1, [&] {
                 return dpf_mixed_begin(n, s->loads, s->mass, a->v, a->external, s->fixed, a->dt, s->r0, s->scales,

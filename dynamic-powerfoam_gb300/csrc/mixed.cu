@@ -153,9 +153,12 @@ struct SetupArgs {
     dpf_history h;
     BondData out;
     double *wrench;
+    float4 *corr;  // optional: the records' float32 rounding errors (the lazy history's corrections)
     int *status;
 };
 
+// One thread per bond, float64 (this pass is float64-bound on this part: one
+// reciprocal square root gives the length and the unit normal, no divisions).
 __global__ void __launch_bounds__(kThreads) setup_bonds(SetupArgs a) {
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= a.m) return;
@@ -163,9 +166,11 @@ __global__ void __launch_bounds__(kThreads) setup_bonds(SetupArgs a) {
     edge(a.edges, b, i, j);
     const d3 xi = ld3(a.h.x, i), xj = ld3(a.h.x, j);
     const d3 dx = xj - xi;
-    const double L0 = norm(dx);
-    if (L0 <= 1e-12) atomicOr(a.status, DPF_ERR_COINCIDENT);
-    const d3 nx = dx / L0;
+    const double l2 = dot(dx, dx);
+    if (l2 <= 1e-24) atomicOr(a.status, DPF_ERR_COINCIDENT);
+    const double inv = rsqrt(l2);
+    const double L0 = l2 * inv;
+    const d3 nx = inv * dx;
     const d3 n0 = ld3(a.h.normal, b);
     const double rh = 0.5 * (a.h.radii[i] - a.h.radii[j]);
     const d3 off = ld3(a.h.offset, b), fs = ld3(a.h.fs, b), mb = ld3(a.h.mb, b);
@@ -189,6 +194,13 @@ __global__ void __launch_bounds__(kThreads) setup_bonds(SetupArgs a) {
     a.out.rec.r5[b] = make_float4((float)off.x, (float)off.y, (float)off.z, ks);
     a.out.rec.r6[b] = make_float4(kb, kt, __int_as_float((int)i), __int_as_float((int)j));
     a.out.t3[b] = make_float4(kt, __int_as_float((int)i), __int_as_float((int)j), 0.0f);
+    if (a.corr) {
+        const auto gap = [](double h) { return (float)(h - (double)(float)h); };
+        const int64_t m = a.m;
+        a.corr[b] = make_float4(gap(fs.x), gap(fs.y), gap(fs.z), gap(fn));
+        a.corr[m + b] = make_float4(gap(mb.x), gap(mb.y), gap(mb.z), gap(mt));
+        a.corr[2 * m + b] = make_float4(gap(off.x), gap(off.y), gap(off.z), 0.0f);
+    }
 }
 
 // r0 = -dt M v - dt^2/2 (L + ext); norms [|dt M v + dt^2/2 ext|, |L on free sites|].
@@ -1422,16 +1434,17 @@ static bool mixed_graph_ok(const dpf_graph *g) {
 
 int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h, const double *mass,
                     const double *v, const double *external, const uint8_t *fixed, double dt, float *bond_data,
-                    double *r0, double *loads, double *scales, double *wrench, double *partials, int *status,
-                    void *stream) {
+                    double *r0, double *loads, double *scales, double *wrench, float *corrections,
+                    double *partials, int *status, void *stream) {
     if (!mixed_graph_ok(g) || !k || !h || !h->x || !h->radii ||
         (g->n_bonds && (!h->normal || !h->offset || !h->fn || !h->fs || !h->mt || !h->mb)) || !mass || !v ||
         !external || !fixed || !bond_data || !r0 || !scales || !partials || !status ||
-        (g->n_bonds && (!wrench || !g->edges)))
+        (g->n_bonds && (!wrench || !g->edges)) || ((uintptr_t)corrections & 15u))
         return DPF_ERR_ARGUMENT;
     cudaStream_t st = (cudaStream_t)stream;
     if (g->n_bonds) {
-        SetupArgs a{g->n_bonds, g->edges, *k, *h, split_bond_data(bond_data, g->n_bonds), wrench, status};
+        SetupArgs a{g->n_bonds, g->edges, *k, *h, split_bond_data(bond_data, g->n_bonds), wrench,
+                    reinterpret_cast<float4 *>(corrections), status};
         setup_bonds<<<blocks_for(g->n_bonds, kThreads), kThreads, 0, st>>>(a);
     }
     SetupSiteArgs s{g->n_sites, g->inc_ptr, g->inc_bond, wrench, mass, v, external, fixed, dt, 0.5 * dt * dt,

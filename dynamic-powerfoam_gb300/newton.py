@@ -1673,15 +1673,14 @@ class MixedNewtonBonds(NewtonBonds):
             self._since_refresh = 0
             self._committed_start = False
             history = self._history_struct()     # folds a lazily committed history first
+            # the lazy history's corrections come out of the same pass
+            corrections = self._history_corrections().data_ptr() if self.lazy_history else None
             self._timed('setup', lambda: self._call(
                 'dpf_mixed_setup', ctypes.byref(self._graph), ctypes.byref(self._stiffness_struct()),
                 ctypes.byref(history), self.mass.data_ptr(), self._v.data_ptr(), external.data_ptr(),
                 self.fixed.data_ptr(), dt, self._bond_data.data_ptr(), self._r0.data_ptr(), self._loads.data_ptr(),
-                scales.data_ptr(), self._wrench.data_ptr(), self._partials.data_ptr(),
+                scales.data_ptr(), self._wrench.data_ptr(), corrections, self._partials.data_ptr(),
                 self._status.data_ptr(), self._stream()))
-            if self.lazy_history:
-                self._call('dpf_mixed_history_corrections', ctypes.byref(self._graph), ctypes.byref(history),
-                           self._bond_data.data_ptr(), self._history_corrections().data_ptr(), self._stream())
         # the scales reach the host with the first residual's fetch (one sync
         # less per step); a setup guard is raised by that residual's own trial
         self._deferred_scale = scales

@@ -197,6 +197,32 @@ class RequestState:
         self.time = 0.
 
 
+def concat_incidence(parts, site_off, bond_off):
+    """Incidence CSR of parts laid end to end (part k's sites from
+    ``site_off[k]``, its bonds from ``bond_off[k]``) from the parts' own CSRs:
+    the rows of part k follow the rows of part k - 1 with its bond ids
+    shifted (v >= 0: the site is the i end of bond v; ~v: the j end).  Equal,
+    entry for entry, to ``device_incidence`` of the concatenated edges: that
+    stable sort orders a site's ends by (side, bond), which the shift keeps."""
+    ptrs, incs = [], []
+    for k, p in enumerate(parts):
+        ptr = p._inc_ptr[:-1] if k + 1 < len(parts) else p._inc_ptr
+        ptrs.append(ptr + 2*int(bond_off[k]))
+        v, b = p._inc_bond, int(bond_off[k])
+        incs.append(torch.where(v >= 0, v + b, v - b))
+    return torch.cat(ptrs).contiguous(), torch.cat(incs).contiguous()
+
+
+def slice_incidence(inc_ptr, inc_bond, sites, incidences, first_bond):
+    """The rows of sites [s0, s1) of an incidence CSR (their incidences
+    [e0, e1), bonds from ``first_bond`` on) as a CSR of their own sites and
+    bonds: the inverse of ``concat_incidence``."""
+    (s0, s1), (e0, e1) = sites, incidences
+    ptr = inc_ptr[s0:s1 + 1]
+    v = inc_bond[e0:e1]
+    return ptr - ptr[0], torch.where(v >= 0, v - first_bond, v + first_bond)
+
+
 class Slice:
     """One request's state inside a previous batch (views, no copies), ready
     to be concatenated into the next batch."""
@@ -211,6 +237,8 @@ class Slice:
         for name in _PER_BOND:
             setattr(self, name, getattr(batch, name)[b0:b1])
         self.edges = batch.edges[b0:b1] - s0
+        self._inc_ptr, self._inc_bond = slice_incidence(batch._inc_ptr, batch._inc_bond, (s0, s1),
+                                                        batch.inc_range[k], b0)
         self.time = batch.time
 
 
@@ -277,6 +305,8 @@ class Batch(MixedNewtonBonds):
         self.site_ptr = torch.as_tensor(rs, dtype=torch.int64, device=self.device)
         self.site_range = [(int(rs[k]), int(rs[k+1])) for k in range(self.n_requests)]
         self.bond_range = [(int(rb[k]), int(rb[k+1])) for k in range(self.n_requests)]
+        # a request's incidences: the CSR rows of its sites (two per bond, contiguous)
+        self.inc_range = [(2*int(rb[k]), 2*int(rb[k+1])) for k in range(self.n_requests)]
         if len(parts) == 1 and isinstance(first, RequestState):
             # a freshly set-up group alone: use its tensors and incidence as they
             # are (the step replaces state tensors, it never writes into them)
@@ -288,7 +318,7 @@ class Batch(MixedNewtonBonds):
             for name in _PER_SITE + _PER_BOND:
                 setattr(self, name, torch.cat([getattr(p, name).contiguous() for p in parts]))
             self.edges = torch.cat([p.edges + int(site_off[k]) for k, p in enumerate(parts)]).contiguous()
-            self._inc_ptr, self._inc_bond = device_incidence(self.edges, n)
+            self._inc_ptr, self._inc_bond = concat_incidence(parts, site_off, bond_off)
         self.i, self.j = self.edges.T
         R = self.n_requests
         self.seg_site = torch.repeat_interleave(torch.arange(R, dtype=torch.int32, device=self.device),

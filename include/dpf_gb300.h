@@ -403,7 +403,8 @@ int dpf_mixed_initial_residual(int64_t n_sites, const double *r0, const uint8_t 
  * what float32 rounding dropped, so that record + correction is the float64
  * history to about 48 bits.
  * dpf_mixed_history_corrections: corrections = h - record, right after a
- * float64 dpf_mixed_setup wrote the records from h.
+ * float64 dpf_mixed_setup wrote the records from h (the same values that
+ * dpf_mixed_setup writes itself when given a corrections array).
  * dpf_mixed_commit_lazy: the accepted increment y as dpf_mixed_commit
  * applies it (x_end = x + y (N, 3), records and loads advanced; dloads: 9 M
  * floats) with the exact rounding error of each record update added to the
@@ -423,12 +424,15 @@ int dpf_mixed_fold_history(const dpf_graph *g, const double *x, const float *bon
 /* Per-step float64 setup: bond records from the committed state, r0 (N, 6),
  * optionally loads(x) (N, 6), and scales[0..1] = [|dt M v + dt^2/2 ext|,
  * |loads on free sites|] (the two terms of rhs_scale).  wrench: 9 M doubles.
+ * corrections (optional, dpf_history_correction_floats(M) floats, 16-byte
+ * aligned): the lazy history's corrections of the records just written.
  * Replaces the loads/rhs_scale prologue of NewtonBonds.step
  * (experiments/bonded_dem_newton.py:137-139, experiments/bonded_dem_finite_gpu.py:82-85). */
 int dpf_mixed_setup(const dpf_graph *g, const dpf_stiffness *k, const dpf_history *h,
                     const double *mass, const double *v, const double *external,
                     const uint8_t *fixed, double dt, float *bond_data, double *r0, double *loads,
-                    double *scales, double *wrench, double *partials, int *status, void *stream);
+                    double *scales, double *wrench, float *corrections, double *partials, int *status,
+                    void *stream);
 
 /* Residual at increment y with every trial guard (status bits as dpf_trial);
  * want_tangent stores the midpoint tangent for dpf_mixed_scaling and K q;

@@ -39,3 +39,31 @@ def test_synthetic_stream_is_seeded():
 def test_footprint_grows_with_size():
     from dpf_gb300.serving import footprint_bytes
     assert 0 < footprint_bytes(1000, 7000) < footprint_bytes(2000, 7000) < footprint_bytes(2000, 14000)
+
+
+def test_concatenated_incidence_equals_the_sorted_one():
+    """A batch's incidence CSR laid end to end from its parts' CSRs equals the
+    stable device sort of the concatenated edges entry for entry, and slicing a
+    request's rows back out gives that request's own CSR."""
+    import torch
+    from dpf_gb300.newton import device_incidence
+    from dpf_gb300.serving import concat_incidence, slice_incidence
+    from types import SimpleNamespace
+    rng = np.random.default_rng(4)
+    parts, edges_all, site_off, bond_off = [], [], [0], [0]
+    for n, m in ((7, 12), (1, 0), (30, 80), (5, 9)):
+        e = rng.integers(0, n, (m, 2)) if n > 1 else np.zeros((0, 2), dtype=np.int64)
+        e = e[e[:, 0] != e[:, 1]]
+        edges = torch.as_tensor(e, dtype=torch.int64).reshape(-1, 2)
+        ptr, inc = device_incidence(edges, n)
+        parts.append(SimpleNamespace(_inc_ptr=ptr, _inc_bond=inc, n_sites=n, n_bonds=len(e)))
+        edges_all.append(edges + site_off[-1])
+        site_off.append(site_off[-1] + n)
+        bond_off.append(bond_off[-1] + len(e))
+    ptr, inc = concat_incidence(parts, site_off, bond_off)
+    ref_ptr, ref_inc = device_incidence(torch.cat(edges_all), site_off[-1])
+    assert torch.equal(ptr, ref_ptr) and torch.equal(inc, ref_inc)
+    for k, p in enumerate(parts):
+        sp, si = slice_incidence(ptr, inc, (site_off[k], site_off[k + 1]), (2*bond_off[k], 2*bond_off[k + 1]),
+                                 bond_off[k])
+        assert torch.equal(sp, p._inc_ptr) and torch.equal(si, p._inc_bond)
