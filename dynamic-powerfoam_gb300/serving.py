@@ -223,6 +223,26 @@ def slice_incidence(inc_ptr, inc_bond, sites, incidences, first_bond):
     return ptr - ptr[0], torch.where(v >= 0, v - first_bond, v + first_bond)
 
 
+def _warm_incidence_ops(device):
+    """Run ``concat_incidence`` and ``slice_incidence`` once on a two-part toy
+    graph: the first launch of a device kernel in a process can cost a module
+    load (about a second was measured on the GPU machine for these int32 ops),
+    which should not land inside the first batch that joins two parts."""
+    ptr = torch.tensor([0, 1, 2], dtype=torch.int32, device=device)
+    inc = torch.tensor([0, -1], dtype=torch.int32, device=device)
+    part = _IncidencePart(ptr, inc)
+    joined = concat_incidence([part, part], [0, 2, 4], [0, 1, 2])
+    slice_incidence(*joined, (2, 4), (2, 4), 1)
+    if device.type == 'cuda':
+        torch.cuda.synchronize(device)
+
+
+@dataclass
+class _IncidencePart:
+    _inc_ptr: torch.Tensor
+    _inc_bond: torch.Tensor
+
+
 class Slice:
     """One request's state inside a previous batch (views, no copies), ready
     to be concatenated into the next batch."""
@@ -696,6 +716,7 @@ class Service:
         self.timers = dict(setup=0., batch=0., solve=0.)
         self.batch_sizes = []
         self.pool = None
+        _warm_incidence_ops(self.device)
 
     def run(self, requests, clock=time.perf_counter):
         pending = sorted(requests)
