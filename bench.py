@@ -84,6 +84,8 @@ def parse():
                    help='served requests checked against a float64 solve of the same request')
     p.add_argument('--served-rate', type=float, default=4000., help='Poisson arrival rate of the stream (1/s)')
     p.add_argument('--served-batch-sites', type=int, default=8_000_000, help='site capacity of one batch')
+    p.add_argument('--served-profile', action='store_true',
+                   help='one more pass of the served stream, untimed, with every batched step profiled')
     p.add_argument('--large-mix', type=int, default=128,
                    help='lattice size of the large served mix (128: one 128^3 foam for 10 steps with '
                         '--large-mix-count requests of 32^3 sites; 0: skip)')
@@ -378,6 +380,15 @@ def run_served(args, device, plan, bases):
                   max_relative_residual=float(max(r.infos[0]['nonlinear_relative_residual'] for r in ok)))
     served['accuracy'] = served_accuracy(finished, args.served_accuracy, device)
     del finished, ok
+    if getattr(args, 'served_profile', False):
+        # per batched step: wall ms (device synced on either side) and the device
+        # ms of every library entry point (the generic FGMRES's Arnoldi launches
+        # are in the wall time only)
+        profiled = serving.Service(device=device, hbm_budget=150e9, max_batch_sites=args.served_batch_sites,
+                                   profile=True)
+        profiled.run(serving.planned_stream(plan, bases))
+        torch.cuda.synchronize()
+        served['profile'] = profiled.profile
     plain = None
     count = len(stream) if args.served_plain < 0 else min(args.served_plain, len(stream))
     if count > 0:

@@ -223,7 +223,16 @@ class LinearBonds:
         return _lib.Tangent(self.n.data_ptr(), self.ri.data_ptr(), self.rj.data_ptr())
 
     def _call(self, name, *args):
+        calls = self.__dict__.get('call_profile')
+        if calls is None:
+            _lib.check(getattr(self._lib, name)(*args), name)
+            return
+        # CUDA events around the library call on the current stream, by entry point
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
         _lib.check(getattr(self._lib, name)(*args), name)
+        end.record()
+        calls.setdefault(name, []).append((start, end))
 
     def _fetch(self, scalars=0, status=False):
         """Copy device scalars (and the status word) to the host with one sync;

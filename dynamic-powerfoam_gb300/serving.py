@@ -706,8 +706,12 @@ class Service:
     Latency = completion - arrival.
     """
 
-    def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=4_000_000, tolerance=1e-6):
+    def __init__(self, device='cuda', hbm_budget=150e9, max_batch_sites=4_000_000, tolerance=1e-6,
+                 profile=False):
         self.device = torch.device(device)
+        # profile: per batched step, the wall time (with a device sync on either
+        # side) and the device time of every library call by entry point
+        self.profile = [] if profile else None
         self.hbm_budget = float(hbm_budget)
         self.max_batch_sites = int(max_batch_sites)
         self.tolerance = float(tolerance)
@@ -825,9 +829,15 @@ class Service:
             staying = sum(r.sites for r in members if r.done_steps + 1 < r.steps)
             stop = threading.Event()
             future = _PREFETCH.submit(collect, stop, self.max_batch_sites - staying, not staying, members[0].dt)
+            if self.profile is not None:
+                torch.cuda.synchronize(self.device)
+                batch.call_profile = {}
             t4 = clock()
             try:
                 results = batch.step_batch(members[0].dt, ext, tolerance=self.tolerance)
+                if self.profile is not None:
+                    torch.cuda.synchronize(self.device)
+                    self.profile.append(_step_profile(batch, results, clock() - t4))
             finally:
                 stop.set()
                 ready += future.result()
@@ -858,6 +868,20 @@ class Service:
                 active = [r for r in active if id(r) not in gone]
                 batch = None
         return finished
+
+
+def _step_profile(batch, results, wall):
+    """One batched step of a profiled ``Service``: requests, sites, wall ms,
+    the largest Newton / FGMRES / CG counts of its requests and the device ms
+    and launch count of every library entry point it called."""
+    calls, batch.call_profile = batch.call_profile, None
+    infos = [r[1] for r in results if not isinstance(r, Exception)]
+    device = {name: [len(ev), round(sum(a.elapsed_time(b) for a, b in ev), 3)] for name, ev in calls.items()}
+    return dict(requests=batch.n_segments, sites=batch.n_sites, wall_ms=round(1e3*wall, 2),
+                device_ms=round(sum(v[1] for v in device.values()), 2),
+                newton=max((i['nonlinear_iterations'] for i in infos), default=0),
+                krylov=max((i['krylov_iterations'] for i in infos), default=0),
+                cg=max((i['cg_iterations'] for i in infos), default=0), calls=device)
 
 
 def latency_stats(finished):
