@@ -226,8 +226,8 @@ def slice_incidence(inc_ptr, inc_bond, sites, incidences, first_bond):
 def _warm_incidence_ops(device):
     """Run ``concat_incidence`` and ``slice_incidence`` once on a two-part toy
     graph: the first launch of a device kernel in a process can cost a module
-    load (about a second was measured on the GPU machine for these int32 ops),
-    which should not land inside the first batch that joins two parts."""
+    load (about 3 s was measured on a GB300 host for these int32 ops), which
+    should not land inside the first batch that joins two parts."""
     ptr = torch.tensor([0, 1, 2], dtype=torch.int32, device=device)
     inc = torch.tensor([0, -1], dtype=torch.int32, device=device)
     part = _IncidencePart(ptr, inc)
